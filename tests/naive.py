@@ -1,0 +1,101 @@
+"""Small, slow, independent Python restatements used to cross-check the oracle:
+global canonical k-mer counting and maximal-unitig construction over the
+bidirected de Bruijn graph of surviving canonical k-mers."""
+from __future__ import annotations
+
+COMP = bytes.maketrans(b"ACGT", b"TGCA")
+
+
+def rc(s: bytes) -> bytes:
+    return s.translate(COMP)[::-1]
+
+
+def canon(s: bytes) -> bytes:
+    r = rc(s)
+    return s if s <= r else r
+
+
+def pieces(seq: bytes, k: int):
+    """Split at every non-ACGT byte (after upper-casing acgt), keep runs >= k."""
+    norm = bytes(c if c in b"ACGT" else (c - 32 if c in b"acgt" else ord("N")) for c in seq)
+    for part in norm.split(b"N"):
+        if len(part) >= k:
+            yield part
+
+
+def kmer_counts(seqs, k: int) -> dict:
+    cnt = {}
+    for s in seqs:
+        for p in pieces(s, k):
+            for i in range(len(p) - k + 1):
+                c = canon(p[i : i + k])
+                cnt[c] = cnt.get(c, 0) + 1
+    return cnt
+
+
+def maximal_unitigs(kmers: set, k: int):
+    """Returns list of (sequence, circular) for the maximal unitigs of a canonical k-mer set."""
+
+    def succ(s):
+        return [s[1:] + b for b in (b"A", b"C", b"G", b"T") if canon(s[1:] + b) in kmers]
+
+    def pred(s):
+        return [b + s[:-1] for b in (b"A", b"C", b"G", b"T") if canon(b + s[:-1]) in kmers]
+
+    def step(s):
+        nx = succ(s)
+        if len(nx) != 1:
+            return None
+        t = nx[0]
+        if len(pred(t)) != 1:
+            return None
+        return t
+
+    used = set()
+    out = []
+
+    def extend(start_oriented, seq, origin):
+        """Extend to the right of start_oriented, appending to seq; stop at branches or
+        at an already used k-mer (as the reference's hash-map extender does)."""
+        cur = start_oriented
+        while True:
+            t = step(cur)
+            if t is None:
+                return False
+            if canon(t) in used:
+                return t == origin
+            used.add(canon(t))
+            seq += t[-1:]
+            cur = t
+
+    for x in sorted(kmers):
+        if x in used:
+            continue
+        used.add(x)
+        fwd = bytearray(x)
+        circ = extend(x, fwd, x)
+        bwd = bytearray(rc(x))
+        extend(rc(x), bwd, rc(x))
+        full = rc(bytes(bwd)) + bytes(fwd[k:])
+        out.append((full, circ and len(bwd) == k))
+    return out
+
+
+def canonical_unitig(seq: bytes, circular: bool, k: int) -> bytes:
+    r = rc(seq)
+    if not circular:
+        return min(seq, r)
+    n = len(seq) - k + 1
+    best = None
+    for src in (seq, r):
+        cyc = src[:n]
+        for rot in range(n):
+            cand = bytes(cyc[(rot + i) % n] for i in range(len(seq)))
+            if best is None or cand < best:
+                best = cand
+    return best
+
+
+def canonical_set(unitigs, k: int) -> bytes:
+    lines = sorted(canonical_unitig(s, c, k) for s, c in unitigs)
+    return b"".join(l + b"\n" for l in lines)

@@ -1,0 +1,74 @@
+"""The oracle's build (bucketing -> per-sub-bucket merge -> link) against an
+independent naive global restatement: same surviving canonical k-mers with the same
+multiplicities, same canonical maximal-unitig set."""
+import numpy as np
+import pytest
+
+import oracle
+from ggcat_gb300 import synth
+from tests import naive
+
+
+def _kmers_to_strings(lo, hi, k):
+    dec = b"ACTG"
+    out = []
+    for a, b in zip(lo.tolist(), hi.tolist()):
+        v = a | (b << 64)
+        out.append(naive.canon(bytes(dec[(v >> (2 * i)) & 3] for i in range(k))))
+    return out
+
+
+def _run(seqs, k=31, m=10, bucket_bits=4, second_bits=2, min_mult=1, threads=2, hash_kind=None):
+    text, off, ln, col = synth.pack_sequences([np.frombuffer(s, np.uint8) for s in seqs])
+    p = oracle.params(k=k, m=m, bucket_bits=bucket_bits, second_bits=second_bits, min_multiplicity=min_mult,
+                      threads=threads, hash_kind=hash_kind)
+    r = oracle.build_graph(text, off, ln, p)
+    lo, hi, mult = r.kmers()
+    got_k = dict(zip(_kmers_to_strings(lo, hi, k), mult.tolist()))
+    exp_all = naive.kmer_counts(seqs, k)
+    exp_k = {x: c for x, c in exp_all.items() if c >= min_mult}
+    assert got_k == exp_k
+    exp_u = naive.canonical_set(naive.maximal_unitigs(set(exp_k), k), k)
+    assert r.unitigs() == exp_u
+    return r
+
+
+def _genome_mix(seed, L=6000, copies=3, sub=0.01, reads=0):
+    rng = np.random.default_rng(seed)
+    g = synth.random_genome(L, rng)
+    g = synth.add_repeats(g, 0.05, 80, 2, 6, rng)
+    seqs = [g.tobytes()]
+    for _ in range(copies - 1):
+        seqs.append(synth.indels(synth.substitute(g, sub, rng), 0.002, 5, rng).tobytes())
+    if reads:
+        rr = synth.sample_reads(g, reads, 100, 0.01, 0.002, rng)
+        seqs.extend(r.tobytes() for r in rr)
+    return seqs
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_build_genomes_min1(seed):
+    _run(_genome_mix(seed))
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_build_reads_min2(seed):
+    _run(_genome_mix(seed, L=3000, copies=1, reads=400), min_mult=2)
+
+
+def test_build_low_complexity_and_n():
+    seqs = [b"A" * 200 + b"N" + b"ACGT" * 50 + b"nnn" + b"acgtacgatcgatcgatcagctagcatcgactagcatcgac" * 3,
+            b"AC" * 100, b"GATTACA" * 40 + b"N" * 5 + b"TTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTT"]
+    _run(seqs, bucket_bits=3, second_bits=1)
+
+
+def test_build_rk128_matches_seqhash():
+    seqs = _genome_mix(7, L=2500, copies=2)
+    a = _run(seqs, hash_kind=oracle.H_CN_SEQ64)
+    b = _run(seqs, hash_kind=oracle.H_CN_RK128)
+    assert a.unitigs() == b.unitigs()
+
+
+def test_build_k63_seq128():
+    seqs = _genome_mix(8, L=2500, copies=2)
+    _run(seqs, k=63, m=12, hash_kind=oracle.H_CN_SEQ128)
