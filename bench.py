@@ -1,0 +1,341 @@
+"""Benchmark of the GB300 build hot path (minimizer bucketing + per-bucket k-mer merge).
+
+One "step" = one pass of the hot path (pack, bucketize, partition, merge with unitig
+extension) over the skewed read workload: a 50 Mbp genome with 2% of its length in
+500-bp repeats copied 20-200 times, sampled at 20x with 150-bp reads from both strands,
+0.5% substitutions, 0.01% N; k=31, m=10, 1024 buckets, min multiplicity 2.  Inputs are
+seeded synthetic data of that shape (the reference names no dataset).
+
+Prints one JSON line (rank 0).  ``value`` is Gbases/s with the input resident in HBM;
+``e2e`` is the same metric through the C ABI call with host buffers (pinned H2D copy of
+the text and D2H of the partial unitigs inside the timed region).
+
+``--impl reference`` times the CPU implementation of the same path on the host cores
+(the oracle restatement with all threads: the Rust reference cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "build Gbases/s bit-exact (batched vs per-bucket launch)"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--genome", type=int, default=50_000_000, help="genome length of the read workload")
+    ap.add_argument("--coverage", type=float, default=20.0)
+    ap.add_argument("--no-per-bucket", action="store_true", help="skip timing the per-bucket launch form")
+    ap.add_argument("--cpu-sample-bases", type=int, default=30_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--verify", action="store_true", help="check batched == per-bucket unitig sets (slow)")
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _workload(args):
+    from ggcat_gb300 import synth
+
+    return synth.config_skewed_reads(genome_len=args.genome, coverage=args.coverage)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.f:
+            return None
+        try:
+            self.f.flush()
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+            os.unlink(self.f.name)
+        except Exception:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(nm)
+            except Exception:
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(w, sample_bases: int, threads: int):
+    """Times the oracle (CPU restatement, all threads) on a bounded prefix of the reads."""
+    import oracle
+
+    n_seq = len(w.seq_off)
+    per = float(w.seq_len.mean()) if n_seq else 1.0
+    take = max(1, min(n_seq, int(sample_bases / per)))
+    end = int(w.seq_off[take - 1] + w.seq_len[take - 1] + 1)
+    text = w.text[:end]
+    p = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6, min_multiplicity=w.min_multiplicity,
+                      threads=threads)
+    t0 = time.perf_counter()
+    r = oracle.build_graph(text, w.seq_off[:take], w.seq_len[:take], p)
+    dt = time.perf_counter() - t0
+    bases = int(w.seq_len[:take].sum())
+    del r
+    return bases / dt / 1e9, bases, dt, take
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle.build()
+    w = _workload(args)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, bases, dt, take = cpu_baseline(w, args.cpu_sample_bases, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 6),
+        "unit": "Gbases/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(bases / value / 1e6, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": w.name + f" (first {take} reads, {bases} bases per step)", "k": w.k, "m": w.m,
+                   "buckets": 1 << w.bucket_bits, "min_multiplicity": w.min_multiplicity},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gbases/s", "cores": threads, "kind": "port",
+                         "sample": f"first {take} reads ({bases} bases) of the workload; the Rust reference cannot be "
+                                   f"compiled here, so the oracle restatement (C, pthreads) is timed"},
+        "e2e": {"value": round(value, 6), "unit": "Gbases/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    from ggcat_gb300 import _native
+
+    ws, rank, local = _dist()
+    dev = local
+    torch.cuda.set_device(dev)
+    dist = None
+    if ws > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+        dist = tdist
+    w = _workload(args)
+    bases = w.bases
+    ctx = _native.GpuContext(dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    d_text = torch.from_numpy(w.text).to(f"cuda:{dev}")
+    torch.cuda.synchronize()
+
+    def params(mode):
+        return _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
+                                   min_multiplicity=w.min_multiplicity, merge_mode=mode)
+
+    def step(p):
+        ctx.bucketize(d_text.data_ptr(), d_text.numel(), p, sptr)
+        ctx.merge(p, sptr)
+
+    def timed(p, steps, warmup):
+        for _ in range(warmup):
+            step(p)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = ctx.kernel_launches
+        e0.record(stream)
+        ph = {"ms_pack": 0.0, "ms_bucketize": 0.0, "ms_merge": 0.0}
+        for _ in range(steps):
+            step(p)
+            st = ctx.stats()
+            for key in ph:
+                ph[key] += st[key]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        if dist:
+            t = torch.tensor([ms], device=f"cuda:{dev}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, (ctx.kernel_launches - l0) // steps, {k2: v / steps for k2, v in ph.items()}, st
+
+    pb = params(_native.GGCAT_MERGE_BATCHED)
+    with ClockSampler(dev) as clk:
+        ms, launches, phases, st = timed(pb, args.steps, args.warmup)
+    clocks = clk.summary()
+    value = bases * ws / (ms * 1e-3) / 1e9
+
+    per_bucket = None
+    if not args.no_per_bucket:
+        pp = params(_native.GGCAT_MERGE_PER_BUCKET)
+        ms_pb, launches_pb, phases_pb, _ = timed(pp, max(1, min(args.steps, 3)), 1)
+        per_bucket = {"value": round(bases * ws / (ms_pb * 1e-3) / 1e9, 4), "ms_per_step": round(ms_pb, 3),
+                      "ms_merge": round(phases_pb["ms_merge"], 3), "gpu_launches": launches_pb,
+                      "merge_speedup_batched": round(phases_pb["ms_merge"] / max(phases["ms_merge"], 1e-9), 2)}
+
+    # e2e through the C ABI with host buffers (pinned input; partial unitigs read back)
+    h_text = torch.from_numpy(w.text).pin_memory()
+    hp = h_text.numpy()
+    for _ in range(max(1, args.warmup)):
+        ctx.build_text(hp, pb, sptr)
+    torch.cuda.synchronize()
+    e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        ctx.build_text(hp, pb, sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / e_steps
+    st2 = ctx.stats()
+    d2h = int(st2["partial_bases"] + st2["partial_unitigs"] * (8 + 4 + 1))
+    e2e_value = bases * ws / wall / 1e9
+
+    # roofline: the bucketing phase (pack + count + write passes) is HBM-bound; its
+    # algorithmic bytes per step are the ASCII read, the 2-bit + validity write, two reads
+    # of the packed input and one 16-byte record write per superkmer.
+    peak, peak_kind = _peaks()
+    n = w.text.size
+    bucket_bytes = n + n * 3 / 8 + 2 * (n * 3 / 8) + 16 * st["superkmers"]
+    bucket_ms = phases["ms_pack"] + phases["ms_bucketize"]
+    achieved = bucket_bytes / (bucket_ms * 1e-3) / 1e9 if bucket_ms > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": "pack_kernel + bucketize_kernel (bucketing phase)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_kind": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_step": int(bucket_bytes), "phase_ms": round(bucket_ms, 3)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, cb, dt, take = cpu_baseline(w, args.cpu_sample_bases, threads)
+        cpu = {"value": round(v, 6), "unit": "Gbases/s", "cores": threads, "kind": "port",
+               "sample": f"first {take} reads ({cb} bases), oracle restatement, {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": round(value, 4),
+            "unit": "Gbases/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "u64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": w.name, "k": w.k, "m": w.m, "buckets": 1 << w.bucket_bits,
+                       "min_multiplicity": w.min_multiplicity, "bases_per_gpu": bases,
+                       "l2": "input (1 GB) larger than L2; no flush", "merge": "batched persistent",
+                       "parallelism": f"replicas x{ws}"},
+            "phases_ms": {k2: round(v, 3) for k2, v in phases.items()},
+            "stats": {"superkmers": int(st["superkmers"]), "kmer_instances": int(st["kmer_instances"]),
+                      "partial_unitigs": int(st["partial_unitigs"]), "small_units": int(st["merge_units_small"]),
+                      "large_units": int(st["merge_units_large"])},
+            "per_bucket": per_bucket,
+            "e2e": {"value": round(e2e_value, 4), "unit": "Gbases/s", "h2d_bytes_per_step": int(n),
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

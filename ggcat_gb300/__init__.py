@@ -1,0 +1,108 @@
+"""ggcat_gb300 — GB300-native (sm_103a) build hot path and query lookup of GGCAT.
+
+The host interface mirrors GGCAT's ``GGCATInstance`` (crates/api/src/lib.rs:118-478):
+``GGCATInstance.create(config)`` returns a process-wide singleton, and
+``build_graph(...)`` builds the compacted de Bruijn graph of FASTA inputs.  The compute
+runs in hand-written CUDA kernels behind the C ABI in ``include/ggcat_gb300.h``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from dataclasses import dataclass
+from typing import Callable, Optional, Sequence
+
+from ._native import (GGCAT_HASH_RABIN_KARP128, GGCAT_HASH_SEQHASH, GGCAT_MERGE_BATCHED, GGCAT_MERGE_PER_BUCKET,
+                      GgcatGpuError, GpuContext, Params, compute_best_m, fasta_parse, load, make_params)
+
+__all__ = [
+    "GGCATConfig",
+    "GGCATInstance",
+    "ExtraElaboration",
+    "GpuContext",
+    "GgcatGpuError",
+    "Params",
+    "make_params",
+    "compute_best_m",
+    "fasta_parse",
+    "GGCAT_MERGE_BATCHED",
+    "GGCAT_MERGE_PER_BUCKET",
+    "GGCAT_HASH_SEQHASH",
+    "GGCAT_HASH_RABIN_KARP128",
+]
+
+
+class ExtraElaboration:
+    """crates/api/src/lib.rs:99-116 (only None is implemented on the device path)."""
+
+    NONE = 0
+    UNITIG_LINKS = 1
+    GREEDY_MATCHTIGS = 2
+    EULERTIGS = 3
+    PATHTIGS = 4
+
+
+@dataclass
+class GGCATConfig:
+    """crates/api/src/lib.rs:75-99."""
+
+    temp_dir: Optional[str] = None
+    memory: float = 2.0
+    prefer_memory: bool = True
+    total_threads_count: int = os.cpu_count() or 1
+    intermediate_compression_level: Optional[int] = None
+    stats_file: Optional[str] = None
+    messages_callback: Optional[Callable[[int, str], None]] = None
+    device: int = 0
+
+
+class GGCATInstance:
+    """Process-wide singleton: a second ``create`` returns the first instance and ignores
+    its config, as the reference does (crates/api/src/lib.rs:141-214)."""
+
+    _instance: Optional["GGCATInstance"] = None
+    _lock = threading.Lock()
+
+    def __init__(self, config: GGCATConfig):
+        self.config = config
+        self.ctx = GpuContext(config.device)
+
+    @classmethod
+    def create(cls, config: GGCATConfig | None = None) -> "GGCATInstance":
+        with cls._lock:
+            if cls._instance is None:
+                cls._instance = GGCATInstance(config or GGCATConfig())
+            return cls._instance
+
+    def build_graph(
+        self,
+        input_streams: Sequence[str],
+        output_file: str,
+        color_names: Optional[Sequence[str]] = None,
+        kmer_length: int = 31,
+        threads_count: int = 1,
+        forward_only: bool = False,
+        minimizer_length: Optional[int] = None,
+        colors: bool = False,
+        min_multiplicity: int = 2,
+        extra_elab: int = ExtraElaboration.NONE,
+        gfa_output_version: Optional[int] = None,
+    ) -> str:
+        """crates/api/src/lib.rs:217-322 — returns the output path ("" on failure, like
+        the C API's ``unwrap_or_default``)."""
+        if colors or color_names:
+            raise GgcatGpuError("coloured builds are not available on the device path yet")
+        if extra_elab != ExtraElaboration.NONE or gfa_output_version:
+            raise GgcatGpuError("extra elaborations / GFA output are outside the device path")
+        L = load()
+        arr = (C.c_char_p * len(input_streams))(*[os.fsencode(p) for p in input_streams])
+        m = (1 << 64) - 1 if minimizer_length is None else minimizer_length
+        rc = L.ggcat_gpu_build_from_files(self.ctx.h, arr, len(input_streams), os.fsencode(output_file), kmer_length,
+                                          threads_count, int(forward_only), m, min_multiplicity)
+        if rc != 0:
+            msg = L.ggcat_gpu_last_error(self.ctx.h)
+            if self.config.messages_callback:
+                self.config.messages_callback(2, msg.decode() if msg else "")
+            return ""
+        return output_file

@@ -1,0 +1,270 @@
+"""ctypes binding of the C ABI declared in include/ggcat_gb300.h.
+
+The CUDA library is the only compute path: if it cannot be built or loaded this module
+raises, there is no CPU fallback."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GGCAT_GPU_OK = 0
+GGCAT_HASH_SEQHASH = 1
+GGCAT_HASH_RABIN_KARP128 = 4
+GGCAT_MERGE_BATCHED = 0
+GGCAT_MERGE_PER_BUCKET = 1
+
+_ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EDEVICE", -5: "EUNSUPPORTED", -6: "EIO"}
+
+
+class GgcatGpuError(RuntimeError):
+    pass
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("k", C.c_int32),
+        ("m", C.c_int32),
+        ("bucket_bits", C.c_int32),
+        ("second_bits", C.c_int32),
+        ("min_multiplicity", C.c_int32),
+        ("hash_kind", C.c_int32),
+        ("forward_only", C.c_int32),
+        ("merge_mode", C.c_int32),
+        ("unit_target", C.c_int32),
+        ("keep_kmers", C.c_int32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("text_bytes", C.c_uint64),
+        ("superkmers", C.c_uint64),
+        ("kmer_instances", C.c_uint64),
+        ("merge_units_small", C.c_uint64),
+        ("merge_units_large", C.c_uint64),
+        ("partial_unitigs", C.c_uint64),
+        ("partial_bases", C.c_uint64),
+        ("surviving_kmers", C.c_uint64),
+        ("final_unitigs", C.c_uint64),
+        ("ms_pack", C.c_double),
+        ("ms_bucketize", C.c_double),
+        ("ms_merge", C.c_double),
+        ("ms_link", C.c_double),
+    ]
+
+
+SUPERKMER = np.dtype(
+    [
+        ("start", "<u8"),
+        ("len", "<u4"),
+        ("bucket", "<u2"),
+        ("second_bucket", "<u2"),
+        ("minimizer_pos", "<u2"),
+        ("rc", "u1"),
+        ("flags", "u1"),
+    ],
+    align=True,
+)
+
+# every symbol include/ggcat_gb300.h declares
+EXPORTED = [
+    "ggcat_gpu_create",
+    "ggcat_gpu_destroy",
+    "ggcat_gpu_last_error",
+    "ggcat_gpu_kernel_launches",
+    "ggcat_gpu_bucketize",
+    "ggcat_gpu_superkmers_copy",
+    "ggcat_gpu_merge",
+    "ggcat_gpu_partial_unitigs_copy",
+    "ggcat_gpu_kmers_copy",
+    "ggcat_gpu_link",
+    "ggcat_gpu_unitigs_copy",
+    "ggcat_gpu_get_stats",
+    "ggcat_gpu_build_text",
+    "ggcat_gpu_fasta_parse",
+    "ggcat_gpu_build_from_files",
+]
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build: bool = True):
+    """Loads (building first if needed) libggcat_gb300.so and declares the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise GgcatGpuError(f"CUDA library missing: {path}")
+    L = C.CDLL(path)
+    P, u64, sz = C.c_void_p, C.c_uint64, C.c_size_t
+    pu64 = C.POINTER(C.c_uint64)
+    L.ggcat_gpu_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    L.ggcat_gpu_destroy.argtypes = [P]
+    L.ggcat_gpu_destroy.restype = None
+    L.ggcat_gpu_last_error.argtypes = [P]
+    L.ggcat_gpu_last_error.restype = C.c_char_p
+    L.ggcat_gpu_kernel_launches.argtypes = [P]
+    L.ggcat_gpu_kernel_launches.restype = u64
+    L.ggcat_gpu_bucketize.argtypes = [P, P, u64, C.POINTER(Params), P, pu64]
+    L.ggcat_gpu_superkmers_copy.argtypes = [P, P, u64, pu64]
+    L.ggcat_gpu_merge.argtypes = [P, C.POINTER(Params), P]
+    L.ggcat_gpu_partial_unitigs_copy.argtypes = [P, P, u64, P, P, P, u64, pu64, pu64]
+    L.ggcat_gpu_kmers_copy.argtypes = [P, P, P, u64, pu64]
+    L.ggcat_gpu_link.argtypes = [P, C.c_int]
+    L.ggcat_gpu_unitigs_copy.argtypes = [P, P, u64, P, P, P, u64, pu64, pu64]
+    L.ggcat_gpu_get_stats.argtypes = [P, C.POINTER(Stats)]
+    L.ggcat_gpu_build_text.argtypes = [P, P, u64, C.POINTER(Params), P]
+    L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
+    L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
+    for name in EXPORTED:
+        if name not in ("ggcat_gpu_destroy", "ggcat_gpu_last_error", "ggcat_gpu_kernel_launches"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def make_params(k=31, m=None, bucket_bits=10, second_bits=3, min_multiplicity=1, hash_kind=GGCAT_HASH_SEQHASH,
+                forward_only=False, merge_mode=GGCAT_MERGE_BATCHED, unit_target=0, keep_kmers=False) -> Params:
+    if m is None:
+        m = compute_best_m(k)
+    return Params(k, m, bucket_bits, second_bits, min_multiplicity, hash_kind, int(forward_only), merge_mode,
+                  unit_target, int(keep_kmers))
+
+
+def compute_best_m(k: int) -> int:
+    """crates/utils/src/lib.rs:29-40."""
+    if k <= 13:
+        return max(k // 2, k - 4)
+    if k <= 15:
+        return 9
+    if k <= 21:
+        return 10
+    if k <= 30:
+        return 11
+    if k <= 37:
+        return 12
+    if k <= 42:
+        return 13
+    if k <= 64:
+        return 14
+    return int(round(k / 4.0))
+
+
+class GpuContext:
+    """One device context of the library (all device buffers are owned by it)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.ggcat_gpu_create(device, C.byref(h))
+        if rc != 0:
+            raise GgcatGpuError(f"ggcat_gpu_create failed ({_ERRORS.get(rc, rc)}): is a CUDA device available?")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ggcat_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.L.ggcat_gpu_last_error(self.h)
+            raise GgcatGpuError(f"{what}: {_ERRORS.get(rc, rc)}: {msg.decode() if msg else ''}")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.ggcat_gpu_kernel_launches(self.h))
+
+    def bucketize(self, d_text_ptr: int, text_len: int, p: Params, stream: int = 0) -> int:
+        n = C.c_uint64()
+        self._check(self.L.ggcat_gpu_bucketize(self.h, C.c_void_p(d_text_ptr), text_len, C.byref(p),
+                                               C.c_void_p(stream), C.byref(n)), "bucketize")
+        return n.value
+
+    def superkmers(self) -> np.ndarray:
+        n = C.c_uint64()
+        self._check(self.L.ggcat_gpu_superkmers_copy(self.h, None, 0, C.byref(n)), "superkmers_copy")
+        out = np.zeros(n.value, SUPERKMER)
+        self._check(self.L.ggcat_gpu_superkmers_copy(self.h, _ptr(out), n.value, C.byref(n)), "superkmers_copy")
+        return out
+
+    def merge(self, p: Params, stream: int = 0):
+        self._check(self.L.ggcat_gpu_merge(self.h, C.byref(p), C.c_void_p(stream)), "merge")
+
+    def build_text(self, text: np.ndarray, p: Params, stream: int = 0):
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        self._check(self.L.ggcat_gpu_build_text(self.h, _ptr(t), len(t), C.byref(p), C.c_void_p(stream)), "build_text")
+
+    def _unitigs(self, fn, what):
+        nu, nb = C.c_uint64(), C.c_uint64()
+        self._check(fn(self.h, None, 0, None, None, None, 0, C.byref(nu), C.byref(nb)), what)
+        bases = np.zeros(nb.value, np.uint8)
+        off = np.zeros(nu.value, np.uint64)
+        ln = np.zeros(nu.value, np.uint32)
+        fl = np.zeros(nu.value, np.uint8)
+        self._check(fn(self.h, _ptr(bases), nb.value, _ptr(off), _ptr(ln), _ptr(fl), nu.value, C.byref(nu),
+                       C.byref(nb)), what)
+        return bases, off, ln, fl
+
+    def partial_unitigs(self):
+        return self._unitigs(self.L.ggcat_gpu_partial_unitigs_copy, "partial_unitigs_copy")
+
+    def kmers(self):
+        n = C.c_uint64()
+        self._check(self.L.ggcat_gpu_kmers_copy(self.h, None, None, 0, C.byref(n)), "kmers_copy")
+        keys = np.zeros(n.value, np.uint64)
+        mult = np.zeros(n.value, np.uint64)
+        self._check(self.L.ggcat_gpu_kmers_copy(self.h, _ptr(keys), _ptr(mult), n.value, C.byref(n)), "kmers_copy")
+        return keys, mult
+
+    def link(self, k: int):
+        self._check(self.L.ggcat_gpu_link(self.h, k), "link")
+
+    def unitigs(self):
+        return self._unitigs(self.L.ggcat_gpu_unitigs_copy, "unitigs_copy")
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.L.ggcat_gpu_get_stats(self.h, C.byref(s)), "get_stats")
+        return {f: getattr(s, f) for f, _ in Stats._fields_}
+
+
+def fasta_parse(data: bytes, copyback: int):
+    """FASTA -> device text layout, with the reference's 4 MiB + copyback chunking."""
+    L = load()
+    buf = np.frombuffer(data, dtype=np.uint8)
+    need, pieces = C.c_uint64(), C.c_uint64()
+    rc = L.ggcat_gpu_fasta_parse(_ptr(buf), len(buf), copyback, None, 0, C.byref(need), C.byref(pieces))
+    if rc:
+        raise GgcatGpuError("fasta_parse failed")
+    text = np.zeros(need.value, np.uint8)
+    rc = L.ggcat_gpu_fasta_parse(_ptr(buf), len(buf), copyback, _ptr(text), need.value, C.byref(need), C.byref(pieces))
+    if rc:
+        raise GgcatGpuError("fasta_parse failed")
+    return text
+
+
+def unitig_lines(bases: np.ndarray, off: np.ndarray, ln: np.ndarray) -> bytes:
+    """'\\n'-terminated unitig lines from (bases, offsets, lengths)."""
+    b = bases.tobytes()
+    return b"".join(b[o : o + l] + b"\n" for o, l in zip(off.tolist(), ln.tolist()))

@@ -1,0 +1,437 @@
+// Minimizer bucketing on sm_103a.
+//
+// Replaces the CPU hot loop of GGCAT's bucketing (MinimizerBucketingExecWriter::execute,
+// crates/minimizer_bucketing/src/lib.rs:296-376, with
+// AssemblerMinimizerBucketingExecutor::process_sequence,
+// crates/assembler_minimizer_bucketing/src/lib.rs:171-270) and its lz4 temp-file bucket
+// store with a device radix partition kept in HBM.
+//
+// Layout: the ASCII text is packed once into 2-bit codes (32 bases per u64) and a
+// validity bitmap (1 bit per base; ACGTacgt are valid).  Each thread then owns a chunk
+// of (k-1)-mer window positions and walks its bases sequentially with a rolling nt-hash
+// and an incremental window minimum; superkmer boundaries owned by the chunk are
+// emitted as 16-byte records into a per-sub-bin partition (count pass + write pass).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ggcat {
+
+// ---------------------------------------------------------------------------
+// Pack: ASCII -> 2-bit codes (A0 C1 T2 G3 = (c >> 1) & 3) + validity bits.
+// One thread per 32 bases: two 16-byte loads, one 8-byte and one 4-byte store.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) pack_kernel(const uint8_t *__restrict__ text, uint64_t n, uint64_t n_words,
+                                                   int aligned16, uint64_t *__restrict__ packed,
+                                                   uint32_t *__restrict__ valid) {
+    uint64_t wi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; wi < n_words; wi += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t base = wi * 32;
+        uint8_t b[32];
+        if (aligned16 && base + 32 <= n) {
+            uint4 a0 = reinterpret_cast<const uint4 *>(text + base)[0];
+            uint4 a1 = reinterpret_cast<const uint4 *>(text + base)[1];
+            const uint8_t *p0 = reinterpret_cast<const uint8_t *>(&a0);
+            const uint8_t *p1 = reinterpret_cast<const uint8_t *>(&a1);
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                b[i] = p0[i];
+                b[16 + i] = p1[i];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 32; i++) b[i] = (base + i < n) ? text[base + i] : (uint8_t)'\n';
+        }
+        uint64_t pw = 0;
+        uint32_t vw = 0;
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            uint32_t c = b[i];
+            uint32_t u = c & 0xDFu;  // upper case
+            bool ok = (u == 'A') | (u == 'C') | (u == 'G') | (u == 'T');
+            pw |= (uint64_t)((c >> 1) & 3u) << (2 * i);
+            vw |= (uint32_t)ok << i;
+        }
+        packed[wi] = pw;
+        valid[wi] = vw;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Bucketize
+// ---------------------------------------------------------------------------
+struct NtTables {
+    uint64_t h[4], rch[4], h_rot_m[4], rch_rot_m1[4];
+};
+
+struct Window {
+    uint64_t mv;      // masked minimum value (unique flag cleared)
+    uint32_t cnt;     // occurrences of mv in the window
+    uint64_t pos;     // absolute m-mer position of the oldest occurrence
+    uint32_t uraw;    // unique-flag bit of the oldest occurrence
+    uint32_t ufw;     // is_forward of the oldest occurrence
+};
+
+__device__ __forceinline__ void win_add(Window &w, uint64_t val, uint32_t isfw, uint64_t pos, bool first) {
+    uint64_t mvr = val & ~1ull;
+    if (first || mvr < w.mv) {
+        w.mv = mvr;
+        w.cnt = 1;
+        w.pos = pos;
+        w.uraw = (uint32_t)(val & 1);
+        w.ufw = isfw;
+    } else if (mvr == w.mv) {
+        w.cnt++;
+    }
+}
+
+// Base of age a (0 = newest) in the 64-base history (r0 newest 32 bases, r1 older 32).
+__device__ __forceinline__ uint32_t hist_base(uint64_t r0, uint64_t r1, int a) {
+    return a < 32 ? (uint32_t)((r0 >> (2 * a)) & 3u) : (uint32_t)((r1 >> (2 * (a - 32))) & 3u);
+}
+
+// nt-hash of the m-mer whose first base has age `a_first` (its last base has age a_first-m+1).
+__device__ __forceinline__ void nt_from_scratch(const NtTables &T, uint64_t r0, uint64_t r1, int a_first, int m,
+                                                uint64_t &fw, uint64_t &rc) {
+    fw = 0;
+    rc = 0;
+    for (int j = 0; j < m; j++) {
+        uint32_t c = hist_base(r0, r1, a_first - j);
+        fw ^= rotl64(T.h[c], (unsigned)(m - 1 - j));
+        rc ^= rotl64(T.rch[c], (unsigned)j);
+    }
+}
+
+__device__ __forceinline__ uint64_t nt_value(uint64_t fw, uint64_t rc) {
+    uint64_t mn = fw < rc ? fw : rc;
+    return (mn << 1) | (uint64_t)(fw != rc);
+}
+
+// Recompute the window state over the w m-mers ending at the newest m-mer (position i).
+__device__ void win_recompute(Window &w, const NtTables &T, uint64_t r0, uint64_t r1, int k, int m, uint64_t i) {
+    const int wn = k - m;
+    uint64_t fw, rc;
+    // first m-mer of the window starts at age k-2 (the window covers the newest k-1 bases)
+    nt_from_scratch(T, r0, r1, k - 2, m, fw, rc);
+    uint64_t lo = i - (uint64_t)(wn - 1);
+    for (int j = 0; j < wn; j++) {
+        if (j > 0) {
+            uint32_t out = hist_base(r0, r1, k - 2 - (j - 1));
+            uint32_t in = hist_base(r0, r1, k - 2 - (j - 1) - m);
+            fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[in];
+            rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[in];
+        }
+        win_add(w, nt_value(fw, rc), (uint32_t)(fw < rc), lo + (uint64_t)j, j == 0);
+    }
+}
+
+template <bool kWrite>
+__global__ void __launch_bounds__(256)
+    bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k, int m,
+                     int bbits, int sbits, int canonical, uint64_t chunk, unsigned long long *__restrict__ bin_count,
+                     unsigned long long *__restrict__ bin_kmers, const unsigned long long *__restrict__ bin_off,
+                     unsigned long long *__restrict__ bin_cursor, SkRec *__restrict__ recs,
+                     unsigned *__restrict__ status) {
+    __shared__ NtTables T;
+    if (threadIdx.x < 4) {
+        uint32_t c = threadIdx.x;
+        uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
+        uint64_t r = (uint64_t)(((2 * c) ^ 4) + 1) * kNtMult;
+        T.h[c] = h;
+        T.rch[c] = r;
+        T.h_rot_m[c] = rotl64(h, (unsigned)m);
+        T.rch_rot_m1[c] = rotl64(r, (unsigned)(m - 1));
+    }
+    __syncthreads();
+
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t x0 = tid * chunk;
+    if (x0 >= n) return;
+    const uint64_t x1 = min(x0 + chunk, n);
+    const int wn = k - m;
+    const uint32_t dup_bucket = 1u << bbits;
+    const uint64_t bmask = (1ull << bbits) - 1, smask = (1ull << sbits) - 1;
+
+    uint64_t lb = (uint64_t)(2 * wn + 2);
+    for (int attempt = 0; attempt < 40; attempt++) {
+        const uint64_t xb = x0 > lb ? x0 - lb : 0;
+        bool anchored = (xb == 0);
+        uint64_t run = 0;
+        uint64_t r0 = 0, r1 = 0, fw = 0, rc = 0;
+        Window W{};
+        uint64_t prev_raw = 0, prev_pos = 0;
+        uint32_t prev_fw = 0;
+        bool prev_valid = false;
+        uint64_t c_prev = 0;
+        bool c_known = false, first_sk = false;
+        bool failed = false;
+
+        uint64_t cur_word = ~0ull, pw = 0;
+        uint32_t vw = 0;
+        const uint64_t p_end = min(x1 + (uint64_t)k - 1, n + 1);
+
+        auto emit = [&](uint64_t c, bool is_final) {
+            // superkmer [c_prev - 1, c + k - 1) with the minimizer of the window before c
+            // (split) or of the last window (final): lib.rs:207-267
+            uint64_t start = c_prev - 1, end = c + (uint64_t)k - 1;
+            uint32_t len = (uint32_t)(end - start);
+            uint32_t inc_first = first_sk ? 1u : 0u, inc_last = is_final ? 1u : 0u;
+            uint32_t bucket, rcf, pos;
+            if ((prev_raw & 1ull) == 0) {
+                bucket = dup_bucket;
+                rcf = 0;
+                pos = 0;
+            } else {
+                rcf = (canonical && !prev_fw) ? 1u : 0u;
+                bucket = (uint32_t)((prev_raw >> 1) & bmask);  // get_bucket(0, b, h), cn_nthash.rs:135-142
+                pos = rcf ? (uint32_t)(end - (prev_pos + (uint64_t)m)) : (uint32_t)(prev_pos - start);
+            }
+            uint32_t second = (uint32_t)((prev_raw >> (bbits + 1)) & smask);
+            uint32_t sub = (uint32_t)((prev_raw >> (bbits + 1)) & 0xffu);
+            uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
+            uint64_t bin = ((uint64_t)bucket << kFineBits) | sub;
+            if (!kWrite) {
+                atomicAdd(&bin_count[bin], 1ull);
+                atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
+            } else {
+                unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
+                if (slot >= bin_off[bin + 1]) {  // count and write passes disagree: internal error
+                    atomicOr(status, kStatusLookback);
+                    first_sk = false;
+                    return;
+                }
+                SkRec r;
+                r.w0 = start | ((uint64_t)len << 40);
+                r.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
+                       ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
+                recs[slot] = r;
+            }
+            first_sk = false;
+        };
+
+        for (uint64_t p = xb; p < p_end; p++) {
+            uint64_t wi = p >> 5;
+            if (wi != cur_word) {
+                cur_word = wi;
+                if (p < n) {
+                    pw = packed[wi];
+                    vw = valid[wi];
+                } else {
+                    pw = 0;
+                    vw = 0;
+                }
+            }
+            const uint32_t sh = (uint32_t)(p & 31);
+            const bool ok = (p < n) && ((vw >> sh) & 1u);
+            if (!ok) {
+                if (run >= (uint64_t)k && prev_valid) {
+                    uint64_t x_last = p - (uint64_t)k + 1;
+                    if (x_last >= x0 && x_last < x1) {
+                        if (!c_known) {
+                            failed = true;
+                            break;
+                        }
+                        emit(x_last, true);
+                    }
+                }
+                run = 0;
+                anchored = true;
+                prev_valid = false;
+                c_known = false;
+                continue;
+            }
+            const uint32_t c = (uint32_t)((pw >> (2 * sh)) & 3u);
+            r1 = (r1 << 2) | (r0 >> 62);
+            r0 = (r0 << 2) | c;
+            run++;
+            if (run < (uint64_t)m) continue;
+            if (run == (uint64_t)m) {
+                nt_from_scratch(T, r0, r1, m - 1, m, fw, rc);
+            } else {
+                uint32_t out = hist_base(r0, r1, m);
+                fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[c];
+                rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[c];
+            }
+            const uint64_t i = p - (uint64_t)m + 1;  // newest m-mer position
+            const uint64_t val = nt_value(fw, rc);
+            const uint32_t isfw = (uint32_t)(fw < rc);
+            if (run < (uint64_t)(k - 1)) {
+                win_add(W, val, isfw, i, run == (uint64_t)m);
+                continue;
+            }
+            if (run == (uint64_t)(k - 1)) {
+                win_add(W, val, isfw, i, run == (uint64_t)m);
+            } else if (W.pos == i - (uint64_t)wn) {
+                win_recompute(W, T, r0, r1, k, m, i);  // the oldest occurrence of the minimum left
+            } else {
+                win_add(W, val, isfw, i, false);
+            }
+            const uint64_t x = p - (uint64_t)k + 2;  // window start
+            const uint64_t cur_raw = W.mv | (W.cnt == 1 ? (uint64_t)W.uraw : 0ull);
+            const uint64_t cur_pos = W.pos;
+            const uint32_t cur_fw = W.ufw;
+            if (run == (uint64_t)(k - 1)) {
+                if (anchored) {
+                    c_prev = x + 1;  // virtual first callback: the first superkmer starts at x
+                    c_known = true;
+                    first_sk = true;
+                } else {
+                    c_known = false;
+                }
+            } else {
+                // get_minimizer_splits split rule, batch_minqueue.rs:146-152
+                bool split = (cur_raw != prev_raw) || ((cur_raw & 1ull) && cur_pos != prev_pos);
+                if (split) {
+                    if (x >= x0 && x < x1) {
+                        if (!c_known) {
+                            failed = true;
+                            break;
+                        }
+                        emit(x, false);
+                    }
+                    c_prev = x;
+                    c_known = true;
+                    first_sk = false;
+                }
+            }
+            prev_raw = cur_raw;
+            prev_pos = cur_pos;
+            prev_fw = cur_fw;
+            prev_valid = true;
+        }
+        if (!failed) return;
+        if (xb == 0) break;  // cannot look back further
+        lb *= 4;
+    }
+    atomicOr(status, kStatusLookback);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan over u64 counts (3 phases; n up to a few million)
+// ---------------------------------------------------------------------------
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;
+
+__device__ unsigned long long block_excl_scan(unsigned long long v, unsigned long long *tmp, unsigned long long &total) {
+    // warp scan
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) tmp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long s = lane < (int)(blockDim.x >> 5) ? tmp[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        tmp[lane] = s;
+    }
+    __syncthreads();
+    unsigned long long base = wid > 0 ? tmp[wid - 1] : 0ull;
+    total = tmp[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_partials_kernel(const unsigned long long *__restrict__ in, uint64_t n,
+                                                                   unsigned long long *__restrict__ block_sums) {
+    __shared__ unsigned long long tmp[32];
+    uint64_t base = (uint64_t)blockIdx.x * kScanBlock * kScanItems + (uint64_t)threadIdx.x * kScanItems;
+    unsigned long long s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++)
+        if (base + j < n) s += in[base + j];
+    unsigned long long total;
+    block_excl_scan(s, tmp, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_top_kernel(unsigned long long *__restrict__ block_sums, uint64_t nb,
+                                                              unsigned long long *__restrict__ grand_total) {
+    __shared__ unsigned long long tmp[32];
+    unsigned long long carry = 0;
+    for (uint64_t s = 0; s < nb; s += kScanBlock) {
+        uint64_t i = s + threadIdx.x;
+        unsigned long long v = i < nb ? block_sums[i] : 0ull;
+        unsigned long long total;
+        unsigned long long ex = block_excl_scan(v, tmp, total);
+        if (i < nb) block_sums[i] = ex + carry;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && grand_total) *grand_total = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_final_kernel(const unsigned long long *__restrict__ in, uint64_t n,
+                                                                const unsigned long long *__restrict__ block_sums,
+                                                                unsigned long long *__restrict__ out) {
+    __shared__ unsigned long long tmp[32];
+    uint64_t base = (uint64_t)blockIdx.x * kScanBlock * kScanItems + (uint64_t)threadIdx.x * kScanItems;
+    unsigned long long v[kScanItems];
+    unsigned long long s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+        v[j] = base + j < n ? in[base + j] : 0ull;
+        s += v[j];
+    }
+    unsigned long long total;
+    unsigned long long ex = block_excl_scan(s, tmp, total) + block_sums[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+        if (base + j < n) out[base + j] = ex;
+        ex += v[j];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = ex;  // total at out[n]
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *valid, cudaStream_t s, int sms) {
+    uint64_t n_words = (n + 31) / 32;
+    if (n_words == 0) return 0;
+    int aligned = ((uintptr_t)d_text % 16) == 0;
+    uint64_t blocks = (n_words + 255) / 256;
+    uint64_t cap = (uint64_t)sms * 16;
+    if (blocks > cap) blocks = cap;
+    pack_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_text, n, n_words, aligned, packed, valid);
+    return 1;
+}
+
+int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
+                     int sbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, const unsigned long long *bin_off,
+                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s) {
+    uint64_t threads = (n + chunk - 1) / chunk;
+    if (threads == 0) return 0;
+    uint64_t blocks = (threads + 255) / 256;
+    if (write)
+        bucketize_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(packed, valid, n, k, m, bbits, sbits, canonical, chunk,
+                                                                 bin_count, bin_kmers, bin_off, bin_cursor, recs, status);
+    else
+        bucketize_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(packed, valid, n, k, m, bbits, sbits, canonical, chunk,
+                                                                  bin_count, bin_kmers, bin_off, bin_cursor, recs, status);
+    return 1;
+}
+
+uint64_t scan_temp_elems(uint64_t n) { return (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems) + 1; }
+
+int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
+                          unsigned long long *tmp, cudaStream_t s) {
+    if (n == 0) {
+        cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+        return 0;
+    }
+    uint64_t nb = (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+    scan_partials_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, tmp);
+    scan_top_kernel<<<1, kScanBlock, 0, s>>>(tmp, nb, nullptr);
+    scan_final_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, tmp, out);
+    return 3;
+}
+
+}  // namespace ggcat

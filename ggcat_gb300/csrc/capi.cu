@@ -1,0 +1,822 @@
+// C ABI of ggcat_gb300: context, device buffers, orchestration of the bucketing and merge
+// kernels, the host link stage, the FASTA reader and the file-level build entry point.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ggcat_gb300.h"
+#include "kernels.h"
+
+using namespace ggcat;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = cnt ? cnt : 1;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+};
+
+struct PinnedBuf {
+    uint8_t *p = nullptr;
+    size_t n = 0;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t ensure(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMallocHost(&p, cnt ? cnt : 1);
+        if (e == cudaSuccess) n = cnt ? cnt : 1;
+        return e;
+    }
+};
+
+struct HostUnitigs {
+    std::vector<uint8_t> bases;
+    std::vector<uint64_t> off;
+    std::vector<uint32_t> len;
+    std::vector<uint8_t> flags;
+    void clear() {
+        bases.clear();
+        off.clear();
+        len.clear();
+        flags.clear();
+    }
+};
+
+}  // namespace
+
+struct ggcat_gpu_ctx {
+    int device = 0;
+    int sms = 1;
+    std::string err;
+    uint64_t launches = 0;
+
+    // input staging
+    DevBuf<uint8_t> d_text;
+    PinnedBuf h_stage;
+
+    // bucketing
+    DevBuf<uint64_t> packed;
+    DevBuf<uint32_t> valid;
+    DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, bin_cursor, scan_tmp;
+    DevBuf<SkRec> recs;
+    DevBuf<unsigned> status;
+    uint64_t n_text = 0, n_recs = 0, n_kmers = 0, n_bins = 0;
+    uint32_t n_buckets = 0;
+    ggcat_gpu_params last_params{};
+    bool have_buckets = false;
+
+    // merge
+    DevBuf<MergeUnit> small_units, large_units, bucket_units;
+    DevBuf<unsigned long long> counters, ones;
+    DevBuf<uint64_t> tkeys;
+    DevBuf<uint32_t> tvals;
+    DevBuf<uint8_t> tvis;
+    DevBuf<uint8_t> out_bases;
+    DevBuf<uint64_t> out_off;
+    DevBuf<uint32_t> out_len;
+    DevBuf<uint8_t> out_flags;
+    DevBuf<uint64_t> kmer_keys;
+    DevBuf<uint32_t> kmer_mult;
+    uint64_t n_partial = 0, n_partial_bases = 0, n_kmers_out = 0;
+    bool have_merge = false;
+
+    HostUnitigs partial;  // copied back by build_text / on demand
+    bool partial_on_host = false;
+    HostUnitigs final_u;
+
+    cudaEvent_t ev[8] = {};
+    ggcat_gpu_stats stats{};
+
+    ~ggcat_gpu_ctx() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+static int fail(ggcat_gpu_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? GGCAT_GPU_ENOMEM : GGCAT_GPU_ECUDA,     \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+    } while (0)
+
+static cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" int ggcat_gpu_create(int device, ggcat_gpu_ctx **out) {
+    if (!out) return GGCAT_GPU_EINVAL;
+    *out = nullptr;
+    auto *ctx = new ggcat_gpu_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return GGCAT_GPU_ECUDA;
+    }
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    ctx->sms = sms > 0 ? sms : 1;
+    for (auto &ev : ctx->ev) {
+        if (cudaEventCreate(&ev) != cudaSuccess) {
+            delete ctx;
+            return GGCAT_GPU_ECUDA;
+        }
+    }
+    if (ctx->status.ensure(2) != cudaSuccess || ctx->counters.ensure(16) != cudaSuccess ||
+        ctx->ones.ensure(1) != cudaSuccess) {
+        delete ctx;
+        return GGCAT_GPU_ENOMEM;
+    }
+    unsigned long long one = 1;
+    cudaMemcpy(ctx->ones.p, &one, sizeof one, cudaMemcpyHostToDevice);
+    *out = ctx;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" void ggcat_gpu_destroy(ggcat_gpu_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    delete ctx;
+}
+
+extern "C" const char *ggcat_gpu_last_error(const ggcat_gpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" uint64_t ggcat_gpu_kernel_launches(const ggcat_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
+    if (!p) return fail(ctx, GGCAT_GPU_EINVAL, "null params");
+    if (p->m < 2 || p->m > 32) return fail(ctx, GGCAT_GPU_EINVAL, "minimizer length m=%d outside [2, 32]", p->m);
+    if (p->k - p->m < 2) return fail(ctx, GGCAT_GPU_EINVAL, "need k - m >= 2 (k=%d, m=%d)", p->k, p->m);
+    if (p->k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "k=%d > 64 is not supported on the device", p->k);
+    if (p->bucket_bits < 1 || p->bucket_bits > 15)
+        return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits=%d outside [1, 15]", p->bucket_bits);
+    if (p->second_bits < 0 || p->second_bits > 8)
+        return fail(ctx, GGCAT_GPU_EINVAL, "second_bits=%d outside [0, 8]", p->second_bits);
+    if (p->bucket_bits + 1 + kFineBits > 63) return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits too large");
+    return GGCAT_GPU_OK;
+}
+
+static int read_status(ggcat_gpu_ctx *ctx, unsigned *st) {
+    CK(cudaMemcpy(st, ctx->status.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len,
+                                   const ggcat_gpu_params *p, void *stream, uint64_t *n_superkmers) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (text_len >= (1ull << 40)) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "text longer than 2^40 bytes");
+    if (text_len > 0 && !d_text) return fail(ctx, GGCAT_GPU_EINVAL, "null text");
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    ctx->have_buckets = false;
+    ctx->have_merge = false;
+    ctx->partial_on_host = false;
+    const uint64_t n_words = (text_len + 31) / 32 + 1;
+    CK(ctx->packed.ensure(n_words));
+    CK(ctx->valid.ensure(n_words));
+    ctx->n_buckets = (1u << p->bucket_bits) + 1;
+    ctx->n_bins = (uint64_t)ctx->n_buckets << kFineBits;
+    const uint64_t nb = ctx->n_bins;
+    CK(ctx->bin_count.ensure(nb + 1));
+    CK(ctx->bin_kmers.ensure(nb + 1));
+    CK(ctx->bin_off.ensure(nb + 1));
+    CK(ctx->kmer_off.ensure(nb + 1));
+    CK(ctx->bin_cursor.ensure(nb + 1));
+    CK(ctx->scan_tmp.ensure(scan_temp_elems(nb) + 2));
+    CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
+    const int canonical = p->forward_only ? 0 : 1;
+    const uint64_t chunk = 512;
+
+    CK(cudaEventRecord(ctx->ev[0], s));
+    ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], s));
+    ctx->launches += launch_bucketize(false, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
+                                      p->second_bits, canonical, chunk, ctx->bin_count.p, ctx->bin_kmers.p, nullptr,
+                                      nullptr, nullptr, ctx->status.p, s);
+    CK(cudaGetLastError());
+    ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
+    ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
+    CK(cudaGetLastError());
+    unsigned long long totals[2];
+    CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->n_recs = totals[0];
+    ctx->n_kmers = totals[1];
+    CK(ctx->recs.ensure(ctx->n_recs + 1));
+    ctx->launches += launch_bucketize(true, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
+                                      p->second_bits, canonical, chunk, nullptr, nullptr, ctx->bin_off.p,
+                                      ctx->bin_cursor.p, ctx->recs.p, ctx->status.p, s);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[2], s));
+    ctx->n_text = text_len;
+    ctx->last_params = *p;
+    ctx->have_buckets = true;
+    ctx->stats = ggcat_gpu_stats{};
+    ctx->stats.text_bytes = text_len;
+    ctx->stats.superkmers = ctx->n_recs;
+    ctx->stats.kmer_instances = ctx->n_kmers;
+    if (n_superkmers) *n_superkmers = ctx->n_recs;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer *h_out, uint64_t cap, uint64_t *n) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_buckets) return fail(ctx, GGCAT_GPU_EINVAL, "no bucketize result");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    unsigned st = 0;
+    int rc = read_status(ctx, &st);
+    if (rc) return rc;
+    if (st & kStatusLookback) return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: lookback limit exceeded");
+    if (n) *n = ctx->n_recs;
+    if (!h_out) return GGCAT_GPU_OK;
+    uint64_t cnt = std::min<uint64_t>(cap, ctx->n_recs);
+    std::vector<SkRec> tmp(cnt);
+    if (cnt) CK(cudaMemcpy(tmp.data(), ctx->recs.p, cnt * sizeof(SkRec), cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < cnt; i++) {
+        const SkRec &r = tmp[i];
+        ggcat_gpu_superkmer o;
+        o.start = rec_start(r);
+        o.len = rec_len(r);
+        o.bucket = (uint16_t)rec_bucket(r);
+        o.second_bucket = (uint16_t)rec_second(r);
+        o.minimizer_pos = (uint16_t)rec_minpos(r);
+        o.rc = (uint8_t)rec_rc(r);
+        o.flags = (uint8_t)rec_flags(r);
+        h_out[i] = o;
+    }
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// merge
+// ---------------------------------------------------------------------------
+static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_t s, uint64_t bases_cap,
+                      uint64_t u_cap, uint64_t kmer_cap, unsigned *st_out) {
+    CK(ctx->out_bases.ensure(bases_cap));
+    CK(ctx->out_off.ensure(u_cap));
+    CK(ctx->out_len.ensure(u_cap));
+    CK(ctx->out_flags.ensure(u_cap));
+    if (p->keep_kmers) {
+        CK(ctx->kmer_keys.ensure(kmer_cap));
+        CK(ctx->kmer_mult.ensure(kmer_cap));
+    }
+    const uint64_t max_units = ctx->n_bins + 1;
+    CK(ctx->small_units.ensure(max_units));
+    CK(ctx->large_units.ensure(max_units));
+    // worst-case slot pool of the global-memory tables: cap < 2 * (1.25 x + 64) per unit
+    uint64_t pool = ctx->n_kmers * 5 / 2 + 128ull * (ctx->n_buckets + ctx->n_kmers / 4096 + 1) + 1024;
+    CK(ctx->tkeys.ensure(pool));
+    CK(ctx->tvals.ensure(pool));
+    CK(ctx->tvis.ensure(pool));
+    CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+
+    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers};
+    MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
+               u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
+               p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
+    const uint64_t small_limit = 6500;
+    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : 4096;
+    if (target > small_limit) target = small_limit;
+
+    CK(cudaEventRecord(ctx->ev[3], s));
+    if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) {
+        // plain form: every bucket is one unit with a global-memory table, three launches per bucket
+        std::vector<unsigned long long> hoff(ctx->n_bins + 1), hk(ctx->n_bins + 1);
+        CK(cudaMemcpyAsync(hoff.data(), ctx->bin_off.p, (ctx->n_bins + 1) * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hk.data(), ctx->kmer_off.p, (ctx->n_bins + 1) * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::vector<MergeUnit> units(ctx->n_buckets);
+        uint64_t slot = 0;
+        for (uint32_t b = 0; b < ctx->n_buckets; b++) {
+            uint64_t b0 = (uint64_t)b << kFineBits, b1 = (uint64_t)(b + 1) << kFineBits;
+            MergeUnit u{};
+            u.rec_begin = hoff[b0];
+            u.rec_end = hoff[b1];
+            u.kmers = hk[b1] - hk[b0];
+            uint64_t cap = 64;
+            while (cap < u.kmers + u.kmers / 4 + 64) cap <<= 1;
+            u.table_off = slot;
+            u.table_cap = (uint32_t)cap;
+            u.bucket = b;
+            slot += cap;
+            units[b] = u;
+        }
+        if (slot > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "per-bucket table pool too small");
+        CK(ctx->bucket_units.ensure(ctx->n_buckets));
+        CK(cudaMemcpyAsync(ctx->bucket_units.p, units.data(), units.size() * sizeof(MergeUnit),
+                           cudaMemcpyHostToDevice, s));
+        ctx->launches += launch_init_tables(ctx->tkeys.p, ctx->tvals.p, ctx->tvis.p, slot, ctx->sms, s);
+        for (uint32_t b = 0; b < ctx->n_buckets; b++) {
+            if (units[b].rec_end == units[b].rec_begin) continue;
+            ctx->launches += launch_merge_large(a, ctx->bucket_units.p + b, ctx->ones.p, 1, ctx->tkeys.p, ctx->tvals.p,
+                                                ctx->tvis.p, o, ctx->sms, s);
+        }
+        CK(cudaGetLastError());
+        ctx->stats.merge_units_small = 0;
+        ctx->stats.merge_units_large = ctx->n_buckets;
+    } else {
+        ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, small_limit, target,
+                                               ctx->small_units.p, ctx->large_units.p, max_units, ctx->tkeys.n,
+                                               ctx->counters.p, ctx->status.p + 1, s);
+        // initialise exactly the slots the large units claimed (counters[6])
+        ctx->launches += launch_init_tables_dyn(ctx->tkeys.p, ctx->tvals.p, ctx->tvis.p, ctx->counters.p + 6,
+                                                ctx->tkeys.n, ctx->sms, s);
+        ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
+        ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + 5, 0, ctx->tkeys.p, ctx->tvals.p,
+                                            ctx->tvis.p, o, ctx->sms, s);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(ctx->ev[4], s));
+    unsigned long long cnt[8];
+    CK(cudaMemcpyAsync(cnt, ctx->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, s));
+    unsigned stw[2] = {0, 0};
+    CK(cudaMemcpyAsync(stw, ctx->status.p, sizeof stw, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    unsigned st = stw[0] | stw[1];
+    ctx->n_partial = cnt[0];
+    ctx->n_partial_bases = cnt[1];
+    ctx->n_kmers_out = cnt[2];
+    if (p->merge_mode != GGCAT_MERGE_PER_BUCKET) {
+        ctx->stats.merge_units_small = cnt[4];
+        ctx->stats.merge_units_large = cnt[5];
+        if (cnt[6] > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "large-unit table pool exceeded");
+    }
+    *st_out = st;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (!ctx->have_buckets) return fail(ctx, GGCAT_GPU_EINVAL, "merge needs a bucketize result");
+    if (p->k != ctx->last_params.k || p->m != ctx->last_params.m || p->bucket_bits != ctx->last_params.bucket_bits)
+        return fail(ctx, GGCAT_GPU_EINVAL, "merge parameters differ from the bucketize parameters");
+    if (p->k > 32 || (p->k % 2) == 0)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports odd k <= 32 (k=%d)", p->k);
+    if (p->hash_kind != GGCAT_HASH_SEQHASH && p->hash_kind != 0)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge for k<=32 uses the 64-bit seq-hash");
+    if (p->min_multiplicity < 1) return fail(ctx, GGCAT_GPU_EINVAL, "min_multiplicity must be >= 1");
+    if (ctx->n_kmers >= (1ull << 29) * 1024ull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "input too large");
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    ctx->have_merge = false;
+    ctx->partial_on_host = false;
+    uint64_t bases_cap = ctx->n_kmers / 2 + (uint64_t)p->k * (ctx->n_recs / 2) + 4096;
+    uint64_t u_cap = ctx->n_recs + 1024;
+    uint64_t kmer_cap = ctx->n_kmers + 1024;
+    unsigned st = 0;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        rc = merge_once(ctx, p, s, bases_cap, u_cap, kmer_cap, &st);
+        if (rc) return rc;
+        if (!(st & (kStatusOutOverflow | kStatusKmerOverflow))) break;
+        bases_cap = std::max<uint64_t>(bases_cap, ctx->n_partial_bases + 4096);
+        u_cap = std::max<uint64_t>(u_cap, ctx->n_partial + 1024);
+        kmer_cap = std::max<uint64_t>(kmer_cap, ctx->n_kmers_out + 1024);
+    }
+    if (st & (kStatusOutOverflow | kStatusKmerOverflow)) return fail(ctx, GGCAT_GPU_EDEVICE, "merge output overflow");
+    if (st & kStatusTableFull) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: hash table full");
+    if (st & kStatusWalkLimit) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: unitig walk bound exceeded");
+    if (st & kStatusLookback) return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: internal lookback/partition error");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    ctx->stats.ms_pack = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    ctx->stats.ms_bucketize = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+    ctx->stats.ms_merge = ms;
+    ctx->stats.partial_unitigs = ctx->n_partial;
+    ctx->stats.partial_bases = ctx->n_partial_bases;
+    ctx->stats.surviving_kmers = ctx->n_kmers_out;
+    ctx->have_merge = true;
+    return GGCAT_GPU_OK;
+}
+
+static int fetch_partial(ggcat_gpu_ctx *ctx) {
+    if (ctx->partial_on_host) return GGCAT_GPU_OK;
+    HostUnitigs &h = ctx->partial;
+    h.bases.resize(ctx->n_partial_bases);
+    h.off.resize(ctx->n_partial);
+    h.len.resize(ctx->n_partial);
+    h.flags.resize(ctx->n_partial);
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->n_partial_bases)
+        CK(cudaMemcpy(h.bases.data(), ctx->out_bases.p, ctx->n_partial_bases, cudaMemcpyDeviceToHost));
+    if (ctx->n_partial) {
+        CK(cudaMemcpy(h.off.data(), ctx->out_off.p, ctx->n_partial * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h.len.data(), ctx->out_len.p, ctx->n_partial * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h.flags.data(), ctx->out_flags.p, ctx->n_partial, cudaMemcpyDeviceToHost));
+    }
+    ctx->partial_on_host = true;
+    return GGCAT_GPU_OK;
+}
+
+static int copy_unitigs_out(const HostUnitigs &h, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,
+                            uint32_t *h_len, uint8_t *h_flags, uint64_t cap, uint64_t *n_unitigs, uint64_t *n_bases) {
+    if (n_unitigs) *n_unitigs = h.off.size();
+    if (n_bases) *n_bases = h.bases.size();
+    if (h_bases) memcpy(h_bases, h.bases.data(), std::min<uint64_t>(bases_cap, h.bases.size()));
+    uint64_t n = std::min<uint64_t>(cap, h.off.size());
+    if (h_off) memcpy(h_off, h.off.data(), n * sizeof(uint64_t));
+    if (h_len) memcpy(h_len, h.len.data(), n * sizeof(uint32_t));
+    if (h_flags) memcpy(h_flags, h.flags.data(), n);
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_partial_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap,
+                                              uint64_t *h_off, uint32_t *h_len, uint8_t *h_flags, uint64_t cap,
+                                              uint64_t *n_unitigs, uint64_t *n_bases) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
+    int rc = fetch_partial(ctx);
+    if (rc) return rc;
+    return copy_unitigs_out(ctx->partial, h_bases, bases_cap, h_off, h_len, h_flags, cap, n_unitigs, n_bases);
+}
+
+extern "C" int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint64_t *h_mult, uint64_t cap, uint64_t *n) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
+    if (n) *n = ctx->n_kmers_out;
+    if (!h_kmers) return GGCAT_GPU_OK;
+    uint64_t cnt = std::min<uint64_t>(cap, ctx->n_kmers_out);
+    CK(cudaSetDevice(ctx->device));
+    if (cnt) {
+        CK(cudaMemcpy(h_kmers, ctx->kmer_keys.p, cnt * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> m(cnt);
+        CK(cudaMemcpy(m.data(), ctx->kmer_mult.p, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < cnt; i++) h_mult[i] = m[i];
+    }
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host link stage
+// ---------------------------------------------------------------------------
+static inline uint8_t code_of(uint8_t a) { return (a >> 1) & 3; }
+
+static uint64_t canon_ascii(const uint8_t *s, int k) {
+    uint64_t fw = 0, rc = 0;
+    for (int i = 0; i < k; i++) {
+        fw |= (uint64_t)code_of(s[i]) << (2 * i);
+        rc |= (uint64_t)(code_of(s[k - 1 - i]) ^ 2) << (2 * i);
+    }
+    return fw < rc ? fw : rc;
+}
+
+static void rc_append(std::vector<uint8_t> &dst, const uint8_t *s, size_t n, size_t skip) {
+    // append reverse complement of s[0..n), skipping its first `skip` bases
+    for (size_t i = skip; i < n; i++) {
+        uint8_t c = s[n - 1 - i];
+        dst.push_back(c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A');
+    }
+}
+
+extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
+    if (k < 3 || k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 32");
+    int rc = fetch_partial(ctx);
+    if (rc) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    const HostUnitigs &P = ctx->partial;
+    HostUnitigs &F = ctx->final_u;
+    F.clear();
+    const size_t n = P.off.size();
+    // endpoints: 2i = left end (backward link), 2i+1 = right end (forward link)
+    std::vector<int64_t> partner(2 * n, -1);
+    std::unordered_map<uint64_t, int64_t> first_end;
+    first_end.reserve(n);
+    for (size_t i = 0; i < n; i++) {
+        for (int side = 0; side < 2; side++) {
+            if (!(P.flags[i] & (side ? 2 : 1))) continue;
+            const uint8_t *s = P.bases.data() + P.off[i] + (side ? P.len[i] - k : 0);
+            uint64_t key = canon_ascii(s, k);
+            auto it = first_end.find(key);
+            int64_t ep = (int64_t)(2 * i + side);
+            if (it == first_end.end()) {
+                first_end.emplace(key, ep);
+            } else if (it->second >= 0) {
+                partner[it->second] = ep;
+                partner[ep] = it->second;
+                it->second = -1;
+            }
+        }
+    }
+    std::vector<uint8_t> done(n, 0);
+    auto emit_chain = [&](size_t i, int enter_side) {
+        size_t start_len = F.bases.size();
+        size_t cur = i;
+        int enter = enter_side;
+        bool circ = false;
+        bool first = true;
+        for (;;) {
+            done[cur] = 1;
+            const uint8_t *s = P.bases.data() + P.off[cur];
+            size_t L = P.len[cur];
+            size_t skip = first ? 0 : (size_t)k;
+            if (enter == 0)
+                F.bases.insert(F.bases.end(), s + skip, s + L);
+            else
+                rc_append(F.bases, s, L, skip);
+            first = false;
+            int64_t exit_ep = (int64_t)(2 * cur + (enter == 0 ? 1 : 0));
+            int64_t nxt = partner[exit_ep];
+            if (nxt < 0) break;
+            size_t nu = (size_t)nxt / 2;
+            if (done[nu]) {
+                circ = (nu == i);
+                break;
+            }
+            cur = nu;
+            enter = (int)(nxt % 2);
+        }
+        if (circ) F.bases.resize(F.bases.size() - 1);  // the string ended with its first k-mer
+        F.off.push_back(start_len);
+        F.len.push_back((uint32_t)(F.bases.size() - start_len));
+        F.flags.push_back(circ ? 4 : 0);
+    };
+    for (size_t i = 0; i < n; i++) {
+        if (done[i]) continue;
+        if (!(P.flags[i] & 3)) {
+            done[i] = 1;
+            size_t st = F.bases.size();
+            F.bases.insert(F.bases.end(), P.bases.begin() + P.off[i], P.bases.begin() + P.off[i] + P.len[i]);
+            F.off.push_back(st);
+            F.len.push_back(P.len[i]);
+            F.flags.push_back(P.flags[i] & 4);
+            continue;
+        }
+        if (partner[2 * i] < 0)
+            emit_chain(i, 0);
+        else if (partner[2 * i + 1] < 0)
+            emit_chain(i, 1);
+    }
+    for (size_t i = 0; i < n; i++)
+        if (!done[i]) emit_chain(i, 0);
+    auto t1 = std::chrono::steady_clock::now();
+    ctx->stats.ms_link = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    ctx->stats.final_unitigs = F.off.size();
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,
+                                      uint32_t *h_len, uint8_t *h_flags, uint64_t cap, uint64_t *n_unitigs,
+                                      uint64_t *n_bases) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    return copy_unitigs_out(ctx->final_u, h_bases, bases_cap, h_off, h_len, h_flags, cap, n_unitigs, n_bases);
+}
+
+extern "C" int ggcat_gpu_get_stats(const ggcat_gpu_ctx *ctx, ggcat_gpu_stats *out) {
+    if (!ctx || !out) return GGCAT_GPU_EINVAL;
+    *out = ctx->stats;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, uint64_t text_len,
+                                    const ggcat_gpu_params *p, void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (text_len > 0 && !h_text) return fail(ctx, GGCAT_GPU_EINVAL, "null text");
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->d_text.ensure(text_len + 64));
+    // stage through pinned memory so the copy is a true async DMA
+    cudaPointerAttributes attr{};
+    bool pinned = cudaPointerGetAttributes(&attr, h_text) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    if (pinned) {
+        CK(cudaMemcpyAsync(ctx->d_text.p, h_text, text_len, cudaMemcpyHostToDevice, s));
+    } else {
+        const uint64_t chunk = 64ull << 20;
+        CK(ctx->h_stage.ensure(2 * chunk));
+        for (uint64_t o = 0, i = 0; o < text_len; o += chunk, i++) {
+            uint64_t nb = std::min<uint64_t>(chunk, text_len - o);
+            uint8_t *st = ctx->h_stage.p + (i & 1) * chunk;
+            if (i >= 2) CK(cudaStreamSynchronize(s));
+            memcpy(st, h_text + o, nb);
+            CK(cudaMemcpyAsync(ctx->d_text.p + o, st, nb, cudaMemcpyHostToDevice, s));
+        }
+    }
+    uint64_t nsk = 0;
+    int rc = ggcat_gpu_bucketize(ctx, ctx->d_text.p, text_len, p, stream, &nsk);
+    if (rc) return rc;
+    rc = ggcat_gpu_merge(ctx, p, stream);
+    if (rc) return rc;
+    return fetch_partial(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// FASTA reader: the line state machine of SequencesReader::process_fasta
+// (crates/io/src/sequences_reader.rs:106-182) over 4 MiB read buffers
+// (LinesReader::process_lines, crates/io/src/lines_reader.rs:147-213).
+// ---------------------------------------------------------------------------
+namespace {
+struct FastaParser {
+    static constexpr size_t kBuf = 4u << 20;
+    std::vector<uint8_t> seq;
+    bool on_comment = false, new_line = true, ident = false;
+    int64_t copyback;
+    size_t flush_size;
+    uint8_t *out;
+    uint64_t cap, used = 0, pieces = 0;
+    uint8_t norm[256];
+
+    FastaParser(int64_t cb, uint8_t *o, uint64_t c) : copyback(cb), out(o), cap(c) {
+        size_t cbz = cb > 0 ? (size_t)cb * 2 : 0;
+        flush_size = std::max(kBuf, cbz);
+        for (int i = 0; i < 256; i++) norm[i] = 'N';
+        const char *v = "ACGT";
+        for (int i = 0; i < 4; i++) {
+            norm[(uint8_t)v[i]] = (uint8_t)v[i];
+            norm[(uint8_t)(v[i] | 0x20)] = (uint8_t)v[i];
+        }
+    }
+    void emit() {
+        if (out && used + seq.size() + 1 <= cap) {
+            for (size_t i = 0; i < seq.size(); i++) out[used + i] = norm[seq[i]];
+            out[used + seq.size()] = '\n';
+        }
+        used += seq.size() + 1;
+        pieces++;
+    }
+    void line(const uint8_t *l, size_t len, bool partial, bool finished) {
+        if (on_comment) {
+            on_comment = !partial;
+        } else if (finished || (new_line && len > 0 && l[0] == '>')) {
+            if (!seq.empty()) emit();
+            seq.clear();
+            ident = partial;
+        } else if (new_line && len > 0 && l[0] == ';') {
+            on_comment = true;
+        } else if (ident) {
+            if (!partial) ident = false;
+        } else {
+            seq.insert(seq.end(), l, l + len);
+        }
+        if (copyback >= 0 && seq.size() >= flush_size) {
+            emit();
+            size_t cb = (size_t)copyback;
+            std::vector<uint8_t> tail(seq.end() - (long)cb, seq.end());
+            seq.swap(tail);
+        }
+        new_line = !partial;
+    }
+    void run(const uint8_t *file, uint64_t n) {
+        for (uint64_t base = 0; base < n; base += kBuf) {
+            uint64_t blen = std::min<uint64_t>(kBuf, n - base);
+            const uint8_t *buf = file + base;
+            uint64_t p = 0;
+            for (;;) {
+                const uint8_t *nl = (const uint8_t *)memchr(buf + p, '\n', blen - p);
+                if (nl) {
+                    uint64_t pos = (uint64_t)(nl - buf), bpos = pos;
+                    if (bpos != p && buf[bpos - 1] == '\r') bpos--;
+                    line(buf + p, bpos - p, false, false);
+                    p = pos + 1;
+                } else {
+                    uint64_t l = blen - p;
+                    if (l > 0 && buf[blen - 1] == '\r') l--;
+                    if (l > 0) line(buf + p, l, true, false);
+                    break;
+                }
+            }
+        }
+        line(nullptr, 0, false, true);
+    }
+};
+}  // namespace
+
+extern "C" int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copyback, uint8_t *h_text,
+                                     uint64_t text_cap, uint64_t *text_len, uint64_t *n_pieces) {
+    if (!h_file && file_len) return GGCAT_GPU_EINVAL;
+    FastaParser fp(copyback, h_text, h_text ? text_cap : 0);
+    fp.run(h_file, file_len);
+    if (text_len) *text_len = fp.used;
+    if (n_pieces) *n_pieces = fp.pieces;
+    if (h_text && fp.used > text_cap) return GGCAT_GPU_EINVAL;
+    return GGCAT_GPU_OK;
+}
+
+static bool read_file(const char *path, std::vector<uint8_t> &out) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return false;
+    fseek(f, 0, SEEK_END);
+    long sz = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    out.resize(sz > 0 ? (size_t)sz : 0);
+    size_t got = sz > 0 ? fread(out.data(), 1, (size_t)sz, f) : 0;
+    fclose(f);
+    return got == out.size();
+}
+
+// buckets count heuristic of compute_stats_from_input_blocks (crates/io/src/lib.rs:67-140)
+static void bucket_counts_for(uint64_t bases, int *bbits, int *sbits) {
+    const uint64_t MAX_BUCKET_SIZE = 1ull << 30, MIN_BUCKET_SIZE = 512ull << 10;
+    uint64_t bc = std::max<uint64_t>(std::min<uint64_t>(1024, bases / MIN_BUCKET_SIZE), bases / MAX_BUCKET_SIZE);
+    uint64_t p2 = 1;
+    while (p2 < bc) p2 <<= 1;
+    p2 = std::max<uint64_t>(std::min<uint64_t>(p2, 1ull << 13), 1ull << 2);
+    int b = 0;
+    while ((1ull << b) < p2) b++;
+    uint64_t per = bases / p2;
+    uint64_t sc = std::max<uint64_t>(std::min<uint64_t>(64, per / (2 * 1024)), per / (4ull << 20));
+    uint64_t s2 = 1;
+    while (s2 < sc) s2 <<= 1;
+    s2 = std::max<uint64_t>(std::min<uint64_t>(s2, 1ull << 8), 1ull << 1);
+    int s = 0;
+    while ((1ull << s) < s2) s++;
+    *bbits = b;
+    *sbits = s;
+}
+
+extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
+                                          const char *output_file, size_t kmer_length, size_t threads_count,
+                                          int forward_only, size_t minimizer_length, size_t min_multiplicity) {
+    (void)threads_count;
+    if (!ctx || !input_files || !output_file) return GGCAT_GPU_EINVAL;
+    std::vector<uint8_t> text;
+    uint64_t est = 0;
+    for (size_t i = 0; i < n_inputs; i++) {
+        std::vector<uint8_t> file;
+        if (!read_file(input_files[i], file)) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", input_files[i]);
+        est += file.size();
+        uint64_t need = 0, pieces = 0;
+        ggcat_gpu_fasta_parse(file.data(), file.size(), (int64_t)kmer_length - 1, nullptr, 0, &need, &pieces);
+        size_t o = text.size();
+        text.resize(o + need);
+        ggcat_gpu_fasta_parse(file.data(), file.size(), (int64_t)kmer_length - 1, text.data() + o, need, &need, &pieces);
+    }
+    ggcat_gpu_params p{};
+    p.k = (int)kmer_length;
+    // compute_best_m (crates/utils/src/lib.rs:29-40) when minimizer_length == SIZE_MAX
+    if (minimizer_length == (size_t)-1) {
+        int k = p.k;
+        p.m = k <= 13 ? std::max(k / 2, k - 4) : k <= 15 ? 9 : k <= 21 ? 10 : k <= 30 ? 11 : k <= 37 ? 12 : k <= 42 ? 13 : 14;
+    } else {
+        p.m = (int)minimizer_length;
+    }
+    bucket_counts_for(est, &p.bucket_bits, &p.second_bits);
+    p.min_multiplicity = (int)min_multiplicity;
+    p.hash_kind = GGCAT_HASH_SEQHASH;
+    p.forward_only = forward_only;
+    p.merge_mode = GGCAT_MERGE_BATCHED;
+    int rc = ggcat_gpu_build_text(ctx, text.data(), text.size(), &p, nullptr);
+    if (rc) return rc;
+    rc = ggcat_gpu_link(ctx, p.k);
+    if (rc) return rc;
+    FILE *f = fopen(output_file, "wb");
+    if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot write %s", output_file);
+    const HostUnitigs &F = ctx->final_u;
+    for (size_t i = 0; i < F.off.size(); i++) {
+        fprintf(f, ">%zu LN:i:%u\n", i, F.len[i]);  // fasta.rs:183-184
+        fwrite(F.bases.data() + F.off[i], 1, F.len[i], f);
+        fputc('\n', f);
+    }
+    fclose(f);
+    return GGCAT_GPU_OK;
+}

@@ -1,0 +1,70 @@
+// Host-side launchers of the device kernels (internal to the library).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ggcat {
+
+// bucketing.cu — each launcher returns the number of kernels it launched
+int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *valid, cudaStream_t s, int sms);
+int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
+                     int sbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, const unsigned long long *bin_off,
+                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s);
+uint64_t scan_temp_elems(uint64_t n);
+// out has n+1 entries: exclusive prefix sums and the total at out[n]
+int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
+                          unsigned long long *tmp, cudaStream_t s);
+
+// merge.cu
+struct MergeUnit {
+    uint64_t rec_begin, rec_end;  // record range in the bucket store
+    uint64_t kmers;               // k-mer instances
+    uint64_t table_off;           // large units: slot offset in the global table pool
+    uint32_t table_cap;           // large units: capacity (power of two)
+    uint32_t bucket;
+};
+
+struct MergeOut {
+    uint8_t *bases;               // partial unitig bases (ASCII)
+    unsigned long long bases_cap;
+    uint64_t *u_off;              // per partial unitig: offset into bases
+    uint32_t *u_len;
+    uint8_t *u_flags;             // bit0 bw link, bit1 fw link, bit2 circular
+    unsigned long long u_cap;
+    unsigned long long *counters; // [0] unitigs, [1] bases, [2] kmers, [3] queue head, [4] small units,
+                                  // [5] large units, [6] large slots, [7] queue head 2
+    uint64_t *kmer_keys;          // optional k-mer dump
+    uint32_t *kmer_mult;
+    unsigned long long kmer_cap;
+    unsigned *status;
+};
+
+struct MergeArgs {
+    const uint64_t *packed;
+    const SkRec *recs;
+    int k;
+    int min_mult;
+    int keep_kmers;
+};
+
+constexpr int kSmallSlots = 8192;     // shared-memory table capacity of one merge CTA
+constexpr int kMergeThreads = 256;
+
+int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
+                          uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units, MergeUnit *large_units,
+                          uint64_t max_units, uint64_t pool_slots, unsigned long long *counters, unsigned *status,
+                          cudaStream_t s);
+int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
+                       const MergeOut &o, int sms, cudaStream_t s);
+int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
+                       uint64_t n_units_host_hint, uint64_t *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
+                       int sms, cudaStream_t s);
+int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
+// initialises the first *n_slots_dev slots (read on the device), at most max_slots
+int launch_init_tables_dyn(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
+                           uint64_t max_slots, int sms, cudaStream_t s);
+
+}  // namespace ggcat

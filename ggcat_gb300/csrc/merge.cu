@@ -1,0 +1,491 @@
+// Per-sub-bucket k-mer merge on sm_103a.
+//
+// Replaces assembler_kmers_merge's per-bucket work (ParallelKmersMergeFinalExecutor::process_map,
+// crates/assembler_kmers_merge/src/final_executor.rs:277-509, with the unitig extenders of
+// crates/assembler_kmers_merge/src/unitigs_extender/{sorting,hashmap}.rs).  A merge unit is a
+// run of sub-bins of one bucket, i.e. a union of whole minimizer groups, so the k-mer
+// multiplicities (MapEntry counting with the both-ends halving rule,
+// crates/structs/src/map_entry.rs:79-84) and the within-unit unitig extension follow the
+// hash-map extender exactly (hashmap.rs:162-297, 361-601).
+//
+// Small units (<= kSmallSlots table slots) are processed one per CTA by a persistent kernel
+// that keeps the unit's hash table in shared memory; large units use a global-memory table
+// processed grid-wide by three kernels (insert, extend, cycles).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ggcat {
+
+struct Table {
+    uint64_t *keys;
+    uint32_t *vals;  // count (30 bits) | flags << 30 (bit30: begin ignored, bit31: end ignored)
+    uint8_t *vis;
+    uint32_t cap;    // power of two
+};
+
+constexpr uint32_t kCountMask = (1u << 30) - 1;
+
+__device__ __forceinline__ uint32_t slot_of(uint64_t key, uint32_t cap) { return (uint32_t)mix64(key) & (cap - 1); }
+
+__device__ __forceinline__ int64_t tfind(const Table &t, uint64_t key) {
+    uint32_t s = slot_of(key, t.cap);
+    for (uint32_t probe = 0; probe < t.cap; probe++) {
+        uint64_t kk = t.keys[s];
+        if (kk == key) return s;
+        if (kk == kEmptyKey) return -1;
+        s = (s + 1) & (t.cap - 1);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int64_t tinsert(const Table &t, uint64_t key, unsigned *status) {
+    uint32_t s = slot_of(key, t.cap);
+    for (uint32_t probe = 0; probe < t.cap; probe++) {
+        uint64_t kk = t.keys[s];
+        if (kk == key) return s;
+        if (kk == kEmptyKey) {
+            unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&t.keys[s]),
+                                               (unsigned long long)kEmptyKey, (unsigned long long)key);
+            if (old == kEmptyKey || old == key) return s;
+        }
+        s = (s + 1) & (t.cap - 1);
+    }
+    atomicOr(status, kStatusTableFull);
+    return -1;
+}
+
+// MapEntry::get_kmer_multiplicity (map_entry.rs:79-84): halve when both ends were ignored.
+__device__ __forceinline__ uint32_t val_mult(uint32_t v) {
+    uint32_t c = v & kCountMask;
+    return (v >> 30) == 3u ? (c >> 1) : c;
+}
+
+struct Graph {
+    Table t;
+    int k;
+    uint32_t min_mult;
+
+    __device__ __forceinline__ uint64_t canon(uint64_t v) const {
+        uint64_t r = rc_packed(v, k);
+        return v < r ? v : r;
+    }
+    // slot of an oriented k-mer if present and surviving, else -1
+    __device__ __forceinline__ int64_t alive(uint64_t v) const {
+        int64_t s = tfind(t, canon(v));
+        if (s < 0) return -1;
+        return val_mult(t.vals[s]) >= min_mult ? s : -1;
+    }
+    // surviving successors of oriented v; *only receives the last one found
+    __device__ __forceinline__ int succ(uint64_t v, uint64_t &only) const {
+        int d = 0;
+        uint64_t base = v >> 2;
+#pragma unroll
+        for (uint32_t b = 0; b < 4; b++) {
+            uint64_t u = base | ((uint64_t)b << (2 * (k - 1)));
+            if (alive(u) >= 0) {
+                d++;
+                only = u;
+            }
+        }
+        return d;
+    }
+    // ignored-side flags in the orientation of v (hashmap.rs:453-465):
+    // canonical orientation: flags == 1 -> left boundary, flags == 2 -> right boundary.
+    __device__ __forceinline__ bool right_boundary(uint64_t v, int64_t slot) const {
+        uint32_t f = t.vals[slot] >> 30;
+        bool is_canon = v <= rc_packed(v, k);
+        return is_canon ? f == 2u : f == 1u;
+    }
+    __device__ __forceinline__ bool left_boundary(uint64_t v, int64_t slot) const {
+        uint32_t f = t.vals[slot] >> 30;
+        bool is_canon = v <= rc_packed(v, k);
+        return is_canon ? f == 1u : f == 2u;
+    }
+    // Traversable successor: unique surviving successor u with a unique surviving
+    // predecessor, no bucket boundary between them, and not the same k-mer.
+    __device__ __forceinline__ bool next(uint64_t v, int64_t sv, uint64_t &u, int64_t &su) const {
+        if (right_boundary(v, sv)) return false;
+        if (succ(v, u) != 1) return false;
+        su = tfind(t, canon(u));
+        if (su == sv) return false;
+        uint64_t w;
+        if (succ(rc_packed(u, k), w) != 1) return false;
+        if (left_boundary(u, su)) return false;
+        return true;
+    }
+    __device__ __forceinline__ bool is_start(uint64_t v, int64_t sv) const {
+        if (left_boundary(v, sv)) return true;
+        uint64_t w;
+        if (succ(rc_packed(v, k), w) != 1) return true;
+        uint64_t y = rc_packed(w, k);  // the unique predecessor, oriented towards v
+        int64_t sy = tfind(t, canon(y));
+        if (sy == sv) return true;
+        uint64_t z;
+        if (succ(y, z) != 1) return true;
+        if (right_boundary(y, sy)) return true;
+        return false;
+    }
+};
+
+__device__ __forceinline__ char base_char(uint32_t c) { return "ACTG"[c & 3]; }
+
+// Walk a path from start v; returns the end node and the number of steps.
+__device__ __forceinline__ uint32_t walk_to_end(const Graph &g, uint64_t v, int64_t sv, uint64_t &end, int64_t &send,
+                                                unsigned *status) {
+    uint32_t steps = 0;
+    uint64_t cur = v;
+    int64_t scur = sv;
+    for (;;) {
+        uint64_t u;
+        int64_t su;
+        if (!g.next(cur, scur, u, su)) break;
+        cur = u;
+        scur = su;
+        if (++steps > g.t.cap) {
+            atomicOr(status, kStatusWalkLimit);
+            break;
+        }
+    }
+    end = cur;
+    send = scur;
+    return steps;
+}
+
+// Emit the path (or cycle of `steps` edges when circular) starting at v.
+__device__ void emit_walk(const Graph &g, uint64_t v, int64_t sv, uint32_t steps, uint8_t flags, const MergeOut &o) {
+    const int k = g.k;
+    uint64_t len = (uint64_t)k + steps;
+    unsigned long long off = atomicAdd(&o.counters[1], (unsigned long long)len);
+    unsigned long long idx = atomicAdd(&o.counters[0], 1ull);
+    bool ok = (off + len <= o.bases_cap) && (idx < o.u_cap);
+    if (!ok) atomicOr(o.status, kStatusOutOverflow);
+    if (ok) {
+        o.u_off[idx] = off;
+        o.u_len[idx] = (uint32_t)len;
+        o.u_flags[idx] = flags;
+        for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
+    }
+    g.t.vis[sv] = 1;
+    uint64_t cur = v;
+    int64_t scur = sv;
+    for (uint32_t s = 0; s < steps; s++) {
+        uint64_t u;
+        int64_t su;
+        if (!g.next(cur, scur, u, su)) break;
+        if (ok) o.bases[off + k + s] = base_char((uint32_t)(u >> (2 * (k - 1))));
+        g.t.vis[su] = 1;
+        cur = u;
+        scur = su;
+    }
+}
+
+// Insert all k-mers of one superkmer record (hashmap.rs:361-431 add_sequence), processing
+// the bases in text orientation with the flags mapped from the stored orientation.
+__device__ __forceinline__ void insert_record(const Table &t, const uint64_t *__restrict__ packed, const SkRec r, int k,
+                                              unsigned *status) {
+    const uint64_t start = rec_start(r);
+    const uint32_t len = rec_len(r);
+    const uint32_t fl = rec_flags(r), rcf = rec_rc(r);
+    // text-orientation included flags: begin <- stored end when reverse-complemented
+    const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
+    const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
+    const uint64_t mask = kmer_mask(k);
+    uint64_t fw = 0, rc = 0;
+    uint64_t cur_word = ~0ull, pw = 0;
+    const uint32_t last = len - (uint32_t)k;
+    for (uint32_t i = 0; i < len; i++) {
+        uint64_t p = start + i;
+        uint64_t wi = p >> 5;
+        if (wi != cur_word) {
+            cur_word = wi;
+            pw = packed[wi];
+        }
+        uint64_t c = (pw >> (2 * (p & 31))) & 3u;
+        fw = (fw >> 2) | (c << (2 * (k - 1)));
+        rc = ((rc << 2) | (c ^ 2u)) & mask;
+        if (i + 1 < (uint32_t)k) continue;
+        uint32_t idx = i + 1 - (uint32_t)k;
+        bool begin_ignored = (idx == 0) && !inc_begin;
+        bool end_ignored = (idx == last) && !inc_end;
+        uint32_t isf = fw < rc ? 1u : 0u;
+        uint64_t key = isf ? fw : rc;
+        int64_t s = tinsert(t, key, status);
+        if (s < 0) continue;
+        uint32_t fbits = ((uint32_t)begin_ignored << (isf ^ 1u)) | ((uint32_t)end_ignored << isf);
+        if (fbits)
+            atomicOr(&t.vals[s], (fbits << 30) | 0u);
+        atomicAdd(&t.vals[s], 1u);
+    }
+}
+
+// Per-slot work of the extension phase: k-mer dump, then path starts in both orientations.
+__device__ __forceinline__ void extend_slot(const Graph &g, uint32_t s, const MergeOut &o, int keep_kmers,
+                                            uint32_t min_mult) {
+    uint64_t key = g.t.keys[s];
+    if (key == kEmptyKey) return;
+    uint32_t mult = val_mult(g.t.vals[s]);
+    if (mult < min_mult) return;
+    if (keep_kmers) {
+        unsigned long long i = atomicAdd(&o.counters[2], 1ull);
+        if (i < o.kmer_cap) {
+            o.kmer_keys[i] = key;
+            o.kmer_mult[i] = mult;
+        } else {
+            atomicOr(o.status, kStatusKmerOverflow);
+        }
+    }
+    for (int orient = 0; orient < 2; orient++) {
+        uint64_t v = orient ? rc_packed(key, g.k) : key;
+        if (!g.is_start(v, s)) continue;
+        uint64_t e;
+        int64_t se;
+        uint32_t steps = walk_to_end(g, v, s, e, se, o.status);
+        bool owner = ((int64_t)s < se) || ((int64_t)s == se && orient == 0);
+        if (!owner) continue;
+        uint8_t flags = (uint8_t)((g.left_boundary(v, s) ? 1u : 0u) | (g.right_boundary(e, se) ? 2u : 0u));
+        emit_walk(g, v, s, steps, flags, o);
+    }
+}
+
+// Cycle phase: surviving k-mers not covered by any path lie on cycles; the cycle is
+// emitted once, from its smallest slot.
+__device__ __forceinline__ void cycle_slot(const Graph &g, uint32_t s, const MergeOut &o, uint32_t min_mult) {
+    uint64_t key = g.t.keys[s];
+    if (key == kEmptyKey || g.t.vis[s]) return;
+    if (val_mult(g.t.vals[s]) < min_mult) return;
+    uint64_t cur = key;
+    int64_t scur = s;
+    uint32_t steps = 0;
+    int64_t min_slot = s;
+    bool closed = false;
+    for (;;) {
+        uint64_t u;
+        int64_t su;
+        if (!g.next(cur, scur, u, su)) break;
+        if (su == (int64_t)s) {
+            closed = (u == key);
+            steps++;
+            break;
+        }
+        if (su < min_slot) min_slot = su;
+        cur = u;
+        scur = su;
+        if (++steps > g.t.cap) {
+            atomicOr(o.status, kStatusWalkLimit);
+            return;
+        }
+    }
+    if (!closed) {
+        atomicOr(o.status, kStatusWalkLimit);
+        return;
+    }
+    if (min_slot != (int64_t)s) return;
+    // a cycle of `steps` k-mers: k + steps - 1 bases, circular flag
+    emit_walk(g, key, s, steps - 1, (uint8_t)4u, o);
+}
+
+// ---------------------------------------------------------------------------
+// classify: pack consecutive sub-bins of each bucket into merge units
+// ---------------------------------------------------------------------------
+__global__ void classify_units_kernel(const unsigned long long *__restrict__ bin_off,
+                                      const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets,
+                                      uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units,
+                                      MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
+                                      unsigned long long *counters, unsigned *status) {
+    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_buckets) return;
+    const uint32_t nsub = 1u << kFineBits;
+    uint64_t cur_begin = 0, cur_k = 0;
+    uint32_t cur_first = 0;
+    bool open = false;
+    auto close_small = [&](uint32_t end_sub) {
+        if (!open) return;
+        unsigned long long i = atomicAdd(&counters[4], 1ull);
+        if (i >= max_units) atomicOr(status, kStatusTableFull);
+        if (i < max_units) {
+            MergeUnit u;
+            u.rec_begin = cur_begin;
+            u.rec_end = bin_off[(uint64_t)b * nsub + end_sub];
+            u.kmers = cur_k;
+            u.table_off = 0;
+            u.table_cap = 0;
+            u.bucket = b;
+            small_units[i] = u;
+        }
+        open = false;
+        cur_k = 0;
+        (void)cur_first;
+    };
+    for (uint32_t j = 0; j < nsub; j++) {
+        uint64_t bin = (uint64_t)b * nsub + j;
+        uint64_t kk = bin_kmers[bin];
+        if (kk == 0) continue;
+        if (kk > small_limit) {
+            close_small(j);
+            unsigned long long i = atomicAdd(&counters[5], 1ull);
+            uint64_t cap = 64;
+            while (cap < kk + kk / 4 + 64) cap <<= 1;
+            unsigned long long off = atomicAdd(&counters[6], (unsigned long long)cap);
+            if (off + cap > pool_slots || i >= max_units) {
+                atomicOr(status, kStatusTableFull);
+                continue;
+            }
+            {
+                MergeUnit u;
+                u.rec_begin = bin_off[bin];
+                u.rec_end = bin_off[bin + 1];
+                u.kmers = kk;
+                u.table_off = off;
+                u.table_cap = (uint32_t)cap;
+                u.bucket = b;
+                large_units[i] = u;
+            }
+            continue;
+        }
+        if (open && cur_k + kk > unit_target) close_small(j);
+        if (!open) {
+            open = true;
+            cur_begin = bin_off[bin];
+            cur_first = j;
+        }
+        cur_k += kk;
+    }
+    close_small(nsub);
+}
+
+// ---------------------------------------------------------------------------
+// small units: persistent CTAs, shared-memory table, device work queue
+// ---------------------------------------------------------------------------
+struct SmallSmem {
+    uint64_t keys[kSmallSlots];
+    uint32_t vals[kSmallSlots];
+    uint8_t vis[kSmallSlots];
+    uint64_t unit;
+};
+
+__global__ void __launch_bounds__(kMergeThreads, 2)
+    merge_small_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
+                       MergeOut o) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    SmallSmem &S = *reinterpret_cast<SmallSmem *>(smem_raw);
+    const uint64_t n_units = counters_ro[4];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[3], 1ull);
+        __syncthreads();
+        const uint64_t ui = S.unit;
+        if (ui >= n_units) break;
+        const MergeUnit U = units[ui];
+        uint32_t cap = 64;
+        while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
+        if (cap > kSmallSlots) cap = kSmallSlots;
+        for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
+            S.keys[i] = kEmptyKey;
+            S.vals[i] = 0;
+            S.vis[i] = 0;
+        }
+        __syncthreads();
+        Table t{S.keys, S.vals, S.vis, cap};
+        for (uint64_t r = U.rec_begin + threadIdx.x; r < U.rec_end; r += blockDim.x)
+            insert_record(t, a.packed, a.recs[r], a.k, o.status);
+        __syncthreads();
+        Graph g{t, a.k, (uint32_t)a.min_mult};
+        for (uint32_t s = threadIdx.x; s < cap; s += blockDim.x) extend_slot(g, s, o, a.keep_kmers, (uint32_t)a.min_mult);
+        __syncthreads();
+        for (uint32_t s = threadIdx.x; s < cap; s += blockDim.x) cycle_slot(g, s, o, (uint32_t)a.min_mult);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// large units: global-memory tables, grid-wide phases
+// ---------------------------------------------------------------------------
+__global__ void init_tables_kernel(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
+                                   uint64_t n_slots_max) {
+    uint64_t n = n_slots_dev ? *n_slots_dev : n_slots_max;
+    if (n > n_slots_max) n = n_slots_max;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        keys[i] = kEmptyKey;
+        vals[i] = 0;
+        vis[i] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) large_insert_kernel(MergeArgs a, const MergeUnit *__restrict__ units,
+                                                           const unsigned long long *__restrict__ n_units_dev,
+                                                           uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o) {
+    const uint64_t n_units = *n_units_dev;
+    const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t u = 0; u < n_units; u++) {
+        const MergeUnit U = units[u];
+        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
+        for (uint64_t r = U.rec_begin + gt; r < U.rec_end; r += gs) insert_record(t, a.packed, a.recs[r], a.k, o.status);
+    }
+}
+
+__global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const MergeUnit *__restrict__ units,
+                                                           const unsigned long long *__restrict__ n_units_dev,
+                                                           uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o,
+                                                           int phase) {
+    const uint64_t n_units = *n_units_dev;
+    const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t u = 0; u < n_units; u++) {
+        const MergeUnit U = units[u];
+        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
+        Graph g{t, a.k, (uint32_t)a.min_mult};
+        for (uint64_t s = gt; s < U.table_cap; s += gs) {
+            if (phase == 0)
+                extend_slot(g, (uint32_t)s, o, a.keep_kmers, (uint32_t)a.min_mult);
+            else
+                cycle_slot(g, (uint32_t)s, o, (uint32_t)a.min_mult);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
+                          uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units, MergeUnit *large_units,
+                          uint64_t max_units, uint64_t pool_slots, unsigned long long *counters, unsigned *status,
+                          cudaStream_t s) {
+    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(bin_off, bin_kmers, n_buckets, small_limit,
+                                                                  unit_target, small_units, large_units, max_units,
+                                                                  pool_slots, counters, status);
+    return 1;
+}
+
+int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
+                       const MergeOut &o, int sms, cudaStream_t s) {
+    static bool configured = false;
+    const int smem = (int)sizeof(SmallSmem);
+    if (!configured) {
+        cudaFuncSetAttribute(merge_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        configured = true;
+    }
+    merge_small_kernel<<<sms * 2, kMergeThreads, smem, s>>>(a, units, counters, o);
+    return 1;
+}
+
+int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s) {
+    if (slots == 0) return 0;
+    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, nullptr, slots);
+    return 1;
+}
+
+int launch_init_tables_dyn(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
+                           uint64_t max_slots, int sms, cudaStream_t s) {
+    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, n_slots_dev, max_slots);
+    return 1;
+}
+
+int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
+                       uint64_t n_units_host_hint, uint64_t *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
+                       int sms, cudaStream_t s) {
+    (void)n_units_host_hint;
+    large_insert_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o);
+    large_extend_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 0);
+    large_extend_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 1);
+    return 3;
+}
+
+}  // namespace ggcat

@@ -1,0 +1,163 @@
+/*
+ * ggcat_gb300 — C ABI of the GB300 (sm_103a) implementation of GGCAT's build hot path
+ * (minimizer bucketing -> per-bucket k-mer merge) and graph query lookup.
+ *
+ * Plain C types only (pointers, sizes, status codes).  Every call returns 0 on success
+ * or a negative GGCAT_GPU_E* code; ggcat_gpu_last_error() describes the last failure.
+ * Calls on one context are not thread-safe; use one context per host thread.
+ *
+ * Device pointers are marked d_, host pointers h_.  `stream` is a cudaStream_t (NULL =
+ * the legacy default stream).  Functions that return results to the host synchronise
+ * the stream.
+ */
+#ifndef GGCAT_GB300_H
+#define GGCAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GGCAT_GPU_OK 0
+#define GGCAT_GPU_EINVAL -1      /* bad argument */
+#define GGCAT_GPU_ECUDA -2       /* CUDA runtime error */
+#define GGCAT_GPU_ENOMEM -3      /* device allocation failed */
+#define GGCAT_GPU_EDEVICE -4     /* a kernel reported an internal error (see last_error) */
+#define GGCAT_GPU_EUNSUPPORTED -5 /* parameters outside what this build supports */
+#define GGCAT_GPU_EIO -6         /* file read/write error */
+
+/* Merging-hash kinds (crates/api/src/utils.rs:10-69). */
+#define GGCAT_HASH_SEQHASH 1
+#define GGCAT_HASH_RABIN_KARP128 4
+
+/* Merge scheduling (both give identical results). */
+#define GGCAT_MERGE_BATCHED 0    /* persistent kernel over a device work queue */
+#define GGCAT_MERGE_PER_BUCKET 1 /* plain form: one launch group per bucket */
+
+typedef struct ggcat_gpu_ctx ggcat_gpu_ctx;
+
+typedef struct {
+    int32_t k;                /* k-mer length (this build: 3..32 for the device merge) */
+    int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
+    int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
+    int32_t second_bits;      /* second-level bucket bits reported in superkmer records */
+    int32_t min_multiplicity; /* keep k-mers with multiplicity >= this */
+    int32_t hash_kind;        /* GGCAT_HASH_* */
+    int32_t forward_only;     /* 1 = do not canonicalise (rc never applied) */
+    int32_t merge_mode;       /* GGCAT_MERGE_* */
+    int32_t unit_target;      /* target k-mer instances per merge unit (0 = auto) */
+    int32_t keep_kmers;       /* 1 = also output the surviving k-mers and multiplicities */
+} ggcat_gpu_params;
+
+/* One superkmer in the semantic form of PushSequenceInfo
+ * (crates/minimizer_bucketing/src/lib.rs:101-110): bases text[start, start+len);
+ * when rc != 0 the reference stores their reverse complement and flags refer to the
+ * stored orientation (bit0 = begin included, bit1 = end included). */
+typedef struct {
+    uint64_t start;
+    uint32_t len;
+    uint16_t bucket;
+    uint16_t second_bucket;
+    uint16_t minimizer_pos;
+    uint8_t rc;
+    uint8_t flags;
+} ggcat_gpu_superkmer;
+
+typedef struct {
+    uint64_t text_bytes;
+    uint64_t superkmers;
+    uint64_t kmer_instances;
+    uint64_t merge_units_small;
+    uint64_t merge_units_large;
+    uint64_t partial_unitigs;
+    uint64_t partial_bases;
+    uint64_t surviving_kmers;   /* counted once per (k-mer, sub-bucket) */
+    uint64_t final_unitigs;
+    double ms_pack, ms_bucketize, ms_merge, ms_link; /* device times (events) and host link time */
+} ggcat_gpu_stats;
+
+/* ---- context ---- */
+/* Creates a context on `device`.  All device memory of the context is owned by it. */
+int ggcat_gpu_create(int device, ggcat_gpu_ctx **out);
+void ggcat_gpu_destroy(ggcat_gpu_ctx *ctx);
+const char *ggcat_gpu_last_error(const ggcat_gpu_ctx *ctx);
+/* Number of kernels this context launched since creation (all entry points). */
+uint64_t ggcat_gpu_kernel_launches(const ggcat_gpu_ctx *ctx);
+
+/* ---- build hot path, device-resident input ----
+ * Input "text": all sequences concatenated, each followed by at least one byte that is
+ * not ACGTacgt (a separator, e.g. '\n'); any such byte splits k-mers like an N
+ * (SequencesSplitter, crates/minimizer_bucketing/src/sequences_splitter.rs:15-40).
+ * Long FASTA records must already be cut into pieces by the FASTA reader
+ * (ggcat_gpu_fasta_parse does this exactly like the reference). */
+
+/* Replaces assembler_minimizer_bucketing::minimizer_bucketing
+ * (crates/assembler_minimizer_bucketing/src/lib.rs:279-340): 2-bit packing, nt-hash
+ * m-mers, (k-1)-mer window minimizers with the duplicate flag, superkmer splitting,
+ * bucket ids, and a device radix partition of the superkmer records (the bucket store,
+ * kept in HBM).  *n_superkmers receives the record count. */
+int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len, const ggcat_gpu_params *p,
+                        void *stream, uint64_t *n_superkmers);
+
+/* Copies the superkmer records of the last bucketize (ordered by bucket, then by an
+ * internal sub-bucket; order inside a sub-bucket is unspecified) to the host. */
+int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer *h_out, uint64_t cap, uint64_t *n);
+
+/* Replaces assembler_kmers_merge::kmers_merge (crates/assembler_kmers_merge/src/lib.rs:159-284):
+ * per sub-bucket canonical k-mer counting with the MapEntry flag/halving rule, the
+ * min-multiplicity filter and within-sub-bucket unitig extension.  Produces partial
+ * unitigs (with open-end link flags) for the link stage.  Runs on the bucket store of
+ * the last ggcat_gpu_bucketize. */
+int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, void *stream);
+
+/* Partial unitigs of the last merge: concatenated ASCII bases, and per unitig
+ * (offset, length, flags) with flags bit0 = backward link, bit1 = forward link,
+ * bit2 = circular.  Pass NULL buffers to query the sizes. */
+int ggcat_gpu_partial_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,
+                                   uint32_t *h_len, uint8_t *h_flags, uint64_t cap, uint64_t *n_unitigs,
+                                   uint64_t *n_bases);
+
+/* Surviving k-mers of the last merge (needs keep_kmers = 1): canonical 2-bit packed
+ * k-mer (seq-hash layout, base i at bits 2i) and multiplicity.  A k-mer on a sub-bucket
+ * boundary is reported once per sub-bucket.  Pass NULL to query the count. */
+int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint64_t *h_mult, uint64_t cap, uint64_t *n);
+
+/* Host link stage (crates/assembler_pipeline/src/extend_unitigs.rs:348-993 semantics):
+ * joins the partial unitigs of the last merge at their link k-mers into the maximal
+ * unitigs.  Output as for ggcat_gpu_partial_unitigs_copy (flags bit2 = circular). */
+int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k);
+int ggcat_gpu_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,
+                           uint32_t *h_len, uint8_t *h_flags, uint64_t cap, uint64_t *n_unitigs, uint64_t *n_bases);
+
+/* Statistics of the last bucketize/merge/link. */
+int ggcat_gpu_get_stats(const ggcat_gpu_ctx *ctx, ggcat_gpu_stats *out);
+
+/* ---- end to end, host input ----
+ * Copies the host text to the device (pinned staging, cudaMemcpyAsync), runs bucketize
+ * + merge on `stream`, and copies the partial unitigs back to host memory owned by the
+ * context (read them with ggcat_gpu_partial_unitigs_copy, or link them with
+ * ggcat_gpu_link).  This is the call the reference's kmers pipeline would make. */
+int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, uint64_t text_len, const ggcat_gpu_params *p,
+                         void *stream);
+
+/* FASTA parsing with the reference's 4 MiB + (k-1) copyback record chunking
+ * (SequencesReader::process_fasta, crates/io/src/sequences_reader.rs:106-182).
+ * Produces the device text layout (pieces separated by '\n').  Pass h_text = NULL to
+ * query the needed capacity. */
+int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copyback, uint8_t *h_text,
+                          uint64_t text_cap, uint64_t *text_len, uint64_t *n_pieces);
+
+/* Mirrors ggcat_build_from_files (crates/capi/src/lib.rs:58-139, api/src/lib.rs:217-322)
+ * for the uncoloured, no-extra-elaboration case: reads FASTA files, builds the graph on
+ * the GPU and writes the maximal unitigs as FASTA ">{id} LN:i:{len}" to output_file.
+ * threads_count is accepted for interface parity.  Returns 0 or a negative code. */
+int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
+                               const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
+                               size_t minimizer_length, size_t min_multiplicity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,120 @@
+"""GPU parity of the build hot path against the oracle: superkmer records, surviving
+k-mers with multiplicities, and the canonical maximal-unitig set (bit-exact)."""
+import numpy as np
+import pytest
+
+import oracle
+from ggcat_gb300 import _native, synth
+from ggcat_gb300._native import GpuContext, make_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = GpuContext(0)
+    yield c
+    c.close()
+
+
+def _workload(kind, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "genomes":
+        g = synth.random_genome(200_000, rng)
+        g = synth.add_repeats(g, 0.03, 300, 3, 12, rng)
+        gs = [g] + [synth.indels(synth.substitute(g, 0.01, rng), 0.001, 10, rng) for _ in range(2)]
+        return synth.pack_sequences(gs)
+    if kind == "reads":
+        g = synth.random_genome(100_000, rng)
+        g = synth.add_repeats(g, 0.02, 500, 20, 60, rng)
+        reads = synth.sample_reads(g, 15_000, 150, 0.005, 0.0005, rng)
+        return synth.pack_reads(reads)
+    if kind == "lowcomplexity":
+        seqs = [np.frombuffer(s, np.uint8) for s in (
+            b"A" * 300, b"AC" * 200 + b"N" + b"ACGT" * 80, b"GATTACA" * 60, b"acgtnNACGTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTTT" * 5,
+            b"CCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGG")]
+        seqs += [synth.random_genome(int(n), rng) for n in rng.integers(25, 120, size=200)]
+        return synth.pack_sequences(seqs)
+    raise ValueError(kind)
+
+
+def _oracle_params(p, threads=8):
+    return oracle.params(k=p.k, m=p.m, bucket_bits=p.bucket_bits, second_bits=p.second_bits,
+                         min_multiplicity=p.min_multiplicity, threads=threads)
+
+
+def _sorted_sk(a):
+    a = np.asarray(a)
+    cols = ["start", "len", "bucket", "second_bucket", "minimizer_pos", "rc", "flags"]
+    arr = np.stack([a[c].astype(np.uint64) for c in cols], axis=1)
+    order = np.lexsort(arr.T[::-1])
+    return arr[order]
+
+
+CASES = [("genomes", 1, 10, 1), ("reads", 2, 10, 2), ("lowcomplexity", 3, 4, 1), ("reads", 4, 6, 1)]
+
+
+@pytest.mark.parametrize("kind,seed,bbits,minm", CASES)
+def test_bucketize_matches_oracle(ctx, kind, seed, bbits, minm):
+    text, off, ln, _ = _workload(kind, seed)
+    p = make_params(k=31, m=10, bucket_bits=bbits, second_bits=3, min_multiplicity=minm, keep_kmers=True)
+    ctx.build_text(text, p)
+    got = ctx.superkmers()
+    exp = oracle.bucketize(text, off, ln, _oracle_params(p))
+    assert len(got) == len(exp)
+    assert (_sorted_sk(got) == _sorted_sk(exp)).all()
+
+
+def _kmer_dict(keys, mult):
+    d = {}
+    for kk, mm in zip(keys.tolist(), mult.tolist()):
+        if kk in d:
+            assert d[kk] == mm, "k-mer multiplicity differs between sub-buckets"
+        d[kk] = mm
+    return d
+
+
+@pytest.mark.parametrize("mode", [_native.GGCAT_MERGE_BATCHED, _native.GGCAT_MERGE_PER_BUCKET])
+@pytest.mark.parametrize("kind,seed,bbits,minm", CASES)
+def test_merge_matches_oracle(ctx, kind, seed, bbits, minm, mode):
+    text, off, ln, _ = _workload(kind, seed)
+    p = make_params(k=31, m=10, bucket_bits=bbits, second_bits=3, min_multiplicity=minm, keep_kmers=True,
+                    merge_mode=mode)
+    ctx.build_text(text, p)
+    keys, mult = ctx.kmers()
+    r = oracle.build_graph(text, off, ln, _oracle_params(p))
+    lo, hi, emult = r.kmers()
+    assert (hi == 0).all()
+    assert _kmer_dict(keys, mult) == dict(zip(lo.tolist(), emult.tolist()))
+    ctx.link(p.k)
+    bases, uo, ul, uf = ctx.unitigs()
+    lines = _native.unitig_lines(bases, uo, ul)
+    got = oracle.canonicalize_unitigs(lines, (uf >> 2) & 1, p.k)
+    assert got == r.unitigs()
+
+
+def test_small_unit_target_changes_nothing(ctx):
+    """Any packing of sub-bins into merge units gives the same unitigs."""
+    text, off, ln, _ = _workload("reads", 7)
+    outs = []
+    for target in (64, 900, 0):
+        p = make_params(k=31, m=10, bucket_bits=8, second_bits=2, min_multiplicity=2, unit_target=target)
+        ctx.build_text(text, p)
+        ctx.link(31)
+        bases, uo, ul, uf = ctx.unitigs()
+        outs.append(oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31))
+    assert outs[0] == outs[1] == outs[2]
+
+
+def test_device_pointer_bucketize(ctx):
+    """bucketize on a caller-owned device buffer and stream (torch only as plumbing)."""
+    torch = pytest.importorskip("torch")
+    text, off, ln, _ = _workload("genomes", 9)
+    d = torch.from_numpy(text).cuda()
+    s = torch.cuda.current_stream()
+    p = make_params(k=31, m=10, bucket_bits=10, second_bits=3)
+    n = ctx.bucketize(d.data_ptr(), d.numel(), p, s.cuda_stream)
+    got = ctx.superkmers()
+    exp = oracle.bucketize(text, off, ln, _oracle_params(p))
+    assert n == len(exp)
+    assert (_sorted_sk(got) == _sorted_sk(exp)).all()
