@@ -58,30 +58,37 @@ __global__ void __launch_bounds__(256) pack_kernel(const uint8_t *__restrict__ t
 
 // ---------------------------------------------------------------------------
 // Bucketize
+//
+// Window minimum with the duplicate flag.  Each m-mer contributes v = (min(fw,rc) << 1) | u
+// with u = 1 unless the m-mer is rc-symmetric (lib.rs:189-199).  Over a set of m-mers the
+// batched queue (batch_minqueue.rs:37-120) reports the masked minimum mv with u = 1 exactly
+// when mv occurs once and that occurrence has u = 1; this is the associative combine `cmb`
+// below (equal masked minima from two disjoint sets clear u).  Canonical nt-hash values of
+// distinct m-mers never collide for the minimizer lengths in use (checked by the oracle's
+// tests), so the combine reproduces the queue's values exactly.
+//
+// The window of w = k-m m-mers ending at m-mer i is split van Herk / Gil-Werman style into
+// blocks of w m-mers aligned at i % w == 0: window = suffix(previous block, from i-w+1)
+// combined with prefix(current block, up to i).  Every thread's chunk starts at a multiple
+// of w, so all lanes of a warp cross block boundaries on the same step and do identical
+// work.  The per-thread block array (w entries) lives in shared memory, column-major.
 // ---------------------------------------------------------------------------
 struct NtTables {
     uint64_t h[4], rch[4], h_rot_m[4], rch_rot_m1[4];
 };
 
-struct Window {
-    uint64_t mv;      // masked minimum value (unique flag cleared)
-    uint32_t cnt;     // occurrences of mv in the window
-    uint64_t pos;     // absolute m-mer position of the oldest occurrence
-    uint32_t uraw;    // unique-flag bit of the oldest occurrence
-    uint32_t ufw;     // is_forward of the oldest occurrence
+struct CState {
+    uint64_t v;    // masked minimum | unique bit
+    uint64_t pos;  // absolute m-mer position of the minimum (meaningful when unique)
+    uint32_t fw;   // is_forward of that m-mer
 };
 
-__device__ __forceinline__ void win_add(Window &w, uint64_t val, uint32_t isfw, uint64_t pos, bool first) {
-    uint64_t mvr = val & ~1ull;
-    if (first || mvr < w.mv) {
-        w.mv = mvr;
-        w.cnt = 1;
-        w.pos = pos;
-        w.uraw = (uint32_t)(val & 1);
-        w.ufw = isfw;
-    } else if (mvr == w.mv) {
-        w.cnt++;
-    }
+__device__ __forceinline__ CState cmb(CState a, const CState &b) {
+    const uint64_t ma = a.v & ~1ull, mb = b.v & ~1ull;
+    if (ma < mb) return a;
+    if (mb < ma) return b;
+    a.v = ma;  // the minimum occurs in both parts: not unique
+    return a;
 }
 
 // Base of age a (0 = newest) in the 64-base history (r0 newest 32 bases, r1 older 32).
@@ -106,32 +113,21 @@ __device__ __forceinline__ uint64_t nt_value(uint64_t fw, uint64_t rc) {
     return (mn << 1) | (uint64_t)(fw != rc);
 }
 
-// Recompute the window state over the w m-mers ending at the newest m-mer (position i).
-__device__ void win_recompute(Window &w, const NtTables &T, uint64_t r0, uint64_t r1, int k, int m, uint64_t i) {
-    const int wn = k - m;
-    uint64_t fw, rc;
-    // first m-mer of the window starts at age k-2 (the window covers the newest k-1 bases)
-    nt_from_scratch(T, r0, r1, k - 2, m, fw, rc);
-    uint64_t lo = i - (uint64_t)(wn - 1);
-    for (int j = 0; j < wn; j++) {
-        if (j > 0) {
-            uint32_t out = hist_base(r0, r1, k - 2 - (j - 1));
-            uint32_t in = hist_base(r0, r1, k - 2 - (j - 1) - m);
-            fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[in];
-            rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[in];
-        }
-        win_add(w, nt_value(fw, rc), (uint32_t)(fw < rc), lo + (uint64_t)j, j == 0);
-    }
-}
+constexpr uint64_t kInf = ~0ull;
 
 template <bool kWrite>
 __global__ void __launch_bounds__(256)
     bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k, int m,
-                     int bbits, int sbits, int canonical, uint64_t chunk, unsigned long long *__restrict__ bin_count,
-                     unsigned long long *__restrict__ bin_kmers, const unsigned long long *__restrict__ bin_off,
-                     unsigned long long *__restrict__ bin_cursor, SkRec *__restrict__ recs,
-                     unsigned *__restrict__ status) {
+                     int bbits, int sbits, int fbits, int canonical, uint64_t chunk,
+                     unsigned long long *__restrict__ bin_count, unsigned long long *__restrict__ bin_kmers,
+                     const unsigned long long *__restrict__ bin_off, unsigned long long *__restrict__ bin_cursor,
+                     SkRec *__restrict__ recs, unsigned *__restrict__ status) {
     __shared__ NtTables T;
+    extern __shared__ __align__(16) uint8_t bk_smem[];
+    const int wn = k - m;
+    const int nthr = blockDim.x;
+    uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                                  // [wn][nthr]
+    uint8_t *blk_meta = reinterpret_cast<uint8_t *>(blk_v + (size_t)wn * nthr);              // [wn][nthr]
     if (threadIdx.x < 4) {
         uint32_t c = threadIdx.x;
         uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
@@ -144,26 +140,28 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
 
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t x0 = tid * chunk;
+    const uint64_t x0 = tid * chunk;  // chunk is a multiple of wn
     if (x0 >= n) return;
     const uint64_t x1 = min(x0 + chunk, n);
-    const int wn = k - m;
     const uint32_t dup_bucket = 1u << bbits;
-    const uint64_t bmask = (1ull << bbits) - 1, smask = (1ull << sbits) - 1;
+    const uint64_t bmask = (1ull << bbits) - 1, smask = (1ull << sbits) - 1, fmask = (1ull << fbits) - 1;
+    uint64_t *my_v = blk_v + threadIdx.x;
+    uint8_t *my_meta = blk_meta + threadIdx.x;
 
-    uint64_t lb = (uint64_t)(2 * wn + 2);
+    uint64_t lb = (uint64_t)wn * 6;
     for (int attempt = 0; attempt < 40; attempt++) {
-        const uint64_t xb = x0 > lb ? x0 - lb : 0;
+        const uint64_t xb = x0 > lb ? x0 - lb : 0;  // multiple of wn
         bool anchored = (xb == 0);
         uint64_t run = 0;
         uint64_t r0 = 0, r1 = 0, fw = 0, rc = 0;
-        Window W{};
         uint64_t prev_raw = 0, prev_pos = 0;
         uint32_t prev_fw = 0;
         bool prev_valid = false;
         uint64_t c_prev = 0;
-        bool c_known = false, first_sk = false;
-        bool failed = false;
+        bool c_known = false, first_sk = false, failed = false;
+        bool have_prev_block = false;
+        CState P{kInf, 0, 0};
+        int o = 0;  // offset of the current m-mer inside its block
 
         uint64_t cur_word = ~0ull, pw = 0;
         uint32_t vw = 0;
@@ -186,9 +184,10 @@ __global__ void __launch_bounds__(256)
                 pos = rcf ? (uint32_t)(end - (prev_pos + (uint64_t)m)) : (uint32_t)(prev_pos - start);
             }
             uint32_t second = (uint32_t)((prev_raw >> (bbits + 1)) & smask);
-            uint32_t sub = (uint32_t)((prev_raw >> (bbits + 1)) & 0xffu);
+            uint32_t sub = (uint32_t)((prev_raw >> (bbits + 1)) & fmask);
             uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
-            uint64_t bin = ((uint64_t)bucket << kFineBits) | sub;
+            uint64_t bin = ((uint64_t)bucket << fbits) | sub;
+            first_sk = false;
             if (!kWrite) {
                 atomicAdd(&bin_count[bin], 1ull);
                 atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
@@ -196,7 +195,6 @@ __global__ void __launch_bounds__(256)
                 unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
                 if (slot >= bin_off[bin + 1]) {  // count and write passes disagree: internal error
                     atomicOr(status, kStatusLookback);
-                    first_sk = false;
                     return;
                 }
                 SkRec r;
@@ -205,11 +203,10 @@ __global__ void __launch_bounds__(256)
                        ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
                 recs[slot] = r;
             }
-            first_sk = false;
         };
 
         for (uint64_t p = xb; p < p_end; p++) {
-            uint64_t wi = p >> 5;
+            const uint64_t wi = p >> 5;
             if (wi != cur_word) {
                 cur_word = wi;
                 if (p < n) {
@@ -222,53 +219,77 @@ __global__ void __launch_bounds__(256)
             }
             const uint32_t sh = (uint32_t)(p & 31);
             const bool ok = (p < n) && ((vw >> sh) & 1u);
-            if (!ok) {
+            uint64_t e_v = kInf;
+            uint32_t e_fw = 0;
+            if (ok) {
+                const uint32_t c = (uint32_t)((pw >> (2 * sh)) & 3u);
+                r1 = (r1 << 2) | (r0 >> 62);
+                r0 = (r0 << 2) | c;
+                run++;
+                if (run == (uint64_t)m) {
+                    nt_from_scratch(T, r0, r1, m - 1, m, fw, rc);
+                } else if (run > (uint64_t)m) {
+                    uint32_t out = hist_base(r0, r1, m);
+                    fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[c];
+                    rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[c];
+                }
+                if (run >= (uint64_t)m) {
+                    e_v = nt_value(fw, rc);
+                    e_fw = (uint32_t)(fw < rc);
+                }
+            } else {
                 if (run >= (uint64_t)k && prev_valid) {
-                    uint64_t x_last = p - (uint64_t)k + 1;
+                    const uint64_t x_last = p - (uint64_t)k + 1;
                     if (x_last >= x0 && x_last < x1) {
-                        if (!c_known) {
-                            failed = true;
-                            break;
-                        }
-                        emit(x_last, true);
+                        if (!c_known) failed = true;
+                        else emit(x_last, true);
                     }
                 }
                 run = 0;
                 anchored = true;
                 prev_valid = false;
                 c_known = false;
-                continue;
             }
-            const uint32_t c = (uint32_t)((pw >> (2 * sh)) & 3u);
-            r1 = (r1 << 2) | (r0 >> 62);
-            r0 = (r0 << 2) | c;
-            run++;
-            if (run < (uint64_t)m) continue;
-            if (run == (uint64_t)m) {
-                nt_from_scratch(T, r0, r1, m - 1, m, fw, rc);
-            } else {
-                uint32_t out = hist_base(r0, r1, m);
-                fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[c];
-                rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[c];
+            if (failed) break;
+            // block bookkeeping over m-mer positions i = p - m + 1 (aligned: xb % wn == 0)
+            if (p + 1 < xb + (uint64_t)m) continue;  // no m-mer position >= xb yet
+            const uint64_t i = p + 1 - (uint64_t)m;
+            if (o == 0 && i > xb) {
+                // the previous block [i - wn, i) is complete: suffix-combine it in place
+                CState s{my_v[(size_t)(wn - 1) * nthr], 0, 0};
+                {
+                    uint8_t mt = my_meta[(size_t)(wn - 1) * nthr];
+                    s.pos = (uint64_t)(mt & 0x7f);
+                    s.fw = mt >> 7;
+                }
+                for (int j = wn - 2; j >= 0; j--) {
+                    uint8_t mt = my_meta[(size_t)j * nthr];
+                    CState c{my_v[(size_t)j * nthr], (uint64_t)(mt & 0x7f), (uint32_t)(mt >> 7)};
+                    s = cmb(c, s);
+                    my_v[(size_t)j * nthr] = s.v;
+                    my_meta[(size_t)j * nthr] = (uint8_t)((s.pos & 0x7f) | (s.fw << 7));
+                }
+                have_prev_block = true;
             }
-            const uint64_t i = p - (uint64_t)m + 1;  // newest m-mer position
-            const uint64_t val = nt_value(fw, rc);
-            const uint32_t isfw = (uint32_t)(fw < rc);
-            if (run < (uint64_t)(k - 1)) {
-                win_add(W, val, isfw, i, run == (uint64_t)m);
-                continue;
+            const CState e{e_v, i, e_fw};
+            P = (o == 0) ? e : cmb(P, e);
+            CState win = P;
+            bool win_avail = (o == wn - 1);
+            if (!win_avail && have_prev_block) {
+                uint8_t mt = my_meta[(size_t)(o + 1) * nthr];
+                CState sp{my_v[(size_t)(o + 1) * nthr], i - (uint64_t)o - (uint64_t)wn + (uint64_t)(mt & 0x7f),
+                          (uint32_t)(mt >> 7)};
+                win = cmb(sp, P);
+                win_avail = true;
             }
-            if (run == (uint64_t)(k - 1)) {
-                win_add(W, val, isfw, i, run == (uint64_t)m);
-            } else if (W.pos == i - (uint64_t)wn) {
-                win_recompute(W, T, r0, r1, k, m, i);  // the oldest occurrence of the minimum left
-            } else {
-                win_add(W, val, isfw, i, false);
-            }
+            my_v[(size_t)o * nthr] = e_v;
+            my_meta[(size_t)o * nthr] = (uint8_t)(o | (e_fw << 7));
+            o = (o + 1 == wn) ? 0 : o + 1;
+
+            if (!ok || run < (uint64_t)(k - 1) || !win_avail) continue;
             const uint64_t x = p - (uint64_t)k + 2;  // window start
-            const uint64_t cur_raw = W.mv | (W.cnt == 1 ? (uint64_t)W.uraw : 0ull);
-            const uint64_t cur_pos = W.pos;
-            const uint32_t cur_fw = W.ufw;
+            const uint64_t cur_raw = win.v, cur_pos = win.pos;
+            const uint32_t cur_fw = win.fw;
             if (run == (uint64_t)(k - 1)) {
                 if (anchored) {
                     c_prev = x + 1;  // virtual first callback: the first superkmer starts at x
@@ -279,7 +300,7 @@ __global__ void __launch_bounds__(256)
                 }
             } else {
                 // get_minimizer_splits split rule, batch_minqueue.rs:146-152
-                bool split = (cur_raw != prev_raw) || ((cur_raw & 1ull) && cur_pos != prev_pos);
+                const bool split = (cur_raw != prev_raw) || ((cur_raw & 1ull) && cur_pos != prev_pos);
                 if (split) {
                     if (x >= x0 && x < x1) {
                         if (!c_known) {
@@ -404,18 +425,30 @@ int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *v
 }
 
 int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
-                     int sbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
+                     int sbits, int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
                      unsigned long long *bin_kmers, const unsigned long long *bin_off,
                      unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s) {
+    const int wn = k - m;
+    const uint64_t chunk = ((chunk_hint + wn - 1) / wn) * wn;
     uint64_t threads = (n + chunk - 1) / chunk;
     if (threads == 0) return 0;
-    uint64_t blocks = (threads + 255) / 256;
+    const int tpb = wn <= 24 ? 256 : 128;
+    const size_t smem = (size_t)wn * tpb * 9;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        configured = true;
+    }
+    uint64_t blocks = (threads + tpb - 1) / tpb;
     if (write)
-        bucketize_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(packed, valid, n, k, m, bbits, sbits, canonical, chunk,
-                                                                 bin_count, bin_kmers, bin_off, bin_cursor, recs, status);
+        bucketize_kernel<true><<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical,
+                                                                   chunk, bin_count, bin_kmers, bin_off, bin_cursor,
+                                                                   recs, status);
     else
-        bucketize_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(packed, valid, n, k, m, bbits, sbits, canonical, chunk,
-                                                                  bin_count, bin_kmers, bin_off, bin_cursor, recs, status);
+        bucketize_kernel<false><<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical,
+                                                                    chunk, bin_count, bin_kmers, bin_off, bin_cursor,
+                                                                    recs, status);
     return 1;
 }
 

@@ -87,11 +87,12 @@ struct ggcat_gpu_ctx {
     DevBuf<unsigned> status;
     uint64_t n_text = 0, n_recs = 0, n_kmers = 0, n_bins = 0;
     uint32_t n_buckets = 0;
+    int fine_bits = 8;
     ggcat_gpu_params last_params{};
     bool have_buckets = false;
 
     // merge
-    DevBuf<MergeUnit> small_units, large_units, bucket_units;
+    DevBuf<MergeUnit> small_units, medium_units, large_units, bucket_units;
     DevBuf<unsigned long long> counters, ones;
     DevBuf<uint64_t> tkeys;
     DevBuf<uint32_t> tvals;
@@ -187,7 +188,6 @@ static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
         return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits=%d outside [1, 15]", p->bucket_bits);
     if (p->second_bits < 0 || p->second_bits > 8)
         return fail(ctx, GGCAT_GPU_EINVAL, "second_bits=%d outside [0, 8]", p->second_bits);
-    if (p->bucket_bits + 1 + kFineBits > 63) return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits too large");
     return GGCAT_GPU_OK;
 }
 
@@ -212,7 +212,11 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->packed.ensure(n_words));
     CK(ctx->valid.ensure(n_words));
     ctx->n_buckets = (1u << p->bucket_bits) + 1;
-    ctx->n_bins = (uint64_t)ctx->n_buckets << kFineBits;
+    // sub-bins per bucket: about 2K k-mer instances per sub-bin on average
+    int fb = 0;
+    while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * 2048ull < text_len) fb++;
+    ctx->fine_bits = fb < 4 ? 4 : fb;
+    ctx->n_bins = (uint64_t)ctx->n_buckets << ctx->fine_bits;
     const uint64_t nb = ctx->n_bins;
     CK(ctx->bin_count.ensure(nb + 1));
     CK(ctx->bin_kmers.ensure(nb + 1));
@@ -232,7 +236,7 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], s));
     ctx->launches += launch_bucketize(false, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                      p->second_bits, canonical, chunk, ctx->bin_count.p, ctx->bin_kmers.p, nullptr,
+                                      p->second_bits, ctx->fine_bits, canonical, chunk, ctx->bin_count.p, ctx->bin_kmers.p, nullptr,
                                       nullptr, nullptr, ctx->status.p, s);
     CK(cudaGetLastError());
     ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
@@ -246,7 +250,7 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     ctx->n_kmers = totals[1];
     CK(ctx->recs.ensure(ctx->n_recs + 1));
     ctx->launches += launch_bucketize(true, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                      p->second_bits, canonical, chunk, nullptr, nullptr, ctx->bin_off.p,
+                                      p->second_bits, ctx->fine_bits, canonical, chunk, nullptr, nullptr, ctx->bin_off.p,
                                       ctx->bin_cursor.p, ctx->recs.p, ctx->status.p, s);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[2], s));
@@ -305,6 +309,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     }
     const uint64_t max_units = ctx->n_bins + 1;
     CK(ctx->small_units.ensure(max_units));
+    CK(ctx->medium_units.ensure(max_units));
     CK(ctx->large_units.ensure(max_units));
     // worst-case slot pool of the global-memory tables: cap < 2 * (1.25 x + 64) per unit
     uint64_t pool = ctx->n_kmers * 5 / 2 + 128ull * (ctx->n_buckets + ctx->n_kmers / 4096 + 1) + 1024;
@@ -334,7 +339,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         std::vector<MergeUnit> units(ctx->n_buckets);
         uint64_t slot = 0;
         for (uint32_t b = 0; b < ctx->n_buckets; b++) {
-            uint64_t b0 = (uint64_t)b << kFineBits, b1 = (uint64_t)(b + 1) << kFineBits;
+            uint64_t b0 = (uint64_t)b << ctx->fine_bits, b1 = (uint64_t)(b + 1) << ctx->fine_bits;
             MergeUnit u{};
             u.rec_begin = hoff[b0];
             u.rec_end = hoff[b1];
@@ -361,31 +366,34 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->stats.merge_units_small = 0;
         ctx->stats.merge_units_large = ctx->n_buckets;
     } else {
-        ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, small_limit, target,
-                                               ctx->small_units.p, ctx->large_units.p, max_units, ctx->tkeys.n,
+        const uint64_t medium_limit = 1ull << 18;
+        ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits,
+                                               small_limit, target, medium_limit, ctx->small_units.p,
+                                               ctx->medium_units.p, ctx->large_units.p, max_units, ctx->tkeys.n,
                                                ctx->counters.p, ctx->status.p + 1, s);
-        // initialise exactly the slots the large units claimed (counters[6])
-        ctx->launches += launch_init_tables_dyn(ctx->tkeys.p, ctx->tvals.p, ctx->tvis.p, ctx->counters.p + 6,
-                                                ctx->tkeys.n, ctx->sms, s);
         ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
-        ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + 5, 0, ctx->tkeys.p, ctx->tvals.p,
-                                            ctx->tvis.p, o, ctx->sms, s);
+        ctx->launches += launch_merge_medium(a, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
+                                             ctx->tvis.p, o, ctx->sms, s);
+        ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p,
+                                                 ctx->tvals.p, ctx->tvis.p, ctx->sms, s);
+        ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p,
+                                            ctx->tvals.p, ctx->tvis.p, o, ctx->sms, s);
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[4], s));
-    unsigned long long cnt[8];
+    unsigned long long cnt[16];
     CK(cudaMemcpyAsync(cnt, ctx->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, s));
     unsigned stw[2] = {0, 0};
     CK(cudaMemcpyAsync(stw, ctx->status.p, sizeof stw, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     unsigned st = stw[0] | stw[1];
-    ctx->n_partial = cnt[0];
-    ctx->n_partial_bases = cnt[1];
-    ctx->n_kmers_out = cnt[2];
+    ctx->n_partial = cnt[kCntUnitigs];
+    ctx->n_partial_bases = cnt[kCntBases];
+    ctx->n_kmers_out = cnt[kCntKmers];
     if (p->merge_mode != GGCAT_MERGE_PER_BUCKET) {
-        ctx->stats.merge_units_small = cnt[4];
-        ctx->stats.merge_units_large = cnt[5];
-        if (cnt[6] > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "large-unit table pool exceeded");
+        ctx->stats.merge_units_small = cnt[kCntSmall];
+        ctx->stats.merge_units_large = cnt[kCntMedium] + cnt[kCntLarge];
+        if (cnt[kCntSlots] > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
     }
     *st_out = st;
     return GGCAT_GPU_OK;

@@ -44,7 +44,7 @@ __device__ __forceinline__ uint64_t kmer_mask(int k) { return k >= 32 ? ~0ull : 
 // Superkmer record of the device bucket store (16 bytes):
 //   w0 = start (40 bits) | len << 40 (24 bits)
 //   w1 = bucket (16) | second_bucket << 16 (8) | flags << 24 (2) | rc << 26 (1)
-//        | minimizer_pos << 32 (16) | sub-bin << 48 (8)
+//        | minimizer_pos << 32 (16) | sub-bin << 48 (16)
 struct __align__(16) SkRec {
     uint64_t w0, w1;
 };
@@ -56,7 +56,9 @@ __host__ __device__ __forceinline__ uint32_t rec_flags(const SkRec &r) { return 
 __host__ __device__ __forceinline__ uint32_t rec_rc(const SkRec &r) { return (uint32_t)((r.w1 >> 26) & 1); }
 __host__ __device__ __forceinline__ uint32_t rec_minpos(const SkRec &r) { return (uint32_t)((r.w1 >> 32) & 0xffff); }
 
-constexpr int kFineBits = 8;  // sub-bins per bucket = 256; merge units are runs of sub-bins
+// Sub-bins per bucket = 2^fine_bits (chosen per input, <= kMaxFineBits); the bucket store
+// is partitioned by (bucket, sub-bin) and merge units are runs of sub-bins of one bucket.
+constexpr int kMaxFineBits = 12;
 
 // Device status word bits (set with atomicOr, read by the host after a sync)
 enum : unsigned {

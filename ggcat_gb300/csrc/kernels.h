@@ -10,7 +10,7 @@ namespace ggcat {
 // bucketing.cu — each launcher returns the number of kernels it launched
 int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *valid, cudaStream_t s, int sms);
 int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
-                     int sbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
+                     int sbits, int fbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
                      unsigned long long *bin_kmers, const unsigned long long *bin_off,
                      unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s);
 uint64_t scan_temp_elems(uint64_t n);
@@ -34,8 +34,7 @@ struct MergeOut {
     uint32_t *u_len;
     uint8_t *u_flags;             // bit0 bw link, bit1 fw link, bit2 circular
     unsigned long long u_cap;
-    unsigned long long *counters; // [0] unitigs, [1] bases, [2] kmers, [3] queue head, [4] small units,
-                                  // [5] large units, [6] large slots, [7] queue head 2
+    unsigned long long *counters; // see kCnt*
     uint64_t *kmer_keys;          // optional k-mer dump
     uint32_t *kmer_mult;
     unsigned long long kmer_cap;
@@ -50,21 +49,36 @@ struct MergeArgs {
     int keep_kmers;
 };
 
+// merge counters (device array of 16 u64)
+enum : int {
+    kCntUnitigs = 0,      // partial unitigs emitted
+    kCntBases = 1,        // partial unitig bases emitted
+    kCntKmers = 2,        // k-mers dumped
+    kCntSmallHead = 3,    // work-queue head of S units
+    kCntSmall = 4,        // number of S units
+    kCntLarge = 5,        // number of L units
+    kCntSlots = 6,        // global table slots claimed by M and L units
+    kCntMediumHead = 7,   // work-queue head of M units
+    kCntMedium = 8,       // number of M units
+};
+
 constexpr int kSmallSlots = 8192;     // shared-memory table capacity of one merge CTA
 constexpr int kMergeThreads = 256;
 
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
-                          uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units, MergeUnit *large_units,
-                          uint64_t max_units, uint64_t pool_slots, unsigned long long *counters, unsigned *status,
-                          cudaStream_t s);
+                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
+                          MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
+                          uint64_t pool_slots, unsigned long long *counters, unsigned *status, cudaStream_t s);
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s);
+int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, uint64_t *keys,
+                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s);
+// grid-wide insert/extend/cycles over the units [0, *n_units_dev)
 int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
                        uint64_t n_units_host_hint, uint64_t *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
                        int sms, cudaStream_t s);
 int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
-// initialises the first *n_slots_dev slots (read on the device), at most max_slots
-int launch_init_tables_dyn(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
-                           uint64_t max_slots, int sms, cudaStream_t s);
+int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, uint64_t *keys, uint32_t *vals,
+                            uint8_t *vis, int sms, cudaStream_t s);
 
 }  // namespace ggcat

@@ -285,22 +285,31 @@ __device__ __forceinline__ void cycle_slot(const Graph &g, uint32_t s, const Mer
 }
 
 // ---------------------------------------------------------------------------
-// classify: pack consecutive sub-bins of each bucket into merge units
+// classify: pack consecutive sub-bins of each bucket into merge units of three tiers
+//   S: <= small_limit k-mer instances, packed up to unit_target, shared-memory table
+//   M: one sub-bin up to medium_limit instances, one CTA with a global-memory table
+//   L: larger sub-bins, global-memory table processed grid-wide
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t table_cap_for(uint64_t kk) {
+    uint64_t cap = 64;
+    while (cap < kk + kk / 4 + 64) cap <<= 1;
+    return (uint32_t)cap;
+}
+
 __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin_off,
-                                      const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets,
-                                      uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units,
-                                      MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
-                                      unsigned long long *counters, unsigned *status) {
+                                      const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets, int fbits,
+                                      uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
+                                      MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units,
+                                      uint64_t max_units, uint64_t pool_slots, unsigned long long *counters,
+                                      unsigned *status) {
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_buckets) return;
-    const uint32_t nsub = 1u << kFineBits;
+    const uint32_t nsub = 1u << fbits;
     uint64_t cur_begin = 0, cur_k = 0;
-    uint32_t cur_first = 0;
     bool open = false;
     auto close_small = [&](uint32_t end_sub) {
         if (!open) return;
-        unsigned long long i = atomicAdd(&counters[4], 1ull);
+        unsigned long long i = atomicAdd(&counters[kCntSmall], 1ull);
         if (i >= max_units) atomicOr(status, kStatusTableFull);
         if (i < max_units) {
             MergeUnit u;
@@ -314,7 +323,6 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
         }
         open = false;
         cur_k = 0;
-        (void)cur_first;
     };
     for (uint32_t j = 0; j < nsub; j++) {
         uint64_t bin = (uint64_t)b * nsub + j;
@@ -322,31 +330,28 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
         if (kk == 0) continue;
         if (kk > small_limit) {
             close_small(j);
-            unsigned long long i = atomicAdd(&counters[5], 1ull);
-            uint64_t cap = 64;
-            while (cap < kk + kk / 4 + 64) cap <<= 1;
-            unsigned long long off = atomicAdd(&counters[6], (unsigned long long)cap);
+            const bool medium = kk <= medium_limit;
+            unsigned long long i = atomicAdd(&counters[medium ? kCntMedium : kCntLarge], 1ull);
+            uint32_t cap = table_cap_for(kk);
+            unsigned long long off = atomicAdd(&counters[kCntSlots], (unsigned long long)cap);
             if (off + cap > pool_slots || i >= max_units) {
                 atomicOr(status, kStatusTableFull);
                 continue;
             }
-            {
-                MergeUnit u;
-                u.rec_begin = bin_off[bin];
-                u.rec_end = bin_off[bin + 1];
-                u.kmers = kk;
-                u.table_off = off;
-                u.table_cap = (uint32_t)cap;
-                u.bucket = b;
-                large_units[i] = u;
-            }
+            MergeUnit u;
+            u.rec_begin = bin_off[bin];
+            u.rec_end = bin_off[bin + 1];
+            u.kmers = kk;
+            u.table_off = off;
+            u.table_cap = cap;
+            u.bucket = b;
+            (medium ? medium_units : large_units)[i] = u;
             continue;
         }
         if (open && cur_k + kk > unit_target) close_small(j);
         if (!open) {
             open = true;
             cur_begin = bin_off[bin];
-            cur_first = j;
         }
         cur_k += kk;
     }
@@ -368,10 +373,10 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
                        MergeOut o) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SmallSmem &S = *reinterpret_cast<SmallSmem *>(smem_raw);
-    const uint64_t n_units = counters_ro[4];
+    const uint64_t n_units = counters_ro[kCntSmall];
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[3], 1ull);
+        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kCntSmallHead], 1ull);
         __syncthreads();
         const uint64_t ui = S.unit;
         if (ui >= n_units) break;
@@ -397,16 +402,59 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
+// medium units: persistent CTAs, one unit per CTA, global-memory (L2-resident) table
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMergeThreads)
+    merge_medium_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
+                        uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o) {
+    __shared__ uint64_t unit_idx;
+    const uint64_t n_units = counters_ro[kCntMedium];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) unit_idx = atomicAdd(&o.counters[kCntMediumHead], 1ull);
+        __syncthreads();
+        const uint64_t ui = unit_idx;
+        if (ui >= n_units) break;
+        const MergeUnit U = units[ui];
+        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
+        for (uint32_t i = threadIdx.x; i < t.cap; i += blockDim.x) {
+            t.keys[i] = kEmptyKey;
+            t.vals[i] = 0;
+            t.vis[i] = 0;
+        }
+        __syncthreads();
+        for (uint64_t r = U.rec_begin + threadIdx.x; r < U.rec_end; r += blockDim.x)
+            insert_record(t, a.packed, a.recs[r], a.k, o.status);
+        __syncthreads();
+        Graph g{t, a.k, (uint32_t)a.min_mult};
+        for (uint32_t s = threadIdx.x; s < t.cap; s += blockDim.x) extend_slot(g, s, o, a.keep_kmers, (uint32_t)a.min_mult);
+        __syncthreads();
+        for (uint32_t s = threadIdx.x; s < t.cap; s += blockDim.x) cycle_slot(g, s, o, (uint32_t)a.min_mult);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // large units: global-memory tables, grid-wide phases
 // ---------------------------------------------------------------------------
-__global__ void init_tables_kernel(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
-                                   uint64_t n_slots_max) {
-    uint64_t n = n_slots_dev ? *n_slots_dev : n_slots_max;
-    if (n > n_slots_max) n = n_slots_max;
+__global__ void init_tables_kernel(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t n) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         keys[i] = kEmptyKey;
         vals[i] = 0;
         vis[i] = 0;
+    }
+}
+
+__global__ void init_unit_tables_kernel(const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ n_units_dev,
+                                        uint64_t *keys, uint32_t *vals, uint8_t *vis) {
+    const uint64_t n_units = *n_units_dev;
+    const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t u = 0; u < n_units; u++) {
+        const MergeUnit U = units[u];
+        for (uint64_t i = gt; i < U.table_cap; i += gs) {
+            keys[U.table_off + i] = kEmptyKey;
+            vals[U.table_off + i] = 0;
+            vis[U.table_off + i] = 0;
+        }
     }
 }
 
@@ -445,12 +493,18 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
 // launchers
 // ---------------------------------------------------------------------------
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
-                          uint64_t small_limit, uint64_t unit_target, MergeUnit *small_units, MergeUnit *large_units,
-                          uint64_t max_units, uint64_t pool_slots, unsigned long long *counters, unsigned *status,
-                          cudaStream_t s) {
-    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(bin_off, bin_kmers, n_buckets, small_limit,
-                                                                  unit_target, small_units, large_units, max_units,
-                                                                  pool_slots, counters, status);
+                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
+                          MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
+                          uint64_t pool_slots, unsigned long long *counters, unsigned *status, cudaStream_t s) {
+    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(bin_off, bin_kmers, n_buckets, fbits, small_limit,
+                                                                  unit_target, medium_limit, small_units, medium_units,
+                                                                  large_units, max_units, pool_slots, counters, status);
+    return 1;
+}
+
+int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, uint64_t *keys,
+                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+    merge_medium_kernel<<<sms * 4, kMergeThreads, 0, s>>>(a, units, counters, keys, vals, vis, o);
     return 1;
 }
 
@@ -468,13 +522,13 @@ int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigne
 
 int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s) {
     if (slots == 0) return 0;
-    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, nullptr, slots);
+    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, slots);
     return 1;
 }
 
-int launch_init_tables_dyn(uint64_t *keys, uint32_t *vals, uint8_t *vis, const unsigned long long *n_slots_dev,
-                           uint64_t max_slots, int sms, cudaStream_t s) {
-    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, n_slots_dev, max_slots);
+int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, uint64_t *keys, uint32_t *vals,
+                            uint8_t *vis, int sms, cudaStream_t s) {
+    init_unit_tables_kernel<<<sms * 4, 256, 0, s>>>(units, n_units_dev, keys, vals, vis);
     return 1;
 }
 
