@@ -212,9 +212,9 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->packed.ensure(n_words));
     CK(ctx->valid.ensure(n_words));
     ctx->n_buckets = (1u << p->bucket_bits) + 1;
-    // sub-bins per bucket: about 2K k-mer instances per sub-bin on average
+    // sub-bins per bucket: about 1K k-mer instances per sub-bin on average
     int fb = 0;
-    while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * 2048ull < text_len) fb++;
+    while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * 1024ull < text_len) fb++;
     ctx->fine_bits = fb < 4 ? 4 : fb;
     ctx->n_bins = (uint64_t)ctx->n_buckets << ctx->fine_bits;
     const uint64_t nb = ctx->n_bins;
@@ -323,8 +323,8 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
-    const uint64_t small_limit = 6500;
-    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : 4096;
+    const uint64_t small_limit = 3200;  // fits kSmallSlots at load <= 0.8
+    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : 2048;
     if (target > small_limit) target = small_limit;
 
     CK(cudaEventRecord(ctx->ev[3], s));

@@ -62,7 +62,7 @@ enum : int {
     kCntMedium = 8,       // number of M units
 };
 
-constexpr int kSmallSlots = 8192;     // shared-memory table capacity of one merge CTA
+constexpr int kSmallSlots = 4096;     // shared-memory table capacity of one merge CTA
 constexpr int kMergeThreads = 256;
 
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,

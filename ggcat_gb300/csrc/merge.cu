@@ -361,12 +361,101 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
 // ---------------------------------------------------------------------------
 // small units: persistent CTAs, shared-memory table, device work queue
 // ---------------------------------------------------------------------------
-struct SmallSmem {
-    uint64_t keys[kSmallSlots];
-    uint32_t vals[kSmallSlots];
-    uint8_t vis[kSmallSlots];
-    uint64_t unit;
+// Shared-memory layout of one S-unit CTA.  After the successor phase the hash table is
+// dead and its bytes are reused by the list-ranking arrays (`r` view).
+constexpr int kSmallMaxSurv = 2048;  // survivors handled by list ranking (else walk fallback)
+constexpr uint16_t kNone16 = 0xffff;
+
+struct SmallTableView {
+    uint64_t keys[kSmallSlots];  // 32 KB
+    uint32_t vals[kSmallSlots];  // 16 KB: count|flags<<30, then alive<<31|flags<<28|dense index
 };
+struct SmallRankView {
+    uint16_t jump[2 * kSmallMaxSurv];  // 8 KB  pointer jumping: ends point to themselves
+    uint16_t rank[2 * kSmallMaxSurv];  // 8 KB  distance to the path end
+    uint32_t offs[2 * kSmallMaxSurv];  // 16 KB local base offset of owner starts
+    uint16_t uidx[2 * kSmallMaxSurv];  // 8 KB  local unitig index of owner starts
+    uint8_t haspred[2 * kSmallMaxSurv];  // 4 KB
+};
+static_assert(sizeof(SmallRankView) <= sizeof(SmallTableView), "rank view must fit in the table bytes");
+
+struct SmallSmem {
+    union {
+        SmallTableView t;
+        SmallRankView r;
+    } u;
+    uint64_t sk[kSmallMaxSurv];        // 16 KB survivor canonical k-mers (dense order)
+    uint16_t succ[2 * kSmallMaxSurv];  // 8 KB  traversable successor of each oriented node
+    uint8_t bflag[2 * kSmallMaxSurv];  // 4 KB  bit0 left boundary, bit1 right boundary (oriented)
+    uint8_t vis[kSmallSlots];          // 4 KB  visited marks of the walk fallback
+    SkRec rec[kMergeThreads];          // 4 KB  record batch
+    uint32_t pref[kMergeThreads + 1];  // 1 KB  k-mer prefix sums of the batch
+    uint32_t warp_tmp[kMergeThreads / 32 + 1];
+    uint64_t unit;
+    uint32_t n_surv, loc_bases, loc_count, ok;
+    unsigned long long gbase, gidx;
+};
+
+// exclusive block scan of one u32 per thread (blockDim.x == kMergeThreads); all threads call it
+__device__ __forceinline__ uint32_t block_scan_u32(uint32_t v, uint32_t *warp_tmp, uint32_t &total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_tmp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t t = lane < (kMergeThreads / 32) ? warp_tmp[lane] : 0u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
+            if (lane >= d) t += y;
+        }
+        if (lane < (kMergeThreads / 32)) warp_tmp[lane] = t;
+    }
+    __syncthreads();
+    total = warp_tmp[kMergeThreads / 32 - 1];
+    uint32_t r = (wid > 0 ? warp_tmp[wid - 1] : 0u) + x - v;
+    __syncthreads();
+    return r;
+}
+
+// k-mer of `k` bases starting at base position `p` of the packed text (seq-hash layout)
+__device__ __forceinline__ uint64_t load_kmer(const uint64_t *__restrict__ packed, uint64_t p, int k) {
+    const uint64_t w = p >> 5;
+    const uint32_t sh = (uint32_t)(p & 31) * 2u;
+    uint64_t v = packed[w] >> sh;
+    if (sh + 2u * (uint32_t)k > 64u) v |= packed[w + 1] << (64u - sh);
+    return v & kmer_mask(k);
+}
+
+__device__ __forceinline__ bool val_alive(uint32_t v) { return (v >> 31) != 0; }
+
+// number of alive successors of oriented v; *only / *s_only receive the last one found
+__device__ __forceinline__ int alive_succ(const Table &t, uint64_t v, int k, uint64_t &only, int64_t &s_only) {
+    int d = 0;
+    const uint64_t bse = v >> 2;
+#pragma unroll
+    for (uint32_t b = 0; b < 4; b++) {
+        const uint64_t w = bse | ((uint64_t)b << (2 * (k - 1)));
+        const uint64_t rw = rc_packed(w, k);
+        const int64_t sw = tfind(t, w < rw ? w : rw);
+        if (sw >= 0 && val_alive(t.vals[sw])) {
+            d++;
+            only = w;
+            s_only = sw;
+        }
+    }
+    return d;
+}
+
+__device__ __forceinline__ uint64_t oriented(const uint64_t *sk, uint32_t u, int k) {
+    const uint64_t x = sk[u >> 1];
+    return (u & 1) ? rc_packed(x, k) : x;
+}
 
 __global__ void __launch_bounds__(kMergeThreads, 2)
     merge_small_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
@@ -374,6 +463,8 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SmallSmem &S = *reinterpret_cast<SmallSmem *>(smem_raw);
     const uint64_t n_units = counters_ro[kCntSmall];
+    const int k = a.k;
+    const uint32_t min_mult = (uint32_t)a.min_mult;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kCntSmallHead], 1ull);
@@ -385,19 +476,256 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
         while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
         if (cap > kSmallSlots) cap = kSmallSlots;
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
-            S.keys[i] = kEmptyKey;
-            S.vals[i] = 0;
+            S.u.t.keys[i] = kEmptyKey;
+            S.u.t.vals[i] = 0;
             S.vis[i] = 0;
         }
+        if (threadIdx.x == 0) {
+            S.n_surv = 0;
+            S.loc_bases = 0;
+            S.loc_count = 0;
+        }
         __syncthreads();
-        Table t{S.keys, S.vals, S.vis, cap};
-        for (uint64_t r = U.rec_begin + threadIdx.x; r < U.rec_end; r += blockDim.x)
-            insert_record(t, a.packed, a.recs[r], a.k, o.status);
+        Table t{S.u.t.keys, S.u.t.vals, S.vis, cap};
+
+        // ---- insert (add_sequence, hashmap.rs:361-431), k-mer parallel over record batches ----
+        for (uint64_t rb = U.rec_begin; rb < U.rec_end; rb += kMergeThreads) {
+            const uint64_t r = rb + threadIdx.x;
+            uint32_t nk = 0;
+            if (r < U.rec_end) {
+                const SkRec rr = a.recs[r];
+                S.rec[threadIdx.x] = rr;
+                nk = rec_len(rr) - (uint32_t)k + 1;
+            }
+            uint32_t total;
+            const uint32_t ex = block_scan_u32(nk, S.warp_tmp, total);
+            S.pref[threadIdx.x] = ex;
+            __syncthreads();
+            for (uint32_t j = threadIdx.x; j < total; j += blockDim.x) {
+                int lo = 0, hi = kMergeThreads - 1;  // record of k-mer j: last prefix <= j
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (S.pref[mid] <= j) lo = mid; else hi = mid - 1;
+                }
+                const SkRec rr = S.rec[lo];
+                const uint32_t off = j - S.pref[lo];
+                const uint32_t last = rec_len(rr) - (uint32_t)k;
+                const uint32_t fl = rec_flags(rr), rcf = rec_rc(rr);
+                // text-orientation included flags (begin <- stored end when reverse-complemented)
+                const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
+                const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
+                const uint64_t fw = load_kmer(a.packed, rec_start(rr) + off, k);
+                const uint64_t rc = rc_packed(fw, k);
+                const uint32_t isf = fw < rc ? 1u : 0u;
+                const int64_t sl = tinsert(t, isf ? fw : rc, o.status);
+                if (sl < 0) continue;
+                const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
+                const uint32_t fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
+                if (fbits) atomicOr(&t.vals[sl], fbits << 30);
+                atomicAdd(&t.vals[sl], 1u);
+            }
+            __syncthreads();
+        }
+
+        // ---- survivors (min-multiplicity filter) ----
+        uint32_t my_surv = 0;
+        for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x)
+            if (t.keys[sl] != kEmptyKey && val_mult(t.vals[sl]) >= min_mult) my_surv++;
+        uint32_t n_surv;
+        (void)block_scan_u32(my_surv, S.warp_tmp, n_surv);
+        if (n_surv > (uint32_t)kSmallMaxSurv) {
+            // walk fallback for a unit with more survivors than the ranking arrays hold
+            Graph g{t, k, min_mult};
+            for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) extend_slot(g, sl, o, a.keep_kmers, min_mult);
+            __syncthreads();
+            for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
+            continue;
+        }
+        // dense numbering in slot order (block scans); vals become alive|flags|dense index
+        for (uint32_t base = 0; base < cap; base += blockDim.x) {
+            const uint32_t sl = base + threadIdx.x;
+            bool alive = false;
+            uint32_t v = 0;
+            uint64_t key = kEmptyKey;
+            if (sl < cap) {
+                v = t.vals[sl];
+                key = t.keys[sl];
+                alive = key != kEmptyKey && val_mult(v) >= min_mult;
+            }
+            uint32_t tot;
+            const uint32_t ex = block_scan_u32(alive ? 1u : 0u, S.warp_tmp, tot);
+            const uint32_t idx = S.n_surv + ex;
+            if (alive) {
+                S.sk[idx] = key;
+                if (a.keep_kmers) {
+                    const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
+                    if (di < o.kmer_cap) {
+                        o.kmer_keys[di] = key;
+                        o.kmer_mult[di] = val_mult(v);
+                    } else {
+                        atomicOr(o.status, kStatusKmerOverflow);
+                    }
+                }
+            }
+            if (sl < cap) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
+            __syncthreads();
+            if (threadIdx.x == 0) S.n_surv += tot;
+            __syncthreads();
+        }
+        const uint32_t ns = S.n_surv;
+        const uint32_t nn = 2 * ns;  // oriented nodes: u = 2*dense + (0 canonical, 1 reverse complement)
+
+        // ---- traversable successor of every oriented node (the extension rules of
+        //      try_extend_function, hashmap.rs:162-297): 8 probes per node ----
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            const uint64_t x = S.sk[u >> 1];
+            const uint64_t v = (u & 1) ? rc_packed(x, k) : x;
+            const int64_t sv = tfind(t, x);
+            const uint32_t fv = (t.vals[sv] >> 28) & 3u;
+            // MapEntry flags in canonical orientation: 1 = left side ignored, 2 = right side ignored
+            const bool lb = (u & 1) ? fv == 2u : fv == 1u;
+            const bool rb = (u & 1) ? fv == 1u : fv == 2u;
+            uint16_t nx = kNone16;
+            if (!rb) {
+                uint64_t only = 0;
+                int64_t s_only = -1;
+                if (alive_succ(t, v, k, only, s_only) == 1 && s_only != sv) {
+                    const uint64_t ru = rc_packed(only, k);
+                    uint64_t dummy;
+                    int64_t sd;
+                    const int d2 = alive_succ(t, ru, k, dummy, sd);  // predecessors of the successor
+                    const uint32_t vu = t.vals[s_only];
+                    const uint32_t fu = (vu >> 28) & 3u;
+                    const bool u_canon = only < ru;
+                    const bool u_lb = u_canon ? fu == 1u : fu == 2u;
+                    if (d2 == 1 && !u_lb) nx = (uint16_t)(2u * (vu & 0xffffu) + (u_canon ? 0u : 1u));
+                }
+            }
+            S.succ[u] = nx;
+            S.bflag[u] = (uint8_t)((lb ? 1u : 0u) | (rb ? 2u : 0u));
+        }
+        __syncthreads();  // the hash table is dead from here on
+
+        // ---- list ranking by pointer jumping ----
+        SmallRankView &R = S.u.r;
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) R.haspred[u] = 0;
         __syncthreads();
-        Graph g{t, a.k, (uint32_t)a.min_mult};
-        for (uint32_t s = threadIdx.x; s < cap; s += blockDim.x) extend_slot(g, s, o, a.keep_kmers, (uint32_t)a.min_mult);
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            const uint16_t nx = S.succ[u];
+            R.jump[u] = nx == kNone16 ? (uint16_t)u : nx;
+            R.rank[u] = nx == kNone16 ? 0 : 1;
+            if (nx != kNone16) R.haspred[nx] = 1;
+        }
         __syncthreads();
-        for (uint32_t s = threadIdx.x; s < cap; s += blockDim.x) cycle_slot(g, s, o, (uint32_t)a.min_mult);
+        for (uint32_t len = 1; len < nn; len <<= 1) {
+            uint16_t nj[kSmallMaxSurv * 2 / kMergeThreads];
+            uint16_t nr[kSmallMaxSurv * 2 / kMergeThreads];
+            int c = 0;
+            for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
+                const uint16_t j = R.jump[u];
+                const uint32_t rr = (uint32_t)R.rank[u] + R.rank[j];
+                nr[c] = (uint16_t)(rr > 0xfffeu ? 0xfffeu : rr);
+                nj[c] = R.jump[j];
+            }
+            __syncthreads();
+            c = 0;
+            for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
+                R.rank[u] = nr[c];
+                R.jump[u] = nj[c];
+            }
+            __syncthreads();
+        }
+
+        // ---- owner starts: one per path (the end with the smaller node, hashmap.rs walks a
+        //      path once), local offsets via shared atomics ----
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            if (R.haspred[u]) continue;
+            const uint16_t e = R.jump[u];
+            if (S.succ[e] != kNone16) continue;  // on a cycle (handled below)
+            const uint32_t su = u >> 1, se = (uint32_t)e >> 1;
+            const bool owner = su < se || (su == se && (u & 1) == 0);
+            if (!owner) continue;
+            const uint32_t len = (uint32_t)k + R.rank[u];
+            R.offs[u] = atomicAdd(&S.loc_bases, len);
+            R.uidx[u] = (uint16_t)atomicAdd(&S.loc_count, 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            S.gbase = atomicAdd(&o.counters[kCntBases], (unsigned long long)S.loc_bases);
+            S.gidx = atomicAdd(&o.counters[kCntUnitigs], (unsigned long long)S.loc_count);
+            S.ok = (S.gbase + S.loc_bases <= o.bases_cap) && (S.gidx + S.loc_count <= o.u_cap);
+            if (!S.ok) atomicOr(o.status, kStatusOutOverflow);
+        }
+        __syncthreads();
+        const bool ok = S.ok != 0;
+        const unsigned long long gbase = S.gbase, gidx = S.gidx;
+
+        // ---- emission: every node of an owned path writes its base(s) ----
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            const uint32_t mu = u ^ 1u;                 // mirror node
+            const uint16_t me = R.jump[mu];             // end of the mirror path = mirror of u's start
+            if (S.succ[me] != kNone16) continue;        // cycle node
+            const uint32_t s0 = (uint32_t)me ^ 1u;      // start of u's path
+            const uint16_t e = R.jump[u];
+            const uint32_t ss = s0 >> 1, se = (uint32_t)e >> 1;
+            const bool owner = ss < se || (ss == se && (s0 & 1) == 0);
+            if (!owner || !ok) continue;
+            const uint32_t dist = R.rank[mu];           // distance from the start
+            const unsigned long long off = gbase + R.offs[s0];
+            const uint64_t v = oriented(S.sk, u, k);
+            if (dist == 0) {
+                for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
+                const unsigned long long ix = gidx + R.uidx[u];
+                o.u_off[ix] = off;
+                o.u_len[ix] = (uint32_t)k + R.rank[u];
+                o.u_flags[ix] = (uint8_t)((S.bflag[u] & 1u) | (S.bflag[e] & 2u));
+            } else {
+                o.bases[off + (uint32_t)k - 1 + dist] = base_char((uint32_t)(v >> (2 * (k - 1))));
+            }
+        }
+
+        // ---- cycles (rare): every node has a successor and a predecessor; the cycle and its
+        //      mirror are emitted once, from the smallest node of the pair ----
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            if (S.succ[R.jump[u]] == kNone16) continue;
+            uint32_t minc = u, minm = u ^ 1u, n = 1;
+            uint32_t cur = S.succ[u];
+            bool closed = false;
+            while (n <= nn) {
+                if (cur == kNone16) break;
+                if (cur == u) {
+                    closed = true;
+                    break;
+                }
+                minc = min(minc, cur);
+                minm = min(minm, cur ^ 1u);
+                cur = S.succ[cur];
+                n++;
+            }
+            if (!closed) {
+                atomicOr(o.status, kStatusWalkLimit);
+                continue;
+            }
+            if (u != minc || minc > minm) continue;
+            const uint64_t len = (uint64_t)k + n - 1;
+            const unsigned long long off = atomicAdd(&o.counters[kCntBases], len);
+            const unsigned long long ix = atomicAdd(&o.counters[kCntUnitigs], 1ull);
+            if (off + len > o.bases_cap || ix >= o.u_cap) {
+                atomicOr(o.status, kStatusOutOverflow);
+                continue;
+            }
+            uint64_t v = oriented(S.sk, u, k);
+            for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
+            cur = S.succ[u];
+            for (uint32_t i = 1; i < n; i++) {
+                v = oriented(S.sk, cur, k);
+                o.bases[off + (uint32_t)k - 1 + i] = base_char((uint32_t)(v >> (2 * (k - 1))));
+                cur = S.succ[cur];
+            }
+            o.u_off[ix] = off;
+            o.u_len[ix] = (uint32_t)len;
+            o.u_flags[ix] = 4;
+        }
     }
 }
 
