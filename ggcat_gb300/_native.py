@@ -17,7 +17,7 @@ GGCAT_HASH_RABIN_KARP128 = 4
 GGCAT_MERGE_BATCHED = 0
 GGCAT_MERGE_PER_BUCKET = 1
 
-_ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EDEVICE", -5: "EUNSUPPORTED", -6: "EIO"}
+_ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EDEVICE", -5: "EUNSUPPORTED", -6: "EIO", -7: "ETOOLARGE"}
 
 
 class GgcatGpuError(RuntimeError):
@@ -87,6 +87,7 @@ EXPORTED = [
     "ggcat_gpu_build_text",
     "ggcat_gpu_fasta_parse",
     "ggcat_gpu_build_from_files",
+    "ggcat_gpu_bucket_histogram_noalloc",
 ]
 
 _lib = None
@@ -125,6 +126,7 @@ def load(build: bool = True):
     L.ggcat_gpu_build_text.argtypes = [P, P, u64, C.POINTER(Params), P]
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
+    L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
     for name in EXPORTED:
         if name not in ("ggcat_gpu_destroy", "ggcat_gpu_last_error", "ggcat_gpu_kernel_launches"):
             getattr(L, name).restype = C.c_int

@@ -27,6 +27,7 @@ extern "C" {
 #define GGCAT_GPU_EDEVICE -4     /* a kernel reported an internal error (see last_error) */
 #define GGCAT_GPU_EUNSUPPORTED -5 /* parameters outside what this build supports */
 #define GGCAT_GPU_EIO -6         /* file read/write error */
+#define GGCAT_GPU_ETOOLARGE -7   /* size beyond a fixed maximum of the entry point */
 
 /* Merging-hash kinds (crates/api/src/utils.rs:10-69). */
 #define GGCAT_HASH_SEQHASH 1
@@ -156,6 +157,29 @@ int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copy
 int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);
+
+/* ---- bucket-size histogram without device allocation ----
+ * For callers that cannot allocate device memory (their memory belongs to another
+ * allocator, or they run where allocating is not allowed, or they only want to size their
+ * own bucket store first).  No counterpart in the reference.
+ *
+ * Runs the superkmer split of ggcat_gpu_bucketize over d_text (device, layout as above)
+ * and writes, for each of the 2^bucket_bits + 1 first-level buckets, the number of
+ * superkmers (d_superkmers) and of k-mer instances (d_kmers), plus d_offsets, the
+ * exclusive prefix sums of d_superkmers with the total in d_offsets[2^bucket_bits + 1].
+ * All three are caller-owned device arrays.  The values equal those of the records
+ * ggcat_gpu_bucketize produces.
+ *
+ * Allocates nothing: its only scratch is a static 131 KB device array (room for
+ * 2^13 + 1 buckets) that every GPU loading the library keeps until exit.  bucket_bits > 13
+ * or text_len >= 2^40 returns GGCAT_GPU_ETOOLARGE.  The first call on each device looks up
+ * the scratch's device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  Every call clears and reuses the same scratch, so
+ * calls that overlap on the GPU (other streams, other host threads) race: serialise them.
+ * Runs on the current device; stream is a cudaStream_t (NULL = legacy default stream). */
+int ggcat_gpu_bucket_histogram_noalloc(const uint8_t *d_text, uint64_t text_len, int32_t k, int32_t m,
+                                       int32_t bucket_bits, uint64_t *d_superkmers, uint64_t *d_kmers,
+                                       uint64_t *d_offsets, void *stream);
 
 #ifdef __cplusplus
 }
