@@ -11,6 +11,8 @@
 // Small units (<= kSmallSlots table slots) are processed one per CTA by a persistent kernel
 // that keeps the unit's hash table in shared memory; large units use a global-memory table
 // processed grid-wide by three kernels (insert, extend, cycles).
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -361,39 +363,51 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
 // ---------------------------------------------------------------------------
 // small units: persistent CTAs, shared-memory table, device work queue
 // ---------------------------------------------------------------------------
-// Shared-memory layout of one S-unit CTA.  After the successor phase the hash table is
-// dead and its bytes are reused by the list-ranking arrays (`r` view).
-constexpr int kSmallMaxSurv = 2048;  // survivors handled by list ranking (else walk fallback)
+// Shared-memory layouts.  S units keep the hash table in shared memory; after the successor
+// phase the table is dead and its bytes are reused by the list-ranking arrays (union).  M
+// units keep the table in the global pool and use the whole shared memory of one CTA for
+// ranking arrays, so they rank more survivors.
+constexpr int kSmallMaxSurv = 2048;  // S units: survivors handled by list ranking (else walk fallback)
+constexpr int kMedMaxSurv = 6016;    // M units
 constexpr uint16_t kNone16 = 0xffff;
 
+template <int N>
+struct RankView {
+    uint16_t jump[2 * N];     // pointer jumping: ends point to themselves
+    uint16_t rank[2 * N];     // distance to the path end
+    uint32_t offs[2 * N];     // local base offset of owner starts
+    uint16_t uidx[2 * N];     // local unitig index of owner starts
+    uint8_t haspred[2 * N];
+};
 struct SmallTableView {
     uint64_t keys[kSmallSlots];  // 32 KB
     uint32_t vals[kSmallSlots];  // 16 KB: count|flags<<30, then alive<<31|flags<<28|dense index
 };
-struct SmallRankView {
-    uint16_t jump[2 * kSmallMaxSurv];  // 8 KB  pointer jumping: ends point to themselves
-    uint16_t rank[2 * kSmallMaxSurv];  // 8 KB  distance to the path end
-    uint32_t offs[2 * kSmallMaxSurv];  // 16 KB local base offset of owner starts
-    uint16_t uidx[2 * kSmallMaxSurv];  // 8 KB  local unitig index of owner starts
-    uint8_t haspred[2 * kSmallMaxSurv];  // 4 KB
-};
-static_assert(sizeof(SmallRankView) <= sizeof(SmallTableView), "rank view must fit in the table bytes");
+static_assert(sizeof(RankView<kSmallMaxSurv>) <= sizeof(SmallTableView), "rank view must fit in the table bytes");
 
-struct SmallSmem {
-    union {
-        SmallTableView t;
-        SmallRankView r;
-    } u;
-    uint64_t sk[kSmallMaxSurv];        // 16 KB survivor canonical k-mers (dense order)
-    uint16_t succ[2 * kSmallMaxSurv];  // 8 KB  traversable successor of each oriented node
-    uint8_t bflag[2 * kSmallMaxSurv];  // 4 KB  bit0 left boundary, bit1 right boundary (oriented)
-    uint8_t vis[kSmallSlots];          // 4 KB  visited marks of the walk fallback
-    SkRec rec[kMergeThreads];          // 4 KB  record batch
-    uint32_t pref[kMergeThreads + 1];  // 1 KB  k-mer prefix sums of the batch
+template <int N>
+struct UnitSmemCommon {
+    uint64_t sk[N];            // survivor canonical k-mers (dense order)
+    uint16_t succ[2 * N];      // traversable successor of each oriented node
+    uint8_t bflag[2 * N];      // bit0 left boundary, bit1 right boundary (oriented)
+    SkRec rec[kMergeThreads];  // record batch
+    uint32_t pref[kMergeThreads + 1];
     uint32_t warp_tmp[kMergeThreads / 32 + 1];
     uint64_t unit;
     uint32_t n_surv, loc_bases, loc_count, ok;
     unsigned long long gbase, gidx;
+};
+struct SmallSmem : UnitSmemCommon<kSmallMaxSurv> {
+    union {
+        SmallTableView t;
+        RankView<kSmallMaxSurv> r;
+    } u;
+    uint8_t vis[kSmallSlots];
+};
+struct MedSmem : UnitSmemCommon<kMedMaxSurv> {
+    union {
+        RankView<kMedMaxSurv> r;
+    } u;
 };
 
 // exclusive block scan of one u32 per thread (blockDim.x == kMergeThreads); all threads call it
@@ -457,28 +471,42 @@ __device__ __forceinline__ uint64_t oriented(const uint64_t *sk, uint32_t u, int
     return (u & 1) ? rc_packed(x, k) : x;
 }
 
-__global__ void __launch_bounds__(kMergeThreads, 2)
-    merge_small_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
-                       MergeOut o) {
+// One merge unit per CTA, persistent over a device work queue.  kGlobalTable = false: S units,
+// hash table in shared memory; true: M units, hash table in the global pool (L2-resident).
+// Both use the shared-memory list-ranking arrays for the extension.
+template <bool kGlobalTable>
+__global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
+    merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
+                      uint64_t *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeOut o) {
+    using Smem = typename std::conditional<kGlobalTable, MedSmem, SmallSmem>::type;
+    constexpr int kMaxSurv = kGlobalTable ? kMedMaxSurv : kSmallMaxSurv;
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    SmallSmem &S = *reinterpret_cast<SmallSmem *>(smem_raw);
-    const uint64_t n_units = counters_ro[kCntSmall];
+    Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+    const uint64_t n_units = counters_ro[kGlobalTable ? kCntMedium : kCntSmall];
     const int k = a.k;
     const uint32_t min_mult = (uint32_t)a.min_mult;
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kCntSmallHead], 1ull);
+        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kGlobalTable ? kCntMediumHead : kCntSmallHead], 1ull);
         __syncthreads();
         const uint64_t ui = S.unit;
         if (ui >= n_units) break;
         const MergeUnit U = units[ui];
-        uint32_t cap = 64;
-        while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
-        if (cap > kSmallSlots) cap = kSmallSlots;
+        uint32_t cap;
+        Table t;
+        if constexpr (kGlobalTable) {
+            cap = U.table_cap;
+            t = Table{pool_keys + U.table_off, pool_vals + U.table_off, pool_vis + U.table_off, cap};
+        } else {
+            cap = 64;
+            while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
+            if (cap > kSmallSlots) cap = kSmallSlots;
+            t = Table{S.u.t.keys, S.u.t.vals, S.vis, cap};
+        }
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
-            S.u.t.keys[i] = kEmptyKey;
-            S.u.t.vals[i] = 0;
-            S.vis[i] = 0;
+            t.keys[i] = kEmptyKey;
+            t.vals[i] = 0;
+            t.vis[i] = 0;
         }
         if (threadIdx.x == 0) {
             S.n_surv = 0;
@@ -486,7 +514,6 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
             S.loc_count = 0;
         }
         __syncthreads();
-        Table t{S.u.t.keys, S.u.t.vals, S.vis, cap};
 
         // ---- insert (add_sequence, hashmap.rs:361-431), k-mer parallel over record batches ----
         for (uint64_t rb = U.rec_begin; rb < U.rec_end; rb += kMergeThreads) {
@@ -527,13 +554,15 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
             __syncthreads();
         }
 
-        // ---- survivors (min-multiplicity filter) ----
+        // ---- survivors (min-multiplicity filter), counted over contiguous slot ranges ----
+        const uint32_t per = (cap + blockDim.x - 1) / blockDim.x;
+        const uint32_t s_lo = min(cap, threadIdx.x * per), s_hi = min(cap, s_lo + per);
         uint32_t my_surv = 0;
-        for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x)
+        for (uint32_t sl = s_lo; sl < s_hi; sl++)
             if (t.keys[sl] != kEmptyKey && val_mult(t.vals[sl]) >= min_mult) my_surv++;
         uint32_t n_surv;
-        (void)block_scan_u32(my_surv, S.warp_tmp, n_surv);
-        if (n_surv > (uint32_t)kSmallMaxSurv) {
+        const uint32_t my_base = block_scan_u32(my_surv, S.warp_tmp, n_surv);
+        if (n_surv > (uint32_t)kMaxSurv) {
             // walk fallback for a unit with more survivors than the ranking arrays hold
             Graph g{t, k, min_mult};
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) extend_slot(g, sl, o, a.keep_kmers, min_mult);
@@ -541,35 +570,31 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
             continue;
         }
-        // dense numbering in slot order (block scans); vals become alive|flags|dense index
-        for (uint32_t base = 0; base < cap; base += blockDim.x) {
-            const uint32_t sl = base + threadIdx.x;
-            bool alive = false;
-            uint32_t v = 0;
-            uint64_t key = kEmptyKey;
-            if (sl < cap) {
-                v = t.vals[sl];
-                key = t.keys[sl];
-                alive = key != kEmptyKey && val_mult(v) >= min_mult;
-            }
-            uint32_t tot;
-            const uint32_t ex = block_scan_u32(alive ? 1u : 0u, S.warp_tmp, tot);
-            const uint32_t idx = S.n_surv + ex;
-            if (alive) {
-                S.sk[idx] = key;
-                if (a.keep_kmers) {
-                    const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
-                    if (di < o.kmer_cap) {
-                        o.kmer_keys[di] = key;
-                        o.kmer_mult[di] = val_mult(v);
-                    } else {
-                        atomicOr(o.status, kStatusKmerOverflow);
+        // dense numbering in slot order; vals become alive<<31 | flags<<28 | dense index
+        {
+            uint32_t idx = my_base;
+            for (uint32_t sl = s_lo; sl < s_hi; sl++) {
+                const uint64_t key = t.keys[sl];
+                const uint32_t v = t.vals[sl];
+                const bool alive = key != kEmptyKey && val_mult(v) >= min_mult;
+                if (alive) {
+                    S.sk[idx] = key;
+                    if (a.keep_kmers) {
+                        const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
+                        if (di < o.kmer_cap) {
+                            o.kmer_keys[di] = key;
+                            o.kmer_mult[di] = val_mult(v);
+                        } else {
+                            atomicOr(o.status, kStatusKmerOverflow);
+                        }
                     }
+                    t.vals[sl] = 0x80000000u | ((v >> 30) << 28) | idx;
+                    idx++;
+                } else {
+                    t.vals[sl] = 0u;
                 }
             }
-            if (sl < cap) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
-            __syncthreads();
-            if (threadIdx.x == 0) S.n_surv += tot;
+            if (threadIdx.x == 0) S.n_surv = n_surv;
             __syncthreads();
         }
         const uint32_t ns = S.n_surv;
@@ -607,7 +632,7 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
         __syncthreads();  // the hash table is dead from here on
 
         // ---- list ranking by pointer jumping ----
-        SmallRankView &R = S.u.r;
+        auto &R = S.u.r;
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) R.haspred[u] = 0;
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
@@ -618,8 +643,8 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
         }
         __syncthreads();
         for (uint32_t len = 1; len < nn; len <<= 1) {
-            uint16_t nj[kSmallMaxSurv * 2 / kMergeThreads];
-            uint16_t nr[kSmallMaxSurv * 2 / kMergeThreads];
+            uint16_t nj[(kMaxSurv * 2 + kMergeThreads - 1) / kMergeThreads];
+            uint16_t nr[(kMaxSurv * 2 + kMergeThreads - 1) / kMergeThreads];
             int c = 0;
             for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
                 const uint16_t j = R.jump[u];
@@ -730,38 +755,6 @@ __global__ void __launch_bounds__(kMergeThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
-// medium units: persistent CTAs, one unit per CTA, global-memory (L2-resident) table
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMergeThreads)
-    merge_medium_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
-                        uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o) {
-    __shared__ uint64_t unit_idx;
-    const uint64_t n_units = counters_ro[kCntMedium];
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) unit_idx = atomicAdd(&o.counters[kCntMediumHead], 1ull);
-        __syncthreads();
-        const uint64_t ui = unit_idx;
-        if (ui >= n_units) break;
-        const MergeUnit U = units[ui];
-        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
-        for (uint32_t i = threadIdx.x; i < t.cap; i += blockDim.x) {
-            t.keys[i] = kEmptyKey;
-            t.vals[i] = 0;
-            t.vis[i] = 0;
-        }
-        __syncthreads();
-        for (uint64_t r = U.rec_begin + threadIdx.x; r < U.rec_end; r += blockDim.x)
-            insert_record(t, a.packed, a.recs[r], a.k, o.status);
-        __syncthreads();
-        Graph g{t, a.k, (uint32_t)a.min_mult};
-        for (uint32_t s = threadIdx.x; s < t.cap; s += blockDim.x) extend_slot(g, s, o, a.keep_kmers, (uint32_t)a.min_mult);
-        __syncthreads();
-        for (uint32_t s = threadIdx.x; s < t.cap; s += blockDim.x) cycle_slot(g, s, o, (uint32_t)a.min_mult);
-    }
-}
-
-// ---------------------------------------------------------------------------
 // large units: global-memory tables, grid-wide phases
 // ---------------------------------------------------------------------------
 __global__ void init_tables_kernel(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t n) {
@@ -832,7 +825,13 @@ int launch_classify_units(const unsigned long long *bin_off, const unsigned long
 
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, uint64_t *keys,
                         uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
-    merge_medium_kernel<<<sms * 4, kMergeThreads, 0, s>>>(a, units, counters, keys, vals, vis, o);
+    static bool configured = false;
+    const int smem = (int)sizeof(MedSmem);
+    if (!configured) {
+        cudaFuncSetAttribute(merge_unit_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        configured = true;
+    }
+    merge_unit_kernel<true><<<sms, kMergeThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
     return 1;
 }
 
@@ -841,10 +840,10 @@ int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigne
     static bool configured = false;
     const int smem = (int)sizeof(SmallSmem);
     if (!configured) {
-        cudaFuncSetAttribute(merge_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(merge_unit_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         configured = true;
     }
-    merge_small_kernel<<<sms * 2, kMergeThreads, smem, s>>>(a, units, counters, o);
+    merge_unit_kernel<false><<<sms * 2, kMergeThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
     return 1;
 }
 
