@@ -115,13 +115,14 @@ __device__ __forceinline__ uint64_t nt_value(uint64_t fw, uint64_t rc) {
 
 constexpr uint64_t kInf = ~0ull;
 
-template <bool kWrite>
+// Single pass: superkmer records are appended to a staging array (warp-aggregated slot
+// reservation) and counted per sub-bin; partition_kernel then scatters them by sub-bin.
 __global__ void __launch_bounds__(256)
     bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k, int m,
                      int bbits, int sbits, int fbits, int canonical, uint64_t chunk,
                      unsigned long long *__restrict__ bin_count, unsigned long long *__restrict__ bin_kmers,
-                     const unsigned long long *__restrict__ bin_off, unsigned long long *__restrict__ bin_cursor,
-                     SkRec *__restrict__ recs, unsigned *__restrict__ status) {
+                     SkRec *__restrict__ stage, unsigned long long stage_cap,
+                     unsigned long long *__restrict__ stage_cursor, unsigned *__restrict__ status) {
     __shared__ NtTables T;
     extern __shared__ __align__(16) uint8_t bk_smem[];
     const int wn = k - m;
@@ -167,6 +168,32 @@ __global__ void __launch_bounds__(256)
         uint32_t vw = 0;
         const uint64_t p_end = min(x1 + (uint64_t)k - 1, n + 1);
 
+        uint64_t rec_w0 = 0, rec_w1 = 0;
+        bool has_rec = false;
+        // append the pending record of every lane that has one: one atomic per warp
+        auto flush = [&]() {
+            const unsigned am = __activemask();
+            const unsigned bm = __ballot_sync(am, has_rec);
+            if (bm == 0) return;
+            const int lane = (int)(threadIdx.x & 31);
+            const int leader = __ffs(bm) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(stage_cursor, (unsigned long long)__popc(bm));
+            base = __shfl_sync(am, base, leader);
+            if (has_rec) {
+                const unsigned long long idx = base + (unsigned long long)__popc(bm & ((1u << lane) - 1u));
+                if (idx < stage_cap) {
+                    SkRec r;
+                    r.w0 = rec_w0;
+                    r.w1 = rec_w1;
+                    stage[idx] = r;
+                } else {
+                    atomicOr(status, kStatusStageOverflow);
+                }
+                has_rec = false;
+            }
+        };
+
         auto emit = [&](uint64_t c, bool is_final) {
             // superkmer [c_prev - 1, c + k - 1) with the minimizer of the window before c
             // (split) or of the last window (final): lib.rs:207-267
@@ -188,24 +215,16 @@ __global__ void __launch_bounds__(256)
             uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
             uint64_t bin = ((uint64_t)bucket << fbits) | sub;
             first_sk = false;
-            if (!kWrite) {
-                atomicAdd(&bin_count[bin], 1ull);
-                atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
-            } else {
-                unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
-                if (slot >= bin_off[bin + 1]) {  // count and write passes disagree: internal error
-                    atomicOr(status, kStatusLookback);
-                    return;
-                }
-                SkRec r;
-                r.w0 = start | ((uint64_t)len << 40);
-                r.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
-                       ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
-                recs[slot] = r;
-            }
+            atomicAdd(&bin_count[bin], 1ull);
+            atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
+            rec_w0 = start | ((uint64_t)len << 40);
+            rec_w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
+                     ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
+            has_rec = true;
         };
 
         for (uint64_t p = xb; p < p_end; p++) {
+            flush();  // the record emitted in the previous iteration (loop stays in lockstep)
             const uint64_t wi = p >> 5;
             if (wi != cur_word) {
                 cur_word = wi;
@@ -319,11 +338,30 @@ __global__ void __launch_bounds__(256)
             prev_fw = cur_fw;
             prev_valid = true;
         }
+        flush();
         if (!failed) return;
         if (xb == 0) break;  // cannot look back further
         lb *= 4;
     }
     atomicOr(status, kStatusLookback);
+}
+
+// Scatter of the staged records into their sub-bin ranges (the device radix partition).
+__global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict__ stage, uint64_t n_stage, int fbits,
+                                                        const unsigned long long *__restrict__ bin_off,
+                                                        unsigned long long *__restrict__ bin_cursor,
+                                                        SkRec *__restrict__ recs, unsigned *__restrict__ status) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_stage;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const SkRec r = stage[i];
+        const uint64_t bin = ((uint64_t)rec_bucket(r) << fbits) | ((r.w1 >> 48) & 0xffffull);
+        const unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
+        if (slot >= bin_off[bin + 1]) {
+            atomicOr(status, kStatusLookback);
+            continue;
+        }
+        recs[slot] = r;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -424,10 +462,10 @@ int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *v
     return 1;
 }
 
-int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
-                     int sbits, int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, const unsigned long long *bin_off,
-                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s) {
+int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
+                     int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long stage_cap,
+                     unsigned long long *stage_cursor, unsigned *status, cudaStream_t s) {
     const int wn = k - m;
     const uint64_t chunk = ((chunk_hint + wn - 1) / wn) * wn;
     uint64_t threads = (n + chunk - 1) / chunk;
@@ -436,19 +474,22 @@ int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, 
     const size_t smem = (size_t)wn * tpb * 9;
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(bucketize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         configured = true;
     }
     uint64_t blocks = (threads + tpb - 1) / tpb;
-    if (write)
-        bucketize_kernel<true><<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical,
-                                                                   chunk, bin_count, bin_kmers, bin_off, bin_cursor,
-                                                                   recs, status);
-    else
-        bucketize_kernel<false><<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical,
-                                                                    chunk, bin_count, bin_kmers, bin_off, bin_cursor,
-                                                                    recs, status);
+    bucketize_kernel<<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical, chunk,
+                                                         bin_count, bin_kmers, stage, stage_cap, stage_cursor, status);
+    return 1;
+}
+
+int launch_partition(const SkRec *stage, uint64_t n_stage, int fbits, const unsigned long long *bin_off,
+                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, int sms, cudaStream_t s) {
+    if (n_stage == 0) return 0;
+    uint64_t blocks = (n_stage + 255) / 256;
+    const uint64_t cap = (uint64_t)sms * 8;
+    if (blocks > cap) blocks = cap;
+    partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(stage, n_stage, fbits, bin_off, bin_cursor, recs, status);
     return 1;
 }
 

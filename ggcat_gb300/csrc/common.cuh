@@ -67,6 +67,7 @@ enum : unsigned {
     kStatusTableFull = 4u,      // a hash table probe ran past its capacity (internal error)
     kStatusWalkLimit = 8u,      // a unitig walk exceeded its bound (internal error)
     kStatusLookback = 16u,      // bucketing needed more than the maximum lookback (internal error)
+    kStatusStageOverflow = 32u, // staging array of the bucket store too small (host retries)
 };
 
 }  // namespace ggcat

@@ -9,10 +9,12 @@ namespace ggcat {
 
 // bucketing.cu — each launcher returns the number of kernels it launched
 int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *valid, cudaStream_t s, int sms);
-int launch_bucketize(bool write, const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits,
-                     int sbits, int fbits, int canonical, uint64_t chunk, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, const unsigned long long *bin_off,
-                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, cudaStream_t s);
+int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
+                     int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long stage_cap,
+                     unsigned long long *stage_cursor, unsigned *status, cudaStream_t s);
+int launch_partition(const SkRec *stage, uint64_t n_stage, int fbits, const unsigned long long *bin_off,
+                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, int sms, cudaStream_t s);
 uint64_t scan_temp_elems(uint64_t n);
 // out has n+1 entries: exclusive prefix sums and the total at out[n]
 int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
@@ -80,5 +82,13 @@ int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigne
 int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
 int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, uint64_t *keys, uint32_t *vals,
                             uint8_t *vis, int sms, cudaStream_t s);
+
+// query.cu
+int launch_index_insert(const uint8_t *text, uint64_t n, int k, const uint64_t *seq_off, const uint32_t *seq_subset,
+                        uint64_t n_seq, uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, cudaStream_t s);
+int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
+                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, const uint32_t *vals, uint64_t mask,
+                 unsigned long long *matched, int colored, uint4 *runs, unsigned long long runs_cap,
+                 unsigned long long *runs_cursor, unsigned *status, cudaStream_t s);
 
 }  // namespace ggcat
