@@ -87,8 +87,15 @@ EXPORTED = [
     "ggcat_gpu_build_text",
     "ggcat_gpu_fasta_parse",
     "ggcat_gpu_build_from_files",
+    "ggcat_gpu_query_index",
+    "ggcat_gpu_query_submit",
+    "ggcat_gpu_query_poll",
+    "ggcat_gpu_query_wait",
+    "ggcat_gpu_query_subset_runs",
     "ggcat_gpu_bucket_histogram_noalloc",
 ]
+
+QUERY_SLOTS = 4
 
 _lib = None
 
@@ -127,6 +134,11 @@ def load(build: bool = True):
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
+    L.ggcat_gpu_query_index.argtypes = [P, P, u64, C.c_int, P, P, u64, P]
+    L.ggcat_gpu_query_submit.argtypes = [P, C.c_int, P, u64, P, P, u64]
+    L.ggcat_gpu_query_poll.argtypes = [P, C.c_int]
+    L.ggcat_gpu_query_wait.argtypes = [P, C.c_int, P, u64, pu64]
+    L.ggcat_gpu_query_subset_runs.argtypes = [P, C.c_int, P, P, P, u64, pu64]
     for name in EXPORTED:
         if name not in ("ggcat_gpu_destroy", "ggcat_gpu_last_error", "ggcat_gpu_kernel_launches"):
             getattr(L, name).restype = C.c_int
@@ -244,6 +256,48 @@ class GpuContext:
 
     def unitigs(self):
         return self._unitigs(self.L.ggcat_gpu_unitigs_copy, "unitigs_copy")
+
+    # ---- query ----
+    def query_index(self, d_graph_ptr: int, length: int, k: int, seq_off=None, seq_subset=None, stream: int = 0):
+        so = None if seq_off is None else np.ascontiguousarray(seq_off, np.uint64)
+        ss = None if seq_subset is None else np.ascontiguousarray(seq_subset, np.uint32)
+        n = 0 if so is None else len(so)
+        self._check(self.L.ggcat_gpu_query_index(self.h, C.c_void_p(d_graph_ptr), length, k, _ptr(so), _ptr(ss), n,
+                                                 C.c_void_p(stream)), "query_index")
+
+    def query_submit(self, slot: int, text: np.ndarray, off: np.ndarray, ln: np.ndarray):
+        t = np.ascontiguousarray(text, np.uint8)
+        o = np.ascontiguousarray(off, np.uint64)
+        l_ = np.ascontiguousarray(ln, np.uint64)
+        self._check(self.L.ggcat_gpu_query_submit(self.h, slot, _ptr(t), len(t), _ptr(o), _ptr(l_), len(o)),
+                    "query_submit")
+        if not hasattr(self, "_slot_nq"):
+            self._slot_nq = {}
+        self._slot_nq[slot] = len(o)
+
+    def query_poll(self, slot: int) -> bool:
+        rc = self.L.ggcat_gpu_query_poll(self.h, slot)
+        if rc < 0:
+            self._check(rc, "query_poll")
+        return rc == 1
+
+    def query_wait(self, slot: int) -> np.ndarray:
+        """Waits for the slot's batch and returns the matched k-mer count of each query."""
+        nq = self._slot_nq.get(slot, 0)
+        out = np.zeros(nq, np.uint64)
+        got = C.c_uint64()
+        self._check(self.L.ggcat_gpu_query_wait(self.h, slot, _ptr(out), nq, C.byref(got)), "query_wait")
+        return out
+
+    def query_subset_runs(self, slot: int):
+        n = C.c_uint64()
+        self._check(self.L.ggcat_gpu_query_subset_runs(self.h, slot, None, None, None, 0, C.byref(n)), "subset_runs")
+        q = np.zeros(n.value, np.uint32)
+        sub = np.zeros(n.value, np.uint32)
+        cnt = np.zeros(n.value, np.uint32)
+        self._check(self.L.ggcat_gpu_query_subset_runs(self.h, slot, _ptr(q), _ptr(sub), _ptr(cnt), n.value,
+                                                       C.byref(n)), "subset_runs")
+        return q, sub, cnt
 
     def stats(self) -> dict:
         s = Stats()

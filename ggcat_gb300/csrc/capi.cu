@@ -83,7 +83,8 @@ struct ggcat_gpu_ctx {
     DevBuf<uint64_t> packed;
     DevBuf<uint32_t> valid;
     DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, bin_cursor, scan_tmp;
-    DevBuf<SkRec> recs;
+    DevBuf<SkRec> recs, stage;
+    DevBuf<unsigned long long> stage_cursor;
     DevBuf<unsigned> status;
     uint64_t n_text = 0, n_recs = 0, n_kmers = 0, n_bins = 0;
     uint32_t n_buckets = 0;
@@ -113,9 +114,37 @@ struct ggcat_gpu_ctx {
     cudaEvent_t ev[8] = {};
     ggcat_gpu_stats stats{};
 
+    // query: resident graph index and in-flight batch slots
+    DevBuf<uint64_t> qkeys;
+    DevBuf<uint32_t> qvals;
+    DevBuf<uint8_t> qgraph_tmp;
+    DevBuf<uint64_t> qseq_off;
+    DevBuf<uint32_t> qseq_subset;
+    uint64_t qmask = 0;
+    int qk = 0;
+    bool qcolored = false, qready = false;
+    struct QuerySlot {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        DevBuf<uint8_t> d_text;
+        DevBuf<uint32_t> d_iq, d_il;
+        DevBuf<uint64_t> d_is;
+        DevBuf<unsigned long long> d_matched, d_runs_cursor;
+        DevBuf<uint4> d_runs;
+        DevBuf<unsigned> d_status;
+        PinnedBuf h_text, h_items, h_out;
+        uint64_t nq = 0, n_items = 0, runs_cap = 0;
+        bool busy = false;
+    };
+    QuerySlot qslots[GGCAT_GPU_QUERY_SLOTS];
+
     ~ggcat_gpu_ctx() {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
+        for (auto &q : qslots) {
+            if (q.done) cudaEventDestroy(q.done);
+            if (q.stream) cudaStreamDestroy(q.stream);
+        }
     }
 };
 
@@ -224,34 +253,46 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->kmer_off.ensure(nb + 1));
     CK(ctx->bin_cursor.ensure(nb + 1));
     CK(ctx->scan_tmp.ensure(scan_temp_elems(nb) + 2));
-    CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
     const int canonical = p->forward_only ? 0 : 1;
-    const uint64_t chunk = 512;
-
+    const uint64_t chunk = 1008;
+    CK(ctx->stage_cursor.ensure(1));
+    // staging capacity: superkmer density is about 2/(w+1) per base; retried when exceeded
+    uint64_t stage_cap = text_len * 3 / (uint64_t)(p->k - p->m + 1) + 4096;
     CK(cudaEventRecord(ctx->ev[0], s));
     ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], s));
-    ctx->launches += launch_bucketize(false, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                      p->second_bits, ctx->fine_bits, canonical, chunk, ctx->bin_count.p, ctx->bin_kmers.p, nullptr,
-                                      nullptr, nullptr, ctx->status.p, s);
-    CK(cudaGetLastError());
-    ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
-    ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
-    CK(cudaGetLastError());
-    unsigned long long totals[2];
-    CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    unsigned long long totals[3];
+    for (int attempt = 0; attempt < 2; attempt++) {
+        CK(ctx->stage.ensure(stage_cap));
+        CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->stage_cursor.p, 0, sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
+        ctx->launches += launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
+                                          p->second_bits, ctx->fine_bits, canonical, chunk, ctx->bin_count.p,
+                                          ctx->bin_kmers.p, ctx->stage.p, ctx->stage.n, ctx->stage_cursor.p,
+                                          ctx->status.p, s);
+        CK(cudaGetLastError());
+        ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
+        ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&totals[2], ctx->stage_cursor.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (totals[2] <= ctx->stage.n) break;
+        stage_cap = totals[2] + 1024;
+    }
+    if (totals[2] > ctx->stage.n || totals[2] != totals[0])
+        return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: staging mismatch (%llu staged, %llu counted)", totals[2],
+                    totals[0]);
     ctx->n_recs = totals[0];
     ctx->n_kmers = totals[1];
     CK(ctx->recs.ensure(ctx->n_recs + 1));
-    ctx->launches += launch_bucketize(true, ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                      p->second_bits, ctx->fine_bits, canonical, chunk, nullptr, nullptr, ctx->bin_off.p,
-                                      ctx->bin_cursor.p, ctx->recs.p, ctx->status.p, s);
+    ctx->launches += launch_partition(ctx->stage.p, ctx->n_recs, ctx->fine_bits, ctx->bin_off.p, ctx->bin_cursor.p,
+                                      ctx->recs.p, ctx->status.p, ctx->sms, s);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[2], s));
     ctx->n_text = text_len;
@@ -826,5 +867,165 @@ extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const 
         fputc('\n', f);
     }
     fclose(f);
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// graph query lookup
+// ---------------------------------------------------------------------------
+extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k,
+                                     const uint64_t *h_seq_off, const uint32_t *h_seq_subset, uint64_t n_seq,
+                                     void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (k < 3 || k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "query index supports k <= 32 (k=%d)", k);
+    if (len > 0 && !d_graph_text) return fail(ctx, GGCAT_GPU_EINVAL, "null graph text");
+    if (h_seq_subset && (!h_seq_off || n_seq == 0)) return fail(ctx, GGCAT_GPU_EINVAL, "colour subsets need offsets");
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    ctx->qready = false;
+    uint64_t cap = 1024;
+    while (cap < 2 * len + 64) cap <<= 1;  // one slot per k-mer position at load <= 0.5
+    CK(ctx->qkeys.ensure(cap));
+    CK(ctx->qvals.ensure(cap));
+    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->qvals.p, 0, cap * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+    const uint64_t *d_off = nullptr;
+    const uint32_t *d_sub = nullptr;
+    if (h_seq_subset) {
+        CK(ctx->qseq_off.ensure(n_seq));
+        CK(ctx->qseq_subset.ensure(n_seq));
+        CK(cudaMemcpyAsync(ctx->qseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->qseq_subset.p, h_seq_subset, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        d_off = ctx->qseq_off.p;
+        d_sub = ctx->qseq_subset.p;
+    }
+    ctx->launches += launch_index_insert(d_graph_text, len, k, d_off, d_sub, n_seq, ctx->qkeys.p, ctx->qvals.p, cap - 1,
+                                         ctx->status.p + 1, s);
+    CK(cudaGetLastError());
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "query index: table full");
+    ctx->qmask = cap - 1;
+    ctx->qk = k;
+    ctx->qcolored = h_seq_subset != nullptr;
+    ctx->qready = true;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_t *h_text, uint64_t len,
+                                      const uint64_t *h_off, const uint64_t *h_len, uint64_t nq) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->qready) return fail(ctx, GGCAT_GPU_EINVAL, "no query index");
+    if (slot < 0 || slot >= GGCAT_GPU_QUERY_SLOTS) return fail(ctx, GGCAT_GPU_EINVAL, "bad slot %d", slot);
+    if (nq >= (1ull << 32)) return fail(ctx, GGCAT_GPU_EINVAL, "too many queries in one batch");
+    auto &q = ctx->qslots[slot];
+    if (q.busy) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d is busy", slot);
+    CK(cudaSetDevice(ctx->device));
+    if (!q.stream) {
+        CK(cudaStreamCreateWithFlags(&q.stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&q.done, cudaEventDisableTiming));
+    }
+    const int k = ctx->qk;
+    const uint64_t kChunk = 2048;
+    // work items: runs of at most kChunk k-mer positions of one query
+    uint64_t n_items = 0;
+    for (uint64_t i = 0; i < nq; i++) {
+        if (h_off[i] + h_len[i] > len) return fail(ctx, GGCAT_GPU_EINVAL, "query %llu outside the text", (unsigned long long)i);
+        const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
+        n_items += (nk + kChunk - 1) / kChunk;
+    }
+    const size_t item_bytes = n_items * (4 + 8 + 4);
+    CK(q.h_text.ensure(len + 1));
+    CK(q.h_items.ensure(item_bytes + 16));
+    CK(q.h_out.ensure(nq * sizeof(unsigned long long) + 16));
+    memcpy(q.h_text.p, h_text, len);
+    uint32_t *iq = reinterpret_cast<uint32_t *>(q.h_items.p);
+    uint64_t *is = reinterpret_cast<uint64_t *>(q.h_items.p + n_items * 4);
+    uint32_t *il = reinterpret_cast<uint32_t *>(q.h_items.p + n_items * 12);
+    uint64_t it = 0;
+    for (uint64_t i = 0; i < nq; i++) {
+        const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
+        for (uint64_t c = 0; c < nk; c += kChunk, it++) {
+            iq[it] = (uint32_t)i;
+            is[it] = h_off[i] + c;
+            il[it] = (uint32_t)std::min<uint64_t>(kChunk, nk - c);
+        }
+    }
+    CK(q.d_text.ensure(len + 1));
+    CK(q.d_iq.ensure(n_items + 1));
+    CK(q.d_is.ensure(n_items + 1));
+    CK(q.d_il.ensure(n_items + 1));
+    CK(q.d_matched.ensure(nq + 1));
+    CK(q.d_runs_cursor.ensure(1));
+    CK(q.d_status.ensure(1));
+    uint64_t runs_cap = ctx->qcolored ? n_items * 4 + 1024 : 1;
+    CK(q.d_runs.ensure(runs_cap));
+    cudaStream_t s = q.stream;
+    CK(cudaMemcpyAsync(q.d_text.p, q.h_text.p, len, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(q.d_iq.p, iq, n_items * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(q.d_is.p, is, n_items * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(q.d_il.p, il, n_items * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(q.d_matched.p, 0, nq * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(q.d_runs_cursor.p, 0, sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(q.d_status.p, 0, sizeof(unsigned), s));
+    ctx->launches += launch_query(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items, ctx->qkeys.p, ctx->qvals.p,
+                                  ctx->qmask, q.d_matched.p, ctx->qcolored ? 1 : 0, q.d_runs.p, q.d_runs.n,
+                                  q.d_runs_cursor.p, q.d_status.p, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(q.h_out.p, q.d_matched.p, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(q.done, s));
+    q.nq = nq;
+    q.n_items = n_items;
+    q.runs_cap = q.d_runs.n;
+    q.busy = true;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_query_poll(ggcat_gpu_ctx *ctx, int slot) {
+    if (!ctx || slot < 0 || slot >= GGCAT_GPU_QUERY_SLOTS) return GGCAT_GPU_EINVAL;
+    auto &q = ctx->qslots[slot];
+    if (!q.busy) return 1;
+    cudaError_t e = cudaEventQuery(q.done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return fail(ctx, GGCAT_GPU_ECUDA, "query poll: %s", cudaGetErrorString(e));
+}
+
+extern "C" int ggcat_gpu_query_wait(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_matched, uint64_t cap, uint64_t *nq) {
+    if (!ctx || slot < 0 || slot >= GGCAT_GPU_QUERY_SLOTS) return GGCAT_GPU_EINVAL;
+    auto &q = ctx->qslots[slot];
+    if (!q.busy) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d has no batch", slot);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventSynchronize(q.done));
+    q.busy = false;
+    unsigned st = 0;
+    CK(cudaMemcpy(&st, q.d_status.p, sizeof st, cudaMemcpyDeviceToHost));
+    if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "query: run buffer overflow");
+    if (nq) *nq = q.nq;
+    if (h_matched) memcpy(h_matched, q.h_out.p, std::min<uint64_t>(cap, q.nq) * sizeof(uint64_t));
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_query_subset_runs(ggcat_gpu_ctx *ctx, int slot, uint32_t *h_query, uint32_t *h_subset,
+                                           uint32_t *h_count, uint64_t cap, uint64_t *n_runs) {
+    if (!ctx || slot < 0 || slot >= GGCAT_GPU_QUERY_SLOTS) return GGCAT_GPU_EINVAL;
+    auto &q = ctx->qslots[slot];
+    if (q.busy) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d still running; wait first", slot);
+    CK(cudaSetDevice(ctx->device));
+    unsigned long long n = 0;
+    CK(cudaMemcpy(&n, q.d_runs_cursor.p, sizeof n, cudaMemcpyDeviceToHost));
+    if (n > q.runs_cap) return fail(ctx, GGCAT_GPU_EDEVICE, "query: run buffer overflow");
+    if (n_runs) *n_runs = n;
+    if (!h_query) return GGCAT_GPU_OK;
+    uint64_t m = std::min<uint64_t>(cap, n);
+    std::vector<uint4> tmp(m);
+    if (m) CK(cudaMemcpy(tmp.data(), q.d_runs.p, m * sizeof(uint4), cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < m; i++) {
+        h_query[i] = tmp[i].x;
+        h_subset[i] = tmp[i].y;
+        h_count[i] = tmp[i].z;
+    }
     return GGCAT_GPU_OK;
 }

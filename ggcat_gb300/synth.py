@@ -209,3 +209,26 @@ def to_fasta(w: Workload, line_width: int = 0) -> bytes:
         else:
             parts.append(s + b"\n")
     return b"".join(parts)
+
+
+def query_stream(genomes: list, n_queries: int, rng: np.random.Generator, min_len: int = 100,
+                 max_len: int = 100_000, member_frac: float = 0.8, sub_rate: float = 0.01,
+                 rate_per_s: float = 1000.0):
+    """Queries with log-uniform lengths in [min_len, max_len]: a fraction `member_frac` are
+    substrings of random member genomes with `sub_rate` substitutions, the rest fresh i.i.d.
+    sequence.  Returns (list of uint8 arrays, Poisson arrival times in seconds)."""
+    lens = np.exp(rng.uniform(np.log(min_len), np.log(max_len), size=n_queries)).astype(np.int64)
+    out = []
+    for L in lens.tolist():
+        if rng.random() < member_frac:
+            g = genomes[int(rng.integers(0, len(genomes)))]
+            L = min(L, len(g))
+            s = int(rng.integers(0, len(g) - L + 1))
+            q = substitute(g[s:s + L], sub_rate, rng)
+            if rng.random() < 0.5:
+                q = revcomp(q)
+        else:
+            q = random_genome(L, rng)
+        out.append(q)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=n_queries))
+    return out, arrivals

@@ -158,6 +158,35 @@ int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_file
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);
 
+/* ---- graph query lookup (querier::run_query, crates/querier/src/lib.rs:54-199) ----
+ * The graph's canonical k-mers stay resident in a device hash table; batches of queries are
+ * looked up asynchronously in up to GGCAT_GPU_QUERY_SLOTS in-flight slots (each with its own
+ * stream and buffers), which is what a continuous-batching serving loop needs. */
+#define GGCAT_GPU_QUERY_SLOTS 4
+
+/* Builds the resident index from the graph's unitigs in the text layout (device memory).
+ * Colour subset ids, if any, are given per sequence: h_seq_subset[i] for the sequence that
+ * starts at byte h_seq_off[i] (NULL for an uncoloured graph).  Replaces the graph side of the
+ * querier's bucketing and per-bucket maps (querier_minimizer_bucketing.rs:233-288,
+ * parallel_kmers_query.rs:362-403).  k <= 32. */
+int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k,
+                          const uint64_t *h_seq_off, const uint32_t *h_seq_subset, uint64_t n_seq, void *stream);
+
+/* Submits a batch of queries (host text layout; query i = h_text[h_off[i], h_off[i]+h_len[i]))
+ * to slot `slot` and returns without waiting.  The slot's H2D copy, lookup kernel and D2H
+ * copy run on the slot's own stream. */
+int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_t *h_text, uint64_t len, const uint64_t *h_off,
+                           const uint64_t *h_len, uint64_t nq);
+/* 1 = the slot's batch has completed (or the slot is idle), 0 = still running, < 0 error. */
+int ggcat_gpu_query_poll(ggcat_gpu_ctx *ctx, int slot);
+/* Waits for the slot's batch; h_matched[i] = number of k-mer occurrences of query i present
+ * in the graph (parallel_kmers_query.rs:437-471 + counters_sorting.rs:106-273). */
+int ggcat_gpu_query_wait(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_matched, uint64_t cap, uint64_t *nq);
+/* Coloured index: the matches of the last batch of `slot` as runs (query, subset id, count);
+ * summing count per (query, subset) gives the querier's per-subset counters. */
+int ggcat_gpu_query_subset_runs(ggcat_gpu_ctx *ctx, int slot, uint32_t *h_query, uint32_t *h_subset, uint32_t *h_count,
+                                uint64_t cap, uint64_t *n_runs);
+
 /* ---- bucket-size histogram without device allocation ----
  * For callers that cannot allocate device memory (their memory belongs to another
  * allocator, or they run where allocating is not allowed, or they only want to size their
