@@ -44,6 +44,10 @@ def _args():
     ap.add_argument("--cpu-sample-bases", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--verify", action="store_true", help="check batched == per-bucket unitig sets (slow)")
+    ap.add_argument("--no-query", action="store_true", help="skip the query-serving measurement")
+    ap.add_argument("--query-genomes", type=int, default=16, help="member genomes of the queried graph")
+    ap.add_argument("--queries", type=int, default=20000)
+    ap.add_argument("--query-rate", type=float, default=20000.0, help="Poisson arrival rate (queries/s)")
     return ap.parse_args()
 
 
@@ -141,6 +145,53 @@ def cpu_baseline(w, sample_bases: int, threads: int):
     bases = int(w.seq_len[:take].sum())
     del r
     return bases / dt / 1e9, bases, dt, take
+
+
+def query_bench(args, ctx, torch, dev):
+    """Query serving: graph of member genomes built on the GPU (bucketize + merge + link),
+    resident index, Poisson arrivals of mixed-length queries, continuous batching vs one
+    query per launch.  Returns the JSON object of the query measurement."""
+    from ggcat_gb300 import _native, serve, synth
+
+    rng = np.random.default_rng(0x67636174 + 3)
+    anc = synth.random_genome(4_000_000, rng)
+    genomes = [synth.indels(synth.substitute(anc, float(rng.uniform(0.001, 0.02)), rng), 0.0005, 50, rng)
+               for _ in range(args.query_genomes)]
+    text, off, ln, _ = synth.pack_sequences(genomes)
+    p = _native.make_params(k=31, m=10, bucket_bits=12, second_bits=4, min_multiplicity=1)
+    ctx.build_text(text, p)
+    ctx.link(31)
+    bases, uo, ul, uf = ctx.unitigs()
+    graph = np.frombuffer(_native.unitig_lines(bases, uo, ul), np.uint8)
+    d_graph = torch.from_numpy(graph.copy()).to(f"cuda:{dev}")
+    t0 = time.perf_counter()
+    ctx.query_index(d_graph.data_ptr(), d_graph.numel(), 31)
+    index_s = time.perf_counter() - t0
+    qt, qo, ql, arr = synth.query_workload(genomes, args.queries, rate_per_s=args.query_rate)
+    # warm-up
+    serve.serve(ctx, 31, qt, qo[:200], ql[:200], np.zeros(200), slots=4)
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = int(max(1 << 22, min(free // 16, 256 << 20)))
+    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget)
+    n1 = min(len(qo), max(1000, args.queries // 10))
+    r1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, one_per_launch=True)
+    same = bool((rb.matched[:n1] == r1.matched).all())
+    return {
+        "metric": "query kmers/s + p50/p99 ms",
+        "graph": f"{args.query_genomes} genomes x 4 Mbp (ancestor + 0.1-2% substitutions, 0.05% indels), "
+                 f"{len(uo)} unitigs, uncoloured",
+        "queries": int(len(qo)),
+        "query_kmers": int(rb.kmers),
+        "arrival_rate_per_s": args.query_rate,
+        "batched": {"kmers_per_s": round(rb.kmers_per_s, 1), "p50_ms": round(rb.pct_ms(50), 3),
+                    "p99_ms": round(rb.pct_ms(99), 3), "batches": rb.batches, "wall_s": round(rb.wall_s, 3),
+                    "max_batch_kmers": budget},
+        "one_per_launch": {"queries": int(n1), "kmers_per_s": round(r1.kmers_per_s, 1),
+                           "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3),
+                           "wall_s": round(r1.wall_s, 3)},
+        "results_identical_alone_vs_batched": same,
+        "index_build_s": round(index_s, 3),
+    }
 
 
 def run_reference(args):
@@ -285,6 +336,10 @@ def run_gpu(args):
                 "peak_kind": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_step": int(bucket_bytes), "phase_ms": round(bucket_ms, 3)}
 
+    query = None
+    if rank == 0 and not args.no_query:
+        query = query_bench(args, ctx, torch, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -320,6 +375,7 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "query": query,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

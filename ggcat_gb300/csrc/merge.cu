@@ -385,33 +385,37 @@ struct SmallTableView {
 };
 static_assert(sizeof(RankView<kSmallMaxSurv>) <= sizeof(SmallTableView), "rank view must fit in the table bytes");
 
-template <int N>
+template <int N, int NT>
 struct UnitSmemCommon {
-    uint64_t sk[N];            // survivor canonical k-mers (dense order)
-    uint16_t succ[2 * N];      // traversable successor of each oriented node
-    uint8_t bflag[2 * N];      // bit0 left boundary, bit1 right boundary (oriented)
-    SkRec rec[kMergeThreads];  // record batch
-    uint32_t pref[kMergeThreads + 1];
-    uint32_t warp_tmp[kMergeThreads / 32 + 1];
+    uint64_t sk[N];        // survivor canonical k-mers (dense order)
+    uint16_t succ[2 * N];  // traversable successor of each oriented node
+    uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
+    SkRec rec[NT];         // record batch
+    uint32_t pref[NT + 1];
+    uint32_t warp_tmp[NT / 32 + 1];
     uint64_t unit;
     uint32_t n_surv, loc_bases, loc_count, ok;
     unsigned long long gbase, gidx;
 };
-struct SmallSmem : UnitSmemCommon<kSmallMaxSurv> {
+constexpr int kSmallThreads = 256;
+constexpr int kMedThreads = 512;
+struct SmallSmem : UnitSmemCommon<kSmallMaxSurv, kSmallThreads> {
     union {
         SmallTableView t;
         RankView<kSmallMaxSurv> r;
     } u;
     uint8_t vis[kSmallSlots];
 };
-struct MedSmem : UnitSmemCommon<kMedMaxSurv> {
+struct MedSmem : UnitSmemCommon<kMedMaxSurv, kMedThreads> {
     union {
         RankView<kMedMaxSurv> r;
     } u;
 };
 
-// exclusive block scan of one u32 per thread (blockDim.x == kMergeThreads); all threads call it
+// exclusive block scan of one u32 per thread (blockDim.x == NT); all threads call it
+template <int NT>
 __device__ __forceinline__ uint32_t block_scan_u32(uint32_t v, uint32_t *warp_tmp, uint32_t &total) {
+    constexpr int NW = NT / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t x = v;
 #pragma unroll
@@ -422,16 +426,16 @@ __device__ __forceinline__ uint32_t block_scan_u32(uint32_t v, uint32_t *warp_tm
     if (lane == 31) warp_tmp[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        uint32_t t = lane < (kMergeThreads / 32) ? warp_tmp[lane] : 0u;
+        uint32_t t = lane < NW ? warp_tmp[lane] : 0u;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
             if (lane >= d) t += y;
         }
-        if (lane < (kMergeThreads / 32)) warp_tmp[lane] = t;
+        if (lane < NW) warp_tmp[lane] = t;
     }
     __syncthreads();
-    total = warp_tmp[kMergeThreads / 32 - 1];
+    total = warp_tmp[NW - 1];
     uint32_t r = (wid > 0 ? warp_tmp[wid - 1] : 0u) + x - v;
     __syncthreads();
     return r;
@@ -474,8 +478,8 @@ __device__ __forceinline__ uint64_t oriented(const uint64_t *sk, uint32_t u, int
 // One merge unit per CTA, persistent over a device work queue.  kGlobalTable = false: S units,
 // hash table in shared memory; true: M units, hash table in the global pool (L2-resident).
 // Both use the shared-memory list-ranking arrays for the extension.
-template <bool kGlobalTable>
-__global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
+template <bool kGlobalTable, int NT>
+__global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
     merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
                       uint64_t *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeOut o) {
     using Smem = typename std::conditional<kGlobalTable, MedSmem, SmallSmem>::type;
@@ -516,7 +520,7 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
         __syncthreads();
 
         // ---- insert (add_sequence, hashmap.rs:361-431), k-mer parallel over record batches ----
-        for (uint64_t rb = U.rec_begin; rb < U.rec_end; rb += kMergeThreads) {
+        for (uint64_t rb = U.rec_begin; rb < U.rec_end; rb += NT) {
             const uint64_t r = rb + threadIdx.x;
             uint32_t nk = 0;
             if (r < U.rec_end) {
@@ -525,11 +529,11 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
                 nk = rec_len(rr) - (uint32_t)k + 1;
             }
             uint32_t total;
-            const uint32_t ex = block_scan_u32(nk, S.warp_tmp, total);
+            const uint32_t ex = block_scan_u32<NT>(nk, S.warp_tmp, total);
             S.pref[threadIdx.x] = ex;
             __syncthreads();
             for (uint32_t j = threadIdx.x; j < total; j += blockDim.x) {
-                int lo = 0, hi = kMergeThreads - 1;  // record of k-mer j: last prefix <= j
+                int lo = 0, hi = NT - 1;  // record of k-mer j: last prefix <= j
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
                     if (S.pref[mid] <= j) lo = mid; else hi = mid - 1;
@@ -554,14 +558,21 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
             __syncthreads();
         }
 
-        // ---- survivors (min-multiplicity filter), counted over contiguous slot ranges ----
-        const uint32_t per = (cap + blockDim.x - 1) / blockDim.x;
-        const uint32_t s_lo = min(cap, threadIdx.x * per), s_hi = min(cap, s_lo + per);
-        uint32_t my_surv = 0;
-        for (uint32_t sl = s_lo; sl < s_hi; sl++)
-            if (t.keys[sl] != kEmptyKey && val_mult(t.vals[sl]) >= min_mult) my_surv++;
+        // ---- survivors (min-multiplicity filter): each warp scans a contiguous segment of
+        //      slots 32 at a time (coalesced), counting with ballots ----
+        constexpr int NW = NT / 32;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        const uint32_t seg = (((cap + NW - 1) / NW) + 31) & ~31u;
+        const uint32_t seg_lo = min(cap, (uint32_t)wid * seg), seg_hi = min(cap, seg_lo + seg);
+        uint32_t warp_surv = 0;
+        for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
+            const uint32_t sl = b0 + lane;
+            bool alive = false;
+            if (sl < seg_hi) alive = t.keys[sl] != kEmptyKey && val_mult(t.vals[sl]) >= min_mult;
+            warp_surv += __popc(__ballot_sync(0xffffffffu, alive));
+        }
         uint32_t n_surv;
-        const uint32_t my_base = block_scan_u32(my_surv, S.warp_tmp, n_surv);
+        const uint32_t warp_base = block_scan_u32<NT>(lane == 0 ? warp_surv : 0u, S.warp_tmp, n_surv);
         if (n_surv > (uint32_t)kMaxSurv) {
             // walk fallback for a unit with more survivors than the ranking arrays hold
             Graph g{t, k, min_mult};
@@ -572,11 +583,19 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
         }
         // dense numbering in slot order; vals become alive<<31 | flags<<28 | dense index
         {
-            uint32_t idx = my_base;
-            for (uint32_t sl = s_lo; sl < s_hi; sl++) {
-                const uint64_t key = t.keys[sl];
-                const uint32_t v = t.vals[sl];
-                const bool alive = key != kEmptyKey && val_mult(v) >= min_mult;
+            uint32_t base = __shfl_sync(0xffffffffu, warp_base, 0);
+            for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
+                const uint32_t sl = b0 + lane;
+                bool alive = false;
+                uint64_t key = kEmptyKey;
+                uint32_t v = 0;
+                if (sl < seg_hi) {
+                    key = t.keys[sl];
+                    v = t.vals[sl];
+                    alive = key != kEmptyKey && val_mult(v) >= min_mult;
+                }
+                const unsigned bm = __ballot_sync(0xffffffffu, alive);
+                const uint32_t idx = base + __popc(bm & ((1u << lane) - 1u));
                 if (alive) {
                     S.sk[idx] = key;
                     if (a.keep_kmers) {
@@ -588,11 +607,9 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
                             atomicOr(o.status, kStatusKmerOverflow);
                         }
                     }
-                    t.vals[sl] = 0x80000000u | ((v >> 30) << 28) | idx;
-                    idx++;
-                } else {
-                    t.vals[sl] = 0u;
                 }
+                if (sl < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
+                base += __popc(bm);
             }
             if (threadIdx.x == 0) S.n_surv = n_surv;
             __syncthreads();
@@ -643,8 +660,8 @@ __global__ void __launch_bounds__(kMergeThreads, kGlobalTable ? 1 : 2)
         }
         __syncthreads();
         for (uint32_t len = 1; len < nn; len <<= 1) {
-            uint16_t nj[(kMaxSurv * 2 + kMergeThreads - 1) / kMergeThreads];
-            uint16_t nr[(kMaxSurv * 2 + kMergeThreads - 1) / kMergeThreads];
+            uint16_t nj[(kMaxSurv * 2 + NT - 1) / NT];
+            uint16_t nr[(kMaxSurv * 2 + NT - 1) / NT];
             int c = 0;
             for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
                 const uint16_t j = R.jump[u];
@@ -828,10 +845,10 @@ int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsign
     static bool configured = false;
     const int smem = (int)sizeof(MedSmem);
     if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(merge_unit_kernel<true, kMedThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         configured = true;
     }
-    merge_unit_kernel<true><<<sms, kMergeThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
+    merge_unit_kernel<true, kMedThreads><<<sms, kMedThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
     return 1;
 }
 
@@ -840,10 +857,11 @@ int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigne
     static bool configured = false;
     const int smem = (int)sizeof(SmallSmem);
     if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(merge_unit_kernel<false, kSmallThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
         configured = true;
     }
-    merge_unit_kernel<false><<<sms * 2, kMergeThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
+    merge_unit_kernel<false, kSmallThreads><<<sms * 2, kSmallThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
     return 1;
 }
 

@@ -2,10 +2,10 @@
 
 Requests (query sequences of mixed lengths) arrive over time.  The server keeps up to
 ``slots`` batches in flight on the GPU (each slot has its own stream and buffers, see
-``ggcat_gpu_query_submit``); whenever a slot is free it admits every queued request that
-fits the batch budget (k-mer positions, bounded by free device memory) and submits them as
-one lookup launch, so requests that arrive while others run are folded into the next batch
-and their work overlaps on the device.  Latency of a request = completion time − arrival.
+``ggcat_gpu_query_submit``); whenever a slot is free it admits the queued requests that fit
+the batch budget (k-mer positions, bounded by free device memory) and submits them as one
+lookup launch, so requests that arrive while others run are folded into the next batch and
+their work overlaps on the device.  Latency of a request = completion time - arrival time.
 
 ``one_per_launch=True`` gives the baseline: every request is its own batch.
 """
@@ -19,7 +19,7 @@ import numpy as np
 
 @dataclass
 class ServeResult:
-    matched: list  # per request: matched k-mer occurrences
+    matched: np.ndarray  # per request: matched k-mer occurrences
     latency_s: np.ndarray  # per request
     wall_s: float
     kmers: int
@@ -39,66 +39,56 @@ def _pack(queries: list) -> tuple:
     off = np.zeros(len(queries), np.uint64)
     if len(queries) > 1:
         off[1:] = np.cumsum(lens[:-1] + 1)
-    text = np.empty(int(lens.sum()) + len(queries), np.uint8)
+    text = np.full(int(lens.sum()) + len(queries), 10, np.uint8)
     for o, q in zip(off.tolist(), queries):
         text[o:o + len(q)] = np.frombuffer(q, np.uint8) if isinstance(q, (bytes, bytearray)) else q
-        text[o + len(q)] = 10
     return text, off, lens
 
 
-def serve(ctx, k: int, queries: list, arrivals: np.ndarray, slots: int = 4, max_batch_kmers: int | None = None,
-          one_per_launch: bool = False, free_bytes: int | None = None) -> ServeResult:
-    """Replays `queries` arriving at `arrivals` (seconds from start) through the server."""
-    n = len(queries)
-    order = np.argsort(arrivals, kind="stable")
-    if max_batch_kmers is None:
-        # budget by free device memory: ~1 byte of text + 16 bytes of work items per 2K k-mers
-        fb = free_bytes if free_bytes is not None else (8 << 30)
-        max_batch_kmers = int(max(1 << 20, min(fb // 8, 512 << 20)))
-    nk = np.array([max(len(q) - k + 1, 0) for q in queries], np.int64)
-    matched = [None] * n
+def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arrivals: np.ndarray, slots: int = 4,
+          max_batch_kmers: int = 64 << 20, one_per_launch: bool = False) -> ServeResult:
+    """Replays the queries (text layout: query i = text[off[i] : off[i] + lens[i]], arrivals
+    non-decreasing, in seconds from the start) through the server."""
+    n = len(off)
+    off = np.asarray(off, np.uint64)
+    lens = np.asarray(lens, np.uint64)
+    nk = np.maximum(lens.astype(np.int64) - (k - 1), 0)
+    cum = np.concatenate([[0], np.cumsum(nk)])
+    matched = np.zeros(n, np.uint64)
     done_t = np.zeros(n)
-    queue: list[int] = []
     inflight: dict[int, tuple] = {}
-    nxt = 0
+    head = 0  # next request not yet submitted (arrival order = index order)
     batches = 0
     sizes = []
     t0 = time.perf_counter()
-    while nxt < n or queue or inflight:
-        now = time.perf_counter() - t0
-        while nxt < n and arrivals[order[nxt]] <= now:
-            queue.append(int(order[nxt]))
-            nxt += 1
-        # completions
+    while head < n or inflight:
         for s in list(inflight):
             if ctx.query_poll(s):
-                ids, _ = inflight.pop(s)
+                a, b = inflight.pop(s)
                 res = ctx.query_wait(s)
-                tdone = time.perf_counter() - t0
-                for i, r in zip(ids, res.tolist()):
-                    matched[i] = r
-                    done_t[i] = tdone
-        # admissions
-        free_slots = [s for s in range(slots) if s not in inflight]
-        while queue and free_slots:
-            s = free_slots.pop(0)
-            take, budget = [], 0
-            while queue and (not take or (not one_per_launch and budget + nk[queue[0]] <= max_batch_kmers)):
-                i = queue.pop(0)
-                take.append(i)
-                budget += int(nk[i])
-                if one_per_launch:
-                    break
-            text, off, ln = _pack([queries[i] for i in take])
-            ctx.query_submit(s, text, off, ln)
-            inflight[s] = (take, time.perf_counter() - t0)
+                matched[a:b] = res
+                done_t[a:b] = time.perf_counter() - t0
+        now = time.perf_counter() - t0
+        arrived = int(np.searchsorted(arrivals, now, side="right"))
+        free = [s for s in range(slots) if s not in inflight]
+        while free and head < arrived:
+            s = free.pop(0)
+            if one_per_launch:
+                b = head + 1
+            else:
+                # admit every arrived request that fits the k-mer budget (at least one)
+                lim = cum[head] + max_batch_kmers
+                b = max(head + 1, min(arrived, int(np.searchsorted(cum, lim, side="right")) - 1))
+            lo = int(off[head])
+            hi = int(off[b - 1] + lens[b - 1])
+            ctx.query_submit(s, text[lo:hi], off[head:b] - np.uint64(lo), lens[head:b])
+            inflight[s] = (head, b)
             batches += 1
-            sizes.append(len(take))
-        if not inflight and not queue and nxt < n:
-            # idle until the next arrival
-            wait = arrivals[order[nxt]] - (time.perf_counter() - t0)
+            sizes.append(b - head)
+            head = b
+        if not inflight and head < n:
+            wait = arrivals[head] - (time.perf_counter() - t0)
             if wait > 0:
-                time.sleep(min(wait, 0.001))
+                time.sleep(min(wait, 0.0005))
     wall = time.perf_counter() - t0
-    lat = done_t - arrivals
-    return ServeResult(matched, lat, wall, int(nk.sum()), batches, sizes)
+    return ServeResult(matched, done_t - arrivals, wall, int(nk.sum()), batches, sizes)

@@ -232,3 +232,42 @@ def query_stream(genomes: list, n_queries: int, rng: np.random.Generator, min_le
         out.append(q)
     arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=n_queries))
     return out, arrivals
+
+
+def query_workload(genomes: list, n_queries: int, seed: int = 0x67636174 + 5, min_len: int = 100,
+                   max_len: int = 100_000, member_frac: float = 0.8, sub_rate: float = 0.01,
+                   rate_per_s: float = 50_000.0):
+    """Vectorised query set of the serving workload: lengths log-uniform in
+    [min_len, max_len], `member_frac` substrings of random member genomes (either strand)
+    with `sub_rate` substitutions, the rest fresh i.i.d. sequence; Poisson arrivals.
+    Returns (text, offsets, lengths, arrivals) in the text layout."""
+    rng = np.random.default_rng(seed)
+    lens = np.exp(rng.uniform(np.log(min_len), np.log(max_len), size=n_queries)).astype(np.int64)
+    member = rng.random(n_queries) < member_frac
+    off = np.zeros(n_queries, np.uint64)
+    off[1:] = np.cumsum(lens[:-1] + 1).astype(np.uint64)
+    text = np.full(int(lens.sum()) + n_queries, 10, np.uint8)
+    which = rng.integers(0, len(genomes), size=n_queries)
+    strand = rng.random(n_queries) < 0.5
+    for i in range(n_queries):
+        L = int(lens[i])
+        o = int(off[i])
+        if member[i]:
+            g = genomes[int(which[i])]
+            L = min(L, len(g))
+            s = int(rng.integers(0, len(g) - L + 1))
+            q = g[s:s + L]
+            if strand[i]:
+                q = revcomp(q)
+            text[o:o + L] = q
+        else:
+            text[o:o + L] = BASES[rng.integers(0, 4, size=L)]
+        lens[i] = L
+        text[o + L] = 10
+    # substitutions on member queries (vectorised over the whole text)
+    m = rng.random(text.size) < sub_rate
+    m &= text != 10
+    code = np.searchsorted(BASES, text[m])
+    text[m] = BASES[(code + rng.integers(1, 4, size=code.shape)) % 4]
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=n_queries))
+    return text, off, lens.astype(np.uint64), arrivals

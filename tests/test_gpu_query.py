@@ -57,9 +57,10 @@ def test_query_alone_equals_mixed(setup):
 
 def test_query_server_continuous_batching(setup):
     ctx, queries, arrivals, exp, _ = setup
-    res = serve.serve(ctx, 31, queries, arrivals, slots=4, max_batch_kmers=200_000)
+    text, off, ln = serve._pack(queries)
+    res = serve.serve(ctx, 31, text, off, ln, arrivals, slots=4, max_batch_kmers=200_000)
     assert [int(x) for x in res.matched] == [int(x) for x in exp]
     assert res.batches < len(queries)  # requests were batched together
-    base = serve.serve(ctx, 31, queries, arrivals, slots=4, one_per_launch=True)
+    base = serve.serve(ctx, 31, text, off, ln, arrivals, slots=4, one_per_launch=True)
     assert [int(x) for x in base.matched] == [int(x) for x in exp]
     assert base.batches == len(queries)
