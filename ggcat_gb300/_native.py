@@ -87,11 +87,16 @@ EXPORTED = [
     "ggcat_gpu_build_text",
     "ggcat_gpu_fasta_parse",
     "ggcat_gpu_build_from_files",
+    "ggcat_gpu_colors",
+    "ggcat_gpu_kmer_subsets_copy",
+    "ggcat_gpu_subsets_copy",
     "ggcat_gpu_query_index",
+    "ggcat_gpu_query_index_colored",
     "ggcat_gpu_query_submit",
     "ggcat_gpu_query_poll",
     "ggcat_gpu_query_wait",
-    "ggcat_gpu_query_subset_runs",
+    "ggcat_gpu_query_color_counts",
+    "ggcat_gpu_kmer_hashes",
     "ggcat_gpu_bucket_histogram_noalloc",
 ]
 
@@ -134,11 +139,16 @@ def load(build: bool = True):
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
-    L.ggcat_gpu_query_index.argtypes = [P, P, u64, C.c_int, P, P, u64, P]
+    L.ggcat_gpu_kmer_hashes.argtypes = [P, P, u64, C.c_int, C.c_int, P, P]
+    L.ggcat_gpu_colors.argtypes = [P, P, P, u64, C.c_uint32, P]
+    L.ggcat_gpu_kmer_subsets_copy.argtypes = [P, P, u64, pu64]
+    L.ggcat_gpu_subsets_copy.argtypes = [P, P, u64, pu64, C.POINTER(C.c_uint32)]
+    L.ggcat_gpu_query_index.argtypes = [P, P, u64, C.c_int, P]
+    L.ggcat_gpu_query_index_colored.argtypes = [P, P]
     L.ggcat_gpu_query_submit.argtypes = [P, C.c_int, P, u64, P, P, u64]
     L.ggcat_gpu_query_poll.argtypes = [P, C.c_int]
     L.ggcat_gpu_query_wait.argtypes = [P, C.c_int, P, u64, pu64]
-    L.ggcat_gpu_query_subset_runs.argtypes = [P, C.c_int, P, P, P, u64, pu64]
+    L.ggcat_gpu_query_color_counts.argtypes = [P, C.c_int, P, u64, C.POINTER(C.c_uint32)]
     for name in EXPORTED:
         if name not in ("ggcat_gpu_destroy", "ggcat_gpu_last_error", "ggcat_gpu_kernel_launches"):
             getattr(L, name).restype = C.c_int
@@ -191,6 +201,7 @@ class GpuContext:
         if rc != 0:
             raise GgcatGpuError(f"ggcat_gpu_create failed ({_ERRORS.get(rc, rc)}): is a CUDA device available?")
         self.h = h
+        self.k = 0  # k of the last bucketize / build
 
     def close(self):
         if getattr(self, "h", None):
@@ -213,6 +224,7 @@ class GpuContext:
         n = C.c_uint64()
         self._check(self.L.ggcat_gpu_bucketize(self.h, C.c_void_p(d_text_ptr), text_len, C.byref(p),
                                                C.c_void_p(stream), C.byref(n)), "bucketize")
+        self.k = p.k
         return n.value
 
     def superkmers(self) -> np.ndarray:
@@ -228,6 +240,7 @@ class GpuContext:
     def build_text(self, text: np.ndarray, p: Params, stream: int = 0):
         t = np.ascontiguousarray(text, dtype=np.uint8)
         self._check(self.L.ggcat_gpu_build_text(self.h, _ptr(t), len(t), C.byref(p), C.c_void_p(stream)), "build_text")
+        self.k = p.k
 
     def _unitigs(self, fn, what):
         nu, nb = C.c_uint64(), C.c_uint64()
@@ -244,9 +257,12 @@ class GpuContext:
         return self._unitigs(self.L.ggcat_gpu_partial_unitigs_copy, "partial_unitigs_copy")
 
     def kmers(self):
+        """Surviving canonical k-mers and multiplicities.  keys: u64 array for k <= 32, an
+        (n, 2) array of (lo, hi) words for k > 32."""
         n = C.c_uint64()
         self._check(self.L.ggcat_gpu_kmers_copy(self.h, None, None, 0, C.byref(n)), "kmers_copy")
-        keys = np.zeros(n.value, np.uint64)
+        wide = self.k > 32
+        keys = np.zeros((n.value, 2) if wide else n.value, np.uint64)
         mult = np.zeros(n.value, np.uint64)
         self._check(self.L.ggcat_gpu_kmers_copy(self.h, _ptr(keys), _ptr(mult), n.value, C.byref(n)), "kmers_copy")
         return keys, mult
@@ -257,13 +273,39 @@ class GpuContext:
     def unitigs(self):
         return self._unitigs(self.L.ggcat_gpu_unitigs_copy, "unitigs_copy")
 
+    def kmer_hashes(self, d_text_ptr: int, length: int, k: int, kind: int, d_out_ptr: int, stream: int = 0):
+        self._check(self.L.ggcat_gpu_kmer_hashes(self.h, C.c_void_p(d_text_ptr), length, k, kind,
+                                                 C.c_void_p(d_out_ptr), C.c_void_p(stream)), "kmer_hashes")
+
+    # ---- colours ----
+    def colors(self, seq_off, seq_color, n_colors: int, stream: int = 0):
+        so = np.ascontiguousarray(seq_off, np.uint64)
+        sc = np.ascontiguousarray(seq_color, np.uint32)
+        self._check(self.L.ggcat_gpu_colors(self.h, _ptr(so), _ptr(sc), len(so), n_colors, C.c_void_p(stream)),
+                    "colors")
+
+    def kmer_subsets(self) -> np.ndarray:
+        n = C.c_uint64()
+        self._check(self.L.ggcat_gpu_kmer_subsets_copy(self.h, None, 0, C.byref(n)), "kmer_subsets_copy")
+        out = np.zeros(n.value, np.uint32)
+        self._check(self.L.ggcat_gpu_kmer_subsets_copy(self.h, _ptr(out), n.value, C.byref(n)), "kmer_subsets_copy")
+        return out
+
+    def subsets(self) -> np.ndarray:
+        """(n_subsets, words) uint32 colour bitmaps."""
+        n, w = C.c_uint64(), C.c_uint32()
+        self._check(self.L.ggcat_gpu_subsets_copy(self.h, None, 0, C.byref(n), C.byref(w)), "subsets_copy")
+        out = np.zeros(n.value * w.value, np.uint32)
+        self._check(self.L.ggcat_gpu_subsets_copy(self.h, _ptr(out), out.size, C.byref(n), C.byref(w)), "subsets_copy")
+        return out.reshape(n.value, w.value)
+
     # ---- query ----
-    def query_index(self, d_graph_ptr: int, length: int, k: int, seq_off=None, seq_subset=None, stream: int = 0):
-        so = None if seq_off is None else np.ascontiguousarray(seq_off, np.uint64)
-        ss = None if seq_subset is None else np.ascontiguousarray(seq_subset, np.uint32)
-        n = 0 if so is None else len(so)
-        self._check(self.L.ggcat_gpu_query_index(self.h, C.c_void_p(d_graph_ptr), length, k, _ptr(so), _ptr(ss), n,
-                                                 C.c_void_p(stream)), "query_index")
+    def query_index(self, d_graph_ptr: int, length: int, k: int, stream: int = 0):
+        self._check(self.L.ggcat_gpu_query_index(self.h, C.c_void_p(d_graph_ptr), length, k, C.c_void_p(stream)),
+                    "query_index")
+
+    def query_index_colored(self, stream: int = 0):
+        self._check(self.L.ggcat_gpu_query_index_colored(self.h, C.c_void_p(stream)), "query_index_colored")
 
     def query_submit(self, slot: int, text: np.ndarray, off: np.ndarray, ln: np.ndarray):
         t = np.ascontiguousarray(text, np.uint8)
@@ -289,15 +331,15 @@ class GpuContext:
         self._check(self.L.ggcat_gpu_query_wait(self.h, slot, _ptr(out), nq, C.byref(got)), "query_wait")
         return out
 
-    def query_subset_runs(self, slot: int):
-        n = C.c_uint64()
-        self._check(self.L.ggcat_gpu_query_subset_runs(self.h, slot, None, None, None, 0, C.byref(n)), "subset_runs")
-        q = np.zeros(n.value, np.uint32)
-        sub = np.zeros(n.value, np.uint32)
-        cnt = np.zeros(n.value, np.uint32)
-        self._check(self.L.ggcat_gpu_query_subset_runs(self.h, slot, _ptr(q), _ptr(sub), _ptr(cnt), n.value,
-                                                       C.byref(n)), "subset_runs")
-        return q, sub, cnt
+    def query_color_counts(self, slot: int) -> np.ndarray:
+        """(nq, n_colors) per-colour counts of the slot's last (waited) coloured batch."""
+        nq = self._slot_nq.get(slot, 0)
+        nc = C.c_uint32()
+        self._check(self.L.ggcat_gpu_query_color_counts(self.h, slot, None, 0, C.byref(nc)), "query_color_counts")
+        out = np.zeros(nq * nc.value, np.uint64)
+        self._check(self.L.ggcat_gpu_query_color_counts(self.h, slot, _ptr(out), out.size, C.byref(nc)),
+                    "query_color_counts")
+        return out.reshape(nq, nc.value)
 
     def stats(self) -> dict:
         s = Stats()

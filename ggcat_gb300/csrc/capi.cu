@@ -91,6 +91,18 @@ struct ggcat_gpu_ctx {
     int fine_bits = 8;
     ggcat_gpu_params last_params{};
     bool have_buckets = false;
+    const uint8_t *last_text = nullptr;  // device text of the last bucketize
+
+    // colour phase
+    DevBuf<uint64_t> ckeys;
+    DevBuf<uint32_t> cvals, cbitmaps, cid_subset, cdump_subset, csub_state, csub_arena;
+    DevBuf<unsigned long long> csub_hash, ccounters;
+    DevBuf<uint64_t> cseq_off;
+    DevBuf<uint32_t> cseq_color;
+    uint64_t cmask = 0, c_n_ids = 0, c_n_subsets = 0;
+    uint32_t c_colors = 0;
+    int c_words = 0;
+    bool have_colors = false;
 
     // merge
     DevBuf<MergeUnit> small_units, medium_units, large_units, bucket_units;
@@ -117,9 +129,6 @@ struct ggcat_gpu_ctx {
     // query: resident graph index and in-flight batch slots
     DevBuf<uint64_t> qkeys;
     DevBuf<uint32_t> qvals;
-    DevBuf<uint8_t> qgraph_tmp;
-    DevBuf<uint64_t> qseq_off;
-    DevBuf<uint32_t> qseq_subset;
     uint64_t qmask = 0;
     int qk = 0;
     bool qcolored = false, qready = false;
@@ -129,12 +138,12 @@ struct ggcat_gpu_ctx {
         DevBuf<uint8_t> d_text;
         DevBuf<uint32_t> d_iq, d_il;
         DevBuf<uint64_t> d_is;
-        DevBuf<unsigned long long> d_matched, d_runs_cursor;
-        DevBuf<uint4> d_runs;
+        DevBuf<unsigned long long> d_matched, d_counts, d_queue;
+        DevBuf<uint64_t> d_qoff, d_qlen;
         DevBuf<unsigned> d_status;
-        PinnedBuf h_text, h_items, h_out;
-        uint64_t nq = 0, n_items = 0, runs_cap = 0;
-        bool busy = false;
+        PinnedBuf h_text, h_items, h_out, h_counts;
+        uint64_t nq = 0, n_items = 0;
+        bool busy = false, colored = false;
     };
     QuerySlot qslots[GGCAT_GPU_QUERY_SLOTS];
 
@@ -296,6 +305,8 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[2], s));
     ctx->n_text = text_len;
+    ctx->last_text = d_text;
+    ctx->have_colors = false;
     ctx->last_params = *p;
     ctx->have_buckets = true;
     ctx->stats = ggcat_gpu_stats{};
@@ -344,8 +355,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->out_off.ensure(u_cap));
     CK(ctx->out_len.ensure(u_cap));
     CK(ctx->out_flags.ensure(u_cap));
+    const int wide = p->k > 32 ? 1 : 0;  // u128 table keys
     if (p->keep_kmers) {
-        CK(ctx->kmer_keys.ensure(kmer_cap));
+        CK(ctx->kmer_keys.ensure(kmer_cap * (wide ? 2 : 1)));
         CK(ctx->kmer_mult.ensure(kmer_cap));
     }
     const uint64_t max_units = ctx->n_bins + 1;
@@ -354,18 +366,18 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->large_units.ensure(max_units));
     // worst-case slot pool of the global-memory tables: cap < 2 * (1.25 x + 64) per unit
     uint64_t pool = ctx->n_kmers * 5 / 2 + 128ull * (ctx->n_buckets + ctx->n_kmers / 4096 + 1) + 1024;
-    CK(ctx->tkeys.ensure(pool));
+    CK(ctx->tkeys.ensure(pool * (wide ? 2 : 1)));
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
     CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
 
-    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers};
+    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers, wide};
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
-    const uint64_t small_limit = 3200;  // fits kSmallSlots at load <= 0.8
-    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : 2048;
+    const uint64_t small_limit = merge_small_limit(wide);
+    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1024 : 2048);
     if (target > small_limit) target = small_limit;
 
     CK(cudaEventRecord(ctx->ev[3], s));
@@ -393,11 +405,11 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
             slot += cap;
             units[b] = u;
         }
-        if (slot > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "per-bucket table pool too small");
+        if (slot > pool) return fail(ctx, GGCAT_GPU_EDEVICE, "per-bucket table pool too small");
         CK(ctx->bucket_units.ensure(ctx->n_buckets));
         CK(cudaMemcpyAsync(ctx->bucket_units.p, units.data(), units.size() * sizeof(MergeUnit),
                            cudaMemcpyHostToDevice, s));
-        ctx->launches += launch_init_tables(ctx->tkeys.p, ctx->tvals.p, ctx->tvis.p, slot, ctx->sms, s);
+        ctx->launches += launch_init_tables(ctx->tkeys.p, wide, ctx->tvals.p, ctx->tvis.p, slot, ctx->sms, s);
         for (uint32_t b = 0; b < ctx->n_buckets; b++) {
             if (units[b].rec_end == units[b].rec_begin) continue;
             ctx->launches += launch_merge_large(a, ctx->bucket_units.p + b, ctx->ones.p, 1, ctx->tkeys.p, ctx->tvals.p,
@@ -410,12 +422,12 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         const uint64_t medium_limit = 1ull << 18;
         ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits,
                                                small_limit, target, medium_limit, ctx->small_units.p,
-                                               ctx->medium_units.p, ctx->large_units.p, max_units, ctx->tkeys.n,
+                                               ctx->medium_units.p, ctx->large_units.p, max_units, pool,
                                                ctx->counters.p, ctx->status.p + 1, s);
         ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
         ctx->launches += launch_merge_medium(a, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
                                              ctx->tvis.p, o, ctx->sms, s);
-        ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p,
+        ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
                                                  ctx->tvals.p, ctx->tvis.p, ctx->sms, s);
         ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p,
                                             ctx->tvals.p, ctx->tvis.p, o, ctx->sms, s);
@@ -434,7 +446,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     if (p->merge_mode != GGCAT_MERGE_PER_BUCKET) {
         ctx->stats.merge_units_small = cnt[kCntSmall];
         ctx->stats.merge_units_large = cnt[kCntMedium] + cnt[kCntLarge];
-        if (cnt[kCntSlots] > ctx->tkeys.n) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
+        if (cnt[kCntSlots] > pool) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
     }
     *st_out = st;
     return GGCAT_GPU_OK;
@@ -447,10 +459,13 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     if (!ctx->have_buckets) return fail(ctx, GGCAT_GPU_EINVAL, "merge needs a bucketize result");
     if (p->k != ctx->last_params.k || p->m != ctx->last_params.m || p->bucket_bits != ctx->last_params.bucket_bits)
         return fail(ctx, GGCAT_GPU_EINVAL, "merge parameters differ from the bucketize parameters");
-    if (p->k > 32 || (p->k % 2) == 0)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports odd k <= 32 (k=%d)", p->k);
-    if (p->hash_kind != GGCAT_HASH_SEQHASH && p->hash_kind != 0)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge for k<=32 uses the 64-bit seq-hash");
+    if (p->k > 64 || (p->k % 2) == 0)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports odd k <= 64 (k=%d)", p->k);
+    // Tables are keyed by the canonical packed k-mer (the seq-hash value).  The Rabin-Karp
+    // u128 hash is injective on the k-mers of any input short of a 128-bit collision, so it
+    // selects the same k-mer identities and gives the same result.
+    if (p->hash_kind != GGCAT_HASH_SEQHASH && p->hash_kind != GGCAT_HASH_RABIN_KARP128 && p->hash_kind != 0)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "unknown merge hash kind %d", p->hash_kind);
     if (p->min_multiplicity < 1) return fail(ctx, GGCAT_GPU_EINVAL, "min_multiplicity must be >= 1");
     if (ctx->n_kmers >= (1ull << 29) * 1024ull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "input too large");
     cudaStream_t s = as_stream(stream);
@@ -534,9 +549,10 @@ extern "C" int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint6
     if (n) *n = ctx->n_kmers_out;
     if (!h_kmers) return GGCAT_GPU_OK;
     uint64_t cnt = std::min<uint64_t>(cap, ctx->n_kmers_out);
+    const uint64_t words = ctx->last_params.k > 32 ? 2 : 1;
     CK(cudaSetDevice(ctx->device));
     if (cnt) {
-        CK(cudaMemcpy(h_kmers, ctx->kmer_keys.p, cnt * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h_kmers, ctx->kmer_keys.p, cnt * words * sizeof(uint64_t), cudaMemcpyDeviceToHost));
         std::vector<uint32_t> m(cnt);
         CK(cudaMemcpy(m.data(), ctx->kmer_mult.p, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         for (uint64_t i = 0; i < cnt; i++) h_mult[i] = m[i];
@@ -549,14 +565,23 @@ extern "C" int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint6
 // ---------------------------------------------------------------------------
 static inline uint8_t code_of(uint8_t a) { return (a >> 1) & 3; }
 
-static uint64_t canon_ascii(const uint8_t *s, int k) {
-    uint64_t fw = 0, rc = 0;
+// canonical packed k-mer of k ASCII bases (KT = uint64_t for k <= 32, unsigned __int128 for k <= 64)
+template <typename KT>
+static KT canon_ascii(const uint8_t *s, int k) {
+    KT fw = 0, rc = 0;
     for (int i = 0; i < k; i++) {
-        fw |= (uint64_t)code_of(s[i]) << (2 * i);
-        rc |= (uint64_t)(code_of(s[k - 1 - i]) ^ 2) << (2 * i);
+        fw |= (KT)code_of(s[i]) << (2 * i);
+        rc |= (KT)(code_of(s[k - 1 - i]) ^ 2) << (2 * i);
     }
     return fw < rc ? fw : rc;
 }
+
+struct KeyHash {
+    size_t operator()(uint64_t x) const { return (size_t)(x * 0x9E3779B97F4A7C15ull >> 17) ^ (size_t)x; }
+    size_t operator()(unsigned __int128 x) const {
+        return operator()((uint64_t)((uint64_t)x ^ ((uint64_t)(x >> 64) * 0xC2B2AE3D27D4EB4Full)));
+    }
+};
 
 static void rc_append(std::vector<uint8_t> &dst, const uint8_t *s, size_t n, size_t skip) {
     // append reverse complement of s[0..n), skipping its first `skip` bases
@@ -566,12 +591,8 @@ static void rc_append(std::vector<uint8_t> &dst, const uint8_t *s, size_t n, siz
     }
 }
 
-extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
-    if (!ctx) return GGCAT_GPU_EINVAL;
-    if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
-    if (k < 3 || k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 32");
-    int rc = fetch_partial(ctx);
-    if (rc) return rc;
+template <typename KT>
+static int link_impl(ggcat_gpu_ctx *ctx, int k) {
     auto t0 = std::chrono::steady_clock::now();
     const HostUnitigs &P = ctx->partial;
     HostUnitigs &F = ctx->final_u;
@@ -579,13 +600,13 @@ extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
     const size_t n = P.off.size();
     // endpoints: 2i = left end (backward link), 2i+1 = right end (forward link)
     std::vector<int64_t> partner(2 * n, -1);
-    std::unordered_map<uint64_t, int64_t> first_end;
+    std::unordered_map<KT, int64_t, KeyHash> first_end;
     first_end.reserve(n);
     for (size_t i = 0; i < n; i++) {
         for (int side = 0; side < 2; side++) {
             if (!(P.flags[i] & (side ? 2 : 1))) continue;
             const uint8_t *s = P.bases.data() + P.off[i] + (side ? P.len[i] - k : 0);
-            uint64_t key = canon_ascii(s, k);
+            const KT key = canon_ascii<KT>(s, k);
             auto it = first_end.find(key);
             int64_t ep = (int64_t)(2 * i + side);
             if (it == first_end.end()) {
@@ -652,6 +673,15 @@ extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
     ctx->stats.ms_link = std::chrono::duration<double, std::milli>(t1 - t0).count();
     ctx->stats.final_unitigs = F.off.size();
     return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
+    if (k < 3 || k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 64");
+    int rc = fetch_partial(ctx);
+    if (rc) return rc;
+    return k > 32 ? link_impl<unsigned __int128>(ctx, k) : link_impl<uint64_t>(ctx, k);
 }
 
 extern "C" int ggcat_gpu_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,
@@ -871,15 +901,103 @@ extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const 
 }
 
 // ---------------------------------------------------------------------------
+// colour subsets
+// ---------------------------------------------------------------------------
+extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, const uint32_t *h_seq_color,
+                                uint64_t n_seq, uint32_t n_colors, void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_merge || !ctx->last_params.keep_kmers)
+        return fail(ctx, GGCAT_GPU_EINVAL, "colours need a merge run with keep_kmers = 1");
+    if (ctx->last_params.k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "colours support k <= 32");
+    if (!h_seq_off || !h_seq_color || n_seq == 0 || n_colors == 0 || n_colors > 65536)
+        return fail(ctx, GGCAT_GPU_EINVAL, "bad colour table (n_seq=%llu, n_colors=%u)", (unsigned long long)n_seq,
+                    n_colors);
+    for (uint64_t i = 0; i < n_seq; i++) {
+        if (h_seq_color[i] >= n_colors) return fail(ctx, GGCAT_GPU_EINVAL, "colour out of range at sequence %llu",
+                                                    (unsigned long long)i);
+        if (i && h_seq_off[i] < h_seq_off[i - 1]) return fail(ctx, GGCAT_GPU_EINVAL, "sequence offsets not sorted");
+    }
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    ctx->have_colors = false;
+    const uint64_t nd = ctx->n_kmers_out;
+    const int words = (int)((n_colors + 31) / 32);
+    uint64_t cap = 1024;
+    while (cap < 2 * nd + 64) cap <<= 1;
+    uint64_t scap = 1024;
+    while (scap < 2 * nd + 64) scap <<= 1;
+    CK(ctx->ckeys.ensure(cap));
+    CK(ctx->cvals.ensure(cap));
+    CK(ctx->cbitmaps.ensure((nd + 1) * (uint64_t)words));
+    CK(ctx->cid_subset.ensure(nd + 1));
+    CK(ctx->cdump_subset.ensure(nd + 1));
+    CK(ctx->csub_hash.ensure(scap));
+    CK(ctx->csub_state.ensure(scap));
+    CK(ctx->csub_arena.ensure((nd + 1) * (uint64_t)words));
+    CK(ctx->ccounters.ensure(4));
+    CK(ctx->cseq_off.ensure(n_seq));
+    CK(ctx->cseq_color.ensure(n_seq));
+    CK(cudaMemcpyAsync(ctx->cseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->cseq_color.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(ctx->ckeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->cbitmaps.p, 0, (nd + 1) * words * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(ctx->csub_hash.p, 0, scap * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->csub_state.p, 0, scap * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(ctx->ccounters.p, 0, 4 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+    ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
+                                        ctx->cseq_off.p, ctx->cseq_color.p, n_seq, words, ctx->ckeys.p, ctx->cvals.p,
+                                        cap - 1, ctx->cbitmaps.p, ctx->ccounters.p, ctx->csub_hash.p,
+                                        ctx->csub_state.p, ctx->csub_arena.p, scap - 1, ctx->cid_subset.p,
+                                        ctx->cdump_subset.p, ctx->status.p + 1, nd, ctx->sms, s);
+    CK(cudaGetLastError());
+    unsigned long long cnt[2];
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(cnt, ctx->ccounters.p, sizeof cnt, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "colour phase: internal error (status %u)", st);
+    ctx->cmask = cap - 1;
+    ctx->c_n_ids = cnt[0];
+    ctx->c_n_subsets = cnt[1];
+    ctx->c_words = words;
+    ctx->c_colors = n_colors;
+    ctx->have_colors = true;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_kmer_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_subset, uint64_t cap, uint64_t *n) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result");
+    if (n) *n = ctx->n_kmers_out;
+    if (!h_subset) return GGCAT_GPU_OK;
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t m = std::min<uint64_t>(cap, ctx->n_kmers_out);
+    if (m) CK(cudaMemcpy(h_subset, ctx->cdump_subset.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_bitmaps, uint64_t cap_words, uint64_t *n_subsets,
+                                      uint32_t *words_per_subset) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result");
+    if (n_subsets) *n_subsets = ctx->c_n_subsets;
+    if (words_per_subset) *words_per_subset = (uint32_t)ctx->c_words;
+    if (!h_bitmaps) return GGCAT_GPU_OK;
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t m = std::min<uint64_t>(cap_words, ctx->c_n_subsets * (uint64_t)ctx->c_words);
+    if (m) CK(cudaMemcpy(h_bitmaps, ctx->csub_arena.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
 // graph query lookup
 // ---------------------------------------------------------------------------
 extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k,
-                                     const uint64_t *h_seq_off, const uint32_t *h_seq_subset, uint64_t n_seq,
                                      void *stream) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     if (k < 3 || k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "query index supports k <= 32 (k=%d)", k);
     if (len > 0 && !d_graph_text) return fail(ctx, GGCAT_GPU_EINVAL, "null graph text");
-    if (h_seq_subset && (!h_seq_off || n_seq == 0)) return fail(ctx, GGCAT_GPU_EINVAL, "colour subsets need offsets");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
     ctx->qready = false;
@@ -888,20 +1006,8 @@ extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_
     CK(ctx->qkeys.ensure(cap));
     CK(ctx->qvals.ensure(cap));
     CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
-    CK(cudaMemsetAsync(ctx->qvals.p, 0, cap * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
-    const uint64_t *d_off = nullptr;
-    const uint32_t *d_sub = nullptr;
-    if (h_seq_subset) {
-        CK(ctx->qseq_off.ensure(n_seq));
-        CK(ctx->qseq_subset.ensure(n_seq));
-        CK(cudaMemcpyAsync(ctx->qseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(ctx->qseq_subset.p, h_seq_subset, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-        d_off = ctx->qseq_off.p;
-        d_sub = ctx->qseq_subset.p;
-    }
-    ctx->launches += launch_index_insert(d_graph_text, len, k, d_off, d_sub, n_seq, ctx->qkeys.p, ctx->qvals.p, cap - 1,
-                                         ctx->status.p + 1, s);
+    ctx->launches += launch_index_insert(d_graph_text, len, k, ctx->qkeys.p, ctx->qvals.p, cap - 1, ctx->status.p + 1, s);
     CK(cudaGetLastError());
     unsigned st = 0;
     CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
@@ -909,7 +1015,33 @@ extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_
     if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "query index: table full");
     ctx->qmask = cap - 1;
     ctx->qk = k;
-    ctx->qcolored = h_seq_subset != nullptr;
+    ctx->qcolored = false;
+    ctx->qready = true;
+    return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result to index");
+    cudaStream_t s = as_stream(stream);
+    CK(cudaSetDevice(ctx->device));
+    ctx->qready = false;
+    uint64_t cap = 1024;
+    while (cap < 2 * ctx->c_n_ids + 64) cap <<= 1;
+    CK(ctx->qkeys.ensure(cap));
+    CK(ctx->qvals.ensure(cap));
+    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+    ctx->launches += launch_index_from_colors(ctx->ckeys.p, ctx->cvals.p, ctx->cmask + 1, ctx->cid_subset.p,
+                                              ctx->qkeys.p, ctx->qvals.p, cap - 1, ctx->status.p + 1, ctx->sms, s);
+    CK(cudaGetLastError());
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "coloured query index: table full");
+    ctx->qmask = cap - 1;
+    ctx->qk = ctx->last_params.k;
+    ctx->qcolored = true;
     ctx->qready = true;
     return GGCAT_GPU_OK;
 }
@@ -928,57 +1060,73 @@ extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_
         CK(cudaEventCreateWithFlags(&q.done, cudaEventDisableTiming));
     }
     const int k = ctx->qk;
-    const uint64_t kChunk = 2048;
-    // work items: runs of at most kChunk k-mer positions of one query
-    uint64_t n_items = 0;
-    for (uint64_t i = 0; i < nq; i++) {
-        if (h_off[i] + h_len[i] > len) return fail(ctx, GGCAT_GPU_EINVAL, "query %llu outside the text", (unsigned long long)i);
-        const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
-        n_items += (nk + kChunk - 1) / kChunk;
-    }
-    const size_t item_bytes = n_items * (4 + 8 + 4);
-    CK(q.h_text.ensure(len + 1));
-    CK(q.h_items.ensure(item_bytes + 16));
-    CK(q.h_out.ensure(nq * sizeof(unsigned long long) + 16));
-    memcpy(q.h_text.p, h_text, len);
-    uint32_t *iq = reinterpret_cast<uint32_t *>(q.h_items.p);
-    uint64_t *is = reinterpret_cast<uint64_t *>(q.h_items.p + n_items * 4);
-    uint32_t *il = reinterpret_cast<uint32_t *>(q.h_items.p + n_items * 12);
-    uint64_t it = 0;
-    for (uint64_t i = 0; i < nq; i++) {
-        const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
-        for (uint64_t c = 0; c < nk; c += kChunk, it++) {
-            iq[it] = (uint32_t)i;
-            is[it] = h_off[i] + c;
-            il[it] = (uint32_t)std::min<uint64_t>(kChunk, nk - c);
-        }
-    }
-    CK(q.d_text.ensure(len + 1));
-    CK(q.d_iq.ensure(n_items + 1));
-    CK(q.d_is.ensure(n_items + 1));
-    CK(q.d_il.ensure(n_items + 1));
-    CK(q.d_matched.ensure(nq + 1));
-    CK(q.d_runs_cursor.ensure(1));
-    CK(q.d_status.ensure(1));
-    uint64_t runs_cap = ctx->qcolored ? n_items * 4 + 1024 : 1;
-    CK(q.d_runs.ensure(runs_cap));
+    for (uint64_t i = 0; i < nq; i++)
+        if (h_off[i] + h_len[i] > len)
+            return fail(ctx, GGCAT_GPU_EINVAL, "query %llu outside the text", (unsigned long long)i);
     cudaStream_t s = q.stream;
+    CK(q.h_text.ensure(len + 1));
+    memcpy(q.h_text.p, h_text, len);
+    CK(q.d_text.ensure(len + 1));
+    CK(q.d_matched.ensure(nq + 1));
+    CK(q.d_status.ensure(1));
+    CK(q.h_out.ensure(nq * sizeof(unsigned long long) + 16));
     CK(cudaMemcpyAsync(q.d_text.p, q.h_text.p, len, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(q.d_iq.p, iq, n_items * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(q.d_is.p, is, n_items * 8, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(q.d_il.p, il, n_items * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(q.d_matched.p, 0, nq * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(q.d_runs_cursor.p, 0, sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(q.d_status.p, 0, sizeof(unsigned), s));
-    ctx->launches += launch_query(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items, ctx->qkeys.p, ctx->qvals.p,
-                                  ctx->qmask, q.d_matched.p, ctx->qcolored ? 1 : 0, q.d_runs.p, q.d_runs.n,
-                                  q.d_runs_cursor.p, q.d_status.p, s);
+    q.colored = ctx->qcolored;
+    if (!ctx->qcolored) {
+        // work items: runs of at most kChunk k-mer positions of one query
+        const uint64_t kChunk = 2048;
+        uint64_t n_items = 0;
+        for (uint64_t i = 0; i < nq; i++) {
+            const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
+            n_items += (nk + kChunk - 1) / kChunk;
+        }
+        CK(q.h_items.ensure(n_items * 16 + 16));
+        uint32_t *iq = reinterpret_cast<uint32_t *>(q.h_items.p);
+        uint64_t *is = reinterpret_cast<uint64_t *>(q.h_items.p + n_items * 4);
+        uint32_t *il = reinterpret_cast<uint32_t *>(q.h_items.p + n_items * 12);
+        uint64_t it = 0;
+        for (uint64_t i = 0; i < nq; i++) {
+            const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
+            for (uint64_t c = 0; c < nk; c += kChunk, it++) {
+                iq[it] = (uint32_t)i;
+                is[it] = h_off[i] + c;
+                il[it] = (uint32_t)std::min<uint64_t>(kChunk, nk - c);
+            }
+        }
+        CK(q.d_iq.ensure(n_items + 1));
+        CK(q.d_is.ensure(n_items + 1));
+        CK(q.d_il.ensure(n_items + 1));
+        CK(cudaMemcpyAsync(q.d_iq.p, iq, n_items * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(q.d_is.p, is, n_items * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(q.d_il.p, il, n_items * 4, cudaMemcpyHostToDevice, s));
+        ctx->launches += launch_query(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items, ctx->qkeys.p, ctx->qmask,
+                                      q.d_matched.p, s);
+        q.n_items = n_items;
+    } else {
+        const uint64_t nc = ctx->c_colors;
+        CK(q.h_items.ensure(nq * 16 + 16));
+        memcpy(q.h_items.p, h_off, nq * 8);
+        memcpy(q.h_items.p + nq * 8, h_len, nq * 8);
+        CK(q.d_qoff.ensure(nq + 1));
+        CK(q.d_qlen.ensure(nq + 1));
+        CK(q.d_counts.ensure(nq * nc + 1));
+        CK(q.d_queue.ensure(1));
+        CK(q.h_counts.ensure(nq * nc * sizeof(unsigned long long) + 16));
+        CK(cudaMemcpyAsync(q.d_qoff.p, q.h_items.p, nq * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(q.d_qlen.p, q.h_items.p + nq * 8, nq * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(q.d_queue.p, 0, sizeof(unsigned long long), s));
+        ctx->launches += launch_query_color(q.d_text.p, k, q.d_qoff.p, q.d_qlen.p, nq, ctx->qkeys.p, ctx->qvals.p,
+                                            ctx->qmask, ctx->csub_arena.p, ctx->c_words, ctx->c_colors, q.d_matched.p,
+                                            q.d_counts.p, q.d_queue.p, ctx->sms, s);
+        CK(cudaMemcpyAsync(q.h_counts.p, q.d_counts.p, nq * nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           s));
+        q.n_items = nq;
+    }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(q.h_out.p, q.d_matched.p, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(q.done, s));
     q.nq = nq;
-    q.n_items = n_items;
-    q.runs_cap = q.d_runs.n;
     q.busy = true;
     return GGCAT_GPU_OK;
 }
@@ -1000,32 +1148,35 @@ extern "C" int ggcat_gpu_query_wait(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_ma
     CK(cudaSetDevice(ctx->device));
     CK(cudaEventSynchronize(q.done));
     q.busy = false;
-    unsigned st = 0;
-    CK(cudaMemcpy(&st, q.d_status.p, sizeof st, cudaMemcpyDeviceToHost));
-    if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "query: run buffer overflow");
     if (nq) *nq = q.nq;
     if (h_matched) memcpy(h_matched, q.h_out.p, std::min<uint64_t>(cap, q.nq) * sizeof(uint64_t));
     return GGCAT_GPU_OK;
 }
 
-extern "C" int ggcat_gpu_query_subset_runs(ggcat_gpu_ctx *ctx, int slot, uint32_t *h_query, uint32_t *h_subset,
-                                           uint32_t *h_count, uint64_t cap, uint64_t *n_runs) {
+extern "C" int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_counts, uint64_t cap,
+                                            uint32_t *n_colors) {
     if (!ctx || slot < 0 || slot >= GGCAT_GPU_QUERY_SLOTS) return GGCAT_GPU_EINVAL;
     auto &q = ctx->qslots[slot];
     if (q.busy) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d still running; wait first", slot);
+    if (!q.colored) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d ran an uncoloured batch", slot);
+    if (n_colors) *n_colors = ctx->c_colors;
+    if (h_counts)
+        memcpy(h_counts, q.h_counts.p, std::min<uint64_t>(cap, q.nq * (uint64_t)ctx->c_colors) * sizeof(uint64_t));
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// hash families
+// ---------------------------------------------------------------------------
+extern "C" int ggcat_gpu_kmer_hashes(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t len, int k, int kind,
+                                     uint64_t *d_out, void *stream) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (kind < 0 || kind > 6) return fail(ctx, GGCAT_GPU_EINVAL, "bad hash kind %d", kind);
+    const int kmax = kind <= 1 ? 32 : kind <= 3 ? 64 : kind == 6 ? 64 : 127;
+    if (k < 2 || k > kmax) return fail(ctx, GGCAT_GPU_EINVAL, "k=%d outside [2, %d] for hash kind %d", k, kmax, kind);
+    if (len && (!d_text || !d_out)) return fail(ctx, GGCAT_GPU_EINVAL, "null buffer");
     CK(cudaSetDevice(ctx->device));
-    unsigned long long n = 0;
-    CK(cudaMemcpy(&n, q.d_runs_cursor.p, sizeof n, cudaMemcpyDeviceToHost));
-    if (n > q.runs_cap) return fail(ctx, GGCAT_GPU_EDEVICE, "query: run buffer overflow");
-    if (n_runs) *n_runs = n;
-    if (!h_query) return GGCAT_GPU_OK;
-    uint64_t m = std::min<uint64_t>(cap, n);
-    std::vector<uint4> tmp(m);
-    if (m) CK(cudaMemcpy(tmp.data(), q.d_runs.p, m * sizeof(uint4), cudaMemcpyDeviceToHost));
-    for (uint64_t i = 0; i < m; i++) {
-        h_query[i] = tmp[i].x;
-        h_subset[i] = tmp[i].y;
-        h_count[i] = tmp[i].z;
-    }
+    ctx->launches += launch_kmer_hash(d_text, len, k, kind, d_out, as_stream(stream));
+    CK(cudaGetLastError());
     return GGCAT_GPU_OK;
 }

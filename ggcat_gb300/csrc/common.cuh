@@ -41,6 +41,88 @@ __device__ __forceinline__ uint64_t rc_packed(uint64_t v, int k) {
 
 __device__ __forceinline__ uint64_t kmer_mask(int k) { return k >= 32 ? ~0ull : ((1ull << (2 * k)) - 1); }
 
+// ---------------------------------------------------------------------------
+// k-mer key types of the merge tables: u64 for k <= 32, u128 for 32 < k <= 64.  Both hold the
+// canonical 2-bit packed k-mer (base i at bits 2i), i.e. the seq-hash value of the reference
+// (crates/hashes/src/base/cn_seqhash_base.rs:22-69, u64 and u128 variants).
+// ---------------------------------------------------------------------------
+typedef unsigned __int128 u128;
+
+template <typename KT>
+struct KeyOps;
+
+template <>
+struct KeyOps<uint64_t> {
+    static constexpr int kMaxK = 32;
+    __device__ static __forceinline__ uint64_t empty() { return ~0ull; }
+    __device__ static __forceinline__ uint32_t hash(uint64_t x) { return (uint32_t)mix64(x); }
+    __device__ static __forceinline__ uint64_t rc(uint64_t v, int k) { return rc_packed(v, k); }
+    __device__ static __forceinline__ uint64_t mask(int k) { return kmer_mask(k); }
+    __device__ static __forceinline__ uint64_t cas(uint64_t *a, uint64_t cmp, uint64_t val) {
+        return atomicCAS(reinterpret_cast<unsigned long long *>(a), (unsigned long long)cmp, (unsigned long long)val);
+    }
+    // k bases starting at base p of the packed text
+    __device__ static __forceinline__ uint64_t load(const uint64_t *__restrict__ packed, uint64_t p, int k) {
+        const uint64_t w = p >> 5;
+        const uint32_t sh = (uint32_t)(p & 31) * 2u;
+        uint64_t v = packed[w] >> sh;
+        if (sh + 2u * (uint32_t)k > 64u) v |= packed[w + 1] << (64u - sh);
+        return v & kmer_mask(k);
+    }
+    __device__ static __forceinline__ void store(uint64_t *arr, uint64_t i, uint64_t key) { arr[i] = key; }
+};
+
+// 128-bit compare-and-swap (PTX atom.cas.b128, sm_90 and later; generic address, so it works on
+// shared and global memory); the address is 16-byte aligned
+__device__ __forceinline__ u128 cas_u128(u128 *addr, u128 cmp, u128 val) {
+    const uint64_t clo = (uint64_t)cmp, chi = (uint64_t)(cmp >> 64), vlo = (uint64_t)val, vhi = (uint64_t)(val >> 64);
+    uint64_t olo, ohi;
+    asm volatile(
+        "{\n\t.reg .b128 d, b, c;\n\t"
+        "mov.b128 b, {%2, %3};\n\t"
+        "mov.b128 c, {%4, %5};\n\t"
+        "atom.cas.b128 d, [%6], b, c;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}\n"
+        : "=l"(olo), "=l"(ohi)
+        : "l"(clo), "l"(chi), "l"(vlo), "l"(vhi), "l"(addr)
+        : "memory");
+    return ((u128)ohi << 64) | (u128)olo;
+}
+
+template <>
+struct KeyOps<u128> {
+    static constexpr int kMaxK = 64;
+    __device__ static __forceinline__ u128 empty() { return ~(u128)0; }
+    __device__ static __forceinline__ uint32_t hash(u128 x) {
+        return (uint32_t)mix64((uint64_t)x ^ mix64((uint64_t)(x >> 64)));
+    }
+    // the 64-base reverse complement is the rc of the two 32-base halves, swapped
+    __device__ static __forceinline__ u128 rc(u128 v, int k) {
+        const uint64_t rlo = rc_packed((uint64_t)(v >> 64), 32), rhi = rc_packed((uint64_t)v, 32);
+        return (((u128)rhi << 64) | (u128)rlo) >> (2 * (64 - k));
+    }
+    __device__ static __forceinline__ u128 mask(int k) { return k >= 64 ? ~(u128)0 : (((u128)1 << (2 * k)) - 1); }
+    __device__ static __forceinline__ u128 cas(u128 *a, u128 cmp, u128 val) { return cas_u128(a, cmp, val); }
+    __device__ static __forceinline__ u128 load(const uint64_t *__restrict__ packed, uint64_t p, int k) {
+        const uint64_t w = p >> 5;
+        const uint32_t sh = (uint32_t)(p & 31) * 2u;
+        const uint32_t need = sh + 2u * (uint32_t)k;  // bits used from word w on
+        uint64_t lo = packed[w] >> sh, hi = 0;
+        if (need > 64u) {
+            const uint64_t a1 = packed[w + 1];
+            if (sh) lo |= a1 << (64u - sh);
+            hi = sh ? a1 >> sh : a1;
+            if (need > 128u) hi |= packed[w + 2] << (64u - sh);  // need > 128 implies sh > 0
+        }
+        return (((u128)hi << 64) | (u128)lo) & mask(k);
+    }
+    // dumped keys are stored as (lo, hi) word pairs
+    __device__ static __forceinline__ void store(uint64_t *arr, uint64_t i, u128 key) {
+        arr[2 * i] = (uint64_t)key;
+        arr[2 * i + 1] = (uint64_t)(key >> 64);
+    }
+};
+
 // Superkmer record of the device bucket store (16 bytes):
 //   w0 = start (40 bits) | len << 40 (24 bits)
 //   w1 = bucket (16) | second_bucket << 16 (8) | flags << 24 (2) | rc << 26 (1)

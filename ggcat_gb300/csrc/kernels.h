@@ -37,7 +37,7 @@ struct MergeOut {
     uint8_t *u_flags;             // bit0 bw link, bit1 fw link, bit2 circular
     unsigned long long u_cap;
     unsigned long long *counters; // see kCnt*
-    uint64_t *kmer_keys;          // optional k-mer dump
+    uint64_t *kmer_keys;          // optional k-mer dump (u128 keys: (lo, hi) word pairs)
     uint32_t *kmer_mult;
     unsigned long long kmer_cap;
     unsigned *status;
@@ -49,6 +49,7 @@ struct MergeArgs {
     int k;
     int min_mult;
     int keep_kmers;
+    int wide;  // 0: u64 keys (k <= 32); 1: u128 keys (k <= 64)
 };
 
 // merge counters (device array of 16 u64)
@@ -73,22 +74,43 @@ int launch_classify_units(const unsigned long long *bin_off, const unsigned long
                           uint64_t pool_slots, unsigned long long *counters, unsigned *status, cudaStream_t s);
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s);
-int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, uint64_t *keys,
+// Table keys are u64 (a.wide == 0) or u128 (a.wide == 1, 16-byte aligned) slots.
+int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
                         uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s);
 // grid-wide insert/extend/cycles over the units [0, *n_units_dev)
 int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
-                       uint64_t n_units_host_hint, uint64_t *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
+                       uint64_t n_units_host_hint, void *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
                        int sms, cudaStream_t s);
-int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
-int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, uint64_t *keys, uint32_t *vals,
-                            uint8_t *vis, int sms, cudaStream_t s);
+int launch_init_tables(void *keys, int wide, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
+int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, void *keys, int wide,
+                            uint32_t *vals, uint8_t *vis, int sms, cudaStream_t s);
+// largest number of k-mer instances of an S unit
+uint64_t merge_small_limit(int wide);
 
 // query.cu
-int launch_index_insert(const uint8_t *text, uint64_t n, int k, const uint64_t *seq_off, const uint32_t *seq_subset,
-                        uint64_t n_seq, uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, cudaStream_t s);
+int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,
+                        unsigned *status, cudaStream_t s);
+int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint64_t ccap, const uint32_t *id_subset,
+                             uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s);
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
-                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, const uint32_t *vals, uint64_t mask,
-                 unsigned long long *matched, int colored, uint4 *runs, unsigned long long runs_cap,
-                 unsigned long long *runs_cursor, unsigned *status, cudaStream_t s);
+                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, uint64_t mask,
+                 unsigned long long *matched, cudaStream_t s);
+int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
+                       const uint64_t *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
+                       uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
+                       unsigned long long *queue, int sms, cudaStream_t s);
+
+// hashes.cu
+int launch_kmer_hash(const uint8_t *text, uint64_t n, int k, int kind, uint64_t *out, cudaStream_t s);
+
+// colors.cu
+int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
+                       const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words, uint64_t *keys,
+                       uint32_t *vals, uint64_t mask, uint32_t *bitmaps, unsigned long long *counters,
+                       unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena, uint64_t sub_mask,
+                       uint32_t *id_subset, uint32_t *dump_subset, unsigned *status, uint64_t n_ids_upper, int sms,
+                       cudaStream_t s);
+int launch_color_text_subsets(const uint8_t *text, uint64_t n, int k, const uint64_t *keys, const uint32_t *vals,
+                              uint64_t mask, const uint32_t *id_subset, uint32_t *out, cudaStream_t s);
 
 }  // namespace ggcat

@@ -18,8 +18,9 @@
 
 namespace ggcat {
 
+template <typename KT>
 struct Table {
-    uint64_t *keys;
+    KT *keys;
     uint32_t *vals;  // count (30 bits) | flags << 30 (bit30: begin ignored, bit31: end ignored)
     uint8_t *vis;
     uint32_t cap;    // power of two
@@ -27,28 +28,30 @@ struct Table {
 
 constexpr uint32_t kCountMask = (1u << 30) - 1;
 
-__device__ __forceinline__ uint32_t slot_of(uint64_t key, uint32_t cap) { return (uint32_t)mix64(key) & (cap - 1); }
+template <typename KT>
+__device__ __forceinline__ uint32_t slot_of(KT key, uint32_t cap) { return KeyOps<KT>::hash(key) & (cap - 1); }
 
-__device__ __forceinline__ int64_t tfind(const Table &t, uint64_t key) {
+template <typename KT>
+__device__ __forceinline__ int64_t tfind(const Table<KT> &t, KT key) {
     uint32_t s = slot_of(key, t.cap);
     for (uint32_t probe = 0; probe < t.cap; probe++) {
-        uint64_t kk = t.keys[s];
+        const KT kk = t.keys[s];
         if (kk == key) return s;
-        if (kk == kEmptyKey) return -1;
+        if (kk == KeyOps<KT>::empty()) return -1;
         s = (s + 1) & (t.cap - 1);
     }
     return -1;
 }
 
-__device__ __forceinline__ int64_t tinsert(const Table &t, uint64_t key, unsigned *status) {
+template <typename KT>
+__device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned *status) {
     uint32_t s = slot_of(key, t.cap);
     for (uint32_t probe = 0; probe < t.cap; probe++) {
-        uint64_t kk = t.keys[s];
+        const KT kk = t.keys[s];
         if (kk == key) return s;
-        if (kk == kEmptyKey) {
-            unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&t.keys[s]),
-                                               (unsigned long long)kEmptyKey, (unsigned long long)key);
-            if (old == kEmptyKey || old == key) return s;
+        if (kk == KeyOps<KT>::empty()) {
+            const KT old = KeyOps<KT>::cas(&t.keys[s], KeyOps<KT>::empty(), key);
+            if (old == KeyOps<KT>::empty() || old == key) return s;
         }
         s = (s + 1) & (t.cap - 1);
     }
@@ -62,28 +65,30 @@ __device__ __forceinline__ uint32_t val_mult(uint32_t v) {
     return (v >> 30) == 3u ? (c >> 1) : c;
 }
 
+template <typename KT>
 struct Graph {
-    Table t;
+    Table<KT> t;
     int k;
     uint32_t min_mult;
 
-    __device__ __forceinline__ uint64_t canon(uint64_t v) const {
-        uint64_t r = rc_packed(v, k);
+    __device__ __forceinline__ KT rc(KT v) const { return KeyOps<KT>::rc(v, k); }
+    __device__ __forceinline__ KT canon(KT v) const {
+        const KT r = rc(v);
         return v < r ? v : r;
     }
     // slot of an oriented k-mer if present and surviving, else -1
-    __device__ __forceinline__ int64_t alive(uint64_t v) const {
+    __device__ __forceinline__ int64_t alive(KT v) const {
         int64_t s = tfind(t, canon(v));
         if (s < 0) return -1;
         return val_mult(t.vals[s]) >= min_mult ? s : -1;
     }
     // surviving successors of oriented v; *only receives the last one found
-    __device__ __forceinline__ int succ(uint64_t v, uint64_t &only) const {
+    __device__ __forceinline__ int succ(KT v, KT &only) const {
         int d = 0;
-        uint64_t base = v >> 2;
+        const KT base = v >> 2;
 #pragma unroll
         for (uint32_t b = 0; b < 4; b++) {
-            uint64_t u = base | ((uint64_t)b << (2 * (k - 1)));
+            const KT u = base | ((KT)b << (2 * (k - 1)));
             if (alive(u) >= 0) {
                 d++;
                 only = u;
@@ -93,36 +98,36 @@ struct Graph {
     }
     // ignored-side flags in the orientation of v (hashmap.rs:453-465):
     // canonical orientation: flags == 1 -> left boundary, flags == 2 -> right boundary.
-    __device__ __forceinline__ bool right_boundary(uint64_t v, int64_t slot) const {
+    __device__ __forceinline__ bool right_boundary(KT v, int64_t slot) const {
         uint32_t f = t.vals[slot] >> 30;
-        bool is_canon = v <= rc_packed(v, k);
+        bool is_canon = v <= rc(v);
         return is_canon ? f == 2u : f == 1u;
     }
-    __device__ __forceinline__ bool left_boundary(uint64_t v, int64_t slot) const {
+    __device__ __forceinline__ bool left_boundary(KT v, int64_t slot) const {
         uint32_t f = t.vals[slot] >> 30;
-        bool is_canon = v <= rc_packed(v, k);
+        bool is_canon = v <= rc(v);
         return is_canon ? f == 1u : f == 2u;
     }
     // Traversable successor: unique surviving successor u with a unique surviving
     // predecessor, no bucket boundary between them, and not the same k-mer.
-    __device__ __forceinline__ bool next(uint64_t v, int64_t sv, uint64_t &u, int64_t &su) const {
+    __device__ __forceinline__ bool next(KT v, int64_t sv, KT &u, int64_t &su) const {
         if (right_boundary(v, sv)) return false;
         if (succ(v, u) != 1) return false;
         su = tfind(t, canon(u));
         if (su == sv) return false;
-        uint64_t w;
-        if (succ(rc_packed(u, k), w) != 1) return false;
+        KT w;
+        if (succ(rc(u), w) != 1) return false;
         if (left_boundary(u, su)) return false;
         return true;
     }
-    __device__ __forceinline__ bool is_start(uint64_t v, int64_t sv) const {
+    __device__ __forceinline__ bool is_start(KT v, int64_t sv) const {
         if (left_boundary(v, sv)) return true;
-        uint64_t w;
-        if (succ(rc_packed(v, k), w) != 1) return true;
-        uint64_t y = rc_packed(w, k);  // the unique predecessor, oriented towards v
+        KT w;
+        if (succ(rc(v), w) != 1) return true;
+        const KT y = rc(w);  // the unique predecessor, oriented towards v
         int64_t sy = tfind(t, canon(y));
         if (sy == sv) return true;
-        uint64_t z;
+        KT z;
         if (succ(y, z) != 1) return true;
         if (right_boundary(y, sy)) return true;
         return false;
@@ -132,13 +137,14 @@ struct Graph {
 __device__ __forceinline__ char base_char(uint32_t c) { return "ACTG"[c & 3]; }
 
 // Walk a path from start v; returns the end node and the number of steps.
-__device__ __forceinline__ uint32_t walk_to_end(const Graph &g, uint64_t v, int64_t sv, uint64_t &end, int64_t &send,
+template <typename KT>
+__device__ __forceinline__ uint32_t walk_to_end(const Graph<KT> &g, KT v, int64_t sv, KT &end, int64_t &send,
                                                 unsigned *status) {
     uint32_t steps = 0;
-    uint64_t cur = v;
+    KT cur = v;
     int64_t scur = sv;
     for (;;) {
-        uint64_t u;
+        KT u;
         int64_t su;
         if (!g.next(cur, scur, u, su)) break;
         cur = u;
@@ -154,7 +160,8 @@ __device__ __forceinline__ uint32_t walk_to_end(const Graph &g, uint64_t v, int6
 }
 
 // Emit the path (or cycle of `steps` edges when circular) starting at v.
-__device__ void emit_walk(const Graph &g, uint64_t v, int64_t sv, uint32_t steps, uint8_t flags, const MergeOut &o) {
+template <typename KT>
+__device__ void emit_walk(const Graph<KT> &g, KT v, int64_t sv, uint32_t steps, uint8_t flags, const MergeOut &o) {
     const int k = g.k;
     uint64_t len = (uint64_t)k + steps;
     unsigned long long off = atomicAdd(&o.counters[1], (unsigned long long)len);
@@ -168,10 +175,10 @@ __device__ void emit_walk(const Graph &g, uint64_t v, int64_t sv, uint32_t steps
         for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
     }
     g.t.vis[sv] = 1;
-    uint64_t cur = v;
+    KT cur = v;
     int64_t scur = sv;
     for (uint32_t s = 0; s < steps; s++) {
-        uint64_t u;
+        KT u;
         int64_t su;
         if (!g.next(cur, scur, u, su)) break;
         if (ok) o.bases[off + k + s] = base_char((uint32_t)(u >> (2 * (k - 1))));
@@ -183,16 +190,17 @@ __device__ void emit_walk(const Graph &g, uint64_t v, int64_t sv, uint32_t steps
 
 // Insert all k-mers of one superkmer record (hashmap.rs:361-431 add_sequence), processing
 // the bases in text orientation with the flags mapped from the stored orientation.
-__device__ __forceinline__ void insert_record(const Table &t, const uint64_t *__restrict__ packed, const SkRec r, int k,
-                                              unsigned *status) {
+template <typename KT>
+__device__ __forceinline__ void insert_record(const Table<KT> &t, const uint64_t *__restrict__ packed, const SkRec r,
+                                              int k, unsigned *status) {
     const uint64_t start = rec_start(r);
     const uint32_t len = rec_len(r);
     const uint32_t fl = rec_flags(r), rcf = rec_rc(r);
     // text-orientation included flags: begin <- stored end when reverse-complemented
     const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
     const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
-    const uint64_t mask = kmer_mask(k);
-    uint64_t fw = 0, rc = 0;
+    const KT mask = KeyOps<KT>::mask(k);
+    KT fw = 0, rc = 0;
     uint64_t cur_word = ~0ull, pw = 0;
     const uint32_t last = len - (uint32_t)k;
     for (uint32_t i = 0; i < len; i++) {
@@ -202,66 +210,67 @@ __device__ __forceinline__ void insert_record(const Table &t, const uint64_t *__
             cur_word = wi;
             pw = packed[wi];
         }
-        uint64_t c = (pw >> (2 * (p & 31))) & 3u;
-        fw = (fw >> 2) | (c << (2 * (k - 1)));
-        rc = ((rc << 2) | (c ^ 2u)) & mask;
+        const uint32_t c = (uint32_t)(pw >> (2 * (p & 31))) & 3u;
+        fw = (fw >> 2) | ((KT)c << (2 * (k - 1)));
+        rc = ((rc << 2) | (KT)(c ^ 2u)) & mask;
         if (i + 1 < (uint32_t)k) continue;
         uint32_t idx = i + 1 - (uint32_t)k;
         bool begin_ignored = (idx == 0) && !inc_begin;
         bool end_ignored = (idx == last) && !inc_end;
         uint32_t isf = fw < rc ? 1u : 0u;
-        uint64_t key = isf ? fw : rc;
+        const KT key = isf ? fw : rc;
         int64_t s = tinsert(t, key, status);
         if (s < 0) continue;
         uint32_t fbits = ((uint32_t)begin_ignored << (isf ^ 1u)) | ((uint32_t)end_ignored << isf);
-        if (fbits)
-            atomicOr(&t.vals[s], (fbits << 30) | 0u);
+        if (fbits) atomicOr(&t.vals[s], fbits << 30);
         atomicAdd(&t.vals[s], 1u);
     }
 }
 
 // Per-slot work of the extension phase: k-mer dump, then path starts in both orientations.
-__device__ __forceinline__ void extend_slot(const Graph &g, uint32_t s, const MergeOut &o, int keep_kmers,
+template <typename KT>
+__device__ __forceinline__ void extend_slot(const Graph<KT> &g, uint32_t s, const MergeOut &o, int keep_kmers,
                                             uint32_t min_mult) {
-    uint64_t key = g.t.keys[s];
-    if (key == kEmptyKey) return;
+    const KT key = g.t.keys[s];
+    if (key == KeyOps<KT>::empty()) return;
     uint32_t mult = val_mult(g.t.vals[s]);
     if (mult < min_mult) return;
     if (keep_kmers) {
         unsigned long long i = atomicAdd(&o.counters[2], 1ull);
         if (i < o.kmer_cap) {
-            o.kmer_keys[i] = key;
+            KeyOps<KT>::store(o.kmer_keys, i, key);
             o.kmer_mult[i] = mult;
         } else {
             atomicOr(o.status, kStatusKmerOverflow);
         }
     }
     for (int orient = 0; orient < 2; orient++) {
-        uint64_t v = orient ? rc_packed(key, g.k) : key;
+        const KT v = orient ? g.rc(key) : key;
         if (!g.is_start(v, s)) continue;
-        uint64_t e;
+        KT e;
         int64_t se;
-        uint32_t steps = walk_to_end(g, v, s, e, se, o.status);
+        uint32_t steps = walk_to_end(g, v, (int64_t)s, e, se, o.status);
         bool owner = ((int64_t)s < se) || ((int64_t)s == se && orient == 0);
         if (!owner) continue;
         uint8_t flags = (uint8_t)((g.left_boundary(v, s) ? 1u : 0u) | (g.right_boundary(e, se) ? 2u : 0u));
-        emit_walk(g, v, s, steps, flags, o);
+        emit_walk(g, v, (int64_t)s, steps, flags, o);
     }
 }
 
 // Cycle phase: surviving k-mers not covered by any path lie on cycles; the cycle is
 // emitted once, from its smallest slot.
-__device__ __forceinline__ void cycle_slot(const Graph &g, uint32_t s, const MergeOut &o, uint32_t min_mult) {
-    uint64_t key = g.t.keys[s];
-    if (key == kEmptyKey || g.t.vis[s]) return;
+template <typename KT>
+__device__ __forceinline__ void cycle_slot(const Graph<KT> &g, uint32_t s, const MergeOut &o, uint32_t min_mult) {
+    const KT key = g.t.keys[s];
+    if (key == KeyOps<KT>::empty() || g.t.vis[s]) return;
     if (val_mult(g.t.vals[s]) < min_mult) return;
-    uint64_t cur = key;
+    KT cur = key;
     int64_t scur = s;
     uint32_t steps = 0;
     int64_t min_slot = s;
     bool closed = false;
     for (;;) {
-        uint64_t u;
+        KT u;
         int64_t su;
         if (!g.next(cur, scur, u, su)) break;
         if (su == (int64_t)s) {
@@ -283,7 +292,7 @@ __device__ __forceinline__ void cycle_slot(const Graph &g, uint32_t s, const Mer
     }
     if (min_slot != (int64_t)s) return;
     // a cycle of `steps` k-mers: k + steps - 1 bases, circular flag
-    emit_walk(g, key, s, steps - 1, (uint8_t)4u, o);
+    emit_walk(g, key, (int64_t)s, steps - 1, (uint8_t)4u, o);
 }
 
 // ---------------------------------------------------------------------------
@@ -367,8 +376,18 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
 // phase the table is dead and its bytes are reused by the list-ranking arrays (union).  M
 // units keep the table in the global pool and use the whole shared memory of one CTA for
 // ranking arrays, so they rank more survivors.
-constexpr int kSmallMaxSurv = 2048;  // S units: survivors handled by list ranking (else walk fallback)
-constexpr int kMedMaxSurv = 6016;    // M units
+// Per key type: S-unit table slots, survivors ranked by S and M units (else walk fallback).
+// u128 keys halve the S table so two CTAs still fit on one SM.
+template <typename KT>
+struct Tier;
+template <>
+struct Tier<uint64_t> {
+    static constexpr int kSlots = kSmallSlots, kSmallSurv = 2048, kMedSurv = 6016;
+};
+template <>
+struct Tier<u128> {
+    static constexpr int kSlots = kSmallSlots / 2, kSmallSurv = 1024, kMedSurv = 4096;
+};
 constexpr uint16_t kNone16 = 0xffff;
 
 template <int N>
@@ -379,15 +398,19 @@ struct RankView {
     uint16_t uidx[2 * N];     // local unitig index of owner starts
     uint8_t haspred[2 * N];
 };
+template <typename KT>
 struct SmallTableView {
-    uint64_t keys[kSmallSlots];  // 32 KB
-    uint32_t vals[kSmallSlots];  // 16 KB: count|flags<<30, then alive<<31|flags<<28|dense index
+    KT keys[Tier<KT>::kSlots];
+    uint32_t vals[Tier<KT>::kSlots];  // count|flags<<30, then alive<<31|flags<<28|dense index
 };
-static_assert(sizeof(RankView<kSmallMaxSurv>) <= sizeof(SmallTableView), "rank view must fit in the table bytes");
+static_assert(sizeof(RankView<Tier<uint64_t>::kSmallSurv>) <= sizeof(SmallTableView<uint64_t>),
+              "rank view must fit in the table bytes");
+static_assert(sizeof(RankView<Tier<u128>::kSmallSurv>) <= sizeof(SmallTableView<u128>),
+              "rank view must fit in the table bytes");
 
-template <int N, int NT>
+template <typename KT, int N, int NT>
 struct UnitSmemCommon {
-    uint64_t sk[N];        // survivor canonical k-mers (dense order)
+    KT sk[N];              // survivor canonical k-mers (dense order)
     uint16_t succ[2 * N];  // traversable successor of each oriented node
     uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
     SkRec rec[NT];         // record batch
@@ -399,16 +422,18 @@ struct UnitSmemCommon {
 };
 constexpr int kSmallThreads = 256;
 constexpr int kMedThreads = 512;
-struct SmallSmem : UnitSmemCommon<kSmallMaxSurv, kSmallThreads> {
+template <typename KT>
+struct SmallSmem : UnitSmemCommon<KT, Tier<KT>::kSmallSurv, kSmallThreads> {
     union {
-        SmallTableView t;
-        RankView<kSmallMaxSurv> r;
+        SmallTableView<KT> t;
+        RankView<Tier<KT>::kSmallSurv> r;
     } u;
-    uint8_t vis[kSmallSlots];
+    uint8_t vis[Tier<KT>::kSlots];
 };
-struct MedSmem : UnitSmemCommon<kMedMaxSurv, kMedThreads> {
+template <typename KT>
+struct MedSmem : UnitSmemCommon<KT, Tier<KT>::kMedSurv, kMedThreads> {
     union {
-        RankView<kMedMaxSurv> r;
+        RankView<Tier<KT>::kMedSurv> r;
     } u;
 };
 
@@ -441,25 +466,17 @@ __device__ __forceinline__ uint32_t block_scan_u32(uint32_t v, uint32_t *warp_tm
     return r;
 }
 
-// k-mer of `k` bases starting at base position `p` of the packed text (seq-hash layout)
-__device__ __forceinline__ uint64_t load_kmer(const uint64_t *__restrict__ packed, uint64_t p, int k) {
-    const uint64_t w = p >> 5;
-    const uint32_t sh = (uint32_t)(p & 31) * 2u;
-    uint64_t v = packed[w] >> sh;
-    if (sh + 2u * (uint32_t)k > 64u) v |= packed[w + 1] << (64u - sh);
-    return v & kmer_mask(k);
-}
-
 __device__ __forceinline__ bool val_alive(uint32_t v) { return (v >> 31) != 0; }
 
 // number of alive successors of oriented v; *only / *s_only receive the last one found
-__device__ __forceinline__ int alive_succ(const Table &t, uint64_t v, int k, uint64_t &only, int64_t &s_only) {
+template <typename KT>
+__device__ __forceinline__ int alive_succ(const Table<KT> &t, KT v, int k, KT &only, int64_t &s_only) {
     int d = 0;
-    const uint64_t bse = v >> 2;
+    const KT bse = v >> 2;
 #pragma unroll
     for (uint32_t b = 0; b < 4; b++) {
-        const uint64_t w = bse | ((uint64_t)b << (2 * (k - 1)));
-        const uint64_t rw = rc_packed(w, k);
+        const KT w = bse | ((KT)b << (2 * (k - 1)));
+        const KT rw = KeyOps<KT>::rc(w, k);
         const int64_t sw = tfind(t, w < rw ? w : rw);
         if (sw >= 0 && val_alive(t.vals[sw])) {
             d++;
@@ -470,20 +487,22 @@ __device__ __forceinline__ int alive_succ(const Table &t, uint64_t v, int k, uin
     return d;
 }
 
-__device__ __forceinline__ uint64_t oriented(const uint64_t *sk, uint32_t u, int k) {
-    const uint64_t x = sk[u >> 1];
-    return (u & 1) ? rc_packed(x, k) : x;
+template <typename KT>
+__device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
+    const KT x = sk[u >> 1];
+    return (u & 1) ? KeyOps<KT>::rc(x, k) : x;
 }
 
 // One merge unit per CTA, persistent over a device work queue.  kGlobalTable = false: S units,
 // hash table in shared memory; true: M units, hash table in the global pool (L2-resident).
 // Both use the shared-memory list-ranking arrays for the extension.
-template <bool kGlobalTable, int NT>
+template <typename KT, bool kGlobalTable, int NT>
 __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
     merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
-                      uint64_t *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeOut o) {
-    using Smem = typename std::conditional<kGlobalTable, MedSmem, SmallSmem>::type;
-    constexpr int kMaxSurv = kGlobalTable ? kMedMaxSurv : kSmallMaxSurv;
+                      KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeOut o) {
+    using Smem = typename std::conditional<kGlobalTable, MedSmem<KT>, SmallSmem<KT>>::type;
+    using K = KeyOps<KT>;
+    constexpr int kMaxSurv = kGlobalTable ? Tier<KT>::kMedSurv : Tier<KT>::kSmallSurv;
     extern __shared__ __align__(16) uint8_t smem_raw[];
     Smem &S = *reinterpret_cast<Smem *>(smem_raw);
     const uint64_t n_units = counters_ro[kGlobalTable ? kCntMedium : kCntSmall];
@@ -497,18 +516,18 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
         if (ui >= n_units) break;
         const MergeUnit U = units[ui];
         uint32_t cap;
-        Table t;
+        Table<KT> t;
         if constexpr (kGlobalTable) {
             cap = U.table_cap;
-            t = Table{pool_keys + U.table_off, pool_vals + U.table_off, pool_vis + U.table_off, cap};
+            t = Table<KT>{pool_keys + U.table_off, pool_vals + U.table_off, pool_vis + U.table_off, cap};
         } else {
             cap = 64;
             while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
-            if (cap > kSmallSlots) cap = kSmallSlots;
-            t = Table{S.u.t.keys, S.u.t.vals, S.vis, cap};
+            if (cap > (uint32_t)Tier<KT>::kSlots) cap = Tier<KT>::kSlots;
+            t = Table<KT>{S.u.t.keys, S.u.t.vals, S.vis, cap};
         }
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
-            t.keys[i] = kEmptyKey;
+            t.keys[i] = K::empty();
             t.vals[i] = 0;
             t.vis[i] = 0;
         }
@@ -545,8 +564,8 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
                 // text-orientation included flags (begin <- stored end when reverse-complemented)
                 const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
                 const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
-                const uint64_t fw = load_kmer(a.packed, rec_start(rr) + off, k);
-                const uint64_t rc = rc_packed(fw, k);
+                const KT fw = K::load(a.packed, rec_start(rr) + off, k);
+                const KT rc = K::rc(fw, k);
                 const uint32_t isf = fw < rc ? 1u : 0u;
                 const int64_t sl = tinsert(t, isf ? fw : rc, o.status);
                 if (sl < 0) continue;
@@ -568,14 +587,14 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
         for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
             const uint32_t sl = b0 + lane;
             bool alive = false;
-            if (sl < seg_hi) alive = t.keys[sl] != kEmptyKey && val_mult(t.vals[sl]) >= min_mult;
+            if (sl < seg_hi) alive = t.keys[sl] != K::empty() && val_mult(t.vals[sl]) >= min_mult;
             warp_surv += __popc(__ballot_sync(0xffffffffu, alive));
         }
         uint32_t n_surv;
         const uint32_t warp_base = block_scan_u32<NT>(lane == 0 ? warp_surv : 0u, S.warp_tmp, n_surv);
         if (n_surv > (uint32_t)kMaxSurv) {
             // walk fallback for a unit with more survivors than the ranking arrays hold
-            Graph g{t, k, min_mult};
+            Graph<KT> g{t, k, min_mult};
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) extend_slot(g, sl, o, a.keep_kmers, min_mult);
             __syncthreads();
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
@@ -587,12 +606,12 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
             for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
                 const uint32_t sl = b0 + lane;
                 bool alive = false;
-                uint64_t key = kEmptyKey;
+                KT key = K::empty();
                 uint32_t v = 0;
                 if (sl < seg_hi) {
                     key = t.keys[sl];
                     v = t.vals[sl];
-                    alive = key != kEmptyKey && val_mult(v) >= min_mult;
+                    alive = key != K::empty() && val_mult(v) >= min_mult;
                 }
                 const unsigned bm = __ballot_sync(0xffffffffu, alive);
                 const uint32_t idx = base + __popc(bm & ((1u << lane) - 1u));
@@ -601,7 +620,7 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
                     if (a.keep_kmers) {
                         const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
                         if (di < o.kmer_cap) {
-                            o.kmer_keys[di] = key;
+                            K::store(o.kmer_keys, di, key);
                             o.kmer_mult[di] = val_mult(v);
                         } else {
                             atomicOr(o.status, kStatusKmerOverflow);
@@ -620,8 +639,8 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
         // ---- traversable successor of every oriented node (the extension rules of
         //      try_extend_function, hashmap.rs:162-297): 8 probes per node ----
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const uint64_t x = S.sk[u >> 1];
-            const uint64_t v = (u & 1) ? rc_packed(x, k) : x;
+            const KT x = S.sk[u >> 1];
+            const KT v = (u & 1) ? K::rc(x, k) : x;
             const int64_t sv = tfind(t, x);
             const uint32_t fv = (t.vals[sv] >> 28) & 3u;
             // MapEntry flags in canonical orientation: 1 = left side ignored, 2 = right side ignored
@@ -629,11 +648,11 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
             const bool rb = (u & 1) ? fv == 1u : fv == 2u;
             uint16_t nx = kNone16;
             if (!rb) {
-                uint64_t only = 0;
+                KT only = 0;
                 int64_t s_only = -1;
                 if (alive_succ(t, v, k, only, s_only) == 1 && s_only != sv) {
-                    const uint64_t ru = rc_packed(only, k);
-                    uint64_t dummy;
+                    const KT ru = K::rc(only, k);
+                    KT dummy;
                     int64_t sd;
                     const int d2 = alive_succ(t, ru, k, dummy, sd);  // predecessors of the successor
                     const uint32_t vu = t.vals[s_only];
@@ -714,7 +733,7 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
             if (!owner || !ok) continue;
             const uint32_t dist = R.rank[mu];           // distance from the start
             const unsigned long long off = gbase + R.offs[s0];
-            const uint64_t v = oriented(S.sk, u, k);
+            const KT v = oriented(S.sk, u, k);
             if (dist == 0) {
                 for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
                 const unsigned long long ix = gidx + R.uidx[u];
@@ -756,7 +775,7 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
                 atomicOr(o.status, kStatusOutOverflow);
                 continue;
             }
-            uint64_t v = oriented(S.sk, u, k);
+            KT v = oriented(S.sk, u, k);
             for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
             cur = S.succ[u];
             for (uint32_t i = 1; i < n; i++) {
@@ -774,50 +793,54 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
 // ---------------------------------------------------------------------------
 // large units: global-memory tables, grid-wide phases
 // ---------------------------------------------------------------------------
-__global__ void init_tables_kernel(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t n) {
+template <typename KT>
+__global__ void init_tables_kernel(KT *keys, uint32_t *vals, uint8_t *vis, uint64_t n) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        keys[i] = kEmptyKey;
+        keys[i] = KeyOps<KT>::empty();
         vals[i] = 0;
         vis[i] = 0;
     }
 }
 
+template <typename KT>
 __global__ void init_unit_tables_kernel(const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ n_units_dev,
-                                        uint64_t *keys, uint32_t *vals, uint8_t *vis) {
+                                        KT *keys, uint32_t *vals, uint8_t *vis) {
     const uint64_t n_units = *n_units_dev;
     const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u = 0; u < n_units; u++) {
         const MergeUnit U = units[u];
         for (uint64_t i = gt; i < U.table_cap; i += gs) {
-            keys[U.table_off + i] = kEmptyKey;
+            keys[U.table_off + i] = KeyOps<KT>::empty();
             vals[U.table_off + i] = 0;
             vis[U.table_off + i] = 0;
         }
     }
 }
 
+template <typename KT>
 __global__ void __launch_bounds__(256) large_insert_kernel(MergeArgs a, const MergeUnit *__restrict__ units,
                                                            const unsigned long long *__restrict__ n_units_dev,
-                                                           uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o) {
+                                                           KT *keys, uint32_t *vals, uint8_t *vis, MergeOut o) {
     const uint64_t n_units = *n_units_dev;
     const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u = 0; u < n_units; u++) {
         const MergeUnit U = units[u];
-        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
+        Table<KT> t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
         for (uint64_t r = U.rec_begin + gt; r < U.rec_end; r += gs) insert_record(t, a.packed, a.recs[r], a.k, o.status);
     }
 }
 
+template <typename KT>
 __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const MergeUnit *__restrict__ units,
                                                            const unsigned long long *__restrict__ n_units_dev,
-                                                           uint64_t *keys, uint32_t *vals, uint8_t *vis, MergeOut o,
+                                                           KT *keys, uint32_t *vals, uint8_t *vis, MergeOut o,
                                                            int phase) {
     const uint64_t n_units = *n_units_dev;
     const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u = 0; u < n_units; u++) {
         const MergeUnit U = units[u];
-        Table t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
-        Graph g{t, a.k, (uint32_t)a.min_mult};
+        Table<KT> t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
+        Graph<KT> g{t, a.k, (uint32_t)a.min_mult};
         for (uint64_t s = gt; s < U.table_cap; s += gs) {
             if (phase == 0)
                 extend_slot(g, (uint32_t)s, o, a.keep_kmers, (uint32_t)a.min_mult);
@@ -840,50 +863,92 @@ int launch_classify_units(const unsigned long long *bin_off, const unsigned long
     return 1;
 }
 
-int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, uint64_t *keys,
-                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+template <typename KT>
+static void merge_medium_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, KT *keys,
+                           uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
     static bool configured = false;
-    const int smem = (int)sizeof(MedSmem);
+    const int smem = (int)sizeof(MedSmem<KT>);
     if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<true, kMedThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(merge_unit_kernel<KT, true, kMedThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
         configured = true;
     }
-    merge_unit_kernel<true, kMedThreads><<<sms, kMedThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
+    merge_unit_kernel<KT, true, kMedThreads><<<sms, kMedThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
+}
+
+int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
+                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+    if (a.wide)
+        merge_medium_t<u128>(a, units, counters, static_cast<u128 *>(keys), vals, vis, o, sms, s);
+    else
+        merge_medium_t<uint64_t>(a, units, counters, static_cast<uint64_t *>(keys), vals, vis, o, sms, s);
     return 1;
+}
+
+template <typename KT>
+static void merge_small_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
+                          const MergeOut &o, int sms, cudaStream_t s) {
+    static bool configured = false;
+    const int smem = (int)sizeof(SmallSmem<KT>);
+    if (!configured) {
+        cudaFuncSetAttribute(merge_unit_kernel<KT, false, kSmallThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        configured = true;
+    }
+    merge_unit_kernel<KT, false, kSmallThreads>
+        <<<sms * 2, kSmallThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
 }
 
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s) {
-    static bool configured = false;
-    const int smem = (int)sizeof(SmallSmem);
-    if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<false, kSmallThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-        configured = true;
-    }
-    merge_unit_kernel<false, kSmallThreads><<<sms * 2, kSmallThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
+    if (a.wide)
+        merge_small_t<u128>(a, units, counters, o, sms, s);
+    else
+        merge_small_t<uint64_t>(a, units, counters, o, sms, s);
     return 1;
 }
 
-int launch_init_tables(uint64_t *keys, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s) {
+uint64_t merge_small_limit(int wide) {
+    // instances of an S unit, so that its table (Tier slots) stays at load <= 0.8
+    static_assert(3200 * 5 <= Tier<uint64_t>::kSlots * 4 && 1600 * 5 <= Tier<u128>::kSlots * 4, "S table load");
+    return wide ? 1600 : 3200;
+}
+
+int launch_init_tables(void *keys, int wide, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s) {
     if (slots == 0) return 0;
-    init_tables_kernel<<<sms * 4, 256, 0, s>>>(keys, vals, vis, slots);
+    if (wide)
+        init_tables_kernel<u128><<<sms * 4, 256, 0, s>>>(static_cast<u128 *>(keys), vals, vis, slots);
+    else
+        init_tables_kernel<uint64_t><<<sms * 4, 256, 0, s>>>(static_cast<uint64_t *>(keys), vals, vis, slots);
     return 1;
 }
 
-int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, uint64_t *keys, uint32_t *vals,
-                            uint8_t *vis, int sms, cudaStream_t s) {
-    init_unit_tables_kernel<<<sms * 4, 256, 0, s>>>(units, n_units_dev, keys, vals, vis);
+int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, void *keys, int wide,
+                            uint32_t *vals, uint8_t *vis, int sms, cudaStream_t s) {
+    if (wide)
+        init_unit_tables_kernel<u128><<<sms * 4, 256, 0, s>>>(units, n_units_dev, static_cast<u128 *>(keys), vals, vis);
+    else
+        init_unit_tables_kernel<uint64_t>
+            <<<sms * 4, 256, 0, s>>>(units, n_units_dev, static_cast<uint64_t *>(keys), vals, vis);
     return 1;
+}
+
+template <typename KT>
+static void merge_large_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev, KT *keys,
+                          uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+    large_insert_kernel<KT><<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o);
+    large_extend_kernel<KT><<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 0);
+    large_extend_kernel<KT><<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 1);
 }
 
 int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
-                       uint64_t n_units_host_hint, uint64_t *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
+                       uint64_t n_units_host_hint, void *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
                        int sms, cudaStream_t s) {
     (void)n_units_host_hint;
-    large_insert_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o);
-    large_extend_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 0);
-    large_extend_kernel<<<sms * 4, 256, 0, s>>>(a, units, n_units_dev, keys, vals, vis, o, 1);
+    if (a.wide)
+        merge_large_t<u128>(a, units, n_units_dev, static_cast<u128 *>(keys), vals, vis, o, sms, s);
+    else
+        merge_large_t<uint64_t>(a, units, n_units_dev, static_cast<uint64_t *>(keys), vals, vis, o, sms, s);
     return 3;
 }
 

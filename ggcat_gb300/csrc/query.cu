@@ -8,6 +8,8 @@
 // query k-mer is one probe and no bucketing pass is needed.  Every query k-mer occurrence
 // that does not span a non-ACGT base is looked up (duplicates included), and the matches of
 // each query are summed (per colour subset when the graph is coloured).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -15,28 +17,16 @@ namespace ggcat {
 
 __device__ __forceinline__ uint32_t qslot(uint64_t key, uint64_t mask) { return (uint32_t)(mix64(key) & mask); }
 
-// Insert every canonical k-mer of the graph text (pieces separated by non-ACGT bytes) with the
-// colour subset of its sequence (subset_of_seq[seq], seq from a binary search of seq_off) or 0.
+// Insert every canonical k-mer of the graph text (pieces separated by non-ACGT bytes).
 __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
-                                                           uint64_t chunk, const uint64_t *__restrict__ seq_off,
-                                                           const uint32_t *__restrict__ seq_subset, uint64_t n_seq,
-                                                           uint64_t *keys, uint32_t *vals, uint64_t mask,
-                                                           unsigned *status) {
+                                                           uint64_t chunk, uint64_t *keys, uint32_t *vals,
+                                                           uint64_t mask, unsigned *status) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t x0 = tid * chunk;  // k-mer start positions [x0, x1)
     if (x0 >= n) return;
     const uint64_t x1 = min(x0 + chunk, n);
     const uint64_t kmask = kmer_mask(k);
     uint64_t fw = 0, rc = 0, run = 0;
-    uint64_t seq = 0;
-    if (seq_subset) {  // sequence containing x0
-        uint64_t lo = 0, hi = n_seq - 1;
-        while (lo < hi) {
-            const uint64_t mid = (lo + hi + 1) >> 1;
-            if (seq_off[mid] <= x0) lo = mid; else hi = mid - 1;
-        }
-        seq = lo;
-    }
     const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
     for (uint64_t p = x0; p < pend; p++) {
         const uint32_t c = text[p];
@@ -49,9 +39,6 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
         fw = (fw >> 2) | (b << (2 * (k - 1)));
         rc = ((rc << 2) | (b ^ 2u)) & kmask;
         if (++run < (uint64_t)k) continue;
-        const uint64_t start = p + 1 - (uint64_t)k;
-        if (seq_subset)
-            while (seq + 1 < n_seq && seq_off[seq + 1] <= start) seq++;
         const uint64_t key = fw < rc ? fw : rc;
         uint64_t s = qslot(key, mask);
         for (uint64_t probe = 0; probe <= mask; probe++) {
@@ -61,7 +48,7 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
                 const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
                                                          (unsigned long long)kEmptyKey, (unsigned long long)key);
                 if (old == kEmptyKey) {
-                    vals[s] = seq_subset ? seq_subset[seq] : 0u;
+                    vals[s] = 0u;
                     break;
                 }
                 if (old == key) break;
@@ -72,17 +59,40 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
     }
 }
 
-// One work item = a run of k-mer positions of one query.  Matches are summed per query;
-// with a coloured graph, runs of equal subset ids are emitted as (query, subset, count).
+// Coloured index: the colour phase's k-mer table (key -> dense id) re-keyed into the query
+// table with value = colour subset id.
+__global__ void index_from_colors_kernel(const uint64_t *__restrict__ ckeys, const uint32_t *__restrict__ cvals,
+                                         uint64_t ccap, const uint32_t *__restrict__ id_subset, uint64_t *keys,
+                                         uint32_t *vals, uint64_t mask, unsigned *status) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ccap; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = ckeys[i];
+        if (key == kEmptyKey) continue;
+        uint64_t s = qslot(key, mask);
+        for (uint64_t probe = 0;; probe++) {
+            if (probe > mask) {
+                atomicOr(status, kStatusTableFull);
+                break;
+            }
+            if (keys[s] == kEmptyKey) {
+                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
+                                                         (unsigned long long)kEmptyKey, (unsigned long long)key);
+                if (old == kEmptyKey) {
+                    vals[s] = id_subset[cvals[i]];
+                    break;
+                }
+            }
+            s = (s + 1) & mask;
+        }
+    }
+}
+
+// One work item = a run of k-mer positions of one query; matches are summed per query.
 __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ text, int k,
                                                    const uint32_t *__restrict__ item_query,
                                                    const uint64_t *__restrict__ item_start,
                                                    const uint32_t *__restrict__ item_len, uint64_t n_items,
-                                                   const uint64_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                                                   uint64_t mask, unsigned long long *__restrict__ matched,
-                                                   int colored, uint4 *__restrict__ runs, unsigned long long runs_cap,
-                                                   unsigned long long *__restrict__ runs_cursor,
-                                                   unsigned *__restrict__ status) {
+                                                   const uint64_t *__restrict__ keys, uint64_t mask,
+                                                   unsigned long long *__restrict__ matched) {
     const uint64_t it = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= n_items) return;
     const uint32_t q = item_query[it];
@@ -90,16 +100,6 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
     const uint64_t x1 = x0 + item_len[it];  // k-mer start positions
     const uint64_t kmask = kmer_mask(k);
     uint64_t fw = 0, rc = 0, run = 0, hits = 0;
-    uint32_t cur_subset = 0xffffffffu, cur_count = 0;
-    auto flush_run = [&]() {
-        if (cur_count == 0) return;
-        const unsigned long long i = atomicAdd(runs_cursor, 1ull);
-        if (i < runs_cap)
-            runs[i] = make_uint4(q, cur_subset, cur_count, 0u);
-        else
-            atomicOr(status, kStatusOutOverflow);
-        cur_count = 0;
-    };
     for (uint64_t p = x0; p < x1 + (uint64_t)k - 1; p++) {
         const uint32_t c = text[p];
         const uint32_t u = c & 0xDFu;
@@ -117,42 +117,138 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
             const uint64_t kk = keys[s];
             if (kk == key) {
                 hits++;
-                if (colored) {
-                    const uint32_t sub = vals[s];
-                    if (sub != cur_subset) {
-                        flush_run();
-                        cur_subset = sub;
-                    }
-                    cur_count++;
-                }
                 break;
             }
             if (kk == kEmptyKey) break;
             s = (s + 1) & mask;
         }
     }
-    if (colored) flush_run();
     if (hits) atomicAdd(&matched[q], (unsigned long long)hits);
 }
 
-int launch_index_insert(const uint8_t *text, uint64_t n, int k, const uint64_t *seq_off, const uint32_t *seq_subset,
-                        uint64_t n_seq, uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, cudaStream_t s) {
+// Coloured lookup, one CTA per query from a device queue: runs of equal subset ids are
+// expanded into per-colour counts in shared memory (colored_query_output.rs:264-309 sums
+// the per-subset counters of a query per colour).
+__global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restrict__ text, int k,
+                                                         const uint64_t *__restrict__ q_off,
+                                                         const uint64_t *__restrict__ q_len, uint64_t nq,
+                                                         const uint64_t *__restrict__ keys,
+                                                         const uint32_t *__restrict__ vals, uint64_t mask,
+                                                         const uint32_t *__restrict__ sub_arena, int words,
+                                                         uint32_t n_colors, unsigned long long *__restrict__ matched,
+                                                         unsigned long long *__restrict__ counts,
+                                                         unsigned long long *__restrict__ queue) {
+    extern __shared__ uint32_t cnt[];  // n_colors counters
+    __shared__ unsigned long long q_cur;
+    __shared__ unsigned long long hits_sh;
+    const uint64_t kmask = kmer_mask(k);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            q_cur = atomicAdd(queue, 1ull);
+            hits_sh = 0;
+        }
+        for (uint32_t c = threadIdx.x; c < n_colors; c += blockDim.x) cnt[c] = 0;
+        __syncthreads();
+        const uint64_t q = q_cur;
+        if (q >= nq) break;
+        const uint64_t L = q_len[q];
+        const uint64_t nk = L >= (uint64_t)k ? L - (uint64_t)k + 1 : 0;
+        const uint64_t per = (nk + blockDim.x - 1) / blockDim.x;
+        const uint64_t a = min(nk, (uint64_t)threadIdx.x * per), b = min(nk, a + per);
+        uint64_t fw = 0, rc = 0, run = 0, hits = 0;
+        uint32_t cur_sub = 0xffffffffu, cur_cnt = 0;
+        auto flush = [&]() {
+            if (!cur_cnt) return;
+            const uint32_t *bm = sub_arena + (uint64_t)cur_sub * words;
+            for (int w = 0; w < words; w++) {
+                uint32_t bits = bm[w];
+                while (bits) {
+                    const int c = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    atomicAdd(&cnt[w * 32 + c], cur_cnt);
+                }
+            }
+            cur_cnt = 0;
+        };
+        if (a < b) {
+            const uint64_t base = q_off[q];
+            for (uint64_t p = base + a; p < base + b + (uint64_t)k - 1; p++) {
+                const uint32_t c = text[p];
+                const uint32_t u = c & 0xDFu;
+                if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                    run = 0;
+                    continue;
+                }
+                const uint64_t bb = (c >> 1) & 3u;
+                fw = (fw >> 2) | (bb << (2 * (k - 1)));
+                rc = ((rc << 2) | (bb ^ 2u)) & kmask;
+                if (++run < (uint64_t)k) continue;
+                const uint64_t key = fw < rc ? fw : rc;
+                uint64_t s = qslot(key, mask);
+                for (uint64_t probe = 0; probe <= mask; probe++) {
+                    const uint64_t kk = keys[s];
+                    if (kk == key) {
+                        hits++;
+                        const uint32_t sub = vals[s];
+                        if (sub != cur_sub) {
+                            flush();
+                            cur_sub = sub;
+                        }
+                        cur_cnt++;
+                        break;
+                    }
+                    if (kk == kEmptyKey) break;
+                    s = (s + 1) & mask;
+                }
+            }
+            flush();
+        }
+        if (hits) atomicAdd(&hits_sh, hits);
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < n_colors; c += blockDim.x) counts[q * n_colors + c] = cnt[c];
+        if (threadIdx.x == 0) matched[q] = hits_sh;
+    }
+}
+
+int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,
+                        unsigned *status, cudaStream_t s) {
     const uint64_t chunk = 256;
     const uint64_t threads = (n + chunk - 1) / chunk;
     if (threads == 0) return 0;
-    index_insert_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n, k, chunk, seq_off, seq_subset, n_seq,
-                                                                          keys, vals, mask, status);
+    index_insert_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n, k, chunk, keys, vals, mask, status);
+    return 1;
+}
+
+int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint64_t ccap, const uint32_t *id_subset,
+                             uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s) {
+    index_from_colors_kernel<<<sms * 8, 256, 0, s>>>(ckeys, cvals, ccap, id_subset, keys, vals, mask, status);
     return 1;
 }
 
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
-                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, const uint32_t *vals, uint64_t mask,
-                 unsigned long long *matched, int colored, uint4 *runs, unsigned long long runs_cap,
-                 unsigned long long *runs_cursor, unsigned *status, cudaStream_t s) {
+                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, uint64_t mask,
+                 unsigned long long *matched, cudaStream_t s) {
     if (n_items == 0) return 0;
     query_kernel<<<(unsigned)((n_items + 255) / 256), 256, 0, s>>>(text, k, item_query, item_start, item_len, n_items,
-                                                                  keys, vals, mask, matched, colored, runs, runs_cap,
-                                                                  runs_cursor, status);
+                                                                  keys, mask, matched);
+    return 1;
+}
+
+int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
+                       const uint64_t *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
+                       uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
+                       unsigned long long *queue, int sms, cudaStream_t s) {
+    if (nq == 0) return 0;
+    const size_t smem = (size_t)n_colors * sizeof(uint32_t);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(query_color_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        configured = true;
+    }
+    uint64_t grid = std::min<uint64_t>(nq, (uint64_t)sms * 8);
+    query_color_kernel<<<(unsigned)grid, 256, smem, s>>>(text, k, q_off, q_len, nq, keys, vals, mask, sub_arena, words,
+                                                        n_colors, matched, counts, queue);
     return 1;
 }
 

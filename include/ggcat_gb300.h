@@ -158,19 +158,35 @@ int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_file
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);
 
+/* ---- colour subsets ----
+ * Replaces the per-k-mer colour sets and subset dedup of MultipleColorsManager
+ * (crates/colors/src/managers/multiple.rs:99-228) and ColorsMemMapWriter::get_id
+ * (crates/colors/src/colors_memmap_writer.rs:43-61).  Needs the last merge run with
+ * keep_kmers = 1 and the input text of the last bucketize still on the device
+ * (ggcat_gpu_build_text keeps its copy; with ggcat_gpu_bucketize the caller's d_text must stay
+ * valid).  Sequence i starts at text byte h_seq_off[i] (non-decreasing) and has colour
+ * h_seq_color[i] < n_colors <= 65536 (the input file index, MinBkSingleColor).  A k-mer's
+ * colour set is the set of colours of all its occurrences; equal sets share one subset id. */
+int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, const uint32_t *h_seq_color, uint64_t n_seq,
+                     uint32_t n_colors, void *stream);
+/* Subset id of every k-mer of ggcat_gpu_kmers_copy (same order). */
+int ggcat_gpu_kmer_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_subset, uint64_t cap, uint64_t *n);
+/* Subsets as colour bitmaps: subset i is words [i*w, (i+1)*w), bit c of word c/32 = colour c. */
+int ggcat_gpu_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_bitmaps, uint64_t cap_words, uint64_t *n_subsets,
+                           uint32_t *words_per_subset);
+
 /* ---- graph query lookup (querier::run_query, crates/querier/src/lib.rs:54-199) ----
  * The graph's canonical k-mers stay resident in a device hash table; batches of queries are
  * looked up asynchronously in up to GGCAT_GPU_QUERY_SLOTS in-flight slots (each with its own
  * stream and buffers), which is what a continuous-batching serving loop needs. */
 #define GGCAT_GPU_QUERY_SLOTS 4
 
-/* Builds the resident index from the graph's unitigs in the text layout (device memory).
- * Colour subset ids, if any, are given per sequence: h_seq_subset[i] for the sequence that
- * starts at byte h_seq_off[i] (NULL for an uncoloured graph).  Replaces the graph side of the
- * querier's bucketing and per-bucket maps (querier_minimizer_bucketing.rs:233-288,
+/* Uncoloured index from the graph's unitigs in the text layout (device memory); replaces the
+ * graph side of the querier's bucketing and per-bucket maps (querier_minimizer_bucketing.rs:233-288,
  * parallel_kmers_query.rs:362-403).  k <= 32. */
-int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k,
-                          const uint64_t *h_seq_off, const uint32_t *h_seq_subset, uint64_t n_seq, void *stream);
+int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k, void *stream);
+/* Coloured index from the last ggcat_gpu_colors result (the build's k-mers and subsets). */
+int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
 
 /* Submits a batch of queries (host text layout; query i = h_text[h_off[i], h_off[i]+h_len[i]))
  * to slot `slot` and returns without waiting.  The slot's H2D copy, lookup kernel and D2H
@@ -182,10 +198,20 @@ int ggcat_gpu_query_poll(ggcat_gpu_ctx *ctx, int slot);
 /* Waits for the slot's batch; h_matched[i] = number of k-mer occurrences of query i present
  * in the graph (parallel_kmers_query.rs:437-471 + counters_sorting.rs:106-273). */
 int ggcat_gpu_query_wait(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_matched, uint64_t cap, uint64_t *nq);
-/* Coloured index: the matches of the last batch of `slot` as runs (query, subset id, count);
- * summing count per (query, subset) gives the querier's per-subset counters. */
-int ggcat_gpu_query_subset_runs(ggcat_gpu_ctx *ctx, int slot, uint32_t *h_query, uint32_t *h_subset, uint32_t *h_count,
-                                uint64_t cap, uint64_t *n_runs);
+/* Coloured index: per query and colour, the number of query k-mer occurrences present in
+ * that colour (h_counts[q * n_colors + c]); colored_query_output.rs:264-309 prints these
+ * divided by the query's k-mer count. */
+int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64_t *h_counts, uint64_t cap, uint32_t *n_colors);
+
+/* ---- hash families (crates/hashes) ----
+ * Writes, for every window start i of d_text, the unextendable hash of the window as
+ * d_out[2i] (low 64 bits), d_out[2i+1] (high 64 bits); windows spanning a non-ACGT byte give
+ * all-ones.  kind: 0 canonical seq-hash u64 (k <= 32), 1 forward seq-hash u64, 2 canonical
+ * seq-hash u128 (k <= 64), 3 forward seq-hash u128, 4 canonical Rabin-Karp u128 (k <= 127),
+ * 5 forward Rabin-Karp u128, 6 canonical nt-hash m-mer value (min(fw,rc) << 1 | unique
+ * flag, the minimizer ordering of cn_nthash.rs:96-99 and lib.rs:189-199; k = m <= 64). */
+int ggcat_gpu_kmer_hashes(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t len, int k, int kind, uint64_t *d_out,
+                          void *stream);
 
 /* ---- bucket-size histogram without device allocation ----
  * For callers that cannot allocate device memory (their memory belongs to another

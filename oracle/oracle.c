@@ -548,7 +548,7 @@ typedef struct {
     u128 packed;   /* canonical 2-bit packed k-mer (seq-hash layout) */
     uint64_t count;
     uint8_t flags, used, occupied;
-    uint32_t color_head; /* index into color pair list (unused here) */
+    uint32_t ordinal;    /* creation order; stable across kmap_grow (colour pairs refer to it) */
 } kentry;
 
 typedef struct {
@@ -754,7 +754,7 @@ typedef struct {
 } merge_job;
 
 typedef struct {
-    uint32_t entry_slot;
+    uint32_t entry_slot; /* kentry ordinal */
     uint32_t color;
 } color_pair;
 
@@ -800,7 +800,10 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
             int isf = orc_hash_is_forward(kind, hs[idx]);
             int created;
             kentry *e = kmap_insert(&m, orc_hash_unext(kind, hs[idx]), &created);
-            if (created) e->packed = pack_canonical(cb + idx, k, orc_hash_is_canonical(kind));
+            if (created) {
+                e->packed = pack_canonical(cb + idx, k, orc_hash_is_canonical(kind));
+                e->ordinal = (uint32_t)(m.n - 1);
+            }
             e->flags |= (uint8_t)(((unsigned)begin_ignored << (unsigned)!isf) | ((unsigned)end_ignored << (unsigned)isf));
             e->count += 1; /* every record has multiplicity 1 (no compaction) */
             if (p->colors) {
@@ -808,7 +811,7 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
                     cpcap = cpcap ? cpcap * 2 : 1024;
                     cpairs = xrealloc(cpairs, cpcap * sizeof(color_pair));
                 }
-                cpairs[ncp].entry_slot = (uint32_t)(e - m.e);
+                cpairs[ncp].entry_slot = e->ordinal;
                 cpairs[ncp].color = job->sh->seq_colors ? job->sh->seq_colors[s->seq_index] : 0;
                 ncp++;
             }
@@ -820,8 +823,8 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
     uint32_t *ucolors = NULL;
     if (p->colors) {
         qsort(cpairs, ncp, sizeof(color_pair), cmp_color_pair);
-        slot_col_off = xcalloc(m.cap, sizeof(uint32_t));
-        slot_col_n = xcalloc(m.cap, sizeof(uint32_t));
+        slot_col_off = xcalloc(m.n + 1, sizeof(uint32_t));
+        slot_col_n = xcalloc(m.n + 1, sizeof(uint32_t));
         ucolors = xmalloc((ncp + 1) * sizeof(uint32_t));
         size_t nu = 0;
         for (size_t i = 0; i < ncp; i++) {
@@ -838,8 +841,8 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
         if (!e->occupied || entry_mult(e) < (uint64_t)p->min_multiplicity) continue;
         kmer_out ko = {e->packed, entry_mult(e), 0, 0};
         if (p->colors) {
-            ko.color_off = kv_push_colors(&job->kmers, ucolors + slot_col_off[i], slot_col_n[i]);
-            ko.color_n = slot_col_n[i];
+            ko.color_off = kv_push_colors(&job->kmers, ucolors + slot_col_off[e->ordinal], slot_col_n[e->ordinal]);
+            ko.color_n = slot_col_n[e->ordinal];
         }
         kv_push(&job->kmers, ko);
     }

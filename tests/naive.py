@@ -33,6 +33,16 @@ def kmer_counts(seqs, k: int) -> dict:
     return cnt
 
 
+def kmer_colors(seqs, colors, k: int) -> dict:
+    """canonical k-mer -> sorted tuple of the colours of the sequences that contain it."""
+    out = {}
+    for s, c in zip(seqs, colors):
+        for p in pieces(s, k):
+            for i in range(len(p) - k + 1):
+                out.setdefault(canon(p[i : i + k]), set()).add(int(c))
+    return {x: tuple(sorted(v)) for x, v in out.items()}
+
+
 def maximal_unitigs(kmers: set, k: int):
     """Returns list of (sequence, circular) for the maximal unitigs of a canonical k-mer set."""
 

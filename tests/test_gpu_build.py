@@ -67,7 +67,8 @@ def test_bucketize_matches_oracle(ctx, kind, seed, bbits, minm):
 
 def _kmer_dict(keys, mult):
     d = {}
-    for kk, mm in zip(keys.tolist(), mult.tolist()):
+    keys = keys.tolist() if isinstance(keys, np.ndarray) else keys
+    for kk, mm in zip(keys, mult.tolist()):
         if kk in d:
             assert d[kk] == mm, "k-mer multiplicity differs between sub-buckets"
         d[kk] = mm
@@ -118,3 +119,32 @@ def test_device_pointer_bucketize(ctx):
     exp = oracle.bucketize(text, off, ln, _oracle_params(p))
     assert n == len(exp)
     assert (_sorted_sk(got) == _sorted_sk(exp)).all()
+
+
+# k > 32: 128-bit table keys (seq-hash u128, and Rabin-Karp u128 which selects the same
+# k-mer identities); the oracle follows the reference hash of each case.
+WIDE = [("reads", 11, 63, 12, oracle.H_CN_SEQ128, _native.GGCAT_HASH_SEQHASH, 2),
+        ("genomes", 12, 63, 12, oracle.H_CN_RK128, _native.GGCAT_HASH_RABIN_KARP128, 1),
+        ("genomes", 13, 33, 11, oracle.H_CN_SEQ128, _native.GGCAT_HASH_SEQHASH, 1),
+        ("lowcomplexity", 14, 45, 9, oracle.H_CN_SEQ128, _native.GGCAT_HASH_SEQHASH, 1)]
+
+
+@pytest.mark.parametrize("mode", [_native.GGCAT_MERGE_BATCHED, _native.GGCAT_MERGE_PER_BUCKET])
+@pytest.mark.parametrize("kind,seed,k,m,okind,hkind,minm", WIDE)
+def test_wide_k_matches_oracle(ctx, kind, seed, k, m, okind, hkind, minm, mode):
+    text, off, ln, _ = _workload(kind, seed)
+    p = make_params(k=k, m=m, bucket_bits=8, second_bits=2, min_multiplicity=minm, hash_kind=hkind,
+                    keep_kmers=True, merge_mode=mode)
+    ctx.build_text(text, p)
+    op = oracle.params(k=k, m=m, bucket_bits=8, second_bits=2, min_multiplicity=minm, hash_kind=okind, threads=8)
+    assert (_sorted_sk(ctx.superkmers()) == _sorted_sk(oracle.bucketize(text, off, ln, op))).all()
+    keys, mult = ctx.kmers()
+    assert keys.ndim == 2
+    got = _kmer_dict([int(a) | (int(b) << 64) for a, b in keys.tolist()], mult)
+    r = oracle.build_graph(text, off, ln, op)
+    lo, hi, emult = r.kmers()
+    assert got == {int(a) | (int(b) << 64): int(c) for a, b, c in zip(lo.tolist(), hi.tolist(), emult.tolist())}
+    ctx.link(k)
+    bases, uo, ul, uf = ctx.unitigs()
+    got_u = oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k)
+    assert got_u == r.unitigs()

@@ -1,0 +1,85 @@
+"""GPU colour-subset dedup against the oracle's MultipleColorsManager restatement: every
+surviving k-mer's decoded colour set, subset uniqueness, and per-colour query counts."""
+import numpy as np
+import pytest
+
+import oracle
+from ggcat_gb300 import _native, serve, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _colored_input(seed=21, n_genomes=12, L=60_000):
+    rng = np.random.default_rng(seed)
+    anc = synth.random_genome(L, rng)
+    gs = [synth.indels(synth.substitute(anc, float(rng.uniform(0.001, 0.03)), rng), 0.001, 20, rng)
+          for _ in range(n_genomes)]
+    # two sequences per colour for some colours (a colour is a file, not a sequence)
+    seqs, cols = [], []
+    for c, g in enumerate(gs):
+        if c % 3 == 0:
+            half = len(g) // 2
+            seqs += [g[:half], g[half:]]
+            cols += [c, c]
+        else:
+            seqs.append(g)
+            cols.append(c)
+    text, off, ln, col = synth.pack_sequences(seqs, cols)
+    return text, off, ln, col, gs, n_genomes
+
+
+@pytest.fixture(scope="module")
+def built():
+    text, off, ln, col, gs, nc = _colored_input()
+    ctx = _native.GpuContext(0)
+    p = _native.make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=1, keep_kmers=True)
+    ctx.build_text(text, p)
+    ctx.colors(off, col, nc)
+    r = oracle.build_graph(text, off, ln, oracle.params(k=31, m=10, bucket_bits=6, second_bits=2, threads=4,
+                                                         colors=True), seq_colors=col)
+    yield ctx, r, text, off, ln, col, gs, nc
+    ctx.close()
+
+
+def _decode(bm_row):
+    cols = []
+    for w, word in enumerate(bm_row.tolist()):
+        for b in range(32):
+            if (word >> b) & 1:
+                cols.append(w * 32 + b)
+    return tuple(cols)
+
+
+def test_kmer_color_sets_match_oracle(built):
+    ctx, r, *_ = built
+    keys, mult = ctx.kmers()
+    subs = ctx.kmer_subsets()
+    bitmaps = ctx.subsets()
+    decoded = [_decode(row) for row in bitmaps]
+    assert len(set(decoded)) == len(decoded)  # every subset appears once
+    got = {}
+    for kk, sid in zip(keys.tolist(), subs.tolist()):
+        cs = decoded[sid]
+        assert got.get(kk, cs) == cs
+        got[kk] = cs
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    exp = {int(lo[i]): tuple(int(c) for c in ccol[coff[i]:coff[i + 1]]) for i in range(len(lo))}
+    assert got == exp
+
+
+def test_colored_query_counts_match_oracle(built):
+    ctx, r, text, off, ln, col, gs, nc = built
+    ctx.query_index_colored()
+    rng = np.random.default_rng(5)
+    queries, _ = synth.query_stream(gs, 60, rng, min_len=20, max_len=8000)
+    qt, qo, ql = serve._pack(queries)
+    ctx.query_submit(1, qt, qo, ql)
+    matched = ctx.query_wait(1)
+    counts = ctx.query_color_counts(1)
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    em, _, epc = oracle.query(lo, hi, qt, qo, ql, 31, gc_off=coff, gc_colors=ccol, ncolors=nc)
+    assert (matched == em).all()
+    assert (counts == epc).all()
+    assert epc.sum() > 0

@@ -72,3 +72,39 @@ def test_build_rk128_matches_seqhash():
 def test_build_k63_seq128():
     seqs = _genome_mix(8, L=2500, copies=2)
     _run(seqs, k=63, m=12, hash_kind=oracle.H_CN_SEQ128)
+
+
+def test_rabin_karp_selects_the_same_kmers_as_seqhash():
+    """The device keys its tables by the canonical packed k-mer for every hash kind; the
+    reference's Rabin-Karp u128 keys give the same multiplicities and unitigs (k = 63)."""
+    rng = np.random.default_rng(3)
+    g = synth.random_genome(40_000, rng)
+    gs = [g, synth.indels(synth.substitute(g, 0.01, rng), 0.001, 10, rng)]
+    text, off, ln, _ = synth.pack_sequences(gs)
+    res = []
+    for kind in (oracle.H_CN_SEQ128, oracle.H_CN_RK128):
+        r = oracle.build_graph(text, off, ln, oracle.params(k=63, m=12, bucket_bits=6, second_bits=2,
+                                                            hash_kind=kind, threads=4))
+        lo, hi, mult = r.kmers()
+        res.append((sorted(zip(lo.tolist(), hi.tolist(), mult.tolist())), r.unitigs()))
+    assert res[0] == res[1]
+
+
+def test_build_colors_match_naive():
+    """Per-k-mer colour sets (MultipleColorsManager semantics: sorted distinct colours of all
+    occurrences), on inputs whose k-mer maps grow while they fill."""
+    rng = np.random.default_rng(8)
+    seqs, cols = [], []
+    for c in range(5):
+        g = synth.random_genome(3000, rng)
+        seqs += [g.tobytes(), synth.substitute(g, 0.02, rng).tobytes()]
+        cols += [c, (c + 1) % 5]
+    text, off, ln, _ = synth.pack_sequences([np.frombuffer(s, np.uint8) for s in seqs])
+    col = np.asarray(cols, np.uint32)
+    r = oracle.build_graph(text, off, ln, oracle.params(k=31, m=10, bucket_bits=3, second_bits=1, threads=2,
+                                                        colors=True), seq_colors=col)
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    names = _kmers_to_strings(lo, hi, 31)
+    got = {names[i]: tuple(int(c) for c in ccol[coff[i]:coff[i + 1]]) for i in range(len(names))}
+    assert got == naive.kmer_colors(seqs, cols, 31)
