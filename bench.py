@@ -31,6 +31,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "build Gbases/s bit-exact (batched vs per-bucket launch)"
 
+# DRAM bytes (read + write) of the merge-phase kernels per k-mer instance, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the 200 Mbp case; None until measured.
+MERGE_DRAM_BYTES_PER_INSTANCE = None
+
 
 def _args():
     ap = argparse.ArgumentParser()
@@ -38,7 +42,10 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--genome", type=int, default=50_000_000, help="genome length of the read workload")
+    ap.add_argument("--workload", default="skewed", choices=["skewed", "longk"],
+                    help="skewed: 150-bp reads of a repeat-rich 50 Mbp genome, k=31 (the headline); "
+                         "longk: 250-bp reads of a 100 Mbp GC-0.4 genome, k=63, Rabin-Karp 128-bit hash")
+    ap.add_argument("--genome", type=int, default=0, help="genome length (0 = the workload's own)")
     ap.add_argument("--coverage", type=float, default=20.0)
     ap.add_argument("--no-per-bucket", action="store_true", help="skip timing the per-bucket launch form")
     ap.add_argument("--cpu-sample-bases", type=int, default=30_000_000)
@@ -61,7 +68,15 @@ def _dist():
 def _workload(args):
     from ggcat_gb300 import synth
 
-    return synth.config_skewed_reads(genome_len=args.genome, coverage=args.coverage)
+    if args.workload == "longk":
+        return synth.config_long_k(genome_len=args.genome or 100_000_000, coverage=args.coverage)
+    return synth.config_skewed_reads(genome_len=args.genome or 50_000_000, coverage=args.coverage)
+
+
+def _hash_kind(w):
+    from ggcat_gb300 import _native
+
+    return _native.GGCAT_HASH_RABIN_KARP128 if getattr(w, "hash_kind", "") == "rk128" else _native.GGCAT_HASH_SEQHASH
 
 
 class ClockSampler:
@@ -138,7 +153,7 @@ def cpu_baseline(w, sample_bases: int, threads: int):
     end = int(w.seq_off[take - 1] + w.seq_len[take - 1] + 1)
     text = w.text[:end]
     p = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6, min_multiplicity=w.min_multiplicity,
-                      threads=threads)
+                      threads=threads, hash_kind=oracle.H_CN_RK128 if getattr(w, "hash_kind", "") == "rk128" else None)
     t0 = time.perf_counter()
     r = oracle.build_graph(text, w.seq_off[:take], w.seq_len[:take], p)
     dt = time.perf_counter() - t0
@@ -258,7 +273,7 @@ def run_gpu(args):
 
     def params(mode):
         return _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
-                                   min_multiplicity=w.min_multiplicity, merge_mode=mode)
+                                   min_multiplicity=w.min_multiplicity, merge_mode=mode, hash_kind=_hash_kind(w))
 
     def step(p):
         ctx.bucketize(d_text.data_ptr(), d_text.numel(), p, sptr)
@@ -323,18 +338,31 @@ def run_gpu(args):
     d2h = int(st2["partial_bases"] + st2["partial_unitigs"] * (8 + 4 + 1))
     e2e_value = bases * ws / wall / 1e9
 
-    # roofline: the bucketing phase (pack + count + write passes) is HBM-bound; its
-    # algorithmic bytes per step are the ASCII read, the 2-bit + validity write, two reads
-    # of the packed input and one 16-byte record write per superkmer.
+    # roofline of the dominant phase, the merge (merge_unit_kernel S and M tiers + L kernels,
+    # about 3/4 of the step).  Algorithmic bytes per step: every superkmer read once in 2-bit
+    # form with an 8-byte header (ceil(L/4) + 8), every k-mer instance's key written and read
+    # once (8 + 8 bytes), every distinct k-mer of a unit written with its count (8 + 4).
     peak, peak_kind = _peaks()
     n = w.text.size
-    bucket_bytes = n + n * 3 / 8 + 2 * (n * 3 / 8) + 16 * st["superkmers"]
-    bucket_ms = phases["ms_pack"] + phases["ms_bucketize"]
-    achieved = bucket_bytes / (bucket_ms * 1e-3) / 1e9 if bucket_ms > 0 else 0.0
-    roofline = {"bound": "hbm", "kernel": "pack_kernel + bucketize_kernel (bucketing phase)",
+    S, I, D = st["superkmers"], st["kmer_instances"], st["distinct_kmers"]
+    merge_bytes = (I + S * (w.k - 1)) / 4 + S * 8.375 + 16 * I + 12 * D
+    merge_ms = phases["ms_merge"]
+    achieved = merge_bytes / (merge_ms * 1e-3) / 1e9 if merge_ms > 0 else 0.0
+    # DRAM bytes of the merge kernels per k-mer instance, from one ncu capture of the 10 Mbp-genome
+    # (200 Mbp of reads) case of this workload, scaled by the instances of this step
+    traffic = round(MERGE_DRAM_BYTES_PER_INSTANCE * I) if MERGE_DRAM_BYTES_PER_INSTANCE else None
+    roofline = {"bound": "hbm", "kernel": "merge_unit_kernel (S + M tiers) + large_* (merge phase)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "peak_kind": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_step": int(bucket_bytes), "phase_ms": round(bucket_ms, 3)}
+                "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_step": int(merge_bytes), "phase_ms": round(merge_ms, 3)}
+    # the bucketing phase (pack + count + write passes): the ASCII read, the 2-bit + validity
+    # write, two reads of the packed input and one 16-byte record write per superkmer
+    bucket_bytes = n + n * 3 / 8 + 2 * (n * 3 / 8) + 16 * S
+    bucket_ms = phases["ms_pack"] + phases["ms_bucketize"]
+    b_ach = bucket_bytes / (bucket_ms * 1e-3) / 1e9 if bucket_ms > 0 else 0.0
+    roofline_bucketing = {"bound": "hbm", "kernel": "pack_kernel + bucketize_kernel", "achieved": round(b_ach, 1),
+                          "peak": peak, "unit": "GB/s", "frac": round(b_ach / peak, 4), "peak_kind": peak_kind,
+                          "algorithmic_bytes_per_step": int(bucket_bytes), "phase_ms": round(bucket_ms, 3)}
 
     query = None
     if rank == 0 and not args.no_query:
@@ -359,21 +387,24 @@ def run_gpu(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "u64",
+            "dtype": "u64" if w.k <= 32 else "u128",
             "data": "synthetic (seeded)",
             "config": {"workload": w.name, "k": w.k, "m": w.m, "buckets": 1 << w.bucket_bits,
                        "min_multiplicity": w.min_multiplicity, "bases_per_gpu": bases,
-                       "l2": "input (1 GB) larger than L2; no flush", "merge": "batched persistent",
+                       "hash": getattr(w, "hash_kind", "seq-hash"),
+                       "l2": f"input ({n / 1e9:.1f} GB) larger than L2; no flush", "merge": "batched persistent",
                        "parallelism": f"replicas x{ws}"},
             "phases_ms": {k2: round(v, 3) for k2, v in phases.items()},
             "stats": {"superkmers": int(st["superkmers"]), "kmer_instances": int(st["kmer_instances"]),
-                      "partial_unitigs": int(st["partial_unitigs"]), "small_units": int(st["merge_units_small"]),
-                      "large_units": int(st["merge_units_large"])},
+                      "distinct_kmers": int(D), "partial_unitigs": int(st["partial_unitigs"]),
+                      "small_units": int(st["merge_units_small"]), "large_units": int(st["merge_units_large"]),
+                      "spilled_units": int(st["merge_units_spilled"])},
             "per_bucket": per_bucket,
             "e2e": {"value": round(e2e_value, 4), "unit": "Gbases/s", "h2d_bytes_per_step": int(n),
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "roofline": roofline,
+            "roofline_bucketing": roofline_bucketing,
             "cpu_baseline": cpu,
             "query": query,
             "clocks": clocks,
@@ -388,6 +419,8 @@ def run_gpu(args):
 
 def main():
     args = _args()
+    if args.workload != "skewed":
+        args.no_query = True  # the query section serves a k=31 graph
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

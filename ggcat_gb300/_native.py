@@ -54,6 +54,8 @@ class Stats(C.Structure):
         ("ms_bucketize", C.c_double),
         ("ms_merge", C.c_double),
         ("ms_link", C.c_double),
+        ("distinct_kmers", C.c_uint64),
+        ("merge_units_spilled", C.c_uint64),
     ]
 
 

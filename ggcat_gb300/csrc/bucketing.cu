@@ -9,8 +9,9 @@
 // Layout: the ASCII text is packed once into 2-bit codes (32 bases per u64) and a
 // validity bitmap (1 bit per base; ACGTacgt are valid).  Each thread then owns a chunk
 // of (k-1)-mer window positions and walks its bases sequentially with a rolling nt-hash
-// and an incremental window minimum; superkmer boundaries owned by the chunk are
-// emitted as 16-byte records into a per-sub-bin partition (count pass + write pass).
+// and a block-decomposed window minimum; the superkmers whose split point falls in the
+// chunk are appended as 16-byte records to a staging array and counted per sub-bin in
+// the same pass, and partition_kernel scatters them by sub-bin after an exclusive scan.
 #include "common.cuh"
 #include "kernels.h"
 

@@ -105,7 +105,7 @@ struct ggcat_gpu_ctx {
     bool have_colors = false;
 
     // merge
-    DevBuf<MergeUnit> small_units, medium_units, large_units, bucket_units;
+    DevBuf<MergeUnit> small_units, wide_units, medium_units, large_units, bucket_units;
     DevBuf<unsigned long long> counters, ones;
     DevBuf<uint64_t> tkeys;
     DevBuf<uint32_t> tvals;
@@ -362,6 +362,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     }
     const uint64_t max_units = ctx->n_bins + 1;
     CK(ctx->small_units.ensure(max_units));
+    CK(ctx->wide_units.ensure(max_units));
     CK(ctx->medium_units.ensure(max_units));
     CK(ctx->large_units.ensure(max_units));
     // worst-case slot pool of the global-memory tables: cap < 2 * (1.25 x + 64) per unit
@@ -420,11 +421,15 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->stats.merge_units_large = ctx->n_buckets;
     } else {
         const uint64_t medium_limit = 1ull << 18;
+        const uint64_t wide_limit = p->unit_target < 0 ? 0 : merge_wide_limit(wide);
         ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits,
-                                               small_limit, target, medium_limit, ctx->small_units.p,
-                                               ctx->medium_units.p, ctx->large_units.p, max_units, pool,
+                                               small_limit, target, wide_limit, medium_limit, ctx->small_units.p,
+                                               ctx->wide_units.p, ctx->medium_units.p, ctx->large_units.p, max_units,
+                                               pool,
                                                ctx->counters.p, ctx->status.p + 1, s);
         ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
+        ctx->launches += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o,
+                                           ctx->sms, s);
         ctx->launches += launch_merge_medium(a, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
                                              ctx->tvis.p, o, ctx->sms, s);
         ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
@@ -443,9 +448,11 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     ctx->n_partial = cnt[kCntUnitigs];
     ctx->n_partial_bases = cnt[kCntBases];
     ctx->n_kmers_out = cnt[kCntKmers];
+    ctx->stats.distinct_kmers = cnt[kCntDistinct];
     if (p->merge_mode != GGCAT_MERGE_PER_BUCKET) {
         ctx->stats.merge_units_small = cnt[kCntSmall];
-        ctx->stats.merge_units_large = cnt[kCntMedium] + cnt[kCntLarge];
+        ctx->stats.merge_units_large = cnt[kCntWide] + cnt[kCntMedium] + cnt[kCntLarge] - cnt[kCntSpilled];
+        ctx->stats.merge_units_spilled = cnt[kCntSpilled];
         if (cnt[kCntSlots] > pool) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
     }
     *st_out = st;

@@ -62,18 +62,29 @@ enum : int {
     kCntLarge = 5,        // number of L units
     kCntSlots = 6,        // global table slots claimed by M and L units
     kCntMediumHead = 7,   // work-queue head of M units
-    kCntMedium = 8,       // number of M units
+    kCntMedium = 8,       // number of M units (including spilled optimistic S units)
+    kCntDistinct = 9,     // distinct k-mers summed over units (table entries)
+    kCntSpilled = 10,     // W units moved to the M tier
+    kCntWide = 11,        // number of W units
+    kCntWideHead = 12,    // work-queue head of W units
 };
 
 constexpr int kSmallSlots = 4096;     // shared-memory table capacity of one merge CTA
 constexpr int kMergeThreads = 256;
 
+// Sub-bins of <= small_limit instances are packed into S units (up to unit_target); single
+// sub-bins of <= wide_limit instances are W units (shared-memory table first, spill to the M
+// queue); <= medium_limit: M units; larger: L units.  W, M and L units reserve a global table.
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
-                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
-                          MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
-                          uint64_t pool_slots, unsigned long long *counters, unsigned *status, cudaStream_t s);
+                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
+                          uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
+                          MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
+                          unsigned long long *counters, unsigned *status, cudaStream_t s);
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s);
+// spill: the M-unit array (W units whose distinct k-mers overflow are appended to it)
+int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
+                      MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms, cudaStream_t s);
 // Table keys are u64 (a.wide == 0) or u128 (a.wide == 1, 16-byte aligned) slots.
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
                         uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s);
@@ -84,8 +95,9 @@ int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigne
 int launch_init_tables(void *keys, int wide, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s);
 int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, void *keys, int wide,
                             uint32_t *vals, uint8_t *vis, int sms, cudaStream_t s);
-// largest number of k-mer instances of an S unit
+// largest number of k-mer instances of an S unit / of an optimistic S unit
 uint64_t merge_small_limit(int wide);
+uint64_t merge_wide_limit(int wide);
 
 // query.cu
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,

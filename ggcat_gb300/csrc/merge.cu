@@ -59,6 +59,28 @@ __device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned 
     return -1;
 }
 
+// tinsert that also reports whether this call created the entry
+template <typename KT>
+__device__ __forceinline__ int64_t tinsert_created(const Table<KT> &t, KT key, unsigned *status, bool &created) {
+    uint32_t s = slot_of(key, t.cap);
+    created = false;
+    for (uint32_t probe = 0; probe < t.cap; probe++) {
+        const KT kk = t.keys[s];
+        if (kk == key) return s;
+        if (kk == KeyOps<KT>::empty()) {
+            const KT old = KeyOps<KT>::cas(&t.keys[s], KeyOps<KT>::empty(), key);
+            if (old == KeyOps<KT>::empty()) {
+                created = true;
+                return s;
+            }
+            if (old == key) return s;
+        }
+        s = (s + 1) & (t.cap - 1);
+    }
+    atomicOr(status, kStatusTableFull);
+    return -1;
+}
+
 // MapEntry::get_kmer_multiplicity (map_entry.rs:79-84): halve when both ends were ignored.
 __device__ __forceinline__ uint32_t val_mult(uint32_t v) {
     uint32_t c = v & kCountMask;
@@ -309,10 +331,10 @@ __device__ __forceinline__ uint32_t table_cap_for(uint64_t kk) {
 
 __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin_off,
                                       const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets, int fbits,
-                                      uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
-                                      MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units,
-                                      uint64_t max_units, uint64_t pool_slots, unsigned long long *counters,
-                                      unsigned *status) {
+                                      uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
+                                      uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
+                                      MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
+                                      uint64_t pool_slots, unsigned long long *counters, unsigned *status) {
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_buckets) return;
     const uint32_t nsub = 1u << fbits;
@@ -341,8 +363,12 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
         if (kk == 0) continue;
         if (kk > small_limit) {
             close_small(j);
+            // wide: a W unit tries the shared-memory table first (it fits when the sub-bin
+            // repeats its k-mers enough) and moves to the M tier with this reserved table when
+            // its distinct k-mers overflow the shared-memory table
+            const bool wide = kk <= wide_limit;
             const bool medium = kk <= medium_limit;
-            unsigned long long i = atomicAdd(&counters[medium ? kCntMedium : kCntLarge], 1ull);
+            unsigned long long i = atomicAdd(&counters[wide ? kCntWide : medium ? kCntMedium : kCntLarge], 1ull);
             uint32_t cap = table_cap_for(kk);
             unsigned long long off = atomicAdd(&counters[kCntSlots], (unsigned long long)cap);
             if (off + cap > pool_slots || i >= max_units) {
@@ -356,7 +382,7 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
             u.table_off = off;
             u.table_cap = cap;
             u.bucket = b;
-            (medium ? medium_units : large_units)[i] = u;
+            (wide ? wide_units : medium ? medium_units : large_units)[i] = u;
             continue;
         }
         if (open && cur_k + kk > unit_target) close_small(j);
@@ -372,21 +398,41 @@ __global__ void classify_units_kernel(const unsigned long long *__restrict__ bin
 // ---------------------------------------------------------------------------
 // small units: persistent CTAs, shared-memory table, device work queue
 // ---------------------------------------------------------------------------
-// Shared-memory layouts.  S units keep the hash table in shared memory; after the successor
-// phase the table is dead and its bytes are reused by the list-ranking arrays (union).  M
-// units keep the table in the global pool and use the whole shared memory of one CTA for
-// ranking arrays, so they rank more survivors.
-// Per key type: S-unit table slots, survivors ranked by S and M units (else walk fallback).
-// u128 keys halve the S table so two CTAs still fit on one SM.
-template <typename KT>
-struct Tier;
+// Tiers of merge_unit_kernel (one unit per CTA, persistent over a device work queue):
+//   S: many sub-bins packed per unit, hash table in shared memory, 256 threads, 2 CTAs/SM;
+//   W: one sub-bin of up to a few ten thousand instances, larger shared-memory table, 512
+//      threads, 1 CTA/SM; the table is sized for the distinct k-mers it can hold, so a unit
+//      whose distinct k-mers overflow it moves to the M queue (with a reserved global table);
+//   M: table in the global pool (L2-resident), 512 threads, the whole shared memory for the
+//      list-ranking arrays.
+// S and W reuse the table bytes for the list-ranking arrays once the successor phase is done
+// (union).  Units with more survivors than kSurv are extended by per-thread walks instead.
+enum : int { kTierS = 0, kTierW = 1, kTierM = 2 };
+template <typename KT, int kTier>
+struct TierCfg;
 template <>
-struct Tier<uint64_t> {
-    static constexpr int kSlots = kSmallSlots, kSmallSurv = 2048, kMedSurv = 6016;
+struct TierCfg<uint64_t, kTierS> {
+    static constexpr int NT = 256, kSlots = kSmallSlots, kSurv = 2048, kMinBlocks = 2;
 };
 template <>
-struct Tier<u128> {
-    static constexpr int kSlots = kSmallSlots / 2, kSmallSurv = 1024, kMedSurv = 4096;
+struct TierCfg<u128, kTierS> {
+    static constexpr int NT = 256, kSlots = kSmallSlots / 2, kSurv = 1024, kMinBlocks = 2;
+};
+template <>
+struct TierCfg<uint64_t, kTierW> {
+    static constexpr int NT = 512, kSlots = 2 * kSmallSlots, kSurv = 4096, kMinBlocks = 1;
+};
+template <>
+struct TierCfg<u128, kTierW> {
+    static constexpr int NT = 512, kSlots = kSmallSlots, kSurv = 2048, kMinBlocks = 1;
+};
+template <>
+struct TierCfg<uint64_t, kTierM> {
+    static constexpr int NT = 512, kSlots = 0, kSurv = 6016, kMinBlocks = 1;
+};
+template <>
+struct TierCfg<u128, kTierM> {
+    static constexpr int NT = 512, kSlots = 0, kSurv = 4096, kMinBlocks = 1;
 };
 constexpr uint16_t kNone16 = 0xffff;
 
@@ -398,15 +444,11 @@ struct RankView {
     uint16_t uidx[2 * N];     // local unitig index of owner starts
     uint8_t haspred[2 * N];
 };
-template <typename KT>
-struct SmallTableView {
-    KT keys[Tier<KT>::kSlots];
-    uint32_t vals[Tier<KT>::kSlots];  // count|flags<<30, then alive<<31|flags<<28|dense index
+template <typename KT, int kSlots>
+struct SmemTableView {
+    KT keys[kSlots];
+    uint32_t vals[kSlots];  // count|flags<<30, then alive<<31|flags<<28|dense index
 };
-static_assert(sizeof(RankView<Tier<uint64_t>::kSmallSurv>) <= sizeof(SmallTableView<uint64_t>),
-              "rank view must fit in the table bytes");
-static_assert(sizeof(RankView<Tier<u128>::kSmallSurv>) <= sizeof(SmallTableView<u128>),
-              "rank view must fit in the table bytes");
 
 template <typename KT, int N, int NT>
 struct UnitSmemCommon {
@@ -418,24 +460,32 @@ struct UnitSmemCommon {
     uint32_t warp_tmp[NT / 32 + 1];
     uint64_t unit;
     uint32_t n_surv, loc_bases, loc_count, ok;
+    uint32_t distinct;  // entries created (optimistic units)
     unsigned long long gbase, gidx;
 };
-constexpr int kSmallThreads = 256;
-constexpr int kMedThreads = 512;
-template <typename KT>
-struct SmallSmem : UnitSmemCommon<KT, Tier<KT>::kSmallSurv, kSmallThreads> {
+template <typename KT, int kTier, bool kShared = (kTier != kTierM)>
+struct UnitSmem;
+template <typename KT, int kTier>
+struct UnitSmem<KT, kTier, true> : UnitSmemCommon<KT, TierCfg<KT, kTier>::kSurv, TierCfg<KT, kTier>::NT> {
+    using C = TierCfg<KT, kTier>;
+    static_assert(sizeof(RankView<C::kSurv>) <= sizeof(SmemTableView<KT, C::kSlots>),
+                  "rank view must fit in the table bytes");
     union {
-        SmallTableView<KT> t;
-        RankView<Tier<KT>::kSmallSurv> r;
+        SmemTableView<KT, C::kSlots> t;
+        RankView<C::kSurv> r;
     } u;
-    uint8_t vis[Tier<KT>::kSlots];
+    uint8_t vis[C::kSlots];
 };
-template <typename KT>
-struct MedSmem : UnitSmemCommon<KT, Tier<KT>::kMedSurv, kMedThreads> {
+template <typename KT, int kTier>
+struct UnitSmem<KT, kTier, false> : UnitSmemCommon<KT, TierCfg<KT, kTier>::kSurv, TierCfg<KT, kTier>::NT> {
     union {
-        RankView<Tier<KT>::kMedSurv> r;
+        RankView<TierCfg<KT, kTier>::kSurv> r;
     } u;
 };
+static_assert(sizeof(UnitSmem<uint64_t, kTierW>) <= 227 * 1024 && sizeof(UnitSmem<u128, kTierW>) <= 227 * 1024 &&
+                  sizeof(UnitSmem<uint64_t, kTierM>) <= 227 * 1024 && sizeof(UnitSmem<u128, kTierM>) <= 227 * 1024 &&
+                  2 * sizeof(UnitSmem<uint64_t, kTierS>) <= 227 * 1024 && 2 * sizeof(UnitSmem<u128, kTierS>) <= 227 * 1024,
+              "shared memory of a merge CTA");
 
 // exclusive block scan of one u32 per thread (blockDim.x == NT); all threads call it
 template <int NT>
@@ -493,24 +543,29 @@ __device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
     return (u & 1) ? KeyOps<KT>::rc(x, k) : x;
 }
 
-// One merge unit per CTA, persistent over a device work queue.  kGlobalTable = false: S units,
-// hash table in shared memory; true: M units, hash table in the global pool (L2-resident).
-// Both use the shared-memory list-ranking arrays for the extension.
-template <typename KT, bool kGlobalTable, int NT>
-__global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
+// One merge unit per CTA, persistent over a device work queue (tiers above).  All tiers use
+// the shared-memory list-ranking arrays for the extension.
+template <typename KT, int kTier>
+__global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kMinBlocks)
     merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
-                      KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeOut o) {
-    using Smem = typename std::conditional<kGlobalTable, MedSmem<KT>, SmallSmem<KT>>::type;
+                      KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeUnit *spill, uint64_t max_units,
+                      MergeOut o) {
+    using Cfg = TierCfg<KT, kTier>;
+    using Smem = UnitSmem<KT, kTier>;
     using K = KeyOps<KT>;
-    constexpr int kMaxSurv = kGlobalTable ? Tier<KT>::kMedSurv : Tier<KT>::kSmallSurv;
+    constexpr int NT = Cfg::NT;
+    constexpr bool kGlobalTable = kTier == kTierM;
+    constexpr int kMaxSurv = Cfg::kSurv;
+    constexpr int kCount = kTier == kTierS ? kCntSmall : kTier == kTierW ? kCntWide : kCntMedium;
+    constexpr int kHead = kTier == kTierS ? kCntSmallHead : kTier == kTierW ? kCntWideHead : kCntMediumHead;
     extern __shared__ __align__(16) uint8_t smem_raw[];
     Smem &S = *reinterpret_cast<Smem *>(smem_raw);
-    const uint64_t n_units = counters_ro[kGlobalTable ? kCntMedium : kCntSmall];
+    const uint64_t n_units = counters_ro[kCount];
     const int k = a.k;
     const uint32_t min_mult = (uint32_t)a.min_mult;
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kGlobalTable ? kCntMediumHead : kCntSmallHead], 1ull);
+        if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kHead], 1ull);
         __syncthreads();
         const uint64_t ui = S.unit;
         if (ui >= n_units) break;
@@ -523,9 +578,14 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
         } else {
             cap = 64;
             while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
-            if (cap > (uint32_t)Tier<KT>::kSlots) cap = Tier<KT>::kSlots;
+            if (cap > (uint32_t)Cfg::kSlots) cap = Cfg::kSlots;
             t = Table<KT>{S.u.t.keys, S.u.t.vals, S.vis, cap};
         }
+        // optimistic unit (W tier, or a unit with a reserved global table): stop creating
+        // entries at kOptLimit (<= 0.8 load with the at most NT - 1 creations in flight when
+        // the count is reached) and spill to the M queue
+        const bool optimistic = !kGlobalTable && U.table_cap != 0;
+        constexpr uint32_t kOptLimit = kGlobalTable ? 0u : (uint32_t)Cfg::kSlots * 4 / 5 - NT;
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
             t.keys[i] = K::empty();
             t.vals[i] = 0;
@@ -535,6 +595,7 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
             S.n_surv = 0;
             S.loc_bases = 0;
             S.loc_count = 0;
+            S.distinct = 0;
         }
         __syncthreads();
 
@@ -567,7 +628,15 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
                 const KT fw = K::load(a.packed, rec_start(rr) + off, k);
                 const KT rc = K::rc(fw, k);
                 const uint32_t isf = fw < rc ? 1u : 0u;
-                const int64_t sl = tinsert(t, isf ? fw : rc, o.status);
+                int64_t sl;
+                if (optimistic) {
+                    if (*(volatile uint32_t *)&S.distinct >= kOptLimit) break;
+                    bool created;
+                    sl = tinsert_created(t, isf ? fw : rc, o.status, created);
+                    if (created) atomicAdd(&S.distinct, 1u);
+                } else {
+                    sl = tinsert(t, isf ? fw : rc, o.status);
+                }
                 if (sl < 0) continue;
                 const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
                 const uint32_t fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
@@ -575,6 +644,20 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
                 atomicAdd(&t.vals[sl], 1u);
             }
             __syncthreads();
+            if (optimistic && S.distinct >= kOptLimit) break;
+        }
+        if (optimistic && S.distinct >= kOptLimit) {
+            // too many distinct k-mers for the shared-memory table: the M tier redoes the
+            // unit with its reserved global table
+            if (threadIdx.x == 0) {
+                atomicAdd(&o.counters[kCntSpilled], 1ull);
+                const unsigned long long i = atomicAdd(&o.counters[kCntMedium], 1ull);
+                if (i < max_units)
+                    spill[i] = U;
+                else
+                    atomicOr(o.status, kStatusTableFull);
+            }
+            continue;
         }
 
         // ---- survivors (min-multiplicity filter): each warp scans a contiguous segment of
@@ -583,13 +666,18 @@ __global__ void __launch_bounds__(NT, kGlobalTable ? 1 : 2)
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const uint32_t seg = (((cap + NW - 1) / NW) + 31) & ~31u;
         const uint32_t seg_lo = min(cap, (uint32_t)wid * seg), seg_hi = min(cap, seg_lo + seg);
-        uint32_t warp_surv = 0;
+        uint32_t warp_surv = 0, warp_occ = 0;
         for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
             const uint32_t sl = b0 + lane;
-            bool alive = false;
-            if (sl < seg_hi) alive = t.keys[sl] != K::empty() && val_mult(t.vals[sl]) >= min_mult;
+            bool alive = false, occ = false;
+            if (sl < seg_hi) {
+                occ = t.keys[sl] != K::empty();
+                alive = occ && val_mult(t.vals[sl]) >= min_mult;
+            }
             warp_surv += __popc(__ballot_sync(0xffffffffu, alive));
+            warp_occ += __popc(__ballot_sync(0xffffffffu, occ));
         }
+        if (lane == 0 && warp_occ) atomicAdd(&o.counters[kCntDistinct], (unsigned long long)warp_occ);
         uint32_t n_surv;
         const uint32_t warp_base = block_scan_u32<NT>(lane == 0 ? warp_surv : 0u, S.warp_tmp, n_surv);
         if (n_surv > (uint32_t)kMaxSurv) {
@@ -841,12 +929,16 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
         const MergeUnit U = units[u];
         Table<KT> t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
         Graph<KT> g{t, a.k, (uint32_t)a.min_mult};
+        unsigned long long occ = 0;
         for (uint64_t s = gt; s < U.table_cap; s += gs) {
-            if (phase == 0)
+            if (phase == 0) {
+                occ += keys[U.table_off + s] != KeyOps<KT>::empty();
                 extend_slot(g, (uint32_t)s, o, a.keep_kmers, (uint32_t)a.min_mult);
-            else
+            } else {
                 cycle_slot(g, (uint32_t)s, o, (uint32_t)a.min_mult);
+            }
         }
+        if (occ) atomicAdd(&o.counters[kCntDistinct], occ);
     }
 }
 
@@ -854,63 +946,65 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
 // launchers
 // ---------------------------------------------------------------------------
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
-                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t medium_limit,
-                          MergeUnit *small_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
-                          uint64_t pool_slots, unsigned long long *counters, unsigned *status, cudaStream_t s) {
-    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(bin_off, bin_kmers, n_buckets, fbits, small_limit,
-                                                                  unit_target, medium_limit, small_units, medium_units,
-                                                                  large_units, max_units, pool_slots, counters, status);
+                          int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
+                          uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
+                          MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
+                          unsigned long long *counters, unsigned *status, cudaStream_t s) {
+    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(
+        bin_off, bin_kmers, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, small_units,
+        wide_units, medium_units, large_units, max_units, pool_slots, counters, status);
     return 1;
 }
 
-template <typename KT>
-static void merge_medium_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, KT *keys,
-                           uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+template <typename KT, int kTier>
+static void merge_tier_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, KT *keys,
+                         uint32_t *vals, uint8_t *vis, MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms,
+                         cudaStream_t s) {
+    using Cfg = TierCfg<KT, kTier>;
     static bool configured = false;
-    const int smem = (int)sizeof(MedSmem<KT>);
+    const int smem = (int)sizeof(UnitSmem<KT, kTier>);
     if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<KT, true, kMedThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
+        cudaFuncSetAttribute(merge_unit_kernel<KT, kTier>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         configured = true;
     }
-    merge_unit_kernel<KT, true, kMedThreads><<<sms, kMedThreads, smem, s>>>(a, units, counters, keys, vals, vis, o);
+    merge_unit_kernel<KT, kTier>
+        <<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(a, units, counters, keys, vals, vis, spill, max_units, o);
 }
 
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
                         uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
     if (a.wide)
-        merge_medium_t<u128>(a, units, counters, static_cast<u128 *>(keys), vals, vis, o, sms, s);
+        merge_tier_t<u128, kTierM>(a, units, counters, static_cast<u128 *>(keys), vals, vis, nullptr, 0, o, sms, s);
     else
-        merge_medium_t<uint64_t>(a, units, counters, static_cast<uint64_t *>(keys), vals, vis, o, sms, s);
+        merge_tier_t<uint64_t, kTierM>(a, units, counters, static_cast<uint64_t *>(keys), vals, vis, nullptr, 0, o,
+                                       sms, s);
     return 1;
-}
-
-template <typename KT>
-static void merge_small_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
-                          const MergeOut &o, int sms, cudaStream_t s) {
-    static bool configured = false;
-    const int smem = (int)sizeof(SmallSmem<KT>);
-    if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<KT, false, kSmallThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-        configured = true;
-    }
-    merge_unit_kernel<KT, false, kSmallThreads>
-        <<<sms * 2, kSmallThreads, smem, s>>>(a, units, counters, nullptr, nullptr, nullptr, o);
 }
 
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s) {
     if (a.wide)
-        merge_small_t<u128>(a, units, counters, o, sms, s);
+        merge_tier_t<u128, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
     else
-        merge_small_t<uint64_t>(a, units, counters, o, sms, s);
+        merge_tier_t<uint64_t, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
     return 1;
 }
 
+int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
+                      MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms, cudaStream_t s) {
+    if (a.wide)
+        merge_tier_t<u128, kTierW>(a, units, counters, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
+    else
+        merge_tier_t<uint64_t, kTierW>(a, units, counters, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
+    return 1;
+}
+
+uint64_t merge_wide_limit(int wide) { return wide ? 16384 : 32768; }
+
 uint64_t merge_small_limit(int wide) {
     // instances of an S unit, so that its table (Tier slots) stays at load <= 0.8
-    static_assert(3200 * 5 <= Tier<uint64_t>::kSlots * 4 && 1600 * 5 <= Tier<u128>::kSlots * 4, "S table load");
+    static_assert(3200 * 5 <= TierCfg<uint64_t, kTierS>::kSlots * 4 && 1600 * 5 <= TierCfg<u128, kTierS>::kSlots * 4,
+                  "S table load");
     return wide ? 1600 : 3200;
 }
 

@@ -48,7 +48,8 @@ typedef struct {
     int32_t hash_kind;        /* GGCAT_HASH_* */
     int32_t forward_only;     /* 1 = do not canonicalise (rc never applied) */
     int32_t merge_mode;       /* GGCAT_MERGE_* */
-    int32_t unit_target;      /* target k-mer instances per merge unit (0 = auto) */
+    int32_t unit_target;      /* target k-mer instances per merge unit (0 = auto; -1 = auto without the
+                                 shared-memory attempt for sub-buckets above the S-unit size) */
     int32_t keep_kmers;       /* 1 = also output the surviving k-mers and multiplicities */
 } ggcat_gpu_params;
 
@@ -77,6 +78,8 @@ typedef struct {
     uint64_t surviving_kmers;   /* counted once per (k-mer, sub-bucket) */
     uint64_t final_unitigs;
     double ms_pack, ms_bucketize, ms_merge, ms_link; /* device times (events) and host link time */
+    uint64_t distinct_kmers;    /* table entries summed over merge units */
+    uint64_t merge_units_spilled; /* shared-memory attempts that moved to a global-memory table */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */

@@ -35,6 +35,16 @@ def _workload(kind, seed):
             b"CCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGG")]
         seqs += [synth.random_genome(int(n), rng) for n in rng.integers(25, 120, size=200)]
         return synth.pack_sequences(seqs)
+    if kind in ("planted31", "planted63"):
+        # a random sequence with the m-mer of smallest canonical nt-hash planted every k - m
+        # bases: every (k-1)-mer window holds exactly one copy, so all its k-mers (all
+        # distinct) fall into one sub-bucket
+        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if kind == "planted31" else (63, 12, b"CAGACTATCGCG", 5000)
+        g = synth.random_genome(n, rng).copy()
+        pat = np.frombuffer(mm, np.uint8)
+        for p in range(0, n - len(pat), k - m):
+            g[p:p + len(pat)] = pat
+        return synth.pack_sequences([g, synth.random_genome(3000, rng)])
     raise ValueError(kind)
 
 
@@ -98,13 +108,39 @@ def test_small_unit_target_changes_nothing(ctx):
     """Any packing of sub-bins into merge units gives the same unitigs."""
     text, off, ln, _ = _workload("reads", 7)
     outs = []
-    for target in (64, 900, 0):
+    for target in (64, 900, 0, -1):
         p = make_params(k=31, m=10, bucket_bits=8, second_bits=2, min_multiplicity=2, unit_target=target)
         ctx.build_text(text, p)
         ctx.link(31)
         bases, uo, ul, uf = ctx.unitigs()
         outs.append(oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31))
-    assert outs[0] == outs[1] == outs[2]
+    assert outs[0] == outs[1] == outs[2] == outs[3]
+
+
+@pytest.mark.parametrize("kind,bbits,minm,k,m", [("planted31", 1, 1, 31, 10), ("planted63", 1, 1, 63, 12),
+                                                 ("reads", 2, 2, 31, 10), ("genomes", 1, 1, 31, 10)])
+def test_shared_memory_attempt_and_spill(ctx, kind, bbits, minm, k, m):
+    """Sub-buckets of several thousand k-mer instances try the shared-memory table first and
+    move to the global-memory tier when their distinct k-mers do not fit (planted: one
+    sub-bucket of all-distinct k-mers).  Same result as the oracle either way."""
+    text, off, ln, _ = _workload(kind, 21)
+    p = make_params(k=k, m=m, bucket_bits=bbits, second_bits=1, min_multiplicity=minm, keep_kmers=True)
+    ctx.build_text(text, p)
+    st = ctx.stats()
+    if kind.startswith("planted"):
+        assert st["merge_units_spilled"] > 0
+    assert st["distinct_kmers"] >= st["surviving_kmers"] > 0
+    keys, mult = ctx.kmers()
+    if k > 32:
+        keys = [int(a) | (int(b) << 64) for a, b in keys.tolist()]
+    got = _kmer_dict(keys, mult)
+    op = oracle.params(k=k, m=m, bucket_bits=bbits, second_bits=1, min_multiplicity=minm, threads=8)
+    r = oracle.build_graph(text, off, ln, op)
+    lo, hi, emult = r.kmers()
+    assert got == {int(a) | (int(b) << 64): int(c) for a, b, c in zip(lo.tolist(), hi.tolist(), emult.tolist())}
+    ctx.link(k)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k) == r.unitigs()
 
 
 def test_device_pointer_bucketize(ctx):
