@@ -55,7 +55,8 @@ template <>
 struct KeyOps<uint64_t> {
     static constexpr int kMaxK = 32;
     __device__ static __forceinline__ uint64_t empty() { return ~0ull; }
-    __device__ static __forceinline__ uint32_t hash(uint64_t x) { return (uint32_t)mix64(x); }
+    // high half of a multiplicative hash; table slots take its top bits
+    __device__ static __forceinline__ uint32_t hash(uint64_t x) { return (uint32_t)((x * 0x9E3779B97F4A7C15ull) >> 32); }
     __device__ static __forceinline__ uint64_t rc(uint64_t v, int k) { return rc_packed(v, k); }
     __device__ static __forceinline__ uint64_t mask(int k) { return kmer_mask(k); }
     __device__ static __forceinline__ uint64_t cas(uint64_t *a, uint64_t cmp, uint64_t val) {
@@ -94,7 +95,8 @@ struct KeyOps<u128> {
     static constexpr int kMaxK = 64;
     __device__ static __forceinline__ u128 empty() { return ~(u128)0; }
     __device__ static __forceinline__ uint32_t hash(u128 x) {
-        return (uint32_t)mix64((uint64_t)x ^ mix64((uint64_t)(x >> 64)));
+        const uint64_t f = (uint64_t)x ^ ((uint64_t)(x >> 64) * 0xC2B2AE3D27D4EB4Full);
+        return (uint32_t)((f * 0x9E3779B97F4A7C15ull) >> 32);
     }
     // the 64-base reverse complement is the rc of the two 32-base halves, swapped
     __device__ static __forceinline__ u128 rc(u128 v, int k) {

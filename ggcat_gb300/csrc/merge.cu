@@ -28,8 +28,11 @@ struct Table {
 
 constexpr uint32_t kCountMask = (1u << 30) - 1;
 
+// Fibonacci hashing: the top log2(cap) bits of the 32-bit multiplicative hash (cap >= 2)
 template <typename KT>
-__device__ __forceinline__ uint32_t slot_of(KT key, uint32_t cap) { return KeyOps<KT>::hash(key) & (cap - 1); }
+__device__ __forceinline__ uint32_t slot_of(KT key, uint32_t cap) {
+    return KeyOps<KT>::hash(key) >> (__clz(cap) + 1);
+}
 
 template <typename KT>
 __device__ __forceinline__ int64_t tfind(const Table<KT> &t, KT key) {
@@ -434,7 +437,7 @@ template <>
 struct TierCfg<u128, kTierM> {
     static constexpr int NT = 512, kSlots = 0, kSurv = 4096, kMinBlocks = 1;
 };
-constexpr uint16_t kNone16 = 0xffff;
+constexpr uint16_t kNone16 = 0xffff, kMulti16 = 0xfffe;
 
 template <int N>
 struct RankView {
@@ -455,8 +458,6 @@ struct UnitSmemCommon {
     KT sk[N];              // survivor canonical k-mers (dense order)
     uint16_t succ[2 * N];  // traversable successor of each oriented node
     uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
-    SkRec rec[NT];         // record batch
-    uint32_t pref[NT + 1];
     uint32_t warp_tmp[NT / 32 + 1];
     uint64_t unit;
     uint32_t n_surv, loc_bases, loc_count, ok;
@@ -585,7 +586,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         // entries at kOptLimit (<= 0.8 load with the at most NT - 1 creations in flight when
         // the count is reached) and spill to the M queue
         const bool optimistic = !kGlobalTable && U.table_cap != 0;
-        constexpr uint32_t kOptLimit = kGlobalTable ? 0u : (uint32_t)Cfg::kSlots * 4 / 5 - NT;
+        constexpr uint32_t kOptLimit = kGlobalTable ? 0xffffffffu : (uint32_t)Cfg::kSlots * 4 / 5 - NT;
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
             t.keys[i] = K::empty();
             t.vals[i] = 0;
@@ -599,52 +600,78 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         }
         __syncthreads();
 
-        // ---- insert (add_sequence, hashmap.rs:361-431), k-mer parallel over record batches ----
-        for (uint64_t rb = U.rec_begin; rb < U.rec_end; rb += NT) {
-            const uint64_t r = rb + threadIdx.x;
-            uint32_t nk = 0;
-            if (r < U.rec_end) {
-                const SkRec rr = a.recs[r];
-                S.rec[threadIdx.x] = rr;
-                nk = rec_len(rr) - (uint32_t)k + 1;
-            }
-            uint32_t total;
-            const uint32_t ex = block_scan_u32<NT>(nk, S.warp_tmp, total);
-            S.pref[threadIdx.x] = ex;
-            __syncthreads();
-            for (uint32_t j = threadIdx.x; j < total; j += blockDim.x) {
-                int lo = 0, hi = NT - 1;  // record of k-mer j: last prefix <= j
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.pref[mid] <= j) lo = mid; else hi = mid - 1;
+        // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes 32 records at a
+        //      time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is
+        //      found from the mask of record starts in the current 32-k-mer window, so the
+        //      insert phase needs no block barrier. ----
+        {
+            constexpr int NW = NT / 32;
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            const unsigned full = 0xffffffffu;
+            bool stop = false;
+            for (uint64_t rb = U.rec_begin + (uint64_t)wid * 32; rb < U.rec_end && !stop; rb += (uint64_t)NW * 32) {
+                const uint64_t r = rb + lane;
+                uint64_t w0 = 0;
+                uint32_t fr = 0, nk = 0;
+                if (r < U.rec_end) {
+                    const SkRec rr = a.recs[r];
+                    w0 = rr.w0;
+                    fr = rec_flags(rr) | (rec_rc(rr) << 2);
+                    nk = rec_len(rr) - (uint32_t)k + 1;  // >= 1: records hold at least one k-mer
                 }
-                const SkRec rr = S.rec[lo];
-                const uint32_t off = j - S.pref[lo];
-                const uint32_t last = rec_len(rr) - (uint32_t)k;
-                const uint32_t fl = rec_flags(rr), rcf = rec_rc(rr);
-                // text-orientation included flags (begin <- stored end when reverse-complemented)
-                const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
-                const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
-                const KT fw = K::load(a.packed, rec_start(rr) + off, k);
-                const KT rc = K::rc(fw, k);
-                const uint32_t isf = fw < rc ? 1u : 0u;
-                int64_t sl;
-                if (optimistic) {
-                    if (*(volatile uint32_t *)&S.distinct >= kOptLimit) break;
-                    bool created;
-                    sl = tinsert_created(t, isf ? fw : rc, o.status, created);
-                    if (created) atomicAdd(&S.distinct, 1u);
-                } else {
-                    sl = tinsert(t, isf ? fw : rc, o.status);
+                uint32_t incl = nk;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t y = __shfl_up_sync(full, incl, d);
+                    if (lane >= d) incl += y;
                 }
-                if (sl < 0) continue;
-                const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
-                const uint32_t fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
-                if (fbits) atomicOr(&t.vals[sl], fbits << 30);
-                atomicAdd(&t.vals[sl], 1u);
+                const uint32_t ex = incl - nk;
+                const uint32_t total = __shfl_sync(full, incl, 31);
+                for (uint32_t J = 0; J < total; J += 32) {
+                    if (optimistic) {
+                        const bool over = *(volatile uint32_t *)&S.distinct >= kOptLimit;
+                        if (__any_sync(full, over)) {
+                            stop = true;
+                            break;
+                        }
+                    }
+                    // records are in lane order with nk >= 1; record of k-mer J + lane =
+                    // (records starting at or before it) - 1
+                    const bool starts = nk > 0 && ex >= J && ex < J + 32u;
+                    const uint32_t smask = __reduce_or_sync(full, starts ? 1u << (ex - J) : 0u);
+                    const uint32_t before = __popc(__ballot_sync(full, nk > 0 && ex < J));
+                    const uint32_t j = J + (uint32_t)lane;
+                    const bool have = j < total;
+                    const uint32_t ri = have ? before + __popc(smask & ((2u << lane) - 1u)) - 1u : 0u;
+                    const uint64_t rw0 = __shfl_sync(full, w0, (int)ri);
+                    const uint32_t rfr = __shfl_sync(full, fr, (int)ri);
+                    const uint32_t rex = __shfl_sync(full, ex, (int)ri);
+                    if (!have) continue;
+                    const uint32_t off = j - rex;
+                    const uint32_t last = (uint32_t)(rw0 >> 40) - (uint32_t)k;
+                    const uint32_t fl = rfr & 3u, rcf = rfr >> 2;
+                    // text-orientation included flags (begin <- stored end when reverse-complemented)
+                    const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
+                    const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
+                    const KT fw = K::load(a.packed, (rw0 & ((1ull << 40) - 1)) + off, k);
+                    const KT rc = K::rc(fw, k);
+                    const uint32_t isf = fw < rc ? 1u : 0u;
+                    int64_t sl;
+                    if (optimistic) {
+                        bool created;
+                        sl = tinsert_created(t, isf ? fw : rc, o.status, created);
+                        if (created) atomicAdd(&S.distinct, 1u);
+                    } else {
+                        sl = tinsert(t, isf ? fw : rc, o.status);
+                    }
+                    if (sl < 0) continue;
+                    const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
+                    const uint32_t fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
+                    if (fbits) atomicOr(&t.vals[sl], fbits << 30);
+                    atomicAdd(&t.vals[sl], 1u);
+                }
             }
             __syncthreads();
-            if (optimistic && S.distinct >= kOptLimit) break;
         }
         if (optimistic && S.distinct >= kOptLimit) {
             // too many distinct k-mers for the shared-memory table: the M tier redoes the
@@ -666,13 +693,16 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const uint32_t seg = (((cap + NW - 1) / NW) + 31) & ~31u;
         const uint32_t seg_lo = min(cap, (uint32_t)wid * seg), seg_hi = min(cap, seg_lo + seg);
+        // (an entry's count is >= 1 from its creation, so the value word alone tells empty
+        // from occupied)
         uint32_t warp_surv = 0, warp_occ = 0;
         for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
             const uint32_t sl = b0 + lane;
             bool alive = false, occ = false;
             if (sl < seg_hi) {
-                occ = t.keys[sl] != K::empty();
-                alive = occ && val_mult(t.vals[sl]) >= min_mult;
+                const uint32_t v = t.vals[sl];
+                occ = v != 0;
+                alive = val_mult(v) >= min_mult;
             }
             warp_surv += __popc(__ballot_sync(0xffffffffu, alive));
             warp_occ += __popc(__ballot_sync(0xffffffffu, occ));
@@ -694,17 +724,21 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
                 const uint32_t sl = b0 + lane;
                 bool alive = false;
-                KT key = K::empty();
                 uint32_t v = 0;
                 if (sl < seg_hi) {
-                    key = t.keys[sl];
                     v = t.vals[sl];
-                    alive = key != K::empty() && val_mult(v) >= min_mult;
+                    alive = val_mult(v) >= min_mult;
                 }
                 const unsigned bm = __ballot_sync(0xffffffffu, alive);
                 const uint32_t idx = base + __popc(bm & ((1u << lane) - 1u));
                 if (alive) {
+                    const KT key = t.keys[sl];
                     S.sk[idx] = key;
+                    // boundary sides of both orientations (MapEntry flags in canonical
+                    // orientation: 1 = left side ignored, 2 = right side ignored)
+                    const uint32_t fv = v >> 30;
+                    S.bflag[2 * idx] = (uint8_t)((fv == 1u ? 1u : 0u) | (fv == 2u ? 2u : 0u));
+                    S.bflag[2 * idx + 1] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
                     if (a.keep_kmers) {
                         const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
                         if (di < o.kmer_cap) {
@@ -724,46 +758,44 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         const uint32_t ns = S.n_surv;
         const uint32_t nn = 2 * ns;  // oriented nodes: u = 2*dense + (0 canonical, 1 reverse complement)
 
-        // ---- traversable successor of every oriented node (the extension rules of
-        //      try_extend_function, hashmap.rs:162-297): 8 probes per node ----
+        // ---- successors (the extension rules of try_extend_function, hashmap.rs:162-297).
+        //      Degrees first: per survivor, the surviving successors of both orientations
+        //      (4 probes each); code = unique successor node, kNone16 (none) or kMulti16.
+        //      A node u -> w is traversable iff u's right side and w's left side are no
+        //      bucket boundary, w is u's only successor, u is w's only predecessor (the
+        //      mirror of w has one successor) and w is another k-mer. ----
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
             const KT x = S.sk[u >> 1];
             const KT v = (u & 1) ? K::rc(x, k) : x;
-            const int64_t sv = tfind(t, x);
-            const uint32_t fv = (t.vals[sv] >> 28) & 3u;
-            // MapEntry flags in canonical orientation: 1 = left side ignored, 2 = right side ignored
-            const bool lb = (u & 1) ? fv == 2u : fv == 1u;
-            const bool rb = (u & 1) ? fv == 1u : fv == 2u;
-            uint16_t nx = kNone16;
-            if (!rb) {
-                KT only = 0;
-                int64_t s_only = -1;
-                if (alive_succ(t, v, k, only, s_only) == 1 && s_only != sv) {
-                    const KT ru = K::rc(only, k);
-                    KT dummy;
-                    int64_t sd;
-                    const int d2 = alive_succ(t, ru, k, dummy, sd);  // predecessors of the successor
-                    const uint32_t vu = t.vals[s_only];
-                    const uint32_t fu = (vu >> 28) & 3u;
-                    const bool u_canon = only < ru;
-                    const bool u_lb = u_canon ? fu == 1u : fu == 2u;
-                    if (d2 == 1 && !u_lb) nx = (uint16_t)(2u * (vu & 0xffffu) + (u_canon ? 0u : 1u));
-                }
+            KT only = 0;
+            int64_t s_only = -1;
+            const int d = alive_succ(t, v, k, only, s_only);
+            uint16_t code = d == 0 ? kNone16 : kMulti16;
+            if (d == 1) {
+                const KT ru = K::rc(only, k);
+                code = (uint16_t)(2u * (t.vals[s_only] & 0xffffu) + (only < ru ? 0u : 1u));
             }
-            S.succ[u] = nx;
-            S.bflag[u] = (uint8_t)((lb ? 1u : 0u) | (rb ? 2u : 0u));
+            S.succ[u] = code;
         }
         __syncthreads();  // the hash table is dead from here on
 
         // ---- list ranking by pointer jumping ----
         auto &R = S.u.r;
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) R.haspred[u] = 0;
-        __syncthreads();
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const uint16_t nx = S.succ[u];
+            const uint16_t c = S.succ[u];
+            uint16_t nx = kNone16;
+            if (c < kMulti16 && !(S.bflag[u] & 2u) && (uint32_t)(c >> 1) != (u >> 1) && S.succ[c ^ 1u] < kMulti16 &&
+                !(S.bflag[c] & 1u))
+                nx = c;
             R.jump[u] = nx == kNone16 ? (uint16_t)u : nx;
             R.rank[u] = nx == kNone16 ? 0 : 1;
-            if (nx != kNone16) R.haspred[nx] = 1;
+            R.haspred[u] = 0;
+        }
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
+            const uint16_t j = R.jump[u];
+            S.succ[u] = j == (uint16_t)u ? kNone16 : j;
+            if (j != (uint16_t)u) R.haspred[j] = 1;
         }
         __syncthreads();
         for (uint32_t len = 1; len < nn; len <<= 1) {
