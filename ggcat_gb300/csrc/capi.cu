@@ -110,6 +110,7 @@ struct ggcat_gpu_ctx {
     DevBuf<uint64_t> tkeys;
     DevBuf<uint32_t> tvals;
     DevBuf<uint8_t> tvis;
+    DevBuf<uint32_t> tlist;  // created-entry lists of the M units
     DevBuf<uint8_t> out_bases;
     DevBuf<uint64_t> out_off;
     DevBuf<uint32_t> out_len;
@@ -370,6 +371,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->tkeys.ensure(pool * (wide ? 2 : 1)));
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
+    CK(ctx->tlist.ensure(pool));
     CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
 
@@ -431,7 +433,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->launches += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o,
                                            ctx->sms, s);
         ctx->launches += launch_merge_medium(a, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
-                                             ctx->tvis.p, o, ctx->sms, s);
+                                             ctx->tvis.p, ctx->tlist.p, o, ctx->sms, s);
         ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
                                                  ctx->tvals.p, ctx->tvis.p, ctx->sms, s);
         ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p,

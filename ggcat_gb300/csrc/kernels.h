@@ -86,8 +86,9 @@ int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigne
 int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                       MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms, cudaStream_t s);
 // Table keys are u64 (a.wide == 0) or u128 (a.wide == 1, 16-byte aligned) slots.
+// list: one u32 per pool slot (created-entry lists of the units)
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
-                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s);
+                        uint32_t *vals, uint8_t *vis, uint32_t *list, const MergeOut &o, int sms, cudaStream_t s);
 // grid-wide insert/extend/cycles over the units [0, *n_units_dev)
 int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigned long long *n_units_dev,
                        uint64_t n_units_host_hint, void *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,

@@ -431,7 +431,7 @@ struct TierCfg<u128, kTierW> {
 };
 template <>
 struct TierCfg<uint64_t, kTierM> {
-    static constexpr int NT = 512, kSlots = 0, kSurv = 6016, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 0, kSurv = 5632, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<u128, kTierM> {
@@ -453,8 +453,11 @@ struct SmemTableView {
     uint32_t vals[kSlots];  // count|flags<<30, then alive<<31|flags<<28|dense index
 };
 
+constexpr int kStageWords = 4;  // packed words staged per record (records spanning more read global memory)
+
 template <typename KT, int N, int NT>
 struct UnitSmemCommon {
+    uint64_t stage[NT][kStageWords];  // per lane: the packed words of its record (insert phase)
     KT sk[N];              // survivor canonical k-mers (dense order)
     uint16_t succ[2 * N];  // traversable successor of each oriented node
     uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
@@ -549,8 +552,8 @@ __device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
 template <typename KT, int kTier>
 __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kMinBlocks)
     merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
-                      KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, MergeUnit *spill, uint64_t max_units,
-                      MergeOut o) {
+                      KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, uint32_t *pool_list, MergeUnit *spill,
+                      uint64_t max_units, MergeOut o) {
     using Cfg = TierCfg<KT, kTier>;
     using Smem = UnitSmem<KT, kTier>;
     using K = KeyOps<KT>;
@@ -573,7 +576,9 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         const MergeUnit U = units[ui];
         uint32_t cap;
         Table<KT> t;
+        uint32_t *t_list = nullptr;  // M units: slots of the created entries (in creation order)
         if constexpr (kGlobalTable) {
+            t_list = pool_list + U.table_off;
             cap = U.table_cap;
             t = Table<KT>{pool_keys + U.table_off, pool_vals + U.table_off, pool_vis + U.table_off, cap};
         } else {
@@ -600,6 +605,8 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         }
         __syncthreads();
 
+        const uint64_t n_items = U.rec_end - U.rec_begin;
+
         // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes 32 records at a
         //      time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is
         //      found from the mask of record starts in the current 32-k-mer window, so the
@@ -609,16 +616,28 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
             const unsigned full = 0xffffffffu;
             bool stop = false;
-            for (uint64_t rb = U.rec_begin + (uint64_t)wid * 32; rb < U.rec_end && !stop; rb += (uint64_t)NW * 32) {
-                const uint64_t r = rb + lane;
+            for (uint64_t ib = (uint64_t)wid * 32; ib < n_items && !stop; ib += (uint64_t)NW * 32) {
+                const uint64_t item = ib + lane;
                 uint64_t w0 = 0;
                 uint32_t fr = 0, nk = 0;
-                if (r < U.rec_end) {
-                    const SkRec rr = a.recs[r];
+                if (item < n_items) {
+                    const SkRec rr = a.recs[U.rec_begin + item];
                     w0 = rr.w0;
                     fr = rec_flags(rr) | (rec_rc(rr) << 2);
                     nk = rec_len(rr) - (uint32_t)k + 1;  // >= 1: records hold at least one k-mer
+                    // stage the record's packed words in shared memory (one round of independent
+                    // loads per 32 records instead of one dependent load per k-mer window)
+                    const uint64_t st = rec_start(rr);
+                    const uint64_t wb = st >> 5, we = (st + rec_len(rr) - 1) >> 5;
+                    if (we - wb < (uint64_t)kStageWords) {
+#pragma unroll
+                        for (int q = 0; q < kStageWords; q++)
+                            if (wb + q <= we) S.stage[threadIdx.x][q] = a.packed[wb + q];
+                    } else {
+                        fr |= 8u;  // long record: k-mers read from global memory
+                    }
                 }
+                __syncwarp();
                 uint32_t incl = nk;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
@@ -646,30 +665,46 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                     const uint64_t rw0 = __shfl_sync(full, w0, (int)ri);
                     const uint32_t rfr = __shfl_sync(full, fr, (int)ri);
                     const uint32_t rex = __shfl_sync(full, ex, (int)ri);
-                    if (!have) continue;
+                    int64_t sl = -1;
+                    bool created = false;
+                    uint32_t fbits = 0;
+                    if (have) {
                     const uint32_t off = j - rex;
                     const uint32_t last = (uint32_t)(rw0 >> 40) - (uint32_t)k;
-                    const uint32_t fl = rfr & 3u, rcf = rfr >> 2;
+                    const uint32_t fl = rfr & 3u, rcf = (rfr >> 2) & 1u;
                     // text-orientation included flags (begin <- stored end when reverse-complemented)
                     const uint32_t inc_begin = rcf ? (fl >> 1) & 1u : fl & 1u;
                     const uint32_t inc_end = rcf ? fl & 1u : (fl >> 1) & 1u;
-                    const KT fw = K::load(a.packed, (rw0 & ((1ull << 40) - 1)) + off, k);
+                    const uint64_t pos = (rw0 & ((1ull << 40) - 1)) + off;
+                    const KT fw = (rfr & 8u) ? K::load(a.packed, pos, k)
+                                             : K::load(S.stage[(threadIdx.x & ~31u) + ri],
+                                                       pos - ((rw0 & ((1ull << 40) - 1)) & ~31ull), k);
                     const KT rc = K::rc(fw, k);
                     const uint32_t isf = fw < rc ? 1u : 0u;
-                    int64_t sl;
-                    if (optimistic) {
-                        bool created;
+                    if (optimistic || kGlobalTable)
                         sl = tinsert_created(t, isf ? fw : rc, o.status, created);
-                        if (created) atomicAdd(&S.distinct, 1u);
-                    } else {
+                    else
                         sl = tinsert(t, isf ? fw : rc, o.status);
+                    const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
+                    fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
+                    }
+                    if (optimistic || kGlobalTable) {
+                        // created entries: counted (W spill test) and, for global tables, listed
+                        // so the survivor scan visits entries instead of every slot
+                        const unsigned cm = __ballot_sync(full, created);
+                        if (cm) {
+                            const int leader = __ffs(cm) - 1;
+                            uint32_t base = 0;
+                            if (lane == leader) base = atomicAdd(&S.distinct, (uint32_t)__popc(cm));
+                            base = __shfl_sync(full, base, leader);
+                            if (kGlobalTable && created) t_list[base + __popc(cm & ((1u << lane) - 1u))] = (uint32_t)sl;
+                        }
                     }
                     if (sl < 0) continue;
-                    const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
-                    const uint32_t fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
                     if (fbits) atomicOr(&t.vals[sl], fbits << 30);
                     atomicAdd(&t.vals[sl], 1u);
                 }
+                __syncwarp();  // the next batch overwrites this warp's staged words
             }
             __syncthreads();
         }
@@ -688,19 +723,21 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         }
 
         // ---- survivors (min-multiplicity filter): each warp scans a contiguous segment of
-        //      slots 32 at a time (coalesced), counting with ballots ----
+        //      slots (shared-memory tables) or of the created-entry list (global tables) 32 at
+        //      a time, counting with ballots ----
         constexpr int NW = NT / 32;
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        const uint32_t seg = (((cap + NW - 1) / NW) + 31) & ~31u;
-        const uint32_t seg_lo = min(cap, (uint32_t)wid * seg), seg_hi = min(cap, seg_lo + seg);
+        const uint32_t n_scan = kGlobalTable ? S.distinct : cap;
+        const uint32_t seg = (((n_scan + NW - 1) / NW) + 31) & ~31u;
+        const uint32_t seg_lo = min(n_scan, (uint32_t)wid * seg), seg_hi = min(n_scan, seg_lo + seg);
         // (an entry's count is >= 1 from its creation, so the value word alone tells empty
         // from occupied)
         uint32_t warp_surv = 0, warp_occ = 0;
         for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
-            const uint32_t sl = b0 + lane;
+            const uint32_t ix = b0 + lane;
             bool alive = false, occ = false;
-            if (sl < seg_hi) {
-                const uint32_t v = t.vals[sl];
+            if (ix < seg_hi) {
+                const uint32_t v = t.vals[kGlobalTable ? t_list[ix] : ix];
                 occ = v != 0;
                 alive = val_mult(v) >= min_mult;
             }
@@ -722,10 +759,11 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         {
             uint32_t base = __shfl_sync(0xffffffffu, warp_base, 0);
             for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
-                const uint32_t sl = b0 + lane;
+                const uint32_t ix = b0 + lane;
+                const uint32_t sl = ix < seg_hi ? (kGlobalTable ? t_list[ix] : ix) : 0u;
                 bool alive = false;
                 uint32_t v = 0;
-                if (sl < seg_hi) {
+                if (ix < seg_hi) {
                     v = t.vals[sl];
                     alive = val_mult(v) >= min_mult;
                 }
@@ -749,7 +787,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                         }
                     }
                 }
-                if (sl < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
+                if (ix < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
                 base += __popc(bm);
             }
             if (threadIdx.x == 0) S.n_surv = n_surv;
@@ -990,8 +1028,8 @@ int launch_classify_units(const unsigned long long *bin_off, const unsigned long
 
 template <typename KT, int kTier>
 static void merge_tier_t(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, KT *keys,
-                         uint32_t *vals, uint8_t *vis, MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms,
-                         cudaStream_t s) {
+                         uint32_t *vals, uint8_t *vis, uint32_t *list, MergeUnit *spill, uint64_t max_units,
+                         const MergeOut &o, int sms, cudaStream_t s) {
     using Cfg = TierCfg<KT, kTier>;
     static bool configured = false;
     const int smem = (int)sizeof(UnitSmem<KT, kTier>);
@@ -1000,15 +1038,16 @@ static void merge_tier_t(const MergeArgs &a, const MergeUnit *units, const unsig
         configured = true;
     }
     merge_unit_kernel<KT, kTier>
-        <<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(a, units, counters, keys, vals, vis, spill, max_units, o);
+        <<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(a, units, counters, keys, vals, vis, list, spill, max_units, o);
 }
 
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
-                        uint32_t *vals, uint8_t *vis, const MergeOut &o, int sms, cudaStream_t s) {
+                        uint32_t *vals, uint8_t *vis, uint32_t *list, const MergeOut &o, int sms, cudaStream_t s) {
     if (a.wide)
-        merge_tier_t<u128, kTierM>(a, units, counters, static_cast<u128 *>(keys), vals, vis, nullptr, 0, o, sms, s);
+        merge_tier_t<u128, kTierM>(a, units, counters, static_cast<u128 *>(keys), vals, vis, list, nullptr, 0, o, sms,
+                                   s);
     else
-        merge_tier_t<uint64_t, kTierM>(a, units, counters, static_cast<uint64_t *>(keys), vals, vis, nullptr, 0, o,
+        merge_tier_t<uint64_t, kTierM>(a, units, counters, static_cast<uint64_t *>(keys), vals, vis, list, nullptr, 0, o,
                                        sms, s);
     return 1;
 }
@@ -1016,18 +1055,19 @@ int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsign
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s) {
     if (a.wide)
-        merge_tier_t<u128, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
+        merge_tier_t<u128, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
     else
-        merge_tier_t<uint64_t, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
+        merge_tier_t<uint64_t, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
     return 1;
 }
 
 int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                       MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms, cudaStream_t s) {
     if (a.wide)
-        merge_tier_t<u128, kTierW>(a, units, counters, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
+        merge_tier_t<u128, kTierW>(a, units, counters, nullptr, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
     else
-        merge_tier_t<uint64_t, kTierW>(a, units, counters, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
+        merge_tier_t<uint64_t, kTierW>(a, units, counters, nullptr, nullptr, nullptr, nullptr, spill, max_units, o, sms,
+                                       s);
     return 1;
 }
 

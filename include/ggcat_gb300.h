@@ -40,7 +40,8 @@ extern "C" {
 typedef struct ggcat_gpu_ctx ggcat_gpu_ctx;
 
 typedef struct {
-    int32_t k;                /* k-mer length (this build: 3..32 for the device merge) */
+    int32_t k;                /* k-mer length: bucketing k <= 64; merge and link odd k <= 64 (u64 keys for
+                                 k <= 32, u128 keys above); colours and query k <= 32 */
     int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
     int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
     int32_t second_bits;      /* second-level bucket bits reported in superkmer records */
@@ -124,7 +125,8 @@ int ggcat_gpu_partial_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_
                                    uint64_t *n_bases);
 
 /* Surviving k-mers of the last merge (needs keep_kmers = 1): canonical 2-bit packed
- * k-mer (seq-hash layout, base i at bits 2i) and multiplicity.  A k-mer on a sub-bucket
+ * k-mer (seq-hash layout, base i at bits 2i) and multiplicity.  For k > 32 every k-mer takes
+ * two words of h_kmers (low, high), so h_kmers holds 2 * cap words.  A k-mer on a sub-bucket
  * boundary is reported once per sub-bucket.  Pass NULL to query the count. */
 int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint64_t *h_mult, uint64_t cap, uint64_t *n);
 
