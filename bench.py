@@ -52,6 +52,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--verify", action="store_true", help="check batched == per-bucket unitig sets (slow)")
     ap.add_argument("--no-query", action="store_true", help="skip the query-serving measurement")
+    ap.add_argument("--no-colored", action="store_true", help="skip the coloured build + query measurement")
+    ap.add_argument("--colors", type=int, default=256, help="genomes (colours) of the coloured workload")
     ap.add_argument("--query-genomes", type=int, default=16, help="member genomes of the queried graph")
     ap.add_argument("--queries", type=int, default=20000)
     ap.add_argument("--query-rate", type=float, default=20000.0, help="Poisson arrival rate (queries/s)")
@@ -206,6 +208,50 @@ def query_bench(args, ctx, torch, dev):
                            "wall_s": round(r1.wall_s, 3)},
         "results_identical_alone_vs_batched": same,
         "index_build_s": round(index_s, 3),
+    }
+
+
+def colored_bench(args, ctx, torch, dev):
+    """Coloured build (256 genomes x 4 Mbp from one ancestor, one colour each, k=31, 4096
+    buckets): device build, colour-subset dedup, then coloured query serving (per query and
+    colour, the number of query k-mers present in that colour)."""
+    from ggcat_gb300 import _native, serve, synth
+
+    w = synth.config_colored(n_genomes=args.colors)
+    p = _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=1, min_multiplicity=1,
+                            keep_kmers=True)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    res = {}
+    for rep_i in range(2):  # the first pass warms up (allocations)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.build_text(w.text, p, stream)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ctx.colors(w.seq_off, w.seq_color, args.colors, stream)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        st = ctx.stats()
+        res = {"build_e2e_ms": round((t1 - t0) * 1e3, 3), "ms_bucketize": round(st["ms_bucketize"], 3),
+               "ms_merge": round(st["ms_merge"], 3), "colors_ms": round((t2 - t1) * 1e3, 3)}
+    n_sub = int(ctx.subsets().shape[0])
+    st = ctx.stats()
+    ctx.query_index_colored()
+    genomes = [w.text[int(o):int(o) + int(ln)] for o, ln in zip(w.seq_off.tolist(), w.seq_len.tolist())]
+    qt, qo, ql, arr = synth.query_workload(genomes, args.queries, rate_per_s=args.query_rate)
+    serve.serve(ctx, 31, qt, qo[:200], ql[:200], np.zeros(200), slots=4, colored=True)
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = int(max(1 << 22, min(free // 16, 256 << 20)))
+    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget, colored=True)
+    return {
+        "workload": w.name, "bases": int(w.bases), "colors": args.colors,
+        "build": {**res, "device_gbases_per_s": round(w.bases / ((res["ms_bucketize"] + res["ms_merge"]) * 1e-3) / 1e9, 3),
+                  "distinct_kmers": int(st["distinct_kmers"]), "surviving_kmers": int(st["surviving_kmers"]),
+                  "color_subsets": n_sub},
+        "query": {"queries": int(len(qo)), "query_kmers": int(rb.kmers), "arrival_rate_per_s": args.query_rate,
+                  "kmers_per_s": round(rb.kmers_per_s, 1), "p50_ms": round(rb.pct_ms(50), 3),
+                  "p99_ms": round(rb.pct_ms(99), 3), "batches": rb.batches, "max_batch_kmers": budget,
+                  "color_hits_total": int(rb.color_totals.sum())},
     }
 
 
@@ -367,6 +413,9 @@ def run_gpu(args):
     query = None
     if rank == 0 and not args.no_query:
         query = query_bench(args, ctx, torch, dev)
+    colored = None
+    if rank == 0 and not args.no_colored:
+        colored = colored_bench(args, ctx, torch, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -407,6 +456,7 @@ def run_gpu(args):
             "roofline_bucketing": roofline_bucketing,
             "cpu_baseline": cpu,
             "query": query,
+            "colored": colored,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -420,7 +470,8 @@ def run_gpu(args):
 def main():
     args = _args()
     if args.workload != "skewed":
-        args.no_query = True  # the query section serves a k=31 graph
+        args.no_query = True  # the query and coloured sections use k=31 graphs
+        args.no_colored = True
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

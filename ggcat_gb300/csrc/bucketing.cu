@@ -116,6 +116,13 @@ __device__ __forceinline__ uint64_t nt_value(uint64_t fw, uint64_t rc) {
 
 constexpr uint64_t kInf = ~0ull;
 
+// Superkmers found by a lane wait in a per-lane queue in shared memory (column-major, one
+// column per thread) and are built, counted and appended together by the whole warp: a split
+// happens every ~(w+1)/2 positions per lane, so emitting at once would run the record code on
+// almost every step with one or two lanes active.
+constexpr int kEmitQueue = 8;   // entries per lane
+constexpr int kEmitDrain = 4;   // the warp drains when a lane holds this many
+
 // Single pass: superkmer records are appended to a staging array (warp-aggregated slot
 // reservation) and counted per sub-bin; partition_kernel then scatters them by sub-bin.
 __global__ void __launch_bounds__(256)
@@ -129,7 +136,10 @@ __global__ void __launch_bounds__(256)
     const int wn = k - m;
     const int nthr = blockDim.x;
     uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                                  // [wn][nthr]
-    uint8_t *blk_meta = reinterpret_cast<uint8_t *>(blk_v + (size_t)wn * nthr);              // [wn][nthr]
+    uint64_t *q_w0 = blk_v + (size_t)wn * nthr;                                              // [kEmitQueue][nthr]
+    uint64_t *q_raw = q_w0 + (size_t)kEmitQueue * nthr;                                      // [kEmitQueue][nthr]
+    uint32_t *q_meta = reinterpret_cast<uint32_t *>(q_raw + (size_t)kEmitQueue * nthr);      // [kEmitQueue][nthr]
+    uint8_t *blk_meta = reinterpret_cast<uint8_t *>(q_meta + (size_t)kEmitQueue * nthr);     // [wn][nthr]
     if (threadIdx.x < 4) {
         uint32_t c = threadIdx.x;
         uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
@@ -169,63 +179,76 @@ __global__ void __launch_bounds__(256)
         uint32_t vw = 0;
         const uint64_t p_end = min(x1 + (uint64_t)k - 1, n + 1);
 
-        uint64_t rec_w0 = 0, rec_w1 = 0;
-        bool has_rec = false;
-        // append the pending record of every lane that has one: one atomic per warp
-        auto flush = [&]() {
+        int qlen = 0;  // superkmers waiting in this lane's queue
+        // build, count and append one queued superkmer of every lane that has one, until all
+        // queues of the warp are empty; one stage-cursor atomic per round
+        auto drain = [&]() {
             const unsigned am = __activemask();
-            const unsigned bm = __ballot_sync(am, has_rec);
-            if (bm == 0) return;
             const int lane = (int)(threadIdx.x & 31);
-            const int leader = __ffs(bm) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(stage_cursor, (unsigned long long)__popc(bm));
-            base = __shfl_sync(am, base, leader);
-            if (has_rec) {
-                const unsigned long long idx = base + (unsigned long long)__popc(bm & ((1u << lane) - 1u));
-                if (idx < stage_cap) {
-                    SkRec r;
-                    r.w0 = rec_w0;
-                    r.w1 = rec_w1;
-                    stage[idx] = r;
-                } else {
-                    atomicOr(status, kStatusStageOverflow);
+            for (;;) {
+                const unsigned bm = __ballot_sync(am, qlen > 0);
+                if (bm == 0) break;
+                SkRec r{0, 0};
+                if (qlen > 0) {
+                    qlen--;
+                    const size_t qi = (size_t)qlen * nthr + threadIdx.x;
+                    const uint64_t w0 = q_w0[qi], raw = q_raw[qi];
+                    const uint32_t meta = q_meta[qi];
+                    // superkmer [start, start + len) with the minimizer of value raw at offset
+                    // moff (lib.rs:207-267)
+                    const uint32_t len = (uint32_t)(w0 >> 40);
+                    const uint32_t moff = meta & 0xffffffu, mfw = (meta >> 24) & 1u;
+                    const uint32_t inc_first = (meta >> 25) & 1u, inc_last = (meta >> 26) & 1u;
+                    uint32_t bucket, rcf, pos;
+                    if ((raw & 1ull) == 0) {
+                        bucket = dup_bucket;
+                        rcf = 0;
+                        pos = 0;
+                    } else {
+                        rcf = (canonical && !mfw) ? 1u : 0u;
+                        bucket = (uint32_t)((raw >> 1) & bmask);  // get_bucket(0, b, h), cn_nthash.rs:135-142
+                        pos = rcf ? len - (moff + (uint32_t)m) : moff;
+                    }
+                    const uint32_t second = (uint32_t)((raw >> (bbits + 1)) & smask);
+                    const uint32_t sub = (uint32_t)((raw >> (bbits + 1)) & fmask);
+                    const uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
+                    const uint64_t bin = ((uint64_t)bucket << fbits) | sub;
+                    atomicAdd(&bin_count[bin], 1ull);
+                    atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
+                    r.w0 = w0;
+                    r.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
+                           ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
                 }
-                has_rec = false;
+                const int leader = __ffs(bm) - 1;
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(stage_cursor, (unsigned long long)__popc(bm));
+                base = __shfl_sync(am, base, leader);
+                if ((bm >> lane) & 1u) {
+                    const unsigned long long idx = base + (unsigned long long)__popc(bm & ((1u << lane) - 1u));
+                    if (idx < stage_cap)
+                        stage[idx] = r;
+                    else
+                        atomicOr(status, kStatusStageOverflow);
+                }
             }
         };
 
         auto emit = [&](uint64_t c, bool is_final) {
-            // superkmer [c_prev - 1, c + k - 1) with the minimizer of the window before c
-            // (split) or of the last window (final): lib.rs:207-267
-            uint64_t start = c_prev - 1, end = c + (uint64_t)k - 1;
-            uint32_t len = (uint32_t)(end - start);
-            uint32_t inc_first = first_sk ? 1u : 0u, inc_last = is_final ? 1u : 0u;
-            uint32_t bucket, rcf, pos;
-            if ((prev_raw & 1ull) == 0) {
-                bucket = dup_bucket;
-                rcf = 0;
-                pos = 0;
-            } else {
-                rcf = (canonical && !prev_fw) ? 1u : 0u;
-                bucket = (uint32_t)((prev_raw >> 1) & bmask);  // get_bucket(0, b, h), cn_nthash.rs:135-142
-                pos = rcf ? (uint32_t)(end - (prev_pos + (uint64_t)m)) : (uint32_t)(prev_pos - start);
-            }
-            uint32_t second = (uint32_t)((prev_raw >> (bbits + 1)) & smask);
-            uint32_t sub = (uint32_t)((prev_raw >> (bbits + 1)) & fmask);
-            uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
-            uint64_t bin = ((uint64_t)bucket << fbits) | sub;
+            // queue the superkmer [c_prev - 1, c + k - 1) with the minimizer of the window
+            // before c (split) or of the last window (final)
+            const uint64_t start = c_prev - 1, end = c + (uint64_t)k - 1;
+            const size_t qi = (size_t)qlen * nthr + threadIdx.x;
+            q_w0[qi] = start | ((end - start) << 40);
+            q_raw[qi] = prev_raw;
+            q_meta[qi] = (uint32_t)((prev_pos - start) & 0xffffffu) | (prev_fw << 24) | ((first_sk ? 1u : 0u) << 25) |
+                         ((is_final ? 1u : 0u) << 26);
+            qlen++;
             first_sk = false;
-            atomicAdd(&bin_count[bin], 1ull);
-            atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
-            rec_w0 = start | ((uint64_t)len << 40);
-            rec_w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
-                     ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
-            has_rec = true;
         };
 
         for (uint64_t p = xb; p < p_end; p++) {
-            flush();  // the record emitted in the previous iteration (loop stays in lockstep)
+            // the warp drains its queues once a lane's queue is half full (loop stays in lockstep)
+            if (__any_sync(__activemask(), qlen >= kEmitDrain)) drain();
             const uint64_t wi = p >> 5;
             if (wi != cur_word) {
                 cur_word = wi;
@@ -339,7 +362,7 @@ __global__ void __launch_bounds__(256)
             prev_fw = cur_fw;
             prev_valid = true;
         }
-        flush();
+        drain();
         if (!failed) return;
         if (xb == 0) break;  // cannot look back further
         lb *= 4;
@@ -472,7 +495,7 @@ int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, 
     uint64_t threads = (n + chunk - 1) / chunk;
     if (threads == 0) return 0;
     const int tpb = wn <= 24 ? 256 : 128;
-    const size_t smem = (size_t)wn * tpb * 9;
+    const size_t smem = (size_t)wn * tpb * 9 + (size_t)kEmitQueue * tpb * 20;
     static bool configured = false;
     if (!configured) {
         cudaFuncSetAttribute(bucketize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

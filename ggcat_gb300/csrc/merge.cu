@@ -522,20 +522,23 @@ __device__ __forceinline__ uint32_t block_scan_u32(uint32_t v, uint32_t *warp_tm
 
 __device__ __forceinline__ bool val_alive(uint32_t v) { return (v >> 31) != 0; }
 
-// number of alive successors of oriented v; *only / *s_only receive the last one found
+// number of alive successors of oriented v (rv = its reverse complement); *s_only receives
+// the slot of the last one found and *fw_only whether it is in canonical orientation.  The
+// successor's reverse complement follows from rv: rc(v[1..] + b) = comp(b) + rc(v)[..k-1].
 template <typename KT>
-__device__ __forceinline__ int alive_succ(const Table<KT> &t, KT v, int k, KT &only, int64_t &s_only) {
+__device__ __forceinline__ int alive_succ(const Table<KT> &t, KT v, KT rv, int k, int64_t &s_only, bool &fw_only) {
     int d = 0;
     const KT bse = v >> 2;
+    const KT rbase = (rv << 2) & KeyOps<KT>::mask(k);
 #pragma unroll
     for (uint32_t b = 0; b < 4; b++) {
         const KT w = bse | ((KT)b << (2 * (k - 1)));
-        const KT rw = KeyOps<KT>::rc(w, k);
+        const KT rw = rbase | (KT)(b ^ 2u);
         const int64_t sw = tfind(t, w < rw ? w : rw);
         if (sw >= 0 && val_alive(t.vals[sw])) {
             d++;
-            only = w;
             s_only = sw;
+            fw_only = w < rw;
         }
     }
     return d;
@@ -804,15 +807,13 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         //      mirror of w has one successor) and w is another k-mer. ----
         for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
             const KT x = S.sk[u >> 1];
-            const KT v = (u & 1) ? K::rc(x, k) : x;
-            KT only = 0;
+            const KT rx = K::rc(x, k);
             int64_t s_only = -1;
-            const int d = alive_succ(t, v, k, only, s_only);
+            bool fw_only = true;
+            const bool odd = (u & 1) != 0;  // select the operands, not the call: lanes alternate parity
+            const int d = alive_succ(t, odd ? rx : x, odd ? x : rx, k, s_only, fw_only);
             uint16_t code = d == 0 ? kNone16 : kMulti16;
-            if (d == 1) {
-                const KT ru = K::rc(only, k);
-                code = (uint16_t)(2u * (t.vals[s_only] & 0xffffu) + (only < ru ? 0u : 1u));
-            }
+            if (d == 1) code = (uint16_t)(2u * (t.vals[s_only] & 0xffffu) + (fw_only ? 0u : 1u));
             S.succ[u] = code;
         }
         __syncthreads();  // the hash table is dead from here on
@@ -836,15 +837,18 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             if (j != (uint16_t)u) R.haspred[j] = 1;
         }
         __syncthreads();
+        // (stops as soon as every jump reaches its path end: log2 of the longest path rounds)
         for (uint32_t len = 1; len < nn; len <<= 1) {
             uint16_t nj[(kMaxSurv * 2 + NT - 1) / NT];
             uint16_t nr[(kMaxSurv * 2 + NT - 1) / NT];
             int c = 0;
+            int moved = 0;
             for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
                 const uint16_t j = R.jump[u];
                 const uint32_t rr = (uint32_t)R.rank[u] + R.rank[j];
                 nr[c] = (uint16_t)(rr > 0xfffeu ? 0xfffeu : rr);
                 nj[c] = R.jump[j];
+                moved |= nj[c] != j;
             }
             __syncthreads();
             c = 0;
@@ -852,7 +856,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                 R.rank[u] = nr[c];
                 R.jump[u] = nj[c];
             }
-            __syncthreads();
+            if (!__syncthreads_or(moved)) break;
         }
 
         // ---- owner starts: one per path (the end with the smaller node, hashmap.rs walks a

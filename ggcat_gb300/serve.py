@@ -25,6 +25,7 @@ class ServeResult:
     kmers: int
     batches: int
     batch_sizes: list = field(default_factory=list)
+    color_totals: np.ndarray | None = None  # coloured index: per request, sum of its per-colour counts
 
     @property
     def kmers_per_s(self) -> float:
@@ -46,15 +47,17 @@ def _pack(queries: list) -> tuple:
 
 
 def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arrivals: np.ndarray, slots: int = 4,
-          max_batch_kmers: int = 64 << 20, one_per_launch: bool = False) -> ServeResult:
+          max_batch_kmers: int = 64 << 20, one_per_launch: bool = False, colored: bool = False) -> ServeResult:
     """Replays the queries (text layout: query i = text[off[i] : off[i] + lens[i]], arrivals
-    non-decreasing, in seconds from the start) through the server."""
+    non-decreasing, in seconds from the start) through the server.  With a coloured index,
+    ``colored=True`` also reads every batch's per-colour counts back."""
     n = len(off)
     off = np.asarray(off, np.uint64)
     lens = np.asarray(lens, np.uint64)
     nk = np.maximum(lens.astype(np.int64) - (k - 1), 0)
     cum = np.concatenate([[0], np.cumsum(nk)])
     matched = np.zeros(n, np.uint64)
+    ctot = np.zeros(n, np.uint64) if colored else None
     done_t = np.zeros(n)
     inflight: dict[int, tuple] = {}
     head = 0  # next request not yet submitted (arrival order = index order)
@@ -67,6 +70,8 @@ def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arri
                 a, b = inflight.pop(s)
                 res = ctx.query_wait(s)
                 matched[a:b] = res
+                if colored:
+                    ctot[a:b] = ctx.query_color_counts(s).sum(axis=1)
                 done_t[a:b] = time.perf_counter() - t0
         now = time.perf_counter() - t0
         arrived = int(np.searchsorted(arrivals, now, side="right"))
@@ -91,4 +96,4 @@ def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arri
             if wait > 0:
                 time.sleep(min(wait, 0.0005))
     wall = time.perf_counter() - t0
-    return ServeResult(matched, done_t - arrivals, wall, int(nk.sum()), batches, sizes)
+    return ServeResult(matched, done_t - arrivals, wall, int(nk.sum()), batches, sizes, ctot)

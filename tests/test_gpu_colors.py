@@ -83,3 +83,20 @@ def test_colored_query_counts_match_oracle(built):
     assert (matched == em).all()
     assert (counts == epc).all()
     assert epc.sum() > 0
+
+
+def test_colored_serving_matches_direct_batch(built):
+    """The continuous-batching loop over a coloured index returns, per query, the same
+    per-colour totals as one direct batch (and as the oracle)."""
+    ctx, r, text, off, ln, col, gs, nc = built
+    ctx.query_index_colored()
+    rng = np.random.default_rng(9)
+    queries, arrivals = synth.query_stream(gs, 40, rng, min_len=40, max_len=5000, rate_per_s=5000.0)
+    qt, qo, ql = serve._pack(queries)
+    res = serve.serve(ctx, 31, qt, qo, ql, arrivals, slots=3, max_batch_kmers=3000, colored=True)
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    em, _, epc = oracle.query(lo, hi, qt, qo, ql, 31, gc_off=coff, gc_colors=ccol, ncolors=nc)
+    assert (res.matched == em).all()
+    assert (res.color_totals == epc.sum(axis=1)).all()
+    assert res.batches > 1
