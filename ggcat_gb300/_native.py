@@ -56,6 +56,8 @@ class Stats(C.Structure):
         ("ms_link", C.c_double),
         ("distinct_kmers", C.c_uint64),
         ("merge_units_spilled", C.c_uint64),
+        ("merge_units_ext_global", C.c_uint64),
+        ("merge_units_walk", C.c_uint64),
     ]
 
 

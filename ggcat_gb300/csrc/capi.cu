@@ -111,6 +111,7 @@ struct ggcat_gpu_ctx {
     DevBuf<uint32_t> tvals;
     DevBuf<uint8_t> tvis;
     DevBuf<uint32_t> tlist;  // created-entry lists of the M units
+    DevBuf<uint8_t> ext_scratch;  // per-CTA extension scratch of units with many survivors
     DevBuf<uint8_t> out_bases;
     DevBuf<uint64_t> out_off;
     DevBuf<uint32_t> out_len;
@@ -372,10 +373,20 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
     CK(ctx->tlist.ensure(pool));
+    // extension scratch: S/W CTAs (2 per SM) up to kExtCapShared survivors each, M CTAs (1 per
+    // SM) up to kExtCapMedium (the instances of an M unit); the tiers run one after another
+    const uint64_t bps = merge_ext_bytes_per_survivor(wide);
+    const uint64_t stride_sw = ((uint64_t)kExtCapShared * bps + 255) & ~255ull;
+    const uint64_t stride_m = ((uint64_t)kExtCapMedium * bps + 255) & ~255ull;
+    CK(ctx->ext_scratch.ensure(std::max<uint64_t>(2ull * ctx->sms * stride_sw, (uint64_t)ctx->sms * stride_m)));
     CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
 
-    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers, wide};
+    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k,           p->min_multiplicity, p->keep_kmers, wide,
+                ctx->ext_scratch.p, stride_sw, kExtCapShared};
+    MergeArgs am = a;
+    am.ext_stride = stride_m;
+    am.ext_cap = kExtCapMedium;
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
@@ -432,7 +443,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
         ctx->launches += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o,
                                            ctx->sms, s);
-        ctx->launches += launch_merge_medium(a, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
+        ctx->launches += launch_merge_medium(am, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
                                              ctx->tvis.p, ctx->tlist.p, o, ctx->sms, s);
         ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
                                                  ctx->tvals.p, ctx->tvis.p, ctx->sms, s);
@@ -455,6 +466,8 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->stats.merge_units_small = cnt[kCntSmall];
         ctx->stats.merge_units_large = cnt[kCntWide] + cnt[kCntMedium] + cnt[kCntLarge] - cnt[kCntSpilled];
         ctx->stats.merge_units_spilled = cnt[kCntSpilled];
+        ctx->stats.merge_units_ext_global = cnt[kCntExtGlobal];
+        ctx->stats.merge_units_walk = cnt[kCntWalk] + cnt[kCntLarge];
         if (cnt[kCntSlots] > pool) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
     }
     *st_out = st;

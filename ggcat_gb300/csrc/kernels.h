@@ -50,7 +50,18 @@ struct MergeArgs {
     int min_mult;
     int keep_kmers;
     int wide;  // 0: u64 keys (k <= 32); 1: u128 keys (k <= 64)
+    // per-CTA global scratch of the extension phase for units with more survivors than the
+    // shared-memory arrays hold (CTA i uses ext_scratch + i * ext_stride, up to ext_cap survivors)
+    uint8_t *ext_scratch;
+    uint64_t ext_stride;
+    uint32_t ext_cap;
 };
+
+// bytes of extension scratch per survivor (keys of key_bytes, 2 oriented nodes of 30 bytes)
+inline uint64_t merge_ext_bytes_per_survivor(int wide) { return (wide ? 16 : 8) + 60; }
+// survivors per CTA the extension scratch is sized for: S and W tiers / M tier
+constexpr uint32_t kExtCapShared = 8192;
+constexpr uint32_t kExtCapMedium = 1u << 18;
 
 // merge counters (device array of 16 u64)
 enum : int {
@@ -67,6 +78,8 @@ enum : int {
     kCntSpilled = 10,     // W units moved to the M tier
     kCntWide = 11,        // number of W units
     kCntWideHead = 12,    // work-queue head of W units
+    kCntExtGlobal = 13,   // units extended with the global-memory scratch arrays
+    kCntWalk = 14,        // units extended by the per-thread walk fallback
 };
 
 constexpr int kSmallSlots = 4096;     // shared-memory table capacity of one merge CTA

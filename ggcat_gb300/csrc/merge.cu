@@ -455,6 +455,12 @@ struct SmemTableView {
 
 constexpr int kStageWords = 4;  // packed words staged per record (records spanning more read global memory)
 
+// block-shared scalars of the extension phase
+struct ExtShared {
+    uint32_t n_surv, loc_bases, loc_count, ok;
+    unsigned long long gbase, gidx;
+};
+
 template <typename KT, int N, int NT>
 struct UnitSmemCommon {
     uint64_t stage[NT][kStageWords];  // per lane: the packed words of its record (insert phase)
@@ -463,9 +469,8 @@ struct UnitSmemCommon {
     uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
     uint32_t warp_tmp[NT / 32 + 1];
     uint64_t unit;
-    uint32_t n_surv, loc_bases, loc_count, ok;
     uint32_t distinct;  // entries created (optimistic units)
-    unsigned long long gbase, gidx;
+    ExtShared x;
 };
 template <typename KT, int kTier, bool kShared = (kTier != kTierM)>
 struct UnitSmem;
@@ -550,6 +555,277 @@ __device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
     return (u & 1) ? KeyOps<KT>::rc(x, k) : x;
 }
 
+// Arrays of the extension phase of one unit: the survivors in dense order, and per oriented
+// node u = 2*dense + (0 canonical, 1 reverse complement) the successor code, boundary sides,
+// pointer-jumping state and emission slots.  IT is the node index type: u16 for the arrays in
+// shared memory, u32 for the per-CTA scratch in global memory that units with more survivors
+// than the shared-memory arrays hold use.
+template <typename KT, typename IT>
+struct ExtArrays {
+    KT *sk;
+    IT *succ;
+    uint8_t *bflag;   // bit0 left boundary, bit1 right boundary (oriented)
+    IT *jump, *rank;
+    IT *jump2, *rank2;  // second pointer-jumping buffer (global scratch; the shared path uses registers)
+    uint32_t *offs;   // local base offset of owner starts
+    IT *uidx;         // local unitig index of owner starts
+    uint8_t *haspred;
+};
+
+// Global scratch of one CTA for up to `cap` survivors: keys, then seven u32 and two u8 arrays
+// of 2*cap oriented nodes.
+__host__ __device__ constexpr uint64_t ext_bytes_per_survivor(uint64_t key_bytes) { return key_bytes + 2 * (7 * 4 + 2); }
+
+template <typename KT>
+__device__ __forceinline__ ExtArrays<KT, uint32_t> ext_global_arrays(uint8_t *base, uint32_t cap) {
+    ExtArrays<KT, uint32_t> A;
+    const size_t nn = 2 * (size_t)cap;
+    A.sk = reinterpret_cast<KT *>(base);
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + sizeof(KT) * (size_t)cap);
+    A.succ = w;
+    A.jump = w + nn;
+    A.rank = w + 2 * nn;
+    A.jump2 = w + 3 * nn;
+    A.rank2 = w + 4 * nn;
+    A.offs = w + 5 * nn;
+    A.uidx = w + 6 * nn;
+    uint8_t *b = reinterpret_cast<uint8_t *>(w + 7 * nn);
+    A.bflag = b;
+    A.haspred = b + nn;
+    return A;
+}
+
+// Extension of one unit after the survivor count (the extension rules of
+// try_extend_function, hashmap.rs:162-297): dense numbering of the survivors, successor of
+// every oriented node, list ranking by pointer jumping, emission of every path once (from the
+// end with the smaller node) and of every cycle once.  All threads of the CTA call it.
+//   list_scan: the survivor scan visits t_list[seg] (created-entry list) instead of slots
+//   warp_base: this warp's first dense index (lane 0 of the block scan of survivor counts)
+//   kRegJ:     per-thread register buffer of the shared-memory pointer jumping
+template <typename KT, typename IT, int NT, int kRegJ, bool kGlobalArr>
+__device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *t_list, bool list_scan,
+                                            uint32_t seg_lo, uint32_t seg_hi, uint32_t warp_base, uint32_t n_surv,
+                                            const ExtArrays<KT, IT> &A, ExtShared &X, int k, uint32_t min_mult,
+                                            int keep_kmers, const MergeOut &o) {
+    using K = KeyOps<KT>;
+    constexpr IT kNone = (IT)~(IT)0;
+    constexpr IT kMulti = (IT)(kNone - 1);
+    constexpr uint32_t kIdxMask = sizeof(IT) == 2 ? 0xffffu : 0x0fffffffu;
+    const int lane = threadIdx.x & 31;
+
+    // dense numbering in slot order; vals become alive<<31 | flags<<28 | dense index
+    {
+        uint32_t base = __shfl_sync(0xffffffffu, warp_base, 0);
+        for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
+            const uint32_t ix = b0 + lane;
+            const uint32_t sl = ix < seg_hi ? (list_scan ? t_list[ix] : ix) : 0u;
+            bool alive = false;
+            uint32_t v = 0;
+            if (ix < seg_hi) {
+                v = t.vals[sl];
+                alive = val_mult(v) >= min_mult;
+            }
+            const unsigned bm = __ballot_sync(0xffffffffu, alive);
+            const uint32_t idx = base + __popc(bm & ((1u << lane) - 1u));
+            if (alive) {
+                const KT key = t.keys[sl];
+                A.sk[idx] = key;
+                // boundary sides of both orientations (MapEntry flags in canonical
+                // orientation: 1 = left side ignored, 2 = right side ignored)
+                const uint32_t fv = v >> 30;
+                A.bflag[2 * idx] = (uint8_t)((fv == 1u ? 1u : 0u) | (fv == 2u ? 2u : 0u));
+                A.bflag[2 * idx + 1] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
+                if (keep_kmers) {
+                    const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
+                    if (di < o.kmer_cap) {
+                        K::store(o.kmer_keys, di, key);
+                        o.kmer_mult[di] = val_mult(v);
+                    } else {
+                        atomicOr(o.status, kStatusKmerOverflow);
+                    }
+                }
+            }
+            if (ix < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
+            base += __popc(bm);
+        }
+        if (threadIdx.x == 0) X.n_surv = n_surv;
+        __syncthreads();
+    }
+    const uint32_t ns = X.n_surv;
+    const uint32_t nn = 2 * ns;
+
+    // ---- successors.  Degrees first: per survivor, the surviving successors of both
+    //      orientations (4 probes each); code = unique successor node, kNone (none) or kMulti.
+    //      A node u -> w is traversable iff u's right side and w's left side are no bucket
+    //      boundary, w is u's only successor, u is w's only predecessor (the mirror of w has
+    //      one successor) and w is another k-mer. ----
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        const KT x = A.sk[u >> 1];
+        const KT rx = K::rc(x, k);
+        int64_t s_only = -1;
+        bool fw_only = true;
+        const bool odd = (u & 1) != 0;  // select the operands, not the call: lanes alternate parity
+        const int d = alive_succ(t, odd ? rx : x, odd ? x : rx, k, s_only, fw_only);
+        IT code = d == 0 ? kNone : kMulti;
+        if (d == 1) code = (IT)(2u * (t.vals[s_only] & kIdxMask) + (fw_only ? 0u : 1u));
+        A.succ[u] = code;
+    }
+    __syncthreads();  // the hash table is dead from here on
+
+    // ---- list ranking by pointer jumping ----
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        const IT c = A.succ[u];
+        IT nx = kNone;
+        if (c < kMulti && !(A.bflag[u] & 2u) && (uint32_t)(c >> 1) != (u >> 1) && A.succ[c ^ 1u] < kMulti &&
+            !(A.bflag[c] & 1u))
+            nx = c;
+        A.jump[u] = nx == kNone ? (IT)u : nx;
+        A.rank[u] = nx == kNone ? (IT)0 : (IT)1;
+        A.haspred[u] = 0;
+    }
+    __syncthreads();
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        const IT j = A.jump[u];
+        A.succ[u] = j == (IT)u ? kNone : j;
+        if (j != (IT)u) A.haspred[j] = 1;
+    }
+    __syncthreads();
+    IT *J = A.jump, *Rk = A.rank;
+    // (stops as soon as every jump reaches its path end: log2 of the longest path rounds)
+    if constexpr (kGlobalArr) {
+        IT *Jn = A.jump2, *Rn = A.rank2;
+        for (uint32_t len = 1; len < nn; len <<= 1) {
+            int moved = 0;
+            for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+                const IT j = J[u];
+                const uint32_t rr = (uint32_t)Rk[u] + (uint32_t)Rk[j];
+                Rn[u] = (IT)(rr > (uint32_t)kMulti ? (uint32_t)kMulti : rr);
+                const IT nj = J[j];
+                Jn[u] = nj;
+                moved |= nj != j;
+            }
+            IT *tj = J, *tr = Rk;
+            J = Jn;
+            Rk = Rn;
+            Jn = tj;
+            Rn = tr;
+            if (!__syncthreads_or(moved)) break;
+        }
+    } else {
+        for (uint32_t len = 1; len < nn; len <<= 1) {
+            IT nj[kRegJ];
+            IT nr[kRegJ];
+            int c = 0;
+            int moved = 0;
+            for (uint32_t u = threadIdx.x; u < nn; u += NT, c++) {
+                const IT j = J[u];
+                const uint32_t rr = (uint32_t)Rk[u] + (uint32_t)Rk[j];
+                nr[c] = (IT)(rr > (uint32_t)kMulti ? (uint32_t)kMulti : rr);
+                nj[c] = J[j];
+                moved |= nj[c] != j;
+            }
+            __syncthreads();
+            c = 0;
+            for (uint32_t u = threadIdx.x; u < nn; u += NT, c++) {
+                Rk[u] = nr[c];
+                J[u] = nj[c];
+            }
+            if (!__syncthreads_or(moved)) break;
+        }
+    }
+
+    // ---- owner starts: one per path (the end with the smaller node, hashmap.rs walks a
+    //      path once), local offsets via shared atomics ----
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        if (A.haspred[u]) continue;
+        const IT e = J[u];
+        if (A.succ[e] != kNone) continue;  // on a cycle (handled below)
+        const uint32_t su = u >> 1, se = (uint32_t)e >> 1;
+        const bool owner = su < se || (su == se && (u & 1) == 0);
+        if (!owner) continue;
+        const uint32_t len = (uint32_t)k + (uint32_t)Rk[u];
+        A.offs[u] = atomicAdd(&X.loc_bases, len);
+        A.uidx[u] = (IT)atomicAdd(&X.loc_count, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        X.gbase = atomicAdd(&o.counters[kCntBases], (unsigned long long)X.loc_bases);
+        X.gidx = atomicAdd(&o.counters[kCntUnitigs], (unsigned long long)X.loc_count);
+        X.ok = (X.gbase + X.loc_bases <= o.bases_cap) && (X.gidx + X.loc_count <= o.u_cap);
+        if (!X.ok) atomicOr(o.status, kStatusOutOverflow);
+    }
+    __syncthreads();
+    const bool ok = X.ok != 0;
+    const unsigned long long gbase = X.gbase, gidx = X.gidx;
+
+    // ---- emission: every node of an owned path writes its base(s) ----
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        const uint32_t mu = u ^ 1u;                 // mirror node
+        const IT me = J[mu];                        // end of the mirror path = mirror of u's start
+        if (A.succ[me] != kNone) continue;          // cycle node
+        const uint32_t s0 = (uint32_t)me ^ 1u;      // start of u's path
+        const IT e = J[u];
+        const uint32_t ss = s0 >> 1, se = (uint32_t)e >> 1;
+        const bool owner = ss < se || (ss == se && (s0 & 1) == 0);
+        if (!owner || !ok) continue;
+        const uint32_t dist = Rk[mu];               // distance from the start
+        const unsigned long long off = gbase + A.offs[s0];
+        const KT v = oriented(A.sk, u, k);
+        if (dist == 0) {
+            for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
+            const unsigned long long ix = gidx + A.uidx[u];
+            o.u_off[ix] = off;
+            o.u_len[ix] = (uint32_t)k + (uint32_t)Rk[u];
+            o.u_flags[ix] = (uint8_t)((A.bflag[u] & 1u) | (A.bflag[e] & 2u));
+        } else {
+            o.bases[off + (uint32_t)k - 1 + dist] = base_char((uint32_t)(v >> (2 * (k - 1))));
+        }
+    }
+
+    // ---- cycles (rare): every node has a successor and a predecessor; the cycle and its
+    //      mirror are emitted once, from the smallest node of the pair ----
+    for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+        if (A.succ[J[u]] == kNone) continue;
+        uint32_t minc = u, minm = u ^ 1u, n = 1;
+        uint32_t cur = A.succ[u];
+        bool closed = false;
+        while (n <= nn) {
+            if (cur == (uint32_t)kNone) break;
+            if (cur == u) {
+                closed = true;
+                break;
+            }
+            minc = min(minc, cur);
+            minm = min(minm, cur ^ 1u);
+            cur = A.succ[cur];
+            n++;
+        }
+        if (!closed) {
+            atomicOr(o.status, kStatusWalkLimit);
+            continue;
+        }
+        if (u != minc || minc > minm) continue;
+        const uint64_t len = (uint64_t)k + n - 1;
+        const unsigned long long off = atomicAdd(&o.counters[kCntBases], len);
+        const unsigned long long ix = atomicAdd(&o.counters[kCntUnitigs], 1ull);
+        if (off + len > o.bases_cap || ix >= o.u_cap) {
+            atomicOr(o.status, kStatusOutOverflow);
+            continue;
+        }
+        KT v = oriented(A.sk, u, k);
+        for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
+        cur = A.succ[u];
+        for (uint32_t i = 1; i < n; i++) {
+            v = oriented(A.sk, cur, k);
+            o.bases[off + (uint32_t)k - 1 + i] = base_char((uint32_t)(v >> (2 * (k - 1))));
+            cur = A.succ[cur];
+        }
+        o.u_off[ix] = off;
+        o.u_len[ix] = (uint32_t)len;
+        o.u_flags[ix] = 4;
+    }
+}
+
 // One merge unit per CTA, persistent over a device work queue (tiers above).  All tiers use
 // the shared-memory list-ranking arrays for the extension.
 template <typename KT, int kTier>
@@ -601,9 +877,9 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             t.vis[i] = 0;
         }
         if (threadIdx.x == 0) {
-            S.n_surv = 0;
-            S.loc_bases = 0;
-            S.loc_count = 0;
+            S.x.n_surv = 0;
+            S.x.loc_bases = 0;
+            S.x.loc_count = 0;
             S.distinct = 0;
         }
         __syncthreads();
@@ -750,204 +1026,26 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         if (lane == 0 && warp_occ) atomicAdd(&o.counters[kCntDistinct], (unsigned long long)warp_occ);
         uint32_t n_surv;
         const uint32_t warp_base = block_scan_u32<NT>(lane == 0 ? warp_surv : 0u, S.warp_tmp, n_surv);
-        if (n_surv > (uint32_t)kMaxSurv) {
-            // walk fallback for a unit with more survivors than the ranking arrays hold
+        if (n_surv <= (uint32_t)kMaxSurv) {
+            ExtArrays<KT, uint16_t> A{S.sk,          S.succ,    S.bflag,      S.u.r.jump, S.u.r.rank,
+                                      nullptr,       nullptr,   S.u.r.offs,   S.u.r.uidx, S.u.r.haspred};
+            extend_unit<KT, uint16_t, NT, (kMaxSurv * 2 + NT - 1) / NT, false>(
+                t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, o);
+        } else if (a.ext_scratch != nullptr && n_surv <= a.ext_cap) {
+            // more survivors than the shared-memory arrays hold: the same ranking on this
+            // CTA's scratch in global memory
+            if (threadIdx.x == 0) atomicAdd(&o.counters[kCntExtGlobal], 1ull);
+            const ExtArrays<KT, uint32_t> A =
+                ext_global_arrays<KT>(a.ext_scratch + (size_t)blockIdx.x * a.ext_stride, a.ext_cap);
+            extend_unit<KT, uint32_t, NT, 1, true>(t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x,
+                                                  k, min_mult, a.keep_kmers, o);
+        } else {
+            // walk fallback (no scratch for this many survivors)
+            if (threadIdx.x == 0) atomicAdd(&o.counters[kCntWalk], 1ull);
             Graph<KT> g{t, k, min_mult};
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) extend_slot(g, sl, o, a.keep_kmers, min_mult);
             __syncthreads();
             for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
-            continue;
-        }
-        // dense numbering in slot order; vals become alive<<31 | flags<<28 | dense index
-        {
-            uint32_t base = __shfl_sync(0xffffffffu, warp_base, 0);
-            for (uint32_t b0 = seg_lo; b0 < seg_hi; b0 += 32) {
-                const uint32_t ix = b0 + lane;
-                const uint32_t sl = ix < seg_hi ? (kGlobalTable ? t_list[ix] : ix) : 0u;
-                bool alive = false;
-                uint32_t v = 0;
-                if (ix < seg_hi) {
-                    v = t.vals[sl];
-                    alive = val_mult(v) >= min_mult;
-                }
-                const unsigned bm = __ballot_sync(0xffffffffu, alive);
-                const uint32_t idx = base + __popc(bm & ((1u << lane) - 1u));
-                if (alive) {
-                    const KT key = t.keys[sl];
-                    S.sk[idx] = key;
-                    // boundary sides of both orientations (MapEntry flags in canonical
-                    // orientation: 1 = left side ignored, 2 = right side ignored)
-                    const uint32_t fv = v >> 30;
-                    S.bflag[2 * idx] = (uint8_t)((fv == 1u ? 1u : 0u) | (fv == 2u ? 2u : 0u));
-                    S.bflag[2 * idx + 1] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
-                    if (a.keep_kmers) {
-                        const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
-                        if (di < o.kmer_cap) {
-                            K::store(o.kmer_keys, di, key);
-                            o.kmer_mult[di] = val_mult(v);
-                        } else {
-                            atomicOr(o.status, kStatusKmerOverflow);
-                        }
-                    }
-                }
-                if (ix < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
-                base += __popc(bm);
-            }
-            if (threadIdx.x == 0) S.n_surv = n_surv;
-            __syncthreads();
-        }
-        const uint32_t ns = S.n_surv;
-        const uint32_t nn = 2 * ns;  // oriented nodes: u = 2*dense + (0 canonical, 1 reverse complement)
-
-        // ---- successors (the extension rules of try_extend_function, hashmap.rs:162-297).
-        //      Degrees first: per survivor, the surviving successors of both orientations
-        //      (4 probes each); code = unique successor node, kNone16 (none) or kMulti16.
-        //      A node u -> w is traversable iff u's right side and w's left side are no
-        //      bucket boundary, w is u's only successor, u is w's only predecessor (the
-        //      mirror of w has one successor) and w is another k-mer. ----
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const KT x = S.sk[u >> 1];
-            const KT rx = K::rc(x, k);
-            int64_t s_only = -1;
-            bool fw_only = true;
-            const bool odd = (u & 1) != 0;  // select the operands, not the call: lanes alternate parity
-            const int d = alive_succ(t, odd ? rx : x, odd ? x : rx, k, s_only, fw_only);
-            uint16_t code = d == 0 ? kNone16 : kMulti16;
-            if (d == 1) code = (uint16_t)(2u * (t.vals[s_only] & 0xffffu) + (fw_only ? 0u : 1u));
-            S.succ[u] = code;
-        }
-        __syncthreads();  // the hash table is dead from here on
-
-        // ---- list ranking by pointer jumping ----
-        auto &R = S.u.r;
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const uint16_t c = S.succ[u];
-            uint16_t nx = kNone16;
-            if (c < kMulti16 && !(S.bflag[u] & 2u) && (uint32_t)(c >> 1) != (u >> 1) && S.succ[c ^ 1u] < kMulti16 &&
-                !(S.bflag[c] & 1u))
-                nx = c;
-            R.jump[u] = nx == kNone16 ? (uint16_t)u : nx;
-            R.rank[u] = nx == kNone16 ? 0 : 1;
-            R.haspred[u] = 0;
-        }
-        __syncthreads();
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const uint16_t j = R.jump[u];
-            S.succ[u] = j == (uint16_t)u ? kNone16 : j;
-            if (j != (uint16_t)u) R.haspred[j] = 1;
-        }
-        __syncthreads();
-        // (stops as soon as every jump reaches its path end: log2 of the longest path rounds)
-        for (uint32_t len = 1; len < nn; len <<= 1) {
-            uint16_t nj[(kMaxSurv * 2 + NT - 1) / NT];
-            uint16_t nr[(kMaxSurv * 2 + NT - 1) / NT];
-            int c = 0;
-            int moved = 0;
-            for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
-                const uint16_t j = R.jump[u];
-                const uint32_t rr = (uint32_t)R.rank[u] + R.rank[j];
-                nr[c] = (uint16_t)(rr > 0xfffeu ? 0xfffeu : rr);
-                nj[c] = R.jump[j];
-                moved |= nj[c] != j;
-            }
-            __syncthreads();
-            c = 0;
-            for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x, c++) {
-                R.rank[u] = nr[c];
-                R.jump[u] = nj[c];
-            }
-            if (!__syncthreads_or(moved)) break;
-        }
-
-        // ---- owner starts: one per path (the end with the smaller node, hashmap.rs walks a
-        //      path once), local offsets via shared atomics ----
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            if (R.haspred[u]) continue;
-            const uint16_t e = R.jump[u];
-            if (S.succ[e] != kNone16) continue;  // on a cycle (handled below)
-            const uint32_t su = u >> 1, se = (uint32_t)e >> 1;
-            const bool owner = su < se || (su == se && (u & 1) == 0);
-            if (!owner) continue;
-            const uint32_t len = (uint32_t)k + R.rank[u];
-            R.offs[u] = atomicAdd(&S.loc_bases, len);
-            R.uidx[u] = (uint16_t)atomicAdd(&S.loc_count, 1u);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            S.gbase = atomicAdd(&o.counters[kCntBases], (unsigned long long)S.loc_bases);
-            S.gidx = atomicAdd(&o.counters[kCntUnitigs], (unsigned long long)S.loc_count);
-            S.ok = (S.gbase + S.loc_bases <= o.bases_cap) && (S.gidx + S.loc_count <= o.u_cap);
-            if (!S.ok) atomicOr(o.status, kStatusOutOverflow);
-        }
-        __syncthreads();
-        const bool ok = S.ok != 0;
-        const unsigned long long gbase = S.gbase, gidx = S.gidx;
-
-        // ---- emission: every node of an owned path writes its base(s) ----
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            const uint32_t mu = u ^ 1u;                 // mirror node
-            const uint16_t me = R.jump[mu];             // end of the mirror path = mirror of u's start
-            if (S.succ[me] != kNone16) continue;        // cycle node
-            const uint32_t s0 = (uint32_t)me ^ 1u;      // start of u's path
-            const uint16_t e = R.jump[u];
-            const uint32_t ss = s0 >> 1, se = (uint32_t)e >> 1;
-            const bool owner = ss < se || (ss == se && (s0 & 1) == 0);
-            if (!owner || !ok) continue;
-            const uint32_t dist = R.rank[mu];           // distance from the start
-            const unsigned long long off = gbase + R.offs[s0];
-            const KT v = oriented(S.sk, u, k);
-            if (dist == 0) {
-                for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
-                const unsigned long long ix = gidx + R.uidx[u];
-                o.u_off[ix] = off;
-                o.u_len[ix] = (uint32_t)k + R.rank[u];
-                o.u_flags[ix] = (uint8_t)((S.bflag[u] & 1u) | (S.bflag[e] & 2u));
-            } else {
-                o.bases[off + (uint32_t)k - 1 + dist] = base_char((uint32_t)(v >> (2 * (k - 1))));
-            }
-        }
-
-        // ---- cycles (rare): every node has a successor and a predecessor; the cycle and its
-        //      mirror are emitted once, from the smallest node of the pair ----
-        for (uint32_t u = threadIdx.x; u < nn; u += blockDim.x) {
-            if (S.succ[R.jump[u]] == kNone16) continue;
-            uint32_t minc = u, minm = u ^ 1u, n = 1;
-            uint32_t cur = S.succ[u];
-            bool closed = false;
-            while (n <= nn) {
-                if (cur == kNone16) break;
-                if (cur == u) {
-                    closed = true;
-                    break;
-                }
-                minc = min(minc, cur);
-                minm = min(minm, cur ^ 1u);
-                cur = S.succ[cur];
-                n++;
-            }
-            if (!closed) {
-                atomicOr(o.status, kStatusWalkLimit);
-                continue;
-            }
-            if (u != minc || minc > minm) continue;
-            const uint64_t len = (uint64_t)k + n - 1;
-            const unsigned long long off = atomicAdd(&o.counters[kCntBases], len);
-            const unsigned long long ix = atomicAdd(&o.counters[kCntUnitigs], 1ull);
-            if (off + len > o.bases_cap || ix >= o.u_cap) {
-                atomicOr(o.status, kStatusOutOverflow);
-                continue;
-            }
-            KT v = oriented(S.sk, u, k);
-            for (int i = 0; i < k; i++) o.bases[off + i] = base_char((uint32_t)(v >> (2 * i)));
-            cur = S.succ[u];
-            for (uint32_t i = 1; i < n; i++) {
-                v = oriented(S.sk, cur, k);
-                o.bases[off + (uint32_t)k - 1 + i] = base_char((uint32_t)(v >> (2 * (k - 1))));
-                cur = S.succ[cur];
-            }
-            o.u_off[ix] = off;
-            o.u_len[ix] = (uint32_t)len;
-            o.u_flags[ix] = 4;
         }
     }
 }

@@ -81,6 +81,8 @@ typedef struct {
     double ms_pack, ms_bucketize, ms_merge, ms_link; /* device times (events) and host link time */
     uint64_t distinct_kmers;    /* table entries summed over merge units */
     uint64_t merge_units_spilled; /* shared-memory attempts that moved to a global-memory table */
+    uint64_t merge_units_ext_global; /* units ranked in global-memory scratch (many survivors) */
+    uint64_t merge_units_walk;  /* units extended by per-thread walks (grid-wide tier, fallback) */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */

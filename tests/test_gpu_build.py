@@ -35,16 +35,20 @@ def _workload(kind, seed):
             b"CCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCCGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGGG")]
         seqs += [synth.random_genome(int(n), rng) for n in rng.integers(25, 120, size=200)]
         return synth.pack_sequences(seqs)
-    if kind in ("planted31", "planted63"):
+    if kind.startswith("planted"):
         # a random sequence with the m-mer of smallest canonical nt-hash planted every k - m
         # bases: every (k-1)-mer window holds exactly one copy, so all its k-mers (all
-        # distinct) fall into one sub-bucket
-        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if kind == "planted31" else (63, 12, b"CAGACTATCGCG", 5000)
+        # distinct) fall into one sub-bucket ("planted31:2500" sets the sequence length)
+        # ("planted31:2500:only" leaves out the second, random sequence)
+        name, _, rest = kind.partition(":")
+        ln_s, _, only = rest.partition(":")
+        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if name == "planted31" else (63, 12, b"CAGACTATCGCG", 5000)
+        n = int(ln_s) if ln_s else n
         g = synth.random_genome(n, rng).copy()
         pat = np.frombuffer(mm, np.uint8)
         for p in range(0, n - len(pat), k - m):
             g[p:p + len(pat)] = pat
-        return synth.pack_sequences([g, synth.random_genome(3000, rng)])
+        return synth.pack_sequences([g] if only else [g, synth.random_genome(3000, rng)])
     raise ValueError(kind)
 
 
@@ -141,6 +145,55 @@ def test_shared_memory_attempt_and_spill(ctx, kind, bbits, minm, k, m):
     ctx.link(k)
     bases, uo, ul, uf = ctx.unitigs()
     assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k) == r.unitigs()
+
+
+@pytest.mark.parametrize("kind,k,m", [("planted31:2500:only", 31, 10), ("planted31:5000:only", 31, 10),
+                                      ("planted31:8000:only", 31, 10), ("planted63:1300:only", 63, 12),
+                                      ("planted63:2500:only", 63, 12), ("planted63:5000:only", 63, 12),
+                                      ("planted31:8000", 31, 10), ("planted63:5000", 63, 12)])
+def test_many_survivors_rank_in_global_scratch(ctx, kind, k, m):
+    """A unit with more surviving k-mers than its tier's shared-memory ranking arrays hold
+    (S, W and M tiers by the planted length) is ranked in the CTA's global scratch: same
+    k-mers and unitigs as the oracle, and no unit falls back to per-thread walks."""
+    text, off, ln, _ = _workload(kind, 23)
+    p = make_params(k=k, m=m, bucket_bits=1, second_bits=1, min_multiplicity=1, keep_kmers=True)
+    ctx.build_text(text, p)
+    st = ctx.stats()
+    assert st["merge_units_ext_global"] > 0
+    assert st["merge_units_walk"] == 0
+    keys, mult = ctx.kmers()
+    if k > 32:
+        keys = [int(a) | (int(b) << 64) for a, b in keys.tolist()]
+    got = _kmer_dict(keys, mult)
+    op = oracle.params(k=k, m=m, bucket_bits=1, second_bits=1, min_multiplicity=1, threads=8)
+    r = oracle.build_graph(text, off, ln, op)
+    lo, hi, emult = r.kmers()
+    assert got == {int(a) | (int(b) << 64): int(c) for a, b, c in zip(lo.tolist(), hi.tolist(), emult.tolist())}
+    ctx.link(k)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k) == r.unitigs()
+
+
+def test_genome_family_min_multiplicity_one(ctx):
+    """Many related genomes (one ancestor, per-genome substitutions and indels) with
+    min multiplicity 1, the shape of a coloured build: big minimizer groups whose k-mers
+    nearly all survive.  Bit-exact against the oracle, no walk fallback."""
+    rng = np.random.default_rng(31)
+    anc = synth.random_genome(60_000, rng)
+    gs = [synth.indels(synth.substitute(anc, float(rng.uniform(0.001, 0.02)), rng), 0.0005, 50, rng)
+          for _ in range(48)]
+    text, off, ln, _ = synth.pack_sequences(gs)
+    p = make_params(k=31, m=10, bucket_bits=6, second_bits=1, min_multiplicity=1, keep_kmers=True)
+    ctx.build_text(text, p)
+    st = ctx.stats()
+    assert st["merge_units_walk"] == 0
+    keys, mult = ctx.kmers()
+    r = oracle.build_graph(text, off, ln, _oracle_params(p))
+    lo, hi, emult = r.kmers()
+    assert _kmer_dict(keys, mult) == dict(zip(lo.tolist(), emult.tolist()))
+    ctx.link(31)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
 
 
 def test_device_pointer_bucketize(ctx):
