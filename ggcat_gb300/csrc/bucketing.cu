@@ -69,314 +69,338 @@ __global__ void __launch_bounds__(256) pack_kernel(const uint8_t *__restrict__ t
 // tests), so the combine reproduces the queue's values exactly.
 //
 // The window of w = k-m m-mers ending at m-mer i is split van Herk / Gil-Werman style into
-// blocks of w m-mers aligned at i % w == 0: window = suffix(previous block, from i-w+1)
-// combined with prefix(current block, up to i).  Every thread's chunk starts at a multiple
-// of w, so all lanes of a warp cross block boundaries on the same step and do identical
-// work.  The per-thread block array (w entries) lives in shared memory, column-major.
+// blocks of w m-mers counted from the thread's first m-mer: window = suffix(previous block,
+// from i-w+1) combined with prefix(current block, up to i).  All lanes of a warp start the
+// same number of bases before a multiple of 32, so they cross block and packed-word
+// boundaries on the same steps and do identical work.  The per-thread block array (w
+// entries) lives in shared memory, column-major.
+//
+// The nt-hash rolls over every code, valid or not, starting from the state of an all-'A'
+// history: the rolling update is exact for any code sequence, so m steps after a separator
+// or an N the value is the m-mer's hash again without a recomputation; validity is tracked
+// by the run length.
 // ---------------------------------------------------------------------------
-struct NtTables {
-    uint64_t h[4], rch[4], h_rot_m[4], rch_rot_m1[4];
+// Rolling nt-hash tables per 2-bit code (cn_nthash.rs:19-58): the leaving base contributes
+// {rotl(h, m), rch} and the entering base {h, rotl(rch, m - 1)}.
+struct __align__(16) NtPair {
+    uint64_t a, b;
 };
 
+// Window-minimum state: v = masked minimum | unique bit, pf = position << 1 | is_forward
 struct CState {
-    uint64_t v;    // masked minimum | unique bit
-    uint64_t pos;  // absolute m-mer position of the minimum (meaningful when unique)
-    uint32_t fw;   // is_forward of that m-mer
+    uint64_t v;
+    uint32_t pf;
 };
 
-__device__ __forceinline__ CState cmb(CState a, const CState &b) {
+__device__ __forceinline__ CState cmb(const CState &a, const CState &b) {
     const uint64_t ma = a.v & ~1ull, mb = b.v & ~1ull;
-    if (ma < mb) return a;
-    if (mb < ma) return b;
-    a.v = ma;  // the minimum occurs in both parts: not unique
-    return a;
-}
-
-// Base of age a (0 = newest) in the 64-base history (r0 newest 32 bases, r1 older 32).
-__device__ __forceinline__ uint32_t hist_base(uint64_t r0, uint64_t r1, int a) {
-    return a < 32 ? (uint32_t)((r0 >> (2 * a)) & 3u) : (uint32_t)((r1 >> (2 * (a - 32))) & 3u);
-}
-
-// nt-hash of the m-mer whose first base has age `a_first` (its last base has age a_first-m+1).
-__device__ __forceinline__ void nt_from_scratch(const NtTables &T, uint64_t r0, uint64_t r1, int a_first, int m,
-                                                uint64_t &fw, uint64_t &rc) {
-    fw = 0;
-    rc = 0;
-    for (int j = 0; j < m; j++) {
-        uint32_t c = hist_base(r0, r1, a_first - j);
-        fw ^= rotl64(T.h[c], (unsigned)(m - 1 - j));
-        rc ^= rotl64(T.rch[c], (unsigned)j);
-    }
-}
-
-__device__ __forceinline__ uint64_t nt_value(uint64_t fw, uint64_t rc) {
-    uint64_t mn = fw < rc ? fw : rc;
-    return (mn << 1) | (uint64_t)(fw != rc);
+    CState r;
+    r.v = ma < mb ? a.v : (mb < ma ? b.v : ma);  // equal minima from two parts: not unique
+    r.pf = mb < ma ? b.pf : a.pf;
+    return r;
 }
 
 constexpr uint64_t kInf = ~0ull;
 
 // Superkmers found by a lane wait in a per-lane queue in shared memory (column-major, one
-// column per thread) and are built, counted and appended together by the whole warp: a split
+// column per thread) and are built, counted and stored together by the whole warp: a split
 // happens every ~(w+1)/2 positions per lane, so emitting at once would run the record code on
-// almost every step with one or two lanes active.
-constexpr int kEmitQueue = 8;   // entries per lane
-constexpr int kEmitDrain = 4;   // the warp drains when a lane holds this many
+// almost every step with one or two lanes active.  A lane gains at most one entry per step
+// and the warp drains as soon as a lane holds kEmitDrain, so kEmitQueue entries suffice.
+constexpr int kEmitQueue = 4;
+constexpr int kEmitDrain = 3;
 
-// Single pass: superkmer records are appended to a staging array (warp-aggregated slot
-// reservation) and counted per sub-bin; partition_kernel then scatters them by sub-bin.
-__global__ void __launch_bounds__(256)
-    bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k, int m,
-                     int bbits, int sbits, int fbits, int canonical, uint64_t chunk,
+// Single pass over the 2-bit text.  Thread t owns the window starts [t*chunk, (t+1)*chunk)
+// (chunk a multiple of 32) and walks the bases from lb (a multiple of 32) before its range,
+// so all lanes of a warp load packed words and cross van Herk block boundaries on the same
+// steps.  Superkmer records go to the block's region of the staging array (block-shared
+// cursor), or to the overflow area when the region is full; partition_kernel scatters them
+// by sub-bin after an exclusive scan of the per-sub-bin counts.
+template <bool kLongM>  // m > 16: the last m codes need a 64-bit shift register
+__global__ void __launch_bounds__(256, 3)
+    bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k,
+                     int m, int bbits, int sbits, int fbits, int canonical, uint32_t chunk, uint32_t lb0,
                      unsigned long long *__restrict__ bin_count, unsigned long long *__restrict__ bin_kmers,
-                     SkRec *__restrict__ stage, unsigned long long stage_cap,
-                     unsigned long long *__restrict__ stage_cursor, unsigned *__restrict__ status) {
-    __shared__ NtTables T;
+                     SkRec *__restrict__ stage, uint32_t region_cap, unsigned long long *__restrict__ block_count,
+                     unsigned long long ovf_cap, unsigned long long *__restrict__ ovf_cursor,
+                     unsigned *__restrict__ status) {
+    __shared__ NtPair t_out[4], t_in[4];
+    __shared__ unsigned s_cnt;
     extern __shared__ __align__(16) uint8_t bk_smem[];
     const int wn = k - m;
     const int nthr = blockDim.x;
-    uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                                  // [wn][nthr]
-    uint64_t *q_w0 = blk_v + (size_t)wn * nthr;                                              // [kEmitQueue][nthr]
-    uint64_t *q_raw = q_w0 + (size_t)kEmitQueue * nthr;                                      // [kEmitQueue][nthr]
-    uint32_t *q_meta = reinterpret_cast<uint32_t *>(q_raw + (size_t)kEmitQueue * nthr);      // [kEmitQueue][nthr]
-    uint8_t *blk_meta = reinterpret_cast<uint8_t *>(q_meta + (size_t)kEmitQueue * nthr);     // [wn][nthr]
+    uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                          // [wn][nthr]
+    uint4 *que = reinterpret_cast<uint4 *>(blk_v + (size_t)wn * nthr);                // [kEmitQueue][nthr]
+    uint8_t *blk_m = reinterpret_cast<uint8_t *>(que + (size_t)kEmitQueue * nthr);    // [wn][nthr]
     if (threadIdx.x < 4) {
-        uint32_t c = threadIdx.x;
-        uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
-        uint64_t r = (uint64_t)(((2 * c) ^ 4) + 1) * kNtMult;
-        T.h[c] = h;
-        T.rch[c] = r;
-        T.h_rot_m[c] = rotl64(h, (unsigned)m);
-        T.rch_rot_m1[c] = rotl64(r, (unsigned)(m - 1));
+        const uint32_t c = threadIdx.x;
+        const uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
+        const uint64_t r = (uint64_t)(((2 * c) ^ 4) + 1) * kNtMult;
+        t_out[c] = NtPair{rotl64(h, (unsigned)m), r};
+        t_in[c] = NtPair{h, rotl64(r, (unsigned)(m - 1))};
+    }
+    if (threadIdx.x == 0) s_cnt = 0;
+    // rolling state of an all-'A' history (code 0): nt-hash of m A's
+    uint64_t fw_a = 0, rc_a = 0;
+    {
+        const uint64_t h0 = kNtMult, r0 = 5ull * kNtMult;
+        for (int j = 0; j < m; j++) {
+            fw_a ^= rotl64(h0, (unsigned)(m - 1 - j));
+            rc_a ^= rotl64(r0, (unsigned)j);
+        }
     }
     __syncthreads();
 
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t x0 = tid * chunk;  // chunk is a multiple of wn
-    if (x0 >= n) return;
-    const uint64_t x1 = min(x0 + chunk, n);
     const uint32_t dup_bucket = 1u << bbits;
-    const uint64_t bmask = (1ull << bbits) - 1, smask = (1ull << sbits) - 1, fmask = (1ull << fbits) - 1;
+    const uint32_t bmask = (1u << bbits) - 1, smask = (1u << sbits) - 1, fmask = (1u << fbits) - 1;
+    const uint64_t n_words = (n + 31) >> 5;
+    const int lane = (int)(threadIdx.x & 31);
+    const uint64_t region = (uint64_t)blockIdx.x * region_cap;
     uint64_t *my_v = blk_v + threadIdx.x;
-    uint8_t *my_meta = blk_meta + threadIdx.x;
+    uint8_t *my_m = blk_m + threadIdx.x;
+    uint4 *my_q = que + threadIdx.x;
+    const uint32_t top_sh = 2u * (uint32_t)(m - 1);
 
-    uint64_t lb = (uint64_t)wn * 6;
-    for (int attempt = 0; attempt < 40; attempt++) {
-        const uint64_t xb = x0 > lb ? x0 - lb : 0;  // multiple of wn
-        bool anchored = (xb == 0);
-        uint64_t run = 0;
-        uint64_t r0 = 0, r1 = 0, fw = 0, rc = 0;
-        uint64_t prev_raw = 0, prev_pos = 0;
-        uint32_t prev_fw = 0;
-        bool prev_valid = false;
-        uint64_t c_prev = 0;
-        bool c_known = false, first_sk = false, failed = false;
-        bool have_prev_block = false;
-        CState P{kInf, 0, 0};
-        int o = 0;  // offset of the current m-mer inside its block
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t x0 = tid * chunk;
+    int qlen = 0;     // superkmers waiting in this lane's queue
+    uint64_t xb = 0;  // first base of the current attempt (queue positions are relative to it)
 
-        uint64_t cur_word = ~0ull, pw = 0;
-        uint32_t vw = 0;
-        const uint64_t p_end = min(x1 + (uint64_t)k - 1, n + 1);
-
-        int qlen = 0;  // superkmers waiting in this lane's queue
-        // build, count and append one queued superkmer of every lane that has one, until all
-        // queues of the warp are empty; one stage-cursor atomic per round
-        auto drain = [&]() {
-            const unsigned am = __activemask();
-            const int lane = (int)(threadIdx.x & 31);
-            for (;;) {
-                const unsigned bm = __ballot_sync(am, qlen > 0);
-                if (bm == 0) break;
-                SkRec r{0, 0};
-                if (qlen > 0) {
-                    qlen--;
-                    const size_t qi = (size_t)qlen * nthr + threadIdx.x;
-                    const uint64_t w0 = q_w0[qi], raw = q_raw[qi];
-                    const uint32_t meta = q_meta[qi];
-                    // superkmer [start, start + len) with the minimizer of value raw at offset
-                    // moff (lib.rs:207-267)
-                    const uint32_t len = (uint32_t)(w0 >> 40);
-                    const uint32_t moff = meta & 0xffffffu, mfw = (meta >> 24) & 1u;
-                    const uint32_t inc_first = (meta >> 25) & 1u, inc_last = (meta >> 26) & 1u;
-                    uint32_t bucket, rcf, pos;
-                    if ((raw & 1ull) == 0) {
-                        bucket = dup_bucket;
-                        rcf = 0;
-                        pos = 0;
-                    } else {
-                        rcf = (canonical && !mfw) ? 1u : 0u;
-                        bucket = (uint32_t)((raw >> 1) & bmask);  // get_bucket(0, b, h), cn_nthash.rs:135-142
-                        pos = rcf ? len - (moff + (uint32_t)m) : moff;
-                    }
-                    const uint32_t second = (uint32_t)((raw >> (bbits + 1)) & smask);
-                    const uint32_t sub = (uint32_t)((raw >> (bbits + 1)) & fmask);
-                    const uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
-                    const uint64_t bin = ((uint64_t)bucket << fbits) | sub;
-                    atomicAdd(&bin_count[bin], 1ull);
-                    atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
-                    r.w0 = w0;
-                    r.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
-                           ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
+    // build, count and store one queued superkmer of every lane that has one, until all
+    // queues of the active lanes are empty
+    auto drain = [&]() {
+        const unsigned am = __activemask();
+        for (;;) {
+            const unsigned bm = __ballot_sync(am, qlen > 0);
+            if (bm == 0) break;
+            SkRec rec{0, 0};
+            if (qlen > 0) {
+                qlen--;
+                const uint4 e = my_q[(size_t)qlen * nthr];
+                // superkmer [start, end) whose last window's minimum (value raw, m-mer
+                // position pos, is_forward mfw) is the minimizer (lib.rs:207-267)
+                const uint32_t start_r = e.x, end_r = e.y & 0x3fffffffu;
+                const uint32_t inc_first = (e.y >> 30) & 1u, inc_last = e.y >> 31;
+                const uint32_t len = end_r - start_r;
+                const uint32_t moff = (e.z >> 1) - start_r, mfw = e.z & 1u;
+                const uint32_t raw = e.w;
+                uint32_t bucket, rcf, pos;
+                if ((raw & 1u) == 0) {
+                    bucket = dup_bucket;
+                    rcf = 0;
+                    pos = 0;
+                } else {
+                    rcf = (canonical && !mfw) ? 1u : 0u;
+                    bucket = (raw >> 1) & bmask;  // get_bucket(0, b, h), cn_nthash.rs:135-142
+                    pos = rcf ? len - (moff + (uint32_t)m) : moff;
                 }
-                const int leader = __ffs(bm) - 1;
-                unsigned long long base = 0;
-                if (lane == leader) base = atomicAdd(stage_cursor, (unsigned long long)__popc(bm));
-                base = __shfl_sync(am, base, leader);
-                if ((bm >> lane) & 1u) {
-                    const unsigned long long idx = base + (unsigned long long)__popc(bm & ((1u << lane) - 1u));
-                    if (idx < stage_cap)
-                        stage[idx] = r;
+                const uint32_t second = (raw >> (bbits + 1)) & smask;
+                const uint32_t sub = (raw >> (bbits + 1)) & fmask;
+                const uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
+                const uint64_t bin = ((uint64_t)bucket << fbits) | sub;
+                atomicAdd(&bin_count[bin], 1ull);
+                atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
+                rec.w0 = (xb + start_r) | ((uint64_t)len << 40);
+                rec.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
+                         ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
+            }
+            const int leader = __ffs(bm) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(&s_cnt, (unsigned)__popc(bm));
+            base = __shfl_sync(am, base, leader);
+            if ((bm >> lane) & 1u) {
+                const unsigned idx = base + (unsigned)__popc(bm & ((1u << lane) - 1u));
+                if (idx < region_cap) {
+                    stage[region + idx] = rec;
+                } else {
+                    const unsigned long long oi = atomicAdd(ovf_cursor, 1ull);
+                    if (oi < ovf_cap)
+                        stage[(uint64_t)gridDim.x * region_cap + oi] = rec;
                     else
                         atomicOr(status, kStatusStageOverflow);
                 }
             }
-        };
+        }
+    };
 
-        auto emit = [&](uint64_t c, bool is_final) {
-            // queue the superkmer [c_prev - 1, c + k - 1) with the minimizer of the window
-            // before c (split) or of the last window (final)
-            const uint64_t start = c_prev - 1, end = c + (uint64_t)k - 1;
-            const size_t qi = (size_t)qlen * nthr + threadIdx.x;
-            q_w0[qi] = start | ((end - start) << 40);
-            q_raw[qi] = prev_raw;
-            q_meta[qi] = (uint32_t)((prev_pos - start) & 0xffffffu) | (prev_fw << 24) | ((first_sk ? 1u : 0u) << 25) |
-                         ((is_final ? 1u : 0u) << 26);
-            qlen++;
-            first_sk = false;
-        };
+    if (x0 < n) {
+        const uint64_t x1 = min(x0 + chunk, n);
+        uint64_t lb = lb0;
+        bool done = false;
+        // (relative positions stay below 2^30: queue entries keep two flags above them)
+        for (int attempt = 0; attempt < 24 && !done && lb <= (1ull << 28); attempt++) {
+            xb = x0 > lb ? x0 - lb : 0;  // a multiple of 32
+            const uint32_t lo_r = (uint32_t)(x0 - xb), hi_r = (uint32_t)(x1 - xb);
+            const uint32_t r_end = (uint32_t)(min(x1 + (uint64_t)k - 1, n + 1) - xb);
+            bool anchored = (xb == 0);
+            uint32_t run = 0;
+            uint64_t fw = fw_a, rc = rc_a;
+            uint64_t hist = 0;  // codes of the last m bases, oldest in the low bits
+            CState P{kInf, 0}, prev{0, 0};
+            bool prev_valid = false, c_known = false, first_sk = false, failed = false, have_prev_block = false;
+            uint32_t c_prev = 0;
+            int o = 0;  // offset of the current m-mer inside its block
 
-        for (uint64_t p = xb; p < p_end; p++) {
-            // the warp drains its queues once a lane's queue is half full (loop stays in lockstep)
-            if (__any_sync(__activemask(), qlen >= kEmitDrain)) drain();
-            const uint64_t wi = p >> 5;
-            if (wi != cur_word) {
-                cur_word = wi;
-                if (p < n) {
-                    pw = packed[wi];
-                    vw = valid[wi];
-                } else {
-                    pw = 0;
-                    vw = 0;
+            uint64_t wi = xb >> 5;
+            uint64_t pw = 0, pw_next = wi < n_words ? packed[wi] : 0ull;
+            uint32_t vw = 0, vw_next = wi < n_words ? valid[wi] : 0u;
+
+            auto push = [&](uint32_t start_r, uint32_t end_r, uint32_t fin) {
+                my_q[(size_t)qlen * nthr] = make_uint4(start_r, end_r | ((first_sk ? 1u : 0u) << 30) | (fin << 31),
+                                                       prev.pf, (uint32_t)prev.v);
+                qlen++;
+                first_sk = false;
+            };
+
+            for (uint32_t r = 0; r < r_end; r++) {
+                // the warp drains its queues once a lane's queue reaches kEmitDrain
+                if (__any_sync(__activemask(), qlen >= kEmitDrain)) drain();
+                if ((r & 31u) == 0) {  // the same step on every lane
+                    pw = pw_next;
+                    vw = vw_next;
+                    wi++;
+                    pw_next = wi < n_words ? packed[wi] : 0ull;
+                    vw_next = wi < n_words ? valid[wi] : 0u;
                 }
-            }
-            const uint32_t sh = (uint32_t)(p & 31);
-            const bool ok = (p < n) && ((vw >> sh) & 1u);
-            uint64_t e_v = kInf;
-            uint32_t e_fw = 0;
-            if (ok) {
-                const uint32_t c = (uint32_t)((pw >> (2 * sh)) & 3u);
-                r1 = (r1 << 2) | (r0 >> 62);
-                r0 = (r0 << 2) | c;
-                run++;
-                if (run == (uint64_t)m) {
-                    nt_from_scratch(T, r0, r1, m - 1, m, fw, rc);
-                } else if (run > (uint64_t)m) {
-                    uint32_t out = hist_base(r0, r1, m);
-                    fw = rotl64(fw, 1) ^ T.h_rot_m[out] ^ T.h[c];
-                    rc = rotr64(rc ^ T.rch[out], 1) ^ T.rch_rot_m1[c];
-                }
-                if (run >= (uint64_t)m) {
-                    e_v = nt_value(fw, rc);
-                    e_fw = (uint32_t)(fw < rc);
-                }
-            } else {
-                if (run >= (uint64_t)k && prev_valid) {
-                    const uint64_t x_last = p - (uint64_t)k + 1;
-                    if (x_last >= x0 && x_last < x1) {
-                        if (!c_known) failed = true;
-                        else emit(x_last, true);
+                const uint32_t c = (uint32_t)pw & 3u;
+                pw >>= 2;
+                const bool ok = (vw & 1u) != 0;
+                vw >>= 1;
+                if (!ok) {
+                    // end of a run: the last superkmer closes at its last window (x_last)
+                    if (run >= (uint32_t)k && prev_valid) {
+                        const uint32_t x_last = r - (uint32_t)k + 1;
+                        if (x_last >= lo_r && x_last < hi_r) {
+                            if (!c_known) {
+                                failed = true;
+                                break;
+                            }
+                            push(c_prev - 1, x_last + (uint32_t)k - 1, 1u);
+                        }
                     }
-                }
-                run = 0;
-                anchored = true;
-                prev_valid = false;
-                c_known = false;
-            }
-            if (failed) break;
-            // block bookkeeping over m-mer positions i = p - m + 1 (aligned: xb % wn == 0)
-            if (p + 1 < xb + (uint64_t)m) continue;  // no m-mer position >= xb yet
-            const uint64_t i = p + 1 - (uint64_t)m;
-            if (o == 0 && i > xb) {
-                // the previous block [i - wn, i) is complete: suffix-combine it in place
-                CState s{my_v[(size_t)(wn - 1) * nthr], 0, 0};
-                {
-                    uint8_t mt = my_meta[(size_t)(wn - 1) * nthr];
-                    s.pos = (uint64_t)(mt & 0x7f);
-                    s.fw = mt >> 7;
-                }
-                for (int j = wn - 2; j >= 0; j--) {
-                    uint8_t mt = my_meta[(size_t)j * nthr];
-                    CState c{my_v[(size_t)j * nthr], (uint64_t)(mt & 0x7f), (uint32_t)(mt >> 7)};
-                    s = cmb(c, s);
-                    my_v[(size_t)j * nthr] = s.v;
-                    my_meta[(size_t)j * nthr] = (uint8_t)((s.pos & 0x7f) | (s.fw << 7));
-                }
-                have_prev_block = true;
-            }
-            const CState e{e_v, i, e_fw};
-            P = (o == 0) ? e : cmb(P, e);
-            CState win = P;
-            bool win_avail = (o == wn - 1);
-            if (!win_avail && have_prev_block) {
-                uint8_t mt = my_meta[(size_t)(o + 1) * nthr];
-                CState sp{my_v[(size_t)(o + 1) * nthr], i - (uint64_t)o - (uint64_t)wn + (uint64_t)(mt & 0x7f),
-                          (uint32_t)(mt >> 7)};
-                win = cmb(sp, P);
-                win_avail = true;
-            }
-            my_v[(size_t)o * nthr] = e_v;
-            my_meta[(size_t)o * nthr] = (uint8_t)(o | (e_fw << 7));
-            o = (o + 1 == wn) ? 0 : o + 1;
-
-            if (!ok || run < (uint64_t)(k - 1) || !win_avail) continue;
-            const uint64_t x = p - (uint64_t)k + 2;  // window start
-            const uint64_t cur_raw = win.v, cur_pos = win.pos;
-            const uint32_t cur_fw = win.fw;
-            if (run == (uint64_t)(k - 1)) {
-                if (anchored) {
-                    c_prev = x + 1;  // virtual first callback: the first superkmer starts at x
-                    c_known = true;
-                    first_sk = true;
-                } else {
+                    anchored = true;
+                    prev_valid = false;
                     c_known = false;
                 }
-            } else {
-                // get_minimizer_splits split rule, batch_minqueue.rs:146-152
-                const bool split = (cur_raw != prev_raw) || ((cur_raw & 1ull) && cur_pos != prev_pos);
-                if (split) {
-                    if (x >= x0 && x < x1) {
-                        if (!c_known) {
-                            failed = true;
-                            break;
-                        }
-                        emit(x, false);
-                    }
-                    c_prev = x;
-                    c_known = true;
-                    first_sk = false;
+                run = ok ? run + 1 : 0u;
+                // rolling nt-hash of the m-mer ending here (every code rolls, valid or not)
+                uint32_t out;
+                if constexpr (kLongM) {
+                    out = (uint32_t)hist & 3u;
+                    hist = (hist >> 2) | ((uint64_t)c << top_sh);
+                } else {
+                    out = (uint32_t)hist & 3u;
+                    hist = (uint64_t)(((uint32_t)hist >> 2) | (c << top_sh));
                 }
+                const NtPair to = t_out[out], ti = t_in[c];
+                fw = rotl64(fw, 1) ^ to.a ^ ti.a;
+                rc = rotr64(rc ^ to.b, 1) ^ ti.b;
+                if (r + 1 < (uint32_t)m) continue;  // no m-mer yet (the same steps on every lane)
+                const bool mv = run >= (uint32_t)m;
+                const bool isf = fw < rc;
+                const uint64_t mn = isf ? fw : rc;
+                const CState e{mv ? ((mn << 1) | (uint64_t)(fw != rc)) : kInf,
+                               ((r + 1 - (uint32_t)m) << 1) | (isf ? 1u : 0u)};
+                // van Herk block window minimum over m-mer indices relative to xb
+                uint64_t *vo = my_v + (size_t)o * nthr;
+                uint8_t *mo = my_m + (size_t)o * nthr;
+                if (o == 0) {
+                    if (r + 1 > (uint32_t)m) {
+                        // the previous block is complete: suffix minima in place (offset 0 unused)
+                        CState s{my_v[(size_t)(wn - 1) * nthr], my_m[(size_t)(wn - 1) * nthr]};
+                        for (int j = wn - 2; j >= 1; j--) {
+                            const CState cj{my_v[(size_t)j * nthr], my_m[(size_t)j * nthr]};
+                            s = cmb(cj, s);
+                            my_v[(size_t)j * nthr] = s.v;
+                            my_m[(size_t)j * nthr] = (uint8_t)s.pf;
+                        }
+                        have_prev_block = true;
+                    }
+                    P = e;
+                } else {
+                    P = cmb(P, e);
+                }
+                CState win = P;
+                bool win_avail = (o == wn - 1);
+                if (!win_avail && have_prev_block) {
+                    const uint8_t mt = mo[nthr];
+                    // suffix of the previous block from offset o + 1: position = block start + offset
+                    const uint32_t ps = (r + 1 - (uint32_t)m) - (uint32_t)o - (uint32_t)wn + (uint32_t)(mt & 0x7f);
+                    win = cmb(CState{vo[nthr], (ps << 1) | (uint32_t)(mt >> 7)}, P);
+                    win_avail = true;
+                }
+                *vo = e.v;
+                *mo = (uint8_t)((uint32_t)o | ((e.pf & 1u) << 7));
+                o = (o + 1 == wn) ? 0 : o + 1;
+
+                if (!ok || run < (uint32_t)(k - 1) || !win_avail) continue;
+                const uint32_t x = r - (uint32_t)k + 2;  // window start
+                if (run == (uint32_t)(k - 1)) {
+                    if (anchored) {
+                        c_prev = x + 1;  // virtual first callback: the first superkmer starts at x
+                        c_known = true;
+                        first_sk = true;
+                    } else {
+                        c_known = false;
+                    }
+                } else {
+                    // get_minimizer_splits split rule, batch_minqueue.rs:146-152
+                    const bool split = (win.v != prev.v) || ((win.v & 1ull) && win.pf != prev.pf);
+                    if (split) {
+                        if (x >= lo_r && x < hi_r) {
+                            if (!c_known) {
+                                failed = true;
+                                break;
+                            }
+                            push(c_prev - 1, x + (uint32_t)k - 1, 0u);
+                        }
+                        c_prev = x;
+                        c_known = true;
+                        first_sk = false;
+                    }
+                }
+                prev = win;
+                prev_valid = true;
             }
-            prev_raw = cur_raw;
-            prev_pos = cur_pos;
-            prev_fw = cur_fw;
-            prev_valid = true;
+            drain();
+            if (!failed) {
+                done = true;
+            } else {
+                if (xb == 0) break;  // cannot look back further
+                lb *= 4;
+            }
         }
-        drain();
-        if (!failed) return;
-        if (xb == 0) break;  // cannot look back further
-        lb *= 4;
+        if (!done) atomicOr(status, kStatusLookback);
     }
-    atomicOr(status, kStatusLookback);
+    __syncthreads();
+    if (threadIdx.x == 0) block_count[blockIdx.x] = min(s_cnt, region_cap);
 }
 
 // Scatter of the staged records into their sub-bin ranges (the device radix partition).
-__global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict__ stage, uint64_t n_stage, int fbits,
+// CTA b < n_regions reads the first block_count[b] records of staging region b; the CTAs
+// after them read slices of kOvfSlice records of the overflow area.
+constexpr uint32_t kOvfSlice = 8192;
+
+__global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict__ stage, uint32_t n_regions,
+                                                        uint32_t region_cap,
+                                                        const unsigned long long *__restrict__ block_count,
+                                                        const unsigned long long *__restrict__ ovf_cursor,
+                                                        unsigned long long ovf_cap, int fbits,
                                                         const unsigned long long *__restrict__ bin_off,
                                                         unsigned long long *__restrict__ bin_cursor,
                                                         SkRec *__restrict__ recs, unsigned *__restrict__ status) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_stage;
-         i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t begin, end;
+    if (blockIdx.x < n_regions) {
+        begin = (uint64_t)blockIdx.x * region_cap;
+        end = begin + min((unsigned long long)region_cap, block_count[blockIdx.x]);
+    } else {
+        const uint64_t used = min(*ovf_cursor, ovf_cap);
+        const uint64_t s0 = (uint64_t)(blockIdx.x - n_regions) * kOvfSlice;
+        if (s0 >= used) return;
+        begin = (uint64_t)n_regions * region_cap + s0;
+        end = (uint64_t)n_regions * region_cap + min(used, s0 + kOvfSlice);
+    }
+    for (uint64_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
         const SkRec r = stage[i];
         const uint64_t bin = ((uint64_t)rec_bucket(r) << fbits) | ((r.w1 >> 48) & 0xffffull);
         const unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
@@ -486,34 +510,51 @@ int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *v
     return 1;
 }
 
-int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
-                     int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long stage_cap,
-                     unsigned long long *stage_cursor, unsigned *status, cudaStream_t s) {
+BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m) {
+    BucketizeGeometry g{};
     const int wn = k - m;
-    const uint64_t chunk = ((chunk_hint + wn - 1) / wn) * wn;
-    uint64_t threads = (n + chunk - 1) / chunk;
-    if (threads == 0) return 0;
-    const int tpb = wn <= 24 ? 256 : 128;
-    const size_t smem = (size_t)wn * tpb * 9 + (size_t)kEmitQueue * tpb * 20;
+    g.threads_per_block = wn <= 24 ? 256 : 128;
+    g.chunk = wn <= 24 ? 1024u : 2048u;
+    g.lookback = (uint32_t)(((2 * wn + 8) + 31) / 32 * 32);
+    const uint64_t threads = (n + g.chunk - 1) / g.chunk;
+    g.blocks = (uint32_t)((threads + g.threads_per_block - 1) / g.threads_per_block);
+    // 1.5x the expected superkmer density 2/(w+1) of random sequence; excess goes to the
+    // overflow area
+    g.region_cap = (uint32_t)((uint64_t)g.threads_per_block * g.chunk * 3 / (uint64_t)(wn + 1) + 64);
+    g.smem = (size_t)wn * g.threads_per_block * 9 + (size_t)kEmitQueue * g.threads_per_block * 16;
+    return g;
+}
+
+int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
+                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
+                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s) {
+    if (g.blocks == 0) return 0;
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(bucketize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         configured = true;
     }
-    uint64_t blocks = (threads + tpb - 1) / tpb;
-    bucketize_kernel<<<(unsigned)blocks, tpb, smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits, canonical, chunk,
-                                                         bin_count, bin_kmers, stage, stage_cap, stage_cursor, status);
+    if (m > 16)
+        bucketize_kernel<true><<<g.blocks, g.threads_per_block, g.smem, s>>>(
+            packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
+            g.region_cap, block_count, ovf_cap, ovf_cursor, status);
+    else
+        bucketize_kernel<false><<<g.blocks, g.threads_per_block, g.smem, s>>>(
+            packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
+            g.region_cap, block_count, ovf_cap, ovf_cursor, status);
     return 1;
 }
 
-int launch_partition(const SkRec *stage, uint64_t n_stage, int fbits, const unsigned long long *bin_off,
-                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, int sms, cudaStream_t s) {
-    if (n_stage == 0) return 0;
-    uint64_t blocks = (n_stage + 255) / 256;
-    const uint64_t cap = (uint64_t)sms * 8;
-    if (blocks > cap) blocks = cap;
-    partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(stage, n_stage, fbits, bin_off, bin_cursor, recs, status);
+int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
+                     const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
+                     const unsigned long long *bin_off, unsigned long long *bin_cursor, SkRec *recs, unsigned *status,
+                     cudaStream_t s) {
+    const uint64_t grid = (uint64_t)g.blocks + (ovf_cap + kOvfSlice - 1) / kOvfSlice;
+    if (grid == 0) return 0;
+    partition_kernel<<<(unsigned)grid, 256, 0, s>>>(stage, g.blocks, g.region_cap, block_count, ovf_cursor, ovf_cap,
+                                                    fbits, bin_off, bin_cursor, recs, status);
     return 1;
 }
 

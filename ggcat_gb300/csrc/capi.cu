@@ -84,7 +84,7 @@ struct ggcat_gpu_ctx {
     DevBuf<uint32_t> valid;
     DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, bin_cursor, scan_tmp;
     DevBuf<SkRec> recs, stage;
-    DevBuf<unsigned long long> stage_cursor;
+    DevBuf<unsigned long long> ovf_cursor, block_count;  // staging overflow cursor, records per region
     DevBuf<unsigned> status;
     uint64_t n_text = 0, n_recs = 0, n_kmers = 0, n_bins = 0;
     uint32_t n_buckets = 0;
@@ -265,45 +265,46 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->bin_cursor.ensure(nb + 1));
     CK(ctx->scan_tmp.ensure(scan_temp_elems(nb) + 2));
     const int canonical = p->forward_only ? 0 : 1;
-    const uint64_t chunk = 1008;
-    CK(ctx->stage_cursor.ensure(1));
-    // staging capacity: superkmer density is about 2/(w+1) per base; retried when exceeded
-    uint64_t stage_cap = text_len * 3 / (uint64_t)(p->k - p->m + 1) + 4096;
+    const BucketizeGeometry geo = bucketize_geometry(text_len, p->k, p->m);
+    CK(ctx->ovf_cursor.ensure(1));
+    CK(ctx->block_count.ensure((size_t)geo.blocks + 1));
+    // overflow area of the staging array (records beyond a block's region); retried when exceeded
+    uint64_t ovf_cap = text_len / 64 + 4096;
     CK(cudaEventRecord(ctx->ev[0], s));
     ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], s));
     unsigned long long totals[3];
     for (int attempt = 0; attempt < 2; attempt++) {
-        CK(ctx->stage.ensure(stage_cap));
+        CK(ctx->stage.ensure((uint64_t)geo.blocks * geo.region_cap + ovf_cap));
         CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-        CK(cudaMemsetAsync(ctx->stage_cursor.p, 0, sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->ovf_cursor.p, 0, sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
         ctx->launches += launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                          p->second_bits, ctx->fine_bits, canonical, chunk, ctx->bin_count.p,
-                                          ctx->bin_kmers.p, ctx->stage.p, ctx->stage.n, ctx->stage_cursor.p,
-                                          ctx->status.p, s);
+                                          p->second_bits, ctx->fine_bits, canonical, geo, ctx->bin_count.p,
+                                          ctx->bin_kmers.p, ctx->stage.p, ctx->block_count.p, ovf_cap,
+                                          ctx->ovf_cursor.p, ctx->status.p, s);
         CK(cudaGetLastError());
         ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
         ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(&totals[2], ctx->stage_cursor.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&totals[2], ctx->ovf_cursor.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        if (totals[2] <= ctx->stage.n) break;
-        stage_cap = totals[2] + 1024;
+        if (totals[2] <= ovf_cap) break;
+        ovf_cap = totals[2] + 1024;
     }
-    if (totals[2] > ctx->stage.n || totals[2] != totals[0])
-        return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: staging mismatch (%llu staged, %llu counted)", totals[2],
-                    totals[0]);
+    if (totals[2] > ovf_cap)
+        return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: staging overflow (%llu overflow records)", totals[2]);
     ctx->n_recs = totals[0];
     ctx->n_kmers = totals[1];
     CK(ctx->recs.ensure(ctx->n_recs + 1));
-    ctx->launches += launch_partition(ctx->stage.p, ctx->n_recs, ctx->fine_bits, ctx->bin_off.p, ctx->bin_cursor.p,
-                                      ctx->recs.p, ctx->status.p, ctx->sms, s);
+    ctx->launches += launch_partition(ctx->stage.p, geo, ctx->block_count.p, ctx->ovf_cursor.p, ovf_cap,
+                                      ctx->fine_bits, ctx->bin_off.p, ctx->bin_cursor.p, ctx->recs.p, ctx->status.p,
+                                      s);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[2], s));
     ctx->n_text = text_len;

@@ -9,12 +9,22 @@ namespace ggcat {
 
 // bucketing.cu — each launcher returns the number of kernels it launched
 int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *valid, cudaStream_t s, int sms);
+// Launch geometry of bucketize_kernel: thread t owns `chunk` window starts and walks
+// `lookback` bases before them; block b stores its records in staging region b
+// (region_cap records), the rest in the overflow area after the regions.
+struct BucketizeGeometry {
+    uint32_t threads_per_block, chunk, lookback, blocks, region_cap;
+    size_t smem;
+};
+BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m);
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
-                     int fbits, int canonical, uint64_t chunk_hint, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long stage_cap,
-                     unsigned long long *stage_cursor, unsigned *status, cudaStream_t s);
-int launch_partition(const SkRec *stage, uint64_t n_stage, int fbits, const unsigned long long *bin_off,
-                     unsigned long long *bin_cursor, SkRec *recs, unsigned *status, int sms, cudaStream_t s);
+                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
+                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
+                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s);
+int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
+                     const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
+                     const unsigned long long *bin_off, unsigned long long *bin_cursor, SkRec *recs, unsigned *status,
+                     cudaStream_t s);
 uint64_t scan_temp_elems(uint64_t n);
 // out has n+1 entries: exclusive prefix sums and the total at out[n]
 int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
