@@ -58,6 +58,8 @@ class Stats(C.Structure):
         ("merge_units_spilled", C.c_uint64),
         ("merge_units_ext_global", C.c_uint64),
         ("merge_units_walk", C.c_uint64),
+        ("merge_graph_captures", C.c_uint64),
+        ("merge_graph_replays", C.c_uint64),
     ]
 
 

@@ -510,6 +510,12 @@ int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *v
     return 1;
 }
 
+cudaError_t bucketize_configure() {
+    cudaError_t e = cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
 BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m) {
     BucketizeGeometry g{};
     const int wn = k - m;
@@ -530,12 +536,6 @@ int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, 
                      unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
                      unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s) {
     if (g.blocks == 0) return 0;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
-    }
     if (m > 16)
         bucketize_kernel<true><<<g.blocks, g.threads_per_block, g.smem, s>>>(
             packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,

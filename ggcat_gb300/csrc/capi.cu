@@ -69,6 +69,13 @@ struct HostUnitigs {
 
 }  // namespace
 
+// Everything the captured merge launches depend on: a replay is valid while all of it is
+// unchanged (zero-initialised with memset so padding compares equal).
+struct MergeGraphKey {
+    const void *ptr[24];
+    uint64_t val[16];
+};
+
 struct ggcat_gpu_ctx {
     int device = 0;
     int sms = 1;
@@ -112,6 +119,12 @@ struct ggcat_gpu_ctx {
     DevBuf<uint8_t> tvis;
     DevBuf<uint32_t> tlist;  // created-entry lists of the M units
     DevBuf<uint8_t> ext_scratch;  // per-CTA extension scratch of units with many survivors
+    // the batched merge phase as a CUDA graph, captured once per buffer/parameter layout
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t merge_exec = nullptr;
+    MergeGraphKey merge_key{};
+    int merge_graph_kernels = 0;
+    uint64_t merge_graph_captures = 0, merge_graph_replays = 0;
     DevBuf<uint8_t> out_bases;
     DevBuf<uint64_t> out_off;
     DevBuf<uint32_t> out_len;
@@ -205,6 +218,11 @@ extern "C" int ggcat_gpu_create(int device, ggcat_gpu_ctx **out) {
     }
     unsigned long long one = 1;
     cudaMemcpy(ctx->ones.p, &one, sizeof one, cudaMemcpyHostToDevice);
+    if (bucketize_configure() != cudaSuccess || merge_configure() != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return GGCAT_GPU_ECUDA;
+    }
     *out = ctx;
     return GGCAT_GPU_OK;
 }
@@ -212,6 +230,8 @@ extern "C" int ggcat_gpu_create(int device, ggcat_gpu_ctx **out) {
 extern "C" void ggcat_gpu_destroy(ggcat_gpu_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    if (ctx->merge_exec) cudaGraphExecDestroy(ctx->merge_exec);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     delete ctx;
 }
 
@@ -380,9 +400,6 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     const uint64_t stride_sw = ((uint64_t)kExtCapShared * bps + 255) & ~255ull;
     const uint64_t stride_m = ((uint64_t)kExtCapMedium * bps + 255) & ~255ull;
     CK(ctx->ext_scratch.ensure(std::max<uint64_t>(2ull * ctx->sms * stride_sw, (uint64_t)ctx->sms * stride_m)));
-    CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
-
     MergeArgs a{ctx->packed.p, ctx->recs.p, p->k,           p->min_multiplicity, p->keep_kmers, wide,
                 ctx->ext_scratch.p, stride_sw, kExtCapShared};
     MergeArgs am = a;
@@ -395,8 +412,10 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1024 : 2048);
     if (target > small_limit) target = small_limit;
 
-    CK(cudaEventRecord(ctx->ev[3], s));
     if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) {
+        CK(cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+        CK(cudaEventRecord(ctx->ev[3], s));
         // plain form: every bucket is one unit with a global-memory table, three launches per bucket
         std::vector<unsigned long long> hoff(ctx->n_bins + 1), hk(ctx->n_bins + 1);
         CK(cudaMemcpyAsync(hoff.data(), ctx->bin_off.p, (ctx->n_bins + 1) * sizeof(unsigned long long),
@@ -436,20 +455,70 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     } else {
         const uint64_t medium_limit = 1ull << 18;
         const uint64_t wide_limit = p->unit_target < 0 ? 0 : merge_wide_limit(wide);
-        ctx->launches += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits,
-                                               small_limit, target, wide_limit, medium_limit, ctx->small_units.p,
-                                               ctx->wide_units.p, ctx->medium_units.p, ctx->large_units.p, max_units,
-                                               pool,
-                                               ctx->counters.p, ctx->status.p + 1, s);
-        ctx->launches += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, s);
-        ctx->launches += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o,
-                                           ctx->sms, s);
-        ctx->launches += launch_merge_medium(am, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
-                                             ctx->tvis.p, ctx->tlist.p, o, ctx->sms, s);
-        ctx->launches += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
-                                                 ctx->tvals.p, ctx->tvis.p, ctx->sms, s);
-        ctx->launches += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p,
-                                            ctx->tvals.p, ctx->tvis.p, o, ctx->sms, s);
+        // the whole batched merge phase: counter reset, classification, the S/W/M persistent
+        // kernels fed by device work queues and the grid-wide L kernels
+        auto enqueue = [&](cudaStream_t q) -> int {
+            int n = 0;
+            if (cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), q) != cudaSuccess) return -1;
+            if (cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), q) != cudaSuccess) return -1;
+            n += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits, small_limit,
+                                       target, wide_limit, medium_limit, ctx->small_units.p, ctx->wide_units.p,
+                                       ctx->medium_units.p, ctx->large_units.p, max_units, pool, ctx->counters.p,
+                                       ctx->status.p + 1, q);
+            n += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, q);
+            n += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o, ctx->sms,
+                                   q);
+            n += launch_merge_medium(am, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
+                                     ctx->tvis.p, ctx->tlist.p, o, ctx->sms, q);
+            n += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
+                                         ctx->tvals.p, ctx->tvis.p, ctx->sms, q);
+            n += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p, ctx->tvals.p,
+                                    ctx->tvis.p, o, ctx->sms, q);
+            return n;
+        };
+        MergeGraphKey key;
+        memset(&key, 0, sizeof key);
+        const void *ptrs[] = {ctx->packed.p,       ctx->recs.p,        ctx->ext_scratch.p,  ctx->out_bases.p,
+                              ctx->out_off.p,      ctx->out_len.p,     ctx->out_flags.p,    ctx->kmer_keys.p,
+                              ctx->kmer_mult.p,    ctx->counters.p,    ctx->status.p,       ctx->bin_off.p,
+                              ctx->bin_kmers.p,    ctx->small_units.p, ctx->wide_units.p,   ctx->medium_units.p,
+                              ctx->large_units.p,  ctx->tkeys.p,       ctx->tvals.p,        ctx->tvis.p,
+                              ctx->tlist.p};
+        static_assert(sizeof(ptrs) / sizeof(ptrs[0]) <= sizeof(key.ptr) / sizeof(key.ptr[0]), "graph key");
+        memcpy(key.ptr, ptrs, sizeof ptrs);
+        const uint64_t vals[] = {(uint64_t)p->k,     (uint64_t)p->min_multiplicity, (uint64_t)p->keep_kmers,
+                                 (uint64_t)wide,     bases_cap,                     u_cap,
+                                 p->keep_kmers ? kmer_cap : 0, ctx->n_buckets,      (uint64_t)ctx->fine_bits,
+                                 target,             wide_limit,                    max_units,
+                                 pool,               stride_sw,                     stride_m,
+                                 (uint64_t)ctx->sms};
+        static_assert(sizeof(vals) / sizeof(vals[0]) <= sizeof(key.val) / sizeof(key.val[0]), "graph key");
+        memcpy(key.val, vals, sizeof vals);
+        if (!ctx->merge_exec || memcmp(&key, &ctx->merge_key, sizeof key) != 0) {
+            if (ctx->merge_exec) {
+                cudaGraphExecDestroy(ctx->merge_exec);
+                ctx->merge_exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeThreadLocal));
+            const int n = enqueue(ctx->cap_stream);
+            const cudaError_t ec = cudaStreamEndCapture(ctx->cap_stream, &g);
+            if (n < 0 || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return fail(ctx, GGCAT_GPU_ECUDA, "merge graph capture failed (%s)", cudaGetErrorString(ec));
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&ctx->merge_exec, g, 0);
+            cudaGraphDestroy(g);
+            CK(ei);
+            ctx->merge_key = key;
+            ctx->merge_graph_kernels = n;
+            ctx->merge_graph_captures++;
+        }
+        CK(cudaEventRecord(ctx->ev[3], s));
+        CK(cudaGraphLaunch(ctx->merge_exec, s));
+        ctx->launches += (uint64_t)ctx->merge_graph_kernels;
+        ctx->merge_graph_replays++;
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[4], s));
@@ -717,6 +786,8 @@ extern "C" int ggcat_gpu_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint
 extern "C" int ggcat_gpu_get_stats(const ggcat_gpu_ctx *ctx, ggcat_gpu_stats *out) {
     if (!ctx || !out) return GGCAT_GPU_EINVAL;
     *out = ctx->stats;
+    out->merge_graph_captures = ctx->merge_graph_captures;
+    out->merge_graph_replays = ctx->merge_graph_replays;
     return GGCAT_GPU_OK;
 }
 

@@ -17,6 +17,10 @@ struct BucketizeGeometry {
     size_t smem;
 };
 BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m);
+// kernel attributes (dynamic shared memory limits) of the current device; called once per
+// context, outside any stream capture
+cudaError_t bucketize_configure();
+cudaError_t merge_configure();
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
                      int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
                      unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,

@@ -332,70 +332,89 @@ __device__ __forceinline__ uint32_t table_cap_for(uint64_t kk) {
     return (uint32_t)cap;
 }
 
-__global__ void classify_units_kernel(const unsigned long long *__restrict__ bin_off,
-                                      const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets, int fbits,
-                                      uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
-                                      uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
-                                      MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
-                                      uint64_t pool_slots, unsigned long long *counters, unsigned *status) {
-    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per bucket: the lanes load 32 sub-bins' counts and offsets at a time (coalesced)
+// and the warp walks them in order with the counts in registers (the same greedy packing on
+// every lane; lane 0 writes the units).
+__global__ void __launch_bounds__(128) classify_units_kernel(
+    const unsigned long long *__restrict__ bin_off, const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets,
+    int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit, uint64_t medium_limit,
+    MergeUnit *small_units, MergeUnit *wide_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
+    uint64_t pool_slots, unsigned long long *counters, unsigned *status) {
+    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (b >= n_buckets) return;
     const uint32_t nsub = 1u << fbits;
-    uint64_t cur_begin = 0, cur_k = 0;
+    uint64_t cur_begin = 0, cur_end = 0, cur_k = 0;
     bool open = false;
-    auto close_small = [&](uint32_t end_sub) {
+    auto close_small = [&]() {
         if (!open) return;
-        unsigned long long i = atomicAdd(&counters[kCntSmall], 1ull);
-        if (i >= max_units) atomicOr(status, kStatusTableFull);
-        if (i < max_units) {
-            MergeUnit u;
-            u.rec_begin = cur_begin;
-            u.rec_end = bin_off[(uint64_t)b * nsub + end_sub];
-            u.kmers = cur_k;
-            u.table_off = 0;
-            u.table_cap = 0;
-            u.bucket = b;
-            small_units[i] = u;
+        if (lane == 0) {
+            unsigned long long i = atomicAdd(&counters[kCntSmall], 1ull);
+            if (i >= max_units) atomicOr(status, kStatusTableFull);
+            if (i < max_units) {
+                MergeUnit u;
+                u.rec_begin = cur_begin;
+                u.rec_end = cur_end;
+                u.kmers = cur_k;
+                u.table_off = 0;
+                u.table_cap = 0;
+                u.bucket = b;
+                small_units[i] = u;
+            }
         }
         open = false;
         cur_k = 0;
     };
-    for (uint32_t j = 0; j < nsub; j++) {
-        uint64_t bin = (uint64_t)b * nsub + j;
-        uint64_t kk = bin_kmers[bin];
-        if (kk == 0) continue;
-        if (kk > small_limit) {
-            close_small(j);
-            // wide: a W unit tries the shared-memory table first (it fits when the sub-bin
-            // repeats its k-mers enough) and moves to the M tier with this reserved table when
-            // its distinct k-mers overflow the shared-memory table
-            const bool wide = kk <= wide_limit;
-            const bool medium = kk <= medium_limit;
-            unsigned long long i = atomicAdd(&counters[wide ? kCntWide : medium ? kCntMedium : kCntLarge], 1ull);
-            uint32_t cap = table_cap_for(kk);
-            unsigned long long off = atomicAdd(&counters[kCntSlots], (unsigned long long)cap);
-            if (off + cap > pool_slots || i >= max_units) {
-                atomicOr(status, kStatusTableFull);
+    for (uint32_t j0 = 0; j0 < nsub; j0 += 32) {
+        const uint64_t my_bin = (uint64_t)b * nsub + j0 + (uint32_t)lane;
+        const bool in = j0 + (uint32_t)lane < nsub;
+        const uint64_t my_k = in ? bin_kmers[my_bin] : 0ull;
+        const uint64_t my_beg = in ? bin_off[my_bin] : 0ull;
+        const uint64_t my_end = in ? bin_off[my_bin + 1] : 0ull;
+        if (__ballot_sync(0xffffffffu, my_k != 0) == 0) continue;
+        const uint32_t cnt = min(32u, nsub - j0);
+        for (uint32_t i = 0; i < cnt; i++) {
+            const uint64_t kk = __shfl_sync(0xffffffffu, my_k, (int)i);
+            const uint64_t beg = __shfl_sync(0xffffffffu, my_beg, (int)i);
+            const uint64_t end = __shfl_sync(0xffffffffu, my_end, (int)i);
+            if (kk == 0) continue;
+            if (kk > small_limit) {
+                close_small();
+                // wide: a W unit tries the shared-memory table first (it fits when the sub-bin
+                // repeats its k-mers enough) and moves to the M tier with this reserved table when
+                // its distinct k-mers overflow the shared-memory table
+                if (lane == 0) {
+                    const bool wide = kk <= wide_limit;
+                    const bool medium = kk <= medium_limit;
+                    unsigned long long ui =
+                        atomicAdd(&counters[wide ? kCntWide : medium ? kCntMedium : kCntLarge], 1ull);
+                    uint32_t cap = table_cap_for(kk);
+                    unsigned long long off = atomicAdd(&counters[kCntSlots], (unsigned long long)cap);
+                    if (off + cap > pool_slots || ui >= max_units) {
+                        atomicOr(status, kStatusTableFull);
+                    } else {
+                        MergeUnit u;
+                        u.rec_begin = beg;
+                        u.rec_end = end;
+                        u.kmers = kk;
+                        u.table_off = off;
+                        u.table_cap = cap;
+                        u.bucket = b;
+                        (wide ? wide_units : medium ? medium_units : large_units)[ui] = u;
+                    }
+                }
                 continue;
             }
-            MergeUnit u;
-            u.rec_begin = bin_off[bin];
-            u.rec_end = bin_off[bin + 1];
-            u.kmers = kk;
-            u.table_off = off;
-            u.table_cap = cap;
-            u.bucket = b;
-            (wide ? wide_units : medium ? medium_units : large_units)[i] = u;
-            continue;
+            if (open && cur_k + kk > unit_target) close_small();
+            if (!open) {
+                open = true;
+                cur_begin = beg;
+            }
+            cur_k += kk;
+            cur_end = end;
         }
-        if (open && cur_k + kk > unit_target) close_small(j);
-        if (!open) {
-            open = true;
-            cur_begin = bin_off[bin];
-        }
-        cur_k += kk;
     }
-    close_small(nsub);
+    close_small();
 }
 
 // ---------------------------------------------------------------------------
@@ -1122,7 +1141,7 @@ int launch_classify_units(const unsigned long long *bin_off, const unsigned long
                           uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
                           MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
                           unsigned long long *counters, unsigned *status, cudaStream_t s) {
-    classify_units_kernel<<<(n_buckets + 127) / 128, 128, 0, s>>>(
+    classify_units_kernel<<<(n_buckets + 3) / 4, 128, 0, s>>>(
         bin_off, bin_kmers, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, small_units,
         wide_units, medium_units, large_units, max_units, pool_slots, counters, status);
     return 1;
@@ -1133,14 +1152,24 @@ static void merge_tier_t(const MergeArgs &a, const MergeUnit *units, const unsig
                          uint32_t *vals, uint8_t *vis, uint32_t *list, MergeUnit *spill, uint64_t max_units,
                          const MergeOut &o, int sms, cudaStream_t s) {
     using Cfg = TierCfg<KT, kTier>;
-    static bool configured = false;
     const int smem = (int)sizeof(UnitSmem<KT, kTier>);
-    if (!configured) {
-        cudaFuncSetAttribute(merge_unit_kernel<KT, kTier>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        configured = true;
-    }
     merge_unit_kernel<KT, kTier>
         <<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(a, units, counters, keys, vals, vis, list, spill, max_units, o);
+}
+
+template <typename KT, int kTier>
+static cudaError_t merge_attr_t() {
+    return cudaFuncSetAttribute(merge_unit_kernel<KT, kTier>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(UnitSmem<KT, kTier>));
+}
+
+cudaError_t merge_configure() {
+    const cudaError_t e[6] = {merge_attr_t<uint64_t, kTierS>(), merge_attr_t<uint64_t, kTierW>(),
+                              merge_attr_t<uint64_t, kTierM>(), merge_attr_t<u128, kTierS>(),
+                              merge_attr_t<u128, kTierW>(),     merge_attr_t<u128, kTierM>()};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,

@@ -83,6 +83,8 @@ typedef struct {
     uint64_t merge_units_spilled; /* shared-memory attempts that moved to a global-memory table */
     uint64_t merge_units_ext_global; /* units ranked in global-memory scratch (many survivors) */
     uint64_t merge_units_walk;  /* units extended by per-thread walks (grid-wide tier, fallback) */
+    uint64_t merge_graph_captures; /* captures of the batched merge phase as a CUDA graph (context lifetime) */
+    uint64_t merge_graph_replays;  /* launches of that graph (context lifetime) */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */

@@ -196,6 +196,30 @@ def test_genome_family_min_multiplicity_one(ctx):
     assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
 
 
+def test_merge_phase_replays_as_cuda_graph():
+    """The batched merge phase is captured as a CUDA graph once per buffer layout and then
+    replayed: a second build of the same input replays without a new capture and gives the
+    same unitigs (both equal to the oracle's)."""
+    c = GpuContext(0)
+    try:
+        text, off, ln, _ = _workload("reads", 11)
+        p = make_params(k=31, m=10, bucket_bits=8, second_bits=2, min_multiplicity=2)
+        outs, st = [], []
+        for _ in range(2):
+            c.build_text(text, p)
+            st.append(c.stats())
+            c.link(31)
+            bases, uo, ul, uf = c.unitigs()
+            outs.append(oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31))
+        assert st[0]["merge_graph_captures"] >= 1
+        assert st[1]["merge_graph_captures"] == st[0]["merge_graph_captures"]
+        assert st[1]["merge_graph_replays"] == st[0]["merge_graph_replays"] + 1
+        r = oracle.build_graph(text, off, ln, _oracle_params(p))
+        assert outs[0] == outs[1] == r.unitigs()
+    finally:
+        c.close()
+
+
 def test_device_pointer_bucketize(ctx):
     """bucketize on a caller-owned device buffer and stream (torch only as plumbing)."""
     torch = pytest.importorskip("torch")
