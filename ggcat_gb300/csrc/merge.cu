@@ -84,6 +84,49 @@ __device__ __forceinline__ int64_t tinsert_created(const Table<KT> &t, KT key, u
     return -1;
 }
 
+// Shared-memory forms of the table operations (explicit state space: the table pointers reach
+// the helpers through a struct, so the shared window is stated rather than inferred).
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t lds_u64(uint32_t a) {
+    uint64_t v;
+    asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t cas_shared_u64(uint32_t a, uint64_t cmp, uint64_t val) {
+    uint64_t o;
+    asm volatile("atom.shared.cas.b64 %0, [%1], %2, %3;" : "=l"(o) : "r"(a), "l"(cmp), "l"(val) : "memory");
+    return o;
+}
+__device__ __forceinline__ void red_shared_add_u32(uint32_t a, uint32_t x) {
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(x) : "memory");
+}
+__device__ __forceinline__ void red_shared_or_b32(uint32_t a, uint32_t x) {
+    asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(a), "r"(x) : "memory");
+}
+
+// tinsert on a shared-memory table of u64 keys; created reports whether this call made the entry
+__device__ __forceinline__ int64_t tinsert_shared(const Table<uint64_t> &t, uint64_t key, unsigned *status,
+                                                  bool &created) {
+    uint32_t s = slot_of(key, t.cap);
+    const uint32_t kb = smem_addr(t.keys);
+    created = false;
+    for (uint32_t probe = 0; probe < t.cap; probe++) {
+        const uint64_t kk = lds_u64(kb + 8u * s);
+        if (kk == key) return s;
+        if (kk == ~0ull) {
+            const uint64_t old = cas_shared_u64(kb + 8u * s, ~0ull, key);
+            if (old == ~0ull) {
+                created = true;
+                return s;
+            }
+            if (old == key) return s;
+        }
+        s = (s + 1) & (t.cap - 1);
+    }
+    atomicOr(status, kStatusTableFull);
+    return -1;
+}
+
 // MapEntry::get_kmer_multiplicity (map_entry.rs:79-84): halve when both ends were ignored.
 __device__ __forceinline__ uint32_t val_mult(uint32_t v) {
     uint32_t c = v & kCountMask;
@@ -473,6 +516,7 @@ struct SmemTableView {
 };
 
 constexpr int kStageWords = 4;  // packed words staged per record (records spanning more read global memory)
+constexpr int kRecBatch = 32;   // records per insert batch of a warp (<= 32)
 
 // block-shared scalars of the extension phase
 struct ExtShared {
@@ -489,6 +533,7 @@ struct UnitSmemCommon {
     uint32_t warp_tmp[NT / 32 + 1];
     uint64_t unit;
     uint32_t distinct;  // entries created (optimistic units)
+    uint32_t batch_head;  // next record batch of the insert phase
     ExtShared x;
 };
 template <typename KT, int kTier, bool kShared = (kTier != kTierM)>
@@ -900,25 +945,32 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             S.x.loc_bases = 0;
             S.x.loc_count = 0;
             S.distinct = 0;
+            S.batch_head = 0;
         }
         __syncthreads();
 
         const uint64_t n_items = U.rec_end - U.rec_begin;
 
-        // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes 32 records at a
-        //      time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is
+        // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes kRecBatch records at
+        //      a time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is
         //      found from the mask of record starts in the current 32-k-mer window, so the
         //      insert phase needs no block barrier. ----
         {
-            constexpr int NW = NT / 32;
-            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            const int lane = threadIdx.x & 31;
             const unsigned full = 0xffffffffu;
             bool stop = false;
-            for (uint64_t ib = (uint64_t)wid * 32; ib < n_items && !stop; ib += (uint64_t)NW * 32) {
+            for (;;) {
+                // batches of kRecBatch records, claimed dynamically (no static warp imbalance at
+                // the barrier that ends the phase)
+                uint32_t bi = 0;
+                if (lane == 0) bi = atomicAdd(&S.batch_head, 1u);
+                bi = __shfl_sync(full, bi, 0);
+                const uint64_t ib = (uint64_t)bi * kRecBatch;
+                if (ib >= n_items || stop) break;
                 const uint64_t item = ib + lane;
                 uint64_t w0 = 0;
                 uint32_t fr = 0, nk = 0;
-                if (item < n_items) {
+                if (lane < kRecBatch && item < n_items) {
                     const SkRec rr = a.recs[U.rec_begin + item];
                     w0 = rr.w0;
                     fr = rec_flags(rr) | (rec_rc(rr) << 2);
@@ -979,7 +1031,9 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                                                        pos - ((rw0 & ((1ull << 40) - 1)) & ~31ull), k);
                     const KT rc = K::rc(fw, k);
                     const uint32_t isf = fw < rc ? 1u : 0u;
-                    if (optimistic || kGlobalTable)
+                    if constexpr (!kGlobalTable && std::is_same<KT, uint64_t>::value)
+                        sl = tinsert_shared(t, isf ? fw : rc, o.status, created);
+                    else if (optimistic || kGlobalTable)
                         sl = tinsert_created(t, isf ? fw : rc, o.status, created);
                     else
                         sl = tinsert(t, isf ? fw : rc, o.status);
@@ -999,8 +1053,14 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                         }
                     }
                     if (sl < 0) continue;
-                    if (fbits) atomicOr(&t.vals[sl], fbits << 30);
-                    atomicAdd(&t.vals[sl], 1u);
+                    if constexpr (!kGlobalTable) {
+                        const uint32_t va = smem_addr(t.vals + sl);
+                        if (fbits) red_shared_or_b32(va, fbits << 30);
+                        red_shared_add_u32(va, 1u);
+                    } else {
+                        if (fbits) atomicOr(&t.vals[sl], fbits << 30);
+                        atomicAdd(&t.vals[sl], 1u);
+                    }
                 }
                 __syncwarp();  // the next batch overwrites this warp's staged words
             }
