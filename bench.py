@@ -55,7 +55,12 @@ def _args():
     ap.add_argument("--no-colored", action="store_true", help="skip the coloured build + query measurement")
     ap.add_argument("--colors", type=int, default=256, help="genomes (colours) of the coloured workload")
     ap.add_argument("--query-genomes", type=int, default=16, help="member genomes of the queried graph")
-    ap.add_argument("--queries", type=int, default=20000)
+    ap.add_argument("--queries", type=int, default=20000, help="queries of the uncoloured serving measurement")
+    ap.add_argument("--colored-queries", type=int, default=100000,
+                    help="queries of the coloured serving measurement (against the 256-genome coloured graph)")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the autotuned-knobs measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 3-genome and long-k build measurements")
     ap.add_argument("--query-rate", type=float, default=20000.0, help="Poisson arrival rate (queries/s)")
     return ap.parse_args()
 
@@ -238,11 +243,14 @@ def colored_bench(args, ctx, torch, dev):
     st = ctx.stats()
     ctx.query_index_colored()
     genomes = [w.text[int(o):int(o) + int(ln)] for o, ln in zip(w.seq_off.tolist(), w.seq_len.tolist())]
-    qt, qo, ql, arr = synth.query_workload(genomes, args.queries, rate_per_s=args.query_rate)
+    qt, qo, ql, arr = synth.query_workload(genomes, args.colored_queries, rate_per_s=args.query_rate)
     serve.serve(ctx, 31, qt, qo[:200], ql[:200], np.zeros(200), slots=4, colored=True)
     free, _ = torch.cuda.mem_get_info(dev)
     budget = int(max(1 << 22, min(free // 16, 256 << 20)))
     rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget, colored=True)
+    n1 = min(len(qo), 2000)
+    r1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, one_per_launch=True, colored=True)
+    same = bool((rb.matched[:n1] == r1.matched).all() and (rb.color_totals[:n1] == r1.color_totals).all())
     return {
         "workload": w.name, "bases": int(w.bases), "colors": args.colors,
         "build": {**res, "device_gbases_per_s": round(w.bases / ((res["ms_bucketize"] + res["ms_merge"]) * 1e-3) / 1e9, 3),
@@ -251,8 +259,83 @@ def colored_bench(args, ctx, torch, dev):
         "query": {"queries": int(len(qo)), "query_kmers": int(rb.kmers), "arrival_rate_per_s": args.query_rate,
                   "kmers_per_s": round(rb.kmers_per_s, 1), "p50_ms": round(rb.pct_ms(50), 3),
                   "p99_ms": round(rb.pct_ms(99), 3), "batches": rb.batches, "max_batch_kmers": budget,
-                  "color_hits_total": int(rb.color_totals.sum())},
+                  "color_hits_total": int(rb.color_totals.sum()),
+                  "one_per_launch": {"queries": int(n1), "kmers_per_s": round(r1.kmers_per_s, 1),
+                                     "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3)},
+                  "results_identical_alone_vs_batched": same},
     }
+
+
+def build_config_bench(w, torch, dev, steps=3, cpu_threads=0, tune=False):
+    """One build workload on a fresh context: device Gbases/s (bucketize + merge, input in
+    HBM, median of `steps` after one warm-up) and end-to-end Gbases/s through the C ABI from
+    pinned host memory (text copy in, partial unitigs out), plus the host link stage time.
+    With cpu_threads > 0 the oracle (CPU restatement) builds the whole input too."""
+    from ggcat_gb300 import _native
+
+    ctx = _native.GpuContext(dev)
+    try:
+        hk = _native.GGCAT_HASH_RABIN_KARP128 if getattr(w, "hash_kind", "") == "rk128" else _native.GGCAT_HASH_SEQHASH
+        p = _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
+                                min_multiplicity=w.min_multiplicity, hash_kind=hk)
+        d = torch.from_numpy(w.text).to(f"cuda:{dev}")
+        ms = []
+        for i in range(steps + 1):
+            ctx.bucketize(d.data_ptr(), d.numel(), p, 0)
+            ctx.merge(p, 0)
+            torch.cuda.synchronize()
+            st = ctx.stats()
+            if i:
+                ms.append(st["ms_pack"] + st["ms_bucketize"] + st["ms_merge"])
+        tuned = None
+        if tune:
+            t0 = time.perf_counter()
+            best, d_ms, b_ms = ctx.autotune(d.data_ptr(), d.numel(), p)
+            tune_s = time.perf_counter() - t0
+            ms_t = []
+            for i in range(steps + 1):
+                ctx.bucketize(d.data_ptr(), d.numel(), best, 0)
+                ctx.merge(best, 0)
+                torch.cuda.synchronize()
+                st = ctx.stats()
+                if i:
+                    ms_t.append(st["ms_pack"] + st["ms_bucketize"] + st["ms_merge"])
+            tuned = {"device_gbases_per_s": round(w.bases / (statistics.median(ms_t) * 1e-3) / 1e9, 3),
+                     "device_ms": round(statistics.median(ms_t), 3), "tuning_s": round(tune_s, 2),
+                     "knobs": {f: int(getattr(best, f)) for f in ("subbin_bytes", "unit_target", "small_limit",
+                                                                 "table_load_pct")}}
+        del d
+        dev_ms = statistics.median(ms)
+        h = torch.from_numpy(w.text).pin_memory()
+        ctx.build_text(h.numpy(), p)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.build_text(h.numpy(), p)
+        e2e_s = time.perf_counter() - t0
+        ctx.link(w.k)
+        st = ctx.stats()
+        out = {"workload": w.name, "bases": int(w.bases), "k": w.k, "m": w.m, "buckets": 1 << w.bucket_bits,
+               "min_multiplicity": w.min_multiplicity, "hash": getattr(w, "hash_kind", "seq-hash"),
+               "device_gbases_per_s": round(w.bases / (dev_ms * 1e-3) / 1e9, 3), "device_ms": round(dev_ms, 3),
+               "e2e_gbases_per_s": round(w.bases / e2e_s / 1e9, 3), "link_ms_host": round(st["ms_link"], 1),
+               "autotuned": tuned,
+               "superkmers": int(st["superkmers"]), "kmer_instances": int(st["kmer_instances"]),
+               "surviving_kmers_by_subbucket": int(st["surviving_kmers"]), "final_unitigs": int(st["final_unitigs"])}
+    finally:
+        ctx.close()
+    if cpu_threads > 0:
+        import oracle
+
+        op = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
+                           min_multiplicity=w.min_multiplicity, threads=cpu_threads,
+                           hash_kind=oracle.H_CN_RK128 if getattr(w, "hash_kind", "") == "rk128" else None)
+        t0 = time.perf_counter()
+        r = oracle.build_graph(w.text, w.seq_off, w.seq_len, op)
+        dt = time.perf_counter() - t0
+        del r
+        out["cpu_oracle"] = {"gbases_per_s": round(w.bases / dt / 1e9, 5), "seconds": round(dt, 2),
+                             "cores": cpu_threads, "kind": "port"}
+    return out
 
 
 def run_reference(args):
@@ -356,6 +439,20 @@ def run_gpu(args):
     clocks = clk.summary()
     value = bases * ws / (ms * 1e-3) / 1e9
 
+    # autotuned knobs (sub-bin digit width, S-unit packing and size limit, table load) on the
+    # same input, timed like the headline
+    autotuned = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        best, d_ms, b_ms = ctx.autotune(d_text.data_ptr(), d_text.numel(), pb, 0, sptr)
+        tune_s = time.perf_counter() - t0
+        ms_t, _, phases_t, _ = timed(best, max(1, min(args.steps, 3)), 1)
+        autotuned = {"value": round(bases * ws / (ms_t * 1e-3) / 1e9, 4), "ms_per_step": round(ms_t, 3),
+                     "phases_ms": {k2: round(v, 3) for k2, v in phases_t.items()},
+                     "knobs": {f: int(getattr(best, f)) for f in ("subbin_bytes", "unit_target", "small_limit",
+                                                                 "table_load_pct")},
+                     "tuning_s": round(tune_s, 2), "trial_ms_default": round(d_ms, 3), "trial_ms_tuned": round(b_ms, 3)}
+
     per_bucket = None
     if not args.no_per_bucket:
         pp = params(_native.GGCAT_MERGE_PER_BUCKET)
@@ -416,6 +513,17 @@ def run_gpu(args):
     colored = None
     if rank == 0 and not args.no_colored:
         colored = colored_bench(args, ctx, torch, dev)
+    ctx.close()
+    del d_text
+    torch.cuda.empty_cache()
+
+    configs = None
+    if rank == 0 and not args.no_configs:
+        from ggcat_gb300 import synth
+
+        configs = {"genomes_3x5Mbp": build_config_bench(synth.config_genomes(), torch, dev, steps=5,
+                                                        cpu_threads=os.cpu_count() or 1)}
+        configs["longk_2Gbp"] = build_config_bench(synth.config_long_k(), torch, dev, steps=3, tune=True)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -449,6 +557,7 @@ def run_gpu(args):
                       "small_units": int(st["merge_units_small"]), "large_units": int(st["merge_units_large"]),
                       "spilled_units": int(st["merge_units_spilled"])},
             "per_bucket": per_bucket,
+            "autotuned": autotuned,
             "e2e": {"value": round(e2e_value, 4), "unit": "Gbases/s", "h2d_bytes_per_step": int(n),
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
@@ -457,13 +566,13 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "query": query,
             "colored": colored,
+            "configs": configs,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
-    ctx.close()
     return 0
 
 
@@ -472,6 +581,7 @@ def main():
     if args.workload != "skewed":
         args.no_query = True  # the query and coloured sections use k=31 graphs
         args.no_colored = True
+        args.no_configs = True
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

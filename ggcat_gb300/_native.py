@@ -36,6 +36,9 @@ class Params(C.Structure):
         ("merge_mode", C.c_int32),
         ("unit_target", C.c_int32),
         ("keep_kmers", C.c_int32),
+        ("subbin_bytes", C.c_int32),
+        ("table_load_pct", C.c_int32),
+        ("small_limit", C.c_int32),
     ]
 
 
@@ -85,6 +88,7 @@ EXPORTED = [
     "ggcat_gpu_bucketize",
     "ggcat_gpu_superkmers_copy",
     "ggcat_gpu_merge",
+    "ggcat_gpu_autotune",
     "ggcat_gpu_partial_unitigs_copy",
     "ggcat_gpu_kmers_copy",
     "ggcat_gpu_link",
@@ -136,6 +140,8 @@ def load(build: bool = True):
     L.ggcat_gpu_bucketize.argtypes = [P, P, u64, C.POINTER(Params), P, pu64]
     L.ggcat_gpu_superkmers_copy.argtypes = [P, P, u64, pu64]
     L.ggcat_gpu_merge.argtypes = [P, C.POINTER(Params), P]
+    L.ggcat_gpu_autotune.argtypes = [P, P, u64, C.POINTER(Params), u64, P, C.POINTER(Params),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ggcat_gpu_partial_unitigs_copy.argtypes = [P, P, u64, P, P, P, u64, pu64, pu64]
     L.ggcat_gpu_kmers_copy.argtypes = [P, P, P, u64, pu64]
     L.ggcat_gpu_link.argtypes = [P, C.c_int]
@@ -171,11 +177,12 @@ def _ptr(a):
 
 
 def make_params(k=31, m=None, bucket_bits=10, second_bits=3, min_multiplicity=1, hash_kind=GGCAT_HASH_SEQHASH,
-                forward_only=False, merge_mode=GGCAT_MERGE_BATCHED, unit_target=0, keep_kmers=False) -> Params:
+                forward_only=False, merge_mode=GGCAT_MERGE_BATCHED, unit_target=0, keep_kmers=False,
+                subbin_bytes=0, table_load_pct=0, small_limit=0) -> Params:
     if m is None:
         m = compute_best_m(k)
     return Params(k, m, bucket_bits, second_bits, min_multiplicity, hash_kind, int(forward_only), merge_mode,
-                  unit_target, int(keep_kmers))
+                  unit_target, int(keep_kmers), subbin_bytes, table_load_pct, small_limit)
 
 
 def compute_best_m(k: int) -> int:
@@ -346,6 +353,16 @@ class GpuContext:
         self._check(self.L.ggcat_gpu_query_color_counts(self.h, slot, _ptr(out), out.size, C.byref(nc)),
                     "query_color_counts")
         return out.reshape(nq, nc.value)
+
+    def autotune(self, d_text: int, n: int, p: Params, sample_bytes: int = 0, stream: int = 0):
+        """Tuned copy of p (device text at d_text), with the device times of p and of the
+        tuned params: (params, default_ms, tuned_ms)."""
+        best = Params()
+        dm, bm = C.c_double(), C.c_double()
+        self._check(self.L.ggcat_gpu_autotune(self.h, C.c_void_p(d_text), n, C.byref(p), sample_bytes,
+                                              C.c_void_p(stream), C.byref(best), C.byref(dm), C.byref(bm)),
+                    "autotune")
+        return best, dm.value, bm.value
 
     def stats(self) -> dict:
         s = Stats()

@@ -73,7 +73,7 @@ struct HostUnitigs {
 // unchanged (zero-initialised with memset so padding compares equal).
 struct MergeGraphKey {
     const void *ptr[24];
-    uint64_t val[16];
+    uint64_t val[24];
 };
 
 struct ggcat_gpu_ctx {
@@ -248,6 +248,10 @@ static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
         return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits=%d outside [1, 15]", p->bucket_bits);
     if (p->second_bits < 0 || p->second_bits > 8)
         return fail(ctx, GGCAT_GPU_EINVAL, "second_bits=%d outside [0, 8]", p->second_bits);
+    if (p->subbin_bytes < 0 || p->table_load_pct < 0 || p->table_load_pct > 95 ||
+        (p->table_load_pct > 0 && p->table_load_pct < 10) || p->small_limit < 0)
+        return fail(ctx, GGCAT_GPU_EINVAL, "tuning knob out of range (subbin_bytes=%d, table_load_pct=%d, small_limit=%d)",
+                    p->subbin_bytes, p->table_load_pct, p->small_limit);
     return GGCAT_GPU_OK;
 }
 
@@ -272,9 +276,10 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->packed.ensure(n_words));
     CK(ctx->valid.ensure(n_words));
     ctx->n_buckets = (1u << p->bucket_bits) + 1;
-    // sub-bins per bucket: about 1K k-mer instances per sub-bin on average
+    // sub-bins per bucket: about subbin_bytes (default 1K) text bytes per sub-bin on average
+    const uint64_t subbin = p->subbin_bytes > 0 ? (uint64_t)p->subbin_bytes : 1024ull;
     int fb = 0;
-    while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * 1024ull < text_len) fb++;
+    while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * subbin < text_len) fb++;
     ctx->fine_bits = fb < 4 ? 4 : fb;
     ctx->n_bins = (uint64_t)ctx->n_buckets << ctx->fine_bits;
     const uint64_t nb = ctx->n_bins;
@@ -388,8 +393,13 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->wide_units.ensure(max_units));
     CK(ctx->medium_units.ensure(max_units));
     CK(ctx->large_units.ensure(max_units));
-    // worst-case slot pool of the global-memory tables: cap < 2 * (1.25 x + 64) per unit
-    uint64_t pool = ctx->n_kmers * 5 / 2 + 128ull * (ctx->n_buckets + ctx->n_kmers / 4096 + 1) + 1024;
+    const uint64_t small_limit = p->small_limit > 0 ? std::min<uint64_t>((uint64_t)p->small_limit, merge_small_limit(wide))
+                                                    : merge_small_limit(wide);
+    // worst-case slot pool of the global-memory tables: cap < 2 * (x * 100 / load + 64) per unit,
+    // units of more than small_limit instances each
+    const uint32_t load_pct = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : 80u;
+    const uint64_t max_big_units = std::min<uint64_t>(ctx->n_bins, ctx->n_kmers / small_limit + 1);
+    uint64_t pool = ctx->n_kmers * 200 / load_pct + 2 + 128ull * (ctx->n_buckets + max_big_units) + 1024;
     CK(ctx->tkeys.ensure(pool * (wide ? 2 : 1)));
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
@@ -408,7 +418,6 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
-    const uint64_t small_limit = merge_small_limit(wide);
     uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1024 : 2048);
     if (target > small_limit) target = small_limit;
 
@@ -462,7 +471,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
             if (cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), q) != cudaSuccess) return -1;
             if (cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), q) != cudaSuccess) return -1;
             n += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits, small_limit,
-                                       target, wide_limit, medium_limit, ctx->small_units.p, ctx->wide_units.p,
+                                       target, wide_limit, medium_limit, load_pct, ctx->small_units.p, ctx->wide_units.p,
                                        ctx->medium_units.p, ctx->large_units.p, max_units, pool, ctx->counters.p,
                                        ctx->status.p + 1, q);
             n += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, q);
@@ -491,7 +500,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                  p->keep_kmers ? kmer_cap : 0, ctx->n_buckets,      (uint64_t)ctx->fine_bits,
                                  target,             wide_limit,                    max_units,
                                  pool,               stride_sw,                     stride_m,
-                                 (uint64_t)ctx->sms};
+                                 (uint64_t)ctx->sms, small_limit,                   load_pct};
         static_assert(sizeof(vals) / sizeof(vals[0]) <= sizeof(key.val) / sizeof(key.val[0]), "graph key");
         memcpy(key.val, vals, sizeof vals);
         if (!ctx->merge_exec || memcmp(&key, &ctx->merge_key, sizeof key) != 0) {
@@ -591,6 +600,90 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     ctx->stats.partial_bases = ctx->n_partial_bases;
     ctx->stats.surviving_kmers = ctx->n_kmers_out;
     ctx->have_merge = true;
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: the tuning knobs of the build hot path chosen by measurement
+// ---------------------------------------------------------------------------
+extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len,
+                                  const ggcat_gpu_params *p, uint64_t sample_bytes, void *stream,
+                                  ggcat_gpu_params *best, double *default_ms, double *best_ms) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (!best) return fail(ctx, GGCAT_GPU_EINVAL, "null output params");
+    if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) return fail(ctx, GGCAT_GPU_EINVAL, "autotune tunes the batched merge");
+    const uint64_t n = sample_bytes ? std::min(sample_bytes, text_len) : text_len;
+    const int wide = p->k > 32;
+    // device time of one candidate: the better of two runs; bucketize is redone only when the
+    // candidate changes the sub-bin digit width
+    auto trial = [&](const ggcat_gpu_params &q, bool rebucket, double &ms_bucket, double &ms_merge) -> int {
+        ms_bucket = ms_merge = 1e30;
+        for (int rep = 0; rep < 2; rep++) {
+            if (rebucket || rep == 0) {
+                uint64_t nsk = 0;
+                int r = ggcat_gpu_bucketize(ctx, d_text, n, &q, stream, &nsk);
+                if (r) return r;
+            }
+            int r = ggcat_gpu_merge(ctx, &q, stream);
+            if (r) return r;
+            if (rebucket) ms_bucket = std::min(ms_bucket, ctx->stats.ms_pack + ctx->stats.ms_bucketize);
+            ms_merge = std::min(ms_merge, ctx->stats.ms_merge);
+        }
+        return GGCAT_GPU_OK;
+    };
+    ggcat_gpu_params cur = *p;
+    double b_ms = 0, m_ms = 0;
+    rc = trial(cur, true, b_ms, m_ms);
+    if (rc) return rc;
+    const double d_ms = b_ms + m_ms;
+    // 1. sub-bin digit width (bucketize + merge)
+    double best_total = d_ms, best_bucket = b_ms, best_merge = m_ms;
+    int best_sb = cur.subbin_bytes;
+    for (int sb : {256, 512, 1024, 2048, 4096}) {
+        ggcat_gpu_params q = cur;
+        q.subbin_bytes = sb;
+        rc = trial(q, true, b_ms, m_ms);
+        if (rc) return rc;
+        if (b_ms + m_ms < best_total) {
+            best_total = b_ms + m_ms;
+            best_bucket = b_ms;
+            best_merge = m_ms;
+            best_sb = sb;
+        }
+    }
+    cur.subbin_bytes = best_sb;
+    {
+        uint64_t nsk = 0;
+        rc = ggcat_gpu_bucketize(ctx, d_text, n, &cur, stream, &nsk);
+        if (rc) return rc;
+    }
+    // 2. merge-only knobs, one at a time: S-unit packing target (-1: no W tier), S-unit size
+    //    limit, global-table load
+    const int targets_u64[] = {0, -1, 1024, 3200}, targets_u128[] = {0, -1, 512, 1600};
+    const int limits_u64[] = {0, 2400, 1600}, limits_u128[] = {0, 1200, 800};
+    const int loads[] = {0, 50, 65, 90};
+    for (int knob = 0; knob < 3; knob++) {
+        const int *vals = knob == 0 ? (wide ? targets_u128 : targets_u64) : knob == 1 ? (wide ? limits_u128 : limits_u64)
+                                                                                         : loads;
+        const int nv = knob == 2 ? 4 : knob == 0 ? 4 : 3;
+        int best_v = knob == 0 ? cur.unit_target : knob == 1 ? cur.small_limit : cur.table_load_pct;
+        for (int i = 0; i < nv; i++) {
+            ggcat_gpu_params q = cur;
+            (knob == 0 ? q.unit_target : knob == 1 ? q.small_limit : q.table_load_pct) = vals[i];
+            rc = trial(q, false, b_ms, m_ms);
+            if (rc) return rc;
+            if (m_ms < best_merge) {
+                best_merge = m_ms;
+                best_v = vals[i];
+            }
+        }
+        (knob == 0 ? cur.unit_target : knob == 1 ? cur.small_limit : cur.table_load_pct) = best_v;
+    }
+    *best = cur;
+    if (default_ms) *default_ms = d_ms;
+    if (best_ms) *best_ms = best_bucket + best_merge;
     return GGCAT_GPU_OK;
 }
 

@@ -104,7 +104,7 @@ constexpr int kMergeThreads = 256;
 // queue); <= medium_limit: M units; larger: L units.  W, M and L units reserve a global table.
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
                           int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
-                          uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
+                          uint64_t medium_limit, uint32_t load_pct, MergeUnit *small_units, MergeUnit *wide_units,
                           MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
                           unsigned long long *counters, unsigned *status, cudaStream_t s);
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,

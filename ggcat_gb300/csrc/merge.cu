@@ -369,9 +369,11 @@ __device__ __forceinline__ void cycle_slot(const Graph<KT> &g, uint32_t s, const
 //   M: one sub-bin up to medium_limit instances, one CTA with a global-memory table
 //   L: larger sub-bins, global-memory table processed grid-wide
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t table_cap_for(uint64_t kk) {
+// global-memory table capacity of a unit of kk instances: a power of two >= kk / load + 64
+__device__ __forceinline__ uint32_t table_cap_for(uint64_t kk, uint32_t load_pct) {
     uint64_t cap = 64;
-    while (cap < kk + kk / 4 + 64) cap <<= 1;
+    const uint64_t want = kk * 100 / load_pct + 64;
+    while (cap < want) cap <<= 1;
     return (uint32_t)cap;
 }
 
@@ -380,7 +382,7 @@ __device__ __forceinline__ uint32_t table_cap_for(uint64_t kk) {
 // every lane; lane 0 writes the units).
 __global__ void __launch_bounds__(128) classify_units_kernel(
     const unsigned long long *__restrict__ bin_off, const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets,
-    int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit, uint64_t medium_limit,
+    int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit, uint64_t medium_limit, uint32_t load_pct,
     MergeUnit *small_units, MergeUnit *wide_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
     uint64_t pool_slots, unsigned long long *counters, unsigned *status) {
     const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -431,7 +433,7 @@ __global__ void __launch_bounds__(128) classify_units_kernel(
                     const bool medium = kk <= medium_limit;
                     unsigned long long ui =
                         atomicAdd(&counters[wide ? kCntWide : medium ? kCntMedium : kCntLarge], 1ull);
-                    uint32_t cap = table_cap_for(kk);
+                    uint32_t cap = table_cap_for(kk, load_pct);
                     unsigned long long off = atomicAdd(&counters[kCntSlots], (unsigned long long)cap);
                     if (off + cap > pool_slots || ui >= max_units) {
                         atomicOr(status, kStatusTableFull);
@@ -1198,11 +1200,11 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
 // ---------------------------------------------------------------------------
 int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
                           int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
-                          uint64_t medium_limit, MergeUnit *small_units, MergeUnit *wide_units,
+                          uint64_t medium_limit, uint32_t load_pct, MergeUnit *small_units, MergeUnit *wide_units,
                           MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
                           unsigned long long *counters, unsigned *status, cudaStream_t s) {
     classify_units_kernel<<<(n_buckets + 3) / 4, 128, 0, s>>>(
-        bin_off, bin_kmers, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, small_units,
+        bin_off, bin_kmers, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, load_pct, small_units,
         wide_units, medium_units, large_units, max_units, pool_slots, counters, status);
     return 1;
 }

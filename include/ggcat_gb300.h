@@ -52,6 +52,12 @@ typedef struct {
     int32_t unit_target;      /* target k-mer instances per merge unit (0 = auto; -1 = auto without the
                                  shared-memory attempt for sub-buckets above the S-unit size) */
     int32_t keep_kmers;       /* 1 = also output the surviving k-mers and multiplicities */
+    /* tuning knobs (0 = default; ggcat_gpu_autotune chooses them), results are identical for any value */
+    int32_t subbin_bytes;     /* text bytes per sub-bin: sets the sub-bin digit width of the bucket store
+                                 partition (default 1024) */
+    int32_t table_load_pct;   /* largest load of a global-memory merge table, percent (default 80) */
+    int32_t small_limit;      /* largest sub-bin, in k-mer instances, merged in a shared-memory S unit
+                                 (default and maximum 3200, 1600 for k > 32) */
 } ggcat_gpu_params;
 
 /* One superkmer in the semantic form of PushSequenceInfo
@@ -120,6 +126,17 @@ int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer *h_out, ui
  * unitigs (with open-end link flags) for the link stage.  Runs on the bucket store of
  * the last ggcat_gpu_bucketize. */
 int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, void *stream);
+
+/* Chooses the tuning knobs of p (subbin_bytes, unit_target, small_limit, table_load_pct) by
+ * measurement: bucketize + merge of the first sample_bytes of d_text (all of it when 0) for
+ * each candidate, coordinate descent on the device time.  *best receives p with the chosen
+ * knobs, *default_ms / *best_ms the device times of p as given and of *best.  Stands where
+ * the reference sizes its buckets by heuristics (compute_stats_from_input_blocks,
+ * crates/io/src/lib.rs:67-140; second-level bucket count, crates/assembler/src/lib.rs:155).
+ * Leaves the bucket store of its last trial; outputs do not depend on the knobs. */
+int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len, const ggcat_gpu_params *p,
+                       uint64_t sample_bytes, void *stream, ggcat_gpu_params *best, double *default_ms,
+                       double *best_ms);
 
 /* Partial unitigs of the last merge: concatenated ASCII bases, and per unitig
  * (offset, length, flags) with flags bit0 = backward link, bit1 = forward link,

@@ -220,6 +220,45 @@ def test_merge_phase_replays_as_cuda_graph():
         c.close()
 
 
+@pytest.mark.parametrize("knobs", [dict(subbin_bytes=256), dict(subbin_bytes=4096), dict(table_load_pct=50),
+                                   dict(table_load_pct=90), dict(small_limit=800),
+                                   dict(unit_target=-1, small_limit=1600, table_load_pct=65)])
+def test_tuning_knobs_change_nothing(ctx, knobs):
+    """Sub-bin digit width, S-unit size limit, packing target and global-table load change
+    only the speed: k-mers and unitigs stay equal to the oracle's."""
+    text, off, ln, _ = _workload("reads", 13)
+    p = make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=2, keep_kmers=True, **knobs)
+    ctx.build_text(text, p)
+    keys, mult = ctx.kmers()
+    r = oracle.build_graph(text, off, ln, _oracle_params(p))
+    lo, hi, emult = r.kmers()
+    assert _kmer_dict(keys, mult) == dict(zip(lo.tolist(), emult.tolist()))
+    ctx.link(31)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
+
+
+def test_autotune_params_build_the_same_graph(ctx):
+    """The autotuner measures candidates on the device and returns knobs from its candidate
+    sets, never slower than the defaults it started from; a build with them equals the oracle."""
+    torch = pytest.importorskip("torch")
+    text, off, ln, _ = _workload("reads", 17)
+    p = make_params(k=31, m=10, bucket_bits=8, second_bits=2, min_multiplicity=2)
+    d = torch.from_numpy(text).cuda()
+    best, default_ms, best_ms = ctx.autotune(d.data_ptr(), d.numel(), p)
+    assert 0 < best_ms <= default_ms
+    assert best.subbin_bytes in (0, 256, 512, 1024, 2048, 4096)
+    assert best.unit_target in (0, -1, 1024, 3200)
+    assert best.small_limit in (0, 2400, 1600)
+    assert best.table_load_pct in (0, 50, 65, 90)
+    assert (best.k, best.m, best.min_multiplicity) == (p.k, p.m, p.min_multiplicity)
+    ctx.build_text(text, best)
+    ctx.link(31)
+    bases, uo, ul, uf = ctx.unitigs()
+    r = oracle.build_graph(text, off, ln, _oracle_params(p))
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
+
+
 def test_device_pointer_bucketize(ctx):
     """bucketize on a caller-owned device buffer and stream (torch only as plumbing)."""
     torch = pytest.importorskip("torch")
