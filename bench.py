@@ -31,9 +31,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "build Gbases/s bit-exact (batched vs per-bucket launch)"
 
-# DRAM bytes (read + write) of the merge-phase kernels per k-mer instance, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) on the 200 Mbp case; None until measured.
-MERGE_DRAM_BYTES_PER_INSTANCE = None
+# DRAM bytes (read + write) of the merge-phase kernels per k-mer instance: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum of the S, W and M merge_unit_kernel launches on
+# the 80 Mbp case of this workload (156.0 MB over 69.47 M instances); scaled by instances.
+MERGE_DRAM_BYTES_PER_INSTANCE = 2.25
 
 
 def _args():
@@ -491,10 +492,10 @@ def run_gpu(args):
     merge_bytes = (I + S * (w.k - 1)) / 4 + S * 8.375 + 16 * I + 12 * D
     merge_ms = phases["ms_merge"]
     achieved = merge_bytes / (merge_ms * 1e-3) / 1e9 if merge_ms > 0 else 0.0
-    # DRAM bytes of the merge kernels per k-mer instance, from one ncu capture of the 10 Mbp-genome
-    # (200 Mbp of reads) case of this workload, scaled by the instances of this step
+    # DRAM bytes of the merge kernels per k-mer instance, from one ncu capture of the 4 Mbp-genome
+    # (80 Mbp of reads) case of this workload, scaled by the instances of this step
     traffic = round(MERGE_DRAM_BYTES_PER_INSTANCE * I) if MERGE_DRAM_BYTES_PER_INSTANCE else None
-    roofline = {"bound": "hbm", "kernel": "merge_unit_kernel (S + M tiers) + large_* (merge phase)",
+    roofline = {"bound": "hbm", "kernel": "merge phase: merge_unit_kernel S/W/M tiers + large_* (one CUDA graph)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_step": int(merge_bytes), "phase_ms": round(merge_ms, 3)}
