@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libggcat_gb300.so")
-SOURCES = ["bucketing.cu", "merge.cu", "query.cu", "colors.cu", "hashes.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["bucketing.cu", "merge.cu", "link.cu", "query.cu", "colors.cu", "hashes.cu", "capi.cu", "noalloc.cu"]
 HEADERS = ["common.cuh", "kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

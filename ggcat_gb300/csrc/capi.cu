@@ -76,6 +76,18 @@ struct MergeGraphKey {
     uint64_t val[24];
 };
 
+// device buffers of the link stage
+struct LinkBufs {
+    DevBuf<uint64_t> keys;  // endpoint table keys (u64, or u128 as word pairs)
+    DevBuf<uint32_t> min12, eslot, succ, jump, jump2, list, cj, cm, cj2, cm2;
+    DevBuf<uint8_t> state;
+    DevBuf<unsigned long long> pr, pr2, chain_off, counters;
+    DevBuf<uint8_t> out_bases;
+    DevBuf<uint64_t> out_off;
+    DevBuf<uint32_t> out_len;
+    DevBuf<uint8_t> out_flags;
+};
+
 struct ggcat_gpu_ctx {
     int device = 0;
     int sms = 1;
@@ -119,6 +131,8 @@ struct ggcat_gpu_ctx {
     DevBuf<uint8_t> tvis;
     DevBuf<uint32_t> tlist;  // created-entry lists of the M units
     DevBuf<uint8_t> ext_scratch;  // per-CTA extension scratch of units with many survivors
+    LinkBufs lk;
+    uint64_t n_final = 0, n_final_bases = 0;
     // the batched merge phase as a CUDA graph, captured once per buffer/parameter layout
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t merge_exec = nullptr;
@@ -746,114 +760,120 @@ extern "C" int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint6
 }
 
 // ---------------------------------------------------------------------------
-// host link stage
+// link stage (device): the kernels of link.cu driven round by round
 // ---------------------------------------------------------------------------
-static inline uint8_t code_of(uint8_t a) { return (a >> 1) & 3; }
-
-// canonical packed k-mer of k ASCII bases (KT = uint64_t for k <= 32, unsigned __int128 for k <= 64)
-template <typename KT>
-static KT canon_ascii(const uint8_t *s, int k) {
-    KT fw = 0, rc = 0;
-    for (int i = 0; i < k; i++) {
-        fw |= (KT)code_of(s[i]) << (2 * i);
-        rc |= (KT)(code_of(s[k - 1 - i]) ^ 2) << (2 * i);
-    }
-    return fw < rc ? fw : rc;
-}
-
-struct KeyHash {
-    size_t operator()(uint64_t x) const { return (size_t)(x * 0x9E3779B97F4A7C15ull >> 17) ^ (size_t)x; }
-    size_t operator()(unsigned __int128 x) const {
-        return operator()((uint64_t)((uint64_t)x ^ ((uint64_t)(x >> 64) * 0xC2B2AE3D27D4EB4Full)));
-    }
-};
-
-static void rc_append(std::vector<uint8_t> &dst, const uint8_t *s, size_t n, size_t skip) {
-    // append reverse complement of s[0..n), skipping its first `skip` bases
-    for (size_t i = skip; i < n; i++) {
-        uint8_t c = s[n - 1 - i];
-        dst.push_back(c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A');
-    }
-}
-
-template <typename KT>
-static int link_impl(ggcat_gpu_ctx *ctx, int k) {
+static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
     auto t0 = std::chrono::steady_clock::now();
-    const HostUnitigs &P = ctx->partial;
     HostUnitigs &F = ctx->final_u;
     F.clear();
-    const size_t n = P.off.size();
-    // endpoints: 2i = left end (backward link), 2i+1 = right end (forward link)
-    std::vector<int64_t> partner(2 * n, -1);
-    std::unordered_map<KT, int64_t, KeyHash> first_end;
-    first_end.reserve(n);
-    for (size_t i = 0; i < n; i++) {
-        for (int side = 0; side < 2; side++) {
-            if (!(P.flags[i] & (side ? 2 : 1))) continue;
-            const uint8_t *s = P.bases.data() + P.off[i] + (side ? P.len[i] - k : 0);
-            const KT key = canon_ascii<KT>(s, k);
-            auto it = first_end.find(key);
-            int64_t ep = (int64_t)(2 * i + side);
-            if (it == first_end.end()) {
-                first_end.emplace(key, ep);
-            } else if (it->second >= 0) {
-                partner[it->second] = ep;
-                partner[ep] = it->second;
-                it->second = -1;
-            }
-        }
-    }
-    std::vector<uint8_t> done(n, 0);
-    auto emit_chain = [&](size_t i, int enter_side) {
-        size_t start_len = F.bases.size();
-        size_t cur = i;
-        int enter = enter_side;
-        bool circ = false;
-        bool first = true;
-        for (;;) {
-            done[cur] = 1;
-            const uint8_t *s = P.bases.data() + P.off[cur];
-            size_t L = P.len[cur];
-            size_t skip = first ? 0 : (size_t)k;
-            if (enter == 0)
-                F.bases.insert(F.bases.end(), s + skip, s + L);
-            else
-                rc_append(F.bases, s, L, skip);
-            first = false;
-            int64_t exit_ep = (int64_t)(2 * cur + (enter == 0 ? 1 : 0));
-            int64_t nxt = partner[exit_ep];
-            if (nxt < 0) break;
-            size_t nu = (size_t)nxt / 2;
-            if (done[nu]) {
-                circ = (nu == i);
-                break;
-            }
-            cur = nu;
-            enter = (int)(nxt % 2);
-        }
-        if (circ) F.bases.resize(F.bases.size() - 1);  // the string ended with its first k-mer
-        F.off.push_back(start_len);
-        F.len.push_back((uint32_t)(F.bases.size() - start_len));
-        F.flags.push_back(circ ? 4 : 0);
+    const uint64_t n = ctx->n_partial, nn = 2 * n;
+    if (nn >= 0xffffffffull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage: too many partial unitigs");
+    const int wide = k > 32;
+    uint64_t cap = 1024;
+    while (cap < 2 * nn) cap <<= 1;
+    LinkBufs &L = ctx->lk;
+    CK(L.keys.ensure(cap * (wide ? 2 : 1)));
+    CK(L.min12.ensure(2 * cap));
+    CK(L.eslot.ensure(nn + 1));
+    CK(L.succ.ensure(nn + 1));
+    CK(L.jump.ensure(nn + 1));
+    CK(L.jump2.ensure(nn + 1));
+    CK(L.list.ensure(nn + 1));
+    CK(L.cj.ensure(nn + 1));
+    CK(L.cm.ensure(nn + 1));
+    CK(L.cj2.ensure(nn + 1));
+    CK(L.cm2.ensure(nn + 1));
+    CK(L.state.ensure(nn + 1));
+    CK(L.pr.ensure(nn + 1));
+    CK(L.pr2.ensure(nn + 1));
+    CK(L.chain_off.ensure(nn + 1));
+    CK(L.counters.ensure(8));
+    CK(L.out_bases.ensure(ctx->n_partial_bases + 1));
+    CK(L.out_off.ensure(n + 1));
+    CK(L.out_len.ensure(n + 1));
+    CK(L.out_flags.ensure(n + 1));
+    CK(cudaMemsetAsync(L.keys.p, 0xff, cap * (wide ? 2 : 1) * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(L.min12.p, 0xff, 2 * cap * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(L.state.p, 0, nn + 1, s));
+    CK(cudaMemsetAsync(L.chain_off.p, 0xff, (nn + 1) * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(L.counters.p, 0, 8 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+    const int sms = ctx->sms;
+    uint32_t *min1 = L.min12.p, *min2 = L.min12.p + cap;
+    // pairing and successors (pj / pr start as "no predecessor")
+    ctx->launches += launch_link_endpoints(ctx->out_bases.p, ctx->out_off.p, ctx->out_len.p, ctx->out_flags.p, n, k,
+                                           L.keys.p, min1, cap - 1, L.eslot.p, ctx->status.p + 1, sms, s);
+    ctx->launches += launch_link_succ(L.eslot.p, min1, min2, nn, L.succ.p, L.jump.p, sms, s);
+    auto read_counter = [&](int i, unsigned long long &v) -> int {
+        CK(cudaMemcpyAsync(&v, L.counters.p + i, sizeof v, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        return GGCAT_GPU_OK;
     };
-    for (size_t i = 0; i < n; i++) {
-        if (done[i]) continue;
-        if (!(P.flags[i] & 3)) {
-            done[i] = 1;
-            size_t st = F.bases.size();
-            F.bases.insert(F.bases.end(), P.bases.begin() + P.off[i], P.bases.begin() + P.off[i] + P.len[i]);
-            F.off.push_back(st);
-            F.len.push_back(P.len[i]);
-            F.flags.push_back(P.flags[i] & 4);
-            continue;
-        }
-        if (partner[2 * i] < 0)
-            emit_chain(i, 0);
-        else if (partner[2 * i + 1] < 0)
-            emit_chain(i, 1);
+    // forward jumping until the unresolved count stops falling: the rest lie on cycles
+    uint32_t *jc = L.jump.p, *jn = L.jump2.p;
+    unsigned long long prev = ~0ull, cnt = 0;
+    int rc = GGCAT_GPU_OK;
+    for (int round = 0; round < 64 && nn; round++) {
+        CK(cudaMemsetAsync(L.counters.p + 2, 0, sizeof(unsigned long long), s));
+        ctx->launches += launch_link_jump(L.succ.p, jc, jn, nn, L.counters.p + 2, sms, s);
+        std::swap(jc, jn);
+        if ((rc = read_counter(2, cnt))) return rc;
+        if (cnt == 0 || cnt == prev) break;
+        prev = cnt;
     }
-    for (size_t i = 0; i < n; i++)
-        if (!done[i]) emit_chain(i, 0);
+    unsigned long long nc = 0;
+    if (cnt) {
+        CK(cudaMemsetAsync(L.counters.p + 3, 0, sizeof(unsigned long long), s));
+        ctx->launches +=
+            launch_link_cycle_list(L.succ.p, jc, nn, L.list.p, L.counters.p + 3, L.cj.p, L.cm.p, sms, s);
+        if ((rc = read_counter(3, nc))) return rc;
+        uint32_t *a_j = L.cj.p, *a_m = L.cm.p, *b_j = L.cj2.p, *b_m = L.cm2.p;
+        for (unsigned long long span = 1; span < 2 * nc; span <<= 1) {
+            ctx->launches += launch_link_cycle_min(L.list.p, nc, a_j, a_m, b_j, b_m, sms, s);
+            std::swap(a_j, b_j);
+            std::swap(a_m, b_m);
+        }
+        ctx->launches += launch_link_cycle_cut(L.list.p, nc, a_m, L.succ.p, L.state.p, sms, s);
+    }
+    // predecessor jumping: chain start and base offset of every node
+    ctx->launches += launch_link_pred_init(L.succ.p, L.state.p, ctx->out_len.p, nn, k, L.jump.p, L.pr.p, sms, s);
+    uint32_t *pc = L.jump.p, *pn = L.jump2.p;
+    unsigned long long *rcur = L.pr.p, *rnext = L.pr2.p;
+    for (int round = 0; round < 64 && nn; round++) {
+        CK(cudaMemsetAsync(L.counters.p + 4, 0, sizeof(unsigned long long), s));
+        ctx->launches += launch_link_pred_jump(pc, rcur, pn, rnext, nn, L.counters.p + 4, sms, s);
+        std::swap(pc, pn);
+        std::swap(rcur, rnext);
+        unsigned long long changed = 0;
+        if ((rc = read_counter(4, changed))) return rc;
+        if (changed == 0) break;
+    }
+    ctx->launches += launch_link_reserve(L.succ.p, L.state.p, pc, rcur, ctx->out_len.p, ctx->out_flags.p, nn,
+                                         L.chain_off.p, L.out_off.p, L.out_len.p, L.out_flags.p, L.counters.p,
+                                         ctx->n_partial_bases + 1, n + 1, ctx->status.p + 1, sms, s);
+    ctx->launches += launch_link_write(ctx->out_bases.p, ctx->out_off.p, ctx->out_len.p, L.state.p, pc, rcur,
+                                       L.chain_off.p, nn, k, L.out_bases.p, sms, s);
+    CK(cudaGetLastError());
+    unsigned long long tot[2] = {0, 0};
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(tot, L.counters.p, sizeof tot, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st & (kStatusOutOverflow | kStatusTableFull))
+        return fail(ctx, GGCAT_GPU_EDEVICE, "link stage: internal overflow (status %u)", st);
+    // the unitigs are packed in reservation order; bytes between them are never read
+    F.bases.resize(tot[0]);
+    F.off.resize(tot[1]);
+    F.len.resize(tot[1]);
+    F.flags.resize(tot[1]);
+    if (tot[0]) CK(cudaMemcpy(F.bases.data(), L.out_bases.p, tot[0], cudaMemcpyDeviceToHost));
+    if (tot[1]) {
+        CK(cudaMemcpy(F.off.data(), L.out_off.p, tot[1] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(F.len.data(), L.out_len.p, tot[1] * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(F.flags.data(), L.out_flags.p, tot[1], cudaMemcpyDeviceToHost));
+    }
+    ctx->n_final = tot[1];
+    ctx->n_final_bases = tot[0];
     auto t1 = std::chrono::steady_clock::now();
     ctx->stats.ms_link = std::chrono::duration<double, std::milli>(t1 - t0).count();
     ctx->stats.final_unitigs = F.off.size();
@@ -864,9 +884,10 @@ extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
     if (k < 3 || k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 64");
-    int rc = fetch_partial(ctx);
-    if (rc) return rc;
-    return k > 32 ? link_impl<unsigned __int128>(ctx, k) : link_impl<uint64_t>(ctx, k);
+    if (k != ctx->last_params.k) return fail(ctx, GGCAT_GPU_EINVAL, "link k=%d differs from the build k=%d", k,
+                                             ctx->last_params.k);
+    CK(cudaSetDevice(ctx->device));
+    return link_device(ctx, k, ctx->cap_stream);
 }
 
 extern "C" int ggcat_gpu_unitigs_copy(ggcat_gpu_ctx *ctx, uint8_t *h_bases, uint64_t bases_cap, uint64_t *h_off,

@@ -140,6 +140,33 @@ int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const 
                        uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
                        unsigned long long *queue, int sms, cudaStream_t s);
 
+// link.cu — cross-bucket link stage (each launcher returns the kernels it launched)
+int launch_link_endpoints(const uint8_t *bases, const uint64_t *off, const uint32_t *len, const uint8_t *flags,
+                          uint64_t n, int k, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
+                          unsigned *status, int sms, cudaStream_t s);
+int launch_link_succ(const uint32_t *eslot, const uint32_t *min1, const uint32_t *min2, uint64_t nn,
+                     uint32_t *succ, uint32_t *jump, int sms, cudaStream_t s);
+int launch_link_jump(const uint32_t *succ, const uint32_t *jump, uint32_t *jump_n, uint64_t nn,
+                     unsigned long long *unresolved, int sms, cudaStream_t s);
+int launch_link_cycle_list(const uint32_t *succ, const uint32_t *jump, uint64_t nn, uint32_t *list,
+                           unsigned long long *count, uint32_t *cyc_jump, uint32_t *cyc_min, int sms, cudaStream_t s);
+int launch_link_cycle_min(const uint32_t *list, uint64_t nc, const uint32_t *cj, const uint32_t *cm, uint32_t *cj_n,
+                          uint32_t *cm_n, int sms, cudaStream_t s);
+int launch_link_cycle_cut(const uint32_t *list, uint64_t nc, const uint32_t *cm, uint32_t *succ, uint8_t *node_state,
+                          int sms, cudaStream_t s);
+int launch_link_pred_init(const uint32_t *succ, const uint8_t *node_state, const uint32_t *len, uint64_t nn, int k,
+                          uint32_t *pjump, unsigned long long *prank, int sms, cudaStream_t s);
+int launch_link_pred_jump(const uint32_t *pj, const unsigned long long *pr, uint32_t *pj_n, unsigned long long *pr_n,
+                          uint64_t nn, unsigned long long *changed, int sms, cudaStream_t s);
+int launch_link_reserve(const uint32_t *succ, const uint8_t *node_state, const uint32_t *pj,
+                        const unsigned long long *pr, const uint32_t *len, const uint8_t *pflags, uint64_t nn,
+                        unsigned long long *chain_off, uint64_t *u_off, uint32_t *u_len, uint8_t *u_flags,
+                        unsigned long long *counters, unsigned long long bases_cap, unsigned long long u_cap,
+                        unsigned *status, int sms, cudaStream_t s);
+int launch_link_write(const uint8_t *bases, const uint64_t *off, const uint32_t *len, const uint8_t *node_state,
+                      const uint32_t *pj, const unsigned long long *pr, const unsigned long long *chain_off,
+                      uint64_t nn, int k, uint8_t *out, int sms, cudaStream_t s);
+
 // hashes.cu
 int launch_kmer_hash(const uint8_t *text, uint64_t n, int k, int kind, uint64_t *out, cudaStream_t s);
 

@@ -259,6 +259,27 @@ def test_autotune_params_build_the_same_graph(ctx):
     assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
 
 
+@pytest.mark.parametrize("k,m,n,extra", [(31, 10, 20_000, False), (31, 10, 3_000, True), (63, 12, 12_000, False)])
+def test_link_joins_cycles_across_buckets(ctx, k, m, n, extra):
+    """A circular genome (its first k-1 bases appended) makes one k-mer cycle that crosses
+    many buckets: the device link stage cuts it once, drops its mirror copy and emits one
+    circular unitig; with a second, linear genome the chains and the cycle coexist."""
+    rng = np.random.default_rng(n + k)
+    g = synth.random_genome(n, rng)
+    seqs = [np.concatenate([g, g[:k - 1]])]
+    if extra:
+        seqs.append(synth.random_genome(5_000, rng))
+    text, off, ln, _ = synth.pack_sequences(seqs)
+    p = make_params(k=k, m=m, bucket_bits=4, second_bits=1, min_multiplicity=1)
+    ctx.build_text(text, p)
+    ctx.link(k)
+    bases, uo, ul, uf = ctx.unitigs()
+    got = oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k)
+    op = oracle.params(k=k, m=m, bucket_bits=4, second_bits=1, min_multiplicity=1, threads=8)
+    assert got == oracle.build_graph(text, off, ln, op).unitigs()
+    assert int(((uf >> 2) & 1).sum()) >= 1
+
+
 def test_device_pointer_bucketize(ctx):
     """bucketize on a caller-owned device buffer and stream (torch only as plumbing)."""
     torch = pytest.importorskip("torch")
