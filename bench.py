@@ -252,6 +252,15 @@ def colored_bench(args, ctx, torch, dev):
     n1 = min(len(qo), 2000)
     r1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, one_per_launch=True, colored=True)
     same = bool((rb.matched[:n1] == r1.matched).all() and (rb.color_totals[:n1] == r1.color_totals).all())
+    # arrival-rate sweep (the knee): the same queries with the Poisson gaps scaled; "inf" = all
+    # queries waiting at t = 0
+    sweep = []
+    for rate in (80_000.0, 320_000.0, float("inf")):
+        a2 = np.zeros_like(arr) if rate == float("inf") else arr * (args.query_rate / rate)
+        r2 = serve.serve(ctx, 31, qt, qo, ql, a2, slots=4, max_batch_kmers=budget, colored=True)
+        sweep.append({"arrival_rate_per_s": rate if rate != float("inf") else "all at t=0",
+                      "kmers_per_s": round(r2.kmers_per_s, 1), "p50_ms": round(r2.pct_ms(50), 3),
+                      "p99_ms": round(r2.pct_ms(99), 3), "batches": r2.batches})
     return {
         "workload": w.name, "bases": int(w.bases), "colors": args.colors,
         "build": {**res, "device_gbases_per_s": round(w.bases / ((res["ms_bucketize"] + res["ms_merge"]) * 1e-3) / 1e9, 3),
@@ -263,7 +272,7 @@ def colored_bench(args, ctx, torch, dev):
                   "color_hits_total": int(rb.color_totals.sum()),
                   "one_per_launch": {"queries": int(n1), "kmers_per_s": round(r1.kmers_per_s, 1),
                                      "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3)},
-                  "results_identical_alone_vs_batched": same},
+                  "results_identical_alone_vs_batched": same, "rate_sweep": sweep},
     }
 
 

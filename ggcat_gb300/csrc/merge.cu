@@ -92,6 +92,11 @@ __device__ __forceinline__ uint64_t lds_u64(uint32_t a) {
     asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
     return v;
 }
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
 __device__ __forceinline__ uint64_t cas_shared_u64(uint32_t a, uint64_t cmp, uint64_t val) {
     uint64_t o;
     asm volatile("atom.shared.cas.b64 %0, [%1], %2, %3;" : "=l"(o) : "r"(a), "l"(cmp), "l"(val) : "memory");
@@ -491,7 +496,7 @@ struct TierCfg<uint64_t, kTierW> {
 };
 template <>
 struct TierCfg<u128, kTierW> {
-    static constexpr int NT = 512, kSlots = kSmallSlots, kSurv = 2048, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 2 * kSmallSlots, kSurv = 2048, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<uint64_t, kTierM> {
@@ -549,7 +554,6 @@ struct UnitSmem<KT, kTier, true> : UnitSmemCommon<KT, TierCfg<KT, kTier>::kSurv,
         SmemTableView<KT, C::kSlots> t;
         RankView<C::kSurv> r;
     } u;
-    uint8_t vis[C::kSlots];
 };
 template <typename KT, int kTier>
 struct UnitSmem<KT, kTier, false> : UnitSmemCommon<KT, TierCfg<KT, kTier>::kSurv, TierCfg<KT, kTier>::NT> {
@@ -615,6 +619,56 @@ __device__ __forceinline__ int alive_succ(const Table<KT> &t, KT v, KT rv, int k
     return d;
 }
 
+// alive_succ on a shared-memory table of u64 keys: the four first probes (key and value words)
+// are issued together; a collision continues probing
+__device__ __forceinline__ int alive_succ_shared(const Table<uint64_t> &t, uint64_t v, uint64_t rv, int k,
+                                                 uint32_t &v_only, bool &fw_only) {
+    const uint64_t bse = v >> 2;
+    const uint64_t rbase = (rv << 2) & kmer_mask(k);
+    const uint32_t kb = smem_addr(t.keys), vb = smem_addr(t.vals);
+    uint64_t key[4], got[4];
+    uint32_t slot[4], val[4];
+    bool isfw[4];
+#pragma unroll
+    for (uint32_t b = 0; b < 4; b++) {
+        const uint64_t w = bse | ((uint64_t)b << (2 * (k - 1)));
+        const uint64_t rw = rbase | (uint64_t)(b ^ 2u);
+        isfw[b] = w < rw;
+        key[b] = isfw[b] ? w : rw;
+        slot[b] = slot_of(key[b], t.cap);
+    }
+#pragma unroll
+    for (uint32_t b = 0; b < 4; b++) {
+        got[b] = lds_u64(kb + 8u * slot[b]);
+        val[b] = lds_u32(vb + 4u * slot[b]);
+    }
+    int d = 0;
+#pragma unroll
+    for (uint32_t b = 0; b < 4; b++) {
+        bool hit = got[b] == key[b];
+        uint32_t vw = val[b];
+        if (!hit && got[b] != ~0ull) {
+            uint32_t s = slot[b];
+            for (uint32_t probe = 1; probe < t.cap; probe++) {
+                s = (s + 1) & (t.cap - 1);
+                const uint64_t kk = lds_u64(kb + 8u * s);
+                if (kk == key[b]) {
+                    hit = true;
+                    vw = lds_u32(vb + 4u * s);
+                    break;
+                }
+                if (kk == ~0ull) break;
+            }
+        }
+        if (hit && val_alive(vw)) {
+            d++;
+            v_only = vw;
+            fw_only = isfw[b];
+        }
+    }
+    return d;
+}
+
 template <typename KT>
 __device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
     const KT x = sk[u >> 1];
@@ -668,7 +722,7 @@ __device__ __forceinline__ ExtArrays<KT, uint32_t> ext_global_arrays(uint8_t *ba
 //   list_scan: the survivor scan visits t_list[seg] (created-entry list) instead of slots
 //   warp_base: this warp's first dense index (lane 0 of the block scan of survivor counts)
 //   kRegJ:     per-thread register buffer of the shared-memory pointer jumping
-template <typename KT, typename IT, int NT, int kRegJ, bool kGlobalArr>
+template <typename KT, typename IT, int NT, int kRegJ, bool kGlobalArr, bool kSharedTable>
 __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *t_list, bool list_scan,
                                             uint32_t seg_lo, uint32_t seg_hi, uint32_t warp_base, uint32_t n_surv,
                                             const ExtArrays<KT, IT> &A, ExtShared &X, int k, uint32_t min_mult,
@@ -728,12 +782,19 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
     for (uint32_t u = threadIdx.x; u < nn; u += NT) {
         const KT x = A.sk[u >> 1];
         const KT rx = K::rc(x, k);
-        int64_t s_only = -1;
         bool fw_only = true;
         const bool odd = (u & 1) != 0;  // select the operands, not the call: lanes alternate parity
-        const int d = alive_succ(t, odd ? rx : x, odd ? x : rx, k, s_only, fw_only);
+        int d;
+        uint32_t v_only = 0;
+        if constexpr (kSharedTable && std::is_same<KT, uint64_t>::value) {
+            d = alive_succ_shared(t, odd ? rx : x, odd ? x : rx, k, v_only, fw_only);
+        } else {
+            int64_t s_only = -1;
+            d = alive_succ(t, odd ? rx : x, odd ? x : rx, k, s_only, fw_only);
+            if (d == 1) v_only = t.vals[s_only];
+        }
         IT code = d == 0 ? kNone : kMulti;
-        if (d == 1) code = (IT)(2u * (t.vals[s_only] & kIdxMask) + (fw_only ? 0u : 1u));
+        if (d == 1) code = (IT)(2u * (v_only & kIdxMask) + (fw_only ? 0u : 1u));
         A.succ[u] = code;
     }
     __syncthreads();  // the hash table is dead from here on
@@ -930,7 +991,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             cap = 64;
             while (cap < U.kmers + U.kmers / 4 + 8) cap <<= 1;
             if (cap > (uint32_t)Cfg::kSlots) cap = Cfg::kSlots;
-            t = Table<KT>{S.u.t.keys, S.u.t.vals, S.vis, cap};
+            t = Table<KT>{S.u.t.keys, S.u.t.vals, nullptr, cap};  // (visited marks: walk fallback only)
         }
         // optimistic unit (W tier, or a unit with a reserved global table): stop creating
         // entries at kOptLimit (<= 0.8 load with the at most NT - 1 creations in flight when
@@ -940,7 +1001,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         for (uint32_t i = threadIdx.x; i < cap; i += blockDim.x) {
             t.keys[i] = K::empty();
             t.vals[i] = 0;
-            t.vis[i] = 0;
+            if constexpr (kGlobalTable) t.vis[i] = 0;
         }
         if (threadIdx.x == 0) {
             S.x.n_surv = 0;
@@ -1110,7 +1171,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         if (n_surv <= (uint32_t)kMaxSurv) {
             ExtArrays<KT, uint16_t> A{S.sk,          S.succ,    S.bflag,      S.u.r.jump, S.u.r.rank,
                                       nullptr,       nullptr,   S.u.r.offs,   S.u.r.uidx, S.u.r.haspred};
-            extend_unit<KT, uint16_t, NT, (kMaxSurv * 2 + NT - 1) / NT, false>(
+            extend_unit<KT, uint16_t, NT, (kMaxSurv * 2 + NT - 1) / NT, false, !kGlobalTable>(
                 t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, o);
         } else if (a.ext_scratch != nullptr && n_surv <= a.ext_cap) {
             // more survivors than the shared-memory arrays hold: the same ranking on this
@@ -1118,15 +1179,21 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             if (threadIdx.x == 0) atomicAdd(&o.counters[kCntExtGlobal], 1ull);
             const ExtArrays<KT, uint32_t> A =
                 ext_global_arrays<KT>(a.ext_scratch + (size_t)blockIdx.x * a.ext_stride, a.ext_cap);
-            extend_unit<KT, uint32_t, NT, 1, true>(t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x,
+            extend_unit<KT, uint32_t, NT, 1, true, !kGlobalTable>(t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x,
                                                   k, min_mult, a.keep_kmers, o);
         } else {
-            // walk fallback (no scratch for this many survivors)
+            // walk fallback (no scratch for this many survivors; a shared-memory table never has
+            // more survivors than the scratch holds)
             if (threadIdx.x == 0) atomicAdd(&o.counters[kCntWalk], 1ull);
-            Graph<KT> g{t, k, min_mult};
-            for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) extend_slot(g, sl, o, a.keep_kmers, min_mult);
-            __syncthreads();
-            for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
+            if constexpr (kGlobalTable) {
+                Graph<KT> g{t, k, min_mult};
+                for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x)
+                    extend_slot(g, sl, o, a.keep_kmers, min_mult);
+                __syncthreads();
+                for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
+            } else {
+                if (threadIdx.x == 0) atomicOr(o.status, kStatusWalkLimit);
+            }
         }
     }
 }

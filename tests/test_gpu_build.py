@@ -42,7 +42,7 @@ def _workload(kind, seed):
         # ("planted31:2500:only" leaves out the second, random sequence)
         name, _, rest = kind.partition(":")
         ln_s, _, only = rest.partition(":")
-        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if name == "planted31" else (63, 12, b"CAGACTATCGCG", 5000)
+        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if name == "planted31" else (63, 12, b"CAGACTATCGCG", 8000)
         n = int(ln_s) if ln_s else n
         g = synth.random_genome(n, rng).copy()
         pat = np.frombuffer(mm, np.uint8)
