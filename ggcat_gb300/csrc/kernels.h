@@ -74,7 +74,7 @@ struct MergeArgs {
 // bytes of extension scratch per survivor (keys of key_bytes, 2 oriented nodes of 30 bytes)
 inline uint64_t merge_ext_bytes_per_survivor(int wide) { return (wide ? 16 : 8) + 60; }
 // survivors per CTA the extension scratch is sized for: S and W tiers / M tier
-constexpr uint32_t kExtCapShared = 8192;
+constexpr uint32_t kExtCapShared = 16384;
 constexpr uint32_t kExtCapMedium = 1u << 18;
 
 // merge counters (device array of 16 u64)

@@ -28,11 +28,15 @@ struct Table {
 
 constexpr uint32_t kCountMask = (1u << 30) - 1;
 
-// Fibonacci hashing: the top log2(cap) bits of the 32-bit multiplicative hash (cap >= 2)
+// Multiplicative range reduction of the 32-bit hash onto [0, cap): any capacity (the W tier's
+// shared table is not a power of two); for a power of two these are the top log2(cap) bits
 template <typename KT>
 __device__ __forceinline__ uint32_t slot_of(KT key, uint32_t cap) {
-    return KeyOps<KT>::hash(key) >> (__clz(cap) + 1);
+    return (uint32_t)(((uint64_t)KeyOps<KT>::hash(key) * cap) >> 32);
 }
+
+// next slot of a linear probe
+__device__ __forceinline__ uint32_t next_slot(uint32_t s, uint32_t cap) { return s + 1 == cap ? 0u : s + 1; }
 
 template <typename KT>
 __device__ __forceinline__ int64_t tfind(const Table<KT> &t, KT key) {
@@ -41,7 +45,7 @@ __device__ __forceinline__ int64_t tfind(const Table<KT> &t, KT key) {
         const KT kk = t.keys[s];
         if (kk == key) return s;
         if (kk == KeyOps<KT>::empty()) return -1;
-        s = (s + 1) & (t.cap - 1);
+        s = next_slot(s, t.cap);
     }
     return -1;
 }
@@ -56,7 +60,7 @@ __device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned 
             const KT old = KeyOps<KT>::cas(&t.keys[s], KeyOps<KT>::empty(), key);
             if (old == KeyOps<KT>::empty() || old == key) return s;
         }
-        s = (s + 1) & (t.cap - 1);
+        s = next_slot(s, t.cap);
     }
     atomicOr(status, kStatusTableFull);
     return -1;
@@ -78,7 +82,7 @@ __device__ __forceinline__ int64_t tinsert_created(const Table<KT> &t, KT key, u
             }
             if (old == key) return s;
         }
-        s = (s + 1) & (t.cap - 1);
+        s = next_slot(s, t.cap);
     }
     atomicOr(status, kStatusTableFull);
     return -1;
@@ -126,7 +130,7 @@ __device__ __forceinline__ int64_t tinsert_shared(const Table<uint64_t> &t, uint
             }
             if (old == key) return s;
         }
-        s = (s + 1) & (t.cap - 1);
+        s = next_slot(s, t.cap);
     }
     atomicOr(status, kStatusTableFull);
     return -1;
@@ -492,7 +496,7 @@ struct TierCfg<u128, kTierS> {
 };
 template <>
 struct TierCfg<uint64_t, kTierW> {
-    static constexpr int NT = 512, kSlots = 2 * kSmallSlots, kSurv = 4096, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 12288, kSurv = 4096, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<u128, kTierW> {
@@ -565,6 +569,10 @@ static_assert(sizeof(UnitSmem<uint64_t, kTierW>) <= 227 * 1024 && sizeof(UnitSme
                   sizeof(UnitSmem<uint64_t, kTierM>) <= 227 * 1024 && sizeof(UnitSmem<u128, kTierM>) <= 227 * 1024 &&
                   2 * sizeof(UnitSmem<uint64_t, kTierS>) <= 227 * 1024 && 2 * sizeof(UnitSmem<u128, kTierS>) <= 227 * 1024,
               "shared memory of a merge CTA");
+// a shared-memory table never holds more survivors than the extension scratch of its CTA
+static_assert(TierCfg<uint64_t, kTierS>::kSlots <= (int)kExtCapShared && TierCfg<uint64_t, kTierW>::kSlots <= (int)kExtCapShared &&
+                  TierCfg<u128, kTierS>::kSlots <= (int)kExtCapShared && TierCfg<u128, kTierW>::kSlots <= (int)kExtCapShared,
+              "extension scratch of the shared-memory tiers");
 
 // exclusive block scan of one u32 per thread (blockDim.x == NT); all threads call it
 template <int NT>
@@ -650,7 +658,7 @@ __device__ __forceinline__ int alive_succ_shared(const Table<uint64_t> &t, uint6
         if (!hit && got[b] != ~0ull) {
             uint32_t s = slot[b];
             for (uint32_t probe = 1; probe < t.cap; probe++) {
-                s = (s + 1) & (t.cap - 1);
+                s = next_slot(s, t.cap);
                 const uint64_t kk = lds_u64(kb + 8u * s);
                 if (kk == key[b]) {
                     hit = true;
@@ -1331,7 +1339,7 @@ int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned
     return 1;
 }
 
-uint64_t merge_wide_limit(int wide) { return wide ? 16384 : 32768; }
+uint64_t merge_wide_limit(int wide) { return wide ? 16384 : 65536; }
 
 uint64_t merge_small_limit(int wide) {
     // instances of an S unit, so that its table (Tier slots) stays at load <= 0.8

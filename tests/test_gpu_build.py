@@ -42,7 +42,7 @@ def _workload(kind, seed):
         # ("planted31:2500:only" leaves out the second, random sequence)
         name, _, rest = kind.partition(":")
         ln_s, _, only = rest.partition(":")
-        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 8000) if name == "planted31" else (63, 12, b"CAGACTATCGCG", 8000)
+        k, m, mm, n = (31, 10, b"CAGAGCTTGC", 12000) if name == "planted31" else (63, 12, b"CAGACTATCGCG", 8000)
         n = int(ln_s) if ln_s else n
         g = synth.random_genome(n, rng).copy()
         pat = np.frombuffer(mm, np.uint8)
@@ -148,7 +148,8 @@ def test_shared_memory_attempt_and_spill(ctx, kind, bbits, minm, k, m):
 
 
 @pytest.mark.parametrize("kind,k,m", [("planted31:2500:only", 31, 10), ("planted31:5000:only", 31, 10),
-                                      ("planted31:8000:only", 31, 10), ("planted63:1300:only", 63, 12),
+                                      ("planted31:8000:only", 31, 10), ("planted31:9000:only", 31, 10),
+                                      ("planted63:1300:only", 63, 12),
                                       ("planted63:2500:only", 63, 12), ("planted63:5000:only", 63, 12),
                                       ("planted31:8000", 31, 10), ("planted63:5000", 63, 12)])
 def test_many_survivors_rank_in_global_scratch(ctx, kind, k, m):
