@@ -106,9 +106,10 @@ constexpr uint64_t kInf = ~0ull;
 // column per thread) and are built, counted and stored together by the whole warp: a split
 // happens every ~(w+1)/2 positions per lane, so emitting at once would run the record code on
 // almost every step with one or two lanes active.  A lane gains at most one entry per step
-// and the warp drains as soon as a lane holds kEmitDrain, so kEmitQueue entries suffice.
-constexpr int kEmitQueue = 4;
-constexpr int kEmitDrain = 3;
+// and the warp drains as soon as a lane holds kEmitDrain, so kEmitQueue entries suffice; six
+// entries keep three 256-thread CTAs per SM (k - m = 21) and halve the drain rounds of four.
+constexpr int kEmitQueue = 6;
+constexpr int kEmitDrain = 5;
 
 // Single pass over the 2-bit text.  Thread t owns the window starts [t*chunk, (t+1)*chunk)
 // (chunk a multiple of 32) and walks the bases from lb (a multiple of 32) before its range,
