@@ -475,20 +475,24 @@ __global__ void __launch_bounds__(128) classify_units_kernel(
 // small units: persistent CTAs, shared-memory table, device work queue
 // ---------------------------------------------------------------------------
 // Tiers of merge_unit_kernel (one unit per CTA, persistent over a device work queue):
-//   S: many sub-bins packed per unit, hash table in shared memory, 256 threads, 2 CTAs/SM;
-//   W: one sub-bin of up to a few ten thousand instances, larger shared-memory table, 512
-//      threads, 1 CTA/SM; the table is sized for the distinct k-mers it can hold, so a unit
-//      whose distinct k-mers overflow it moves to the M queue (with a reserved global table);
+//   S: many sub-bins packed per unit, hash table in shared memory; u64 keys: 512 threads,
+//      2 CTAs/SM (u128: 256 threads, 2 CTAs/SM);
+//   W: one sub-bin of up to 65536 (u128: 16384) instances, the largest shared-memory table;
+//      u64 keys: 1024 threads and 11264 slots, u128: 512 threads and 8192 slots, 1 CTA/SM; a
+//      unit whose distinct k-mers overflow the table moves to the M queue (with a reserved
+//      global table);
 //   M: table in the global pool (L2-resident), 512 threads, the whole shared memory for the
 //      list-ranking arrays.
-// S and W reuse the table bytes for the list-ranking arrays once the successor phase is done
-// (union).  Units with more survivors than kSurv are extended by per-thread walks instead.
+// The phases of a unit are separated by block barriers and bound by shared-memory latency, so
+// the u64 tiers run 32 warps per SM (the kernel fits 64 registers per thread).  S and W reuse
+// the table bytes for the list-ranking arrays once the successor phase is done (union).  Units
+// with more survivors than kSurv rank in the CTA's global scratch (extend_unit).
 enum : int { kTierS = 0, kTierW = 1, kTierM = 2 };
 template <typename KT, int kTier>
 struct TierCfg;
 template <>
 struct TierCfg<uint64_t, kTierS> {
-    static constexpr int NT = 256, kSlots = kSmallSlots, kSurv = 2048, kMinBlocks = 2;
+    static constexpr int NT = 512, kSlots = kSmallSlots, kSurv = 2048, kMinBlocks = 2;
 };
 template <>
 struct TierCfg<u128, kTierS> {
@@ -496,7 +500,7 @@ struct TierCfg<u128, kTierS> {
 };
 template <>
 struct TierCfg<uint64_t, kTierW> {
-    static constexpr int NT = 512, kSlots = 12288, kSurv = 4096, kMinBlocks = 1;
+    static constexpr int NT = 1024, kSlots = 11264, kSurv = 4096, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<u128, kTierW> {
