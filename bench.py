@@ -33,8 +33,8 @@ METRIC = "build Gbases/s bit-exact (batched vs per-bucket launch)"
 
 # DRAM bytes (read + write) of the merge-phase kernels per k-mer instance: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum of the S, W and M merge_unit_kernel launches on
-# the 80 Mbp case of this workload (156.0 MB over 69.47 M instances); scaled by instances.
-MERGE_DRAM_BYTES_PER_INSTANCE = 2.25
+# the 80 Mbp case of this workload (154.8 MB over 69.47 M instances); scaled by instances.
+MERGE_DRAM_BYTES_PER_INSTANCE = 2.23
 
 
 def _args():
