@@ -418,12 +418,15 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
     CK(ctx->tlist.ensure(pool));
-    // extension scratch: S/W CTAs (2 per SM) up to kExtCapShared survivors each, M CTAs (1 per
-    // SM) up to kExtCapMedium (the instances of an M unit); the tiers run one after another
+    // extension scratch: one region per CTA of the tier running (the tiers run one after
+    // another): S/W CTAs up to kExtCapShared survivors each, M CTAs up to kExtCapMedium (the
+    // instances of an M unit)
     const uint64_t bps = merge_ext_bytes_per_survivor(wide);
     const uint64_t stride_sw = ((uint64_t)kExtCapShared * bps + 255) & ~255ull;
     const uint64_t stride_m = ((uint64_t)kExtCapMedium * bps + 255) & ~255ull;
-    CK(ctx->ext_scratch.ensure(std::max<uint64_t>(2ull * ctx->sms * stride_sw, (uint64_t)ctx->sms * stride_m)));
+    const uint64_t ctas_sw = (uint64_t)ctx->sms * std::max(merge_ctas_per_sm(0, wide), merge_ctas_per_sm(1, wide));
+    const uint64_t ctas_m = (uint64_t)ctx->sms * merge_ctas_per_sm(2, wide);
+    CK(ctx->ext_scratch.ensure(std::max<uint64_t>(ctas_sw * stride_sw, ctas_m * stride_m)));
     MergeArgs a{ctx->packed.p, ctx->recs.p, p->k,           p->min_multiplicity, p->keep_kmers, wide,
                 ctx->ext_scratch.p, stride_sw, kExtCapShared};
     MergeArgs am = a;

@@ -126,6 +126,8 @@ int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_
 // largest number of k-mer instances of an S unit / of an optimistic S unit
 uint64_t merge_small_limit(int wide);
 uint64_t merge_wide_limit(int wide);
+// CTAs per SM of a merge tier (0 = S, 1 = W, 2 = M): the persistent grids are SMs x this
+int merge_ctas_per_sm(int tier, int wide);
 
 // query.cu
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,

@@ -481,8 +481,8 @@ __global__ void __launch_bounds__(128) classify_units_kernel(
 //      u64 keys: 1024 threads and 11264 slots, u128: 512 threads and 8192 slots, 1 CTA/SM; a
 //      unit whose distinct k-mers overflow the table moves to the M queue (with a reserved
 //      global table);
-//   M: table in the global pool (L2-resident), 512 threads, the whole shared memory for the
-//      list-ranking arrays.
+//   M: table in the global pool (L2-resident), 512 threads, 2 CTAs/SM, shared memory for the
+//      list-ranking arrays of up to 2048 (u128: 1536) survivors.
 // The phases of a unit are separated by block barriers and bound by shared-memory latency, so
 // the u64 tiers run 32 warps per SM (the kernel fits 64 registers per thread).  S and W reuse
 // the table bytes for the list-ranking arrays once the successor phase is done (union).  Units
@@ -504,15 +504,15 @@ struct TierCfg<uint64_t, kTierW> {
 };
 template <>
 struct TierCfg<u128, kTierW> {
-    static constexpr int NT = 512, kSlots = 2 * kSmallSlots, kSurv = 2048, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 7936, kSurv = 2048, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<uint64_t, kTierM> {
-    static constexpr int NT = 512, kSlots = 0, kSurv = 5632, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 0, kSurv = 2048, kMinBlocks = 2;
 };
 template <>
 struct TierCfg<u128, kTierM> {
-    static constexpr int NT = 512, kSlots = 0, kSurv = 4096, kMinBlocks = 1;
+    static constexpr int NT = 512, kSlots = 0, kSurv = 1536, kMinBlocks = 2;
 };
 constexpr uint16_t kNone16 = 0xffff, kMulti16 = 0xfffe;
 
@@ -530,7 +530,10 @@ struct SmemTableView {
     uint32_t vals[kSlots];  // count|flags<<30, then alive<<31|flags<<28|dense index
 };
 
-constexpr int kStageWords = 4;  // packed words staged per record (records spanning more read global memory)
+// packed words staged per record in the insert phase (records spanning more read global
+// memory): k <= 32 superkmers are short; k > 32 superkmers of long reads often span 5-6 words
+template <typename KT>
+constexpr int stage_words() { return std::is_same<KT, uint64_t>::value ? 4 : 6; }
 constexpr int kRecBatch = 32;   // records per insert batch of a warp (<= 32)
 
 // block-shared scalars of the extension phase
@@ -541,7 +544,7 @@ struct ExtShared {
 
 template <typename KT, int N, int NT>
 struct UnitSmemCommon {
-    uint64_t stage[NT][kStageWords];  // per lane: the packed words of its record (insert phase)
+    uint64_t stage[NT][stage_words<KT>()];  // per lane: the packed words of its record (insert phase)
     KT sk[N];              // survivor canonical k-mers (dense order)
     uint16_t succ[2 * N];  // traversable successor of each oriented node
     uint8_t bflag[2 * N];  // bit0 left boundary, bit1 right boundary (oriented)
@@ -1054,9 +1057,9 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                     // loads per 32 records instead of one dependent load per k-mer window)
                     const uint64_t st = rec_start(rr);
                     const uint64_t wb = st >> 5, we = (st + rec_len(rr) - 1) >> 5;
-                    if (we - wb < (uint64_t)kStageWords) {
+                    if (we - wb < (uint64_t)stage_words<KT>()) {
 #pragma unroll
-                        for (int q = 0; q < kStageWords; q++)
+                        for (int q = 0; q < stage_words<KT>(); q++)
                             if (wb + q <= we) S.stage[threadIdx.x][q] = a.packed[wb + q];
                     } else {
                         fr |= 8u;  // long record: k-mers read from global memory
@@ -1341,6 +1344,14 @@ int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned
         merge_tier_t<uint64_t, kTierW>(a, units, counters, nullptr, nullptr, nullptr, nullptr, spill, max_units, o, sms,
                                        s);
     return 1;
+}
+
+int merge_ctas_per_sm(int tier, int wide) {
+    if (wide)
+        return tier == 0 ? TierCfg<u128, kTierS>::kMinBlocks
+                         : tier == 1 ? TierCfg<u128, kTierW>::kMinBlocks : TierCfg<u128, kTierM>::kMinBlocks;
+    return tier == 0 ? TierCfg<uint64_t, kTierS>::kMinBlocks
+                     : tier == 1 ? TierCfg<uint64_t, kTierW>::kMinBlocks : TierCfg<uint64_t, kTierM>::kMinBlocks;
 }
 
 uint64_t merge_wide_limit(int wide) { return wide ? 16384 : 65536; }
