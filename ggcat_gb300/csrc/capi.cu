@@ -585,6 +585,10 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     if (p->hash_kind != GGCAT_HASH_SEQHASH && p->hash_kind != GGCAT_HASH_RABIN_KARP128 && p->hash_kind != 0)
         return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "unknown merge hash kind %d", p->hash_kind);
     if (p->min_multiplicity < 1) return fail(ctx, GGCAT_GPU_EINVAL, "min_multiplicity must be >= 1");
+    // forward-only builds (fw seq-hash / Rabin-Karp, crates/hashes/src/fw_seqhash.rs) count and
+    // extend k-mers without canonicalisation; the device merge is canonical only
+    if (p->forward_only)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device merge builds canonical graphs only (forward_only=1)");
     if (ctx->n_kmers >= (1ull << 29) * 1024ull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "input too large");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));

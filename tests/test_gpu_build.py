@@ -281,6 +281,68 @@ def test_link_joins_cycles_across_buckets(ctx, k, m, n, extra):
     assert int(((uf >> 2) & 1).sum()) >= 1
 
 
+@pytest.mark.parametrize("case", ["empty", "short", "all_n", "one_kmer", "separators"])
+def test_edge_case_inputs_match_oracle(ctx, case):
+    """Inputs without k-mers or with a single one: empty text, sequences shorter than k, only
+    N, exactly k bases, and a text of separators with k-mers split by them."""
+    rng = np.random.default_rng(5)
+    g = synth.random_genome(31, rng)
+    seqs = {"empty": [],
+            "short": [synth.random_genome(int(n), rng) for n in (1, 5, 29, 30)],
+            "all_n": [np.frombuffer(b"N" * 200, np.uint8), np.frombuffer(b"n" * 40, np.uint8)],
+            "one_kmer": [g],
+            "separators": [synth.random_genome(35, rng), np.frombuffer(b"ACGT" * 20, np.uint8)]}[case]
+    text, off, ln, _ = synth.pack_sequences(seqs) if seqs else (np.zeros(0, np.uint8), np.zeros(0, np.uint64),
+                                                                 np.zeros(0, np.uint64), None)
+    p = make_params(k=31, m=10, bucket_bits=4, second_bits=1, min_multiplicity=1, keep_kmers=True)
+    ctx.build_text(text, p)
+    keys, mult = ctx.kmers()
+    r = oracle.build_graph(text, off, ln, _oracle_params(p))
+    lo, hi, emult = r.kmers()
+    assert _kmer_dict(keys, mult) == dict(zip(lo.tolist(), emult.tolist()))
+    ctx.link(31)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
+
+
+def test_forward_only_merge_is_rejected(ctx):
+    """Forward-only bucketing runs; the canonical device merge refuses forward-only builds
+    instead of returning canonical results."""
+    text, off, ln, _ = _workload("genomes", 3)
+    p = make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=1, forward_only=True)
+    with pytest.raises(_native.GgcatGpuError, match="EUNSUPPORTED"):
+        ctx.build_text(text, p)
+
+
+def test_build_graph_from_fasta_files_matches_oracle(tmp_path):
+    """GGCATInstance.build_graph on FASTA files (FASTA reader, device build, device link,
+    FASTA writer): the unitigs of the written file equal the oracle's for the same reads."""
+    import ggcat_gb300
+
+    rng = np.random.default_rng(9)
+    g = synth.random_genome(60_000, rng)
+    files = []
+    for i in range(2):
+        reads = synth.sample_reads(g, 3000, 150, 0.003, 0.0, rng)
+        path = tmp_path / f"r{i}.fa"
+        with open(path, "wb") as f:
+            for j, rd in enumerate(reads):
+                f.write(b">r%d_%d\n" % (i, j) + rd.tobytes() + b"\n")
+        files.append(str(path))
+    inst = ggcat_gb300.GGCATInstance.create(ggcat_gb300.GGCATConfig())
+    out = tmp_path / "out.fa"
+    assert inst.build_graph(files, str(out), kmer_length=31, minimizer_length=10, min_multiplicity=2) == str(out)
+    lines = open(out, "rb").read().split(b"\n")
+    assert all(h.startswith(b">") and b" LN:i:" in h for h in lines[0:-1:2])
+    seqs = [x for x in lines[1::2] if x]
+    got = oracle.canonicalize_unitigs(b"".join(x + b"\n" for x in seqs), np.zeros(len(seqs), np.uint8), 31)
+    # the unitig set does not depend on the bucket counts the file path picks
+    ftext, foff, fln = oracle.fasta_parse(b"".join(open(f, "rb").read() for f in files), 30)
+    r = oracle.build_graph(ftext, foff, fln, oracle.params(k=31, m=10, bucket_bits=10, second_bits=3,
+                                                          min_multiplicity=2, threads=8))
+    assert got == r.unitigs()
+
+
 def test_device_pointer_bucketize(ctx):
     """bucketize on a caller-owned device buffer and stream (torch only as plumbing)."""
     torch = pytest.importorskip("torch")
