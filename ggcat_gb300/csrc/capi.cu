@@ -427,7 +427,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     const uint64_t ctas_sw = (uint64_t)ctx->sms * std::max(merge_ctas_per_sm(0, wide), merge_ctas_per_sm(1, wide));
     const uint64_t ctas_m = (uint64_t)ctx->sms * merge_ctas_per_sm(2, wide);
     CK(ctx->ext_scratch.ensure(std::max<uint64_t>(ctas_sw * stride_sw, ctas_m * stride_m)));
-    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k,           p->min_multiplicity, p->keep_kmers, wide,
+    // forward-only builds (forward seq-hash / Rabin-Karp, crates/hashes/src/fw_seqhash.rs) count
+    // and extend k-mers as read, without canonicalisation
+    MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers, wide, p->forward_only ? 1 : 0,
                 ctx->ext_scratch.p, stride_sw, kExtCapShared};
     MergeArgs am = a;
     am.ext_stride = stride_m;
@@ -517,7 +519,8 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                  p->keep_kmers ? kmer_cap : 0, ctx->n_buckets,      (uint64_t)ctx->fine_bits,
                                  target,             wide_limit,                    max_units,
                                  pool,               stride_sw,                     stride_m,
-                                 (uint64_t)ctx->sms, small_limit,                   load_pct};
+                                 (uint64_t)ctx->sms, small_limit,                   load_pct,
+                                 (uint64_t)a.forward};
         static_assert(sizeof(vals) / sizeof(vals[0]) <= sizeof(key.val) / sizeof(key.val[0]), "graph key");
         memcpy(key.val, vals, sizeof vals);
         if (!ctx->merge_exec || memcmp(&key, &ctx->merge_key, sizeof key) != 0) {
@@ -585,10 +588,6 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     if (p->hash_kind != GGCAT_HASH_SEQHASH && p->hash_kind != GGCAT_HASH_RABIN_KARP128 && p->hash_kind != 0)
         return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "unknown merge hash kind %d", p->hash_kind);
     if (p->min_multiplicity < 1) return fail(ctx, GGCAT_GPU_EINVAL, "min_multiplicity must be >= 1");
-    // forward-only builds (fw seq-hash / Rabin-Karp, crates/hashes/src/fw_seqhash.rs) count and
-    // extend k-mers without canonicalisation; the device merge is canonical only
-    if (p->forward_only)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device merge builds canonical graphs only (forward_only=1)");
     if (ctx->n_kmers >= (1ull << 29) * 1024ull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "input too large");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
@@ -809,7 +808,8 @@ static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
     uint32_t *min1 = L.min12.p, *min2 = L.min12.p + cap;
     // pairing and successors (pj / pr start as "no predecessor")
     ctx->launches += launch_link_endpoints(ctx->out_bases.p, ctx->out_off.p, ctx->out_len.p, ctx->out_flags.p, n, k,
-                                           L.keys.p, min1, cap - 1, L.eslot.p, ctx->status.p + 1, sms, s);
+                                           ctx->last_params.forward_only ? 1 : 0, L.keys.p, min1, cap - 1, L.eslot.p,
+                                           ctx->status.p + 1, sms, s);
     ctx->launches += launch_link_succ(L.eslot.p, min1, min2, nn, L.succ.p, L.jump.p, sms, s);
     auto read_counter = [&](int i, unsigned long long &v) -> int {
         CK(cudaMemcpyAsync(&v, L.counters.p + i, sizeof v, cudaMemcpyDeviceToHost, s));

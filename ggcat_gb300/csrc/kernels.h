@@ -64,6 +64,7 @@ struct MergeArgs {
     int min_mult;
     int keep_kmers;
     int wide;  // 0: u64 keys (k <= 32); 1: u128 keys (k <= 64)
+    int forward;  // 1: forward-only build (k-mers keyed and extended as read, not canonicalised)
     // per-CTA global scratch of the extension phase for units with more survivors than the
     // shared-memory arrays hold (CTA i uses ext_scratch + i * ext_stride, up to ext_cap survivors)
     uint8_t *ext_scratch;
@@ -144,7 +145,7 @@ int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const 
 
 // link.cu — cross-bucket link stage (each launcher returns the kernels it launched)
 int launch_link_endpoints(const uint8_t *bases, const uint64_t *off, const uint32_t *len, const uint8_t *flags,
-                          uint64_t n, int k, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
+                          uint64_t n, int k, int fwd, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
                           unsigned *status, int sms, cudaStream_t s);
 int launch_link_succ(const uint32_t *eslot, const uint32_t *min1, const uint32_t *min2, uint64_t nn,
                      uint32_t *succ, uint32_t *jump, int sms, cudaStream_t s);

@@ -5,8 +5,10 @@
 // where a partial unitig end flagged as a sub-bucket boundary carries a "link" k-mer that is
 // also the end of exactly one other partial unitig.
 //
-//   1. endpoints: the canonical k-mer of every flagged end goes into a hash table; per key the
-//      two smallest endpoint ids (2*piece + side) are paired, the rest stay unpaired;
+//   1. endpoints: the k-mer of every flagged end goes into a hash table, keyed like the build's
+//      hash family (canonical, or as read for forward-only builds: the extremities are keyed
+//      by hash.to_unextendable(), extend_unitigs.rs:142-147); per key the two smallest endpoint
+//      ids (2*piece + side) are paired, the rest stay unpaired;
 //   2. oriented nodes v = 2*piece + d (d = 0: stored orientation, entered by its left end;
 //      d = 1: reverse complement): succ(v) = partner(v ^ 1), the endpoint entered next;
 //   3. forward pointer jumping separates chains (every jump reaches an end) from cycles; the
@@ -38,7 +40,7 @@ __global__ void __launch_bounds__(256) link_endpoints_kernel(const uint8_t *__re
                                                              const uint64_t *__restrict__ off,
                                                              const uint32_t *__restrict__ len,
                                                              const uint8_t *__restrict__ flags, uint64_t n, int k,
-                                                             KT *keys, uint32_t *min1, uint64_t mask,
+                                                             int fwd, KT *keys, uint32_t *min1, uint64_t mask,
                                                              uint32_t *__restrict__ eslot, unsigned *status) {
     using K = KeyOps<KT>;
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * n;
@@ -52,7 +54,7 @@ __global__ void __launch_bounds__(256) link_endpoints_kernel(const uint8_t *__re
         const uint8_t *s = bases + off[i] + (side ? len[i] - (uint32_t)k : 0u);
         const KT fw = ascii_kmer<KT>(s, k);
         const KT rc = K::rc(fw, k);
-        const KT key = fw < rc ? fw : rc;
+        const KT key = (fwd || fw < rc) ? fw : rc;
         uint64_t slot = K::hash(key) & mask;
         uint32_t found = kNoNode;
         for (uint64_t probe = 0; probe <= mask; probe++) {
@@ -300,15 +302,15 @@ static unsigned grid_for(uint64_t n, int sms) {
 }
 
 int launch_link_endpoints(const uint8_t *bases, const uint64_t *off, const uint32_t *len, const uint8_t *flags,
-                          uint64_t n, int k, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
+                          uint64_t n, int k, int fwd, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
                           unsigned *status, int sms, cudaStream_t s) {
     if (n == 0) return 0;
     if (k > 32)
         link_endpoints_kernel<u128><<<grid_for(2 * n, sms), 256, 0, s>>>(
-            bases, off, len, flags, n, k, static_cast<u128 *>(keys), min1, mask, eslot, status);
+            bases, off, len, flags, n, k, fwd, static_cast<u128 *>(keys), min1, mask, eslot, status);
     else
         link_endpoints_kernel<uint64_t><<<grid_for(2 * n, sms), 256, 0, s>>>(
-            bases, off, len, flags, n, k, static_cast<uint64_t *>(keys), min1, mask, eslot, status);
+            bases, off, len, flags, n, k, fwd, static_cast<uint64_t *>(keys), min1, mask, eslot, status);
     link_second_kernel<<<grid_for(2 * n, sms), 256, 0, s>>>(eslot, min1, min1 + (mask + 1), 2 * n);
     return 2;
 }

@@ -142,14 +142,19 @@ __device__ __forceinline__ uint32_t val_mult(uint32_t v) {
     return (v >> 30) == 3u ? (c >> 1) : c;
 }
 
+// The k-mer graph of one unit's table.  Canonical builds key a k-mer and its reverse
+// complement by the smaller of the two and walk both orientations; forward-only builds
+// (fwd = 1, the forward seq-hash / Rabin-Karp families) key and walk k-mers as read.
 template <typename KT>
 struct Graph {
     Table<KT> t;
     int k;
     uint32_t min_mult;
+    int fwd;
 
     __device__ __forceinline__ KT rc(KT v) const { return KeyOps<KT>::rc(v, k); }
     __device__ __forceinline__ KT canon(KT v) const {
+        if (fwd) return v;
         const KT r = rc(v);
         return v < r ? v : r;
     }
@@ -173,16 +178,37 @@ struct Graph {
         }
         return d;
     }
+    // surviving predecessors of oriented v; *only receives the last one found, oriented
+    // towards v
+    __device__ __forceinline__ int pred(KT v, KT &only) const {
+        if (fwd) {
+            int d = 0;
+            const KT base = (v << 2) & KeyOps<KT>::mask(k);
+#pragma unroll
+            for (uint32_t b = 0; b < 4; b++) {
+                const KT u = base | (KT)b;
+                if (alive(u) >= 0) {
+                    d++;
+                    only = u;
+                }
+            }
+            return d;
+        }
+        KT w;
+        const int d = succ(rc(v), w);
+        only = rc(w);
+        return d;
+    }
     // ignored-side flags in the orientation of v (hashmap.rs:453-465):
     // canonical orientation: flags == 1 -> left boundary, flags == 2 -> right boundary.
     __device__ __forceinline__ bool right_boundary(KT v, int64_t slot) const {
         uint32_t f = t.vals[slot] >> 30;
-        bool is_canon = v <= rc(v);
+        bool is_canon = fwd || v <= rc(v);
         return is_canon ? f == 2u : f == 1u;
     }
     __device__ __forceinline__ bool left_boundary(KT v, int64_t slot) const {
         uint32_t f = t.vals[slot] >> 30;
-        bool is_canon = v <= rc(v);
+        bool is_canon = fwd || v <= rc(v);
         return is_canon ? f == 1u : f == 2u;
     }
     // Traversable successor: unique surviving successor u with a unique surviving
@@ -193,15 +219,14 @@ struct Graph {
         su = tfind(t, canon(u));
         if (su == sv) return false;
         KT w;
-        if (succ(rc(u), w) != 1) return false;
+        if (pred(u, w) != 1) return false;
         if (left_boundary(u, su)) return false;
         return true;
     }
     __device__ __forceinline__ bool is_start(KT v, int64_t sv) const {
         if (left_boundary(v, sv)) return true;
-        KT w;
-        if (succ(rc(v), w) != 1) return true;
-        const KT y = rc(w);  // the unique predecessor, oriented towards v
+        KT y;  // the unique predecessor, oriented towards v
+        if (pred(v, y) != 1) return true;
         int64_t sy = tfind(t, canon(y));
         if (sy == sv) return true;
         KT z;
@@ -269,7 +294,7 @@ __device__ void emit_walk(const Graph<KT> &g, KT v, int64_t sv, uint32_t steps, 
 // the bases in text orientation with the flags mapped from the stored orientation.
 template <typename KT>
 __device__ __forceinline__ void insert_record(const Table<KT> &t, const uint64_t *__restrict__ packed, const SkRec r,
-                                              int k, unsigned *status) {
+                                              int k, int fwd, unsigned *status) {
     const uint64_t start = rec_start(r);
     const uint32_t len = rec_len(r);
     const uint32_t fl = rec_flags(r), rcf = rec_rc(r);
@@ -294,7 +319,7 @@ __device__ __forceinline__ void insert_record(const Table<KT> &t, const uint64_t
         uint32_t idx = i + 1 - (uint32_t)k;
         bool begin_ignored = (idx == 0) && !inc_begin;
         bool end_ignored = (idx == last) && !inc_end;
-        uint32_t isf = fw < rc ? 1u : 0u;
+        uint32_t isf = (fwd || fw < rc) ? 1u : 0u;
         const KT key = isf ? fw : rc;
         int64_t s = tinsert(t, key, status);
         if (s < 0) continue;
@@ -321,13 +346,15 @@ __device__ __forceinline__ void extend_slot(const Graph<KT> &g, uint32_t s, cons
             atomicOr(o.status, kStatusKmerOverflow);
         }
     }
-    for (int orient = 0; orient < 2; orient++) {
+    for (int orient = 0; orient < (g.fwd ? 1 : 2); orient++) {
         const KT v = orient ? g.rc(key) : key;
         if (!g.is_start(v, s)) continue;
         KT e;
         int64_t se;
         uint32_t steps = walk_to_end(g, v, (int64_t)s, e, se, o.status);
-        bool owner = ((int64_t)s < se) || ((int64_t)s == se && orient == 0);
+        // canonical: a path is found from both ends, the lower slot emits it; forward-only: it
+        // is found from its start only
+        bool owner = g.fwd || ((int64_t)s < se) || ((int64_t)s == se && orient == 0);
         if (!owner) continue;
         uint8_t flags = (uint8_t)((g.left_boundary(v, s) ? 1u : 0u) | (g.right_boundary(e, se) ? 2u : 0u));
         emit_walk(g, v, (int64_t)s, steps, flags, o);
@@ -684,6 +711,30 @@ __device__ __forceinline__ int alive_succ_shared(const Table<uint64_t> &t, uint6
     return d;
 }
 
+// forward-only builds: surviving successors of the k-mer x read forward (back = 0) or its
+// predecessors (back = 1, the node that walks x backwards); v_only receives the value word of
+// the last one found
+template <typename KT>
+__device__ __forceinline__ int alive_succ_fwd(const Table<KT> &t, KT x, bool back, int k, uint32_t &v_only,
+                                              bool &fw_only) {
+    int d = 0;
+    const KT mask = KeyOps<KT>::mask(k);
+#pragma unroll
+    for (uint32_t b = 0; b < 4; b++) {
+        const KT w = back ? (((x << 2) & mask) | (KT)b) : ((x >> 2) | ((KT)b << (2 * (k - 1))));
+        const int64_t sw = tfind(t, w);
+        if (sw >= 0) {
+            const uint32_t vw = t.vals[sw];
+            if (val_alive(vw)) {
+                d++;
+                v_only = vw;
+            }
+        }
+    }
+    fw_only = !back;
+    return d;
+}
+
 template <typename KT>
 __device__ __forceinline__ KT oriented(const KT *sk, uint32_t u, int k) {
     const KT x = sk[u >> 1];
@@ -741,7 +792,7 @@ template <typename KT, typename IT, int NT, int kRegJ, bool kGlobalArr, bool kSh
 __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *t_list, bool list_scan,
                                             uint32_t seg_lo, uint32_t seg_hi, uint32_t warp_base, uint32_t n_surv,
                                             const ExtArrays<KT, IT> &A, ExtShared &X, int k, uint32_t min_mult,
-                                            int keep_kmers, const MergeOut &o) {
+                                            int keep_kmers, int fwd, const MergeOut &o) {
     using K = KeyOps<KT>;
     constexpr IT kNone = (IT)~(IT)0;
     constexpr IT kMulti = (IT)(kNone - 1);
@@ -801,7 +852,10 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
         const bool odd = (u & 1) != 0;  // select the operands, not the call: lanes alternate parity
         int d;
         uint32_t v_only = 0;
-        if constexpr (kSharedTable && std::is_same<KT, uint64_t>::value) {
+        if (fwd) {
+            // forward-only: even node = x read forward, odd node = x walked backwards
+            d = alive_succ_fwd(t, x, odd, k, v_only, fw_only);
+        } else if constexpr (kSharedTable && std::is_same<KT, uint64_t>::value) {
             d = alive_succ_shared(t, odd ? rx : x, odd ? x : rx, k, v_only, fw_only);
         } else {
             int64_t s_only = -1;
@@ -883,7 +937,8 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
         const IT e = J[u];
         if (A.succ[e] != kNone) continue;  // on a cycle (handled below)
         const uint32_t su = u >> 1, se = (uint32_t)e >> 1;
-        const bool owner = su < se || (su == se && (u & 1) == 0);
+        // a path and its mirror: the one starting lower (forward-only: the one read forward)
+        const bool owner = fwd ? (u & 1) == 0 : (su < se || (su == se && (u & 1) == 0));
         if (!owner) continue;
         const uint32_t len = (uint32_t)k + (uint32_t)Rk[u];
         A.offs[u] = atomicAdd(&X.loc_bases, len);
@@ -908,7 +963,7 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
         const uint32_t s0 = (uint32_t)me ^ 1u;      // start of u's path
         const IT e = J[u];
         const uint32_t ss = s0 >> 1, se = (uint32_t)e >> 1;
-        const bool owner = ss < se || (ss == se && (s0 & 1) == 0);
+        const bool owner = fwd ? (s0 & 1) == 0 : (ss < se || (ss == se && (s0 & 1) == 0));
         if (!owner || !ok) continue;
         const uint32_t dist = Rk[mu];               // distance from the start
         const unsigned long long off = gbase + A.offs[s0];
@@ -1108,7 +1163,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                                              : K::load(S.stage[(threadIdx.x & ~31u) + ri],
                                                        pos - ((rw0 & ((1ull << 40) - 1)) & ~31ull), k);
                     const KT rc = K::rc(fw, k);
-                    const uint32_t isf = fw < rc ? 1u : 0u;
+                    const uint32_t isf = (a.forward || fw < rc) ? 1u : 0u;
                     if constexpr (!kGlobalTable && std::is_same<KT, uint64_t>::value)
                         sl = tinsert_shared(t, isf ? fw : rc, o.status, created);
                     else if (optimistic || kGlobalTable)
@@ -1187,7 +1242,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             ExtArrays<KT, uint16_t> A{S.sk,          S.succ,    S.bflag,      S.u.r.jump, S.u.r.rank,
                                       nullptr,       nullptr,   S.u.r.offs,   S.u.r.uidx, S.u.r.haspred};
             extend_unit<KT, uint16_t, NT, (kMaxSurv * 2 + NT - 1) / NT, false, !kGlobalTable>(
-                t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, o);
+                t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, a.forward, o);
         } else if (a.ext_scratch != nullptr && n_surv <= a.ext_cap) {
             // more survivors than the shared-memory arrays hold: the same ranking on this
             // CTA's scratch in global memory
@@ -1195,13 +1250,13 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             const ExtArrays<KT, uint32_t> A =
                 ext_global_arrays<KT>(a.ext_scratch + (size_t)blockIdx.x * a.ext_stride, a.ext_cap);
             extend_unit<KT, uint32_t, NT, 1, true, !kGlobalTable>(t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x,
-                                                  k, min_mult, a.keep_kmers, o);
+                                                  k, min_mult, a.keep_kmers, a.forward, o);
         } else {
             // walk fallback (no scratch for this many survivors; a shared-memory table never has
             // more survivors than the scratch holds)
             if (threadIdx.x == 0) atomicAdd(&o.counters[kCntWalk], 1ull);
             if constexpr (kGlobalTable) {
-                Graph<KT> g{t, k, min_mult};
+                Graph<KT> g{t, k, min_mult, a.forward};
                 for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x)
                     extend_slot(g, sl, o, a.keep_kmers, min_mult);
                 __syncthreads();
@@ -1249,7 +1304,7 @@ __global__ void __launch_bounds__(256) large_insert_kernel(MergeArgs a, const Me
     for (uint64_t u = 0; u < n_units; u++) {
         const MergeUnit U = units[u];
         Table<KT> t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
-        for (uint64_t r = U.rec_begin + gt; r < U.rec_end; r += gs) insert_record(t, a.packed, a.recs[r], a.k, o.status);
+        for (uint64_t r = U.rec_begin + gt; r < U.rec_end; r += gs) insert_record(t, a.packed, a.recs[r], a.k, a.forward, o.status);
     }
 }
 
@@ -1263,7 +1318,7 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
     for (uint64_t u = 0; u < n_units; u++) {
         const MergeUnit U = units[u];
         Table<KT> t{keys + U.table_off, vals + U.table_off, vis + U.table_off, U.table_cap};
-        Graph<KT> g{t, a.k, (uint32_t)a.min_mult};
+        Graph<KT> g{t, a.k, (uint32_t)a.min_mult, a.forward};
         unsigned long long occ = 0;
         for (uint64_t s = gt; s < U.table_cap; s += gs) {
             if (phase == 0) {

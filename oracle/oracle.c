@@ -945,10 +945,13 @@ static void rc_ascii(uint8_t *s, size_t n) {
         }
     }
 }
-static u128 pack_ascii_canon(const uint8_t *a, int k) {
+/* link key of a boundary k-mer: its unextendable hash identity, i.e. the canonical packed
+ * k-mer for the canonical hash families and the k-mer as read for the forward ones
+ * (extend_unitigs.rs:142-147, 196-240 key the extremities by hash.to_unextendable()) */
+static u128 pack_ascii_key(const uint8_t *a, int k, int canonical) {
     uint8_t tmp[128];
     for (int i = 0; i < k; i++) tmp[i] = orc_compress_base(a[i]);
-    return pack_canonical(tmp, k, 1);
+    return pack_canonical(tmp, k, canonical);
 }
 
 typedef struct {
@@ -957,7 +960,7 @@ typedef struct {
     uint8_t occupied;
 } link_entry;
 
-static void link_stage(unitig_vec *in, int k, unitig_vec *out) {
+static void link_stage(unitig_vec *in, int k, int canonical, unitig_vec *out) {
     size_t n = in->n;
     /* endpoint 2i = left end (bw link), 2i+1 = right end (fw link) */
     size_t cap = 64;
@@ -970,7 +973,7 @@ static void link_stage(unitig_vec *in, int k, unitig_vec *out) {
             unitig_t *u = &in->v[i];
             if (!(side ? u->fw_link : u->bw_link)) continue;
             const uint8_t *km = side ? u->seq + u->len - k : u->seq;
-            u128 key = pack_ascii_canon(km, k);
+            u128 key = pack_ascii_key(km, k, canonical);
             size_t h = khash(key) & (cap - 1);
             while (tab[h].occupied && tab[h].key != key) h = (h + 1) & (cap - 1);
             if (!tab[h].occupied) {
@@ -1230,7 +1233,7 @@ orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const 
         else
             ut_push(&fin, partial.v[i]);
     }
-    link_stage(&linked, p->k, &fin);
+    link_stage(&linked, p->k, orc_hash_is_canonical(p->hash_kind), &fin);
     for (size_t i = 0; i < linked.n; i++) free(linked.v[i].seq);
     free(linked.v);
     free(partial.v);

@@ -305,13 +305,29 @@ def test_edge_case_inputs_match_oracle(ctx, case):
     assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, 31) == r.unitigs()
 
 
-def test_forward_only_merge_is_rejected(ctx):
-    """Forward-only bucketing runs; the canonical device merge refuses forward-only builds
-    instead of returning canonical results."""
-    text, off, ln, _ = _workload("genomes", 3)
-    p = make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=1, forward_only=True)
-    with pytest.raises(_native.GgcatGpuError, match="EUNSUPPORTED"):
-        ctx.build_text(text, p)
+@pytest.mark.parametrize("mode", [_native.GGCAT_MERGE_BATCHED, _native.GGCAT_MERGE_PER_BUCKET])
+@pytest.mark.parametrize("kind,k,m,okind", [("genomes", 31, 10, oracle.H_FW_SEQ64), ("reads", 31, 10, oracle.H_FW_SEQ64),
+                                            ("reads", 63, 12, oracle.H_FW_SEQ128)])
+def test_forward_only_matches_oracle(ctx, kind, k, m, okind, mode):
+    """Forward-only builds (forward seq-hash): records stay in text orientation, k-mers are
+    keyed and extended as read (successors forward, predecessors backward) and only forward
+    paths are emitted; k-mers and unitigs equal the oracle's forward-hash build."""
+    text, off, ln, _ = _workload(kind, 41)
+    p = make_params(k=k, m=m, bucket_bits=6, second_bits=2, min_multiplicity=1, keep_kmers=True, forward_only=True,
+                    merge_mode=mode)
+    ctx.build_text(text, p)
+    keys, mult = ctx.kmers()
+    if k > 32:
+        keys = [int(a) | (int(b) << 64) for a, b in keys.tolist()]
+    op = oracle.params(k=k, m=m, bucket_bits=6, second_bits=2, canonical=False, hash_kind=okind, min_multiplicity=1,
+                       threads=8)
+    r = oracle.build_graph(text, off, ln, op)
+    lo, hi, emult = r.kmers()
+    assert _kmer_dict(keys, mult) == {int(a) | (int(b) << 64): int(c)
+                                      for a, b, c in zip(lo.tolist(), hi.tolist(), emult.tolist())}
+    ctx.link(k)
+    bases, uo, ul, uf = ctx.unitigs()
+    assert oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k) == r.unitigs()
 
 
 def test_build_graph_from_fasta_files_matches_oracle(tmp_path):
