@@ -106,3 +106,32 @@ class GGCATInstance:
                 self.config.messages_callback(2, msg.decode() if msg else "")
             return ""
         return output_file
+
+    def query_graph(
+        self,
+        input_graph: str,
+        input_query: str,
+        output_file_prefix: str,
+        kmer_length: int = 31,
+        threads_count: int = 1,
+        forward_only: bool = False,
+        minimizer_length: Optional[int] = None,
+        colors: bool = False,
+        color_output_format: int = 0,
+    ) -> str:
+        """crates/api/src/lib.rs:325-382 for uncoloured graphs: writes the querier's CSV
+        (query_index,matched_kmers,query_kmers,match_percentage) and returns its path ("" on
+        failure, like the C API)."""
+        if colors:
+            raise GgcatGpuError("coloured queries from files need the colormap file, which the device path does not write")
+        L = load()
+        out = C.create_string_buffer(4096)
+        rc = L.ggcat_gpu_query_from_files(self.ctx.h, os.fsencode(input_graph), os.fsencode(input_query),
+                                          os.fsencode(output_file_prefix), kmer_length, int(forward_only), out,
+                                          len(out))
+        if rc != 0:
+            msg = L.ggcat_gpu_last_error(self.ctx.h)
+            if self.config.messages_callback:
+                self.config.messages_callback(2, msg.decode() if msg else "")
+            return ""
+        return out.value.decode()

@@ -102,6 +102,7 @@ EXPORTED = [
     "ggcat_gpu_subsets_copy",
     "ggcat_gpu_query_index",
     "ggcat_gpu_query_index_colored",
+    "ggcat_gpu_query_from_files",
     "ggcat_gpu_query_submit",
     "ggcat_gpu_query_poll",
     "ggcat_gpu_query_wait",
@@ -140,6 +141,8 @@ def load(build: bool = True):
     L.ggcat_gpu_bucketize.argtypes = [P, P, u64, C.POINTER(Params), P, pu64]
     L.ggcat_gpu_superkmers_copy.argtypes = [P, P, u64, pu64]
     L.ggcat_gpu_merge.argtypes = [P, C.POINTER(Params), P]
+    L.ggcat_gpu_query_from_files.argtypes = [P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_char_p,
+                                             u64]
     L.ggcat_gpu_autotune.argtypes = [P, P, u64, C.POINTER(Params), u64, P, C.POINTER(Params),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ggcat_gpu_partial_unitigs_copy.argtypes = [P, P, u64, P, P, P, u64, pu64, pu64]

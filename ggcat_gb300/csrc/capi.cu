@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <unordered_map>
+#include <cmath>
 #include <vector>
 
 #include "../../include/ggcat_gb300.h"
@@ -132,6 +133,7 @@ struct ggcat_gpu_ctx {
     DevBuf<uint32_t> tlist;  // created-entry lists of the M units
     DevBuf<uint8_t> ext_scratch;  // per-CTA extension scratch of units with many survivors
     LinkBufs lk;
+    DevBuf<uint8_t> qgraph;  // graph text of the file-level query
     uint64_t n_final = 0, n_final_bases = 0;
     // the batched merge phase as a CUDA graph, captured once per buffer/parameter layout
     cudaStream_t cap_stream = nullptr;
@@ -1377,6 +1379,133 @@ extern "C" int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64
     if (n_colors) *n_colors = ctx->c_colors;
     if (h_counts)
         memcpy(h_counts, q.h_counts.p, std::min<uint64_t>(cap, q.nq * (uint64_t)ctx->c_colors) * sizeof(uint64_t));
+    return GGCAT_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// file-level query: the uncoloured path of GGCATInstance::query_graph
+// ---------------------------------------------------------------------------
+namespace {
+// FASTA records as whole sequences (one query per record), bases normalised like
+// SequencesReader (ACGTacgt -> upper case, anything else -> N), each followed by '\n'
+bool read_fasta_records(const char *path, std::vector<uint8_t> &text, std::vector<uint64_t> &off,
+                        std::vector<uint64_t> &len) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return false;
+    std::vector<uint8_t> data;
+    uint8_t buf[1 << 16];
+    size_t r;
+    while ((r = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + r);
+    fclose(f);
+    uint8_t norm[256];
+    for (int i = 0; i < 256; i++) norm[i] = 'N';
+    for (const char c : {'A', 'C', 'G', 'T'}) norm[(uint8_t)c] = norm[(uint8_t)(c | 0x20)] = (uint8_t)c;
+    bool in_seq = false;
+    size_t i = 0;
+    while (i < data.size()) {
+        size_t e = i;
+        while (e < data.size() && data[e] != '\n') e++;
+        size_t le = e;
+        if (le > i && data[le - 1] == '\r') le--;
+        if (le > i && data[i] == '>') {
+            if (in_seq) {
+                len.push_back(text.size() - off.back());
+                text.push_back('\n');
+            }
+            off.push_back(text.size());
+            in_seq = true;
+        } else if (in_seq && !(le > i && data[i] == ';')) {
+            for (size_t j = i; j < le; j++) text.push_back(norm[data[j]]);
+        }
+        i = e + 1;
+    }
+    if (in_seq) {
+        len.push_back(text.size() - off.back());
+        text.push_back('\n');
+    }
+    return true;
+}
+}  // namespace
+
+extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
+                                          const char *output_prefix, int k, int forward_only, char *out_path,
+                                          uint64_t out_cap) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!graph_fasta || !query_fasta || !output_prefix) return fail(ctx, GGCAT_GPU_EINVAL, "null path");
+    if (forward_only) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
+    // graph: the unitigs as text (records cut like the reference's reader, k-1 copyback)
+    std::vector<uint8_t> graph;
+    {
+        FILE *f = fopen(graph_fasta, "rb");
+        if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", graph_fasta);
+        std::vector<uint8_t> data;
+        uint8_t buf[1 << 16];
+        size_t r;
+        while ((r = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + r);
+        fclose(f);
+        uint64_t need = 0, pieces = 0;
+        int rc = ggcat_gpu_fasta_parse(data.data(), data.size(), k - 1, nullptr, 0, &need, &pieces);
+        if (rc) return rc;
+        graph.resize(need);
+        rc = ggcat_gpu_fasta_parse(data.data(), data.size(), k - 1, graph.data(), need, &need, &pieces);
+        if (rc) return rc;
+    }
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->qgraph.ensure(graph.size() + 64));
+    if (!graph.empty()) CK(cudaMemcpy(ctx->qgraph.p, graph.data(), graph.size(), cudaMemcpyHostToDevice));
+    int rc = ggcat_gpu_query_index(ctx, ctx->qgraph.p, graph.size(), k, nullptr);
+    if (rc) return rc;
+    // queries: one per FASTA record, submitted in batches of bounded text size
+    std::vector<uint8_t> qtext;
+    std::vector<uint64_t> qoff, qlen;
+    if (!read_fasta_records(query_fasta, qtext, qoff, qlen)) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", query_fasta);
+    const uint64_t nq = qoff.size();
+    std::vector<uint64_t> matched(nq, 0);
+    const uint64_t kBatchBytes = 256ull << 20;
+    for (uint64_t a = 0; a < nq;) {
+        uint64_t b = a + 1;
+        while (b < nq && qoff[b] + qlen[b] - qoff[a] <= kBatchBytes) b++;
+        const uint64_t lo = qoff[a], hi = qoff[b - 1] + qlen[b - 1];
+        std::vector<uint64_t> o(b - a), l(b - a);
+        for (uint64_t i = a; i < b; i++) {
+            o[i - a] = qoff[i] - lo;
+            l[i - a] = qlen[i];
+        }
+        rc = ggcat_gpu_query_submit(ctx, 0, qtext.data() + lo, hi - lo, o.data(), l.data(), b - a);
+        if (rc) return rc;
+        uint64_t got = 0;
+        rc = ggcat_gpu_query_wait(ctx, 0, matched.data() + a, b - a, &got);
+        if (rc) return rc;
+        a = b;
+    }
+    // the CSV of counters_sorting (crates/querier/src/pipeline/counters_sorting.rs:235-268):
+    // query_index, matched_kmers, query_kmers = len - (k - 1), matched / query_kmers to 2 places
+    std::string path = output_prefix;
+    {
+        const size_t slash = path.find_last_of('/');
+        const size_t dot = path.find_last_of('.');
+        if (dot == std::string::npos || (slash != std::string::npos && dot < slash) || dot == slash + 1) path += ".csv";
+    }
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot write %s", path.c_str());
+    fprintf(f, "query_index,matched_kmers,query_kmers,match_percentage\n");
+    for (uint64_t i = 0; i < nq; i++) {
+        const uint64_t qk = qlen[i] >= (uint64_t)(k - 1) ? qlen[i] - (uint64_t)(k - 1) : 0;
+        const double frac = (double)matched[i] / (double)qk;
+        char num[64];
+        if (std::isnan(frac))
+            snprintf(num, sizeof num, "NaN");
+        else if (std::isinf(frac))
+            snprintf(num, sizeof num, "inf");
+        else
+            snprintf(num, sizeof num, "%.2f", frac);
+        fprintf(f, "%llu,%llu,%llu,%s\n", (unsigned long long)i, (unsigned long long)matched[i],
+                (unsigned long long)qk, num);
+    }
+    fclose(f);
+    if (out_path && out_cap) {
+        snprintf(out_path, out_cap, "%s", path.c_str());
+    }
     return GGCAT_GPU_OK;
 }
 

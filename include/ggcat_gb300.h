@@ -214,6 +214,15 @@ int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint6
 /* Coloured index from the last ggcat_gpu_colors result (the build's k-mers and subsets). */
 int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
 
+/* Replaces ggcat_query_graph (crates/capi/src/lib.rs:324-380) / GGCATInstance::query_graph
+ * (crates/api/src/lib.rs:325-382) for uncoloured graphs: indexes the unitigs of graph_fasta,
+ * looks up every k-mer of every record of query_fasta and writes the querier's CSV
+ * (query_index,matched_kmers,query_kmers,match_percentage; counters_sorting.rs:235-268) to
+ * output_prefix, ".csv" appended when it has no extension; the written path is copied to
+ * out_path.  Canonical k-mers, k <= 32. */
+int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
+                               const char *output_prefix, int k, int forward_only, char *out_path, uint64_t out_cap);
+
 /* Submits a batch of queries (host text layout; query i = h_text[h_off[i], h_off[i]+h_len[i]))
  * to slot `slot` and returns without waiting.  The slot's H2D copy, lookup kernel and D2H
  * copy run on the slot's own stream. */

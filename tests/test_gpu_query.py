@@ -64,3 +64,33 @@ def test_query_server_continuous_batching(setup):
     base = serve.serve(ctx, 31, text, off, ln, arrivals, slots=4, one_per_launch=True)
     assert [int(x) for x in base.matched] == [int(x) for x in exp]
     assert base.batches == len(queries)
+
+
+def test_query_graph_from_files_writes_the_querier_csv(setup, tmp_path):
+    """GGCATInstance.query_graph on FASTA files: the graph's unitigs indexed on the device,
+    one query per FASTA record, and the querier's CSV (query_index, matched_kmers,
+    query_kmers = len - (k - 1), matched / query_kmers to two places) with the oracle's
+    counts."""
+    import ggcat_gb300
+
+    ctx, queries, arrivals, exp, d_graph = setup
+    graph = d_graph.cpu().numpy().tobytes()
+    gpath, qpath = tmp_path / "graph.fa", tmp_path / "queries.fa"
+    with open(gpath, "wb") as f:
+        for i, line in enumerate(x for x in graph.split(b"\n") if x):
+            f.write(b">%d LN:i:%d\n" % (i, len(line)) + line + b"\n")
+    with open(qpath, "wb") as f:
+        for i, q in enumerate(queries):
+            seq = q.tobytes()
+            f.write(b">q%d\n" % i + b"\n".join(seq[j:j + 70] for j in range(0, len(seq), 70)) + b"\n")
+    inst = ggcat_gb300.GGCATInstance.create(ggcat_gb300.GGCATConfig())
+    out = inst.query_graph(str(gpath), str(qpath), str(tmp_path / "result"), kmer_length=31)
+    assert out == str(tmp_path / "result.csv")
+    rows = open(out).read().strip().split("\n")
+    assert rows[0] == "query_index,matched_kmers,query_kmers,match_percentage"
+    assert len(rows) == 1 + len(queries)
+    for i, row in enumerate(rows[1:]):
+        qi, matched, qk, pct = row.split(",")
+        n = max(0, len(queries[i]) - 30)
+        assert (int(qi), int(matched), int(qk)) == (i, int(exp[i]), n)
+        assert pct == ("NaN" if n == 0 else f"{int(exp[i]) / n:.2f}")
