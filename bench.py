@@ -66,6 +66,22 @@ def _args():
     return ap.parse_args()
 
 
+def max_over_ranks(value: float, dist, device) -> float:
+    """The slowest rank's time (replicas: every rank builds its own copy of the workload)."""
+    if not dist:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbases_per_s(bases_per_rank: int, world_size: int, ms: float) -> float:
+    """Whole-job throughput of N replicas: all ranks' bases over the slowest rank's time."""
+    return bases_per_rank * world_size / (ms * 1e-3) / 1e9
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -438,18 +454,14 @@ def run_gpu(args):
                 ph[key] += st[key]
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        if dist:
-            t = torch.tensor([ms], device=f"cuda:{dev}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, dist, f"cuda:{dev}")
         return ms, (ctx.kernel_launches - l0) // steps, {k2: v / steps for k2, v in ph.items()}, st
 
     pb = params(_native.GGCAT_MERGE_BATCHED)
     with ClockSampler(dev) as clk:
         ms, launches, phases, st = timed(pb, args.steps, args.warmup)
     clocks = clk.summary()
-    value = bases * ws / (ms * 1e-3) / 1e9
+    value = job_gbases_per_s(bases, ws, ms)
 
     # autotuned knobs (sub-bin digit width, S-unit packing and size limit, table load) on the
     # same input, timed like the headline
