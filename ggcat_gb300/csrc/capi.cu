@@ -1213,16 +1213,17 @@ extern "C" int ggcat_gpu_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_bitmaps, u
 extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k,
                                      void *stream) {
     if (!ctx) return GGCAT_GPU_EINVAL;
-    if (k < 3 || k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "query index supports k <= 32 (k=%d)", k);
+    if (k < 3 || k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "query index supports k <= 64 (k=%d)", k);
+    const uint64_t kw = k > 32 ? 2 : 1;  // key words (u128 keys above k = 32)
     if (len > 0 && !d_graph_text) return fail(ctx, GGCAT_GPU_EINVAL, "null graph text");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
     ctx->qready = false;
     uint64_t cap = 1024;
     while (cap < 2 * len + 64) cap <<= 1;  // one slot per k-mer position at load <= 0.5
-    CK(ctx->qkeys.ensure(cap));
+    CK(ctx->qkeys.ensure(cap * kw));
     CK(ctx->qvals.ensure(cap));
-    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * kw * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
     ctx->launches += launch_index_insert(d_graph_text, len, k, ctx->qkeys.p, ctx->qvals.p, cap - 1, ctx->status.p + 1, s);
     CK(cudaGetLastError());

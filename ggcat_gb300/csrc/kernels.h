@@ -131,12 +131,13 @@ uint64_t merge_wide_limit(int wide);
 int merge_ctas_per_sm(int tier, int wide);
 
 // query.cu
-int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,
+// uncoloured index keys: u64 for k <= 32, u128 (16-byte aligned) for k <= 64
+int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
                         unsigned *status, cudaStream_t s);
 int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint64_t ccap, const uint32_t *id_subset,
                              uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s);
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
-                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, uint64_t mask,
+                 const uint32_t *item_len, uint64_t n_items, const void *keys, uint64_t mask,
                  unsigned long long *matched, cudaStream_t s);
 int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
                        const uint64_t *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,

@@ -17,16 +17,25 @@ namespace ggcat {
 
 __device__ __forceinline__ uint32_t qslot(uint64_t key, uint64_t mask) { return (uint32_t)(mix64(key) & mask); }
 
+// slot of a key in the uncoloured index (u64 keys for k <= 32, u128 for k <= 64)
+__device__ __forceinline__ uint32_t qslot_key(uint64_t key, uint64_t mask) { return qslot(key, mask); }
+__device__ __forceinline__ uint32_t qslot_key(u128 key, uint64_t mask) {
+    return (uint32_t)(mix64((uint64_t)key ^ ((uint64_t)(key >> 64) * 0x9E3779B97F4A7C15ull)) & mask);
+}
+
 // Insert every canonical k-mer of the graph text (pieces separated by non-ACGT bytes).
+template <typename KT>
 __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
-                                                           uint64_t chunk, uint64_t *keys, uint32_t *vals,
-                                                           uint64_t mask, unsigned *status) {
+                                                           uint64_t chunk, KT *keys, uint32_t *vals, uint64_t mask,
+                                                           unsigned *status) {
+    using K = KeyOps<KT>;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t x0 = tid * chunk;  // k-mer start positions [x0, x1)
     if (x0 >= n) return;
     const uint64_t x1 = min(x0 + chunk, n);
-    const uint64_t kmask = kmer_mask(k);
-    uint64_t fw = 0, rc = 0, run = 0;
+    const KT kmask = K::mask(k);
+    KT fw = 0, rc = 0;
+    uint64_t run = 0;
     const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
     for (uint64_t p = x0; p < pend; p++) {
         const uint32_t c = text[p];
@@ -35,19 +44,18 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
             run = 0;
             continue;
         }
-        const uint64_t b = (c >> 1) & 3u;
-        fw = (fw >> 2) | (b << (2 * (k - 1)));
-        rc = ((rc << 2) | (b ^ 2u)) & kmask;
+        const uint32_t b = (c >> 1) & 3u;
+        fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
+        rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
         if (++run < (uint64_t)k) continue;
-        const uint64_t key = fw < rc ? fw : rc;
-        uint64_t s = qslot(key, mask);
+        const KT key = fw < rc ? fw : rc;
+        uint64_t s = qslot_key(key, mask);
         for (uint64_t probe = 0; probe <= mask; probe++) {
-            const uint64_t kk = keys[s];
+            const KT kk = keys[s];
             if (kk == key) break;
-            if (kk == kEmptyKey) {
-                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
-                                                         (unsigned long long)kEmptyKey, (unsigned long long)key);
-                if (old == kEmptyKey) {
+            if (kk == K::empty()) {
+                const KT old = K::cas(&keys[s], K::empty(), key);
+                if (old == K::empty()) {
                     vals[s] = 0u;
                     break;
                 }
@@ -87,19 +95,22 @@ __global__ void index_from_colors_kernel(const uint64_t *__restrict__ ckeys, con
 }
 
 // One work item = a run of k-mer positions of one query; matches are summed per query.
+template <typename KT>
 __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ text, int k,
                                                    const uint32_t *__restrict__ item_query,
                                                    const uint64_t *__restrict__ item_start,
                                                    const uint32_t *__restrict__ item_len, uint64_t n_items,
-                                                   const uint64_t *__restrict__ keys, uint64_t mask,
+                                                   const KT *__restrict__ keys, uint64_t mask,
                                                    unsigned long long *__restrict__ matched) {
+    using K = KeyOps<KT>;
     const uint64_t it = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= n_items) return;
     const uint32_t q = item_query[it];
     const uint64_t x0 = item_start[it];
     const uint64_t x1 = x0 + item_len[it];  // k-mer start positions
-    const uint64_t kmask = kmer_mask(k);
-    uint64_t fw = 0, rc = 0, run = 0, hits = 0;
+    const KT kmask = K::mask(k);
+    KT fw = 0, rc = 0;
+    uint64_t run = 0, hits = 0;
     for (uint64_t p = x0; p < x1 + (uint64_t)k - 1; p++) {
         const uint32_t c = text[p];
         const uint32_t u = c & 0xDFu;
@@ -107,19 +118,19 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
             run = 0;
             continue;
         }
-        const uint64_t b = (c >> 1) & 3u;
-        fw = (fw >> 2) | (b << (2 * (k - 1)));
-        rc = ((rc << 2) | (b ^ 2u)) & kmask;
+        const uint32_t b = (c >> 1) & 3u;
+        fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
+        rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
         if (++run < (uint64_t)k) continue;
-        const uint64_t key = fw < rc ? fw : rc;
-        uint64_t s = qslot(key, mask);
+        const KT key = fw < rc ? fw : rc;
+        uint64_t s = qslot_key(key, mask);
         for (uint64_t probe = 0; probe <= mask; probe++) {
-            const uint64_t kk = keys[s];
+            const KT kk = keys[s];
             if (kk == key) {
                 hits++;
                 break;
             }
-            if (kk == kEmptyKey) break;
+            if (kk == K::empty()) break;
             s = (s + 1) & mask;
         }
     }
@@ -211,12 +222,17 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
     }
 }
 
-int launch_index_insert(const uint8_t *text, uint64_t n, int k, uint64_t *keys, uint32_t *vals, uint64_t mask,
+int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
                         unsigned *status, cudaStream_t s) {
     const uint64_t chunk = 256;
     const uint64_t threads = (n + chunk - 1) / chunk;
     if (threads == 0) return 0;
-    index_insert_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n, k, chunk, keys, vals, mask, status);
+    const unsigned grid = (unsigned)((threads + 255) / 256);
+    if (k > 32)
+        index_insert_kernel<u128><<<grid, 256, 0, s>>>(text, n, k, chunk, static_cast<u128 *>(keys), vals, mask, status);
+    else
+        index_insert_kernel<uint64_t>
+            <<<grid, 256, 0, s>>>(text, n, k, chunk, static_cast<uint64_t *>(keys), vals, mask, status);
     return 1;
 }
 
@@ -227,11 +243,16 @@ int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint6
 }
 
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
-                 const uint32_t *item_len, uint64_t n_items, const uint64_t *keys, uint64_t mask,
+                 const uint32_t *item_len, uint64_t n_items, const void *keys, uint64_t mask,
                  unsigned long long *matched, cudaStream_t s) {
     if (n_items == 0) return 0;
-    query_kernel<<<(unsigned)((n_items + 255) / 256), 256, 0, s>>>(text, k, item_query, item_start, item_len, n_items,
-                                                                  keys, mask, matched);
+    const unsigned grid = (unsigned)((n_items + 255) / 256);
+    if (k > 32)
+        query_kernel<u128><<<grid, 256, 0, s>>>(text, k, item_query, item_start, item_len, n_items,
+                                                static_cast<const u128 *>(keys), mask, matched);
+    else
+        query_kernel<uint64_t><<<grid, 256, 0, s>>>(text, k, item_query, item_start, item_len, n_items,
+                                                    static_cast<const uint64_t *>(keys), mask, matched);
     return 1;
 }
 

@@ -209,7 +209,7 @@ int ggcat_gpu_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_bitmaps, uint64_t cap
 
 /* Uncoloured index from the graph's unitigs in the text layout (device memory); replaces the
  * graph side of the querier's bucketing and per-bucket maps (querier_minimizer_bucketing.rs:233-288,
- * parallel_kmers_query.rs:362-403).  k <= 32. */
+ * parallel_kmers_query.rs:362-403).  k <= 64 (u128 keys above 32). */
 int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_text, uint64_t len, int k, void *stream);
 /* Coloured index from the last ggcat_gpu_colors result (the build's k-mers and subsets). */
 int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
@@ -219,7 +219,7 @@ int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
  * looks up every k-mer of every record of query_fasta and writes the querier's CSV
  * (query_index,matched_kmers,query_kmers,match_percentage; counters_sorting.rs:235-268) to
  * output_prefix, ".csv" appended when it has no extension; the written path is copied to
- * out_path.  Canonical k-mers, k <= 32. */
+ * out_path.  Canonical k-mers, k <= 64. */
 int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
                                const char *output_prefix, int k, int forward_only, char *out_path, uint64_t out_cap);
 

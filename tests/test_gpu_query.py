@@ -94,3 +94,33 @@ def test_query_graph_from_files_writes_the_querier_csv(setup, tmp_path):
         n = max(0, len(queries[i]) - 30)
         assert (int(qi), int(matched), int(qk)) == (i, int(exp[i]), n)
         assert pct == ("NaN" if n == 0 else f"{int(exp[i]) / n:.2f}")
+
+
+def test_query_k63_matches_oracle():
+    """k = 63 (u128 index keys): a graph built on the GPU from related genomes, queries with
+    substitutions and N, matched counts equal the oracle's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(63)
+    g = synth.random_genome(80_000, rng)
+    gs = [g, synth.substitute(g, 0.01, rng)]
+    text, off, ln, _ = synth.pack_sequences(gs)
+    ctx = _native.GpuContext(0)
+    try:
+        p = _native.make_params(k=63, m=12, bucket_bits=6, second_bits=2, min_multiplicity=1)
+        ctx.build_text(text, p)
+        ctx.link(63)
+        bases, uo, ul, uf = ctx.unitigs()
+        graph = np.frombuffer(_native.unitig_lines(bases, uo, ul), np.uint8).copy()
+        d_graph = torch.from_numpy(graph).cuda()
+        ctx.query_index(d_graph.data_ptr(), d_graph.numel(), 63)
+        r = oracle.build_graph(text, off, ln, oracle.params(k=63, m=12, bucket_bits=6, second_bits=2, threads=4))
+        lo, hi, _ = r.kmers()
+        queries, _ = synth.query_stream(gs, 60, rng, min_len=40, max_len=5_000, rate_per_s=1000.0)
+        queries[2] = np.frombuffer(b"ACGTN" * 40, np.uint8)
+        qt, qo, ql = serve._pack(queries)
+        exp, _, _ = oracle.query(lo, hi, qt, qo, ql, 63)
+        ctx.query_submit(0, qt, qo, ql)
+        got = ctx.query_wait(0)
+        assert (got == exp).all() and exp.sum() > 0
+    finally:
+        ctx.close()
