@@ -19,38 +19,53 @@ namespace ggcat {
 
 // ---------------------------------------------------------------------------
 // Pack: ASCII -> 2-bit codes (A0 C1 T2 G3 = (c >> 1) & 3) + validity bits.
-// One thread per 32 bases: two 16-byte loads, one 8-byte and one 4-byte store.
+// One thread per 32 bases: two 16-byte loads, one 8-byte and one 4-byte store; the bytes are
+// processed four at a time inside 32-bit words.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack4_codes(uint32_t w) {
+    // byte i's code (bits 1-2 of the ASCII letter) moves to bits 2i..2i+1
+    const uint32_t x = (w >> 1) & 0x03030303u;
+    return (x | (x >> 6) | (x >> 12) | (x >> 18)) & 0xFFu;
+}
+__device__ __forceinline__ uint32_t pack4_valid(uint32_t w) {
+    // one bit per byte: ACGT in either case (upper-cased by clearing bit 5)
+    const uint32_t u = w & 0xDFDFDFDFu;
+    const uint32_t m = __vcmpeq4(u, 0x41414141u) | __vcmpeq4(u, 0x43434343u) | __vcmpeq4(u, 0x47474747u) |
+                       __vcmpeq4(u, 0x54545454u);
+    const uint32_t y = m & 0x01010101u;
+    return (y | (y >> 7) | (y >> 14) | (y >> 21)) & 0xFu;
+}
+
 __global__ void __launch_bounds__(256) pack_kernel(const uint8_t *__restrict__ text, uint64_t n, uint64_t n_words,
                                                    int aligned16, uint64_t *__restrict__ packed,
                                                    uint32_t *__restrict__ valid) {
     uint64_t wi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     for (; wi < n_words; wi += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t base = wi * 32;
-        uint8_t b[32];
+        uint32_t w[8];
         if (aligned16 && base + 32 <= n) {
-            uint4 a0 = reinterpret_cast<const uint4 *>(text + base)[0];
-            uint4 a1 = reinterpret_cast<const uint4 *>(text + base)[1];
-            const uint8_t *p0 = reinterpret_cast<const uint8_t *>(&a0);
-            const uint8_t *p1 = reinterpret_cast<const uint8_t *>(&a1);
-#pragma unroll
-            for (int i = 0; i < 16; i++) {
-                b[i] = p0[i];
-                b[16 + i] = p1[i];
-            }
+            const uint4 a0 = reinterpret_cast<const uint4 *>(text + base)[0];
+            const uint4 a1 = reinterpret_cast<const uint4 *>(text + base)[1];
+            w[0] = a0.x, w[1] = a0.y, w[2] = a0.z, w[3] = a0.w;
+            w[4] = a1.x, w[5] = a1.y, w[6] = a1.z, w[7] = a1.w;
         } else {
 #pragma unroll
-            for (int i = 0; i < 32; i++) b[i] = (base + i < n) ? text[base + i] : (uint8_t)'\n';
+            for (int j = 0; j < 8; j++) {
+                uint32_t x = 0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const uint64_t p = base + 4 * j + i;
+                    x |= (uint32_t)(p < n ? text[p] : (uint8_t)'\n') << (8 * i);
+                }
+                w[j] = x;
+            }
         }
         uint64_t pw = 0;
         uint32_t vw = 0;
 #pragma unroll
-        for (int i = 0; i < 32; i++) {
-            uint32_t c = b[i];
-            uint32_t u = c & 0xDFu;  // upper case
-            bool ok = (u == 'A') | (u == 'C') | (u == 'G') | (u == 'T');
-            pw |= (uint64_t)((c >> 1) & 3u) << (2 * i);
-            vw |= (uint32_t)ok << i;
+        for (int j = 0; j < 8; j++) {
+            pw |= (uint64_t)pack4_codes(w[j]) << (8 * j);
+            vw |= pack4_valid(w[j]) << (4 * j);
         }
         packed[wi] = pw;
         valid[wi] = vw;
@@ -388,7 +403,7 @@ __global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict_
                                                         const unsigned long long *__restrict__ ovf_cursor,
                                                         unsigned long long ovf_cap, int fbits,
                                                         const unsigned long long *__restrict__ bin_off,
-                                                        unsigned long long *__restrict__ bin_cursor,
+                                                        unsigned *__restrict__ bin_cursor,
                                                         SkRec *__restrict__ recs, unsigned *__restrict__ status) {
     uint64_t begin, end;
     if (blockIdx.x < n_regions) {
@@ -404,7 +419,7 @@ __global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict_
     for (uint64_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
         const SkRec r = stage[i];
         const uint64_t bin = ((uint64_t)rec_bucket(r) << fbits) | ((r.w1 >> 48) & 0xffffull);
-        const unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1ull);
+        const unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1u);
         if (slot >= bin_off[bin + 1]) {
             atomicOr(status, kStatusLookback);
             continue;
@@ -550,7 +565,7 @@ int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, 
 
 int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
                      const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
-                     const unsigned long long *bin_off, unsigned long long *bin_cursor, SkRec *recs, unsigned *status,
+                     const unsigned long long *bin_off, unsigned *bin_cursor, SkRec *recs, unsigned *status,
                      cudaStream_t s) {
     const uint64_t grid = (uint64_t)g.blocks + (ovf_cap + kOvfSlice - 1) / kOvfSlice;
     if (grid == 0) return 0;

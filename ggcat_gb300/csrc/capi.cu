@@ -102,7 +102,8 @@ struct ggcat_gpu_ctx {
     // bucketing
     DevBuf<uint64_t> packed;
     DevBuf<uint32_t> valid;
-    DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, bin_cursor, scan_tmp;
+    DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, scan_tmp;
+    DevBuf<unsigned> bin_cursor;  // records placed per sub-bin by the partition
     DevBuf<SkRec> recs, stage;
     DevBuf<unsigned long long> ovf_cursor, block_count;  // staging overflow cursor, records per region
     DevBuf<unsigned> status;
@@ -320,7 +321,7 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
         CK(ctx->stage.ensure((uint64_t)geo.blocks * geo.region_cap + ovf_cap));
         CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-        CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned), s));
         CK(cudaMemsetAsync(ctx->ovf_cursor.p, 0, sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
         ctx->launches += launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,

@@ -27,7 +27,7 @@ int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, 
                      unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s);
 int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
                      const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
-                     const unsigned long long *bin_off, unsigned long long *bin_cursor, SkRec *recs, unsigned *status,
+                     const unsigned long long *bin_off, unsigned *bin_cursor, SkRec *recs, unsigned *status,
                      cudaStream_t s);
 uint64_t scan_temp_elems(uint64_t n);
 // out has n+1 entries: exclusive prefix sums and the total at out[n]
