@@ -505,13 +505,14 @@ __global__ void __launch_bounds__(128) classify_units_kernel(
 //   S: many sub-bins packed per unit, hash table in shared memory; u64 keys: 512 threads,
 //      2 CTAs/SM (u128: 256 threads, 2 CTAs/SM);
 //   W: one sub-bin of up to 65536 (u128: 16384) instances, the largest shared-memory table;
-//      u64 keys: 1024 threads and 11264 slots, u128: 512 threads and 8192 slots, 1 CTA/SM; a
+//      u64 keys: 1024 threads and 11264 slots, u128: 1024 threads and 7936 slots, 1 CTA/SM; a
 //      unit whose distinct k-mers overflow the table moves to the M queue (with a reserved
 //      global table);
 //   M: table in the global pool (L2-resident), 512 threads, 2 CTAs/SM, shared memory for the
 //      list-ranking arrays of up to 2048 (u128: 1536) survivors.
 // The phases of a unit are separated by block barriers and bound by shared-memory latency, so
-// the u64 tiers run 32 warps per SM (the kernel fits 64 registers per thread).  S and W reuse
+// the u64 tiers and the u128 W tier run 32 warps per SM (the kernel fits 64 registers per
+// thread; u128 W keeps shared ranking arrays for 1024 survivors to make room for them).  S and W reuse
 // the table bytes for the list-ranking arrays once the successor phase is done (union).  Units
 // with more survivors than kSurv rank in the CTA's global scratch (extend_unit).
 enum : int { kTierS = 0, kTierW = 1, kTierM = 2 };
@@ -531,7 +532,7 @@ struct TierCfg<uint64_t, kTierW> {
 };
 template <>
 struct TierCfg<u128, kTierW> {
-    static constexpr int NT = 512, kSlots = 7936, kSurv = 2048, kMinBlocks = 1;
+    static constexpr int NT = 1024, kSlots = 7936, kSurv = 1024, kMinBlocks = 1;
 };
 template <>
 struct TierCfg<uint64_t, kTierM> {
