@@ -115,8 +115,8 @@ struct ggcat_gpu_ctx {
     const uint8_t *last_text = nullptr;  // device text of the last bucketize
 
     // colour phase
-    DevBuf<uint64_t> ckeys;
-    DevBuf<uint32_t> cvals, cbitmaps, cid_subset, cdump_subset, csub_state, csub_arena;
+    DevBuf<uint64_t> cslots;  // {key, id} pairs
+    DevBuf<uint32_t> cowner, cbitmaps, cid_subset, cdump_subset, csub_state, csub_arena;
     DevBuf<unsigned long long> csub_hash, ccounters;
     DevBuf<uint64_t> cseq_off;
     DevBuf<uint32_t> cseq_color;
@@ -1139,13 +1139,14 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(cudaSetDevice(ctx->device));
     ctx->have_colors = false;
     const uint64_t nd = ctx->n_kmers_out;
+    if (nd >= 0xffffffffull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "colours support < 2^32 k-mers");
     const int words = (int)((n_colors + 31) / 32);
     uint64_t cap = 1024;
     while (cap < 2 * nd + 64) cap <<= 1;
     uint64_t scap = 1024;
     while (scap < 2 * nd + 64) scap <<= 1;
-    CK(ctx->ckeys.ensure(cap));
-    CK(ctx->cvals.ensure(cap));
+    CK(ctx->cslots.ensure(2 * cap));
+    CK(ctx->cowner.ensure(nd + 1));
     CK(ctx->cbitmaps.ensure((nd + 1) * (uint64_t)words));
     CK(ctx->cid_subset.ensure(nd + 1));
     CK(ctx->cdump_subset.ensure(nd + 1));
@@ -1157,17 +1158,18 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(ctx->cseq_color.ensure(n_seq));
     CK(cudaMemcpyAsync(ctx->cseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->cseq_color.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(ctx->ckeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->cslots.p, 0xff, 2 * cap * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(ctx->cbitmaps.p, 0, (nd + 1) * words * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->csub_hash.p, 0, scap * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->csub_state.p, 0, scap * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->ccounters.p, 0, 4 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
     ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
-                                        ctx->cseq_off.p, ctx->cseq_color.p, n_seq, words, ctx->ckeys.p, ctx->cvals.p,
-                                        cap - 1, ctx->cbitmaps.p, ctx->ccounters.p, ctx->csub_hash.p,
-                                        ctx->csub_state.p, ctx->csub_arena.p, scap - 1, ctx->cid_subset.p,
-                                        ctx->cdump_subset.p, ctx->status.p + 1, nd, ctx->sms, s);
+                                        ctx->last_params.forward_only ? 0 : 1, ctx->cseq_off.p, ctx->cseq_color.p,
+                                        n_seq, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
+                                        ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p, ctx->csub_arena.p,
+                                        scap - 1, ctx->cid_subset.p, ctx->cdump_subset.p, ctx->status.p + 1,
+                                        ctx->sms, s);
     CK(cudaGetLastError());
     unsigned long long cnt[2];
     unsigned st = 0;
@@ -1176,7 +1178,7 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(cudaStreamSynchronize(s));
     if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "colour phase: internal error (status %u)", st);
     ctx->cmask = cap - 1;
-    ctx->c_n_ids = cnt[0];
+    ctx->c_n_ids = nd;  // ids are dump indices (holes for k-mers dumped twice)
     ctx->c_n_subsets = cnt[1];
     ctx->c_words = words;
     ctx->c_colors = n_colors;
@@ -1242,6 +1244,8 @@ extern "C" int ggcat_gpu_query_index(ggcat_gpu_ctx *ctx, const uint8_t *d_graph_
 extern "C" int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result to index");
+    if (ctx->last_params.forward_only)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
     ctx->qready = false;
@@ -1251,7 +1255,7 @@ extern "C" int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream) {
     CK(ctx->qvals.ensure(cap));
     CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
-    ctx->launches += launch_index_from_colors(ctx->ckeys.p, ctx->cvals.p, ctx->cmask + 1, ctx->cid_subset.p,
+    ctx->launches += launch_index_from_colors(ctx->cslots.p, ctx->cmask + 1, ctx->cid_subset.p,
                                               ctx->qkeys.p, ctx->qvals.p, cap - 1, ctx->status.p + 1, ctx->sms, s);
     CK(cudaGetLastError());
     unsigned st = 0;

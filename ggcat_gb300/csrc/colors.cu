@@ -12,71 +12,99 @@
 //   3. every bitmap is deduplicated into a subset table (exact: hash, then compare).
 // Subset ids are assigned in arrival order (as in the reference they are not deterministic);
 // the sets they decode to are.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace ggcat {
 
 __device__ __forceinline__ uint64_t cslot(uint64_t key, uint64_t mask) { return mix64(key) & mask; }
 
-// 1a. insert the dumped survivors (duplicates across sub-buckets collapse)
-__global__ void color_kmer_insert_kernel(const uint64_t *__restrict__ kmers, uint64_t n, uint64_t *keys,
-                                         uint32_t *vals, uint64_t mask, unsigned *status) {
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// The k-mer table: 16-byte slots {key, id}, empty = all-ones in both words.  A k-mer's id is
+// the dump index of the thread that inserted it (its owner), claimed together with the key by
+// one 128-bit compare-and-swap, so a lookup reads one slot and no numbering pass is needed;
+// ids of duplicate dump entries are holes whose colour bitmap stays empty.
+__device__ __forceinline__ void cas_slot(uint64_t *slot, uint64_t cmp_key, uint64_t cmp_id, uint64_t key, uint64_t id,
+                                         uint64_t &old_key, uint64_t &old_id) {
+    asm volatile(
+        "{\n\t.reg .b128 c, v, d;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 v, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], c, v;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(old_key), "=l"(old_id)
+        : "l"(cmp_key), "l"(cmp_id), "l"(key), "l"(id), "l"(slot)
+        : "memory");
+}
+
+// 1. insert the dumped survivors; owner[i] = id of dump entry i's k-mer (i itself unless the
+//    k-mer was dumped twice)
+__global__ void color_kmer_insert_kernel(const uint64_t *__restrict__ kmers, uint64_t n, uint64_t *slots,
+                                         uint64_t mask, uint32_t *owner, unsigned *status) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = kmers[i];
         uint64_t s = cslot(key, mask);
-        for (uint64_t probe = 0;; probe++) {
-            if (probe > mask) {
-                atomicOr(status, kStatusTableFull);
-                break;
-            }
-            const uint64_t kk = keys[s];
-            if (kk == key) break;
-            if (kk == kEmptyKey) {
-                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
-                                                         (unsigned long long)kEmptyKey, (unsigned long long)key);
-                if (old == kEmptyKey || old == key) break;
+        uint64_t own = kEmptyKey;
+        for (uint64_t probe = 0; probe <= mask; probe++) {
+            const uint64_t kk = slots[2 * s];
+            if (kk == key || kk == kEmptyKey) {
+                // a failed compare returns the slot atomically: for kk == key this is a read of
+                // the owner's {key, id} pair
+                uint64_t ok, oid;
+                cas_slot(slots + 2 * s, kEmptyKey, kEmptyKey, key, i, ok, oid);
+                if (ok == kEmptyKey) {
+                    own = i;
+                    break;
+                }
+                if (ok == key) {
+                    own = oid;
+                    break;
+                }
             }
             s = (s + 1) & mask;
         }
+        if (own == kEmptyKey) atomicOr(status, kStatusTableFull);
+        owner[i] = (uint32_t)own;
     }
 }
 
-// 1b. dense ids for the occupied slots (warp-aggregated counter)
-__global__ void color_kmer_number_kernel(const uint64_t *__restrict__ keys, uint32_t *vals, uint64_t cap,
-                                         unsigned long long *counter) {
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < cap; base += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t s = base + threadIdx.x;
-        const bool occ = s < cap && keys[s] != kEmptyKey;
-        const unsigned bm = __ballot_sync(0xffffffffu, occ);
-        const int lane = threadIdx.x & 31;
-        unsigned long long b = 0;
-        if (lane == 0 && bm) b = atomicAdd(counter, (unsigned long long)__popc(bm));
-        b = __shfl_sync(0xffffffffu, b, 0);
-        if (occ) vals[s] = (uint32_t)(b + __popc(bm & ((1u << lane) - 1u)));
-    }
-}
-
-__device__ __forceinline__ int64_t color_find(const uint64_t *keys, uint64_t mask, uint64_t key) {
+// id of `key` or -1; the table is read-only while this runs
+__device__ __forceinline__ int64_t color_find(const uint64_t *__restrict__ slots, uint64_t mask, uint64_t key) {
     uint64_t s = cslot(key, mask);
     for (uint64_t probe = 0; probe <= mask; probe++) {
-        const uint64_t kk = keys[s];
-        if (kk == key) return (int64_t)s;
-        if (kk == kEmptyKey) return -1;
+        const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2 *>(slots) + s);
+        if (e.x == key) return (int64_t)e.y;
+        if (e.x == kEmptyKey) return -1;
         s = (s + 1) & mask;
     }
     return -1;
 }
 
 // 2. occurrences: every k-mer of the text sets its sequence's colour bit
+constexpr uint64_t kOccMaxRows = 65536;
 __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
-                                                       uint64_t chunk, const uint64_t *__restrict__ seq_off,
+                                                       int canonical, uint64_t chunk,
+                                                       const uint64_t *__restrict__ seq_off,
                                                        const uint32_t *__restrict__ seq_color, uint64_t n_seq,
-                                                       const uint64_t *__restrict__ keys,
-                                                       const uint32_t *__restrict__ vals, uint64_t mask,
-                                                       uint32_t *bitmaps, int words) {
+                                                       const uint64_t *__restrict__ slots, uint64_t mask,
+                                                       uint32_t *bitmaps, int words, uint64_t rows,
+                                                       uint64_t row_chunks) {
+    // chunk order: the text is viewed as `rows` rows of `row_chunks` chunks and walked column
+    // by column, so that with one row per sequence chunk c of every sequence is in flight at
+    // once -- related genomes then touch the same table slots and bitmaps while they are in L2
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t x0 = tid * chunk;
+    const uint64_t column = tid / rows;
+    if (column >= row_chunks) return;
+    const uint64_t x0 = ((tid - column * rows) * row_chunks + column) * chunk;
     if (x0 >= n) return;
     const uint64_t x1 = min(x0 + chunk, n);
     uint64_t lo = 0, hi = n_seq - 1;  // sequence containing x0
@@ -85,26 +113,51 @@ __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restric
         if (seq_off[mid] <= x0) lo = mid; else hi = mid - 1;
     }
     uint64_t seq = lo;
+    uint64_t next_off = seq + 1 < n_seq ? seq_off[seq + 1] : ~0ull;
+    uint32_t col = seq_color[seq];
     const uint64_t kmask = kmer_mask(k);
     uint64_t fw = 0, rc = 0, run = 0;
     const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
-    for (uint64_t p = x0; p < pend; p++) {
-        const uint32_t c = text[p];
-        const uint32_t u = c & 0xDFu;
-        if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
-            run = 0;
-            continue;
+    // the text is read 16 bytes per load into registers (x0 is a multiple of the chunk): one
+    // byte per load would refetch each sector from DRAM, as the table traffic evicts it
+    const bool vec = (reinterpret_cast<uintptr_t>(text) & 15u) == 0;
+    for (uint64_t q = x0; q < pend;) {
+        uint64_t wlo, whi;
+        int nb;
+        if (vec && q + 16 <= n) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(text + q));
+            wlo = (uint64_t)v.x | ((uint64_t)v.y << 32);
+            whi = (uint64_t)v.z | ((uint64_t)v.w << 32);
+            nb = pend - q < 16 ? (int)(pend - q) : 16;
+        } else {
+            wlo = text[q];
+            whi = 0;
+            nb = 1;
         }
-        const uint64_t b = (c >> 1) & 3u;
-        fw = (fw >> 2) | (b << (2 * (k - 1)));
-        rc = ((rc << 2) | (b ^ 2u)) & kmask;
-        if (++run < (uint64_t)k) continue;
-        const uint64_t start = p + 1 - (uint64_t)k;
-        while (seq + 1 < n_seq && seq_off[seq + 1] <= start) seq++;
-        const int64_t s = color_find(keys, mask, fw < rc ? fw : rc);
-        if (s < 0) continue;  // not a surviving k-mer
-        const uint32_t col = seq_color[seq];
-        atomicOr(&bitmaps[(uint64_t)vals[s] * words + (col >> 5)], 1u << (col & 31));
+        for (int j = 0; j < nb; j++) {
+            const uint32_t c = (uint32_t)(wlo & 0xffu);
+            wlo = (wlo >> 8) | (whi << 56);
+            whi >>= 8;
+            const uint32_t u = c & 0xDFu;
+            if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                run = 0;
+                continue;
+            }
+            const uint64_t b = (c >> 1) & 3u;
+            fw = (fw >> 2) | (b << (2 * (k - 1)));
+            rc = ((rc << 2) | (b ^ 2u)) & kmask;
+            if (++run < (uint64_t)k) continue;
+            const uint64_t start = q + j + 1 - (uint64_t)k;
+            while (start >= next_off) {
+                seq++;
+                next_off = seq + 1 < n_seq ? seq_off[seq + 1] : ~0ull;
+                col = seq_color[seq];
+            }
+            const int64_t id = color_find(slots, mask, (canonical && rc < fw) ? rc : fw);
+            if (id < 0) continue;  // not a surviving k-mer
+            atomicOr(&bitmaps[(uint64_t)id * words + (col >> 5)], 1u << (col & 31));
+        }
+        q += nb;
     }
 }
 
@@ -117,14 +170,20 @@ __device__ __forceinline__ uint64_t bitmap_hash(const uint32_t *bm, int words) {
 // 3. subset dedup: a subset slot holds (hash, state) and its bitmap in the arena; the
 //    inserting thread publishes the bitmap before the ready flag, readers wait (bounded)
 //    for ready and compare the whole bitmap, so equal hashes of different sets stay apart.
-__global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, const unsigned long long *n_ids_dev, int words,
+//    Ids with an empty bitmap are holes (see the k-mer table) and get no subset.
+__global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, uint64_t n_ids, int words,
                                     unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena,
                                     uint64_t sub_mask, unsigned long long *sub_count, uint32_t *id_subset,
                                     unsigned *status) {
-    const uint64_t n_ids = *n_ids_dev;
     for (uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; id < n_ids;
          id += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t *bm = bitmaps + id * words;
+        uint32_t any = 0;
+        for (int w = 0; w < words; w++) any |= bm[w];
+        if (!any) {
+            id_subset[id] = 0xffffffffu;
+            continue;
+        }
         const uint64_t h = bitmap_hash(bm, words);
         uint64_t s = h & sub_mask;
         uint32_t result = 0xffffffffu;
@@ -133,8 +192,12 @@ __global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, const 
             if (cur == 0ull) {
                 cur = atomicCAS(&sub_hash[s], 0ull, (unsigned long long)h);
                 if (cur == 0ull) {
-                    // claimed: a new id, its bitmap in the arena, then the ready flag
-                    const unsigned long long sid = atomicAdd(sub_count, 1ull);
+                    // claimed: a new id (one counter atomic for the threads claiming together),
+                    // its bitmap in the arena, then the ready flag
+                    const cg::coalesced_group g = cg::coalesced_threads();
+                    unsigned long long base = 0;
+                    if (g.thread_rank() == 0) base = atomicAdd(sub_count, (unsigned long long)g.size());
+                    const unsigned long long sid = g.shfl(base, 0) + g.thread_rank();
                     for (int w = 0; w < words; w++) sub_arena[sid * words + w] = bm[w];
                     __threadfence();
                     atomicExch(&sub_state[s], (uint32_t)sid | 0x80000000u);
@@ -143,17 +206,17 @@ __global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, const 
                 }
             }
             if (cur == h) {
-                uint32_t st = 0;
-                for (int spin = 0; spin < (1 << 22); spin++) {
-                    st = atomicAdd(&sub_state[s], 0u);
-                    if (st & 0x80000000u) break;
+                // acquire load, not an atomic: the popular subsets (one colour, all colours) are
+                // polled by millions of threads, and same-address atomics serialise in L2
+                uint32_t st = ld_acquire_u32(&sub_state[s]);
+                for (int spin = 0; !(st & 0x80000000u) && spin < (1 << 22); spin++) {
                     __nanosleep(32);
+                    st = ld_acquire_u32(&sub_state[s]);
                 }
                 if (!(st & 0x80000000u)) {
                     atomicOr(status, kStatusWalkLimit);  // the waited-for publisher never finished
                     break;
                 }
-                __threadfence();
                 const uint64_t sid = st & 0x7fffffffu;
                 bool same = true;
                 for (int w = 0; w < words && same; w++) same = sub_arena[sid * words + w] == bm[w];
@@ -169,83 +232,44 @@ __global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, const 
     }
 }
 
-// subset id of every dumped k-mer
-__global__ void color_dump_subsets_kernel(const uint64_t *__restrict__ kmers, uint64_t n,
-                                          const uint64_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                                          uint64_t mask, const uint32_t *__restrict__ id_subset, uint32_t *out) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const int64_t s = color_find(keys, mask, kmers[i]);
-        out[i] = s < 0 ? 0xffffffffu : id_subset[vals[s]];
-    }
-}
-
-// per k-mer start position of a text (e.g. the final unitigs): subset id or ~0
-__global__ void __launch_bounds__(256) color_text_subsets_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
-                                                                uint64_t chunk, const uint64_t *__restrict__ keys,
-                                                                const uint32_t *__restrict__ vals, uint64_t mask,
-                                                                const uint32_t *__restrict__ id_subset,
-                                                                uint32_t *out) {
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t x0 = tid * chunk;
-    if (x0 >= n) return;
-    const uint64_t x1 = min(x0 + chunk, n);
-    const uint64_t kmask = kmer_mask(k);
-    uint64_t fw = 0, rc = 0, run = 0;
-    for (uint64_t p = x0; p < x1; p++) out[p] = 0xffffffffu;
-    const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
-    for (uint64_t p = x0; p < pend; p++) {
-        const uint32_t c = text[p];
-        const uint32_t u = c & 0xDFu;
-        if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
-            run = 0;
-            continue;
-        }
-        const uint64_t b = (c >> 1) & 3u;
-        fw = (fw >> 2) | (b << (2 * (k - 1)));
-        rc = ((rc << 2) | (b ^ 2u)) & kmask;
-        if (++run < (uint64_t)k) continue;
-        const uint64_t start = p + 1 - (uint64_t)k;
-        const int64_t s = color_find(keys, mask, fw < rc ? fw : rc);
-        out[start] = s < 0 ? 0xffffffffu : id_subset[vals[s]];
-    }
+// subset id of every dumped k-mer: a gather through its owner (almost always itself)
+__global__ void color_dump_subsets_kernel(const uint32_t *__restrict__ owner, uint64_t n,
+                                          const uint32_t *__restrict__ id_subset, uint32_t *out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = id_subset[owner[i]];
 }
 
 // ---------------------------------------------------------------------------
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
-                       const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words, uint64_t *keys,
-                       uint32_t *vals, uint64_t mask, uint32_t *bitmaps, unsigned long long *counters,
-                       unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena, uint64_t sub_mask,
-                       uint32_t *id_subset, uint32_t *dump_subset, unsigned *status, uint64_t n_ids_upper, int sms,
-                       cudaStream_t s) {
+                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words,
+                       uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
+                       unsigned long long *sub_count, unsigned long long *sub_hash, uint32_t *sub_state,
+                       uint32_t *sub_arena, uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset,
+                       unsigned *status, int sms, cudaStream_t s) {
     int n = 0;
-    color_kmer_insert_kernel<<<sms * 8, 256, 0, s>>>(dump, n_dump, keys, vals, mask, status);
-    n++;
-    color_kmer_number_kernel<<<sms * 8, 256, 0, s>>>(keys, vals, mask + 1, counters);
-    n++;
-    const uint64_t chunk = 256;
-    const uint64_t threads = (n_text + chunk - 1) / chunk;
-    if (threads) {
-        color_occ_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n_text, k, chunk, seq_off, seq_color,
-                                                                          n_seq, keys, vals, mask, bitmaps, words);
+    if (n_dump) {
+        color_kmer_insert_kernel<<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
         n++;
     }
-    (void)n_ids_upper;
-    color_subset_kernel<<<sms * 8, 256, 0, s>>>(bitmaps, counters, words, sub_hash, sub_state, sub_arena, sub_mask,
-                                                counters + 1, id_subset, status);
-    n++;
-    color_dump_subsets_kernel<<<sms * 8, 256, 0, s>>>(dump, n_dump, keys, vals, mask, id_subset, dump_subset);
-    n++;
-    return n;
-}
-
-int launch_color_text_subsets(const uint8_t *text, uint64_t n, int k, const uint64_t *keys, const uint32_t *vals,
-                              uint64_t mask, const uint32_t *id_subset, uint32_t *out, cudaStream_t s) {
     const uint64_t chunk = 256;
-    const uint64_t threads = (n + chunk - 1) / chunk;
-    if (!threads) return 0;
-    color_text_subsets_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n, k, chunk, keys, vals, mask,
-                                                                               id_subset, out);
-    return 1;
+    const uint64_t chunks = (n_text + chunk - 1) / chunk;
+    if (chunks && n_dump) {
+        // one row per sequence for collections of genomes; read sets keep text order
+        const uint64_t rows = std::max<uint64_t>(1, std::min<uint64_t>(n_seq <= kOccMaxRows ? n_seq : 1, chunks));
+        const uint64_t row_chunks = (chunks + rows - 1) / rows;
+        const uint64_t threads = rows * row_chunks;
+        color_occ_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n_text, k, canonical, chunk, seq_off,
+                                                                          seq_color, n_seq, slots, mask, bitmaps,
+                                                                          words, rows, row_chunks);
+        n++;
+    }
+    if (n_dump) {
+        color_subset_kernel<<<sms * 8, 256, 0, s>>>(bitmaps, n_dump, words, sub_hash, sub_state, sub_arena, sub_mask,
+                                                    sub_count, id_subset, status);
+        color_dump_subsets_kernel<<<sms * 8, 256, 0, s>>>(owner, n_dump, id_subset, dump_subset);
+        n += 2;
+    }
+    return n;
 }
 
 }  // namespace ggcat

@@ -134,8 +134,9 @@ int merge_ctas_per_sm(int tier, int wide);
 // uncoloured index keys: u64 for k <= 32, u128 (16-byte aligned) for k <= 64
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
                         unsigned *status, cudaStream_t s);
-int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint64_t ccap, const uint32_t *id_subset,
-                             uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s);
+// cslots: the colour phase's {key, id} table of ccap slots
+int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset, uint64_t *keys,
+                             uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s);
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
                  const uint32_t *item_len, uint64_t n_items, const void *keys, uint64_t mask,
                  unsigned long long *matched, cudaStream_t s);
@@ -175,13 +176,13 @@ int launch_link_write(const uint8_t *bases, const uint64_t *off, const uint32_t 
 int launch_kmer_hash(const uint8_t *text, uint64_t n, int k, int kind, uint64_t *out, cudaStream_t s);
 
 // colors.cu
+// slots: 2 x (mask + 1) words ({key, id} pairs, all-ones when empty); owner, id_subset,
+// dump_subset: n_dump entries; bitmaps: n_dump x words (zeroed)
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
-                       const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words, uint64_t *keys,
-                       uint32_t *vals, uint64_t mask, uint32_t *bitmaps, unsigned long long *counters,
-                       unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena, uint64_t sub_mask,
-                       uint32_t *id_subset, uint32_t *dump_subset, unsigned *status, uint64_t n_ids_upper, int sms,
-                       cudaStream_t s);
-int launch_color_text_subsets(const uint8_t *text, uint64_t n, int k, const uint64_t *keys, const uint32_t *vals,
-                              uint64_t mask, const uint32_t *id_subset, uint32_t *out, cudaStream_t s);
+                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words,
+                       uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
+                       unsigned long long *sub_count, unsigned long long *sub_hash, uint32_t *sub_state,
+                       uint32_t *sub_arena, uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset,
+                       unsigned *status, int sms, cudaStream_t s);
 
 }  // namespace ggcat

@@ -67,13 +67,14 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
     }
 }
 
-// Coloured index: the colour phase's k-mer table (key -> dense id) re-keyed into the query
+// Coloured index: the colour phase's k-mer table ({key, id} slots) re-keyed into the query
 // table with value = colour subset id.
-__global__ void index_from_colors_kernel(const uint64_t *__restrict__ ckeys, const uint32_t *__restrict__ cvals,
-                                         uint64_t ccap, const uint32_t *__restrict__ id_subset, uint64_t *keys,
-                                         uint32_t *vals, uint64_t mask, unsigned *status) {
+__global__ void index_from_colors_kernel(const uint64_t *__restrict__ cslots, uint64_t ccap,
+                                         const uint32_t *__restrict__ id_subset, uint64_t *keys, uint32_t *vals,
+                                         uint64_t mask, unsigned *status) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ccap; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t key = ckeys[i];
+        const ulonglong2 e = reinterpret_cast<const ulonglong2 *>(cslots)[i];
+        const uint64_t key = e.x;
         if (key == kEmptyKey) continue;
         uint64_t s = qslot(key, mask);
         for (uint64_t probe = 0;; probe++) {
@@ -85,7 +86,7 @@ __global__ void index_from_colors_kernel(const uint64_t *__restrict__ ckeys, con
                 const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
                                                          (unsigned long long)kEmptyKey, (unsigned long long)key);
                 if (old == kEmptyKey) {
-                    vals[s] = id_subset[cvals[i]];
+                    vals[s] = id_subset[(uint32_t)e.y];
                     break;
                 }
             }
@@ -236,9 +237,9 @@ int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint
     return 1;
 }
 
-int launch_index_from_colors(const uint64_t *ckeys, const uint32_t *cvals, uint64_t ccap, const uint32_t *id_subset,
+int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset,
                              uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s) {
-    index_from_colors_kernel<<<sms * 8, 256, 0, s>>>(ckeys, cvals, ccap, id_subset, keys, vals, mask, status);
+    index_from_colors_kernel<<<sms * 8, 256, 0, s>>>(cslots, ccap, id_subset, keys, vals, mask, status);
     return 1;
 }
 
