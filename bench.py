@@ -63,6 +63,9 @@ def _args():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the 3-genome and long-k build measurements")
     ap.add_argument("--query-rate", type=float, default=20000.0, help="Poisson arrival rate (queries/s)")
+    ap.add_argument("--colored-only", action="store_true",
+                    help="run only the coloured build + query section and print its JSON object "
+                         "(a small case for profiling the colour kernels: --colors 64 --colored-queries 1000)")
     return ap.parse_args()
 
 
@@ -610,8 +613,24 @@ def run_gpu(args):
     return 0
 
 
+def run_colored_only(args):
+    import torch
+
+    from ggcat_gb300 import _native
+
+    torch.cuda.set_device(0)
+    ctx = _native.GpuContext(0)
+    try:
+        print(json.dumps({"section": "colored", **colored_bench(args, ctx, torch, 0)}), flush=True)
+    finally:
+        ctx.close()
+    return 0
+
+
 def main():
     args = _args()
+    if args.colored_only:
+        return run_colored_only(args)
     if args.workload != "skewed":
         args.no_query = True  # the query and coloured sections use k=31 graphs
         args.no_colored = True

@@ -1130,10 +1130,15 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     if (!h_seq_off || !h_seq_color || n_seq == 0 || n_colors == 0 || n_colors > 65536)
         return fail(ctx, GGCAT_GPU_EINVAL, "bad colour table (n_seq=%llu, n_colors=%u)", (unsigned long long)n_seq,
                     n_colors);
+    uint64_t max_len = 0;
     for (uint64_t i = 0; i < n_seq; i++) {
         if (h_seq_color[i] >= n_colors) return fail(ctx, GGCAT_GPU_EINVAL, "colour out of range at sequence %llu",
                                                     (unsigned long long)i);
         if (i && h_seq_off[i] < h_seq_off[i - 1]) return fail(ctx, GGCAT_GPU_EINVAL, "sequence offsets not sorted");
+        const uint64_t end = i + 1 < n_seq ? h_seq_off[i + 1] : ctx->n_text;
+        if (end < h_seq_off[i] || end > ctx->n_text)
+            return fail(ctx, GGCAT_GPU_EINVAL, "sequence %llu outside the text", (unsigned long long)i);
+        max_len = std::max<uint64_t>(max_len, end - h_seq_off[i]);
     }
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
@@ -1166,7 +1171,7 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
     ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
                                         ctx->last_params.forward_only ? 0 : 1, ctx->cseq_off.p, ctx->cseq_color.p,
-                                        n_seq, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
+                                        n_seq, h_seq_off[0] == 0 ? max_len : 0, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
                                         ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p, ctx->csub_arena.p,
                                         scap - 1, ctx->cid_subset.p, ctx->cdump_subset.p, ctx->status.p + 1,
                                         ctx->sms, s);

@@ -97,34 +97,44 @@ __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restric
                                                        const uint32_t *__restrict__ seq_color, uint64_t n_seq,
                                                        const uint64_t *__restrict__ slots, uint64_t mask,
                                                        uint32_t *bitmaps, int words, uint64_t rows,
-                                                       uint64_t row_chunks) {
-    // chunk order: the text is viewed as `rows` rows of `row_chunks` chunks and walked column
-    // by column, so that with one row per sequence chunk c of every sequence is in flight at
-    // once -- related genomes then touch the same table slots and bitmaps while they are in L2
+                                                       uint64_t row_chunks, int seq_rows) {
+    // chunk order: `rows` rows of `row_chunks` chunks walked column by column.  With one row per
+    // sequence (seq_rows: row r = sequence r from its first base) chunk c of every sequence is
+    // in flight at once, so related genomes touch the same table slots and bitmaps while those
+    // are in L2; otherwise the rows are equal slices of the text.
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t column = tid / rows;
     if (column >= row_chunks) return;
-    const uint64_t x0 = ((tid - column * rows) * row_chunks + column) * chunk;
-    if (x0 >= n) return;
-    const uint64_t x1 = min(x0 + chunk, n);
-    uint64_t lo = 0, hi = n_seq - 1;  // sequence containing x0
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi + 1) >> 1;
-        if (seq_off[mid] <= x0) lo = mid; else hi = mid - 1;
+    const uint64_t row = tid - column * rows;
+    uint64_t x0, x1, seq;
+    if (seq_rows) {
+        const uint64_t end = row + 1 < n_seq ? seq_off[row + 1] : n;
+        x0 = seq_off[row] + column * chunk;
+        if (x0 >= end) return;
+        x1 = min(x0 + chunk, end);
+        seq = row;
+    } else {
+        x0 = (row * row_chunks + column) * chunk;
+        if (x0 >= n) return;
+        x1 = min(x0 + chunk, n);
+        uint64_t lo = 0, hi = n_seq - 1;  // sequence containing x0
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi + 1) >> 1;
+            if (seq_off[mid] <= x0) lo = mid; else hi = mid - 1;
+        }
+        seq = lo;
     }
-    uint64_t seq = lo;
     uint64_t next_off = seq + 1 < n_seq ? seq_off[seq + 1] : ~0ull;
     uint32_t col = seq_color[seq];
     const uint64_t kmask = kmer_mask(k);
     uint64_t fw = 0, rc = 0, run = 0;
     const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
-    // the text is read 16 bytes per load into registers (x0 is a multiple of the chunk): one
-    // byte per load would refetch each sector from DRAM, as the table traffic evicts it
-    const bool vec = (reinterpret_cast<uintptr_t>(text) & 15u) == 0;
+    // the text is read 16 bytes per aligned load into registers: one byte per load would
+    // refetch each sector from DRAM, as the table traffic evicts it
     for (uint64_t q = x0; q < pend;) {
         uint64_t wlo, whi;
         int nb;
-        if (vec && q + 16 <= n) {
+        if (((reinterpret_cast<uintptr_t>(text) + q) & 15u) == 0 && q + 16 <= n) {
             const uint4 v = __ldg(reinterpret_cast<const uint4 *>(text + q));
             wlo = (uint64_t)v.x | ((uint64_t)v.y << 32);
             whi = (uint64_t)v.z | ((uint64_t)v.w << 32);
@@ -241,8 +251,8 @@ __global__ void color_dump_subsets_kernel(const uint32_t *__restrict__ owner, ui
 
 // ---------------------------------------------------------------------------
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
-                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq, int words,
-                       uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
+                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq,
+                       uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
                        unsigned long long *sub_count, unsigned long long *sub_hash, uint32_t *sub_state,
                        uint32_t *sub_arena, uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset,
                        unsigned *status, int sms, cudaStream_t s) {
@@ -254,13 +264,18 @@ int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *tex
     const uint64_t chunk = 256;
     const uint64_t chunks = (n_text + chunk - 1) / chunk;
     if (chunks && n_dump) {
-        // one row per sequence for collections of genomes; read sets keep text order
-        const uint64_t rows = std::max<uint64_t>(1, std::min<uint64_t>(n_seq <= kOccMaxRows ? n_seq : 1, chunks));
-        const uint64_t row_chunks = (chunks + rows - 1) / rows;
+        // collections of genomes: one row per sequence, from its first base, when the lengths
+        // are alike (rows x the longest sequence's chunks <= 2 x the text's chunks); else equal
+        // slices of the text, one per sequence; read sets (many sequences) keep text order
+        const uint64_t max_chunks = (max_seq_len + chunk - 1) / chunk;
+        const int seq_rows = max_seq_len > 0 && n_seq <= kOccMaxRows && n_seq * max_chunks <= 2 * chunks;
+        const uint64_t rows =
+            seq_rows ? n_seq : std::max<uint64_t>(1, std::min<uint64_t>(n_seq <= kOccMaxRows ? n_seq : 1, chunks));
+        const uint64_t row_chunks = seq_rows ? max_chunks : (chunks + rows - 1) / rows;
         const uint64_t threads = rows * row_chunks;
         color_occ_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n_text, k, canonical, chunk, seq_off,
                                                                           seq_color, n_seq, slots, mask, bitmaps,
-                                                                          words, rows, row_chunks);
+                                                                          words, rows, row_chunks, seq_rows);
         n++;
     }
     if (n_dump) {

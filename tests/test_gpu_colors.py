@@ -100,3 +100,40 @@ def test_colored_serving_matches_direct_batch(built):
     assert (res.matched == em).all()
     assert (res.color_totals == epc.sum(axis=1)).all()
     assert res.batches > 1
+
+
+def _check_color_sets(ctx, r):
+    keys, _ = ctx.kmers()
+    subs = ctx.kmer_subsets()
+    decoded = [_decode(row) for row in ctx.subsets()]
+    assert len(set(decoded)) == len(decoded)
+    got = {}
+    for kk, sid in zip(keys.tolist(), subs.tolist()):
+        assert got.get(kk, decoded[sid]) == decoded[sid]
+        got[kk] = decoded[sid]
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    assert got == {int(lo[i]): tuple(int(c) for c in ccol[coff[i]:coff[i + 1]]) for i in range(len(lo))}
+
+
+@pytest.mark.parametrize("n_reads,read_len,colors", [(300, 150, 5), (70_000, 60, 4)])
+def test_color_sets_mixed_lengths_and_read_sets(n_reads, read_len, colors):
+    """The occurrence pass's other chunk orders: a genome beside short reads (rows are equal
+    slices of the text) and more sequences than it keeps rows for (text order)."""
+    rng = np.random.default_rng(n_reads)
+    g = synth.random_genome(200_000, rng)
+    reads = synth.sample_reads(g, n_reads, read_len, 0.002, 0.0, rng)
+    seqs = [g] + list(reads)
+    cols = [0] + [1 + i % (colors - 1) for i in range(n_reads)]
+    text, off, ln, col = synth.pack_sequences(seqs, cols)
+    ctx = _native.GpuContext(0)
+    try:
+        p = _native.make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=1, keep_kmers=True)
+        ctx.build_text(text, p)
+        ctx.colors(off, col, colors)
+        r = oracle.build_graph(text, off, ln, oracle.params(k=31, m=10, bucket_bits=6, second_bits=2, threads=4,
+                                                             colors=True), seq_colors=col)
+        _check_color_sets(ctx, r)
+    finally:
+        ctx.close()
+
