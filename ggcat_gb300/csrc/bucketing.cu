@@ -12,6 +12,8 @@
 // and a block-decomposed window minimum; the superkmers whose split point falls in the
 // chunk are appended as 16-byte records to a staging array and counted per sub-bin in
 // the same pass, and partition_kernel scatters them by sub-bin after an exclusive scan.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(256, 3)
                      unsigned long long *__restrict__ bin_count, unsigned long long *__restrict__ bin_kmers,
                      SkRec *__restrict__ stage, uint32_t region_cap, unsigned long long *__restrict__ block_count,
                      unsigned long long ovf_cap, unsigned long long *__restrict__ ovf_cursor,
-                     unsigned *__restrict__ status) {
+                     unsigned *__restrict__ status, uint32_t block_base, uint32_t total_blocks) {
     __shared__ NtPair t_out[4], t_in[4];
     __shared__ unsigned s_cnt;
     extern __shared__ __align__(16) uint8_t bk_smem[];
@@ -171,13 +173,15 @@ __global__ void __launch_bounds__(256, 3)
     const uint32_t bmask = (1u << bbits) - 1, smask = (1u << sbits) - 1, fmask = (1u << fbits) - 1;
     const uint64_t n_words = (n + 31) >> 5;
     const int lane = (int)(threadIdx.x & 31);
-    const uint64_t region = (uint64_t)blockIdx.x * region_cap;
+    // this launch covers blocks [block_base, block_base + gridDim.x) of total_blocks
+    const uint64_t bid = (uint64_t)blockIdx.x + block_base;
+    const uint64_t region = bid * region_cap;
     uint64_t *my_v = blk_v + threadIdx.x;
     uint8_t *my_m = blk_m + threadIdx.x;
     uint4 *my_q = que + threadIdx.x;
     const uint32_t top_sh = 2u * (uint32_t)(m - 1);
 
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t tid = bid * blockDim.x + threadIdx.x;
     const uint64_t x0 = tid * chunk;
     int qlen = 0;     // superkmers waiting in this lane's queue
     uint64_t xb = 0;  // first base of the current attempt (queue positions are relative to it)
@@ -231,7 +235,7 @@ __global__ void __launch_bounds__(256, 3)
                 } else {
                     const unsigned long long oi = atomicAdd(ovf_cursor, 1ull);
                     if (oi < ovf_cap)
-                        stage[(uint64_t)gridDim.x * region_cap + oi] = rec;
+                        stage[(uint64_t)total_blocks * region_cap + oi] = rec;
                     else
                         atomicOr(status, kStatusStageOverflow);
                 }
@@ -389,7 +393,7 @@ __global__ void __launch_bounds__(256, 3)
         if (!done) atomicOr(status, kStatusLookback);
     }
     __syncthreads();
-    if (threadIdx.x == 0) block_count[blockIdx.x] = min(s_cnt, region_cap);
+    if (threadIdx.x == 0) block_count[bid] = min(s_cnt, region_cap);
 }
 
 // Scatter of the staged records into their sub-bin ranges (the device radix partition).
@@ -550,16 +554,19 @@ BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m) {
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
                      int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
                      unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
-                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s) {
-    if (g.blocks == 0) return 0;
+                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, uint32_t block_base,
+                     uint32_t n_blocks, cudaStream_t s) {
+    if (block_base >= g.blocks) return 0;
+    n_blocks = std::min(n_blocks, g.blocks - block_base);
+    if (n_blocks == 0) return 0;
     if (m > 16)
-        bucketize_kernel<true><<<g.blocks, g.threads_per_block, g.smem, s>>>(
+        bucketize_kernel<true><<<n_blocks, g.threads_per_block, g.smem, s>>>(
             packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
-            g.region_cap, block_count, ovf_cap, ovf_cursor, status);
+            g.region_cap, block_count, ovf_cap, ovf_cursor, status, block_base, g.blocks);
     else
-        bucketize_kernel<false><<<g.blocks, g.threads_per_block, g.smem, s>>>(
+        bucketize_kernel<false><<<n_blocks, g.threads_per_block, g.smem, s>>>(
             packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
-            g.region_cap, block_count, ovf_cap, ovf_cursor, status);
+            g.region_cap, block_count, ovf_cap, ovf_cursor, status, block_base, g.blocks);
     return 1;
 }
 

@@ -38,6 +38,8 @@ struct DevBuf {
     }
 };
 
+constexpr int kFeedPieces = 4;  // pieces of build_text's pipelined host text copy
+
 struct PinnedBuf {
     uint8_t *p = nullptr;
     size_t n = 0;
@@ -55,11 +57,45 @@ struct PinnedBuf {
     }
 };
 
+// Host array in pinned memory for device results: it only grows (with 1/8 headroom) and
+// resize() leaves the elements uninitialised, since a device copy fills them, so reading back
+// a result is one direct DMA and no host-side fill.
+template <typename T>
+struct PinnedArray {
+    T *p = nullptr;
+    size_t n = 0, cap = 0;
+    PinnedArray() = default;
+    PinnedArray(const PinnedArray &) = delete;
+    PinnedArray &operator=(const PinnedArray &) = delete;
+    ~PinnedArray() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t resize(size_t cnt) {
+        if (cnt > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            n = cap = 0;
+            const size_t want = cnt + cnt / 8;
+            cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(&p), want * sizeof(T));
+            if (e != cudaSuccess) return e;
+            cap = want;
+        }
+        n = cnt;
+        return cudaSuccess;
+    }
+    void clear() { n = 0; }
+    T *data() { return p; }
+    const T *data() const { return p; }
+    size_t size() const { return n; }
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
+};
+
 struct HostUnitigs {
-    std::vector<uint8_t> bases;
-    std::vector<uint64_t> off;
-    std::vector<uint32_t> len;
-    std::vector<uint8_t> flags;
+    PinnedArray<uint8_t> bases;
+    PinnedArray<uint64_t> off;
+    PinnedArray<uint32_t> len;
+    PinnedArray<uint8_t> flags;
     void clear() {
         bases.clear();
         off.clear();
@@ -138,6 +174,8 @@ struct ggcat_gpu_ctx {
     uint64_t n_final = 0, n_final_bases = 0;
     // the batched merge phase as a CUDA graph, captured once per buffer/parameter layout
     cudaStream_t cap_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;         // pipelined host text copies of build_text
+    cudaEvent_t feed_ev[kFeedPieces + 1] = {};  // [0]: compute stream ready, [1 + i]: piece i copied
     cudaGraphExec_t merge_exec = nullptr;
     MergeGraphKey merge_key{};
     int merge_graph_kernels = 0;
@@ -182,6 +220,9 @@ struct ggcat_gpu_ctx {
     ~ggcat_gpu_ctx() {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
+        for (auto &e : feed_ev)
+            if (e) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         for (auto &q : qslots) {
             if (q.done) cudaEventDestroy(q.done);
             if (q.stream) cudaStreamDestroy(q.stream);
@@ -266,9 +307,11 @@ static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
     if (p->second_bits < 0 || p->second_bits > 8)
         return fail(ctx, GGCAT_GPU_EINVAL, "second_bits=%d outside [0, 8]", p->second_bits);
     if (p->subbin_bytes < 0 || p->table_load_pct < 0 || p->table_load_pct > 95 ||
-        (p->table_load_pct > 0 && p->table_load_pct < 10) || p->small_limit < 0)
-        return fail(ctx, GGCAT_GPU_EINVAL, "tuning knob out of range (subbin_bytes=%d, table_load_pct=%d, small_limit=%d)",
-                    p->subbin_bytes, p->table_load_pct, p->small_limit);
+        (p->table_load_pct > 0 && p->table_load_pct < 10) || p->small_limit < 0 || p->copy_pieces < 0 ||
+        p->copy_pieces > kFeedPieces)
+        return fail(ctx, GGCAT_GPU_EINVAL,
+                    "tuning knob out of range (subbin_bytes=%d, table_load_pct=%d, small_limit=%d, copy_pieces=%d)",
+                    p->subbin_bytes, p->table_load_pct, p->small_limit, p->copy_pieces);
     return GGCAT_GPU_OK;
 }
 
@@ -277,8 +320,19 @@ static int read_status(ggcat_gpu_ctx *ctx, unsigned *st) {
     return GGCAT_GPU_OK;
 }
 
-extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len,
-                                   const ggcat_gpu_params *p, void *stream, uint64_t *n_superkmers) {
+// Text arriving on the device in pieces (the pipelined host copy of build_text): piece i is
+// [off[i], off[i + 1]), the offsets are multiples of a bucketize block's bases, and the piece is
+// in place once ev[i] has completed.  Piece i is packed when it arrives and its blocks are
+// bucketized once piece i + 1 is packed too: a block reads at most k - 1 bases and one
+// prefetched 32-base word past its last window start, and any amount before its first one.
+struct TextFeed {
+    int pieces;
+    const uint64_t *off;
+    const cudaEvent_t *ev;
+};
+
+static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len, const ggcat_gpu_params *p,
+                          void *stream, uint64_t *n_superkmers, const TextFeed *feed) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     int rc = check_params(ctx, p);
     if (rc) return rc;
@@ -312,22 +366,50 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     CK(ctx->block_count.ensure((size_t)geo.blocks + 1));
     // overflow area of the staging array (records beyond a block's region); retried when exceeded
     uint64_t ovf_cap = text_len / 64 + 4096;
-    CK(cudaEventRecord(ctx->ev[0], s));
-    ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[1], s));
-    unsigned long long totals[3];
-    for (int attempt = 0; attempt < 2; attempt++) {
+    const uint64_t block_bases = bucketize_block_bases(geo);
+    auto bucketize_blocks = [&](uint64_t b0, uint64_t b1) {
+        return launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits, p->second_bits,
+                                ctx->fine_bits, canonical, geo, ctx->bin_count.p, ctx->bin_kmers.p, ctx->stage.p,
+                                ctx->block_count.p, ovf_cap, ctx->ovf_cursor.p, ctx->status.p, (uint32_t)b0,
+                                (uint32_t)(b1 - b0), s);
+    };
+    auto clear_counts = [&]() -> int {
         CK(ctx->stage.ensure((uint64_t)geo.blocks * geo.region_cap + ovf_cap));
         CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned), s));
         CK(cudaMemsetAsync(ctx->ovf_cursor.p, 0, sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
-        ctx->launches += launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
-                                          p->second_bits, ctx->fine_bits, canonical, geo, ctx->bin_count.p,
-                                          ctx->bin_kmers.p, ctx->stage.p, ctx->block_count.p, ovf_cap,
-                                          ctx->ovf_cursor.p, ctx->status.p, s);
+        return GGCAT_GPU_OK;
+    };
+    CK(cudaEventRecord(ctx->ev[0], s));
+    if (feed) {
+        // pipelined: pack each piece as it arrives, bucketize a piece's blocks one piece later
+        // (ms_pack stays 0; ms_bucketize covers the whole pipeline, copy waits included)
+        CK(cudaEventRecord(ctx->ev[1], s));
+        rc = clear_counts();
+        if (rc) return rc;
+        for (int i = 0; i < feed->pieces; i++) {
+            const uint64_t o0 = feed->off[i], o1 = feed->off[i + 1];
+            CK(cudaStreamWaitEvent(s, feed->ev[i], 0));
+            ctx->launches += launch_pack(d_text + o0, o1 - o0, ctx->packed.p + o0 / 32, ctx->valid.p + o0 / 32, s,
+                                         ctx->sms);
+            if (i > 0) ctx->launches += bucketize_blocks(feed->off[i - 1] / block_bases, o0 / block_bases);
+        }
+        ctx->launches += bucketize_blocks(feed->off[feed->pieces - 1] / block_bases, geo.blocks);
+        CK(cudaGetLastError());
+    } else {
+        ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[1], s));
+    }
+    unsigned long long totals[3];
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (attempt > 0 || !feed) {
+            rc = clear_counts();
+            if (rc) return rc;
+            ctx->launches += bucketize_blocks(0, geo.blocks);
+        }
         CK(cudaGetLastError());
         ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
         ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
@@ -360,6 +442,11 @@ extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, ui
     ctx->stats.kmer_instances = ctx->n_kmers;
     if (n_superkmers) *n_superkmers = ctx->n_recs;
     return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_bucketize(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len,
+                                   const ggcat_gpu_params *p, void *stream, uint64_t *n_superkmers) {
+    return bucketize_impl(ctx, d_text, text_len, p, stream, n_superkmers, nullptr);
 }
 
 extern "C" int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer *h_out, uint64_t cap, uint64_t *n) {
@@ -713,18 +800,20 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
 static int fetch_partial(ggcat_gpu_ctx *ctx) {
     if (ctx->partial_on_host) return GGCAT_GPU_OK;
     HostUnitigs &h = ctx->partial;
-    h.bases.resize(ctx->n_partial_bases);
-    h.off.resize(ctx->n_partial);
-    h.len.resize(ctx->n_partial);
-    h.flags.resize(ctx->n_partial);
     CK(cudaSetDevice(ctx->device));
+    CK(h.bases.resize(ctx->n_partial_bases));
+    CK(h.off.resize(ctx->n_partial));
+    CK(h.len.resize(ctx->n_partial));
+    CK(h.flags.resize(ctx->n_partial));
+    // the merge has completed (its output counts were read on the host), so any stream will do
     if (ctx->n_partial_bases)
-        CK(cudaMemcpy(h.bases.data(), ctx->out_bases.p, ctx->n_partial_bases, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(h.bases.data(), ctx->out_bases.p, ctx->n_partial_bases, cudaMemcpyDeviceToHost, 0));
     if (ctx->n_partial) {
-        CK(cudaMemcpy(h.off.data(), ctx->out_off.p, ctx->n_partial * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(h.len.data(), ctx->out_len.p, ctx->n_partial * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(h.flags.data(), ctx->out_flags.p, ctx->n_partial, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(h.off.data(), ctx->out_off.p, ctx->n_partial * sizeof(uint64_t), cudaMemcpyDeviceToHost, 0));
+        CK(cudaMemcpyAsync(h.len.data(), ctx->out_len.p, ctx->n_partial * sizeof(uint32_t), cudaMemcpyDeviceToHost, 0));
+        CK(cudaMemcpyAsync(h.flags.data(), ctx->out_flags.p, ctx->n_partial, cudaMemcpyDeviceToHost, 0));
     }
+    CK(cudaStreamSynchronize(0));
     ctx->partial_on_host = true;
     return GGCAT_GPU_OK;
 }
@@ -872,10 +961,10 @@ static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
     if (st & (kStatusOutOverflow | kStatusTableFull))
         return fail(ctx, GGCAT_GPU_EDEVICE, "link stage: internal overflow (status %u)", st);
     // the unitigs are packed in reservation order; bytes between them are never read
-    F.bases.resize(tot[0]);
-    F.off.resize(tot[1]);
-    F.len.resize(tot[1]);
-    F.flags.resize(tot[1]);
+    CK(F.bases.resize(tot[0]));
+    CK(F.off.resize(tot[1]));
+    CK(F.len.resize(tot[1]));
+    CK(F.flags.resize(tot[1]));
     if (tot[0]) CK(cudaMemcpy(F.bases.data(), L.out_bases.p, tot[0], cudaMemcpyDeviceToHost));
     if (tot[1]) {
         CK(cudaMemcpy(F.off.data(), L.out_off.p, tot[1] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
@@ -927,7 +1016,47 @@ extern "C" int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, u
     bool pinned = cudaPointerGetAttributes(&attr, h_text) == cudaSuccess && attr.type == cudaMemoryTypeHost;
     cudaGetLastError();
     if (pinned) {
-        CK(cudaMemcpyAsync(ctx->d_text.p, h_text, text_len, cudaMemcpyHostToDevice, s));
+        // pipelined: the copy runs on its own stream in kFeedPieces pieces (multiples of a
+        // bucketize block), each packed and bucketized while the next ones are in flight
+        int rc = check_params(ctx, p);
+        if (rc) return rc;
+        const BucketizeGeometry geo = bucketize_geometry(text_len, p->k, p->m);
+        const uint64_t bb = bucketize_block_bases(geo);
+        // every piece at least two full waves of bucketize blocks (3 per SM): the pieces'
+        // launches run one after another, so a piece of less than a wave costs a whole wave
+        const uint64_t wave = (uint64_t)ctx->sms * 3;
+        const int want = p->copy_pieces > 0 ? (int)std::min<uint64_t>(p->copy_pieces, geo.blocks)
+                                            : (int)std::min<uint64_t>(kFeedPieces, geo.blocks / (2 * wave));
+        const uint64_t per = want > 1 ? (geo.blocks + want - 1) / want : geo.blocks;
+        uint64_t off[kFeedPieces + 1];
+        int pieces = 0;
+        off[0] = 0;
+        while (off[pieces] < text_len && pieces < kFeedPieces) {
+            off[pieces + 1] = std::min<uint64_t>(text_len, off[pieces] + per * bb);
+            pieces++;
+        }
+        if (pieces <= 1) {
+            CK(cudaMemcpyAsync(ctx->d_text.p, h_text, text_len, cudaMemcpyHostToDevice, s));
+        } else {
+            if (!ctx->copy_stream) CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+            for (auto &e : ctx->feed_ev)
+                if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            // the copies overwrite the text only after the work already queued on s
+            CK(cudaEventRecord(ctx->feed_ev[0], s));
+            CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->feed_ev[0], 0));
+            for (int i = 0; i < pieces; i++) {
+                CK(cudaMemcpyAsync(ctx->d_text.p + off[i], h_text + off[i], off[i + 1] - off[i], cudaMemcpyHostToDevice,
+                                   ctx->copy_stream));
+                CK(cudaEventRecord(ctx->feed_ev[1 + i], ctx->copy_stream));
+            }
+            const TextFeed feed{pieces, off, ctx->feed_ev + 1};
+            uint64_t nsk = 0;
+            rc = bucketize_impl(ctx, ctx->d_text.p, text_len, p, stream, &nsk, &feed);
+            if (rc) return rc;
+            rc = ggcat_gpu_merge(ctx, p, stream);
+            if (rc) return rc;
+            return fetch_partial(ctx);
+        }
     } else {
         const uint64_t chunk = 64ull << 20;
         CK(ctx->h_stage.ensure(2 * chunk));

@@ -24,7 +24,10 @@ cudaError_t merge_configure();
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
                      int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
                      unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
-                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, cudaStream_t s);
+                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, uint32_t block_base,
+                     uint32_t n_blocks, cudaStream_t s);
+// text bases covered by one bucketize block (pieces of a pipelined launch are multiples of it)
+inline uint64_t bucketize_block_bases(const BucketizeGeometry &g) { return (uint64_t)g.threads_per_block * g.chunk; }
 int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
                      const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
                      const unsigned long long *bin_off, unsigned *bin_cursor, SkRec *recs, unsigned *status,

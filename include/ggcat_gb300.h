@@ -58,6 +58,10 @@ typedef struct {
     int32_t table_load_pct;   /* largest load of a global-memory merge table, percent (default 80) */
     int32_t small_limit;      /* largest sub-bin, in k-mer instances, merged in a shared-memory S unit
                                  (default and maximum 3200, 1600 for k > 32) */
+    int32_t copy_pieces;      /* pieces of the host text copy of ggcat_gpu_build_text from pinned memory,
+                                 each packed and bucketized while the next ones are in flight (0 = auto:
+                                 up to 4, each at least two waves of bucketize blocks; 1 = one copy;
+                                 at most 4) */
 } ggcat_gpu_params;
 
 /* One superkmer in the semantic form of PushSequenceInfo

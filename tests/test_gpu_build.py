@@ -400,3 +400,54 @@ def test_wide_k_matches_oracle(ctx, kind, seed, k, m, okind, hkind, minm, mode):
     bases, uo, ul, uf = ctx.unitigs()
     got_u = oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k)
     assert got_u == r.unitigs()
+
+
+_RC = bytes.maketrans(b"ACGT", b"TGCA")
+
+
+def _unitig_multiset(ctx):
+    """Partial unitigs up to orientation: which end a path is written from depends on the
+    table slots its k-mers landed in, so each is taken as min(s, revcomp(s)) with its link
+    flags (bit 0 backward, bit 1 forward) swapped when reversed.  Circular ones (bit 2) start
+    anywhere and are left to the final-unitig comparison."""
+    bases, off, ln, fl = ctx.partial_unitigs()
+    out = []
+    for o, n, f in zip(off.tolist(), ln.tolist(), fl.tolist()):
+        if f & 4:
+            continue
+        s = bases[o:o + n].tobytes()
+        r = s.translate(_RC)[::-1]
+        if r < s:
+            s, f = r, (f & ~3) | ((f & 1) << 1) | ((f >> 1) & 1)
+        out.append((s, f))
+    return sorted(out)
+
+
+@pytest.mark.parametrize("k,m,read_len", [(31, 10, 150), (63, 12, 250)])
+def test_pinned_text_pipelined_equals_pageable(ctx, k, m, read_len):
+    """build_text from pinned host memory copies the text in pieces on its own stream and
+    packs / bucketizes each piece while the next ones are in flight; the records, k-mers and
+    partial unitigs equal those of the one-copy (pageable) path."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(k)
+    g = synth.random_genome(300_000, rng)
+    reads = synth.sample_reads(g, 6_000_000 // read_len, read_len, 0.005, 0.0002, rng)
+    text, _, _, _ = synth.pack_reads(reads)
+    assert len(text) > 8 * 262144  # several bucketize blocks per piece
+    p = make_params(k=k, m=m, bucket_bits=8, second_bits=3, min_multiplicity=2, keep_kmers=True, copy_pieces=4)
+
+    def run(t):
+        ctx.build_text(t, p)
+        sk, (keys, mult), parts = _sorted_sk(ctx.superkmers()), ctx.kmers(), _unitig_multiset(ctx)
+        ctx.link(k)
+        bases, uo, ul, uf = ctx.unitigs()
+        final = oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, k)
+        kk = sorted(zip(map(tuple, keys.reshape(len(mult), -1).tolist()), mult.tolist()))
+        return sk, kk, parts, final
+
+    sk_a, k_a, u_a, f_a = run(text)
+    sk_b, k_b, u_b, f_b = run(torch.from_numpy(text).pin_memory().numpy())
+    assert len(sk_a) > 0 and (sk_a == sk_b).all()
+    assert k_a == k_b
+    assert u_a == u_b
+    assert f_a == f_b and len(f_a) > 0
