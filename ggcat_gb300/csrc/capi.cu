@@ -1255,7 +1255,6 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     if (!ctx) return GGCAT_GPU_EINVAL;
     if (!ctx->have_merge || !ctx->last_params.keep_kmers)
         return fail(ctx, GGCAT_GPU_EINVAL, "colours need a merge run with keep_kmers = 1");
-    if (ctx->last_params.k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "colours support k <= 32");
     if (!h_seq_off || !h_seq_color || n_seq == 0 || n_colors == 0 || n_colors > 65536)
         return fail(ctx, GGCAT_GPU_EINVAL, "bad colour table (n_seq=%llu, n_colors=%u)", (unsigned long long)n_seq,
                     n_colors);
@@ -1279,7 +1278,9 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     while (cap < 2 * nd + 64) cap <<= 1;
     uint64_t scap = 1024;
     while (scap < 2 * nd + 64) scap <<= 1;
-    CK(ctx->cslots.ensure(2 * cap));
+    const int wide = ctx->last_params.k > 32;
+    const uint64_t slot_words = wide ? 4 : 2;
+    CK(ctx->cslots.ensure(slot_words * cap));
     CK(ctx->cowner.ensure(nd + 1));
     CK(ctx->cbitmaps.ensure((nd + 1) * (uint64_t)words));
     CK(ctx->cid_subset.ensure(nd + 1));
@@ -1292,14 +1293,14 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(ctx->cseq_color.ensure(n_seq));
     CK(cudaMemcpyAsync(ctx->cseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->cseq_color.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(ctx->cslots.p, 0xff, 2 * cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->cslots.p, 0xff, slot_words * cap * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(ctx->cbitmaps.p, 0, (nd + 1) * words * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->csub_hash.p, 0, scap * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->csub_state.p, 0, scap * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->ccounters.p, 0, 4 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
     ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
-                                        ctx->last_params.forward_only ? 0 : 1, ctx->cseq_off.p, ctx->cseq_color.p,
+                                        ctx->last_params.forward_only ? 0 : 1, wide, ctx->cseq_off.p, ctx->cseq_color.p,
                                         n_seq, h_seq_off[0] == 0 ? max_len : 0, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
                                         ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p, ctx->csub_arena.p,
                                         scap - 1, ctx->cid_subset.p, ctx->cdump_subset.p, ctx->status.p + 1,
@@ -1380,6 +1381,7 @@ extern "C" int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream) {
     if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result to index");
     if (ctx->last_params.forward_only)
         return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
+    if (ctx->last_params.k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the coloured query index supports k <= 32");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
     ctx->qready = false;

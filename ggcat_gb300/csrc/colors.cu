@@ -21,76 +21,148 @@ namespace cg = cooperative_groups;
 
 namespace ggcat {
 
-__device__ __forceinline__ uint64_t cslot(uint64_t key, uint64_t mask) { return mix64(key) & mask; }
-
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(uint64_t *p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
-// The k-mer table: 16-byte slots {key, id}, empty = all-ones in both words.  A k-mer's id is
-// the dump index of the thread that inserted it (its owner), claimed together with the key by
-// one 128-bit compare-and-swap, so a lookup reads one slot and no numbering pass is needed;
-// ids of duplicate dump entries are holes whose colour bitmap stays empty.
-__device__ __forceinline__ void cas_slot(uint64_t *slot, uint64_t cmp_key, uint64_t cmp_id, uint64_t key, uint64_t id,
-                                         uint64_t &old_key, uint64_t &old_id) {
+// 128-bit compare-and-swap on a global 16-byte word pair; returns the previous pair
+__device__ __forceinline__ void cas_pair(uint64_t *slot, uint64_t c0, uint64_t c1, uint64_t v0, uint64_t v1,
+                                         uint64_t &o0, uint64_t &o1) {
     asm volatile(
         "{\n\t.reg .b128 c, v, d;\n\t"
         "mov.b128 c, {%2, %3};\n\t"
         "mov.b128 v, {%4, %5};\n\t"
         "atom.global.cas.b128 d, [%6], c, v;\n\t"
         "mov.b128 {%0, %1}, d;\n\t}"
-        : "=l"(old_key), "=l"(old_id)
-        : "l"(cmp_key), "l"(cmp_id), "l"(key), "l"(id), "l"(slot)
+        : "=l"(o0), "=l"(o1)
+        : "l"(c0), "l"(c1), "l"(v0), "l"(v1), "l"(slot)
         : "memory");
 }
 
-// 1. insert the dumped survivors; owner[i] = id of dump entry i's k-mer (i itself unless the
-//    k-mer was dumped twice)
-__global__ void color_kmer_insert_kernel(const uint64_t *__restrict__ kmers, uint64_t n, uint64_t *slots,
-                                         uint64_t mask, uint32_t *owner, unsigned *status) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t key = kmers[i];
-        uint64_t s = cslot(key, mask);
-        uint64_t own = kEmptyKey;
+// The k-mer table, empty = all-ones.  A k-mer's id is the dump index of the thread that
+// inserted it (its owner), so no numbering pass is needed; ids of k-mers dumped twice are
+// holes whose colour bitmap stays empty.
+//   u64 keys (k <= 32):  16-byte slots {key, id}, key and id claimed together by one 128-bit
+//                        compare-and-swap (a failed compare returns the owner's pair);
+//   u128 keys (k <= 64): 32-byte slots {key lo, key hi, id, -}, the key claimed by a 128-bit
+//                        compare-and-swap and the id stored right after it; a thread that
+//                        finds the key waits (bounded) for the id.
+// A lookup reads one slot (one 32-byte sector).
+template <typename KT>
+struct ColorTable;
+
+template <>
+struct ColorTable<uint64_t> {
+    static constexpr int kWords = 2;
+    __device__ static __forceinline__ uint64_t slot(uint64_t key, uint64_t mask) { return mix64(key) & mask; }
+    __device__ static __forceinline__ uint64_t dumped(const uint64_t *kmers, uint64_t i) { return kmers[i]; }
+    // owner id of key, inserting it as dump entry i; kEmptyKey on failure
+    __device__ static __forceinline__ uint64_t insert(uint64_t *slots, uint64_t mask, uint64_t key, uint64_t i,
+                                                      bool &waited_out) {
+        uint64_t s = slot(key, mask);
         for (uint64_t probe = 0; probe <= mask; probe++) {
             const uint64_t kk = slots[2 * s];
             if (kk == key || kk == kEmptyKey) {
-                // a failed compare returns the slot atomically: for kk == key this is a read of
-                // the owner's {key, id} pair
                 uint64_t ok, oid;
-                cas_slot(slots + 2 * s, kEmptyKey, kEmptyKey, key, i, ok, oid);
-                if (ok == kEmptyKey) {
-                    own = i;
-                    break;
-                }
-                if (ok == key) {
-                    own = oid;
-                    break;
-                }
+                cas_pair(slots + 2 * s, kEmptyKey, kEmptyKey, key, i, ok, oid);
+                if (ok == kEmptyKey) return i;
+                if (ok == key) return oid;
             }
             s = (s + 1) & mask;
         }
-        if (own == kEmptyKey) atomicOr(status, kStatusTableFull);
+        waited_out = false;
+        return kEmptyKey;
+    }
+    // id of key or -1; the table is read-only while this runs
+    __device__ static __forceinline__ int64_t find(const uint64_t *__restrict__ slots, uint64_t mask, uint64_t key) {
+        uint64_t s = slot(key, mask);
+        for (uint64_t probe = 0; probe <= mask; probe++) {
+            const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2 *>(slots) + s);
+            if (e.x == key) return (int64_t)e.y;
+            if (e.x == kEmptyKey) return -1;
+            s = (s + 1) & mask;
+        }
+        return -1;
+    }
+};
+
+template <>
+struct ColorTable<u128> {
+    static constexpr int kWords = 4;
+    __device__ static __forceinline__ uint64_t slot(u128 key, uint64_t mask) {
+        return mix64((uint64_t)key ^ ((uint64_t)(key >> 64) * 0x9E3779B97F4A7C15ull)) & mask;
+    }
+    __device__ static __forceinline__ u128 dumped(const uint64_t *kmers, uint64_t i) {
+        return ((u128)kmers[2 * i + 1] << 64) | (u128)kmers[2 * i];
+    }
+    __device__ static __forceinline__ uint64_t insert(uint64_t *slots, uint64_t mask, u128 key, uint64_t i,
+                                                      bool &waited_out) {
+        const uint64_t lo = (uint64_t)key, hi = (uint64_t)(key >> 64);
+        uint64_t s = slot(key, mask);
+        for (uint64_t probe = 0; probe <= mask; probe++) {
+            uint64_t *sp = slots + 4 * s;
+            // the key pair is only ever read whole, through the compare-and-swap
+            uint64_t o0, o1;
+            cas_pair(sp, kEmptyKey, kEmptyKey, lo, hi, o0, o1);
+            if (o0 == kEmptyKey && o1 == kEmptyKey) {
+                st_relaxed_u64(sp + 2, i);
+                return i;
+            }
+            if (o0 == lo && o1 == hi) {
+                uint64_t v = ld_relaxed_u64(sp + 2);
+                for (int spin = 0; v == kEmptyKey && spin < (1 << 22); spin++) {
+                    __nanosleep(32);
+                    v = ld_relaxed_u64(sp + 2);
+                }
+                waited_out = v == kEmptyKey;
+                return v;
+            }
+            s = (s + 1) & mask;
+        }
+        waited_out = false;
+        return kEmptyKey;
+    }
+    __device__ static __forceinline__ int64_t find(const uint64_t *__restrict__ slots, uint64_t mask, u128 key) {
+        const uint64_t lo = (uint64_t)key, hi = (uint64_t)(key >> 64);
+        uint64_t s = slot(key, mask);
+        for (uint64_t probe = 0; probe <= mask; probe++) {
+            const ulonglong2 kk = __ldg(reinterpret_cast<const ulonglong2 *>(slots + 4 * s));
+            const ulonglong2 id = __ldg(reinterpret_cast<const ulonglong2 *>(slots + 4 * s + 2));
+            if (kk.x == lo && kk.y == hi) return (int64_t)id.x;
+            if (kk.x == kEmptyKey && kk.y == kEmptyKey) return -1;
+            s = (s + 1) & mask;
+        }
+        return -1;
+    }
+};
+
+// 1. insert the dumped survivors; owner[i] = id of dump entry i's k-mer (i itself unless the
+//    k-mer was dumped twice)
+template <typename KT>
+__global__ void color_kmer_insert_kernel(const uint64_t *__restrict__ kmers, uint64_t n, uint64_t *slots,
+                                         uint64_t mask, uint32_t *owner, unsigned *status) {
+    using T = ColorTable<KT>;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        bool waited_out = false;
+        const uint64_t own = T::insert(slots, mask, T::dumped(kmers, i), i, waited_out);
+        if (own == kEmptyKey) atomicOr(status, waited_out ? kStatusWalkLimit : kStatusTableFull);
         owner[i] = (uint32_t)own;
     }
 }
 
-// id of `key` or -1; the table is read-only while this runs
-__device__ __forceinline__ int64_t color_find(const uint64_t *__restrict__ slots, uint64_t mask, uint64_t key) {
-    uint64_t s = cslot(key, mask);
-    for (uint64_t probe = 0; probe <= mask; probe++) {
-        const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2 *>(slots) + s);
-        if (e.x == key) return (int64_t)e.y;
-        if (e.x == kEmptyKey) return -1;
-        s = (s + 1) & mask;
-    }
-    return -1;
-}
-
 // 2. occurrences: every k-mer of the text sets its sequence's colour bit
 constexpr uint64_t kOccMaxRows = 65536;
+template <typename KT>
 __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
                                                        int canonical, uint64_t chunk,
                                                        const uint64_t *__restrict__ seq_off,
@@ -126,8 +198,9 @@ __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restric
     }
     uint64_t next_off = seq + 1 < n_seq ? seq_off[seq + 1] : ~0ull;
     uint32_t col = seq_color[seq];
-    const uint64_t kmask = kmer_mask(k);
-    uint64_t fw = 0, rc = 0, run = 0;
+    const KT kmask = KeyOps<KT>::mask(k);
+    KT fw = 0, rc = 0;
+    uint64_t run = 0;
     const uint64_t pend = min(x1 + (uint64_t)k - 1, n);
     // the text is read 16 bytes per aligned load into registers: one byte per load would
     // refetch each sector from DRAM, as the table traffic evicts it
@@ -153,9 +226,9 @@ __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restric
                 run = 0;
                 continue;
             }
-            const uint64_t b = (c >> 1) & 3u;
-            fw = (fw >> 2) | (b << (2 * (k - 1)));
-            rc = ((rc << 2) | (b ^ 2u)) & kmask;
+            const uint32_t b = (c >> 1) & 3u;
+            fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
+            rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
             if (++run < (uint64_t)k) continue;
             const uint64_t start = q + j + 1 - (uint64_t)k;
             while (start >= next_off) {
@@ -163,7 +236,7 @@ __global__ void __launch_bounds__(256) color_occ_kernel(const uint8_t *__restric
                 next_off = seq + 1 < n_seq ? seq_off[seq + 1] : ~0ull;
                 col = seq_color[seq];
             }
-            const int64_t id = color_find(slots, mask, (canonical && rc < fw) ? rc : fw);
+            const int64_t id = ColorTable<KT>::find(slots, mask, (canonical && rc < fw) ? rc : fw);
             if (id < 0) continue;  // not a surviving k-mer
             atomicOr(&bitmaps[(uint64_t)id * words + (col >> 5)], 1u << (col & 31));
         }
@@ -251,14 +324,17 @@ __global__ void color_dump_subsets_kernel(const uint32_t *__restrict__ owner, ui
 
 // ---------------------------------------------------------------------------
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
-                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq,
-                       uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
+                       int canonical, int wide, const uint64_t *seq_off, const uint32_t *seq_color,
+                       uint64_t n_seq, uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
                        unsigned long long *sub_count, unsigned long long *sub_hash, uint32_t *sub_state,
                        uint32_t *sub_arena, uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset,
                        unsigned *status, int sms, cudaStream_t s) {
     int n = 0;
     if (n_dump) {
-        color_kmer_insert_kernel<<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
+        if (wide)
+            color_kmer_insert_kernel<u128><<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
+        else
+            color_kmer_insert_kernel<uint64_t><<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
         n++;
     }
     const uint64_t chunk = 256;
@@ -273,9 +349,14 @@ int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *tex
             seq_rows ? n_seq : std::max<uint64_t>(1, std::min<uint64_t>(n_seq <= kOccMaxRows ? n_seq : 1, chunks));
         const uint64_t row_chunks = seq_rows ? max_chunks : (chunks + rows - 1) / rows;
         const uint64_t threads = rows * row_chunks;
-        color_occ_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(text, n_text, k, canonical, chunk, seq_off,
-                                                                          seq_color, n_seq, slots, mask, bitmaps,
-                                                                          words, rows, row_chunks, seq_rows);
+        const unsigned grid = (unsigned)((threads + 255) / 256);
+        if (wide)
+            color_occ_kernel<u128><<<grid, 256, 0, s>>>(text, n_text, k, canonical, chunk, seq_off, seq_color, n_seq,
+                                                        slots, mask, bitmaps, words, rows, row_chunks, seq_rows);
+        else
+            color_occ_kernel<uint64_t><<<grid, 256, 0, s>>>(text, n_text, k, canonical, chunk, seq_off, seq_color,
+                                                            n_seq, slots, mask, bitmaps, words, rows, row_chunks,
+                                                            seq_rows);
         n++;
     }
     if (n_dump) {

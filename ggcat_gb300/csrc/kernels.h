@@ -179,12 +179,13 @@ int launch_link_write(const uint8_t *bases, const uint64_t *off, const uint32_t 
 int launch_kmer_hash(const uint8_t *text, uint64_t n, int k, int kind, uint64_t *out, cudaStream_t s);
 
 // colors.cu
-// slots: 2 x (mask + 1) words ({key, id} pairs, all-ones when empty); owner, id_subset,
+// dump: the merge's k-mer dump (u64 keys, or (lo, hi) pairs when wide, k > 32); slots:
+// (wide ? 4 : 2) x (mask + 1) words ({key, id} slots, all-ones when empty); owner, id_subset,
 // dump_subset: n_dump entries; bitmaps: n_dump x words (zeroed); max_seq_len: the longest
 // sequence (seq_off[i + 1] - seq_off[i], the last one up to n_text), 0 when seq_off[0] > 0
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
-                       int canonical, const uint64_t *seq_off, const uint32_t *seq_color, uint64_t n_seq,
-                       uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
+                       int canonical, int wide, const uint64_t *seq_off, const uint32_t *seq_color,
+                       uint64_t n_seq, uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,
                        unsigned long long *sub_count, unsigned long long *sub_hash, uint32_t *sub_state,
                        uint32_t *sub_arena, uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset,
                        unsigned *status, int sms, cudaStream_t s);

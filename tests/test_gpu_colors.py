@@ -137,3 +137,31 @@ def test_color_sets_mixed_lengths_and_read_sets(n_reads, read_len, colors):
     finally:
         ctx.close()
 
+
+def test_color_sets_k63_match_oracle():
+    """Colours for k > 32: u128 keys in 32-byte table slots (key claimed by a 128-bit
+    compare-and-swap, id stored after it), 128-bit rolling in the occurrence pass."""
+    text, off, ln, col, gs, nc = _colored_input(seed=33, n_genomes=10, L=50_000)
+    ctx = _native.GpuContext(0)
+    try:
+        p = _native.make_params(k=63, m=12, bucket_bits=6, second_bits=2, min_multiplicity=1, keep_kmers=True)
+        ctx.build_text(text, p)
+        ctx.colors(off, col, nc)
+        keys, _ = ctx.kmers()
+        subs = ctx.kmer_subsets()
+        decoded = [_decode(row) for row in ctx.subsets()]
+        assert len(set(decoded)) == len(decoded)
+        got = {}
+        for (lo_w, hi_w), sid in zip(keys.tolist(), subs.tolist()):
+            assert got.get((lo_w, hi_w), decoded[sid]) == decoded[sid]
+            got[(lo_w, hi_w)] = decoded[sid]
+        r = oracle.build_graph(text, off, ln, oracle.params(k=63, m=12, bucket_bits=6, second_bits=2, threads=4,
+                                                             colors=True), seq_colors=col)
+        lo, hi, _ = r.kmers()
+        coff, ccol = r.kmer_colors()
+        exp = {(int(lo[i]), int(hi[i])): tuple(int(c) for c in ccol[coff[i]:coff[i + 1]]) for i in range(len(lo))}
+        assert got == exp and len(exp) > 0
+        with pytest.raises(_native.GgcatGpuError):
+            ctx.query_index_colored()  # the coloured query index is k <= 32
+    finally:
+        ctx.close()
