@@ -1381,18 +1381,19 @@ extern "C" int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream) {
     if (!ctx->have_colors) return fail(ctx, GGCAT_GPU_EINVAL, "no colour result to index");
     if (ctx->last_params.forward_only)
         return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
-    if (ctx->last_params.k > 32) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the coloured query index supports k <= 32");
     cudaStream_t s = as_stream(stream);
     CK(cudaSetDevice(ctx->device));
     ctx->qready = false;
+    const int wide = ctx->last_params.k > 32;
+    const uint64_t kw = wide ? 2 : 1;  // key words (u128 keys above k = 32)
     uint64_t cap = 1024;
     while (cap < 2 * ctx->c_n_ids + 64) cap <<= 1;
-    CK(ctx->qkeys.ensure(cap));
+    CK(ctx->qkeys.ensure(cap * kw));
     CK(ctx->qvals.ensure(cap));
-    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * kw * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
-    ctx->launches += launch_index_from_colors(ctx->cslots.p, ctx->cmask + 1, ctx->cid_subset.p,
-                                              ctx->qkeys.p, ctx->qvals.p, cap - 1, ctx->status.p + 1, ctx->sms, s);
+    ctx->launches += launch_index_from_colors(ctx->cslots.p, ctx->cmask + 1, ctx->cid_subset.p, wide, ctx->qkeys.p,
+                                              ctx->qvals.p, cap - 1, ctx->status.p + 1, ctx->sms, s);
     CK(cudaGetLastError());
     unsigned st = 0;
     CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));

@@ -138,13 +138,14 @@ int merge_ctas_per_sm(int tier, int wide);
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
                         unsigned *status, cudaStream_t s);
 // cslots: the colour phase's {key, id} table of ccap slots
-int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset, uint64_t *keys,
+// keys: u64 (wide = 0) or u128 query table keys, 16-byte aligned
+int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset, int wide, void *keys,
                              uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s);
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
                  const uint32_t *item_len, uint64_t n_items, const void *keys, uint64_t mask,
                  unsigned long long *matched, cudaStream_t s);
 int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
-                       const uint64_t *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
+                       const void *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
                        uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
                        unsigned long long *queue, int sms, cudaStream_t s);
 

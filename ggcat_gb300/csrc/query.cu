@@ -67,26 +67,31 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
     }
 }
 
-// Coloured index: the colour phase's k-mer table ({key, id} slots) re-keyed into the query
-// table with value = colour subset id.
+// Coloured index: the colour phase's k-mer table ({key, id} slots: 2 words for u64 keys, 4
+// for u128) re-keyed into the query table with value = colour subset id.
+template <typename KT>
 __global__ void index_from_colors_kernel(const uint64_t *__restrict__ cslots, uint64_t ccap,
-                                         const uint32_t *__restrict__ id_subset, uint64_t *keys, uint32_t *vals,
+                                         const uint32_t *__restrict__ id_subset, KT *keys, uint32_t *vals,
                                          uint64_t mask, unsigned *status) {
+    using K = KeyOps<KT>;
+    constexpr int kSlotWords = sizeof(KT) == 8 ? 2 : 4;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ccap; i += (uint64_t)gridDim.x * blockDim.x) {
-        const ulonglong2 e = reinterpret_cast<const ulonglong2 *>(cslots)[i];
-        const uint64_t key = e.x;
-        if (key == kEmptyKey) continue;
-        uint64_t s = qslot(key, mask);
+        const uint64_t *e = cslots + kSlotWords * i;
+        KT key;
+        if constexpr (sizeof(KT) == 8) key = e[0];
+        else key = ((u128)e[1] << 64) | (u128)e[0];
+        if (key == K::empty()) continue;
+        const uint32_t id = (uint32_t)e[kSlotWords / 2];
+        uint64_t s = qslot_key(key, mask);
         for (uint64_t probe = 0;; probe++) {
             if (probe > mask) {
                 atomicOr(status, kStatusTableFull);
                 break;
             }
-            if (keys[s] == kEmptyKey) {
-                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[s]),
-                                                         (unsigned long long)kEmptyKey, (unsigned long long)key);
-                if (old == kEmptyKey) {
-                    vals[s] = id_subset[(uint32_t)e.y];
+            if (keys[s] == K::empty()) {
+                const KT old = K::cas(&keys[s], K::empty(), key);
+                if (old == K::empty()) {
+                    vals[s] = id_subset[id];
                     break;
                 }
             }
@@ -141,19 +146,21 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
 // Coloured lookup, one CTA per query from a device queue: runs of equal subset ids are
 // expanded into per-colour counts in shared memory (colored_query_output.rs:264-309 sums
 // the per-subset counters of a query per colour).
+template <typename KT>
 __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restrict__ text, int k,
                                                          const uint64_t *__restrict__ q_off,
                                                          const uint64_t *__restrict__ q_len, uint64_t nq,
-                                                         const uint64_t *__restrict__ keys,
+                                                         const KT *__restrict__ keys,
                                                          const uint32_t *__restrict__ vals, uint64_t mask,
                                                          const uint32_t *__restrict__ sub_arena, int words,
                                                          uint32_t n_colors, unsigned long long *__restrict__ matched,
                                                          unsigned long long *__restrict__ counts,
                                                          unsigned long long *__restrict__ queue) {
+    using K = KeyOps<KT>;
     extern __shared__ uint32_t cnt[];  // n_colors counters
     __shared__ unsigned long long q_cur;
     __shared__ unsigned long long hits_sh;
-    const uint64_t kmask = kmer_mask(k);
+    const KT kmask = K::mask(k);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -168,7 +175,8 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
         const uint64_t nk = L >= (uint64_t)k ? L - (uint64_t)k + 1 : 0;
         const uint64_t per = (nk + blockDim.x - 1) / blockDim.x;
         const uint64_t a = min(nk, (uint64_t)threadIdx.x * per), b = min(nk, a + per);
-        uint64_t fw = 0, rc = 0, run = 0, hits = 0;
+        KT fw = 0, rc = 0;
+        uint64_t run = 0, hits = 0;
         uint32_t cur_sub = 0xffffffffu, cur_cnt = 0;
         auto flush = [&]() {
             if (!cur_cnt) return;
@@ -192,14 +200,14 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
                     run = 0;
                     continue;
                 }
-                const uint64_t bb = (c >> 1) & 3u;
-                fw = (fw >> 2) | (bb << (2 * (k - 1)));
-                rc = ((rc << 2) | (bb ^ 2u)) & kmask;
+                const uint32_t bb = (c >> 1) & 3u;
+                fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
+                rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
                 if (++run < (uint64_t)k) continue;
-                const uint64_t key = fw < rc ? fw : rc;
-                uint64_t s = qslot(key, mask);
+                const KT key = fw < rc ? fw : rc;
+                uint64_t s = qslot_key(key, mask);
                 for (uint64_t probe = 0; probe <= mask; probe++) {
-                    const uint64_t kk = keys[s];
+                    const KT kk = keys[s];
                     if (kk == key) {
                         hits++;
                         const uint32_t sub = vals[s];
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
                         cur_cnt++;
                         break;
                     }
-                    if (kk == kEmptyKey) break;
+                    if (kk == K::empty()) break;
                     s = (s + 1) & mask;
                 }
             }
@@ -237,9 +245,14 @@ int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint
     return 1;
 }
 
-int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset,
-                             uint64_t *keys, uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s) {
-    index_from_colors_kernel<<<sms * 8, 256, 0, s>>>(cslots, ccap, id_subset, keys, vals, mask, status);
+int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset, int wide, void *keys,
+                             uint32_t *vals, uint64_t mask, unsigned *status, int sms, cudaStream_t s) {
+    if (wide)
+        index_from_colors_kernel<u128><<<sms * 8, 256, 0, s>>>(cslots, ccap, id_subset, static_cast<u128 *>(keys), vals,
+                                                               mask, status);
+    else
+        index_from_colors_kernel<uint64_t><<<sms * 8, 256, 0, s>>>(cslots, ccap, id_subset,
+                                                                   static_cast<uint64_t *>(keys), vals, mask, status);
     return 1;
 }
 
@@ -258,19 +271,25 @@ int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const u
 }
 
 int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
-                       const uint64_t *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
+                       const void *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
                        uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
                        unsigned long long *queue, int sms, cudaStream_t s) {
     if (nq == 0) return 0;
     const size_t smem = (size_t)n_colors * sizeof(uint32_t);
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(query_color_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(query_color_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(query_color_kernel<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         configured = true;
     }
-    uint64_t grid = std::min<uint64_t>(nq, (uint64_t)sms * 8);
-    query_color_kernel<<<(unsigned)grid, 256, smem, s>>>(text, k, q_off, q_len, nq, keys, vals, mask, sub_arena, words,
-                                                        n_colors, matched, counts, queue);
+    const unsigned grid = (unsigned)std::min<uint64_t>(nq, (uint64_t)sms * 8);
+    if (k > 32)
+        query_color_kernel<u128><<<grid, 256, smem, s>>>(text, k, q_off, q_len, nq, static_cast<const u128 *>(keys),
+                                                         vals, mask, sub_arena, words, n_colors, matched, counts, queue);
+    else
+        query_color_kernel<uint64_t><<<grid, 256, smem, s>>>(text, k, q_off, q_len, nq,
+                                                             static_cast<const uint64_t *>(keys), vals, mask, sub_arena,
+                                                             words, n_colors, matched, counts, queue);
     return 1;
 }
 

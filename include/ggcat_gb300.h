@@ -41,8 +41,7 @@ typedef struct ggcat_gpu_ctx ggcat_gpu_ctx;
 
 typedef struct {
     int32_t k;                /* k-mer length: bucketing k <= 64; merge and link odd k <= 64 (u64 keys for
-                                 k <= 32, u128 keys above); colours and the uncoloured query k <= 64, the
-                                 coloured query k <= 32 */
+                                 k <= 32, u128 keys above); colours and both queries k <= 64 */
     int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
     int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
     int32_t second_bits;      /* second-level bucket bits reported in superkmer records */

@@ -138,9 +138,10 @@ def test_color_sets_mixed_lengths_and_read_sets(n_reads, read_len, colors):
         ctx.close()
 
 
-def test_color_sets_k63_match_oracle():
+def test_color_sets_and_query_k63_match_oracle():
     """Colours for k > 32: u128 keys in 32-byte table slots (key claimed by a 128-bit
-    compare-and-swap, id stored after it), 128-bit rolling in the occurrence pass."""
+    compare-and-swap, id stored after it), 128-bit rolling in the occurrence pass, and the
+    coloured query over a u128 index."""
     text, off, ln, col, gs, nc = _colored_input(seed=33, n_genomes=10, L=50_000)
     ctx = _native.GpuContext(0)
     try:
@@ -161,7 +162,15 @@ def test_color_sets_k63_match_oracle():
         coff, ccol = r.kmer_colors()
         exp = {(int(lo[i]), int(hi[i])): tuple(int(c) for c in ccol[coff[i]:coff[i + 1]]) for i in range(len(lo))}
         assert got == exp and len(exp) > 0
-        with pytest.raises(_native.GgcatGpuError):
-            ctx.query_index_colored()  # the coloured query index is k <= 32
+        ctx.query_index_colored()
+        rng = np.random.default_rng(8)
+        queries, _ = synth.query_stream(gs, 40, rng, min_len=70, max_len=6000)
+        qt, qo, ql = serve._pack(queries)
+        ctx.query_submit(1, qt, qo, ql)
+        matched = ctx.query_wait(1)
+        counts = ctx.query_color_counts(1)
+        em, _, epc = oracle.query(lo, hi, qt, qo, ql, 63, gc_off=coff, gc_colors=ccol, ncolors=nc)
+        assert (matched == em).all() and em.sum() > 0
+        assert (counts == epc).all()
     finally:
         ctx.close()
