@@ -97,6 +97,8 @@ EXPORTED = [
     "ggcat_gpu_get_stats",
     "ggcat_gpu_build_text",
     "ggcat_gpu_fasta_parse",
+    "ggcat_gpu_fastq_parse",
+    "ggcat_gpu_read_sequences_file",
     "ggcat_gpu_build_from_files",
     "ggcat_gpu_colors",
     "ggcat_gpu_kmer_subsets_copy",
@@ -153,6 +155,8 @@ def load(build: bool = True):
     L.ggcat_gpu_get_stats.argtypes = [P, C.POINTER(Stats)]
     L.ggcat_gpu_build_text.argtypes = [P, P, u64, C.POINTER(Params), P]
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
+    L.ggcat_gpu_fastq_parse.argtypes = [P, u64, P, u64, pu64, pu64]
+    L.ggcat_gpu_read_sequences_file.argtypes = [C.c_char_p, C.c_int64, P, u64, pu64, pu64, C.c_char_p, u64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
     L.ggcat_gpu_kmer_hashes.argtypes = [P, P, u64, C.c_int, C.c_int, P, P]
@@ -386,6 +390,35 @@ def fasta_parse(data: bytes, copyback: int):
     rc = L.ggcat_gpu_fasta_parse(_ptr(buf), len(buf), copyback, _ptr(text), need.value, C.byref(need), C.byref(pieces))
     if rc:
         raise GgcatGpuError("fasta_parse failed")
+    return text
+
+
+def fastq_parse(data: bytes):
+    """FASTQ -> device text layout, one piece per record."""
+    L = load()
+    buf = np.frombuffer(data, dtype=np.uint8)
+    need, n = C.c_uint64(), C.c_uint64()
+    if L.ggcat_gpu_fastq_parse(_ptr(buf), len(buf), None, 0, C.byref(need), C.byref(n)):
+        raise GgcatGpuError("fastq_parse failed")
+    text = np.zeros(need.value, np.uint8)
+    if L.ggcat_gpu_fastq_parse(_ptr(buf), len(buf), _ptr(text), need.value, C.byref(need), C.byref(n)):
+        raise GgcatGpuError("fastq_parse failed")
+    return text
+
+
+def read_sequences_file(path: str, copyback: int = -1):
+    """One FASTA / FASTQ file (plain or gz, lz4, bz2, xz, zst) -> device text layout."""
+    L = load()
+    need, n = C.c_uint64(), C.c_uint64()
+    err = C.create_string_buffer(512)
+    rc = L.ggcat_gpu_read_sequences_file(os.fsencode(path), copyback, None, 0, C.byref(need), C.byref(n), err, 512)
+    if rc:
+        raise GgcatGpuError(f"read_sequences_file failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
+    text = np.zeros(need.value, np.uint8)
+    rc = L.ggcat_gpu_read_sequences_file(os.fsencode(path), copyback, _ptr(text), need.value, C.byref(need),
+                                         C.byref(n), err, 512)
+    if rc:
+        raise GgcatGpuError(f"read_sequences_file failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
     return text
 
 

@@ -13,8 +13,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libggcat_gb300.so")
-SOURCES = ["bucketing.cu", "merge.cu", "link.cu", "query.cu", "colors.cu", "hashes.cu", "capi.cu", "noalloc.cu"]
-HEADERS = ["common.cuh", "kernels.h"]
+SOURCES = ["bucketing.cu", "merge.cu", "link.cu", "query.cu", "colors.cu", "hashes.cu", "capi.cu", "noalloc.cu",
+           "input.cpp"]
+HEADERS = ["common.cuh", "kernels.h", "input.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +56,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

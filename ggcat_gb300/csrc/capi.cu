@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/ggcat_gb300.h"
+#include "input.h"
 #include "kernels.h"
 
 using namespace ggcat;
@@ -1076,110 +1077,6 @@ extern "C" int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, u
     return fetch_partial(ctx);
 }
 
-// ---------------------------------------------------------------------------
-// FASTA reader: the line state machine of SequencesReader::process_fasta
-// (crates/io/src/sequences_reader.rs:106-182) over 4 MiB read buffers
-// (LinesReader::process_lines, crates/io/src/lines_reader.rs:147-213).
-// ---------------------------------------------------------------------------
-namespace {
-struct FastaParser {
-    static constexpr size_t kBuf = 4u << 20;
-    std::vector<uint8_t> seq;
-    bool on_comment = false, new_line = true, ident = false;
-    int64_t copyback;
-    size_t flush_size;
-    uint8_t *out;
-    uint64_t cap, used = 0, pieces = 0;
-    uint8_t norm[256];
-
-    FastaParser(int64_t cb, uint8_t *o, uint64_t c) : copyback(cb), out(o), cap(c) {
-        size_t cbz = cb > 0 ? (size_t)cb * 2 : 0;
-        flush_size = std::max(kBuf, cbz);
-        for (int i = 0; i < 256; i++) norm[i] = 'N';
-        const char *v = "ACGT";
-        for (int i = 0; i < 4; i++) {
-            norm[(uint8_t)v[i]] = (uint8_t)v[i];
-            norm[(uint8_t)(v[i] | 0x20)] = (uint8_t)v[i];
-        }
-    }
-    void emit() {
-        if (out && used + seq.size() + 1 <= cap) {
-            for (size_t i = 0; i < seq.size(); i++) out[used + i] = norm[seq[i]];
-            out[used + seq.size()] = '\n';
-        }
-        used += seq.size() + 1;
-        pieces++;
-    }
-    void line(const uint8_t *l, size_t len, bool partial, bool finished) {
-        if (on_comment) {
-            on_comment = !partial;
-        } else if (finished || (new_line && len > 0 && l[0] == '>')) {
-            if (!seq.empty()) emit();
-            seq.clear();
-            ident = partial;
-        } else if (new_line && len > 0 && l[0] == ';') {
-            on_comment = true;
-        } else if (ident) {
-            if (!partial) ident = false;
-        } else {
-            seq.insert(seq.end(), l, l + len);
-        }
-        if (copyback >= 0 && seq.size() >= flush_size) {
-            emit();
-            size_t cb = (size_t)copyback;
-            std::vector<uint8_t> tail(seq.end() - (long)cb, seq.end());
-            seq.swap(tail);
-        }
-        new_line = !partial;
-    }
-    void run(const uint8_t *file, uint64_t n) {
-        for (uint64_t base = 0; base < n; base += kBuf) {
-            uint64_t blen = std::min<uint64_t>(kBuf, n - base);
-            const uint8_t *buf = file + base;
-            uint64_t p = 0;
-            for (;;) {
-                const uint8_t *nl = (const uint8_t *)memchr(buf + p, '\n', blen - p);
-                if (nl) {
-                    uint64_t pos = (uint64_t)(nl - buf), bpos = pos;
-                    if (bpos != p && buf[bpos - 1] == '\r') bpos--;
-                    line(buf + p, bpos - p, false, false);
-                    p = pos + 1;
-                } else {
-                    uint64_t l = blen - p;
-                    if (l > 0 && buf[blen - 1] == '\r') l--;
-                    if (l > 0) line(buf + p, l, true, false);
-                    break;
-                }
-            }
-        }
-        line(nullptr, 0, false, true);
-    }
-};
-}  // namespace
-
-extern "C" int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copyback, uint8_t *h_text,
-                                     uint64_t text_cap, uint64_t *text_len, uint64_t *n_pieces) {
-    if (!h_file && file_len) return GGCAT_GPU_EINVAL;
-    FastaParser fp(copyback, h_text, h_text ? text_cap : 0);
-    fp.run(h_file, file_len);
-    if (text_len) *text_len = fp.used;
-    if (n_pieces) *n_pieces = fp.pieces;
-    if (h_text && fp.used > text_cap) return GGCAT_GPU_EINVAL;
-    return GGCAT_GPU_OK;
-}
-
-static bool read_file(const char *path, std::vector<uint8_t> &out) {
-    FILE *f = fopen(path, "rb");
-    if (!f) return false;
-    fseek(f, 0, SEEK_END);
-    long sz = ftell(f);
-    fseek(f, 0, SEEK_SET);
-    out.resize(sz > 0 ? (size_t)sz : 0);
-    size_t got = sz > 0 ? fread(out.data(), 1, (size_t)sz, f) : 0;
-    fclose(f);
-    return got == out.size();
-}
-
 // buckets count heuristic of compute_stats_from_input_blocks (crates/io/src/lib.rs:67-140)
 static void bucket_counts_for(uint64_t bases, int *bbits, int *sbits) {
     const uint64_t MAX_BUCKET_SIZE = 1ull << 30, MIN_BUCKET_SIZE = 512ull << 10;
@@ -1206,17 +1103,13 @@ extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const 
     (void)threads_count;
     if (!ctx || !input_files || !output_file) return GGCAT_GPU_EINVAL;
     std::vector<uint8_t> text;
-    uint64_t est = 0;
     for (size_t i = 0; i < n_inputs; i++) {
-        std::vector<uint8_t> file;
-        if (!read_file(input_files[i], file)) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", input_files[i]);
-        est += file.size();
-        uint64_t need = 0, pieces = 0;
-        ggcat_gpu_fasta_parse(file.data(), file.size(), (int64_t)kmer_length - 1, nullptr, 0, &need, &pieces);
-        size_t o = text.size();
-        text.resize(o + need);
-        ggcat_gpu_fasta_parse(file.data(), file.size(), (int64_t)kmer_length - 1, text.data() + o, need, &need, &pieces);
+        // FASTA / FASTQ by extension, decompressed by the last one (input.cpp)
+        std::string err;
+        const int rc = ggcat::read_sequences(input_files[i], (int64_t)kmer_length - 1, text, nullptr, nullptr, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
     }
+    const uint64_t est = text.size();
     ggcat_gpu_params p{};
     p.k = (int)kmer_length;
     // compute_best_m (crates/utils/src/lib.rs:29-40) when minimizer_length == SIZE_MAX
@@ -1528,48 +1421,6 @@ extern "C" int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64
 // ---------------------------------------------------------------------------
 // file-level query: the uncoloured path of GGCATInstance::query_graph
 // ---------------------------------------------------------------------------
-namespace {
-// FASTA records as whole sequences (one query per record), bases normalised like
-// SequencesReader (ACGTacgt -> upper case, anything else -> N), each followed by '\n'
-bool read_fasta_records(const char *path, std::vector<uint8_t> &text, std::vector<uint64_t> &off,
-                        std::vector<uint64_t> &len) {
-    FILE *f = fopen(path, "rb");
-    if (!f) return false;
-    std::vector<uint8_t> data;
-    uint8_t buf[1 << 16];
-    size_t r;
-    while ((r = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + r);
-    fclose(f);
-    uint8_t norm[256];
-    for (int i = 0; i < 256; i++) norm[i] = 'N';
-    for (const char c : {'A', 'C', 'G', 'T'}) norm[(uint8_t)c] = norm[(uint8_t)(c | 0x20)] = (uint8_t)c;
-    bool in_seq = false;
-    size_t i = 0;
-    while (i < data.size()) {
-        size_t e = i;
-        while (e < data.size() && data[e] != '\n') e++;
-        size_t le = e;
-        if (le > i && data[le - 1] == '\r') le--;
-        if (le > i && data[i] == '>') {
-            if (in_seq) {
-                len.push_back(text.size() - off.back());
-                text.push_back('\n');
-            }
-            off.push_back(text.size());
-            in_seq = true;
-        } else if (in_seq && !(le > i && data[i] == ';')) {
-            for (size_t j = i; j < le; j++) text.push_back(norm[data[j]]);
-        }
-        i = e + 1;
-    }
-    if (in_seq) {
-        len.push_back(text.size() - off.back());
-        text.push_back('\n');
-    }
-    return true;
-}
-}  // namespace
-
 extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
                                           const char *output_prefix, int k, int forward_only, char *out_path,
                                           uint64_t out_cap) {
@@ -1579,29 +1430,24 @@ extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_
     // graph: the unitigs as text (records cut like the reference's reader, k-1 copyback)
     std::vector<uint8_t> graph;
     {
-        FILE *f = fopen(graph_fasta, "rb");
-        if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", graph_fasta);
-        std::vector<uint8_t> data;
-        uint8_t buf[1 << 16];
-        size_t r;
-        while ((r = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + r);
-        fclose(f);
-        uint64_t need = 0, pieces = 0;
-        int rc = ggcat_gpu_fasta_parse(data.data(), data.size(), k - 1, nullptr, 0, &need, &pieces);
-        if (rc) return rc;
-        graph.resize(need);
-        rc = ggcat_gpu_fasta_parse(data.data(), data.size(), k - 1, graph.data(), need, &need, &pieces);
-        if (rc) return rc;
+        std::string err;
+        const int rc = ggcat::read_sequences(graph_fasta, k - 1, graph, nullptr, nullptr, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
     }
     CK(cudaSetDevice(ctx->device));
     CK(ctx->qgraph.ensure(graph.size() + 64));
     if (!graph.empty()) CK(cudaMemcpy(ctx->qgraph.p, graph.data(), graph.size(), cudaMemcpyHostToDevice));
     int rc = ggcat_gpu_query_index(ctx, ctx->qgraph.p, graph.size(), k, nullptr);
     if (rc) return rc;
-    // queries: one per FASTA record, submitted in batches of bounded text size
+    // queries: one per record the reader emits (FASTA records with bases, every FASTQ
+    // record; never cut), submitted in batches of bounded text size
     std::vector<uint8_t> qtext;
     std::vector<uint64_t> qoff, qlen;
-    if (!read_fasta_records(query_fasta, qtext, qoff, qlen)) return fail(ctx, GGCAT_GPU_EIO, "cannot read %s", query_fasta);
+    {
+        std::string err;
+        rc = ggcat::read_sequences(query_fasta, -1, qtext, &qoff, &qlen, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+    }
     const uint64_t nq = qoff.size();
     std::vector<uint64_t> matched(nq, 0);
     const uint64_t kBatchBytes = 256ull << 20;

@@ -180,8 +180,25 @@ int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, uint64_t tex
 int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copyback, uint8_t *h_text,
                           uint64_t text_cap, uint64_t *text_len, uint64_t *n_pieces);
 
+/* FASTQ parsing (SequencesReader::process_fastq, crates/io/src/sequences_reader.rs:183-241):
+ * four-line records, one piece per record (never cut), the same text layout. */
+int ggcat_gpu_fastq_parse(const uint8_t *h_file, uint64_t file_len, uint8_t *h_text, uint64_t text_cap,
+                          uint64_t *text_len, uint64_t *n_records);
+
+/* One input file the way the reference's SequencesReader reads it
+ * (process_file_extended, sequences_reader.rs:56-104; LinesReader::read_binary_file,
+ * crates/io/src/lines_reader.rs:60-143): FASTA (fa, fasta, fna, ffn) or FASTQ (fq, fastq)
+ * by the extension chain, decompressed by the last extension (gz, lz4, bz2, xz, zst/zstd;
+ * the system's libz / liblz4 / libbz2 / liblzma / libzstd, opened at run time).  FASTA
+ * records are cut with `copyback` (< 0: whole records).  h_text = NULL queries the size; err
+ * (optional) receives the reason of a failure (GGCAT_GPU_EUNSUPPORTED: unknown file type or
+ * missing decompressor; GGCAT_GPU_EIO: unreadable or corrupt file). */
+int ggcat_gpu_read_sequences_file(const char *path, int64_t copyback, uint8_t *h_text, uint64_t text_cap,
+                                  uint64_t *text_len, uint64_t *n_pieces, char *err, uint64_t err_cap);
+
 /* Mirrors ggcat_build_from_files (crates/capi/src/lib.rs:58-139, api/src/lib.rs:217-322)
- * for the uncoloured, no-extra-elaboration case: reads FASTA files, builds the graph on
+ * for the uncoloured, no-extra-elaboration case: reads the input files like
+ * ggcat_gpu_read_sequences_file (FASTA / FASTQ, plain or compressed), builds the graph on
  * the GPU and writes the maximal unitigs as FASTA ">{id} LN:i:{len}" to output_file.
  * threads_count is accepted for interface parity.  Returns 0 or a negative code. */
 int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
@@ -220,7 +237,9 @@ int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
 
 /* Replaces ggcat_query_graph (crates/capi/src/lib.rs:324-380) / GGCATInstance::query_graph
  * (crates/api/src/lib.rs:325-382) for uncoloured graphs: indexes the unitigs of graph_fasta,
- * looks up every k-mer of every record of query_fasta and writes the querier's CSV
+ * looks up every k-mer of every record of query_fasta (both read like
+ * ggcat_gpu_read_sequences_file: FASTA / FASTQ, plain or compressed; one query per record
+ * the reader emits) and writes the querier's CSV
  * (query_index,matched_kmers,query_kmers,match_percentage; counters_sorting.rs:235-268) to
  * output_prefix, ".csv" appended when it has no extension; the written path is copied to
  * out_path.  Canonical k-mers, k <= 64. */

@@ -109,3 +109,54 @@ def canonical_unitig(seq: bytes, circular: bool, k: int) -> bytes:
 def canonical_set(unitigs, k: int) -> bytes:
     lines = sorted(canonical_unitig(s, c, k) for s, c in unitigs)
     return b"".join(l + b"\n" for l in lines)
+
+
+def _lines(data: bytes):
+    """LinesReader::process_lines over one buffer (crates/io/src/lines_reader.rs:147-213):
+    (line, partial) per line, '\\r' before the line end dropped; a last line without a
+    newline is partial."""
+    p = 0
+    while True:
+        e = data.find(b"\n", p)
+        if e < 0:
+            last = data[p:]
+            if last.endswith(b"\r"):
+                last = last[:-1]
+            if last:
+                yield last, True
+            return
+        line = data[p:e]
+        if line.endswith(b"\r") and e != p:
+            line = line[:-1]
+        yield line, False
+        p = e + 1
+
+
+def normalize(seq: bytes) -> bytes:
+    return bytes(c if c in b"ACGT" else (c - 32 if c in b"acgt" else ord("N")) for c in seq)
+
+
+def fastq_records(data: bytes) -> list[bytes]:
+    """SequencesReader::process_fastq (crates/io/src/sequences_reader.rs:183-241) for inputs
+    below the 4 MiB line buffer: the state cycles ident -> sequence -> quality; in the quality
+    state the first full line (the '+' line) is skipped without advancing, the next full line
+    emits the record (even with an empty sequence); at the end a non-empty sequence read so
+    far is emitted."""
+    out, state, skipped_plus, seq = [], 0, False, b""
+    for line, partial in _lines(data):
+        if state == 2:
+            if not skipped_plus:
+                if not partial:
+                    skipped_plus = True
+                continue
+            if not partial:
+                out.append(normalize(seq))
+                seq = b""
+                skipped_plus = False
+        elif state == 1:
+            seq += line
+        if not partial:
+            state = (state + 1) % 3
+    if seq:
+        out.append(normalize(seq))
+    return out
