@@ -6,7 +6,8 @@
 // subset id by ColorsMemMapWriter::get_id, crates/colors/src/colors_memmap_writer.rs:43-61).
 // A k-mer's colour set is the set of colours (input files) of all its occurrences, which
 // this phase computes globally instead of per bucket:
-//   1. the surviving k-mers of the merge go into one device table (key -> dense id),
+//   1. the surviving k-mers of the merge go into one device table (key -> id, the dump index
+//      of the entry that inserted the key),
 //   2. one pass over the input text sets bit `colour` of the k-mer's bitmap for every
 //      occurrence (the occurrence's colour is that of the sequence containing it),
 //   3. every bitmap is deduplicated into a subset table (exact: hash, then compare).
