@@ -144,6 +144,8 @@ void parse_fastq(const uint8_t *file, uint64_t n, Sink &sink) {
 
 // ---- decompression through the system libraries ----
 
+// the first of the names that loads; each decompressor keeps its handle in a function-local
+// static, so a library is opened once per process
 void *open_first(std::initializer_list<const char *> names) {
     for (const char *nm : names)
         if (void *h = dlopen(nm, RTLD_NOW | RTLD_LOCAL)) return h;
@@ -173,7 +175,7 @@ struct ZStream {
     unsigned long adler, reserved;
 };
 int inflate_gz(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std::string &err) {
-    void *h = open_first({"libz.so.1", "libz.so"});
+    static void *const h = open_first({"libz.so.1", "libz.so"});
     if (!h) return err = "gz input needs libz.so.1", GGCAT_GPU_EUNSUPPORTED;
     const char *(*version)() = nullptr;
     int (*init2)(ZStream *, int, const char *, int) = nullptr;
@@ -232,7 +234,7 @@ struct BzStream {
     void *bzalloc, *bzfree, *opaque;
 };
 int inflate_bz2(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std::string &err) {
-    void *h = open_first({"libbz2.so.1.0", "libbz2.so.1", "libbz2.so"});
+    static void *const h = open_first({"libbz2.so.1.0", "libbz2.so.1", "libbz2.so"});
     if (!h) return err = "bz2 input needs libbz2.so.1.0", GGCAT_GPU_EUNSUPPORTED;
     int (*init)(BzStream *, int, int) = nullptr;
     int (*dec)(BzStream *) = nullptr;
@@ -285,7 +287,7 @@ struct LzmaStream {
     int reserved_enum[2];
 };
 int inflate_xz(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std::string &err) {
-    void *h = open_first({"liblzma.so.5", "liblzma.so"});
+    static void *const h = open_first({"liblzma.so.5", "liblzma.so"});
     if (!h) return err = "xz input needs liblzma.so.5", GGCAT_GPU_EUNSUPPORTED;
     int (*decoder)(LzmaStream *, uint64_t, uint32_t) = nullptr;
     int (*code)(LzmaStream *, int) = nullptr;
@@ -326,7 +328,7 @@ struct ZstdOut {
     size_t size, pos;
 };
 int inflate_zstd(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std::string &err) {
-    void *h = open_first({"libzstd.so.1", "libzstd.so"});
+    static void *const h = open_first({"libzstd.so.1", "libzstd.so"});
     if (!h) return err = "zst input needs libzstd.so.1", GGCAT_GPU_EUNSUPPORTED;
     void *(*create)() = nullptr;
     size_t (*init)(void *) = nullptr;
@@ -366,7 +368,7 @@ int inflate_zstd(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std:
 
 // lz4 frame format (LZ4F_* of lz4frame.h), concatenated frames
 int inflate_lz4(const std::vector<uint8_t> &in, std::vector<uint8_t> &out, std::string &err) {
-    void *h = open_first({"liblz4.so.1", "liblz4.so"});
+    static void *const h = open_first({"liblz4.so.1", "liblz4.so"});
     if (!h) return err = "lz4 input needs liblz4.so.1", GGCAT_GPU_EUNSUPPORTED;
     size_t (*create)(void **, unsigned) = nullptr;
     size_t (*dec)(void *, void *, size_t *, const void *, size_t *, const void *) = nullptr;
