@@ -20,6 +20,7 @@ __all__ = [
     "GGCATConfig",
     "GGCATInstance",
     "ExtraElaboration",
+    "GfaVersion",
     "GpuContext",
     "GgcatGpuError",
     "Params",
@@ -34,13 +35,21 @@ __all__ = [
 
 
 class ExtraElaboration:
-    """crates/api/src/lib.rs:99-116 (only None is implemented on the device path)."""
+    """crates/api/src/lib.rs:99-116 (None and UnitigLinks are built; the matchtig family is
+    not)."""
 
     NONE = 0
     UNITIG_LINKS = 1
     GREEDY_MATCHTIGS = 2
     EULERTIGS = 3
     PATHTIGS = 4
+
+
+class GfaVersion:
+    """crates/api/src/lib.rs:69-72 (as the C API's gfa_output_version: 1, 2)."""
+
+    V1 = 1
+    V2 = 2
 
 
 @dataclass
@@ -93,13 +102,21 @@ class GGCATInstance:
         the C API's ``unwrap_or_default``)."""
         if colors or color_names:
             raise GgcatGpuError("coloured builds are not available on the device path yet")
-        if extra_elab != ExtraElaboration.NONE or gfa_output_version:
-            raise GgcatGpuError("extra elaborations / GFA output are outside the device path")
+        if extra_elab not in (ExtraElaboration.NONE, ExtraElaboration.UNITIG_LINKS):
+            raise GgcatGpuError("matchtigs, eulertigs and pathtigs are not built")
+        gfa = int(gfa_output_version or 0)
+        if gfa not in (0, GfaVersion.V1, GfaVersion.V2):
+            raise GgcatGpuError(f"gfa_output_version {gfa_output_version} is not 1 or 2")
         L = load()
         arr = (C.c_char_p * len(input_streams))(*[os.fsencode(p) for p in input_streams])
         m = (1 << 64) - 1 if minimizer_length is None else minimizer_length
-        rc = L.ggcat_gpu_build_from_files(self.ctx.h, arr, len(input_streams), os.fsencode(output_file), kmer_length,
-                                          threads_count, int(forward_only), m, min_multiplicity)
+        if extra_elab == ExtraElaboration.NONE and gfa == 0:
+            rc = L.ggcat_gpu_build_from_files(self.ctx.h, arr, len(input_streams), os.fsencode(output_file),
+                                              kmer_length, threads_count, int(forward_only), m, min_multiplicity)
+        else:  # the unitigs, then the links / GFA writer on the host
+            rc = L.ggcat_gpu_build_from_files_ex(self.ctx.h, arr, len(input_streams), os.fsencode(output_file),
+                                                 kmer_length, threads_count, int(forward_only), m, min_multiplicity,
+                                                 int(extra_elab), gfa)
         if rc != 0:
             msg = L.ggcat_gpu_last_error(self.ctx.h)
             if self.config.messages_callback:

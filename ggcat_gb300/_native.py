@@ -99,7 +99,10 @@ EXPORTED = [
     "ggcat_gpu_fasta_parse",
     "ggcat_gpu_fastq_parse",
     "ggcat_gpu_read_sequences_file",
+    "ggcat_gpu_unitig_links",
+    "ggcat_gpu_write_graph",
     "ggcat_gpu_build_from_files",
+    "ggcat_gpu_build_from_files_ex",
     "ggcat_gpu_colors",
     "ggcat_gpu_kmer_subsets_copy",
     "ggcat_gpu_subsets_copy",
@@ -157,7 +160,11 @@ def load(build: bool = True):
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
     L.ggcat_gpu_fastq_parse.argtypes = [P, u64, P, u64, pu64, pu64]
     L.ggcat_gpu_read_sequences_file.argtypes = [C.c_char_p, C.c_int64, P, u64, pu64, pu64, C.c_char_p, u64]
+    L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
+    L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
+    L.ggcat_gpu_build_from_files_ex.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz,
+                                                C.c_int, C.c_int]
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
     L.ggcat_gpu_kmer_hashes.argtypes = [P, P, u64, C.c_int, C.c_int, P, P]
     L.ggcat_gpu_colors.argtypes = [P, P, P, u64, C.c_uint32, P]
@@ -420,6 +427,39 @@ def read_sequences_file(path: str, copyback: int = -1):
     if rc:
         raise GgcatGpuError(f"read_sequences_file failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
     return text
+
+
+def unitig_links(bases: np.ndarray, off: np.ndarray, ln: np.ndarray, k: int):
+    """Maximal-unitig links: (list_off, other, overlap, flags); list 2i = links from unitig
+    i's end, 2i + 1 = from its beginning; flags bit 0 flip_current, bit 1 flip_other."""
+    L = load()
+    b = np.ascontiguousarray(bases, np.uint8)
+    o = np.ascontiguousarray(off, np.uint64)
+    n_ = np.ascontiguousarray(ln, np.uint64)
+    n = len(o)
+    lo = np.zeros(2 * n + 1, np.uint64)
+    cnt = C.c_uint64()
+    rc = L.ggcat_gpu_unitig_links(_ptr(b), _ptr(o), _ptr(n_), n, k, _ptr(lo), None, None, None, 0, C.byref(cnt))
+    if rc:
+        raise GgcatGpuError(f"unitig_links failed ({_ERRORS.get(rc, rc)})")
+    other = np.zeros(cnt.value, np.uint64)
+    overlap = np.zeros(cnt.value, np.uint64)
+    flags = np.zeros(cnt.value, np.uint8)
+    rc = L.ggcat_gpu_unitig_links(_ptr(b), _ptr(o), _ptr(n_), n, k, _ptr(lo), _ptr(other), _ptr(overlap),
+                                  _ptr(flags), cnt.value, C.byref(cnt))
+    if rc:
+        raise GgcatGpuError(f"unitig_links failed ({_ERRORS.get(rc, rc)})")
+    return lo, other, overlap, flags
+
+
+def write_graph(unitigs_fasta: str, output_file: str, k: int, unitig_links: bool = False, gfa_version: int = 0):
+    """A FASTA of unitigs rewritten as FASTA with link annotations or as GFA v1 / v2."""
+    L = load()
+    err = C.create_string_buffer(512)
+    rc = L.ggcat_gpu_write_graph(os.fsencode(unitigs_fasta), os.fsencode(output_file), k, int(unitig_links),
+                                 gfa_version, err, 512)
+    if rc:
+        raise GgcatGpuError(f"write_graph failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
 
 
 def unitig_lines(bases: np.ndarray, off: np.ndarray, ln: np.ndarray) -> bytes:

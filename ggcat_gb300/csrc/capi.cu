@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/ggcat_gb300.h"
+#include "graph_out.h"
 #include "input.h"
 #include "kernels.h"
 
@@ -1137,6 +1138,36 @@ extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const 
         fputc('\n', f);
     }
     fclose(f);
+    return GGCAT_GPU_OK;
+}
+
+// ggcat_build_from_files with its extra_elab and gfa_output_version arguments
+// (crates/capi/src/lib.rs:58-139): the unitigs are built to a temporary FASTA, which the
+// links / GFA writer of graph_out.cpp rewrites into output_file
+extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
+                                             const char *output_file, size_t kmer_length, size_t threads_count,
+                                             int forward_only, size_t minimizer_length, size_t min_multiplicity,
+                                             int extra_elab, int gfa_output_version) {
+    if (!ctx || !output_file) return GGCAT_GPU_EINVAL;
+    if (extra_elab < 0 || extra_elab > 4 || gfa_output_version < 0 || gfa_output_version > 2)
+        return fail(ctx, GGCAT_GPU_EINVAL, "extra_elab %d / gfa_output_version %d out of range", extra_elab,
+                    gfa_output_version);
+    if (extra_elab >= 2)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "matchtigs, eulertigs and pathtigs are not built");
+    if (extra_elab == 0 && gfa_output_version == 0)
+        return ggcat_gpu_build_from_files(ctx, input_files, n_inputs, output_file, kmer_length, threads_count,
+                                          forward_only, minimizer_length, min_multiplicity);
+    const std::string tmp = std::string(output_file) + ".unitigs.tmp.fa";
+    int rc = ggcat_gpu_build_from_files(ctx, input_files, n_inputs, tmp.c_str(), kmer_length, threads_count,
+                                        forward_only, minimizer_length, min_multiplicity);
+    if (rc) {
+        std::remove(tmp.c_str());
+        return rc;
+    }
+    std::string err;
+    rc = ggcat::write_graph(tmp.c_str(), output_file, (int)kmer_length, extra_elab == 1, gfa_output_version, err);
+    std::remove(tmp.c_str());
+    if (rc) return fail(ctx, rc, "%s", err.c_str());
     return GGCAT_GPU_OK;
 }
 

@@ -196,6 +196,25 @@ int ggcat_gpu_fastq_parse(const uint8_t *h_file, uint64_t file_len, uint8_t *h_t
 int ggcat_gpu_read_sequences_file(const char *path, int64_t copyback, uint8_t *h_text, uint64_t text_cap,
                                   uint64_t *text_len, uint64_t *n_pieces, char *err, uint64_t err_cap);
 
+/* Maximal-unitig links (build_maximal_unitigs_links,
+ * crates/assembler_pipeline/src/maximal_unitig_links.rs:55-417) of n unitigs
+ * bases[off[i], off[i] + len[i]) (ACGT, len >= k, k <= 64): list 2i = links from unitig i's
+ * end, list 2i + 1 = from its beginning, entries [list_off[l], list_off[l + 1]) (list_off:
+ * 2n + 1 entries).  Per link: the other unitig, the start of the shared (k-1)-mer in it, flags
+ * bit 0 = flip_current, bit 1 = flip_other.  Pass other = NULL to query *n_links. */
+int ggcat_gpu_unitig_links(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k,
+                           uint64_t *list_off, uint64_t *other, uint64_t *overlap, uint8_t *flags, uint64_t cap,
+                           uint64_t *n_links);
+
+/* Rewrites a FASTA of unitigs (">i LN:i:len" records in index order, as ggcat_gpu_build_from_files
+ * writes them) as FASTA with the links in the headers (" L:+:j:-", gfa_version = 0,
+ * unitig_links = 1) or as GFA v1 / v2 (gfa_version 1 / 2; L / E lines when unitig_links): the
+ * output of ExtraElaboration::UnitigLinks and of gfa_output_version in
+ * GGCATInstance::build_graph (crates/api/src/lib.rs:217-322; writers in
+ * crates/sequence_output/src/structured_sequences/{fasta,gfa}.rs). */
+int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *output_file, int k, int unitig_links,
+                          int gfa_version, char *err, uint64_t err_cap);
+
 /* Mirrors ggcat_build_from_files (crates/capi/src/lib.rs:58-139, api/src/lib.rs:217-322)
  * for the uncoloured, no-extra-elaboration case: reads the input files like
  * ggcat_gpu_read_sequences_file (FASTA / FASTQ, plain or compressed), builds the graph on
@@ -204,6 +223,16 @@ int ggcat_gpu_read_sequences_file(const char *path, int64_t copyback, uint8_t *h
 int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);
+
+/* ggcat_build_from_files with its last two arguments (crates/capi/src/lib.rs:58-139):
+ * extra_elab 0 none, 1 unitig links (L: annotations, or L / E lines in GFA); 2-4
+ * (matchtigs, eulertigs, pathtigs) return GGCAT_GPU_EUNSUPPORTED; gfa_output_version 0 FASTA,
+ * 1 GFA v1, 2 GFA v2.  The unitigs go through a temporary "<output_file>.unitigs.tmp.fa" that
+ * ggcat_gpu_write_graph rewrites. */
+int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
+                                  const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
+                                  size_t minimizer_length, size_t min_multiplicity, int extra_elab,
+                                  int gfa_output_version);
 
 /* ---- colour subsets ----
  * Replaces the per-k-mer colour sets and subset dedup of MultipleColorsManager

@@ -160,3 +160,37 @@ def fastq_records(data: bytes) -> list[bytes]:
     if seq:
         out.append(normalize(seq))
     return out
+
+
+def unitig_links(unitigs: list[bytes], k: int):
+    """build_maximal_unitigs_links (crates/assembler_pipeline/src/maximal_unitig_links.rs:55-417)
+    restated over strings: per unitig (links from its end, links from its beginning), each a
+    list of (other, overlap start, flip_current, flip_other) ordered by the other index.
+    is_forward of a (k-1)-mer = it is below its reverse complement; for one equal to its
+    reverse complement the is_forward entry's list is kept when it is not empty."""
+    w = k - 1
+    groups = {}
+    for i, u in enumerate(unitigs):
+        first, last = u[:w], u[len(u) - w:]
+        for pos, x, ov in ((0, first, 0), (1, last, len(u) - w)):
+            r = rc(x)
+            fwd = x < r
+            d = fwd if pos == 0 else (not fwd)
+            key = min(x, r)
+            groups.setdefault(key, []).append((i, pos, ov, d, True))
+            if x == r:
+                groups[key].append((i, pos, ov, not d, False))
+    slots = [[None, None] for _ in unitigs]  # [end, beginning]
+    for ents in groups.values():
+        if len(ents) < 2:
+            continue
+        ents.sort(key=lambda e: (e[0], e[1], not e[4]))
+        for i, pos, ov, d, primary in ents:
+            lst = [(j, jov, pos == 0, jpos == 1) for j, jpos, jov, jd, _ in ents if jd != d]
+            if not lst:
+                continue
+            s = 1 if pos == 0 else 0
+            cur = slots[i][s]
+            if cur is None or (primary and not cur[1]):
+                slots[i][s] = (lst, primary)
+    return [tuple(s[0] if s else [] for s in sl) for sl in slots]
