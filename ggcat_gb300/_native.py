@@ -99,6 +99,7 @@ EXPORTED = [
     "ggcat_gpu_fasta_parse",
     "ggcat_gpu_fastq_parse",
     "ggcat_gpu_read_sequences_file",
+    "ggcat_gpu_read_sequences_files",
     "ggcat_gpu_unitig_links",
     "ggcat_gpu_write_graph",
     "ggcat_gpu_build_from_files",
@@ -160,6 +161,8 @@ def load(build: bool = True):
     L.ggcat_gpu_fasta_parse.argtypes = [P, u64, C.c_int64, P, u64, pu64, pu64]
     L.ggcat_gpu_fastq_parse.argtypes = [P, u64, P, u64, pu64, pu64]
     L.ggcat_gpu_read_sequences_file.argtypes = [C.c_char_p, C.c_int64, P, u64, pu64, pu64, C.c_char_p, u64]
+    L.ggcat_gpu_read_sequences_files.argtypes = [C.POINTER(C.c_char_p), u64, C.c_int64, C.c_int, P, u64, pu64,
+                                                 C.c_char_p, u64]
     L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
     L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
@@ -426,6 +429,23 @@ def read_sequences_file(path: str, copyback: int = -1):
                                          C.byref(n), err, 512)
     if rc:
         raise GgcatGpuError(f"read_sequences_file failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
+    return text
+
+
+def read_sequences_files(paths, copyback: int = -1, threads: int = 4):
+    """Several files read on `threads` host threads, concatenated in input order."""
+    L = load()
+    arr = (C.c_char_p * len(paths))(*[os.fsencode(p) for p in paths])
+    need = C.c_uint64()
+    err = C.create_string_buffer(512)
+    rc = L.ggcat_gpu_read_sequences_files(arr, len(paths), copyback, threads, None, 0, C.byref(need), err, 512)
+    if rc:
+        raise GgcatGpuError(f"read_sequences_files failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
+    text = np.zeros(need.value, np.uint8)
+    rc = L.ggcat_gpu_read_sequences_files(arr, len(paths), copyback, threads, _ptr(text), need.value, C.byref(need),
+                                          err, 512)
+    if rc:
+        raise GgcatGpuError(f"read_sequences_files failed ({_ERRORS.get(rc, rc)}): {err.value.decode()}")
     return text
 
 

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <cmath>
 #include <vector>
@@ -1101,13 +1102,15 @@ static void bucket_counts_for(uint64_t bases, int *bbits, int *sbits) {
 extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                           const char *output_file, size_t kmer_length, size_t threads_count,
                                           int forward_only, size_t minimizer_length, size_t min_multiplicity) {
-    (void)threads_count;
     if (!ctx || !input_files || !output_file) return GGCAT_GPU_EINVAL;
     std::vector<uint8_t> text;
-    for (size_t i = 0; i < n_inputs; i++) {
-        // FASTA / FASTQ by extension, decompressed by the last one (input.cpp)
+    {
+        // FASTA / FASTQ by extension, decompressed by the last one, files on threads_count host
+        // threads (all of them when 0) and concatenated in input order (input.cpp)
+        const int nt = threads_count > 0 ? (int)std::min<size_t>(threads_count, 1024)
+                                         : (int)std::max(1u, std::thread::hardware_concurrency());
         std::string err;
-        const int rc = ggcat::read_sequences(input_files[i], (int64_t)kmer_length - 1, text, nullptr, nullptr, err);
+        const int rc = ggcat::read_sequences_files(input_files, n_inputs, (int64_t)kmer_length - 1, nt, text, err);
         if (rc) return fail(ctx, rc, "%s", err.c_str());
     }
     const uint64_t est = text.size();

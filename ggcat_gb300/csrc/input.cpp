@@ -15,6 +15,8 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -489,7 +491,59 @@ int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &tex
     return rc;
 }
 
+int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
+                         std::string &err) {
+    // each file into its own buffer on a pool of threads (files are claimed in order), then
+    // concatenated in input order: the same text as reading them one after another
+    std::vector<std::vector<uint8_t>> parts(n);
+    std::vector<std::string> errs(n);
+    std::vector<int> rcs(n, GGCAT_GPU_OK);
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t i = next++; i < n; i = next++)
+            rcs[i] = read_sequences(paths[i], copyback, parts[i], nullptr, nullptr, errs[i]);
+    };
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(n, threads > 0 ? (size_t)threads : 1));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto &th : pool) th.join();
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (rcs[i]) return err = errs[i], rcs[i];
+        total += parts[i].size();
+    }
+    text.clear();
+    text.reserve(total);
+    for (auto &p : parts) {
+        text.insert(text.end(), p.begin(), p.end());
+        std::vector<uint8_t>().swap(p);
+    }
+    return GGCAT_GPU_OK;
+}
+
 }  // namespace ggcat
+
+extern "C" int ggcat_gpu_read_sequences_files(const char *const *paths, uint64_t n, int64_t copyback, int threads,
+                                              uint8_t *h_text, uint64_t text_cap, uint64_t *text_len, char *err,
+                                              uint64_t err_cap) {
+    if (n && !paths) return GGCAT_GPU_EINVAL;
+    std::string e;
+    std::vector<uint8_t> text;
+    const int rc = ggcat::read_sequences_files(paths, (size_t)n, copyback, threads, text, e);
+    if (err && err_cap) {
+        const size_t m = std::min<size_t>(e.size(), err_cap - 1);
+        memcpy(err, e.data(), m);
+        err[m] = 0;
+    }
+    if (rc) return rc;
+    if (text_len) *text_len = text.size();
+    if (h_text) {
+        if (text.size() > text_cap) return GGCAT_GPU_EINVAL;
+        memcpy(h_text, text.data(), text.size());
+    }
+    return GGCAT_GPU_OK;
+}
 
 extern "C" int ggcat_gpu_fasta_parse(const uint8_t *h_file, uint64_t file_len, int64_t copyback, uint8_t *h_text,
                                      uint64_t text_cap, uint64_t *text_len, uint64_t *n_pieces) {

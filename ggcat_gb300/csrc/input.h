@@ -21,5 +21,8 @@ int parse_sequences(const uint8_t *data, uint64_t n, int format, int64_t copybac
 // read + parse, appending to text (off, len: pieces, offsets into text)
 int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &text, std::vector<uint64_t> *off,
                    std::vector<uint64_t> *len, std::string &err);
+// several files on up to `threads` threads, concatenated in input order into text
+int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
+                         std::string &err);
 
 }  // namespace ggcat

@@ -196,6 +196,13 @@ int ggcat_gpu_fastq_parse(const uint8_t *h_file, uint64_t file_len, uint8_t *h_t
 int ggcat_gpu_read_sequences_file(const char *path, int64_t copyback, uint8_t *h_text, uint64_t text_cap,
                                   uint64_t *text_len, uint64_t *n_pieces, char *err, uint64_t err_cap);
 
+/* Several input files read like ggcat_gpu_read_sequences_file on up to `threads` host
+ * threads (the reference's reader threads) and concatenated in input order: the text of
+ * ggcat_gpu_build_from_files.  h_text = NULL queries the size. */
+int ggcat_gpu_read_sequences_files(const char *const *paths, uint64_t n, int64_t copyback, int threads,
+                                   uint8_t *h_text, uint64_t text_cap, uint64_t *text_len, char *err,
+                                   uint64_t err_cap);
+
 /* Maximal-unitig links (build_maximal_unitigs_links,
  * crates/assembler_pipeline/src/maximal_unitig_links.rs:55-417) of n unitigs
  * bases[off[i], off[i] + len[i]) (ACGT, len >= k, k <= 64): list 2i = links from unitig i's
@@ -219,7 +226,7 @@ int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *output_file, in
  * for the uncoloured, no-extra-elaboration case: reads the input files like
  * ggcat_gpu_read_sequences_file (FASTA / FASTQ, plain or compressed), builds the graph on
  * the GPU and writes the maximal unitigs as FASTA ">{id} LN:i:{len}" to output_file.
- * threads_count is accepted for interface parity.  Returns 0 or a negative code. */
+ * threads_count = host threads reading the input files (0: all).  Returns 0 or a negative code. */
 int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);

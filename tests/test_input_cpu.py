@@ -159,3 +159,22 @@ def test_extension_chain(tmp_path):
     path = tmp_path / "x.fa.backup.gz"
     path.write_bytes(gzip.compress(data))
     assert _native.read_sequences_file(str(path), 30).tobytes() == _native.fasta_parse(data, 30).tobytes()
+
+
+@pytest.mark.parametrize("threads", [1, 3, 16])
+def test_many_files_in_input_order(tmp_path, threads):
+    """Files read on several threads are concatenated in input order, like one after another."""
+    paths, exp = [], b""
+    for i in range(11):
+        kind = i % 3
+        data = _fasta_bytes(seed=100 + i, n=5) if kind else _fastq_bytes(seed=200 + i, n=20)
+        name = f"f{i}." + ("fa" if kind else "fq") + (".gz" if i % 2 else "")
+        p = tmp_path / name
+        p.write_bytes(gzip.compress(data) if i % 2 else data)
+        paths.append(str(p))
+        exp += _native.read_sequences_file(str(p), 30).tobytes()
+    assert _native.read_sequences_files(paths, 30, threads).tobytes() == exp
+    bad = paths[:4] + [str(tmp_path / "missing.fa")] + paths[4:]
+    with pytest.raises(_native.GgcatGpuError, match="EIO"):
+        _native.read_sequences_files(bad, 30, threads)
+
