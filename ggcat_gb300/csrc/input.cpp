@@ -58,11 +58,15 @@ struct Sink {
 
 // The line splitter of LinesReader over 4 MiB buffers: a line that crosses a buffer end is
 // delivered in parts (partial = true), '\r' before '\n' and at a buffer end is dropped.
+// [s, e) of the file is split into the buffers the whole file would be read in (file
+// positions that are multiples of 4 MiB), so a range that starts at a line start gives the
+// same callbacks as the whole-file pass; the final (finished) callback closes the range.
 template <typename F>
-void for_each_line(const uint8_t *file, uint64_t n, F &&line) {
+void for_each_line(const uint8_t *file, uint64_t s, uint64_t e, F &&line) {
     constexpr uint64_t kBuf = 4u << 20;
-    for (uint64_t base = 0; base < n; base += kBuf) {
-        const uint64_t blen = std::min<uint64_t>(kBuf, n - base);
+    for (uint64_t base = s; base < e;) {
+        const uint64_t bend = std::min<uint64_t>(e, (base / kBuf + 1) * kBuf);
+        const uint64_t blen = bend - base;
         const uint8_t *buf = file + base;
         uint64_t p = 0;
         for (;;) {
@@ -80,18 +84,23 @@ void for_each_line(const uint8_t *file, uint64_t n, F &&line) {
                 break;
             }
         }
+        base = bend;
     }
     line(nullptr, 0, false, true);
+}
+template <typename F>
+void for_each_line(const uint8_t *file, uint64_t n, F &&line) {
+    for_each_line(file, 0, n, line);
 }
 
 // process_fasta: records from '>' lines, ';' comment lines skipped, empty records dropped;
 // with copyback >= 0 a record reaching max(4 MiB, 2 copyback) bases is emitted and restarted
 // from its last copyback bases.
-void parse_fasta(const uint8_t *file, uint64_t n, int64_t copyback, Sink &sink) {
+void parse_fasta(const uint8_t *file, uint64_t s, uint64_t e, int64_t copyback, Sink &sink) {
     const size_t flush = std::max<size_t>(4u << 20, copyback > 0 ? (size_t)copyback * 2 : 0);
     std::vector<uint8_t> seq;
     bool on_comment = false, new_line = true, ident = false;
-    for_each_line(file, n, [&](const uint8_t *l, size_t len, bool partial, bool finished) {
+    for_each_line(file, s, e, [&](const uint8_t *l, size_t len, bool partial, bool finished) {
         if (on_comment) {
             on_comment = !partial;
         } else if (finished || (new_line && len > 0 && l[0] == '>')) {
@@ -438,9 +447,17 @@ int read_input_file(const char *path, std::vector<uint8_t> &out, std::string &er
     FILE *f = fopen(path, "rb");
     if (!f) return err = std::string("cannot read ") + path, GGCAT_GPU_EIO;
     std::vector<uint8_t> raw;
+    // one read of the whole file when its size is known (a regular file), else in pieces
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long sz = ftell(f);
+        if (sz > 0 && fseek(f, 0, SEEK_SET) == 0) {
+            raw.resize((size_t)sz);
+            raw.resize(fread(raw.data(), 1, raw.size(), f));
+        }
+    }
     uint8_t buf[1 << 16];
     size_t r;
-    while ((r = fread(buf, 1, sizeof buf, f)) > 0) raw.insert(raw.end(), buf, buf + r);
+    while ((r = fread(buf, 1, sizeof buf, f)) > 0) raw.insert(raw.end(), buf, buf + r);  // the rest, if any
     const bool bad = ferror(f) != 0;
     fclose(f);
     if (bad) return err = std::string("cannot read ") + path, GGCAT_GPU_EIO;
@@ -463,7 +480,7 @@ int parse_sequences(const uint8_t *data, uint64_t n, int format, int64_t copybac
     sink.off = off;
     sink.len = len;
     if (format == kFormatFastq) parse_fastq(data, n, sink);
-    else if (format == kFormatFasta) parse_fasta(data, n, copyback, sink);
+    else if (format == kFormatFasta) parse_fasta(data, 0, n, copyback, sink);
     else return GGCAT_GPU_EINVAL;
     if (text_len) *text_len = sink.used;
     if (n_pieces) *n_pieces = sink.pieces;
@@ -471,14 +488,87 @@ int parse_sequences(const uint8_t *data, uint64_t n, int format, int64_t copybac
     return GGCAT_GPU_OK;
 }
 
+namespace {
+
+bool has_comment_line(const uint8_t *data, uint64_t n) {
+    if (n && data[0] == ';') return true;
+    for (const uint8_t *p = data; (p = (const uint8_t *)memchr(p, ';', (size_t)(data + n - p))) != nullptr; p++)
+        if (p > data && p[-1] == '\n') return true;
+    return false;
+}
+
+// FASTA parsed in ranges on threads, appended to text: the ranges start at record starts
+// ('>' after '\n') near equal shares of the file and keep the whole-file line buffers, so the
+// output is the whole-file parse's byte for byte.  Not used when the file has a ';' comment
+// line: after one the reference skips lines across records.
+void parse_fasta_threads(const uint8_t *data, uint64_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
+                         std::vector<uint64_t> *off, std::vector<uint64_t> *len) {
+    std::vector<uint64_t> cuts{0};
+    for (int t = 1; t < threads; t++) {
+        uint64_t q = std::max<uint64_t>(cuts.back() + 1, n * (uint64_t)t / (uint64_t)threads);
+        for (; q < n; q++) {
+            const uint8_t *gt = (const uint8_t *)memchr(data + q, '>', (size_t)(n - q));
+            if (!gt) {
+                q = n;
+                break;
+            }
+            q = (uint64_t)(gt - data);
+            if (q > 0 && data[q - 1] == '\n') break;
+        }
+        if (q >= n) break;
+        cuts.push_back(q);
+    }
+    cuts.push_back(n);
+    const size_t nc = cuts.size() - 1;
+    // sizes of every range, then each range parsed straight into its place in text
+    std::vector<uint64_t> at(nc + 1, 0);
+    std::vector<std::vector<uint64_t>> offs(nc), lens(nc);
+    const uint64_t base = text.size();
+    auto run = [&](auto &&body) {
+        std::atomic<size_t> next{0};
+        auto work = [&]() {
+            for (size_t c = next++; c < nc; c = next++) body(c);
+        };
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < std::min<size_t>(nc, (size_t)threads); t++) pool.emplace_back(work);
+        work();
+        for (auto &th : pool) th.join();
+    };
+    run([&](size_t c) {
+        Sink count{nullptr, 0};
+        parse_fasta(data, cuts[c], cuts[c + 1], copyback, count);
+        at[c + 1] = count.used;
+    });
+    for (size_t c = 0; c < nc; c++) at[c + 1] += at[c];
+    text.resize(base + at[nc]);
+    run([&](size_t c) {
+        Sink fill{text.data() + base + at[c], at[c + 1] - at[c]};
+        fill.off = off ? &offs[c] : nullptr;
+        fill.len = len ? &lens[c] : nullptr;
+        parse_fasta(data, cuts[c], cuts[c + 1], copyback, fill);
+    });
+    for (size_t c = 0; c < nc; c++) {
+        if (off)
+            for (uint64_t v : offs[c]) off->push_back(base + at[c] + v);
+        if (len) len->insert(len->end(), lens[c].begin(), lens[c].end());
+    }
+}
+
+}  // namespace
+
 int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &text, std::vector<uint64_t> *off,
-                   std::vector<uint64_t> *len, std::string &err) {
+                   std::vector<uint64_t> *len, std::string &err, int threads) {
     const int format = sequence_format(path);
     if (format == kFormatUnknown)
         return err = std::string("cannot recognize the file type of ") + path, GGCAT_GPU_EUNSUPPORTED;
     std::vector<uint8_t> data;
     int rc = read_input_file(path, data, err);
     if (rc) return rc;
+    if (format == kFormatFasta && threads > 1 && data.size() >= (16u << 20) &&
+        !has_comment_line(data.data(), data.size())) {
+        parse_fasta_threads(data.data(), data.size(), copyback, threads, text, off, len);
+        return GGCAT_GPU_OK;
+    }
     uint64_t need = 0, pieces = 0;
     parse_sequences(data.data(), data.size(), format, copyback, nullptr, 0, &need, &pieces, nullptr, nullptr);
     const size_t o = text.size();
@@ -499,9 +589,11 @@ int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, i
     std::vector<std::string> errs(n);
     std::vector<int> rcs(n, GGCAT_GPU_OK);
     std::atomic<size_t> next{0};
+    // threads left over by fewer files than threads parse inside the files
+    const int per_file = std::max(1, (threads > 0 ? threads : 1) / (int)std::max<size_t>(1, n));
     auto work = [&]() {
         for (size_t i = next++; i < n; i = next++)
-            rcs[i] = read_sequences(paths[i], copyback, parts[i], nullptr, nullptr, errs[i]);
+            rcs[i] = read_sequences(paths[i], copyback, parts[i], nullptr, nullptr, errs[i], per_file);
     };
     const size_t nt = std::max<size_t>(1, std::min<size_t>(n, threads > 0 ? (size_t)threads : 1));
     std::vector<std::thread> pool;

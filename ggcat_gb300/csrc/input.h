@@ -18,9 +18,10 @@ int read_input_file(const char *path, std::vector<uint8_t> &out, std::string &er
 // piece's offset and length
 int parse_sequences(const uint8_t *data, uint64_t n, int format, int64_t copyback, uint8_t *h_text, uint64_t cap,
                     uint64_t *text_len, uint64_t *n_pieces, std::vector<uint64_t> *off, std::vector<uint64_t> *len);
-// read + parse, appending to text (off, len: pieces, offsets into text)
+// read + parse, appending to text (off, len: pieces, offsets into text); FASTA files of
+// 16 MiB or more are parsed on `threads` threads (the same output)
 int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &text, std::vector<uint64_t> *off,
-                   std::vector<uint64_t> *len, std::string &err);
+                   std::vector<uint64_t> *len, std::string &err, int threads = 1);
 // several files on up to `threads` threads, concatenated in input order into text
 int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
                          std::string &err);

@@ -178,3 +178,35 @@ def test_many_files_in_input_order(tmp_path, threads):
     with pytest.raises(_native.GgcatGpuError, match="EIO"):
         _native.read_sequences_files(bad, 30, threads)
 
+
+
+def _big_fasta(seed, crlf=False, comment=False):
+    rng = np.random.default_rng(seed)
+    parts = []
+    total = 0
+    i = 0
+    while total < 20 << 20:
+        n = int(rng.choice([200, 5_000, 300_000, 5_000_000]))  # some records above the 4 MiB buffer
+        s = synth.random_genome(n, rng).tobytes()
+        eol = b"\r\n" if crlf else b"\n"
+        width = int(rng.choice([60, 80, 1 << 30]))
+        body = eol.join(s[j:j + width] for j in range(0, len(s), width))
+        parts.append(b">rec%d len=%d" % (i, n) + eol + body + eol)
+        if comment and i == 3:
+            parts.append(b";a comment" + eol)
+        total += len(parts[-1])
+        i += 1
+    return b"".join(parts)
+
+
+@pytest.mark.parametrize("crlf,comment", [(False, False), (True, False), (False, True)])
+@pytest.mark.parametrize("threads", [2, 5, 16])
+def test_large_fasta_parsed_on_threads_equals_whole_file_parse(tmp_path, crlf, comment, threads):
+    """A FASTA file of 16 MiB or more is parsed in record-aligned ranges on threads; the text
+    (pieces cut with the copyback across the 4 MiB buffers) equals the whole-file parse.  A
+    file with a ';' comment line is parsed whole."""
+    data = _big_fasta(crlf * 2 + comment, crlf, comment)
+    p = tmp_path / "big.fa"
+    p.write_bytes(data)
+    got = _native.read_sequences_files([str(p)], 30, threads).tobytes()
+    assert got == _native.fasta_parse(data, 30).tobytes()
