@@ -56,7 +56,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart", "-ldl"]
+    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
