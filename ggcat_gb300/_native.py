@@ -102,6 +102,7 @@ EXPORTED = [
     "ggcat_gpu_read_sequences_files",
     "ggcat_gpu_unitig_links",
     "ggcat_gpu_write_graph",
+    "ggcat_gpu_dump_unitigs",
     "ggcat_gpu_build_from_files",
     "ggcat_gpu_build_from_files_ex",
     "ggcat_gpu_colors",
@@ -125,6 +126,10 @@ _lib = None
 
 def library_path() -> str:
     return _build.LIB
+
+
+# ggcat_gpu_dump_fn: (fn_ctx, seq, len, colors, n_colors, same_colors)
+DUMP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int)
 
 
 def load(build: bool = True):
@@ -165,6 +170,7 @@ def load(build: bool = True):
                                                  C.c_char_p, u64]
     L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
     L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
+    L.ggcat_gpu_dump_unitigs.argtypes = [C.c_char_p, C.c_int, C.c_int, DUMP_FN, C.c_void_p]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_build_from_files_ex.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz,
                                                 C.c_int, C.c_int]
@@ -470,6 +476,21 @@ def unitig_links(bases: np.ndarray, off: np.ndarray, ln: np.ndarray, k: int):
     if rc:
         raise GgcatGpuError(f"unitig_links failed ({_ERRORS.get(rc, rc)})")
     return lo, other, overlap, flags
+
+
+def dump_unitigs(graph_input: str, k: int) -> list:
+    """ggcat_dump_unitigs for an uncoloured graph: the pieces of the graph FASTA as bytes."""
+    L = load()
+    out = []
+
+    def cb(_ctx, seq, n, _colors, _nc, _same):
+        out.append(C.string_at(seq, n))
+
+    fn = DUMP_FN(cb)
+    rc = L.ggcat_gpu_dump_unitigs(os.fsencode(graph_input), k, 0, fn, None)
+    if rc:
+        raise GgcatGpuError(f"dump_unitigs failed ({_ERRORS.get(rc, rc)})")
+    return out
 
 
 def write_graph(unitigs_fasta: str, output_file: str, k: int, unitig_links: bool = False, gfa_version: int = 0):

@@ -242,3 +242,16 @@ extern "C" int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *outp
     }
     return rc;
 }
+
+extern "C" int ggcat_gpu_dump_unitigs(const char *graph_input, int k, int colors, ggcat_gpu_dump_fn fn, void *fn_ctx) {
+    if (!graph_input || !fn || k < 2) return GGCAT_GPU_EINVAL;
+    if (colors) return GGCAT_GPU_EUNSUPPORTED;  // needs the colormap file, which is not built
+    std::vector<uint8_t> text;
+    std::vector<uint64_t> off, len;
+    std::string err;
+    const int rc = ggcat::read_sequences(graph_input, k - 1, text, &off, &len, err);
+    if (rc) return rc;
+    for (size_t i = 0; i < off.size(); i++) fn(fn_ctx, text.data() + off[i], len[i], nullptr, 0, 0);
+    return GGCAT_GPU_OK;
+}
+

@@ -222,6 +222,17 @@ int ggcat_gpu_unitig_links(const uint8_t *bases, const uint64_t *off, const uint
 int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *output_file, int k, int unitig_links,
                           int gfa_version, char *err, uint64_t err_cap);
 
+/* ggcat_dump_unitigs (crates/capi/src/lib.rs:407-452; GGCATInstance::dump_unitigs,
+ * crates/api/src/lib.rs:434-477) for uncoloured graphs: calls fn once per piece of the graph
+ * FASTA, read like the reference's reader with a k-1 copyback, with colors = NULL, n_colors = 0
+ * and same_colors = 0, on the calling thread.  The reference's uncoloured branch hands the
+ * function the record's identifier buffer, which its reader leaves empty there (it copies no
+ * identifiers); this hands it the piece's bases.  colors = 1 (the colormap) returns
+ * GGCAT_GPU_EUNSUPPORTED. */
+typedef void (*ggcat_gpu_dump_fn)(void *fn_ctx, const uint8_t *seq, uint64_t len, const uint32_t *colors,
+                                  uint64_t n_colors, int same_colors);
+int ggcat_gpu_dump_unitigs(const char *graph_input, int k, int colors, ggcat_gpu_dump_fn fn, void *fn_ctx);
+
 /* Mirrors ggcat_build_from_files (crates/capi/src/lib.rs:58-139, api/src/lib.rs:217-322)
  * for the uncoloured, no-extra-elaboration case: reads the input files like
  * ggcat_gpu_read_sequences_file (FASTA / FASTQ, plain or compressed), builds the graph on

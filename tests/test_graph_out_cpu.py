@@ -136,3 +136,17 @@ def test_errors(tmp_path):
     src.write_bytes(b">0 LN:i:8\nACGTACGT\n")
     with pytest.raises(_native.GgcatGpuError, match="EINVAL"):
         _native.write_graph(str(src), str(tmp_path / "o.gfa"), 5, True, 3)
+
+
+def test_dump_unitigs(tmp_path):
+    """ggcat_dump_unitigs on an uncoloured graph: one call per piece of the graph FASTA (records
+    cut with the k - 1 copyback), the piece's bases."""
+    rng = np.random.default_rng(3)
+    unitigs = [synth.random_genome(int(rng.integers(31, 400)), rng).tobytes() for _ in range(50)]
+    src = tmp_path / "graph.fa"
+    src.write_bytes(_fasta(unitigs))
+    assert _native.dump_unitigs(str(src), 31) == unitigs
+    L = _native.load()
+    fn = _native.DUMP_FN(lambda *a: None)
+    assert L.ggcat_gpu_dump_unitigs(str(src).encode(), 31, 1, fn, None) == -5  # colours: EUNSUPPORTED
+
