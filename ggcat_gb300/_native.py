@@ -103,6 +103,8 @@ EXPORTED = [
     "ggcat_gpu_unitig_links",
     "ggcat_gpu_write_graph",
     "ggcat_gpu_dump_unitigs",
+    "ggcat_gpu_collect_streams",
+    "ggcat_gpu_build_from_streams",
     "ggcat_gpu_build_from_files",
     "ggcat_gpu_build_from_files_ex",
     "ggcat_gpu_colors",
@@ -130,6 +132,13 @@ def library_path() -> str:
 
 # ggcat_gpu_dump_fn: (fn_ctx, seq, len, colors, n_colors, same_colors)
 DUMP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int)
+# ggcat_gpu_seq_fn and ggcat_gpu_stream
+SEQ_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_uint64)
+READ_BLOCK_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, SEQ_FN, C.c_void_p)
+
+
+class Stream(C.Structure):
+    _fields_ = [("stream_ctx", C.c_void_p), ("read_block", READ_BLOCK_FN)]
 
 
 def load(build: bool = True):
@@ -171,6 +180,8 @@ def load(build: bool = True):
     L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
     L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
     L.ggcat_gpu_dump_unitigs.argtypes = [C.c_char_p, C.c_int, C.c_int, DUMP_FN, C.c_void_p]
+    L.ggcat_gpu_collect_streams.argtypes = [C.POINTER(Stream), u64, C.c_int64, P, u64, pu64]
+    L.ggcat_gpu_build_from_streams.argtypes = [P, C.POINTER(Stream), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_build_from_files_ex.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz,
                                                 C.c_int, C.c_int]
@@ -491,6 +502,38 @@ def dump_unitigs(graph_input: str, k: int) -> list:
     if rc:
         raise GgcatGpuError(f"dump_unitigs failed ({_ERRORS.get(rc, rc)})")
     return out
+
+
+def make_streams(sources: list, seen_copyback: list | None = None):
+    """ggcat_gpu_stream array over Python sources (each a list of byte strings, emitted in
+    order); keep the returned tuple alive while the library uses it."""
+    keep = []
+    arr = (Stream * len(sources))()
+    for i, seqs in enumerate(sources):
+        def read_block(_ctx, copyback, emit, emit_ctx, seqs=seqs):
+            if seen_copyback is not None:
+                seen_copyback.append(copyback)
+            for s in seqs:
+                buf = C.create_string_buffer(bytes(s), len(s))
+                emit(emit_ctx, C.cast(buf, C.c_void_p), len(s))
+        fn = READ_BLOCK_FN(read_block)
+        keep.append(fn)
+        arr[i].stream_ctx = None
+        arr[i].read_block = fn
+    return arr, keep
+
+
+def collect_streams(sources: list, copyback: int, seen_copyback: list | None = None) -> np.ndarray:
+    L = load()
+    arr, keep = make_streams(sources, seen_copyback)
+    need = C.c_uint64()
+    if L.ggcat_gpu_collect_streams(arr, len(sources), copyback, None, 0, C.byref(need)):
+        raise GgcatGpuError("collect_streams failed")
+    text = np.zeros(need.value, np.uint8)
+    if L.ggcat_gpu_collect_streams(arr, len(sources), copyback, _ptr(text), need.value, C.byref(need)):
+        raise GgcatGpuError("collect_streams failed")
+    del keep
+    return text
 
 
 def write_graph(unitigs_fasta: str, output_file: str, k: int, unitig_links: bool = False, gfa_version: int = 0):

@@ -1099,20 +1099,10 @@ static void bucket_counts_for(uint64_t bases, int *bbits, int *sbits) {
     *sbits = s;
 }
 
-extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
-                                          const char *output_file, size_t kmer_length, size_t threads_count,
-                                          int forward_only, size_t minimizer_length, size_t min_multiplicity) {
-    if (!ctx || !input_files || !output_file) return GGCAT_GPU_EINVAL;
-    std::vector<uint8_t> text;
-    {
-        // FASTA / FASTQ by extension, decompressed by the last one, files on threads_count host
-        // threads (all of them when 0) and concatenated in input order (input.cpp)
-        const int nt = threads_count > 0 ? (int)std::min<size_t>(threads_count, 1024)
-                                         : (int)std::max(1u, std::thread::hardware_concurrency());
-        std::string err;
-        const int rc = ggcat::read_sequences_files(input_files, n_inputs, (int64_t)kmer_length - 1, nt, text, err);
-        if (rc) return fail(ctx, rc, "%s", err.c_str());
-    }
+// The build of ggcat_build_from_files once its inputs are text: the parameters as the
+// reference derives them, the device build and link, the unitigs written as FASTA.
+static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text, const char *output_file,
+                           size_t kmer_length, int forward_only, size_t minimizer_length, size_t min_multiplicity) {
     const uint64_t est = text.size();
     ggcat_gpu_params p{};
     p.k = (int)kmer_length;
@@ -1142,6 +1132,34 @@ extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const 
     }
     fclose(f);
     return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
+                                          const char *output_file, size_t kmer_length, size_t threads_count,
+                                          int forward_only, size_t minimizer_length, size_t min_multiplicity) {
+    if (!ctx || !input_files || !output_file) return GGCAT_GPU_EINVAL;
+    std::vector<uint8_t> text;
+    {
+        // FASTA / FASTQ by extension, decompressed by the last one, files on threads_count host
+        // threads (all of them when 0) and concatenated in input order (input.cpp)
+        const int nt = threads_count > 0 ? (int)std::min<size_t>(threads_count, 1024)
+                                         : (int)std::max(1u, std::thread::hardware_concurrency());
+        std::string err;
+        const int rc = ggcat::read_sequences_files(input_files, n_inputs, (int64_t)kmer_length - 1, nt, text, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+    }
+    return build_and_write(ctx, text, output_file, kmer_length, forward_only, minimizer_length, min_multiplicity);
+}
+
+extern "C" int ggcat_gpu_build_from_streams(ggcat_gpu_ctx *ctx, const ggcat_gpu_stream *streams, size_t n_streams,
+                                            const char *output_file, size_t kmer_length, size_t threads_count,
+                                            int forward_only, size_t minimizer_length, size_t min_multiplicity) {
+    (void)threads_count;  // the streams are read on the calling thread
+    if (!ctx || (n_streams && !streams) || !output_file) return GGCAT_GPU_EINVAL;
+    std::vector<uint8_t> text;
+    const int rc = ggcat::collect_streams(streams, n_streams, (int64_t)kmer_length - 1, text);
+    if (rc) return fail(ctx, rc, "a stream has no read_block function");
+    return build_and_write(ctx, text, output_file, kmer_length, forward_only, minimizer_length, min_multiplicity);
 }
 
 // ggcat_build_from_files with its extra_elab and gfa_output_version arguments

@@ -614,7 +614,35 @@ int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, i
     return GGCAT_GPU_OK;
 }
 
+int collect_streams(const ggcat_gpu_stream *streams, size_t n, int64_t copyback, std::vector<uint8_t> &text) {
+    for (size_t i = 0; i < n; i++)
+        if (!streams[i].read_block) return GGCAT_GPU_EINVAL;
+    auto emit = [](void *c, const uint8_t *seq, uint64_t len) {
+        auto &t = *static_cast<std::vector<uint8_t> *>(c);
+        const size_t o = t.size();
+        t.resize(o + len + 1);
+        for (uint64_t j = 0; j < len; j++) t[o + j] = kNorm.t[seq[j]];
+        t[o + len] = '\n';
+    };
+    for (size_t i = 0; i < n; i++) streams[i].read_block(streams[i].stream_ctx, copyback, emit, &text);
+    return GGCAT_GPU_OK;
+}
+
 }  // namespace ggcat
+
+extern "C" int ggcat_gpu_collect_streams(const ggcat_gpu_stream *streams, uint64_t n, int64_t copyback, uint8_t *h_text,
+                                         uint64_t text_cap, uint64_t *text_len) {
+    if (n && !streams) return GGCAT_GPU_EINVAL;
+    std::vector<uint8_t> text;
+    const int rc = ggcat::collect_streams(streams, (size_t)n, copyback, text);
+    if (rc) return rc;
+    if (text_len) *text_len = text.size();
+    if (h_text) {
+        if (text.size() > text_cap) return GGCAT_GPU_EINVAL;
+        memcpy(h_text, text.data(), text.size());
+    }
+    return GGCAT_GPU_OK;
+}
 
 extern "C" int ggcat_gpu_read_sequences_files(const char *const *paths, uint64_t n, int64_t copyback, int threads,
                                               uint8_t *h_text, uint64_t text_cap, uint64_t *text_len, char *err,

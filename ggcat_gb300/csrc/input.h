@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "ggcat_gb300.h"
+
 namespace ggcat {
 
 enum : int { kFormatUnknown = 0, kFormatFasta = 1, kFormatFastq = 2 };
@@ -22,6 +24,8 @@ int parse_sequences(const uint8_t *data, uint64_t n, int format, int64_t copybac
 // 16 MiB or more are parsed on `threads` threads (the same output)
 int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &text, std::vector<uint64_t> *off,
                    std::vector<uint64_t> *len, std::string &err, int threads = 1);
+// the sequences the streams emit, normalised, each followed by '\n', appended to text
+int collect_streams(const ggcat_gpu_stream *streams, size_t n, int64_t copyback, std::vector<uint8_t> &text);
 // several files on up to `threads` threads, concatenated in input order into text
 int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
                          std::string &err);

@@ -233,6 +233,28 @@ typedef void (*ggcat_gpu_dump_fn)(void *fn_ctx, const uint8_t *seq, uint64_t len
                                   uint64_t n_colors, int same_colors);
 int ggcat_gpu_dump_unitigs(const char *graph_input, int k, int colors, ggcat_gpu_dump_fn fn, void *fn_ctx);
 
+/* A sequence source (InputStreamFFI of ggcat_build_from_streams, crates/capi/src/lib.rs:226-292,
+ * 551-558): read_block calls emit once per sequence, on the calling thread; a sequence is any
+ * bytes (ACGTacgt are bases, anything else splits k-mers like an N); partial_read_copyback is
+ * the overlap (k - 1) a stream that cuts long sequences keeps between the pieces. */
+typedef void (*ggcat_gpu_seq_fn)(void *emit_ctx, const uint8_t *seq, uint64_t len);
+typedef struct {
+    void *stream_ctx;
+    void (*read_block)(void *stream_ctx, int64_t partial_read_copyback, ggcat_gpu_seq_fn emit, void *emit_ctx);
+} ggcat_gpu_stream;
+
+/* The text a build from streams starts from: every emitted sequence normalised like the
+ * reader (ACGTacgt -> upper case, anything else -> N), each followed by '\n'.  h_text = NULL
+ * queries the size. */
+int ggcat_gpu_collect_streams(const ggcat_gpu_stream *streams, uint64_t n, int64_t copyback, uint8_t *h_text,
+                              uint64_t text_cap, uint64_t *text_len);
+
+/* ggcat_build_from_streams (crates/capi/src/lib.rs:226-292): ggcat_gpu_build_from_files with
+ * the sequences of the streams instead of files. */
+int ggcat_gpu_build_from_streams(ggcat_gpu_ctx *ctx, const ggcat_gpu_stream *streams, size_t n_streams,
+                                 const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
+                                 size_t minimizer_length, size_t min_multiplicity);
+
 /* Mirrors ggcat_build_from_files (crates/capi/src/lib.rs:58-139, api/src/lib.rs:217-322)
  * for the uncoloured, no-extra-elaboration case: reads the input files like
  * ggcat_gpu_read_sequences_file (FASTA / FASTQ, plain or compressed), builds the graph on

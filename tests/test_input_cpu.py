@@ -210,3 +210,16 @@ def test_large_fasta_parsed_on_threads_equals_whole_file_parse(tmp_path, crlf, c
     p.write_bytes(data)
     got = _native.read_sequences_files([str(p)], 30, threads).tobytes()
     assert got == _native.fasta_parse(data, 30).tobytes()
+
+
+def test_collect_streams():
+    """ggcat_gpu_collect_streams (the text of ggcat_gpu_build_from_streams): every emitted
+    sequence normalised like the reader and followed by a newline, streams in order, the
+    copyback handed to each stream."""
+    srcs = [[b"ACGTacgtNx", b"", b"GATTACA"], [b"ccccRYTT", b"A" * 100]]
+    seen = []
+    got = _native.collect_streams(srcs, 30, seen).tobytes()
+    exp = b"".join(naive.normalize(s) + b"\n" for src in srcs for s in src)
+    assert got == exp
+    assert seen == [30] * (2 * len(srcs))  # the wrapper reads every stream twice: size, then text
+
