@@ -49,7 +49,12 @@ def _args():
     ap.add_argument("--genome", type=int, default=0, help="genome length (0 = the workload's own)")
     ap.add_argument("--coverage", type=float, default=20.0)
     ap.add_argument("--no-per-bucket", action="store_true", help="skip timing the per-bucket launch form")
-    ap.add_argument("--cpu-sample-bases", type=int, default=30_000_000)
+    ap.add_argument("--cpu-sample-bases", type=int, default=0,
+                    help="reads prefix (bases) the CPU baseline builds; 0 = the whole input")
+    ap.add_argument("--ref-budget-s", type=float, default=420.0,
+                    help="--impl reference: stop timing steps once this many seconds are spent")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the parity checks of the GPU outputs against the oracle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--verify", action="store_true", help="check batched == per-bucket unitig sets (slow)")
     ap.add_argument("--no-query", action="store_true", help="skip the query-serving measurement")
@@ -170,13 +175,15 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(w, sample_bases: int, threads: int):
-    """Times the oracle (CPU restatement, all threads) on a bounded prefix of the reads."""
+def cpu_baseline(w, sample_bases: int, threads: int, keep: bool = False):
+    """Times the oracle (CPU restatement, all threads) on the whole input (sample_bases = 0)
+    or on a bounded prefix of the reads.  With keep, also returns the oracle's build, which
+    then checks the GPU's output on the same input."""
     import oracle
 
     n_seq = len(w.seq_off)
     per = float(w.seq_len.mean()) if n_seq else 1.0
-    take = max(1, min(n_seq, int(sample_bases / per)))
+    take = n_seq if sample_bases <= 0 else max(1, min(n_seq, int(sample_bases / per)))
     end = int(w.seq_off[take - 1] + w.seq_len[take - 1] + 1)
     text = w.text[:end]
     p = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6, min_multiplicity=w.min_multiplicity,
@@ -185,8 +192,99 @@ def cpu_baseline(w, sample_bases: int, threads: int):
     r = oracle.build_graph(text, w.seq_off[:take], w.seq_len[:take], p)
     dt = time.perf_counter() - t0
     bases = int(w.seq_len[:take].sum())
-    del r
-    return bases / dt / 1e9, bases, dt, take
+    if not keep:
+        del r
+        r = None
+    return bases / dt / 1e9, bases, dt, take, r
+
+
+def gpu_build_outputs(ctx, text, p, stream=0):
+    """Surviving k-mers (with multiplicities) and the canonical final-unitig set of one GPU
+    build of host `text` through the C ABI (ggcat_gpu_build_text with keep_kmers, then the
+    device link stage)."""
+    import oracle
+    from ggcat_gb300 import _native
+
+    pk = _native.Params.from_buffer_copy(p)
+    pk.keep_kmers = 1
+    ctx.build_text(text, pk, stream)
+    keys, mult = ctx.kmers()
+    ctx.link(p.k)
+    bases, uo, ul, uf = ctx.unitigs()
+    lines = oracle.canonicalize_unitigs(_native.unitig_lines(bases, uo, ul), (uf >> 2) & 1, p.k)
+    return keys, mult, lines
+
+
+def build_parity(ctx, text, p, oracle_result, stream=0) -> dict:
+    """GPU build of `text` against the oracle's build of the same input: k-mers with
+    multiplicities and the final unitig set, both order-free."""
+    from oracle import parity
+
+    keys, mult, lines = gpu_build_outputs(ctx, text, p, stream)
+    km = parity.compare_kmers(keys, mult, oracle_result)
+    un = parity.compare_unitigs(lines, oracle_result)
+    return {"equal": bool(km["equal"] and un["equal"]), "kmers": km, "unitigs": un}
+
+
+def longk_slice_parity(w, n_reads: int, threads: int, dev) -> dict:
+    """The first n_reads reads of the long-k workload (k=63, m=12, Rabin-Karp u128, 4096
+    buckets, min multiplicity 2): GPU build against the oracle's."""
+    import oracle
+    from ggcat_gb300 import _native
+
+    take = min(n_reads, len(w.seq_off))
+    end = int(w.seq_off[take - 1] + w.seq_len[take - 1] + 1)
+    text = w.text[:end]
+    op = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6, min_multiplicity=w.min_multiplicity,
+                       threads=threads, hash_kind=oracle.H_CN_RK128)
+    r = oracle.build_graph(text, w.seq_off[:take], w.seq_len[:take], op)
+    ctx = _native.GpuContext(dev)
+    try:
+        p = _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
+                                min_multiplicity=w.min_multiplicity, hash_kind=_native.GGCAT_HASH_RABIN_KARP128)
+        out = build_parity(ctx, text, p, r)
+    finally:
+        ctx.close()
+    out["input"] = f"first {take} reads ({int(w.seq_len[:take].sum())} bases) of {w.name}"
+    return out
+
+
+def colored_parity(n_genomes: int, n_queries: int, threads: int, dev) -> dict:
+    """The first n_genomes genomes of the coloured workload (one colour each, k=31, m=10,
+    4096 buckets): per-k-mer colour sets against the oracle's, then the first n_queries
+    queries of the coloured query workload (lengths log-uniform 100 bp - 100 kbp, 80%
+    substrings of member genomes) looked up on the GPU's coloured index against the oracle's
+    per-query matched and per-colour counts."""
+    import oracle
+    from oracle import parity
+    from ggcat_gb300 import _native, synth
+
+    w = synth.config_colored(n_genomes=n_genomes)
+    op = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=1, min_multiplicity=1, threads=threads,
+                       colors=True)
+    r = oracle.build_graph(w.text, w.seq_off, w.seq_len, op, seq_colors=w.seq_color)
+    ctx = _native.GpuContext(dev)
+    try:
+        p = _native.make_params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=1, min_multiplicity=1,
+                                keep_kmers=True)
+        ctx.build_text(w.text, p)
+        ctx.colors(w.seq_off, w.seq_color, n_genomes)
+        keys, _ = ctx.kmers()
+        cs = parity.compare_color_sets(keys, ctx.kmer_subsets(), ctx.subsets(), r)
+        ctx.query_index_colored()
+        genomes = [w.text[int(o):int(o) + int(ln)] for o, ln in zip(w.seq_off.tolist(), w.seq_len.tolist())]
+        qt, qo, ql, _ = synth.query_workload(genomes, n_queries)
+        ctx.query_submit(0, qt, qo, ql)
+        matched = ctx.query_wait(0)
+        counts = ctx.query_color_counts(0)
+    finally:
+        ctx.close()
+    lo, hi, _ = r.kmers()
+    coff, ccol = r.kmer_colors()
+    em, _, epc = oracle.query(lo, hi, qt, qo, ql, w.k, gc_off=coff, gc_colors=ccol, ncolors=n_genomes)
+    q = parity.compare_query_counts(matched, counts, em, epc)
+    return {"colors": {**cs, "input": f"first {n_genomes} genomes of the coloured workload ({w.name})"},
+            "query": {**q, "input": f"first {n_queries} queries of the coloured query workload"}}
 
 
 def query_bench(args, ctx, torch, dev):
@@ -351,25 +449,32 @@ def build_config_bench(w, torch, dev, steps=3, cpu_threads=0, tune=False):
                "e2e_final_unitigs_gbases_per_s": round(w.bases / (e2e_s + link_ms * 1e-3) / 1e9, 3),
                "autotuned": tuned,
                "superkmers": int(st["superkmers"]), "kmer_instances": int(st["kmer_instances"]),
-               "surviving_kmers_by_subbucket": int(st["surviving_kmers"]), "final_unitigs": int(st["final_unitigs"])}
+               "final_unitigs": int(st["final_unitigs"])}
+        if cpu_threads > 0:
+            # the oracle builds the whole input (timed), then checks the GPU's k-mers and unitigs
+            import oracle
+
+            op = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
+                               min_multiplicity=w.min_multiplicity, threads=cpu_threads,
+                               hash_kind=oracle.H_CN_RK128 if getattr(w, "hash_kind", "") == "rk128" else None)
+            t0 = time.perf_counter()
+            r = oracle.build_graph(w.text, w.seq_off, w.seq_len, op)
+            dt = time.perf_counter() - t0
+            out["cpu_oracle"] = {"gbases_per_s": round(w.bases / dt / 1e9, 5), "seconds": round(dt, 2),
+                                 "cores": cpu_threads, "kind": "port"}
+            out["parity"] = build_parity(ctx, w.text, p, r)
+            out["surviving_kmers"] = out["parity"]["kmers"]["kmers_gpu"]
+            del r
     finally:
         ctx.close()
-    if cpu_threads > 0:
-        import oracle
-
-        op = oracle.params(k=w.k, m=w.m, bucket_bits=w.bucket_bits, second_bits=6,
-                           min_multiplicity=w.min_multiplicity, threads=cpu_threads,
-                           hash_kind=oracle.H_CN_RK128 if getattr(w, "hash_kind", "") == "rk128" else None)
-        t0 = time.perf_counter()
-        r = oracle.build_graph(w.text, w.seq_off, w.seq_len, op)
-        dt = time.perf_counter() - t0
-        del r
-        out["cpu_oracle"] = {"gbases_per_s": round(w.bases / dt / 1e9, 5), "seconds": round(dt, 2),
-                             "cores": cpu_threads, "kind": "port"}
     return out
 
 
 def run_reference(args):
+    """The CPU arm: the oracle restatement (C, all host threads) builds the whole input of the
+    GPU arm's workload in every timed step (the Rust reference cannot be compiled here).
+    Warm-up steps build a 30 Mbp prefix.  A full-input step takes tens of seconds, so timed
+    steps stop once --ref-budget-s is spent; the line reports the steps actually timed."""
     ws, rank, local = _dist()
     if rank != 0:
         return 0
@@ -378,35 +483,52 @@ def run_reference(args):
     oracle.build()
     w = _workload(args)
     threads = os.cpu_count() or 1
-    vals = []
-    for i in range(args.warmup + args.steps):
-        v, bases, dt, take = cpu_baseline(w, args.cpu_sample_bases, threads)
-        if i >= args.warmup:
-            vals.append(v)
+    for _ in range(args.warmup):
+        cpu_baseline(w, 30_000_000, threads)
+    vals, t_start = [], time.perf_counter()
+    bases = take = 0
+    for i in range(args.steps):
+        v, bases, dt, take, _ = cpu_baseline(w, args.cpu_sample_bases, threads)
+        vals.append(v)
+        spent = time.perf_counter() - t_start
+        if spent + dt > args.ref_budget_s:
+            break
     value = statistics.median(vals)
+    whole = take == len(w.seq_off)
     line = {
         "impl": "reference",
         "metric": METRIC,
         "value": round(value, 6),
         "unit": "Gbases/s",
         "n_gpus": args.gpus,
-        "steps": args.steps,
+        "steps": len(vals),
+        "steps_requested": args.steps,
         "warmup": args.warmup,
         "ms_per_step": round(bases / value / 1e6, 3),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "u64",
+        "dtype": "u64" if w.k <= 32 else "u128",
         "data": "synthetic (seeded)",
-        "config": {"workload": w.name + f" (first {take} reads, {bases} bases per step)", "k": w.k, "m": w.m,
-                   "buckets": 1 << w.bucket_bits, "min_multiplicity": w.min_multiplicity},
+        "config": _config(w, ws) if whole else {**_config(w, ws), "workload": w.name + f" (first {take} reads)"},
         "cpu_baseline": {"value": round(value, 6), "unit": "Gbases/s", "cores": threads, "kind": "port",
-                         "sample": f"first {take} reads ({bases} bases) of the workload; the Rust reference cannot be "
-                                   f"compiled here, so the oracle restatement (C, pthreads) is timed"},
+                         "sample": (f"whole input ({take} reads, {bases} bases) per step" if whole else
+                                    f"first {take} reads ({bases} bases) per step") +
+                                   "; the Rust reference cannot be compiled here, so the oracle restatement "
+                                   "(C, pthreads) is timed; warm-up steps on a 30 Mbp prefix"},
         "e2e": {"value": round(value, 6), "unit": "Gbases/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _config(w, ws):
+    return {"workload": w.name, "k": w.k, "m": w.m, "buckets": 1 << w.bucket_bits,
+            "min_multiplicity": w.min_multiplicity, "bases_per_gpu": int(w.bases),
+            "hash": getattr(w, "hash_kind", "seq-hash"),
+            "l2": (f"input ({w.text.size / 1e9:.2f} GB) larger than L2 (129 MB); no flush" if w.text.size > 129e6
+                   else f"input ({w.text.size / 1e6:.1f} MB) fits in L2; no flush"),
+            "parallelism": f"replicas x{ws}"}
 
 
 def run_gpu(args):
@@ -534,14 +656,32 @@ def run_gpu(args):
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_step": int(merge_bytes), "phase_ms": round(merge_ms, 3)}
-    # the bucketing phase (pack + count + write passes): the ASCII read, the 2-bit + validity
-    # write, two reads of the packed input and one 16-byte record write per superkmer
-    bucket_bytes = n + n * 3 / 8 + 2 * (n * 3 / 8) + 16 * S
+    # the bucketing phase (pack + bucketize + partition), algorithmic bytes per step: the ASCII
+    # text read once and every superkmer written once in 2-bit form with an 8-byte header,
+    # N + sum(ceil(L/4) + 8) (the bucket store's record payload)
+    bucket_bytes = n + (I + S * (w.k - 1)) / 4 + S * 8.375
     bucket_ms = phases["ms_pack"] + phases["ms_bucketize"]
     b_ach = bucket_bytes / (bucket_ms * 1e-3) / 1e9 if bucket_ms > 0 else 0.0
-    roofline_bucketing = {"bound": "hbm", "kernel": "pack_kernel + bucketize_kernel", "achieved": round(b_ach, 1),
+    roofline_bucketing = {"bound": "hbm", "kernel": "pack_kernel + bucketize_kernel + partition_kernel",
+                          "achieved": round(b_ach, 1),
                           "peak": peak, "unit": "GB/s", "frac": round(b_ach / peak, 4), "peak_kind": peak_kind,
                           "algorithmic_bytes_per_step": int(bucket_bytes), "phase_ms": round(bucket_ms, 3)}
+
+    # CPU baseline: the oracle builds the whole input once (timed); its output then checks the
+    # GPU's build of the same input (k-mers with multiplicities, final unitigs), outside every
+    # timed region
+    cpu, parity = None, {}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, cb, dt, take, r = cpu_baseline(w, args.cpu_sample_bases, threads, keep=not args.no_parity)
+        whole = take == len(w.seq_off)
+        cpu = {"value": round(v, 6), "unit": "Gbases/s", "cores": threads, "kind": "port",
+               "sample": (f"whole input ({take} reads, {cb} bases)" if whole else f"first {take} reads ({cb} bases)")
+                         + f", oracle restatement (C, pthreads), one run of {dt:.1f} s"}
+        if r is not None:
+            end = int(w.seq_off[take - 1] + w.seq_len[take - 1] + 1)
+            parity["C2_" + ("whole_input" if whole else "prefix")] = build_parity(ctx, w.text[:end], pb, r, sptr)
+            del r
 
     query = None
     if rank == 0 and not args.no_query:
@@ -558,15 +698,21 @@ def run_gpu(args):
         from ggcat_gb300 import synth
 
         configs = {"genomes_3x5Mbp": build_config_bench(synth.config_genomes(), torch, dev, steps=5,
-                                                        cpu_threads=os.cpu_count() or 1)}
-        configs["longk_2Gbp"] = build_config_bench(synth.config_long_k(), torch, dev, steps=3, tune=True)
+                                                        cpu_threads=0 if args.no_cpu_baseline else
+                                                        os.cpu_count() or 1)}
+        w_longk = synth.config_long_k()
+        configs["longk_2Gbp"] = build_config_bench(w_longk, torch, dev, steps=3, tune=True)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if configs is not None and not args.no_parity:
+        parity.update({"C1_" + k2: v2["parity"] for k2, v2 in configs.items() if "parity" in v2})
+    if rank == 0 and not args.no_parity and not args.no_configs and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, cb, dt, take = cpu_baseline(w, args.cpu_sample_bases, threads)
-        cpu = {"value": round(v, 6), "unit": "Gbases/s", "cores": threads, "kind": "port",
-               "sample": f"first {take} reads ({cb} bases), oracle restatement, {dt:.1f} s"}
+        parity["C4_longk_slice"] = longk_slice_parity(w_longk, 400_000, threads, dev)
+        parity["C3_C5_colored_32"] = colored_parity(32, 2000, threads, dev)
+    if parity:
+        flags = [v.get("equal", all(x.get("equal") for x in v.values() if isinstance(x, dict)))
+                 for v in parity.values()]
+        parity["all_equal"] = bool(all(flags))
 
     if rank == 0:
         line = {
@@ -582,11 +728,8 @@ def run_gpu(args):
             "vs_baseline": None,
             "dtype": "u64" if w.k <= 32 else "u128",
             "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "k": w.k, "m": w.m, "buckets": 1 << w.bucket_bits,
-                       "min_multiplicity": w.min_multiplicity, "bases_per_gpu": bases,
-                       "hash": getattr(w, "hash_kind", "seq-hash"),
-                       "l2": f"input ({n / 1e9:.1f} GB) larger than L2; no flush", "merge": "batched persistent",
-                       "parallelism": f"replicas x{ws}"},
+            "config": _config(w, ws),
+            "merge": "batched persistent",
             "phases_ms": {k2: round(v, 3) for k2, v in phases.items()},
             "stats": {"superkmers": int(st["superkmers"]), "kmer_instances": int(st["kmer_instances"]),
                       "distinct_kmers": int(D), "partial_unitigs": int(st["partial_unitigs"]),
@@ -601,6 +744,7 @@ def run_gpu(args):
             "roofline": roofline,
             "roofline_bucketing": roofline_bucketing,
             "cpu_baseline": cpu,
+            "parity": parity or None,
             "query": query,
             "colored": colored,
             "configs": configs,

@@ -547,6 +547,17 @@ def write_graph(unitigs_fasta: str, output_file: str, k: int, unitig_links: bool
 
 
 def unitig_lines(bases: np.ndarray, off: np.ndarray, ln: np.ndarray) -> bytes:
-    """'\\n'-terminated unitig lines from (bases, offsets, lengths)."""
-    b = bases.tobytes()
-    return b"".join(b[o : o + l] + b"\n" for o, l in zip(off.tolist(), ln.tolist()))
+    """'\\n'-terminated unitig lines from (bases, offsets, lengths), gathered in one pass."""
+    ln64 = np.asarray(ln).astype(np.int64)
+    n = ln64.size
+    if n == 0:
+        return b""
+    if bases.size == 0:
+        return b"\n" * n
+    out_start = np.zeros(n, np.int64)
+    out_start[1:] = np.cumsum(ln64[:-1] + 1)
+    total = int(ln64.sum()) + n
+    src = np.arange(total, dtype=np.int64) + np.repeat(np.asarray(off).astype(np.int64) - out_start, ln64 + 1)
+    out = bases[np.minimum(src, bases.size - 1)]  # the newline slots are overwritten below
+    out[out_start + ln64] = 10
+    return out.tobytes()
