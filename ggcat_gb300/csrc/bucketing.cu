@@ -86,24 +86,29 @@ __global__ void __launch_bounds__(256) pack_kernel(const uint8_t *__restrict__ t
 // tests), so the combine reproduces the queue's values exactly.
 //
 // The window of w = k-m m-mers ending at m-mer i is split van Herk / Gil-Werman style into
-// blocks of w m-mers counted from the thread's first m-mer: window = suffix(previous block,
-// from i-w+1) combined with prefix(current block, up to i).  All lanes of a warp start the
-// same number of bases before a multiple of 32, so they cross block and packed-word
-// boundaries on the same steps and do identical work.  The per-thread block array (w
-// entries) lives in shared memory, column-major.
+// blocks of w m-mers counted from the thread's first base: window = suffix(previous block,
+// from i-w+1) combined with prefix(current block, up to i).  M-mers are indexed by their
+// last base, counted from the walk's first base; a window is only used when its k-1 bases
+// are valid, which puts it in the second block or later and makes all its m-mers valid.
+// All lanes of a warp start the same number of bases before a multiple of 32, so they load
+// packed words and cross block boundaries on the same steps.  The per-thread block array (w
+// entries: value, and a byte with the offset of the suffix minimum and its orientation) lives
+// in shared memory, column-major.
 //
 // The nt-hash rolls over every code, valid or not, starting from the state of an all-'A'
 // history: the rolling update is exact for any code sequence, so m steps after a separator
 // or an N the value is the m-mer's hash again without a recomputation; validity is tracked
-// by the run length.
+// by the run length.  One 16-byte table entry per (leaving code, entering code) pair holds
+// both XOR terms of the roll.
 // ---------------------------------------------------------------------------
-// Rolling nt-hash tables per 2-bit code (cn_nthash.rs:19-58): the leaving base contributes
-// {rotl(h, m), rch} and the entering base {h, rotl(rch, m - 1)}.
-struct __align__(16) NtPair {
-    uint64_t a, b;
+// Roll terms (cn_nthash.rs:19-58) of the pair (out, in): f = rotl(h(out), m) ^ h(in),
+// r = rotr(rch(out), 1) ^ rotl(rch(in), m - 1); fw' = rotl(fw, 1) ^ f, rc' = rotr(rc, 1) ^ r.
+struct __align__(16) NtRoll {
+    uint64_t f, r;
 };
 
-// Window-minimum state: v = masked minimum | unique bit, pf = position << 1 | is_forward
+// Window-minimum state: v = masked minimum | unique bit, pf = (last base of the m-mer) << 1 |
+// is_forward
 struct CState {
     uint64_t v;
     uint32_t pf;
@@ -111,51 +116,60 @@ struct CState {
 
 __device__ __forceinline__ CState cmb(const CState &a, const CState &b) {
     const uint64_t ma = a.v & ~1ull, mb = b.v & ~1ull;
+    const bool lt = mb < ma, eq = ma == mb;
     CState r;
-    r.v = ma < mb ? a.v : (mb < ma ? b.v : ma);  // equal minima from two parts: not unique
-    r.pf = mb < ma ? b.pf : a.pf;
+    r.v = lt ? b.v : (eq ? ma : a.v);  // equal minima from two parts: not unique
+    r.pf = lt ? b.pf : a.pf;
     return r;
 }
-
-constexpr uint64_t kInf = ~0ull;
 
 // Superkmers found by a lane wait in a per-lane queue in shared memory (column-major, one
 // column per thread) and are built, counted and stored together by the whole warp: a split
 // happens every ~(w+1)/2 positions per lane, so emitting at once would run the record code on
-// almost every step with one or two lanes active.  A lane gains at most one entry per step
-// and the warp drains as soon as a lane holds kEmitDrain, so kEmitQueue entries suffice; six
-// entries keep three 256-thread CTAs per SM (k - m = 21) and halve the drain rounds of four.
+// almost every step with one or two lanes active.  The queues are checked every kCheck steps
+// (a lane gains at most kCheck entries in between) and drained while some lane holds
+// kEmitDrain or more, one entry of every non-empty lane per round.
 constexpr int kEmitQueue = 6;
-constexpr int kEmitDrain = 5;
+constexpr int kCheck = 2;
+constexpr int kEmitDrain = kEmitQueue - kCheck;
+
+// Per-sub-bin counts: one 64-bit atomic per superkmer, records in the high half and k-mer
+// instances in the low half (packed).  A count that does not fit its half carries into the
+// other one or out of the word; the host detects that from the record total and runs again
+// with separate counters (split).
+struct BinCounters {
+    unsigned long long *packed;  // packed mode: records << 32 | k-mers
+    unsigned long long *kmers;   // split mode: k-mers (records in `packed`)
+    unsigned long long *total;   // records of all CTAs
+    int split;
+};
 
 // Single pass over the 2-bit text.  Thread t owns the window starts [t*chunk, (t+1)*chunk)
 // (chunk a multiple of 32) and walks the bases from lb (a multiple of 32) before its range,
-// so all lanes of a warp load packed words and cross van Herk block boundaries on the same
-// steps.  Superkmer records go to the block's region of the staging array (block-shared
-// cursor), or to the overflow area when the region is full; partition_kernel scatters them
-// by sub-bin after an exclusive scan of the per-sub-bin counts.
-template <bool kLongM>  // m > 16: the last m codes need a 64-bit shift register
-__global__ void __launch_bounds__(256, 3)
+// one packed word (32 bases) per outer iteration.  Superkmer records go to the block's
+// region of the staging array (block-shared cursor), or to the overflow area when the region
+// is full; partition_kernel scatters them by sub-bin after an exclusive scan of the
+// per-sub-bin counts.
+template <int kTPB, bool kLongM>  // kLongM: m > 16, the last m codes need a 64-bit shift register
+__global__ void __launch_bounds__(kTPB, kTPB == 256 ? 3 : 6)
     bucketize_kernel(const uint64_t *__restrict__ packed, const uint32_t *__restrict__ valid, uint64_t n, int k,
                      int m, int bbits, int sbits, int fbits, int canonical, uint32_t chunk, uint32_t lb0,
-                     unsigned long long *__restrict__ bin_count, unsigned long long *__restrict__ bin_kmers,
-                     SkRec *__restrict__ stage, uint32_t region_cap, unsigned long long *__restrict__ block_count,
-                     unsigned long long ovf_cap, unsigned long long *__restrict__ ovf_cursor,
-                     unsigned *__restrict__ status, uint32_t block_base, uint32_t total_blocks) {
-    __shared__ NtPair t_out[4], t_in[4];
+                     BinCounters bc, SkRec *__restrict__ stage, uint32_t region_cap,
+                     unsigned long long *__restrict__ block_count, unsigned long long ovf_cap,
+                     unsigned long long *__restrict__ ovf_cursor, unsigned *__restrict__ status, uint32_t block_base,
+                     uint32_t stage_block0, uint32_t stage_blocks) {
+    __shared__ NtRoll tab[16];
     __shared__ unsigned s_cnt;
     extern __shared__ __align__(16) uint8_t bk_smem[];
-    const int wn = k - m;
-    const int nthr = blockDim.x;
-    uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                          // [wn][nthr]
-    uint4 *que = reinterpret_cast<uint4 *>(blk_v + (size_t)wn * nthr);                // [kEmitQueue][nthr]
-    uint8_t *blk_m = reinterpret_cast<uint8_t *>(que + (size_t)kEmitQueue * nthr);    // [wn][nthr]
-    if (threadIdx.x < 4) {
-        const uint32_t c = threadIdx.x;
-        const uint64_t h = (uint64_t)(2 * c + 1) * kNtMult;
-        const uint64_t r = (uint64_t)(((2 * c) ^ 4) + 1) * kNtMult;
-        t_out[c] = NtPair{rotl64(h, (unsigned)m), r};
-        t_in[c] = NtPair{h, rotl64(r, (unsigned)(m - 1))};
+    const uint32_t wn = (uint32_t)(k - m);
+    uint64_t *blk_v = reinterpret_cast<uint64_t *>(bk_smem);                       // [wn][kTPB]
+    uint4 *que = reinterpret_cast<uint4 *>(blk_v + (size_t)wn * kTPB);             // [kEmitQueue][kTPB]
+    uint8_t *blk_m = reinterpret_cast<uint8_t *>(que + (size_t)kEmitQueue * kTPB); // [wn][kTPB]
+    if (threadIdx.x < 16) {
+        const uint32_t out = threadIdx.x >> 2, in = threadIdx.x & 3;
+        const uint64_t ho = (uint64_t)(2 * out + 1) * kNtMult, ro = (uint64_t)(((2 * out) ^ 4) + 1) * kNtMult;
+        const uint64_t hi = (uint64_t)(2 * in + 1) * kNtMult, ri = (uint64_t)(((2 * in) ^ 4) + 1) * kNtMult;
+        tab[threadIdx.x] = NtRoll{rotl64(ho, (unsigned)m) ^ hi, rotr64(ro, 1) ^ rotl64(ri, (unsigned)(m - 1))};
     }
     if (threadIdx.x == 0) s_cnt = 0;
     // rolling state of an all-'A' history (code 0): nt-hash of m A's
@@ -173,36 +187,38 @@ __global__ void __launch_bounds__(256, 3)
     const uint32_t bmask = (1u << bbits) - 1, smask = (1u << sbits) - 1, fmask = (1u << fbits) - 1;
     const uint64_t n_words = (n + 31) >> 5;
     const int lane = (int)(threadIdx.x & 31);
-    // this launch covers blocks [block_base, block_base + gridDim.x) of total_blocks
+    // this launch covers blocks [block_base, block_base + gridDim.x); the staging array holds the
+    // regions of blocks [stage_block0, stage_block0 + stage_blocks), then the overflow area
     const uint64_t bid = (uint64_t)blockIdx.x + block_base;
-    const uint64_t region = bid * region_cap;
+    const uint64_t region = (bid - stage_block0) * region_cap;
     uint64_t *my_v = blk_v + threadIdx.x;
     uint8_t *my_m = blk_m + threadIdx.x;
     uint4 *my_q = que + threadIdx.x;
     const uint32_t top_sh = 2u * (uint32_t)(m - 1);
+    const uint32_t km1 = (uint32_t)(k - 1);
 
-    const uint64_t tid = bid * blockDim.x + threadIdx.x;
+    const uint64_t tid = bid * kTPB + threadIdx.x;
     const uint64_t x0 = tid * chunk;
     int qlen = 0;     // superkmers waiting in this lane's queue
     uint64_t xb = 0;  // first base of the current attempt (queue positions are relative to it)
 
-    // build, count and store one queued superkmer of every lane that has one, until all
-    // queues of the active lanes are empty
-    auto drain = [&]() {
+    // Builds, counts and stores one queued superkmer of every lane that has one, in rounds,
+    // while some lane holds at least `keep` entries (keep = 1: until all queues are empty).
+    auto drain = [&](int keep) {
         const unsigned am = __activemask();
         for (;;) {
+            if (!__any_sync(am, qlen >= keep)) break;
             const unsigned bm = __ballot_sync(am, qlen > 0);
-            if (bm == 0) break;
             SkRec rec{0, 0};
             if (qlen > 0) {
                 qlen--;
-                const uint4 e = my_q[(size_t)qlen * nthr];
-                // superkmer [start, end) whose last window's minimum (value raw, m-mer
-                // position pos, is_forward mfw) is the minimizer (lib.rs:207-267)
+                const uint4 e = my_q[(size_t)qlen * kTPB];
+                // superkmer [start, end) whose last window's minimum (value raw, last base of
+                // the m-mer and is_forward in pf) is the minimizer (lib.rs:207-267)
                 const uint32_t start_r = e.x, end_r = e.y & 0x3fffffffu;
                 const uint32_t inc_first = (e.y >> 30) & 1u, inc_last = e.y >> 31;
                 const uint32_t len = end_r - start_r;
-                const uint32_t moff = (e.z >> 1) - start_r, mfw = e.z & 1u;
+                const uint32_t moff = (e.z >> 1) + 1u - (uint32_t)m - start_r, mfw = e.z & 1u;
                 const uint32_t raw = e.w;
                 uint32_t bucket, rcf, pos;
                 if ((raw & 1u) == 0) {
@@ -218,8 +234,13 @@ __global__ void __launch_bounds__(256, 3)
                 const uint32_t sub = (raw >> (bbits + 1)) & fmask;
                 const uint32_t flags = (inc_first << rcf) | (inc_last << (rcf ^ 1u));
                 const uint64_t bin = ((uint64_t)bucket << fbits) | sub;
-                atomicAdd(&bin_count[bin], 1ull);
-                atomicAdd(&bin_kmers[bin], (unsigned long long)(len - (uint32_t)k + 1));
+                const unsigned long long nk = (unsigned long long)(len - (uint32_t)k + 1);
+                if (bc.split) {
+                    atomicAdd(&bc.packed[bin], 1ull);
+                    atomicAdd(&bc.kmers[bin], nk);
+                } else {
+                    atomicAdd(&bc.packed[bin], (1ull << 32) + nk);
+                }
                 rec.w0 = (xb + start_r) | ((uint64_t)len << 40);
                 rec.w1 = (uint64_t)bucket | ((uint64_t)(second & 0xff) << 16) | ((uint64_t)flags << 24) |
                          ((uint64_t)rcf << 26) | ((uint64_t)(pos & 0xffff) << 32) | ((uint64_t)sub << 48);
@@ -235,7 +256,7 @@ __global__ void __launch_bounds__(256, 3)
                 } else {
                     const unsigned long long oi = atomicAdd(ovf_cursor, 1ull);
                     if (oi < ovf_cap)
-                        stage[(uint64_t)total_blocks * region_cap + oi] = rec;
+                        stage[(uint64_t)stage_blocks * region_cap + oi] = rec;
                     else
                         atomicOr(status, kStatusStageOverflow);
                 }
@@ -250,56 +271,41 @@ __global__ void __launch_bounds__(256, 3)
         // (relative positions stay below 2^30: queue entries keep two flags above them)
         for (int attempt = 0; attempt < 24 && !done && lb <= (1ull << 28); attempt++) {
             xb = x0 > lb ? x0 - lb : 0;  // a multiple of 32
-            const uint32_t lo_r = (uint32_t)(x0 - xb), hi_r = (uint32_t)(x1 - xb);
+            const uint32_t lo_r = (uint32_t)(x0 - xb);
+            uint32_t hi_r = (uint32_t)(x1 - xb);
             const uint32_t r_end = (uint32_t)(min(x1 + (uint64_t)k - 1, n + 1) - xb);
-            bool anchored = (xb == 0);
-            uint32_t run = 0;
+            bool anchored = (xb == 0), c_known = false, first_sk = false, failed = false;
+            uint32_t run = 0, c_prev = 0;
             uint64_t fw = fw_a, rc = rc_a;
             uint64_t hist = 0;  // codes of the last m bases, oldest in the low bits
-            CState P{kInf, 0}, prev{0, 0};
-            bool prev_valid = false, c_known = false, first_sk = false, failed = false, have_prev_block = false;
-            uint32_t c_prev = 0;
-            int o = 0;  // offset of the current m-mer inside its block
+            CState P{~0ull, 0}, prev{0, 0};
+            uint32_t o = 0;  // offset of the current m-mer inside its block
+            for (uint32_t j = 0; j < wn; j++) {
+                my_v[(size_t)j * kTPB] = ~0ull;
+                my_m[(size_t)j * kTPB] = 0;
+            }
 
-            uint64_t wi = xb >> 5;
-            uint64_t pw = 0, pw_next = wi < n_words ? packed[wi] : 0ull;
-            uint32_t vw = 0, vw_next = wi < n_words ? valid[wi] : 0u;
-
-            auto push = [&](uint32_t start_r, uint32_t end_r, uint32_t fin) {
-                my_q[(size_t)qlen * nthr] = make_uint4(start_r, end_r | ((first_sk ? 1u : 0u) << 30) | (fin << 31),
-                                                       prev.pf, (uint32_t)prev.v);
-                qlen++;
-                first_sk = false;
-            };
-
-            for (uint32_t r = 0; r < r_end; r++) {
-                // the warp drains its queues once a lane's queue reaches kEmitDrain
-                if (__any_sync(__activemask(), qlen >= kEmitDrain)) drain();
-                if ((r & 31u) == 0) {  // the same step on every lane
-                    pw = pw_next;
-                    vw = vw_next;
-                    wi++;
-                    pw_next = wi < n_words ? packed[wi] : 0ull;
-                    vw_next = wi < n_words ? valid[wi] : 0u;
-                }
-                const uint32_t c = (uint32_t)pw & 3u;
-                pw >>= 2;
-                const bool ok = (vw & 1u) != 0;
-                vw >>= 1;
+            // one base: c its 2-bit code, ok its validity, r its offset from xb
+            auto step = [&](uint32_t c, bool ok, uint32_t r) {
                 if (!ok) {
                     // end of a run: the last superkmer closes at its last window (x_last)
-                    if (run >= (uint32_t)k && prev_valid) {
+                    if (run >= (uint32_t)k) {
                         const uint32_t x_last = r - (uint32_t)k + 1;
                         if (x_last >= lo_r && x_last < hi_r) {
                             if (!c_known) {
                                 failed = true;
-                                break;
+                                hi_r = 0;  // no further records in this attempt
+                            } else {
+                                my_q[(size_t)qlen * kTPB] =
+                                    make_uint4(c_prev - 1, (x_last + (uint32_t)k - 1) | ((first_sk ? 1u : 0u) << 30) |
+                                                               (1u << 31),
+                                               prev.pf, (uint32_t)prev.v);
+                                qlen++;
+                                first_sk = false;
                             }
-                            push(c_prev - 1, x_last + (uint32_t)k - 1, 1u);
                         }
                     }
                     anchored = true;
-                    prev_valid = false;
                     c_known = false;
                 }
                 run = ok ? run + 1 : 0u;
@@ -312,77 +318,86 @@ __global__ void __launch_bounds__(256, 3)
                     out = (uint32_t)hist & 3u;
                     hist = (uint64_t)(((uint32_t)hist >> 2) | (c << top_sh));
                 }
-                const NtPair to = t_out[out], ti = t_in[c];
-                fw = rotl64(fw, 1) ^ to.a ^ ti.a;
-                rc = rotr64(rc ^ to.b, 1) ^ ti.b;
-                if (r + 1 < (uint32_t)m) continue;  // no m-mer yet (the same steps on every lane)
-                const bool mv = run >= (uint32_t)m;
+                const NtRoll t = tab[(out << 2) | c];
+                fw = rotl64(fw, 1) ^ t.f;
+                rc = rotr64(rc, 1) ^ t.r;
                 const bool isf = fw < rc;
                 const uint64_t mn = isf ? fw : rc;
-                const CState e{mv ? ((mn << 1) | (uint64_t)(fw != rc)) : kInf,
-                               ((r + 1 - (uint32_t)m) << 1) | (isf ? 1u : 0u)};
-                // van Herk block window minimum over m-mer indices relative to xb
-                uint64_t *vo = my_v + (size_t)o * nthr;
-                uint8_t *mo = my_m + (size_t)o * nthr;
-                if (o == 0) {
-                    if (r + 1 > (uint32_t)m) {
-                        // the previous block is complete: suffix minima in place (offset 0 unused)
-                        CState s{my_v[(size_t)(wn - 1) * nthr], my_m[(size_t)(wn - 1) * nthr]};
-                        for (int j = wn - 2; j >= 1; j--) {
-                            const CState cj{my_v[(size_t)j * nthr], my_m[(size_t)j * nthr]};
-                            s = cmb(cj, s);
-                            my_v[(size_t)j * nthr] = s.v;
-                            my_m[(size_t)j * nthr] = (uint8_t)s.pf;
-                        }
-                        have_prev_block = true;
+                // (an m-mer over a non-ACGT byte gets a meaningless value: the windows that are
+                // used hold valid m-mers only, and the van Herk parts of a window cover exactly
+                // its m-mers, so such values never reach a used window)
+                const CState e{(mn << 1) | (uint64_t)(fw != rc), (r << 1) | (isf ? 1u : 0u)};
+                // van Herk block window minimum
+                if (o == 0) {  // the previous block is complete: suffix minima in place (offset 0 unused)
+                    CState sfx{my_v[(size_t)(wn - 1) * kTPB], my_m[(size_t)(wn - 1) * kTPB]};
+                    for (uint32_t j = wn - 2; j >= 1; j--) {
+                        const CState cj{my_v[(size_t)j * kTPB], my_m[(size_t)j * kTPB]};
+                        sfx = cmb(cj, sfx);
+                        my_v[(size_t)j * kTPB] = sfx.v;
+                        my_m[(size_t)j * kTPB] = (uint8_t)sfx.pf;
                     }
                     P = e;
                 } else {
                     P = cmb(P, e);
                 }
                 CState win = P;
-                bool win_avail = (o == wn - 1);
-                if (!win_avail && have_prev_block) {
-                    const uint8_t mt = mo[nthr];
-                    // suffix of the previous block from offset o + 1: position = block start + offset
-                    const uint32_t ps = (r + 1 - (uint32_t)m) - (uint32_t)o - (uint32_t)wn + (uint32_t)(mt & 0x7f);
-                    win = cmb(CState{vo[nthr], (ps << 1) | (uint32_t)(mt >> 7)}, P);
-                    win_avail = true;
+                if (o + 1 < wn) {  // suffix of the previous block from offset o + 1
+                    const uint8_t mt = my_m[(size_t)(o + 1) * kTPB];
+                    const uint32_t ps = r - o - wn + (uint32_t)(mt & 0x7f);
+                    win = cmb(CState{my_v[(size_t)(o + 1) * kTPB], (ps << 1) | (uint32_t)(mt >> 7)}, P);
                 }
-                *vo = e.v;
-                *mo = (uint8_t)((uint32_t)o | ((e.pf & 1u) << 7));
+                my_v[(size_t)o * kTPB] = e.v;
+                my_m[(size_t)o * kTPB] = (uint8_t)(o | ((e.pf & 1u) << 7));
                 o = (o + 1 == wn) ? 0 : o + 1;
 
-                if (!ok || run < (uint32_t)(k - 1) || !win_avail) continue;
-                const uint32_t x = r - (uint32_t)k + 2;  // window start
-                if (run == (uint32_t)(k - 1)) {
-                    if (anchored) {
-                        c_prev = x + 1;  // virtual first callback: the first superkmer starts at x
-                        c_known = true;
-                        first_sk = true;
-                    } else {
-                        c_known = false;
-                    }
-                } else {
-                    // get_minimizer_splits split rule, batch_minqueue.rs:146-152
-                    const bool split = (win.v != prev.v) || ((win.v & 1ull) && win.pf != prev.pf);
-                    if (split) {
-                        if (x >= lo_r && x < hi_r) {
-                            if (!c_known) {
-                                failed = true;
-                                break;
-                            }
-                            push(c_prev - 1, x + (uint32_t)k - 1, 0u);
-                        }
-                        c_prev = x;
-                        c_known = true;
-                        first_sk = false;
+                // Superkmer bookkeeping as predicated assignments (some lane of a warp splits on
+                // almost every step, so a divergent branch would run nearly always):
+                //   a run starts (first valid window): with an anchor, a virtual first callback
+                //     (the first superkmer starts at x); otherwise the start is not known yet;
+                //   a split (get_minimizer_splits split rule, batch_minqueue.rs:146-152) closes
+                //     the current superkmer at the window before x.
+                const bool wv = ok && run >= km1;  // the (k-1)-mer ending here is a valid window
+                const uint32_t x = r - (uint32_t)k + 2;
+                const bool first = wv && run == km1;
+                const bool split = wv && !first && ((win.v != prev.v) || ((win.v & 1ull) && win.pf != prev.pf));
+                const bool inr = split && x >= lo_r && x < hi_r;
+                if (inr && c_known) {
+                    my_q[(size_t)qlen * kTPB] = make_uint4(
+                        c_prev - 1, (x + (uint32_t)k - 1) | ((first_sk ? 1u : 0u) << 30), prev.pf, (uint32_t)prev.v);
+                    qlen++;
+                }
+                if (inr && !c_known) {
+                    failed = true;
+                    hi_r = 0;
+                }
+                c_prev = first ? x + 1 : (split ? x : c_prev);
+                first_sk = first ? anchored : (first_sk && !split);
+                c_known = first ? anchored : (c_known || split);
+                if (wv) prev = win;
+            };
+
+            uint64_t wi = xb >> 5;
+            uint64_t pw_next = wi < n_words ? packed[wi] : 0ull;
+            uint32_t vw_next = wi < n_words ? valid[wi] : 0u;
+            for (uint32_t r0 = 0; r0 < r_end && !failed; r0 += 32) {  // the same words on every lane
+                uint64_t pw = pw_next;
+                uint32_t vw = vw_next;
+                wi++;
+                pw_next = wi < n_words ? packed[wi] : 0ull;
+                vw_next = wi < n_words ? valid[wi] : 0u;
+#pragma unroll 1
+                for (uint32_t j = 0; j < 32; j += kCheck) {
+                    // a lane gains at most kCheck queue entries between two checks
+                    if (__any_sync(__activemask(), qlen >= kEmitDrain)) drain(kEmitDrain);
+#pragma unroll
+                    for (uint32_t t = 0; t < (uint32_t)kCheck; t++) {
+                        step((uint32_t)pw & 3u, (vw & 1u) != 0, r0 + j + t);
+                        pw >>= 2;
+                        vw >>= 1;
                     }
                 }
-                prev = win;
-                prev_valid = true;
             }
-            drain();
+            drain(1);
             if (!failed) {
                 done = true;
             } else {
@@ -393,7 +408,10 @@ __global__ void __launch_bounds__(256, 3)
         if (!done) atomicOr(status, kStatusLookback);
     }
     __syncthreads();
-    if (threadIdx.x == 0) block_count[bid] = min(s_cnt, region_cap);
+    if (threadIdx.x == 0) {
+        block_count[bid - stage_block0] = min(s_cnt, region_cap);
+        atomicAdd(bc.total, (unsigned long long)s_cnt);
+    }
 }
 
 // Scatter of the staged records into their sub-bin ranges (the device radix partition).
@@ -465,14 +483,19 @@ __device__ unsigned long long block_excl_scan(unsigned long long v, unsigned lon
     return base + x - v;
 }
 
+// field of a scanned word: the whole word, or one half of a packed (high << 32 | low) count
+__device__ __forceinline__ unsigned long long scan_field(unsigned long long x, int field) {
+    return field == 0 ? x : (field == 1 ? (x >> 32) : (x & 0xffffffffull));
+}
+
 __global__ void __launch_bounds__(kScanBlock) scan_partials_kernel(const unsigned long long *__restrict__ in, uint64_t n,
-                                                                   unsigned long long *__restrict__ block_sums) {
+                                                                   int field, unsigned long long *__restrict__ block_sums) {
     __shared__ unsigned long long tmp[32];
     uint64_t base = (uint64_t)blockIdx.x * kScanBlock * kScanItems + (uint64_t)threadIdx.x * kScanItems;
     unsigned long long s = 0;
 #pragma unroll
     for (int j = 0; j < kScanItems; j++)
-        if (base + j < n) s += in[base + j];
+        if (base + j < n) s += scan_field(in[base + j], field);
     unsigned long long total;
     block_excl_scan(s, tmp, total);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
@@ -495,6 +518,7 @@ __global__ void __launch_bounds__(kScanBlock) scan_top_kernel(unsigned long long
 }
 
 __global__ void __launch_bounds__(kScanBlock) scan_final_kernel(const unsigned long long *__restrict__ in, uint64_t n,
+                                                                int field,
                                                                 const unsigned long long *__restrict__ block_sums,
                                                                 unsigned long long *__restrict__ out) {
     __shared__ unsigned long long tmp[32];
@@ -503,7 +527,7 @@ __global__ void __launch_bounds__(kScanBlock) scan_final_kernel(const unsigned l
     unsigned long long s = 0;
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        v[j] = base + j < n ? in[base + j] : 0ull;
+        v[j] = base + j < n ? scan_field(in[base + j], field) : 0ull;
         s += v[j];
     }
     unsigned long long total;
@@ -531,9 +555,15 @@ int launch_pack(const uint8_t *d_text, uint64_t n, uint64_t *packed, uint32_t *v
 }
 
 cudaError_t bucketize_configure() {
-    cudaError_t e = cudaFuncSetAttribute(bucketize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(bucketize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(bucketize_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(bucketize_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(bucketize_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(bucketize_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return e;
 }
 
 BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m) {
@@ -552,47 +582,60 @@ BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m) {
 }
 
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
-                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
-                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, uint32_t block_base,
-                     uint32_t n_blocks, cudaStream_t s) {
+                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_counts,
+                     unsigned long long *bin_kmers, int split_counts, unsigned long long *total_recs, SkRec *stage,
+                     unsigned long long *block_count, unsigned long long ovf_cap, unsigned long long *ovf_cursor,
+                     unsigned *status, uint32_t block_base, uint32_t n_blocks, cudaStream_t s, uint32_t stage_block0,
+                     uint32_t stage_blocks) {
     if (block_base >= g.blocks) return 0;
+    if (stage_blocks == 0) stage_blocks = g.blocks;
     n_blocks = std::min(n_blocks, g.blocks - block_base);
     if (n_blocks == 0) return 0;
-    if (m > 16)
-        bucketize_kernel<true><<<n_blocks, g.threads_per_block, g.smem, s>>>(
-            packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
-            g.region_cap, block_count, ovf_cap, ovf_cursor, status, block_base, g.blocks);
-    else
-        bucketize_kernel<false><<<n_blocks, g.threads_per_block, g.smem, s>>>(
-            packed, valid, n, k, m, bbits, sbits, fbits, canonical, g.chunk, g.lookback, bin_count, bin_kmers, stage,
-            g.region_cap, block_count, ovf_cap, ovf_cursor, status, block_base, g.blocks);
+    const BinCounters bc{bin_counts, bin_kmers, total_recs, split_counts};
+#define GGCAT_BUCKETIZE_LAUNCH(TPB, LONGM)                                                                        \
+    bucketize_kernel<TPB, LONGM><<<n_blocks, TPB, g.smem, s>>>(packed, valid, n, k, m, bbits, sbits, fbits,       \
+                                                              canonical, g.chunk, g.lookback, bc, stage,          \
+                                                              g.region_cap, block_count, ovf_cap, ovf_cursor,     \
+                                                              status, block_base, stage_block0, stage_blocks)
+    if (g.threads_per_block == 256) {
+        if (m > 16)
+            GGCAT_BUCKETIZE_LAUNCH(256, true);
+        else
+            GGCAT_BUCKETIZE_LAUNCH(256, false);
+    } else {
+        if (m > 16)
+            GGCAT_BUCKETIZE_LAUNCH(128, true);
+        else
+            GGCAT_BUCKETIZE_LAUNCH(128, false);
+    }
+#undef GGCAT_BUCKETIZE_LAUNCH
     return 1;
 }
 
 int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
                      const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
                      const unsigned long long *bin_off, unsigned *bin_cursor, SkRec *recs, unsigned *status,
-                     cudaStream_t s) {
-    const uint64_t grid = (uint64_t)g.blocks + (ovf_cap + kOvfSlice - 1) / kOvfSlice;
+                     cudaStream_t s, uint32_t stage_blocks) {
+    if (stage_blocks == 0) stage_blocks = g.blocks;
+    const uint64_t grid = (uint64_t)stage_blocks + (ovf_cap + kOvfSlice - 1) / kOvfSlice;
     if (grid == 0) return 0;
-    partition_kernel<<<(unsigned)grid, 256, 0, s>>>(stage, g.blocks, g.region_cap, block_count, ovf_cursor, ovf_cap,
-                                                    fbits, bin_off, bin_cursor, recs, status);
+    partition_kernel<<<(unsigned)grid, 256, 0, s>>>(stage, stage_blocks, g.region_cap, block_count, ovf_cursor,
+                                                    ovf_cap, fbits, bin_off, bin_cursor, recs, status);
     return 1;
 }
 
 uint64_t scan_temp_elems(uint64_t n) { return (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems) + 1; }
 
 int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
-                          unsigned long long *tmp, cudaStream_t s) {
+                          unsigned long long *tmp, cudaStream_t s, int field) {
     if (n == 0) {
         cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
         return 0;
     }
     uint64_t nb = (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
-    scan_partials_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, tmp);
+    scan_partials_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, field, tmp);
     scan_top_kernel<<<1, kScanBlock, 0, s>>>(tmp, nb, nullptr);
-    scan_final_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, tmp, out);
+    scan_final_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(in, n, field, tmp, out);
     return 3;
 }
 

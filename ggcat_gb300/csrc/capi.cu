@@ -141,7 +141,9 @@ struct ggcat_gpu_ctx {
     // bucketing
     DevBuf<uint64_t> packed;
     DevBuf<uint32_t> valid;
-    DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, scan_tmp;
+    // per sub-bin: bin_count = records << 32 | k-mer instances (packed), or records only with the
+    // k-mer instances in bin_kmers (split counters, after a packed count overflowed)
+    DevBuf<unsigned long long> bin_count, bin_kmers, bin_off, kmer_off, scan_tmp, rec_total;
     DevBuf<unsigned> bin_cursor;  // records placed per sub-bin by the partition
     DevBuf<SkRec> recs, stage;
     DevBuf<unsigned long long> ovf_cursor, block_count;  // staging overflow cursor, records per region
@@ -358,7 +360,6 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     ctx->n_bins = (uint64_t)ctx->n_buckets << ctx->fine_bits;
     const uint64_t nb = ctx->n_bins;
     CK(ctx->bin_count.ensure(nb + 1));
-    CK(ctx->bin_kmers.ensure(nb + 1));
     CK(ctx->bin_off.ensure(nb + 1));
     CK(ctx->kmer_off.ensure(nb + 1));
     CK(ctx->bin_cursor.ensure(nb + 1));
@@ -370,16 +371,19 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     // overflow area of the staging array (records beyond a block's region); retried when exceeded
     uint64_t ovf_cap = text_len / 64 + 4096;
     const uint64_t block_bases = bucketize_block_bases(geo);
+    CK(ctx->rec_total.ensure(1));
+    int split_counts = 0;
     auto bucketize_blocks = [&](uint64_t b0, uint64_t b1) {
         return launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits, p->second_bits,
-                                ctx->fine_bits, canonical, geo, ctx->bin_count.p, ctx->bin_kmers.p, ctx->stage.p,
-                                ctx->block_count.p, ovf_cap, ctx->ovf_cursor.p, ctx->status.p, (uint32_t)b0,
-                                (uint32_t)(b1 - b0), s);
+                                ctx->fine_bits, canonical, geo, ctx->bin_count.p, ctx->bin_kmers.p, split_counts,
+                                ctx->rec_total.p, ctx->stage.p, ctx->block_count.p, ovf_cap, ctx->ovf_cursor.p,
+                                ctx->status.p, (uint32_t)b0, (uint32_t)(b1 - b0), s);
     };
     auto clear_counts = [&]() -> int {
         CK(ctx->stage.ensure((uint64_t)geo.blocks * geo.region_cap + ovf_cap));
         CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
-        CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        if (split_counts) CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(ctx->rec_total.p, 0, sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned), s));
         CK(cudaMemsetAsync(ctx->ovf_cursor.p, 0, sizeof(unsigned long long), s));
         CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
@@ -406,24 +410,40 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[1], s));
     }
-    unsigned long long totals[3];
-    for (int attempt = 0; attempt < 2; attempt++) {
+    unsigned long long totals[4];
+    for (int attempt = 0; attempt < 3; attempt++) {
         if (attempt > 0 || !feed) {
             rc = clear_counts();
             if (rc) return rc;
             ctx->launches += bucketize_blocks(0, geo.blocks);
         }
         CK(cudaGetLastError());
-        ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s);
-        ctx->launches += launch_exclusive_scan(ctx->bin_kmers.p, nb, ctx->kmer_off.p, ctx->scan_tmp.p, s);
+        ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s,
+                                               split_counts ? 0 : 1);
+        ctx->launches += launch_exclusive_scan(split_counts ? ctx->bin_kmers.p : ctx->bin_count.p, nb,
+                                               ctx->kmer_off.p, ctx->scan_tmp.p, s, split_counts ? 0 : 2);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(&totals[2], ctx->ovf_cursor.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&totals[3], ctx->rec_total.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        if (totals[2] <= ovf_cap) break;
-        ovf_cap = totals[2] + 1024;
+        bool again = false;
+        if (!split_counts && totals[0] != totals[3]) {
+            // a packed per-sub-bin count overflowed its 32-bit half: count again with separate
+            // counters
+            split_counts = 1;
+            CK(ctx->bin_kmers.ensure(nb + 1));
+            again = true;
+        }
+        if (totals[2] > ovf_cap) {
+            ovf_cap = totals[2] + 1024;
+            again = true;
+        }
+        if (!again) break;
     }
+    if (totals[0] != totals[3])
+        return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: record count mismatch (%llu vs %llu)", totals[0], totals[3]);
     if (totals[2] > ovf_cap)
         return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: staging overflow (%llu overflow records)", totals[2]);
     ctx->n_recs = totals[0];
@@ -582,7 +602,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
             int n = 0;
             if (cudaMemsetAsync(ctx->counters.p, 0, 16 * sizeof(unsigned long long), q) != cudaSuccess) return -1;
             if (cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), q) != cudaSuccess) return -1;
-            n += launch_classify_units(ctx->bin_off.p, ctx->bin_kmers.p, ctx->n_buckets, ctx->fine_bits, small_limit,
+            n += launch_classify_units(ctx->bin_off.p, ctx->kmer_off.p, ctx->n_buckets, ctx->fine_bits, small_limit,
                                        target, wide_limit, medium_limit, load_pct, ctx->small_units.p, ctx->wide_units.p,
                                        ctx->medium_units.p, ctx->large_units.p, max_units, pool, ctx->counters.p,
                                        ctx->status.p + 1, q);
@@ -602,7 +622,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         const void *ptrs[] = {ctx->packed.p,       ctx->recs.p,        ctx->ext_scratch.p,  ctx->out_bases.p,
                               ctx->out_off.p,      ctx->out_len.p,     ctx->out_flags.p,    ctx->kmer_keys.p,
                               ctx->kmer_mult.p,    ctx->counters.p,    ctx->status.p,       ctx->bin_off.p,
-                              ctx->bin_kmers.p,    ctx->small_units.p, ctx->wide_units.p,   ctx->medium_units.p,
+                              ctx->kmer_off.p,     ctx->small_units.p, ctx->wide_units.p,   ctx->medium_units.p,
                               ctx->large_units.p,  ctx->tkeys.p,       ctx->tvals.p,        ctx->tvis.p,
                               ctx->tlist.p};
         static_assert(sizeof(ptrs) / sizeof(ptrs[0]) <= sizeof(key.ptr) / sizeof(key.ptr[0]), "graph key");
@@ -1130,7 +1150,8 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
         fwrite(F.bases.data() + F.off[i], 1, F.len[i], f);
         fputc('\n', f);
     }
-    fclose(f);
+    const bool write_err = ferror(f) != 0;
+    if (fclose(f) != 0 || write_err) return fail(ctx, GGCAT_GPU_EIO, "error writing %s", output_file);
     return GGCAT_GPU_OK;
 }
 

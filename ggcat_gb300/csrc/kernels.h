@@ -21,21 +21,28 @@ BucketizeGeometry bucketize_geometry(uint64_t n, int k, int m);
 // context, outside any stream capture
 cudaError_t bucketize_configure();
 cudaError_t merge_configure();
+// bin_counts: per sub-bin records << 32 | k-mer instances (one packed atomic per superkmer),
+// or with split_counts records only and k-mer instances in bin_kmers; total_recs receives the
+// record total of all blocks (a packed count that overflowed shows as a smaller scanned total).
+// The staging array holds the regions of blocks [stage_block0, stage_block0 + stage_blocks)
+// (default: all blocks) followed by the overflow area.
 int launch_bucketize(const uint64_t *packed, const uint32_t *valid, uint64_t n, int k, int m, int bbits, int sbits,
-                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_count,
-                     unsigned long long *bin_kmers, SkRec *stage, unsigned long long *block_count,
-                     unsigned long long ovf_cap, unsigned long long *ovf_cursor, unsigned *status, uint32_t block_base,
-                     uint32_t n_blocks, cudaStream_t s);
+                     int fbits, int canonical, const BucketizeGeometry &g, unsigned long long *bin_counts,
+                     unsigned long long *bin_kmers, int split_counts, unsigned long long *total_recs, SkRec *stage,
+                     unsigned long long *block_count, unsigned long long ovf_cap, unsigned long long *ovf_cursor,
+                     unsigned *status, uint32_t block_base, uint32_t n_blocks, cudaStream_t s,
+                     uint32_t stage_block0 = 0, uint32_t stage_blocks = 0);
 // text bases covered by one bucketize block (pieces of a pipelined launch are multiples of it)
 inline uint64_t bucketize_block_bases(const BucketizeGeometry &g) { return (uint64_t)g.threads_per_block * g.chunk; }
 int launch_partition(const SkRec *stage, const BucketizeGeometry &g, const unsigned long long *block_count,
                      const unsigned long long *ovf_cursor, unsigned long long ovf_cap, int fbits,
                      const unsigned long long *bin_off, unsigned *bin_cursor, SkRec *recs, unsigned *status,
-                     cudaStream_t s);
+                     cudaStream_t s, uint32_t stage_blocks = 0);
 uint64_t scan_temp_elems(uint64_t n);
-// out has n+1 entries: exclusive prefix sums and the total at out[n]
+// out has n+1 entries: exclusive prefix sums and the total at out[n]; field 0 scans the words,
+// 1 their high halves, 2 their low halves
 int launch_exclusive_scan(const unsigned long long *in, uint64_t n, unsigned long long *out,
-                          unsigned long long *tmp, cudaStream_t s);
+                          unsigned long long *tmp, cudaStream_t s, int field = 0);
 
 // merge.cu
 struct MergeUnit {
@@ -106,7 +113,8 @@ constexpr int kMergeThreads = 256;
 // Sub-bins of <= small_limit instances are packed into S units (up to unit_target); single
 // sub-bins of <= wide_limit instances are W units (shared-memory table first, spill to the M
 // queue); <= medium_limit: M units; larger: L units.  W, M and L units reserve a global table.
-int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
+// kmer_off: exclusive prefix sums of the per-sub-bin k-mer instances
+int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *kmer_off, uint32_t n_buckets,
                           int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
                           uint64_t medium_limit, uint32_t load_pct, MergeUnit *small_units, MergeUnit *wide_units,
                           MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,

@@ -417,7 +417,7 @@ __device__ __forceinline__ uint32_t table_cap_for(uint64_t kk, uint32_t load_pct
 // and the warp walks them in order with the counts in registers (the same greedy packing on
 // every lane; lane 0 writes the units).
 __global__ void __launch_bounds__(128) classify_units_kernel(
-    const unsigned long long *__restrict__ bin_off, const unsigned long long *__restrict__ bin_kmers, uint32_t n_buckets,
+    const unsigned long long *__restrict__ bin_off, const unsigned long long *__restrict__ kmer_off, uint32_t n_buckets,
     int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit, uint64_t medium_limit, uint32_t load_pct,
     MergeUnit *small_units, MergeUnit *wide_units, MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units,
     uint64_t pool_slots, unsigned long long *counters, unsigned *status) {
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(128) classify_units_kernel(
     for (uint32_t j0 = 0; j0 < nsub; j0 += 32) {
         const uint64_t my_bin = (uint64_t)b * nsub + j0 + (uint32_t)lane;
         const bool in = j0 + (uint32_t)lane < nsub;
-        const uint64_t my_k = in ? bin_kmers[my_bin] : 0ull;
+        const uint64_t my_k = in ? kmer_off[my_bin + 1] - kmer_off[my_bin] : 0ull;
         const uint64_t my_beg = in ? bin_off[my_bin] : 0ull;
         const uint64_t my_end = in ? bin_off[my_bin + 1] : 0ull;
         if (__ballot_sync(0xffffffffu, my_k != 0) == 0) continue;
@@ -1336,13 +1336,13 @@ __global__ void __launch_bounds__(256) large_extend_kernel(MergeArgs a, const Me
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *bin_kmers, uint32_t n_buckets,
+int launch_classify_units(const unsigned long long *bin_off, const unsigned long long *kmer_off, uint32_t n_buckets,
                           int fbits, uint64_t small_limit, uint64_t unit_target, uint64_t wide_limit,
                           uint64_t medium_limit, uint32_t load_pct, MergeUnit *small_units, MergeUnit *wide_units,
                           MergeUnit *medium_units, MergeUnit *large_units, uint64_t max_units, uint64_t pool_slots,
                           unsigned long long *counters, unsigned *status, cudaStream_t s) {
     classify_units_kernel<<<(n_buckets + 3) / 4, 128, 0, s>>>(
-        bin_off, bin_kmers, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, load_pct, small_units,
+        bin_off, kmer_off, n_buckets, fbits, small_limit, unit_target, wide_limit, medium_limit, load_pct, small_units,
         wide_units, medium_units, large_units, max_units, pool_slots, counters, status);
     return 1;
 }

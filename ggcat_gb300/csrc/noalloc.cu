@@ -276,9 +276,12 @@ extern "C" int ggcat_gpu_bucket_histogram_noalloc(const uint8_t *d_text, uint64_
         scratch = noalloc::g_addr[dev];
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // an error left by earlier work is not this call's: report it without clearing it
+    if (cudaPeekAtLastError() != cudaSuccess) return GGCAT_GPU_ECUDA;
     const uint32_t nb = (1u << bucket_bits) + 1;
     const int wn = k - m;
     noalloc::clear_kernel<<<(nb + 255) / 256, 256, 0, s>>>(scratch, nb);
+    if (cudaGetLastError() != cudaSuccess) return GGCAT_GPU_ECUDA;
     if (text_len > 0) {
         const uint64_t chunk = ((512 + wn - 1) / wn) * wn;
         const uint64_t threads = (text_len + chunk - 1) / chunk;
@@ -290,6 +293,7 @@ extern "C" int ggcat_gpu_bucket_histogram_noalloc(const uint8_t *d_text, uint64_
             return GGCAT_GPU_ECUDA;
         noalloc::histogram_kernel<<<(unsigned)((threads + tpb - 1) / tpb), tpb, smem, s>>>(d_text, text_len, k, m,
                                                                                          bucket_bits, chunk, scratch);
+        if (cudaGetLastError() != cudaSuccess) return GGCAT_GPU_ECUDA;
     }
     noalloc::finalize_kernel<<<1, 1024, 0, s>>>(scratch, nb, d_superkmers, d_kmers, d_offsets);
     return cudaGetLastError() == cudaSuccess ? GGCAT_GPU_OK : GGCAT_GPU_ECUDA;

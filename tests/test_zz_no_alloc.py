@@ -27,6 +27,35 @@ def _inputs():
     return [(a, 31, 10, 10), (b, 31, 10, 6), (a, 63, 12, 8)]
 
 
+def _edge_text(k, m, seed=5):
+    """Pieces of length k - 1, k and k + 1, then a long sequence whose N runs and record
+    boundaries sit just before, on and just after multiples of the histogram kernel's
+    per-thread chunk (the pending-first, continued and piece-end paths)."""
+    rng = np.random.default_rng(seed)
+    wn = k - m
+    chunk = ((512 + wn - 1) // wn) * wn
+    pieces = []
+    for ln in (k - 1, k, k + 1) * 6:
+        pieces.append(synth.random_genome(ln, rng))
+    g = synth.random_genome(40 * chunk, rng).copy()
+    offs = (-k, -2, -1, 0, 1, k - 1)
+    for c in range(1, 38):
+        p = c * chunk + offs[c % len(offs)]
+        if c % 3 == 0:
+            g[p:p + 3] = ord("N")
+        else:
+            g[p] = ord("N")
+    pieces.append(g)
+    text = synth.pack_sequences(pieces)[0]
+    # separators on chunk multiples of the whole text too
+    for c in range(3, text.size // chunk, 7):
+        text[c * chunk + offs[c % len(offs)]] = 10
+    return text
+
+
+EDGE_CASES = [(31, 10, 6), (12, 10, 5), (64, 32, 8)]
+
+
 def _expected(ctx, torch, text, k, m, bbits):
     d = torch.from_numpy(text).cuda()
     p = _native.make_params(k=k, m=m, bucket_bits=bbits, second_bits=2)
@@ -73,3 +102,29 @@ def test_noalloc_rejects_too_many_buckets():
     rc = L.ggcat_gpu_bucket_histogram_noalloc(C.c_void_p(d.data_ptr()), 64, 31, 10, 14, C.c_void_p(o.data_ptr()),
                                               C.c_void_p(o.data_ptr()), C.c_void_p(o.data_ptr()), None)
     assert rc == -7  # GGCAT_GPU_ETOOLARGE: more buckets than the static scratch holds
+
+
+def test_noalloc_edge_pieces_and_chunk_boundaries():
+    """Pieces shorter than, equal to and one longer than k, N runs and separators next to the
+    per-thread chunk boundaries, k - m = 2 and k = 64 with m = 32: equal to ggcat_gpu_bucketize."""
+    torch = pytest.importorskip("torch")
+    L = _native.load()
+    ctx = _native.GpuContext(0)
+    try:
+        for k, m, bbits in EDGE_CASES:
+            text = _edge_text(k, m)
+            nb = (1 << bbits) + 1
+            exp = _expected(ctx, torch, text, k, m, bbits)
+            assert exp[0].sum() > 0
+            d_text = torch.from_numpy(text).cuda()
+            outs = [torch.full((n,), 0xDEAD, dtype=torch.int64, device="cuda") for n in (nb, nb, nb + 1)]
+            rc = L.ggcat_gpu_bucket_histogram_noalloc(C.c_void_p(d_text.data_ptr()), d_text.numel(), k, m, bbits,
+                                                      C.c_void_p(outs[0].data_ptr()), C.c_void_p(outs[1].data_ptr()),
+                                                      C.c_void_p(outs[2].data_ptr()),
+                                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+            assert rc == 0
+            torch.cuda.synchronize()
+            for g_, e_ in zip([o.cpu().numpy().astype(np.uint64) for o in outs], exp):
+                assert (g_ == e_).all(), (k, m)
+    finally:
+        ctx.close()
