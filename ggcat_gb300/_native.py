@@ -118,6 +118,10 @@ EXPORTED = [
     "ggcat_gpu_query_wait",
     "ggcat_gpu_query_color_counts",
     "ggcat_gpu_kmer_hashes",
+    "ggcat_gpu_colormap_file",
+    "ggcat_gpu_write_colormap",
+    "ggcat_gpu_dump_colors",
+    "ggcat_gpu_query_colormap",
     "ggcat_gpu_bucket_histogram_noalloc",
 ]
 
@@ -132,6 +136,7 @@ def library_path() -> str:
 
 # ggcat_gpu_dump_fn: (fn_ctx, seq, len, colors, n_colors, same_colors)
 DUMP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int)
+COLORMAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint64)
 # ggcat_gpu_seq_fn and ggcat_gpu_stream
 SEQ_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_uint64)
 READ_BLOCK_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, SEQ_FN, C.c_void_p)
@@ -180,6 +185,10 @@ def load(build: bool = True):
     L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
     L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
     L.ggcat_gpu_dump_unitigs.argtypes = [C.c_char_p, C.c_int, C.c_int, DUMP_FN, C.c_void_p]
+    L.ggcat_gpu_colormap_file.argtypes = [C.c_char_p, C.c_char_p, u64]
+    L.ggcat_gpu_write_colormap.argtypes = [C.c_char_p, C.POINTER(C.c_char_p), u64, P, P, u64]
+    L.ggcat_gpu_dump_colors.argtypes = [C.c_char_p, P, u64, pu64, pu64]
+    L.ggcat_gpu_query_colormap.argtypes = [C.c_char_p, P, u64, C.c_int, COLORMAP_FN, C.c_void_p]
     L.ggcat_gpu_collect_streams.argtypes = [C.POINTER(Stream), u64, C.c_int64, P, u64, pu64]
     L.ggcat_gpu_build_from_streams.argtypes = [P, C.POINTER(Stream), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
@@ -561,3 +570,58 @@ def unitig_lines(bases: np.ndarray, off: np.ndarray, ln: np.ndarray) -> bytes:
     out = bases[np.minimum(src, bases.size - 1)]  # the newline slots are overwritten below
     out[out_start + ln64] = 10
     return out.tobytes()
+
+
+# ---- colormap file ----
+def colormap_file(graph_file: str) -> str:
+    """The colormap path of a graph file (the graph path with its extension replaced by
+    "colors.dat")."""
+    L = load()
+    out = C.create_string_buffer(len(os.fsencode(graph_file)) + 64)
+    rc = L.ggcat_gpu_colormap_file(os.fsencode(graph_file), out, len(out))
+    if rc:
+        raise GgcatGpuError(f"colormap_file failed ({_ERRORS.get(rc, rc)})")
+    return os.fsdecode(out.value)
+
+
+def write_colormap(path: str, color_names: list, subsets: list):
+    """Writes a colormap file: colour names and subsets (each a sorted list of colour indices)."""
+    L = load()
+    names = (C.c_char_p * max(1, len(color_names)))(*[n.encode() for n in color_names])
+    off = np.zeros(len(subsets) + 1, np.uint64)
+    off[1:] = np.cumsum([len(x) for x in subsets])
+    cols = np.ascontiguousarray(np.concatenate([np.asarray(x, np.uint32) for x in subsets]) if subsets
+                                else np.zeros(1, np.uint32), np.uint32)
+    rc = L.ggcat_gpu_write_colormap(os.fsencode(path), names, len(color_names), _ptr(off), _ptr(cols), len(subsets))
+    if rc:
+        raise GgcatGpuError(f"write_colormap failed ({_ERRORS.get(rc, rc)})")
+
+
+def dump_colors(colormap: str) -> list:
+    """Colour names of a colormap, in colour index order (ggcat_dump_colors)."""
+    L = load()
+    nb, nc = C.c_uint64(), C.c_uint64()
+    rc = L.ggcat_gpu_dump_colors(os.fsencode(colormap), None, 0, C.byref(nb), C.byref(nc))
+    if rc:
+        raise GgcatGpuError(f"dump_colors failed ({_ERRORS.get(rc, rc)})")
+    buf = C.create_string_buffer(max(1, nb.value))
+    rc = L.ggcat_gpu_dump_colors(os.fsencode(colormap), buf, nb.value, C.byref(nb), C.byref(nc))
+    if rc:
+        raise GgcatGpuError(f"dump_colors failed ({_ERRORS.get(rc, rc)})")
+    return [x.decode() for x in buf.raw[:nb.value].split(b"\0")[:nc.value]]
+
+
+def query_colormap(colormap: str, subsets) -> dict:
+    """Colours of the given subsets: {subset: [colours]} (ggcat_query_colormap)."""
+    L = load()
+    out = {}
+
+    def cb(_ctx, subset, cols, n):
+        out[int(subset)] = [int(cols[i]) for i in range(n)]
+
+    fn = COLORMAP_FN(cb)
+    q = np.ascontiguousarray(np.asarray(subsets, np.uint32))
+    rc = L.ggcat_gpu_query_colormap(os.fsencode(colormap), _ptr(q), len(q), 1, fn, None)
+    if rc:
+        raise GgcatGpuError(f"query_colormap failed ({_ERRORS.get(rc, rc)})")
+    return out

@@ -291,6 +291,38 @@ int ggcat_gpu_kmer_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_subset, uint64_t
 int ggcat_gpu_subsets_copy(ggcat_gpu_ctx *ctx, uint32_t *h_bitmaps, uint64_t cap_words, uint64_t *n_subsets,
                            uint32_t *words_per_subset);
 
+/* ---- colormap file (the colour subsets of a coloured graph) ----
+ * "<graph>.colors.dat" in the reference's run-length colormap layout
+ * (crates/colors/src/storage/{serializer,run_length,deserializer}.rs): header, LZ4 frame of the
+ * colour names, LZ4 frames of 20000 encoded subsets each, chunk index.  Frames are written with
+ * uncompressed blocks; compressed frames (as the reference writes them) are read too. */
+
+/* GGCATInstance::get_colormap_file / ggcat_get_colormap_file (crates/api/src/lib.rs:385-387,
+ * crates/capi/src/lib.rs:384-390): the graph path with its last extension replaced by
+ * "colors.dat". */
+int ggcat_gpu_colormap_file(const char *graph_file, char *out, uint64_t out_cap);
+
+/* Writes a colormap: colour names, and subset i = colours subset_colors[subset_off[i] ..
+ * subset_off[i + 1]) (strictly ascending, non-empty; subset_off has n_subsets + 1 entries).
+ * The writer half of ColorsSerializer (serializer.rs:56-241). */
+int ggcat_gpu_write_colormap(const char *path, const char *const *color_names, uint64_t n_colors,
+                             const uint64_t *subset_off, const uint32_t *subset_colors, uint64_t n_subsets);
+
+/* ggcat_dump_colors (crates/capi/src/lib.rs:392-401; GGCATInstance::dump_colors,
+ * crates/api/src/lib.rs:392-408): the colour names of a colormap, each '\0'-terminated, in colour
+ * index order.  h_names = NULL queries *names_bytes and *n_colors. */
+int ggcat_gpu_dump_colors(const char *colormap, char *h_names, uint64_t cap, uint64_t *names_bytes,
+                          uint64_t *n_colors);
+
+/* ggcat_query_colormap (crates/capi/src/lib.rs:454-490; dump_colormap_query,
+ * crates/dumper/src/pipeline/dumper_colormap_querying.rs:11-61): fn(fn_ctx, subset, colors,
+ * n_colors) once per distinct requested subset, in ascending subset order, on the calling
+ * thread (so single_thread_output_function holds either way).  A subset id the colormap does
+ * not hold returns GGCAT_GPU_EINVAL. */
+typedef void (*ggcat_gpu_colormap_fn)(void *fn_ctx, uint32_t subset, const uint32_t *colors, uint64_t n_colors);
+int ggcat_gpu_query_colormap(const char *colormap, const uint32_t *subsets, uint64_t n_subsets,
+                             int single_thread_output_function, ggcat_gpu_colormap_fn fn, void *fn_ctx);
+
 /* ---- graph query lookup (querier::run_query, crates/querier/src/lib.rs:54-199) ----
  * The graph's canonical k-mers stay resident in a device hash table; batches of queries are
  * looked up asynchronously in up to GGCAT_GPU_QUERY_SLOTS in-flight slots (each with its own
