@@ -99,9 +99,8 @@ class GGCATInstance:
         gfa_output_version: Optional[int] = None,
     ) -> str:
         """crates/api/src/lib.rs:217-322 — returns the output path ("" on failure, like
-        the C API's ``unwrap_or_default``)."""
-        if colors or color_names:
-            raise GgcatGpuError("coloured builds are not available on the device path yet")
+        the C API's ``unwrap_or_default``).  With ``colors`` every input is one colour and the
+        colormap is written beside the graph (``get_colormap_file``)."""
         if extra_elab not in (ExtraElaboration.NONE, ExtraElaboration.UNITIG_LINKS):
             raise GgcatGpuError("matchtigs, eulertigs and pathtigs are not built")
         gfa = int(gfa_output_version or 0)
@@ -110,13 +109,11 @@ class GGCATInstance:
         L = load()
         arr = (C.c_char_p * len(input_streams))(*[os.fsencode(p) for p in input_streams])
         m = (1 << 64) - 1 if minimizer_length is None else minimizer_length
-        if extra_elab == ExtraElaboration.NONE and gfa == 0:
-            rc = L.ggcat_gpu_build_from_files(self.ctx.h, arr, len(input_streams), os.fsencode(output_file),
-                                              kmer_length, threads_count, int(forward_only), m, min_multiplicity)
-        else:  # the unitigs, then the links / GFA writer on the host
-            rc = L.ggcat_gpu_build_from_files_ex(self.ctx.h, arr, len(input_streams), os.fsencode(output_file),
-                                                 kmer_length, threads_count, int(forward_only), m, min_multiplicity,
-                                                 int(extra_elab), gfa)
+        names = list(color_names or [])
+        carr = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+        rc = L.ggcat_gpu_build_from_files_ex(self.ctx.h, arr, len(input_streams), os.fsencode(output_file), carr,
+                                             len(names), kmer_length, threads_count, int(forward_only), m,
+                                             int(bool(colors)), min_multiplicity, int(extra_elab), gfa)
         if rc != 0:
             msg = L.ggcat_gpu_last_error(self.ctx.h)
             if self.config.messages_callback:
@@ -136,19 +133,53 @@ class GGCATInstance:
         colors: bool = False,
         color_output_format: int = 0,
     ) -> str:
-        """crates/api/src/lib.rs:325-382 for uncoloured graphs: writes the querier's CSV
-        (query_index,matched_kmers,query_kmers,match_percentage) and returns its path ("" on
-        failure, like the C API)."""
-        if colors:
-            raise GgcatGpuError("coloured queries from files need the colormap file, which the device path does not write")
+        """crates/api/src/lib.rs:325-382: the querier's CSV (query_index,matched_kmers,
+        query_kmers,match_percentage), or with ``colors`` the JSON lines of per-colour match
+        fractions (``color_output_format`` 0: colour indices, 1: colour names); returns the
+        output path ("" on failure, like the C API)."""
         L = load()
         out = C.create_string_buffer(4096)
-        rc = L.ggcat_gpu_query_from_files(self.ctx.h, os.fsencode(input_graph), os.fsencode(input_query),
-                                          os.fsencode(output_file_prefix), kmer_length, int(forward_only), out,
-                                          len(out))
+        m = (1 << 64) - 1 if minimizer_length is None else minimizer_length
+        rc = L.ggcat_gpu_query_graph(self.ctx.h, os.fsencode(input_graph), os.fsencode(input_query),
+                                     os.fsencode(output_file_prefix), kmer_length, threads_count, int(forward_only), m,
+                                     int(bool(colors)), int(color_output_format), out, len(out))
         if rc != 0:
             msg = L.ggcat_gpu_last_error(self.ctx.h)
             if self.config.messages_callback:
                 self.config.messages_callback(2, msg.decode() if msg else "")
             return ""
         return out.value.decode()
+
+    @staticmethod
+    def get_colormap_file(graph_file: str) -> str:
+        """crates/api/src/lib.rs:385-387."""
+        from . import _native
+
+        return _native.colormap_file(graph_file)
+
+    @staticmethod
+    def dump_colors(input_colormap: str) -> list:
+        """crates/api/src/lib.rs:392-408: the colour names, by colour index."""
+        from . import _native
+
+        return _native.dump_colors(input_colormap)
+
+    def query_colormap(self, colormap_file: str, subsets, single_thread_output_function: bool,
+                       output_function: Callable[[int, list], None]) -> None:
+        """crates/api/src/lib.rs:412-429: output_function(subset, colours) per distinct subset."""
+        from . import _native
+
+        for sub, cols in sorted(_native.query_colormap(colormap_file, subsets).items()):
+            output_function(sub, cols)
+
+    def dump_unitigs(self, graph_input: str, kmer_length: int, minimizer_length: Optional[int], colors: bool,
+                     threads_count: int, single_thread_output_function: bool,
+                     output_function: Callable[[bytes, list, bool], None]) -> None:
+        """crates/api/src/lib.rs:434-477."""
+        from . import _native
+
+        for item in _native.dump_unitigs(graph_input, kmer_length, colors):
+            if colors:
+                output_function(*item)
+            else:
+                output_function(item, [], False)

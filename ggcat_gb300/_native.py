@@ -113,6 +113,7 @@ EXPORTED = [
     "ggcat_gpu_query_index",
     "ggcat_gpu_query_index_colored",
     "ggcat_gpu_query_from_files",
+    "ggcat_gpu_query_graph",
     "ggcat_gpu_query_submit",
     "ggcat_gpu_query_poll",
     "ggcat_gpu_query_wait",
@@ -167,6 +168,8 @@ def load(build: bool = True):
     L.ggcat_gpu_bucketize.argtypes = [P, P, u64, C.POINTER(Params), P, pu64]
     L.ggcat_gpu_superkmers_copy.argtypes = [P, P, u64, pu64]
     L.ggcat_gpu_merge.argtypes = [P, C.POINTER(Params), P]
+    L.ggcat_gpu_query_graph.argtypes = [P, C.c_char_p, C.c_char_p, C.c_char_p, sz, sz, C.c_int, sz, C.c_int, sz,
+                                        C.c_char_p, u64]
     L.ggcat_gpu_query_from_files.argtypes = [P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_char_p,
                                              u64]
     L.ggcat_gpu_autotune.argtypes = [P, P, u64, C.POINTER(Params), u64, P, C.POINTER(Params),
@@ -192,8 +195,8 @@ def load(build: bool = True):
     L.ggcat_gpu_collect_streams.argtypes = [C.POINTER(Stream), u64, C.c_int64, P, u64, pu64]
     L.ggcat_gpu_build_from_streams.argtypes = [P, C.POINTER(Stream), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
     L.ggcat_gpu_build_from_files.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz]
-    L.ggcat_gpu_build_from_files_ex.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, sz, sz, C.c_int, sz, sz,
-                                                C.c_int, C.c_int]
+    L.ggcat_gpu_build_from_files_ex.argtypes = [P, C.POINTER(C.c_char_p), sz, C.c_char_p, C.POINTER(C.c_char_p), sz,
+                                                sz, sz, C.c_int, sz, C.c_int, sz, C.c_int, C.c_int]
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
     L.ggcat_gpu_kmer_hashes.argtypes = [P, P, u64, C.c_int, C.c_int, P, P]
     L.ggcat_gpu_colors.argtypes = [P, P, P, u64, C.c_uint32, P]
@@ -498,16 +501,22 @@ def unitig_links(bases: np.ndarray, off: np.ndarray, ln: np.ndarray, k: int):
     return lo, other, overlap, flags
 
 
-def dump_unitigs(graph_input: str, k: int) -> list:
-    """ggcat_dump_unitigs for an uncoloured graph: the pieces of the graph FASTA as bytes."""
+def dump_unitigs(graph_input: str, k: int, colors: bool = False) -> list:
+    """ggcat_dump_unitigs: the pieces of the graph FASTA as bytes; with colors, tuples
+    (bases, colours, same_colors) of the single-subset pieces."""
     L = load()
     out = []
 
-    def cb(_ctx, seq, n, _colors, _nc, _same):
-        out.append(C.string_at(seq, n))
+    def cb(_ctx, seq, n, cols, nc, same):
+        b = C.string_at(seq, n)
+        if colors:
+            cp = C.cast(cols, C.POINTER(C.c_uint32))
+            out.append((b, [int(cp[i]) for i in range(nc)], bool(same)))
+        else:
+            out.append(b)
 
     fn = DUMP_FN(cb)
-    rc = L.ggcat_gpu_dump_unitigs(os.fsencode(graph_input), k, 0, fn, None)
+    rc = L.ggcat_gpu_dump_unitigs(os.fsencode(graph_input), k, int(bool(colors)), fn, None)
     if rc:
         raise GgcatGpuError(f"dump_unitigs failed ({_ERRORS.get(rc, rc)})")
     return out

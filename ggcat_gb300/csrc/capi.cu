@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/ggcat_gb300.h"
+#include "colormap.h"
 #include "graph_out.h"
 #include "input.h"
 #include "kernels.h"
@@ -1119,10 +1120,83 @@ static void bucket_counts_for(uint64_t bases, int *bbits, int *sbits) {
     *sbits = s;
 }
 
-// The build of ggcat_build_from_files once its inputs are text: the parameters as the
-// reference derives them, the device build and link, the unitigs written as FASTA.
+// Colour subset of every k-mer of the final unitigs of the last link stage, through the
+// coloured index (built here from the last ggcat_gpu_colors result): subs[kbase[u] + j] is the
+// subset of k-mer j of unitig u.
+static int final_kmer_subsets(ggcat_gpu_ctx *ctx, std::vector<uint32_t> &subs, std::vector<uint64_t> &kbase) {
+    const int k = ctx->last_params.k;
+    int rc = ggcat_gpu_query_index_colored(ctx, nullptr);
+    if (rc) return rc;
+    const HostUnitigs &F = ctx->final_u;
+    const uint64_t n = F.off.size();
+    kbase.assign(n + 1, 0);
+    std::vector<uint32_t> iu, ifirst, icnt;
+    constexpr uint32_t kItem = 512;
+    for (uint64_t u = 0; u < n; u++) {
+        const uint64_t nk = F.len[u] >= (uint32_t)k ? F.len[u] - (uint32_t)k + 1 : 0;
+        kbase[u + 1] = kbase[u] + nk;
+        for (uint64_t j = 0; j < nk; j += kItem) {
+            iu.push_back((uint32_t)u);
+            ifirst.push_back((uint32_t)j);
+            icnt.push_back((uint32_t)std::min<uint64_t>(kItem, nk - j));
+        }
+    }
+    const uint64_t total = kbase[n], ni = iu.size();
+    subs.assign(total, 0xffffffffu);
+    if (!ni) return GGCAT_GPU_OK;
+    DevBuf<uint32_t> d_iu, d_if, d_ic, d_out;
+    DevBuf<uint64_t> d_kb;
+    CK(d_iu.ensure(ni));
+    CK(d_if.ensure(ni));
+    CK(d_ic.ensure(ni));
+    CK(d_kb.ensure(n + 1));
+    CK(d_out.ensure(total));
+    cudaStream_t s = ctx->cap_stream;
+    CK(cudaMemcpyAsync(d_iu.p, iu.data(), ni * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_if.p, ifirst.data(), ni * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_ic.p, icnt.data(), ni * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_kb.p, kbase.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
+    ctx->launches += launch_unitig_subsets(ctx->lk.out_bases.p, ctx->lk.out_off.p, ctx->lk.out_len.p, d_iu.p, d_if.p,
+                                           d_ic.p, ni, d_kb.p, k, ctx->qkeys.p, ctx->qvals.p, ctx->qmask, d_out.p, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(subs.data(), d_out.p, total * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (uint64_t i = 0; i < total; i++)
+        if (subs[i] == 0xffffffffu)
+            return fail(ctx, GGCAT_GPU_EDEVICE, "a k-mer of the final unitigs has no colour subset");
+    return GGCAT_GPU_OK;
+}
+
+// The colormap of the last colour result: subset i = the set bits of its bitmap.
+static int write_colormap_of(ggcat_gpu_ctx *ctx, const std::string &path, const std::vector<std::string> &names) {
+    const uint64_t ns = ctx->c_n_subsets;
+    const int w = ctx->c_words;
+    std::vector<uint32_t> bm(ns * (uint64_t)w);
+    if (!bm.empty()) CK(cudaMemcpy(bm.data(), ctx->csub_arena.p, bm.size() * 4, cudaMemcpyDeviceToHost));
+    const int rc = cmap::write(path.c_str(), names, ns, [&](uint64_t i, std::vector<uint32_t> &out) {
+        out.clear();
+        for (int j = 0; j < w; j++)
+            for (uint32_t x = bm[i * (uint64_t)w + j]; x; x &= x - 1) out.push_back((uint32_t)(32 * j + __builtin_ctz(x)));
+    });
+    if (rc) return fail(ctx, rc, "cannot write the colormap %s", path.c_str());
+    return GGCAT_GPU_OK;
+}
+
+// The build of ggcat_build_from_files / GGCATInstance::build_graph once its inputs are text:
+// the parameters as the reference derives them, the device build (with colours: the colour
+// subsets of every k-mer), the link stage, then the output: FASTA ">{id} LN:i:{len}" with the
+// C:{subset}:{count} runs of a coloured graph and the L: annotations of ExtraElaboration::
+// UnitigLinks, or GFA v1 / v2; with colours also the colormap "<output>.colors.dat".
+// seq_off: with colours, the text offset where each colour's sequences start (colour i =
+// input i, MinBkSingleColor).
 static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text, const char *output_file,
-                           size_t kmer_length, int forward_only, size_t minimizer_length, size_t min_multiplicity) {
+                           size_t kmer_length, int forward_only, size_t minimizer_length, size_t min_multiplicity,
+                           int colors = 0, const std::vector<uint64_t> *seq_off = nullptr,
+                           const std::vector<std::string> *color_names = nullptr, int extra_elab = 0,
+                           int gfa_output_version = 0) {
+    if (colors && gfa_output_version) return fail(ctx, GGCAT_GPU_EINVAL, "GFA output is not supported with colors");
+    if (colors && forward_only)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "coloured forward-only builds are not built (canonical index)");
     const uint64_t est = text.size();
     ggcat_gpu_params p{};
     p.k = (int)kmer_length;
@@ -1138,20 +1212,50 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
     p.hash_kind = GGCAT_HASH_SEQHASH;
     p.forward_only = forward_only;
     p.merge_mode = GGCAT_MERGE_BATCHED;
+    p.keep_kmers = colors ? 1 : 0;
     int rc = ggcat_gpu_build_text(ctx, text.data(), text.size(), &p, nullptr);
     if (rc) return rc;
+    std::vector<std::string> names;
+    if (colors) {
+        const uint64_t nc = seq_off ? seq_off->size() : 0;
+        if (nc == 0 || nc > 65536) return fail(ctx, GGCAT_GPU_EINVAL, "colours need 1 to 65536 inputs (%llu)",
+                                               (unsigned long long)nc);
+        std::vector<uint32_t> col(nc);
+        for (uint64_t i = 0; i < nc; i++) col[i] = (uint32_t)i;
+        rc = ggcat_gpu_colors(ctx, seq_off->data(), col.data(), nc, (uint32_t)nc, nullptr);
+        if (rc) return rc;
+        if (color_names) names = *color_names;
+    }
     rc = ggcat_gpu_link(ctx, p.k);
     if (rc) return rc;
-    FILE *f = fopen(output_file, "wb");
-    if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot write %s", output_file);
     const HostUnitigs &F = ctx->final_u;
-    for (size_t i = 0; i < F.off.size(); i++) {
-        fprintf(f, ">%zu LN:i:%u\n", i, F.len[i]);  // fasta.rs:183-184
-        fwrite(F.bases.data() + F.off[i], 1, F.len[i], f);
-        fputc('\n', f);
+    const uint64_t n = F.off.size();
+    std::vector<uint32_t> subs;
+    std::vector<uint64_t> kbase;
+    if (colors) {
+        rc = final_kmer_subsets(ctx, subs, kbase);
+        if (rc) return rc;
+        rc = write_colormap_of(ctx, ggcat_colormap_path(output_file), names);
+        if (rc) return rc;
     }
-    const bool write_err = ferror(f) != 0;
-    if (fclose(f) != 0 || write_err) return fail(ctx, GGCAT_GPU_EIO, "error writing %s", output_file);
+    // " C:{subset:x}:{count}" per run of equal subsets along the unitig (multiple.rs:705-740)
+    HeaderExtra runs = [&](uint64_t u, std::string &line) {
+        char buf[48];
+        uint64_t j = kbase[u];
+        while (j < kbase[u + 1]) {
+            uint64_t e = j + 1;
+            while (e < kbase[u + 1] && subs[e] == subs[j]) e++;
+            snprintf(buf, sizeof buf, " C:%x:%llu", subs[j], (unsigned long long)(e - j));
+            line += buf;
+            j = e;
+        }
+    };
+    std::vector<uint64_t> off64(F.off.data(), F.off.data() + n), len64(n);
+    for (uint64_t i = 0; i < n; i++) len64[i] = F.len[i];
+    std::string err;
+    rc = ggcat::write_graph_arrays(F.bases.data(), off64.data(), len64.data(), n, p.k, extra_elab == 1,
+                                   gfa_output_version, colors ? &runs : nullptr, output_file, err);
+    if (rc) return fail(ctx, rc, "%s", err.c_str());
     return GGCAT_GPU_OK;
 }
 
@@ -1183,34 +1287,34 @@ extern "C" int ggcat_gpu_build_from_streams(ggcat_gpu_ctx *ctx, const ggcat_gpu_
     return build_and_write(ctx, text, output_file, kmer_length, forward_only, minimizer_length, min_multiplicity);
 }
 
-// ggcat_build_from_files with its extra_elab and gfa_output_version arguments
-// (crates/capi/src/lib.rs:58-139): the unitigs are built to a temporary FASTA, which the
-// links / GFA writer of graph_out.cpp rewrites into output_file
+// ggcat_build_from_files with every argument (crates/capi/src/lib.rs:58-139, same order):
+// colour names and colours (colour i = input file i), extra_elab (0 none, 1 unitig links;
+// 2-4 matchtigs, eulertigs, pathtigs are not built) and gfa_output_version (0 FASTA, 1, 2)
 extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
-                                             const char *output_file, size_t kmer_length, size_t threads_count,
-                                             int forward_only, size_t minimizer_length, size_t min_multiplicity,
-                                             int extra_elab, int gfa_output_version) {
-    if (!ctx || !output_file) return GGCAT_GPU_EINVAL;
+                                             const char *output_file, const char *const *color_names,
+                                             size_t n_color_names, size_t kmer_length, size_t threads_count,
+                                             int forward_only, size_t minimizer_length, int colors,
+                                             size_t min_multiplicity, int extra_elab, int gfa_output_version) {
+    if (!ctx || !input_files || !output_file || (n_color_names && !color_names)) return GGCAT_GPU_EINVAL;
     if (extra_elab < 0 || extra_elab > 4 || gfa_output_version < 0 || gfa_output_version > 2)
         return fail(ctx, GGCAT_GPU_EINVAL, "extra_elab %d / gfa_output_version %d out of range", extra_elab,
                     gfa_output_version);
     if (extra_elab >= 2)
         return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "matchtigs, eulertigs and pathtigs are not built");
-    if (extra_elab == 0 && gfa_output_version == 0)
-        return ggcat_gpu_build_from_files(ctx, input_files, n_inputs, output_file, kmer_length, threads_count,
-                                          forward_only, minimizer_length, min_multiplicity);
-    const std::string tmp = std::string(output_file) + ".unitigs.tmp.fa";
-    int rc = ggcat_gpu_build_from_files(ctx, input_files, n_inputs, tmp.c_str(), kmer_length, threads_count,
-                                        forward_only, minimizer_length, min_multiplicity);
-    if (rc) {
-        std::remove(tmp.c_str());
-        return rc;
+    std::vector<uint8_t> text;
+    std::vector<uint64_t> file_off;
+    {
+        const int nt = threads_count > 0 ? (int)std::min<size_t>(threads_count, 1024)
+                                         : (int)std::max(1u, std::thread::hardware_concurrency());
+        std::string err;
+        const int rc = ggcat::read_sequences_files(input_files, n_inputs, (int64_t)kmer_length - 1, nt, text, err,
+                                                   &file_off);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
     }
-    std::string err;
-    rc = ggcat::write_graph(tmp.c_str(), output_file, (int)kmer_length, extra_elab == 1, gfa_output_version, err);
-    std::remove(tmp.c_str());
-    if (rc) return fail(ctx, rc, "%s", err.c_str());
-    return GGCAT_GPU_OK;
+    std::vector<std::string> names;
+    for (size_t i = 0; i < n_color_names; i++) names.emplace_back(color_names[i] ? color_names[i] : "");
+    return build_and_write(ctx, text, output_file, kmer_length, forward_only, minimizer_length, min_multiplicity,
+                           colors, &file_off, &names, extra_elab, gfa_output_version);
 }
 
 // ---------------------------------------------------------------------------
@@ -1492,37 +1596,219 @@ extern "C" int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64
 }
 
 // ---------------------------------------------------------------------------
-// file-level query: the uncoloured path of GGCATInstance::query_graph
+// file-level query: GGCATInstance::query_graph
 // ---------------------------------------------------------------------------
-extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
-                                          const char *output_prefix, int k, int forward_only, char *out_path,
-                                          uint64_t out_cap) {
-    if (!ctx) return GGCAT_GPU_EINVAL;
-    if (!graph_fasta || !query_fasta || !output_prefix) return fail(ctx, GGCAT_GPU_EINVAL, "null path");
-    if (forward_only) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
-    // graph: the unitigs as text (records cut like the reference's reader, k-1 copyback)
-    std::vector<uint8_t> graph;
-    {
-        std::string err;
-        const int rc = ggcat::read_sequences(graph_fasta, k - 1, graph, nullptr, nullptr, err);
-        if (rc) return fail(ctx, rc, "%s", err.c_str());
-    }
-    CK(cudaSetDevice(ctx->device));
-    CK(ctx->qgraph.ensure(graph.size() + 64));
-    if (!graph.empty()) CK(cudaMemcpy(ctx->qgraph.p, graph.data(), graph.size(), cudaMemcpyHostToDevice));
-    int rc = ggcat_gpu_query_index(ctx, ctx->qgraph.p, graph.size(), k, nullptr);
+
+// A coloured graph's FASTA (as build_and_write or the reference writes it: ">{id} LN:i:{len}
+// C:{subset:x}:{count}... [L:...]" then the bases, possibly over several lines, plain or
+// compressed by its extension): the unitigs in the text layout and, per text position, the
+// colour subset of the k-mer starting there.
+static int read_colored_graph(const char *path, int k, std::vector<uint8_t> &text, std::vector<uint32_t> &pos_subset,
+                              std::string &err) {
+    std::vector<uint8_t> raw;
+    int rc = ggcat::read_input_file(path, raw, err);
     if (rc) return rc;
+    text.clear();
+    pos_subset.clear();
+    std::vector<std::pair<uint32_t, uint64_t>> runs;
+    bool in_rec = false;
+    uint64_t rec_start = 0;
+    auto close_rec = [&]() -> bool {
+        if (!in_rec) return true;
+        const uint64_t len = text.size() - rec_start;
+        uint64_t nk = len >= (uint64_t)k ? len - (uint64_t)k + 1 : 0, covered = 0;
+        pos_subset.resize(text.size() + 1, 0xffffffffu);
+        for (const auto &r : runs) {
+            for (uint64_t j = 0; j < r.second && covered + j < nk; j++) pos_subset[rec_start + covered + j] = r.first;
+            covered += r.second;
+        }
+        text.push_back('\n');
+        in_rec = false;
+        return covered == nk;
+    };
+    const uint8_t *p = raw.data(), *end = raw.data() + raw.size();
+    while (p < end) {
+        const uint8_t *nl = static_cast<const uint8_t *>(memchr(p, '\n', (size_t)(end - p)));
+        const uint8_t *le = nl ? nl : end;
+        const uint8_t *lend = (le > p && le[-1] == '\r') ? le - 1 : le;
+        if (p < lend && *p == '>') {
+            if (!close_rec()) return err = std::string(path) + ": colour runs do not cover a unitig", GGCAT_GPU_EIO;
+            runs.clear();
+            // tokens " C:{hex}:{count}"
+            for (const uint8_t *q = p; q + 3 < lend; q++) {
+                if (q[0] == ' ' && q[1] == 'C' && q[2] == ':') {
+                    char *e1 = nullptr, *e2 = nullptr;
+                    const std::string tok(reinterpret_cast<const char *>(q + 3), (size_t)(lend - q - 3));
+                    const unsigned long sub = strtoul(tok.c_str(), &e1, 16);
+                    if (!e1 || *e1 != ':') return err = std::string(path) + ": bad C: annotation", GGCAT_GPU_EIO;
+                    const unsigned long long cnt = strtoull(e1 + 1, &e2, 10);
+                    runs.emplace_back((uint32_t)sub, (uint64_t)cnt);
+                }
+            }
+            rec_start = text.size();
+            in_rec = true;
+        } else if (in_rec) {
+            for (const uint8_t *q = p; q < lend; q++) {
+                const uint8_t c = *q & 0xDF;
+                text.push_back((c == 'A' || c == 'C' || c == 'G' || c == 'T') ? c : 'N');
+            }
+        }
+        p = nl ? nl + 1 : end;
+    }
+    if (!close_rec()) return err = std::string(path) + ": colour runs do not cover a unitig", GGCAT_GPU_EIO;
+    pos_subset.resize(text.size(), 0xffffffffu);
+    return GGCAT_GPU_OK;
+}
+
+// The coloured branch of ggcat_dump_unitigs (dumper::dump_unitigs,
+// crates/dumper/src/pipeline/dumper_colormap_reading.rs:62-146): every k-mer of the graph once,
+// in pieces of one colour subset (maximal runs of equal subsets along a unitig), grouped by
+// subset in ascending order; colors = the subset's colours from the colormap, same_colors = 1
+// for every piece of a group but the first.
+int dump_colored_unitigs(const char *graph_input, int k, ggcat_gpu_dump_fn fn, void *fn_ctx) {
+    std::vector<uint8_t> graph;
+    std::vector<uint32_t> pos_subset;
+    std::string err;
+    int rc = read_colored_graph(graph_input, k, graph, pos_subset, err);
+    if (rc) return rc;
+    cmap::Reader cm;
+    rc = cm.open(ggcat_colormap_path(graph_input).c_str(), &err);
+    if (rc) return rc;
+    struct Piece {
+        uint32_t subset;
+        uint64_t start, kmers;
+    };
+    std::vector<Piece> pieces;
+    for (uint64_t p = 0; p < pos_subset.size();) {
+        if (pos_subset[p] == 0xffffffffu) {
+            p++;
+            continue;
+        }
+        uint64_t e = p + 1;
+        while (e < pos_subset.size() && pos_subset[e] == pos_subset[p]) e++;
+        pieces.push_back(Piece{pos_subset[p], p, e - p});
+        p = e;
+    }
+    std::stable_sort(pieces.begin(), pieces.end(), [](const Piece &a, const Piece &b) { return a.subset < b.subset; });
+    std::vector<uint32_t> cols;
+    for (size_t i = 0; i < pieces.size(); i++) {
+        const bool same = i > 0 && pieces[i - 1].subset == pieces[i].subset;
+        if (!same && !cm.get(pieces[i].subset, cols)) return GGCAT_GPU_EIO;
+        fn(fn_ctx, graph.data() + pieces[i].start, pieces[i].kmers + (uint64_t)k - 1, cols.data(), cols.size(),
+           same ? 1 : 0);
+    }
+    return GGCAT_GPU_OK;
+}
+
+// The query output path: output_file_prefix with `ext` when it has no extension
+// (Path::with_extension of an extension-less path, querier/src/lib.rs:190)
+static std::string query_output_path(const char *prefix, const char *ext) {
+    std::string path = prefix;
+    const size_t slash = path.find_last_of('/');
+    const size_t dot = path.find_last_of('.');
+    const size_t name = slash == std::string::npos ? 0 : slash + 1;
+    if (dot == std::string::npos || dot < name || dot == name) path += std::string(".") + ext;
+    return path;
+}
+
+// Rust's f64 "{:.2}" for the fractions of the query outputs
+static void fmt_frac(char *num, size_t cap, double frac) {
+    if (std::isnan(frac))
+        snprintf(num, cap, "NaN");
+    else if (std::isinf(frac))
+        snprintf(num, cap, "inf");
+    else
+        snprintf(num, cap, "%.2f", frac);
+}
+
+static int query_graph_impl(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
+                            const char *output_prefix, int k, int colors, int color_output_format, char *out_path,
+                            uint64_t out_cap) {
+    CK(cudaSetDevice(ctx->device));
+    std::vector<std::string> color_names;
+    uint32_t n_colors = 0;
+    if (!colors) {
+        // graph: the unitigs as text (records cut like the reference's reader, k-1 copyback)
+        std::vector<uint8_t> graph;
+        std::string err;
+        int rc = ggcat::read_sequences(graph_fasta, k - 1, graph, nullptr, nullptr, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+        CK(ctx->qgraph.ensure(graph.size() + 64));
+        if (!graph.empty()) CK(cudaMemcpy(ctx->qgraph.p, graph.data(), graph.size(), cudaMemcpyHostToDevice));
+        rc = ggcat_gpu_query_index(ctx, ctx->qgraph.p, graph.size(), k, nullptr);
+        if (rc) return rc;
+    } else {
+        // coloured graph: the k-mers' subsets from the C: runs, the subsets' colours from the
+        // colormap beside the graph (colormap_reading.rs:28-183 reads the same two files)
+        std::vector<uint8_t> graph;
+        std::vector<uint32_t> pos_subset;
+        std::string err;
+        int rc = read_colored_graph(graph_fasta, k, graph, pos_subset, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+        cmap::Reader cm;
+        const std::string cpath = ggcat_colormap_path(graph_fasta);
+        rc = cm.open(cpath.c_str(), &err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+        color_names = cm.names;
+        n_colors = (uint32_t)std::max<uint64_t>(cm.colors_count, 1);
+        const int words = (int)((n_colors + 31) / 32);
+        std::vector<uint32_t> bm(cm.subsets_count * (uint64_t)words, 0), cols;
+        for (uint64_t sidx = 0; sidx < cm.subsets_count; sidx++) {
+            if (!cm.get((uint32_t)sidx, cols))
+                return fail(ctx, GGCAT_GPU_EIO, "%s: bad subset %llu", cpath.c_str(), (unsigned long long)sidx);
+            for (uint32_t c : cols) {
+                if (c >= n_colors) return fail(ctx, GGCAT_GPU_EIO, "%s: colour %u out of range", cpath.c_str(), c);
+                bm[sidx * words + c / 32] |= 1u << (c % 32);
+            }
+        }
+        for (uint32_t v : pos_subset)
+            if (v != 0xffffffffu && v >= cm.subsets_count)
+                return fail(ctx, GGCAT_GPU_EIO, "%s: subset %u not in the colormap", graph_fasta, v);
+        const uint64_t kw = k > 32 ? 2 : 1;
+        uint64_t cap = 1024;
+        while (cap < 2 * graph.size() + 64) cap <<= 1;
+        CK(ctx->qgraph.ensure(graph.size() + 64));
+        DevBuf<uint32_t> d_pos;
+        CK(d_pos.ensure(graph.size() + 1));
+        CK(ctx->qkeys.ensure(cap * kw));
+        CK(ctx->qvals.ensure(cap));
+        CK(ctx->csub_arena.ensure(bm.size() + 1));
+        cudaStream_t s = ctx->cap_stream;
+        if (!graph.empty()) {
+            CK(cudaMemcpyAsync(ctx->qgraph.p, graph.data(), graph.size(), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_pos.p, pos_subset.data(), graph.size() * 4, cudaMemcpyHostToDevice, s));
+        }
+        if (!bm.empty()) CK(cudaMemcpyAsync(ctx->csub_arena.p, bm.data(), bm.size() * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(ctx->qkeys.p, 0xff, cap * kw * sizeof(uint64_t), s));
+        CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
+        ctx->launches += launch_index_insert(ctx->qgraph.p, graph.size(), k, ctx->qkeys.p, ctx->qvals.p, cap - 1,
+                                             ctx->status.p + 1, s, d_pos.p);
+        CK(cudaGetLastError());
+        unsigned st = 0;
+        CK(cudaMemcpyAsync(&st, ctx->status.p + 1, sizeof st, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (st) return fail(ctx, GGCAT_GPU_EDEVICE, "query index: table full");
+        ctx->have_colors = false;  // the colour state now describes the loaded graph's subsets
+        ctx->c_words = words;
+        ctx->c_colors = n_colors;
+        ctx->c_n_subsets = cm.subsets_count;
+        ctx->qmask = cap - 1;
+        ctx->qk = k;
+        ctx->qcolored = true;
+        ctx->qready = true;
+    }
     // queries: one per record the reader emits (FASTA records with bases, every FASTQ
     // record; never cut), submitted in batches of bounded text size
     std::vector<uint8_t> qtext;
     std::vector<uint64_t> qoff, qlen;
     {
         std::string err;
-        rc = ggcat::read_sequences(query_fasta, -1, qtext, &qoff, &qlen, err);
+        const int rc = ggcat::read_sequences(query_fasta, -1, qtext, &qoff, &qlen, err);
         if (rc) return fail(ctx, rc, "%s", err.c_str());
     }
     const uint64_t nq = qoff.size();
-    std::vector<uint64_t> matched(nq, 0);
+    std::vector<uint64_t> matched(nq, 0), counts;
+    if (colors) counts.assign(nq * (uint64_t)n_colors, 0);
     const uint64_t kBatchBytes = 256ull << 20;
     for (uint64_t a = 0; a < nq;) {
         uint64_t b = a + 1;
@@ -1533,42 +1819,100 @@ extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_
             o[i - a] = qoff[i] - lo;
             l[i - a] = qlen[i];
         }
-        rc = ggcat_gpu_query_submit(ctx, 0, qtext.data() + lo, hi - lo, o.data(), l.data(), b - a);
+        int rc = ggcat_gpu_query_submit(ctx, 0, qtext.data() + lo, hi - lo, o.data(), l.data(), b - a);
         if (rc) return rc;
         uint64_t got = 0;
         rc = ggcat_gpu_query_wait(ctx, 0, matched.data() + a, b - a, &got);
         if (rc) return rc;
+        if (colors) {
+            uint32_t ncol = 0;
+            rc = ggcat_gpu_query_color_counts(ctx, 0, counts.data() + a * n_colors, (b - a) * n_colors, &ncol);
+            if (rc) return rc;
+        }
         a = b;
     }
-    // the CSV of counters_sorting (crates/querier/src/pipeline/counters_sorting.rs:235-268):
-    // query_index, matched_kmers, query_kmers = len - (k - 1), matched / query_kmers to 2 places
-    std::string path = output_prefix;
-    {
-        const size_t slash = path.find_last_of('/');
-        const size_t dot = path.find_last_of('.');
-        if (dot == std::string::npos || (slash != std::string::npos && dot < slash) || dot == slash + 1) path += ".csv";
-    }
+    const std::string path = query_output_path(output_prefix, colors ? "jsonl" : "csv");
     FILE *f = fopen(path.c_str(), "wb");
     if (!f) return fail(ctx, GGCAT_GPU_EIO, "cannot write %s", path.c_str());
-    fprintf(f, "query_index,matched_kmers,query_kmers,match_percentage\n");
-    for (uint64_t i = 0; i < nq; i++) {
-        const uint64_t qk = qlen[i] >= (uint64_t)(k - 1) ? qlen[i] - (uint64_t)(k - 1) : 0;
-        const double frac = (double)matched[i] / (double)qk;
-        char num[64];
-        if (std::isnan(frac))
-            snprintf(num, sizeof num, "NaN");
-        else if (std::isinf(frac))
-            snprintf(num, sizeof num, "inf");
-        else
-            snprintf(num, sizeof num, "%.2f", frac);
-        fprintf(f, "%llu,%llu,%llu,%s\n", (unsigned long long)i, (unsigned long long)matched[i],
-                (unsigned long long)qk, num);
+    char num[64];
+    if (!colors) {
+        // the CSV of counters_sorting (crates/querier/src/pipeline/counters_sorting.rs:235-268):
+        // query_index, matched_kmers, query_kmers = len - (k - 1), matched / query_kmers to 2 places
+        fprintf(f, "query_index,matched_kmers,query_kmers,match_percentage\n");
+        for (uint64_t i = 0; i < nq; i++) {
+            const uint64_t qk = qlen[i] >= (uint64_t)(k - 1) ? qlen[i] - (uint64_t)(k - 1) : 0;
+            fmt_frac(num, sizeof num, (double)matched[i] / (double)qk);
+            fprintf(f, "%llu,%llu,%llu,%s\n", (unsigned long long)i, (unsigned long long)matched[i],
+                    (unsigned long long)qk, num);
+        }
+    } else {
+        // JSON lines of colored_query_output.rs:264-309: queries with at least one match, in
+        // index order; per colour present, the query k-mers found in it over the query's k-mers
+        // to 2 places, keyed by the colour index or its JSON-escaped name (the reference escapes
+        // '"' first, then '\' -- also the backslash it has just added)
+        std::vector<std::string> esc(color_names.size());
+        for (size_t c = 0; c < color_names.size(); c++) {
+            std::string a;
+            for (char ch : color_names[c]) {
+                if (ch == '"') a += "\\\"";
+                else a += ch;
+            }
+            std::string b2;
+            for (char ch : a) {
+                if (ch == '\\') b2 += "\\\\";
+                else b2 += ch;
+            }
+            esc[c] = b2;
+        }
+        for (uint64_t i = 0; i < nq; i++) {
+            const uint64_t *cc = counts.data() + i * n_colors;
+            bool any = false;
+            for (uint32_t c = 0; c < n_colors && !any; c++) any = cc[c] != 0;
+            if (!any) continue;
+            const uint64_t qk = qlen[i] >= (uint64_t)(k - 1) ? qlen[i] - (uint64_t)(k - 1) : 0;
+            fprintf(f, "{\"query_index\":%llu, \"matches\":{", (unsigned long long)i);
+            bool first = true;
+            for (uint32_t c = 0; c < n_colors; c++) {
+                if (!cc[c]) continue;
+                fmt_frac(num, sizeof num, (double)cc[c] / (double)qk);
+                if (color_output_format == 1 && c < esc.size())
+                    fprintf(f, "%s\"%s\": %s", first ? "" : ",", esc[c].c_str(), num);
+                else
+                    fprintf(f, "%s\"%u\": %s", first ? "" : ",", c, num);
+                first = false;
+            }
+            fprintf(f, "}}\n");
+        }
     }
-    fclose(f);
-    if (out_path && out_cap) {
-        snprintf(out_path, out_cap, "%s", path.c_str());
-    }
+    const bool werr = ferror(f) != 0;
+    if (fclose(f) != 0 || werr) return fail(ctx, GGCAT_GPU_EIO, "error writing %s", path.c_str());
+    if (out_path && out_cap) snprintf(out_path, out_cap, "%s", path.c_str());
     return GGCAT_GPU_OK;
+}
+
+extern "C" int ggcat_gpu_query_graph(ggcat_gpu_ctx *ctx, const char *input_graph, const char *input_query,
+                                     const char *output_file_prefix, size_t kmer_length, size_t threads_count,
+                                     int forward_only, size_t minimizer_length, int colors, size_t color_output_format,
+                                     char *out_path, uint64_t out_cap) {
+    (void)threads_count;     // the files are read on the calling thread; the lookup is on the device
+    (void)minimizer_length;  // the device index needs no minimizer bucketing
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    if (!input_graph || !input_query || !output_file_prefix) return fail(ctx, GGCAT_GPU_EINVAL, "null path");
+    if (kmer_length < 3 || kmer_length > 64)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "query supports k <= 64 (k=%zu)", kmer_length);
+    if (forward_only) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "the device query index is canonical (forward_only=1)");
+    if (color_output_format > 1)
+        return fail(ctx, GGCAT_GPU_EINVAL, "color_output_format %zu is not 0 (numbers) or 1 (names)",
+                    color_output_format);
+    return query_graph_impl(ctx, input_graph, input_query, output_file_prefix, (int)kmer_length, colors ? 1 : 0,
+                            (int)color_output_format, out_path, out_cap);
+}
+
+extern "C" int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
+                                          const char *output_prefix, int k, int forward_only, char *out_path,
+                                          uint64_t out_cap) {
+    return ggcat_gpu_query_graph(ctx, graph_fasta, query_fasta, output_prefix, (size_t)(k > 0 ? k : 0), 0,
+                                 forward_only, (size_t)-1, 0, 0, out_path, out_cap);
 }
 
 // ---------------------------------------------------------------------------

@@ -141,23 +141,33 @@ int write_graph(const char *unitigs_fasta, const char *output_file, int k, int w
     std::vector<uint64_t> off, len;
     int rc = read_sequences(unitigs_fasta, -1, text, &off, &len, err);
     if (rc) return rc;
-    const uint64_t n = off.size();
+    return write_graph_arrays(text.data(), off.data(), len.data(), off.size(), k, with_links, gfa_version, nullptr,
+                              output_file, err);
+}
+
+int write_graph_arrays(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k,
+                       int with_links, int gfa_version, const HeaderExtra *extra, const char *output_file,
+                       std::string &err) {
+    if (gfa_version != 0 && gfa_version != 1 && gfa_version != 2)
+        return err = "gfa_version must be 0 (FASTA), 1 or 2", GGCAT_GPU_EINVAL;
     std::vector<UnitigLink> links;
     std::vector<uint64_t> lo;
     if (with_links) {
-        rc = unitig_links(text.data(), off.data(), len.data(), n, k, links, lo, err);
+        const int rc = unitig_links(bases, off, len, n, k, links, lo, err);
         if (rc) return rc;
     }
     FILE *f = fopen(output_file, "wb");
     if (!f) return err = std::string("cannot write ") + output_file, GGCAT_GPU_EIO;
     std::string line;
     for (uint64_t i = 0; i < n; i++) {
-        const char *seq = reinterpret_cast<const char *>(text.data() + off[i]);
+        const char *seq = reinterpret_cast<const char *>(bases + off[i]);
         const unsigned long long L = len[i];
         char buf[128];
         if (gfa_version == 0) {
+            // ">id LN:i:len", then the colour runs, then the links (fasta.rs:183-211)
             snprintf(buf, sizeof buf, ">%llu LN:i:%llu", (unsigned long long)i, L);
             line = buf;
+            if (extra) (*extra)(i, line);
             if (with_links)
                 for (uint64_t j = lo[2 * i]; j < lo[2 * i + 2]; j++) {
                     snprintf(buf, sizeof buf, " L:%c:%llu:%c", (links[j].flags & 1) ? '-' : '+',
@@ -243,9 +253,11 @@ extern "C" int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *outp
     return rc;
 }
 
+int dump_colored_unitigs(const char *graph_input, int k, ggcat_gpu_dump_fn fn, void *fn_ctx);  // capi.cu
+
 extern "C" int ggcat_gpu_dump_unitigs(const char *graph_input, int k, int colors, ggcat_gpu_dump_fn fn, void *fn_ctx) {
     if (!graph_input || !fn || k < 2) return GGCAT_GPU_EINVAL;
-    if (colors) return GGCAT_GPU_EUNSUPPORTED;  // needs the colormap file, which is not built
+    if (colors) return dump_colored_unitigs(graph_input, k, fn, fn_ctx);
     std::vector<uint8_t> text;
     std::vector<uint64_t> off, len;
     std::string err;

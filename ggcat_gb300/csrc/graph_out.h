@@ -1,6 +1,7 @@
 // Graph output on the host (graph_out.cpp): maximal-unitig links and the FASTA / GFA writers.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -22,5 +23,13 @@ int unitig_links(const uint8_t *bases, const uint64_t *off, const uint64_t *len,
 // annotations (gfa_version 0, with_links 1) or as GFA v1 / v2 (links when with_links)
 int write_graph(const char *unitigs_fasta, const char *output_file, int k, int with_links, int gfa_version,
                 std::string &err);
+
+// appends header content of unitig i after ">i LN:i:len" (the colour runs of a coloured graph)
+typedef std::function<void(uint64_t, std::string &)> HeaderExtra;
+
+// the same from unitigs in memory (bases[off[i], off[i] + len[i]), index order)
+int write_graph_arrays(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k,
+                       int with_links, int gfa_version, const HeaderExtra *extra, const char *output_file,
+                       std::string &err);
 
 }  // namespace ggcat

@@ -582,7 +582,7 @@ int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &tex
 }
 
 int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
-                         std::string &err) {
+                         std::string &err, std::vector<uint64_t> *file_off) {
     // each file into its own buffer on a pool of threads (files are claimed in order), then
     // concatenated in input order: the same text as reading them one after another
     std::vector<std::vector<uint8_t>> parts(n);
@@ -607,7 +607,9 @@ int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, i
     }
     text.clear();
     text.reserve(total);
+    if (file_off) file_off->clear();
     for (auto &p : parts) {
+        if (file_off) file_off->push_back(text.size());
         text.insert(text.end(), p.begin(), p.end());
         std::vector<uint8_t>().swap(p);
     }

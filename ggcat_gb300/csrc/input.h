@@ -26,8 +26,9 @@ int read_sequences(const char *path, int64_t copyback, std::vector<uint8_t> &tex
                    std::vector<uint64_t> *len, std::string &err, int threads = 1);
 // the sequences the streams emit, normalised, each followed by '\n', appended to text
 int collect_streams(const ggcat_gpu_stream *streams, size_t n, int64_t copyback, std::vector<uint8_t> &text);
-// several files on up to `threads` threads, concatenated in input order into text
+// several files on up to `threads` threads, concatenated in input order into text; file_off
+// (optional) receives the text offset where each file's sequences start
 int read_sequences_files(const char *const *paths, size_t n, int64_t copyback, int threads, std::vector<uint8_t> &text,
-                         std::string &err);
+                         std::string &err, std::vector<uint64_t> *file_off = nullptr);
 
 }  // namespace ggcat

@@ -143,8 +143,9 @@ int merge_ctas_per_sm(int tier, int wide);
 
 // query.cu
 // uncoloured index keys: u64 for k <= 32, u128 (16-byte aligned) for k <= 64
+// pos_val (optional): the value of the k-mer starting at each text position (else 0)
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
-                        unsigned *status, cudaStream_t s);
+                        unsigned *status, cudaStream_t s, const uint32_t *pos_val = nullptr);
 // cslots: the colour phase's {key, id} table of ccap slots
 // keys: u64 (wide = 0) or u128 query table keys, 16-byte aligned
 int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32_t *id_subset, int wide, void *keys,
@@ -156,6 +157,13 @@ int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const 
                        const void *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
                        uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,
                        unsigned long long *queue, int sms, cudaStream_t s);
+
+// per-k-mer colour subsets of the final unitigs through the coloured index (items of at most
+// a few hundred k-mers of one unitig)
+int launch_unitig_subsets(const uint8_t *bases, const uint64_t *u_off, const uint32_t *u_len,
+                          const uint32_t *item_unitig, const uint32_t *item_first, const uint32_t *item_count,
+                          uint64_t n_items, const uint64_t *kmer_base, int k, const void *keys, const uint32_t *vals,
+                          uint64_t mask, uint32_t *out, cudaStream_t s);
 
 // link.cu — cross-bucket link stage (each launcher returns the kernels it launched)
 int launch_link_endpoints(const uint8_t *bases, const uint64_t *off, const uint32_t *len, const uint8_t *flags,

@@ -23,10 +23,13 @@ __device__ __forceinline__ uint32_t qslot_key(u128 key, uint64_t mask) {
     return (uint32_t)(mix64((uint64_t)key ^ ((uint64_t)(key >> 64) * 0x9E3779B97F4A7C15ull)) & mask);
 }
 
-// Insert every canonical k-mer of the graph text (pieces separated by non-ACGT bytes).
+// Insert every canonical k-mer of the graph text (pieces separated by non-ACGT bytes); the
+// value of the k-mer starting at text position p is pos_val[p] (the colour subset of a coloured
+// graph's k-mer), or 0 without pos_val.
 template <typename KT>
 __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__restrict__ text, uint64_t n, int k,
-                                                           uint64_t chunk, KT *keys, uint32_t *vals, uint64_t mask,
+                                                           uint64_t chunk, const uint32_t *__restrict__ pos_val,
+                                                           KT *keys, uint32_t *vals, uint64_t mask,
                                                            unsigned *status) {
     using K = KeyOps<KT>;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -56,7 +59,7 @@ __global__ void __launch_bounds__(256) index_insert_kernel(const uint8_t *__rest
             if (kk == K::empty()) {
                 const KT old = K::cas(&keys[s], K::empty(), key);
                 if (old == K::empty()) {
-                    vals[s] = 0u;
+                    vals[s] = pos_val ? pos_val[p + 1 - (uint64_t)k] : 0u;
                     break;
                 }
                 if (old == key) break;
@@ -231,17 +234,87 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
     }
 }
 
+// Colour subset of every k-mer of the final unitigs, the C: runs of a coloured graph's FASTA
+// (UnitigColorData::write_as_ident, crates/colors/src/managers/multiple.rs:705-740).  Item i
+// covers k-mers [item_first[i], item_first[i] + item_count[i]) of unitig item_unitig[i]
+// (bases[u_off[u], u_off[u] + u_len[u])); k-mer j of unitig u goes to out[kmer_base[u] + j].
+// The lookup is the coloured index (canonical k-mer -> subset id); a k-mer missing from it
+// gets 0xffffffff.
+template <typename KT>
+__global__ void __launch_bounds__(256) unitig_subsets_kernel(
+    const uint8_t *__restrict__ bases, const uint64_t *__restrict__ u_off, const uint32_t *__restrict__ u_len,
+    const uint32_t *__restrict__ item_unitig, const uint32_t *__restrict__ item_first,
+    const uint32_t *__restrict__ item_count, uint64_t n_items, const uint64_t *__restrict__ kmer_base, int k,
+    const KT *__restrict__ keys, const uint32_t *__restrict__ vals, uint64_t mask, uint32_t *__restrict__ out) {
+    using K = KeyOps<KT>;
+    const uint64_t it = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n_items) return;
+    const uint32_t u = item_unitig[it], j0 = item_first[it], cnt = item_count[it];
+    const uint8_t *seq = bases + u_off[u];
+    if ((uint64_t)j0 + cnt + (uint64_t)k - 1 > u_len[u]) return;
+    const KT kmask = K::mask(k);
+    KT fw = 0, rc = 0;
+    uint64_t run = 0;
+    for (uint32_t p = j0; p < j0 + cnt + (uint32_t)k - 1; p++) {
+        const uint32_t c = seq[p];
+        const uint32_t uc = c & 0xDFu;
+        if (!((uc == 'A') | (uc == 'C') | (uc == 'G') | (uc == 'T'))) {
+            run = 0;
+            if (p + 1 >= j0 + (uint32_t)k) out[kmer_base[u] + p + 1 - (uint32_t)k] = 0xffffffffu;
+            continue;
+        }
+        const uint32_t b = (c >> 1) & 3u;
+        fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
+        rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
+        if (++run < (uint64_t)k) {
+            if (p + 1 >= j0 + (uint32_t)k) out[kmer_base[u] + p + 1 - (uint32_t)k] = 0xffffffffu;
+            continue;
+        }
+        const KT key = fw < rc ? fw : rc;
+        uint64_t sl = qslot_key(key, mask);
+        uint32_t sub = 0xffffffffu;
+        for (uint64_t probe = 0; probe <= mask; probe++) {
+            const KT kk = keys[sl];
+            if (kk == key) {
+                sub = vals[sl];
+                break;
+            }
+            if (kk == K::empty()) break;
+            sl = (sl + 1) & mask;
+        }
+        out[kmer_base[u] + p + 1 - (uint32_t)k] = sub;
+    }
+}
+
+int launch_unitig_subsets(const uint8_t *bases, const uint64_t *u_off, const uint32_t *u_len,
+                          const uint32_t *item_unitig, const uint32_t *item_first, const uint32_t *item_count,
+                          uint64_t n_items, const uint64_t *kmer_base, int k, const void *keys, const uint32_t *vals,
+                          uint64_t mask, uint32_t *out, cudaStream_t s) {
+    if (n_items == 0) return 0;
+    const unsigned grid = (unsigned)((n_items + 255) / 256);
+    if (k > 32)
+        unitig_subsets_kernel<u128><<<grid, 256, 0, s>>>(bases, u_off, u_len, item_unitig, item_first, item_count,
+                                                         n_items, kmer_base, k, static_cast<const u128 *>(keys),
+                                                         vals, mask, out);
+    else
+        unitig_subsets_kernel<uint64_t><<<grid, 256, 0, s>>>(bases, u_off, u_len, item_unitig, item_first,
+                                                             item_count, n_items, kmer_base, k,
+                                                             static_cast<const uint64_t *>(keys), vals, mask, out);
+    return 1;
+}
+
 int launch_index_insert(const uint8_t *text, uint64_t n, int k, void *keys, uint32_t *vals, uint64_t mask,
-                        unsigned *status, cudaStream_t s) {
+                        unsigned *status, cudaStream_t s, const uint32_t *pos_val) {
     const uint64_t chunk = 256;
     const uint64_t threads = (n + chunk - 1) / chunk;
     if (threads == 0) return 0;
     const unsigned grid = (unsigned)((threads + 255) / 256);
     if (k > 32)
-        index_insert_kernel<u128><<<grid, 256, 0, s>>>(text, n, k, chunk, static_cast<u128 *>(keys), vals, mask, status);
+        index_insert_kernel<u128>
+            <<<grid, 256, 0, s>>>(text, n, k, chunk, pos_val, static_cast<u128 *>(keys), vals, mask, status);
     else
         index_insert_kernel<uint64_t>
-            <<<grid, 256, 0, s>>>(text, n, k, chunk, static_cast<uint64_t *>(keys), vals, mask, status);
+            <<<grid, 256, 0, s>>>(text, n, k, chunk, pos_val, static_cast<uint64_t *>(keys), vals, mask, status);
     return 1;
 }
 

@@ -223,12 +223,14 @@ int ggcat_gpu_write_graph(const char *unitigs_fasta, const char *output_file, in
                           int gfa_version, char *err, uint64_t err_cap);
 
 /* ggcat_dump_unitigs (crates/capi/src/lib.rs:407-452; GGCATInstance::dump_unitigs,
- * crates/api/src/lib.rs:434-477) for uncoloured graphs: calls fn once per piece of the graph
- * FASTA, read like the reference's reader with a k-1 copyback, with colors = NULL, n_colors = 0
- * and same_colors = 0, on the calling thread.  The reference's uncoloured branch hands the
- * function the record's identifier buffer, which its reader leaves empty there (it copies no
- * identifiers); this hands it the piece's bases.  colors = 1 (the colormap) returns
- * GGCAT_GPU_EUNSUPPORTED. */
+ * crates/api/src/lib.rs:434-477), on the calling thread.  Uncoloured (colors = 0): fn once per
+ * piece of the graph FASTA, read like the reference's reader with a k-1 copyback, with colors =
+ * NULL, n_colors = 0, same_colors = 0 (the reference's uncoloured branch hands the function the
+ * record's identifier buffer, which its reader leaves empty there; this hands it the piece's
+ * bases).  Coloured (colors = 1; dumper_colormap_reading.rs:62-146): every k-mer once, in
+ * pieces of one colour subset (runs of the " C:" annotations), grouped by subset in ascending
+ * order; colors = the subset's colours from the colormap beside the graph, same_colors = 1 for
+ * every piece of a group but the first.  As in the reference, pieces are not maximal unitigs. */
 typedef void (*ggcat_gpu_dump_fn)(void *fn_ctx, const uint8_t *seq, uint64_t len, const uint32_t *colors,
                                   uint64_t n_colors, int same_colors);
 int ggcat_gpu_dump_unitigs(const char *graph_input, int k, int colors, ggcat_gpu_dump_fn fn, void *fn_ctx);
@@ -264,15 +266,21 @@ int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_file
                                const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
                                size_t minimizer_length, size_t min_multiplicity);
 
-/* ggcat_build_from_files with its last two arguments (crates/capi/src/lib.rs:58-139):
- * extra_elab 0 none, 1 unitig links (L: annotations, or L / E lines in GFA); 2-4
- * (matchtigs, eulertigs, pathtigs) return GGCAT_GPU_EUNSUPPORTED; gfa_output_version 0 FASTA,
- * 1 GFA v1, 2 GFA v2.  The unitigs go through a temporary "<output_file>.unitigs.tmp.fa" that
- * ggcat_gpu_write_graph rewrites. */
+/* ggcat_build_from_files with all its arguments, in its order (crates/capi/src/lib.rs:58-139;
+ * GGCATInstance::build_graph, crates/api/src/lib.rs:217-322):
+ *   color_names / n_color_names: the names written to the colormap (colour i = input i);
+ *   colors: 1 = coloured graph: every k-mer's colour set (the inputs it occurs in) is deduped
+ *     into subsets, the FASTA headers carry " C:{subset:x}:{count}" runs of the k-mers' subsets
+ *     (UnitigColorData::write_as_ident, crates/colors/src/managers/multiple.rs:705-740) and the
+ *     subsets go to the colormap "<output_file without its extension>.colors.dat"
+ *     (ggcat_gpu_colormap_file); canonical builds only;
+ *   extra_elab: 0 none, 1 unitig links (" L:+:j:-" after the colour runs, or GFA L / E lines);
+ *     2-4 (matchtigs, eulertigs, pathtigs) return GGCAT_GPU_EUNSUPPORTED;
+ *   gfa_output_version: 0 FASTA, 1 GFA v1, 2 GFA v2 (not with colours, as in the reference). */
 int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
-                                  const char *output_file, size_t kmer_length, size_t threads_count, int forward_only,
-                                  size_t minimizer_length, size_t min_multiplicity, int extra_elab,
-                                  int gfa_output_version);
+                                  const char *output_file, const char *const *color_names, size_t n_color_names,
+                                  size_t kmer_length, size_t threads_count, int forward_only, size_t minimizer_length,
+                                  int colors, size_t min_multiplicity, int extra_elab, int gfa_output_version);
 
 /* ---- colour subsets ----
  * Replaces the per-k-mer colour sets and subset dedup of MultipleColorsManager
@@ -346,6 +354,24 @@ int ggcat_gpu_query_index_colored(ggcat_gpu_ctx *ctx, void *stream);
  * out_path.  Canonical k-mers, k <= 64. */
 int ggcat_gpu_query_from_files(ggcat_gpu_ctx *ctx, const char *graph_fasta, const char *query_fasta,
                                const char *output_prefix, int k, int forward_only, char *out_path, uint64_t out_cap);
+
+/* ggcat_query_graph with all its arguments, in its order (crates/capi/src/lib.rs:324-380;
+ * GGCATInstance::query_graph, crates/api/src/lib.rs:325-382).  The graph's canonical k-mers are
+ * indexed on the device and every k-mer of every query record (FASTA / FASTQ, plain or
+ * compressed) is looked up.  colors = 0: the querier's CSV
+ * (query_index,matched_kmers,query_kmers,match_percentage; counters_sorting.rs:235-268) at
+ * output_file_prefix (".csv" appended when it has no extension).  colors = 1: the graph's
+ * " C:" runs give every k-mer's subset and the colormap beside the graph the subsets' colours;
+ * the JSON lines of colored_query_output.rs:264-309 at output_file_prefix (".jsonl" appended
+ * when it has no extension): {"query_index":i, "matches":{"c": f, ...}} for every query with a
+ * match, f = the query's k-mers found in colour c over its k-mers, to 2 places; c is the colour
+ * index (color_output_format 0) or its name (1).  threads_count and minimizer_length are
+ * accepted and unused (no host threads, no minimizer bucketing).  The written path is copied to
+ * out_path.  k <= 64, canonical only. */
+int ggcat_gpu_query_graph(ggcat_gpu_ctx *ctx, const char *input_graph, const char *input_query,
+                          const char *output_file_prefix, size_t kmer_length, size_t threads_count, int forward_only,
+                          size_t minimizer_length, int colors, size_t color_output_format, char *out_path,
+                          uint64_t out_cap);
 
 /* Submits a batch of queries (host text layout; query i = h_text[h_off[i], h_off[i]+h_len[i]))
  * to slot `slot` and returns without waiting.  The slot's H2D copy, lookup kernel and D2H

@@ -148,5 +148,46 @@ def test_dump_unitigs(tmp_path):
     assert _native.dump_unitigs(str(src), 31) == unitigs
     L = _native.load()
     fn = _native.DUMP_FN(lambda *a: None)
-    assert L.ggcat_gpu_dump_unitigs(str(src).encode(), 31, 1, fn, None) == -5  # colours: EUNSUPPORTED
+    assert L.ggcat_gpu_dump_unitigs(str(src).encode(), 31, 1, fn, None) == -6  # colours, no colormap: EIO
+
+
+def test_dump_unitigs_colored(tmp_path):
+    """The coloured branch of ggcat_dump_unitigs on a hand-made coloured graph (C: runs in the
+    headers, a colormap beside it): every k-mer once, in single-subset pieces grouped by subset
+    in ascending order, with the subset's colours and same_colors on all but the first piece of
+    a group."""
+    rng = np.random.default_rng(8)
+    k = 11
+    subsets = [[0], [1, 3], [0, 1, 2, 3], [2]]
+    recs, truth = [], []
+    for u in range(20):
+        seq = synth.random_genome(int(rng.integers(k, 120)), rng).tobytes()
+        nk = len(seq) - k + 1
+        runs, left, pos = [], nk, 0
+        while left:
+            c = int(rng.integers(1, left + 1))
+            sub = int(rng.integers(0, len(subsets)))
+            if runs and runs[-1][0] == sub:
+                runs[-1][1] += c
+            else:
+                runs.append([sub, c])
+            for j in range(c):
+                truth.append((seq[pos + j:pos + j + k], sub))
+            pos += c
+            left -= c
+        hdr = f">{u} LN:i:{len(seq)}" + "".join(f" C:{a:x}:{b}" for a, b in runs)
+        recs.append(hdr.encode() + b"\n" + seq + b"\n")
+    g = tmp_path / "cg.fa"
+    g.write_bytes(b"".join(recs))
+    _native.write_colormap(str(tmp_path / "cg.colors.dat"), ["a", "b", "c", "d"], subsets)
+    out = _native.dump_unitigs(str(g), k, colors=True)
+    got, last = [], None
+    for bases, cols, same in out:
+        sub = subsets.index(cols)
+        assert same == (last == sub)
+        assert last is None or sub >= last
+        last = sub
+        for j in range(len(bases) - k + 1):
+            got.append((bases[j:j + k], sub))
+    assert sorted(got) == sorted(truth)
 
