@@ -310,12 +310,13 @@ def query_bench(args, ctx, torch, dev):
     qt, qo, ql, arr = synth.query_workload(genomes, args.queries, rate_per_s=args.query_rate)
     # warm-up
     serve.serve(ctx, 31, qt, qo[:200], ql[:200], np.zeros(200), slots=4)
-    free, _ = torch.cuda.mem_get_info(dev)
-    budget = int(max(1 << 22, min(free // 16, 256 << 20)))
-    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget)
+    budget = 256 << 20
+    free_fn = lambda: torch.cuda.mem_get_info(dev)[0]  # noqa: E731  (asked at every admission)
+    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget, free_bytes=free_fn)
     n1 = min(len(qo), max(1000, args.queries // 10))
     r1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, one_per_launch=True)
-    same = bool((rb.matched[:n1] == r1.matched).all())
+    rb1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, max_batch_kmers=budget, free_bytes=free_fn)
+    same = bool((rb.matched[:n1] == r1.matched).all() and (rb1.matched == r1.matched).all())
     return {
         "metric": "query kmers/s + p50/p99 ms",
         "graph": f"{args.query_genomes} genomes x 4 Mbp (ancestor + 0.1-2% substitutions, 0.05% indels), "
@@ -329,6 +330,11 @@ def query_bench(args, ctx, torch, dev):
         "one_per_launch": {"queries": int(n1), "kmers_per_s": round(r1.kmers_per_s, 1),
                            "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3),
                            "wall_s": round(r1.wall_s, 3)},
+        "like_for_like": {"queries": int(n1), "batched": {"kmers_per_s": round(rb1.kmers_per_s, 1),
+                                                          "p50_ms": round(rb1.pct_ms(50), 3),
+                                                          "p99_ms": round(rb1.pct_ms(99), 3)},
+                          "one_per_launch": {"kmers_per_s": round(r1.kmers_per_s, 1),
+                                             "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3)}},
         "results_identical_alone_vs_batched": same,
         "index_build_s": round(index_s, 3),
     }
@@ -363,18 +369,21 @@ def colored_bench(args, ctx, torch, dev):
     genomes = [w.text[int(o):int(o) + int(ln)] for o, ln in zip(w.seq_off.tolist(), w.seq_len.tolist())]
     qt, qo, ql, arr = synth.query_workload(genomes, args.colored_queries, rate_per_s=args.query_rate)
     serve.serve(ctx, 31, qt, qo[:200], ql[:200], np.zeros(200), slots=4, colored=True)
-    free, _ = torch.cuda.mem_get_info(dev)
-    budget = int(max(1 << 22, min(free // 16, 256 << 20)))
-    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget, colored=True)
-    n1 = min(len(qo), 2000)
+    budget = 256 << 20
+    free_fn = lambda: torch.cuda.mem_get_info(dev)[0]  # noqa: E731  (asked at every admission)
+    rb = serve.serve(ctx, 31, qt, qo, ql, arr, slots=4, max_batch_kmers=budget, colored=True, free_bytes=free_fn)
+    n1 = min(len(qo), 10000)
     r1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, one_per_launch=True, colored=True)
-    same = bool((rb.matched[:n1] == r1.matched).all() and (rb.color_totals[:n1] == r1.color_totals).all())
+    rb1 = serve.serve(ctx, 31, qt, qo[:n1], ql[:n1], arr[:n1], slots=4, max_batch_kmers=budget, colored=True,
+                      free_bytes=free_fn)
+    same = bool((rb.matched[:n1] == r1.matched).all() and (rb.color_totals[:n1] == r1.color_totals).all()
+                and (rb1.matched == r1.matched).all())
     # arrival-rate sweep (the knee): the same queries with the Poisson gaps scaled; "inf" = all
     # queries waiting at t = 0
     sweep = []
     for rate in (80_000.0, 320_000.0, float("inf")):
         a2 = np.zeros_like(arr) if rate == float("inf") else arr * (args.query_rate / rate)
-        r2 = serve.serve(ctx, 31, qt, qo, ql, a2, slots=4, max_batch_kmers=budget, colored=True)
+        r2 = serve.serve(ctx, 31, qt, qo, ql, a2, slots=4, max_batch_kmers=budget, colored=True, free_bytes=free_fn)
         sweep.append({"arrival_rate_per_s": rate if rate != float("inf") else "all at t=0",
                       "kmers_per_s": round(r2.kmers_per_s, 1), "p50_ms": round(r2.pct_ms(50), 3),
                       "p99_ms": round(r2.pct_ms(99), 3), "batches": r2.batches})
@@ -389,6 +398,12 @@ def colored_bench(args, ctx, torch, dev):
                   "color_hits_total": int(rb.color_totals.sum()),
                   "one_per_launch": {"queries": int(n1), "kmers_per_s": round(r1.kmers_per_s, 1),
                                      "p50_ms": round(r1.pct_ms(50), 3), "p99_ms": round(r1.pct_ms(99), 3)},
+                  "like_for_like": {"queries": int(n1),
+                                    "batched": {"kmers_per_s": round(rb1.kmers_per_s, 1),
+                                                "p50_ms": round(rb1.pct_ms(50), 3), "p99_ms": round(rb1.pct_ms(99), 3)},
+                                    "one_per_launch": {"kmers_per_s": round(r1.kmers_per_s, 1),
+                                                       "p50_ms": round(r1.pct_ms(50), 3),
+                                                       "p99_ms": round(r1.pct_ms(99), 3)}},
                   "results_identical_alone_vs_batched": same, "rate_sweep": sweep},
     }
 

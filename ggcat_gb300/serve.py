@@ -47,10 +47,14 @@ def _pack(queries: list) -> tuple:
 
 
 def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arrivals: np.ndarray, slots: int = 4,
-          max_batch_kmers: int = 64 << 20, one_per_launch: bool = False, colored: bool = False) -> ServeResult:
+          max_batch_kmers: int = 64 << 20, one_per_launch: bool = False, colored: bool = False,
+          free_bytes=None, bytes_per_kmer: float = 2.0) -> ServeResult:
     """Replays the queries (text layout: query i = text[off[i] : off[i] + lens[i]], arrivals
     non-decreasing, in seconds from the start) through the server.  With a coloured index,
-    ``colored=True`` also reads every batch's per-colour counts back."""
+    ``colored=True`` also reads every batch's per-colour counts back.  ``free_bytes`` (a
+    callable returning the device's free memory) is asked at every admission: a batch admits
+    at most half of the free memory's worth of k-mer positions (``bytes_per_kmer`` device bytes
+    each) and never more than ``max_batch_kmers``; at least one request is always admitted."""
     n = len(off)
     off = np.asarray(off, np.uint64)
     lens = np.asarray(lens, np.uint64)
@@ -81,8 +85,12 @@ def serve(ctx, k: int, text: np.ndarray, off: np.ndarray, lens: np.ndarray, arri
             if one_per_launch:
                 b = head + 1
             else:
-                # admit every arrived request that fits the k-mer budget (at least one)
-                lim = cum[head] + max_batch_kmers
+                # admit every arrived request that fits the k-mer budget (at least one); the
+                # budget shrinks with the device's free memory
+                budget = max_batch_kmers
+                if free_bytes is not None:
+                    budget = max(1, min(budget, int(free_bytes() / (2.0 * bytes_per_kmer))))
+                lim = cum[head] + budget
                 b = max(head + 1, min(arrived, int(np.searchsorted(cum, lim, side="right")) - 1))
             lo = int(off[head])
             hi = int(off[b - 1] + lens[b - 1])

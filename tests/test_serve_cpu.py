@@ -94,3 +94,25 @@ def test_colored_totals(graph):
     res = serve.serve(dev, K, qt, qo, ql, arrivals, slots=2, max_batch_kmers=4000, colored=True)
     assert (res.matched == alone).all()
     assert (res.color_totals == pc.sum(axis=1)).all()
+
+
+def test_admission_follows_free_memory(graph):
+    """The batch budget is recomputed from the device's free memory at every admission: with
+    free memory shrinking over time, every multi-request batch fits the budget its admission
+    saw, and results still equal each request's result alone."""
+    lo, hi, coff, ccol, qt, qo, ql, arrivals, alone, pc = graph
+    dev = FakeDevice(lo, hi, np.random.default_rng(13))
+    seen = []
+
+    def free_bytes():
+        # 40 KB free at first, 400 bytes less at every admission (never below 2 KB)
+        f = max(2048, 40_000 - 400 * len(seen))
+        seen.append(f)
+        return f
+
+    res = serve.serve(dev, K, qt, qo, ql, np.zeros_like(arrivals), slots=2, max_batch_kmers=1 << 20,
+                      free_bytes=free_bytes, bytes_per_kmer=2.0)
+    assert (res.matched == alone).all()
+    assert len(seen) == res.batches
+    for (_, n, nk), f in zip(dev.submitted, seen):
+        assert n == 1 or nk <= f / 4.0
