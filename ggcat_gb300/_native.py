@@ -40,6 +40,7 @@ class Params(C.Structure):
         ("table_load_pct", C.c_int32),
         ("small_limit", C.c_int32),
         ("copy_pieces", C.c_int32),
+        ("spill_mb", C.c_int32),
     ]
 
 
@@ -64,6 +65,9 @@ class Stats(C.Structure):
         ("merge_units_walk", C.c_uint64),
         ("merge_graph_captures", C.c_uint64),
         ("merge_graph_replays", C.c_uint64),
+        ("spill_pieces", C.c_uint64),
+        ("spill_ranges", C.c_uint64),
+        ("spill_bytes", C.c_uint64),
     ]
 
 
@@ -225,11 +229,11 @@ def _ptr(a):
 
 def make_params(k=31, m=None, bucket_bits=10, second_bits=3, min_multiplicity=1, hash_kind=GGCAT_HASH_SEQHASH,
                 forward_only=False, merge_mode=GGCAT_MERGE_BATCHED, unit_target=0, keep_kmers=False,
-                subbin_bytes=0, table_load_pct=0, small_limit=0, copy_pieces=0) -> Params:
+                subbin_bytes=0, table_load_pct=0, small_limit=0, copy_pieces=0, spill_mb=0) -> Params:
     if m is None:
         m = compute_best_m(k)
     return Params(k, m, bucket_bits, second_bits, min_multiplicity, hash_kind, int(forward_only), merge_mode,
-                  unit_target, int(keep_kmers), subbin_bytes, table_load_pct, small_limit, copy_pieces)
+                  unit_target, int(keep_kmers), subbin_bytes, table_load_pct, small_limit, copy_pieces, spill_mb)
 
 
 def compute_best_m(k: int) -> int:

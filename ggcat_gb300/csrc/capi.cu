@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -199,6 +200,15 @@ struct ggcat_gpu_ctx {
     bool partial_on_host = false;
     HostUnitigs final_u;
 
+    // host bucket store of a spilled bucketize: per piece of the text, its records partitioned
+    // by (bucket, sub-bin) with the piece's sub-bin offsets (empty: the store is in HBM)
+    struct SpillPiece {
+        PinnedArray<SkRec> recs;
+        std::vector<unsigned long long> bin_off, kmer_off;
+    };
+    std::vector<std::unique_ptr<SpillPiece>> spill;
+    uint64_t spill_budget = 0;  // device bytes of the bucket store the spill was sized for
+
     cudaEvent_t ev[8] = {};
     ggcat_gpu_stats stats{};
 
@@ -337,6 +347,123 @@ struct TextFeed {
     const cudaEvent_t *ev;
 };
 
+// Bucketize with the bucket store in pinned host memory: the text (packed whole, it stays on the
+// device for the merge) is bucketized in pieces of bucketize blocks, each sized so that its
+// staging and partitioned records fit `budget` bytes; every piece's records, partitioned by
+// (bucket, sub-bin) with its own sub-bin offsets, are copied to host memory.  The merge then
+// works bucket range by bucket range (merge_spill).  The records equal those of the resident
+// path (each block's superkmers do not depend on the launch it runs in).
+static int bucketize_spill(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len, const ggcat_gpu_params *p,
+                           cudaStream_t s, const TextFeed *feed, uint64_t budget, uint64_t *n_superkmers) {
+    const uint64_t n_words = (text_len + 31) / 32 + 1;
+    CK(ctx->packed.ensure(n_words));
+    CK(ctx->valid.ensure(n_words));
+    const uint64_t nb = ctx->n_bins;
+    CK(ctx->bin_count.ensure(nb + 1));
+    CK(ctx->bin_off.ensure(nb + 1));
+    CK(ctx->kmer_off.ensure(nb + 1));
+    CK(ctx->bin_cursor.ensure(nb + 1));
+    CK(ctx->scan_tmp.ensure(scan_temp_elems(nb) + 2));
+    CK(ctx->rec_total.ensure(1));
+    CK(ctx->ovf_cursor.ensure(1));
+    const int canonical = p->forward_only ? 0 : 1;
+    const BucketizeGeometry geo = bucketize_geometry(text_len, p->k, p->m);
+    const uint64_t block_bases = bucketize_block_bases(geo);
+    CK(cudaEventRecord(ctx->ev[0], s));
+    if (feed)
+        for (int i = 0; i < feed->pieces; i++) CK(cudaStreamWaitEvent(s, feed->ev[i], 0));
+    ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], s));
+    // a block's staging region and, at most, as many partitioned records
+    const uint64_t per_block = (uint64_t)geo.region_cap * sizeof(SkRec) * 2 + block_bases / 32;
+    const uint64_t piece_blocks = std::max<uint64_t>(1, budget / per_block);
+    ctx->spill.clear();
+    ctx->spill_budget = budget;
+    uint64_t tot_recs = 0, tot_kmers = 0;
+    for (uint64_t B0 = 0; B0 < geo.blocks; B0 += piece_blocks) {
+        const uint64_t B1 = std::min<uint64_t>(geo.blocks, B0 + piece_blocks), nbp = B1 - B0;
+        uint64_t ovf_cap = nbp * block_bases / 64 + 4096;
+        int split_counts = 0;
+        unsigned long long totals[4] = {0, 0, 0, 0};
+        CK(ctx->block_count.ensure(nbp + 1));
+        for (int attempt = 0; attempt < 3; attempt++) {
+            CK(ctx->stage.ensure(nbp * geo.region_cap + ovf_cap));
+            if (split_counts) CK(ctx->bin_kmers.ensure(nb + 1));
+            CK(cudaMemsetAsync(ctx->bin_count.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+            if (split_counts) CK(cudaMemsetAsync(ctx->bin_kmers.p, 0, (nb + 1) * sizeof(unsigned long long), s));
+            CK(cudaMemsetAsync(ctx->rec_total.p, 0, sizeof(unsigned long long), s));
+            CK(cudaMemsetAsync(ctx->bin_cursor.p, 0, (nb + 1) * sizeof(unsigned), s));
+            CK(cudaMemsetAsync(ctx->ovf_cursor.p, 0, sizeof(unsigned long long), s));
+            CK(cudaMemsetAsync(ctx->status.p, 0, 2 * sizeof(unsigned), s));
+            ctx->launches += launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits,
+                                              p->second_bits, ctx->fine_bits, canonical, geo, ctx->bin_count.p,
+                                              ctx->bin_kmers.p, split_counts, ctx->rec_total.p, ctx->stage.p,
+                                              ctx->block_count.p, ovf_cap, ctx->ovf_cursor.p, ctx->status.p,
+                                              (uint32_t)B0, (uint32_t)nbp, s, (uint32_t)B0, (uint32_t)nbp);
+            CK(cudaGetLastError());
+            ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s,
+                                                   split_counts ? 0 : 1);
+            ctx->launches += launch_exclusive_scan(split_counts ? ctx->bin_kmers.p : ctx->bin_count.p, nb,
+                                                   ctx->kmer_off.p, ctx->scan_tmp.p, s, split_counts ? 0 : 2);
+            CK(cudaMemcpyAsync(&totals[0], ctx->bin_off.p + nb, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(&totals[1], ctx->kmer_off.p + nb, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(&totals[2], ctx->ovf_cursor.p, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(&totals[3], ctx->rec_total.p, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            bool again = false;
+            if (!split_counts && totals[0] != totals[3]) {
+                split_counts = 1;
+                again = true;
+            }
+            if (totals[2] > ovf_cap) {
+                ovf_cap = totals[2] + 1024;
+                again = true;
+            }
+            if (!again) break;
+        }
+        if (totals[0] != totals[3] || totals[2] > ovf_cap)
+            return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize (spill): staging or count overflow");
+        const uint64_t nr = totals[0];
+        CK(ctx->recs.ensure(nr + 1));
+        ctx->launches += launch_partition(ctx->stage.p, geo, ctx->block_count.p, ctx->ovf_cursor.p, ovf_cap,
+                                          ctx->fine_bits, ctx->bin_off.p, ctx->bin_cursor.p, ctx->recs.p,
+                                          ctx->status.p, s, (uint32_t)nbp);
+        CK(cudaGetLastError());
+        auto piece = std::make_unique<ggcat_gpu_ctx::SpillPiece>();
+        CK(piece->recs.resize(nr));
+        piece->bin_off.resize(nb + 1);
+        piece->kmer_off.resize(nb + 1);
+        if (nr) CK(cudaMemcpyAsync(piece->recs.data(), ctx->recs.p, nr * sizeof(SkRec), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(piece->bin_off.data(), ctx->bin_off.p, (nb + 1) * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(piece->kmer_off.data(), ctx->kmer_off.p, (nb + 1) * 8, cudaMemcpyDeviceToHost, s));
+        unsigned st = 0;
+        CK(cudaMemcpyAsync(&st, ctx->status.p, sizeof st, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (st & (kStatusLookback | kStatusStageOverflow))
+            return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize (spill): internal error (status %u)", st);
+        tot_recs += nr;
+        tot_kmers += totals[1];
+        ctx->spill.push_back(std::move(piece));
+    }
+    CK(cudaEventRecord(ctx->ev[2], s));
+    ctx->n_text = text_len;
+    ctx->last_text = d_text;
+    ctx->have_colors = false;
+    ctx->last_params = *p;
+    ctx->n_recs = tot_recs;
+    ctx->n_kmers = tot_kmers;
+    ctx->have_buckets = true;
+    ctx->stats = ggcat_gpu_stats{};
+    ctx->stats.text_bytes = text_len;
+    ctx->stats.superkmers = tot_recs;
+    ctx->stats.kmer_instances = tot_kmers;
+    ctx->stats.spill_pieces = ctx->spill.size();
+    ctx->stats.spill_bytes = tot_recs * sizeof(SkRec);
+    if (n_superkmers) *n_superkmers = tot_recs;
+    return GGCAT_GPU_OK;
+}
+
 static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t text_len, const ggcat_gpu_params *p,
                           void *stream, uint64_t *n_superkmers, const TextFeed *feed) {
     if (!ctx) return GGCAT_GPU_EINVAL;
@@ -359,6 +486,20 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * subbin < text_len) fb++;
     ctx->fine_bits = fb < 4 ? 4 : fb;
     ctx->n_bins = (uint64_t)ctx->n_buckets << ctx->fine_bits;
+    ctx->spill.clear();
+    {
+        // the bucket store goes to host memory when its records (with their staging) would pass
+        // the spill_mb budget or half of the device's free memory
+        const uint64_t est = text_len / (uint64_t)(p->k - p->m + 1) * 3 + 4096;  // 1.5x density 2/(w+1)
+        const uint64_t need = est * sizeof(SkRec) * 2;
+        uint64_t budget = p->spill_mb > 0 ? ((uint64_t)p->spill_mb << 20) : 0;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            const uint64_t have = (uint64_t)free_b / 2 + ctx->stage.n * sizeof(SkRec) + ctx->recs.n * sizeof(SkRec);
+            if (need > have && (budget == 0 || budget > have)) budget = std::max<uint64_t>(have, 64ull << 20);
+        }
+        if (budget && need > budget) return bucketize_spill(ctx, d_text, text_len, p, s, feed, budget, n_superkmers);
+    }
     const uint64_t nb = ctx->n_bins;
     CK(ctx->bin_count.ensure(nb + 1));
     CK(ctx->bin_off.ensure(nb + 1));
@@ -486,7 +627,15 @@ extern "C" int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer
     if (!h_out) return GGCAT_GPU_OK;
     uint64_t cnt = std::min<uint64_t>(cap, ctx->n_recs);
     std::vector<SkRec> tmp(cnt);
-    if (cnt) CK(cudaMemcpy(tmp.data(), ctx->recs.p, cnt * sizeof(SkRec), cudaMemcpyDeviceToHost));
+    if (!ctx->spill.empty()) {
+        // spilled store: the pieces' records sub-bin by sub-bin
+        uint64_t pos = 0;
+        for (uint64_t bin = 0; bin < ctx->n_bins && pos < cnt; bin++)
+            for (const auto &pc : ctx->spill)
+                for (uint64_t i = pc->bin_off[bin]; i < pc->bin_off[bin + 1] && pos < cnt; i++) tmp[pos++] = pc->recs[i];
+    } else if (cnt) {
+        CK(cudaMemcpy(tmp.data(), ctx->recs.p, cnt * sizeof(SkRec), cudaMemcpyDeviceToHost));
+    }
     for (uint64_t i = 0; i < cnt; i++) {
         const SkRec &r = tmp[i];
         ggcat_gpu_superkmer o;
@@ -687,6 +836,163 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     return GGCAT_GPU_OK;
 }
 
+// merge_once with the output capacities grown until nothing overflows
+static int merge_retry(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_t s) {
+    uint64_t bases_cap = ctx->n_kmers / 2 + (uint64_t)p->k * (ctx->n_recs / 2) + 4096;
+    uint64_t u_cap = ctx->n_recs + 1024;
+    uint64_t kmer_cap = ctx->n_kmers + 1024;
+    unsigned st = 0;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        const int rc = merge_once(ctx, p, s, bases_cap, u_cap, kmer_cap, &st);
+        if (rc) return rc;
+        if (!(st & (kStatusOutOverflow | kStatusKmerOverflow))) break;
+        bases_cap = std::max<uint64_t>(bases_cap, ctx->n_partial_bases + 4096);
+        u_cap = std::max<uint64_t>(u_cap, ctx->n_partial + 1024);
+        kmer_cap = std::max<uint64_t>(kmer_cap, ctx->n_kmers_out + 1024);
+    }
+    if (st & (kStatusOutOverflow | kStatusKmerOverflow)) return fail(ctx, GGCAT_GPU_EDEVICE, "merge output overflow");
+    if (st & kStatusTableFull) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: hash table full");
+    if (st & kStatusWalkLimit) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: unitig walk bound exceeded");
+    if (st & kStatusLookback) return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: internal lookback/partition error");
+    return GGCAT_GPU_OK;
+}
+
+// The merge of a spilled bucket store: consecutive bucket ranges whose records (over all
+// pieces) fit the spill budget, one after another.  A range's records are gathered on the host
+// in (sub-bin, piece) order, so that every sub-bin is contiguous, copied to the device in one
+// copy with offsets that leave the other buckets empty, and merged by the usual merge phase;
+// its partial unitigs (and dumped k-mers) are appended on the host and finally put back on the
+// device for the link and colour stages.  Every merge unit lies inside one bucket, so the
+// result is the resident path's.
+static int merge_spill(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_t s) {
+    const uint64_t nb = ctx->n_bins, nbk = ctx->n_buckets;
+    const int fb = ctx->fine_bits;
+    const uint64_t kw = p->k > 32 ? 2 : 1;
+    const uint64_t tot_recs = ctx->n_recs, tot_kmers = ctx->n_kmers;
+    std::vector<uint64_t> brec(nbk, 0);
+    for (const auto &pc : ctx->spill)
+        for (uint64_t b = 0; b < nbk; b++) brec[b] += pc->bin_off[(b + 1) << fb] - pc->bin_off[b << fb];
+    const uint64_t budget_recs = std::max<uint64_t>(1, ctx->spill_budget / (2 * sizeof(SkRec)));
+    std::vector<uint8_t> a_bases, a_flags;
+    std::vector<uint64_t> a_off, kkeys;
+    std::vector<uint32_t> a_len, kmult;
+    PinnedArray<SkRec> gather;
+    std::vector<unsigned long long> roff(nb + 1), rkoff(nb + 1);
+    double ms_merge = 0;
+    uint64_t ranges = 0, distinct = 0, small_u = 0, large_u = 0, spilled_u = 0, extg = 0, walk = 0;
+    auto restore = [&]() {
+        ctx->n_recs = tot_recs;
+        ctx->n_kmers = tot_kmers;
+    };
+    for (uint64_t b0 = 0; b0 < nbk;) {
+        uint64_t b1 = b0 + 1, nr = brec[b0];
+        while (b1 < nbk && nr + brec[b1] <= budget_recs) nr += brec[b1++];
+        // gather the range's records and its offsets (empty sub-bins outside the range)
+        CK(gather.resize(nr));
+        uint64_t pos = 0, kpos = 0;
+        const uint64_t bin0 = b0 << fb, bin1 = b1 << fb;
+        for (uint64_t bin = 0; bin <= nb; bin++) {
+            roff[bin] = pos;
+            rkoff[bin] = kpos;
+            if (bin < bin0 || bin >= bin1) continue;
+            for (const auto &pc : ctx->spill) {
+                const uint64_t a = pc->bin_off[bin], e = pc->bin_off[bin + 1];
+                if (e > a) memcpy(gather.data() + pos, pc->recs.data() + a, (e - a) * sizeof(SkRec));
+                pos += e - a;
+                kpos += pc->kmer_off[bin + 1] - pc->kmer_off[bin];
+            }
+        }
+        CK(ctx->recs.ensure(nr + 1));
+        if (nr) CK(cudaMemcpyAsync(ctx->recs.p, gather.data(), nr * sizeof(SkRec), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->bin_off.p, roff.data(), (nb + 1) * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->kmer_off.p, rkoff.data(), (nb + 1) * 8, cudaMemcpyHostToDevice, s));
+        ctx->n_recs = nr;
+        ctx->n_kmers = kpos;
+        const int rc = merge_retry(ctx, p, s);
+        if (rc) {
+            restore();
+            return rc;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+        ms_merge += ms;
+        distinct += ctx->stats.distinct_kmers;
+        small_u += ctx->stats.merge_units_small;
+        large_u += ctx->stats.merge_units_large;
+        spilled_u += ctx->stats.merge_units_spilled;
+        extg += ctx->stats.merge_units_ext_global;
+        walk += ctx->stats.merge_units_walk;
+        // append the range's partial unitigs and k-mers
+        const uint64_t nu = ctx->n_partial, nbs = ctx->n_partial_bases, base0 = a_bases.size(), u0 = a_off.size();
+        a_bases.resize(base0 + nbs);
+        a_off.resize(u0 + nu);
+        a_len.resize(u0 + nu);
+        a_flags.resize(u0 + nu);
+        if (nbs) CK(cudaMemcpy(a_bases.data() + base0, ctx->out_bases.p, nbs, cudaMemcpyDeviceToHost));
+        if (nu) {
+            CK(cudaMemcpy(a_off.data() + u0, ctx->out_off.p, nu * 8, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(a_len.data() + u0, ctx->out_len.p, nu * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(a_flags.data() + u0, ctx->out_flags.p, nu, cudaMemcpyDeviceToHost));
+            for (uint64_t i = u0; i < u0 + nu; i++) a_off[i] += base0;
+        }
+        if (p->keep_kmers && ctx->n_kmers_out) {
+            const uint64_t nk = ctx->n_kmers_out, k0 = kmult.size();
+            kkeys.resize((k0 + nk) * kw);
+            kmult.resize(k0 + nk);
+            CK(cudaMemcpy(kkeys.data() + k0 * kw, ctx->kmer_keys.p, nk * kw * 8, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(kmult.data() + k0, ctx->kmer_mult.p, nk * 4, cudaMemcpyDeviceToHost));
+        }
+        ranges++;
+        b0 = b1;
+    }
+    restore();
+    // the appended partial unitigs (and k-mers) back on the device for the link and colour
+    // stages, and in the pinned host arrays the partial-unitig copy reads
+    const uint64_t nu = a_off.size(), nbs = a_bases.size();
+    CK(ctx->out_bases.ensure(nbs + 1));
+    CK(ctx->out_off.ensure(nu + 1));
+    CK(ctx->out_len.ensure(nu + 1));
+    CK(ctx->out_flags.ensure(nu + 1));
+    if (nbs) CK(cudaMemcpy(ctx->out_bases.p, a_bases.data(), nbs, cudaMemcpyHostToDevice));
+    if (nu) {
+        CK(cudaMemcpy(ctx->out_off.p, a_off.data(), nu * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->out_len.p, a_len.data(), nu * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->out_flags.p, a_flags.data(), nu, cudaMemcpyHostToDevice));
+    }
+    HostUnitigs &h = ctx->partial;
+    CK(h.bases.resize(nbs));
+    CK(h.off.resize(nu));
+    CK(h.len.resize(nu));
+    CK(h.flags.resize(nu));
+    if (nbs) memcpy(h.bases.data(), a_bases.data(), nbs);
+    if (nu) {
+        memcpy(h.off.data(), a_off.data(), nu * 8);
+        memcpy(h.len.data(), a_len.data(), nu * 4);
+        memcpy(h.flags.data(), a_flags.data(), nu);
+    }
+    ctx->n_partial = nu;
+    ctx->n_partial_bases = nbs;
+    ctx->n_kmers_out = kmult.size();
+    if (p->keep_kmers) {
+        CK(ctx->kmer_keys.ensure(kmult.size() * kw + 1));
+        CK(ctx->kmer_mult.ensure(kmult.size() + 1));
+        if (!kmult.empty()) {
+            CK(cudaMemcpy(ctx->kmer_keys.p, kkeys.data(), kkeys.size() * 8, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ctx->kmer_mult.p, kmult.data(), kmult.size() * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    ctx->partial_on_host = true;
+    ctx->stats.ms_merge = ms_merge;
+    ctx->stats.distinct_kmers = distinct;
+    ctx->stats.merge_units_small = small_u;
+    ctx->stats.merge_units_large = large_u;
+    ctx->stats.merge_units_spilled = spilled_u;
+    ctx->stats.merge_units_ext_global = extg;
+    ctx->stats.merge_units_walk = walk;
+    ctx->stats.spill_ranges = ranges;
+    return GGCAT_GPU_OK;
+}
+
 extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, void *stream) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     int rc = check_params(ctx, p);
@@ -707,29 +1013,17 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     CK(cudaSetDevice(ctx->device));
     ctx->have_merge = false;
     ctx->partial_on_host = false;
-    uint64_t bases_cap = ctx->n_kmers / 2 + (uint64_t)p->k * (ctx->n_recs / 2) + 4096;
-    uint64_t u_cap = ctx->n_recs + 1024;
-    uint64_t kmer_cap = ctx->n_kmers + 1024;
-    unsigned st = 0;
-    for (int attempt = 0; attempt < 3; attempt++) {
-        rc = merge_once(ctx, p, s, bases_cap, u_cap, kmer_cap, &st);
-        if (rc) return rc;
-        if (!(st & (kStatusOutOverflow | kStatusKmerOverflow))) break;
-        bases_cap = std::max<uint64_t>(bases_cap, ctx->n_partial_bases + 4096);
-        u_cap = std::max<uint64_t>(u_cap, ctx->n_partial + 1024);
-        kmer_cap = std::max<uint64_t>(kmer_cap, ctx->n_kmers_out + 1024);
-    }
-    if (st & (kStatusOutOverflow | kStatusKmerOverflow)) return fail(ctx, GGCAT_GPU_EDEVICE, "merge output overflow");
-    if (st & kStatusTableFull) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: hash table full");
-    if (st & kStatusWalkLimit) return fail(ctx, GGCAT_GPU_EDEVICE, "merge: unitig walk bound exceeded");
-    if (st & kStatusLookback) return fail(ctx, GGCAT_GPU_EDEVICE, "bucketize: internal lookback/partition error");
+    rc = ctx->spill.empty() ? merge_retry(ctx, p, s) : merge_spill(ctx, p, s);
+    if (rc) return rc;
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     ctx->stats.ms_pack = ms;
     cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
     ctx->stats.ms_bucketize = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
-    ctx->stats.ms_merge = ms;
+    if (ctx->spill.empty()) {
+        cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+        ctx->stats.ms_merge = ms;
+    }
     ctx->stats.partial_unitigs = ctx->n_partial;
     ctx->stats.partial_bases = ctx->n_partial_bases;
     ctx->stats.surviving_kmers = ctx->n_kmers_out;

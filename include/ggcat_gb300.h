@@ -62,6 +62,12 @@ typedef struct {
                                  each packed and bucketized while the next ones are in flight (0 = auto:
                                  up to 4, each at least two waves of bucketize blocks; 1 = one copy;
                                  at most 4) */
+    int32_t spill_mb;         /* device memory for the bucket store, MiB (0 = no limit).  When the superkmer
+                                 records would exceed it, or do not fit the device's free memory, the text is
+                                 bucketized in pieces whose partitioned records go to pinned host memory, and
+                                 the merge runs bucket range by bucket range, each range's records copied back
+                                 to the device (the reference's bucket files spilled from its in-memory
+                                 store, crates/minimizer_bucketing/src/lib.rs:569-586).  Results are the same. */
 } ggcat_gpu_params;
 
 /* One superkmer in the semantic form of PushSequenceInfo
@@ -95,6 +101,9 @@ typedef struct {
     uint64_t merge_units_walk;  /* units extended by per-thread walks (grid-wide tier, fallback) */
     uint64_t merge_graph_captures; /* captures of the batched merge phase as a CUDA graph (context lifetime) */
     uint64_t merge_graph_replays;  /* launches of that graph (context lifetime) */
+    uint64_t spill_pieces;      /* bucketize pieces whose records went to host memory (0: resident store) */
+    uint64_t spill_ranges;      /* bucket ranges merged one after another from the host store */
+    uint64_t spill_bytes;       /* record bytes held in host memory */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */
