@@ -1000,8 +1000,11 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     if (!ctx->have_buckets) return fail(ctx, GGCAT_GPU_EINVAL, "merge needs a bucketize result");
     if (p->k != ctx->last_params.k || p->m != ctx->last_params.m || p->bucket_bits != ctx->last_params.bucket_bits)
         return fail(ctx, GGCAT_GPU_EINVAL, "merge parameters differ from the bucketize parameters");
-    if (p->k > 64 || (p->k % 2) == 0)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports odd k <= 64 (k=%d)", p->k);
+    if (p->k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports k <= 64 (k=%d)", p->k);
+    // a forward-only k-mer of all G at k = 32 / 64 is the tables' empty key (all ones); canonical
+    // keys never are (the reverse complement, all C, is smaller)
+    if (p->forward_only && (p->k == 32 || p->k == 64))
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "forward-only builds at k = %d are not supported", p->k);
     // Tables are keyed by the canonical packed k-mer (the seq-hash value).  The Rabin-Karp
     // u128 hash is injective on the k-mers of any input short of a 128-bit collision, so it
     // selects the same k-mer identities and gives the same result.

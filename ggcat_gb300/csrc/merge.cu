@@ -153,6 +153,9 @@ struct Graph {
     int fwd;
 
     __device__ __forceinline__ KT rc(KT v) const { return KeyOps<KT>::rc(v, k); }
+    // even k: a k-mer equal to its reverse complement; a walk starts at it and a walk that
+    // enters it stops there (its successor is the mirror of where the walk came from)
+    __device__ __forceinline__ bool pal(KT v) const { return !fwd && v == rc(v); }
     __device__ __forceinline__ KT canon(KT v) const {
         if (fwd) return v;
         const KT r = rc(v);
@@ -224,6 +227,7 @@ struct Graph {
         return true;
     }
     __device__ __forceinline__ bool is_start(KT v, int64_t sv) const {
+        if (pal(v)) return true;
         if (left_boundary(v, sv)) return true;
         KT y;  // the unique predecessor, oriented towards v
         if (pred(v, y) != 1) return true;
@@ -248,6 +252,7 @@ __device__ __forceinline__ uint32_t walk_to_end(const Graph<KT> &g, KT v, int64_
     for (;;) {
         KT u;
         int64_t su;
+        if (steps > 0 && g.pal(cur)) break;  // entered a reverse-complement-symmetric k-mer
         if (!g.next(cur, scur, u, su)) break;
         cur = u;
         scur = su;
@@ -865,6 +870,12 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
         }
         IT code = d == 0 ? kNone : kMulti;
         if (d == 1) code = (IT)(2u * (v_only & kIdxMask) + (fw_only ? 0u : 1u));
+        // even k: a k-mer equal to its reverse complement (both nodes read it the same way).
+        // Edges into it always reach its odd node (a successor search finds it with
+        // fw_only = false), so the odd node ends paths and the even node starts them: a walk
+        // that enters it stops there, as the hash-map walk does when the next k-mer (the
+        // mirror of the one it came from) is already used
+        if (odd && !fwd && x == rx) code = kNone;
         A.succ[u] = code;
     }
     __syncthreads();  // the hash table is dead from here on

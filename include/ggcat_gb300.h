@@ -40,8 +40,9 @@ extern "C" {
 typedef struct ggcat_gpu_ctx ggcat_gpu_ctx;
 
 typedef struct {
-    int32_t k;                /* k-mer length: bucketing k <= 64; merge and link odd k <= 64 (u64 keys for
-                                 k <= 32, u128 keys above); colours and both queries k <= 64 */
+    int32_t k;                /* k-mer length <= 64 (u64 keys for k <= 32, u128 keys above), odd or even;
+                                 forward-only merges exclude k = 32 and 64 (their all-G k-mer is the
+                                 tables' empty key) */
     int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
     int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
     int32_t second_bits;      /* second-level bucket bits reported in superkmer records */
