@@ -204,15 +204,34 @@ struct Graph {
     }
     // ignored-side flags in the orientation of v (hashmap.rs:453-465):
     // canonical orientation: flags == 1 -> left boundary, flags == 2 -> right boundary.
+    // A k-mer equal to its reverse complement blocks no edge: a walk that enters it takes it
+    // and stops there whatever its flags (hashmap.rs:162-297 tests the flags of a k-mer only
+    // after appending it), and a walk leaving it is the mirror of one that enters it.
     __device__ __forceinline__ bool right_boundary(KT v, int64_t slot) const {
+        if (pal(v)) return false;
         uint32_t f = t.vals[slot] >> 30;
         bool is_canon = fwd || v <= rc(v);
         return is_canon ? f == 2u : f == 1u;
     }
     __device__ __forceinline__ bool left_boundary(KT v, int64_t slot) const {
+        if (pal(v)) return false;
         uint32_t f = t.vals[slot] >> 30;
         bool is_canon = fwd || v <= rc(v);
         return is_canon ? f == 1u : f == 2u;
+    }
+    // link flags of an emitted path from v to e (bit0 left end, bit1 right end).  A
+    // reverse-complement-symmetric end is a link end when exactly one of its flags is set; a
+    // path of that k-mer alone takes the sides a walk started on it gives (hashmap.rs:453-465
+    // with is_forward false: flags 1 -> right end, flags 2 -> left end).
+    __device__ __forceinline__ uint8_t path_flags(KT v, int64_t sv, KT e, int64_t se, uint32_t steps) const {
+        if (steps == 0 && pal(v)) {
+            const uint32_t f = t.vals[sv] >> 30;
+            return (uint8_t)((f == 2u ? 1u : 0u) | (f == 1u ? 2u : 0u));
+        }
+        const uint32_t fv = t.vals[sv] >> 30, fe = t.vals[se] >> 30;
+        const bool lb = pal(v) ? (fv == 1u || fv == 2u) : left_boundary(v, sv);
+        const bool rb = pal(e) ? (fe == 1u || fe == 2u) : right_boundary(e, se);
+        return (uint8_t)((lb ? 1u : 0u) | (rb ? 2u : 0u));
     }
     // Traversable successor: unique surviving successor u with a unique surviving
     // predecessor, no bucket boundary between them, and not the same k-mer.
@@ -295,6 +314,16 @@ __device__ void emit_walk(const Graph<KT> &g, KT v, int64_t sv, uint32_t steps, 
     }
 }
 
+// Which of a k-mer's ignored ends sets which MapEntry flag bit (hashmap.rs:393-396: begin <<
+// !is_forward, end << is_forward, in the record's stored orientation).  The k-mers are read in
+// text orientation; a reverse-complemented record swaps begin and end and flips is_forward,
+// which cancels, except for a k-mer equal to its reverse complement (even k): its is_forward
+// (fw < rc) is false in both orientations, so in a reverse-complemented record the text-order
+// ends map to the bits as if it were forward.
+__device__ __forceinline__ uint32_t flag_orientation(uint32_t isf, bool symmetric, uint32_t rcf) {
+    return isf | ((symmetric && rcf) ? 1u : 0u);
+}
+
 // Insert all k-mers of one superkmer record (hashmap.rs:361-431 add_sequence), processing
 // the bases in text orientation with the flags mapped from the stored orientation.
 template <typename KT>
@@ -328,7 +357,8 @@ __device__ __forceinline__ void insert_record(const Table<KT> &t, const uint64_t
         const KT key = isf ? fw : rc;
         int64_t s = tinsert(t, key, status);
         if (s < 0) continue;
-        uint32_t fbits = ((uint32_t)begin_ignored << (isf ^ 1u)) | ((uint32_t)end_ignored << isf);
+        const uint32_t fo = flag_orientation(isf, fw == rc, rcf);
+        uint32_t fbits = ((uint32_t)begin_ignored << (fo ^ 1u)) | ((uint32_t)end_ignored << fo);
         if (fbits) atomicOr(&t.vals[s], fbits << 30);
         atomicAdd(&t.vals[s], 1u);
     }
@@ -353,6 +383,7 @@ __device__ __forceinline__ void extend_slot(const Graph<KT> &g, uint32_t s, cons
     }
     for (int orient = 0; orient < (g.fwd ? 1 : 2); orient++) {
         const KT v = orient ? g.rc(key) : key;
+        if (orient && v == key) break;  // reverse-complement-symmetric: one orientation
         if (!g.is_start(v, s)) continue;
         KT e;
         int64_t se;
@@ -361,8 +392,7 @@ __device__ __forceinline__ void extend_slot(const Graph<KT> &g, uint32_t s, cons
         // is found from its start only
         bool owner = g.fwd || ((int64_t)s < se) || ((int64_t)s == se && orient == 0);
         if (!owner) continue;
-        uint8_t flags = (uint8_t)((g.left_boundary(v, s) ? 1u : 0u) | (g.right_boundary(e, se) ? 2u : 0u));
-        emit_walk(g, v, (int64_t)s, steps, flags, o);
+        emit_walk(g, v, (int64_t)s, steps, g.path_flags(v, (int64_t)s, e, se, steps), o);
     }
 }
 
@@ -825,8 +855,18 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
                 // boundary sides of both orientations (MapEntry flags in canonical
                 // orientation: 1 = left side ignored, 2 = right side ignored)
                 const uint32_t fv = v >> 30;
-                A.bflag[2 * idx] = (uint8_t)((fv == 1u ? 1u : 0u) | (fv == 2u ? 2u : 0u));
-                A.bflag[2 * idx + 1] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
+                if (!fwd && !(k & 1) && key == K::rc(key, k)) {
+                    // reverse-complement-symmetric (even k): edges enter its odd node and leave
+                    // its even node whatever its flags; a single flag makes the path end there
+                    // (odd node) and the mirror path start there (even node) link ends.  Bit 2
+                    // marks the k-mer, bits 3-4 keep the flags for a path of it alone.
+                    const uint32_t one = (fv == 1u || fv == 2u) ? 1u : 0u;
+                    A.bflag[2 * idx] = (uint8_t)(one | 4u | (fv << 3));
+                    A.bflag[2 * idx + 1] = (uint8_t)((one << 1) | 4u | (fv << 3));
+                } else {
+                    A.bflag[2 * idx] = (uint8_t)((fv == 1u ? 1u : 0u) | (fv == 2u ? 2u : 0u));
+                    A.bflag[2 * idx + 1] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
+                }
                 if (keep_kmers) {
                     const unsigned long long di = atomicAdd(&o.counters[kCntKmers], 1ull);
                     if (di < o.kmer_cap) {
@@ -985,7 +1025,15 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
             const unsigned long long ix = gidx + A.uidx[u];
             o.u_off[ix] = off;
             o.u_len[ix] = (uint32_t)k + (uint32_t)Rk[u];
-            o.u_flags[ix] = (uint8_t)((A.bflag[u] & 1u) | (A.bflag[e] & 2u));
+            const uint8_t bu = A.bflag[u];
+            if (Rk[u] == 0 && (bu & 4u)) {
+                // a reverse-complement-symmetric k-mer alone: the sides a walk started on it
+                // gives (flags 1 -> right end, flags 2 -> left end)
+                const uint32_t fv = (bu >> 3) & 3u;
+                o.u_flags[ix] = (uint8_t)((fv == 2u ? 1u : 0u) | (fv == 1u ? 2u : 0u));
+            } else {
+                o.u_flags[ix] = (uint8_t)((bu & 1u) | (A.bflag[e] & 2u));
+            }
         } else {
             o.bases[off + (uint32_t)k - 1 + dist] = base_char((uint32_t)(v >> (2 * (k - 1))));
         }
@@ -1183,7 +1231,8 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                     else
                         sl = tinsert(t, isf ? fw : rc, o.status);
                     const bool bi = (off == 0) && !inc_begin, ei = (off == last) && !inc_end;
-                    fbits = ((uint32_t)bi << (isf ^ 1u)) | ((uint32_t)ei << isf);
+                    const uint32_t fo = flag_orientation(isf, fw == rc, rcf);
+                    fbits = ((uint32_t)bi << (fo ^ 1u)) | ((uint32_t)ei << fo);
                     }
                     if (optimistic || kGlobalTable) {
                         // created entries: counted (W spill test) and, for global tables, listed
