@@ -597,7 +597,12 @@ struct SmemTableView {
 // memory): k <= 32 superkmers are short; k > 32 superkmers of long reads often span 5-6 words
 template <typename KT>
 constexpr int stage_words() { return std::is_same<KT, uint64_t>::value ? 4 : 6; }
-constexpr int kRecBatch = 32;   // records per insert batch of a warp (<= 32)
+// records per insert batch of a warp (<= 32): 16 in the shared-memory tiers, whose units
+// give each warp one or two batches (smaller batches even out the warps at the barrier that
+// ends the insert), 32 in the M tier
+template <int kTier>
+constexpr int rec_batch() { return kTier == kTierM ? 32 : 16; }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // block-shared scalars of the extension phase
 struct ExtShared {
@@ -1143,6 +1148,28 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         __syncthreads();
 
         const uint64_t n_items = U.rec_end - U.rec_begin;
+        constexpr int kRecBatch = rec_batch<kTier>();
+        if constexpr (!kGlobalTable) {
+            // warm L2 with the packed words of the unit's records before the insert batches
+            // load them: one dependent round trip (record, then its words) per unit instead of
+            // one per batch
+            for (uint64_t r0 = threadIdx.x; r0 < n_items; r0 += 4 * NT) {
+                uint64_t w0s[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint64_t r = r0 + (uint64_t)q * NT;
+                    w0s[q] = r < n_items ? a.recs[U.rec_begin + r].w0 : ~0ull;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (w0s[q] == ~0ull) continue;
+                    const SkRec rr{w0s[q], 0};
+                    const uint64_t wb = rec_start(rr) >> 5, we = (rec_start(rr) + rec_len(rr) - 1) >> 5;
+                    prefetch_l2(a.packed + wb);
+                    if ((we >> 4) != (wb >> 4)) prefetch_l2(a.packed + we);  // another 128-byte line
+                }
+            }
+        }
 
         // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes kRecBatch records at
         //      a time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is

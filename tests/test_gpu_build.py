@@ -1,5 +1,7 @@
 """GPU parity of the build hot path against the oracle: superkmer records, surviving
 k-mers with multiplicities, and the canonical maximal-unitig set (bit-exact)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -451,3 +453,45 @@ def test_pinned_text_pipelined_equals_pageable(ctx, k, m, read_len):
     assert k_a == k_b
     assert u_a == u_b
     assert f_a == f_b and len(f_a) > 0
+
+
+def test_build_from_streams_matches_files(tmp_path):
+    """ggcat_gpu_build_from_streams (crates/capi/src/lib.rs:226-292): two streams emitting the
+    reads of two FASTA files, in pieces of varying size, build the same graph file as
+    ggcat_gpu_build_from_files on those files, and its unitigs equal the oracle's."""
+    import ctypes as C
+
+    rng = np.random.default_rng(21)
+    g = synth.random_genome(50_000, rng)
+    files, sources = [], []
+    for i in range(2):
+        reads = synth.sample_reads(g, 2500, 150, 0.003, 0.0, rng)
+        path = tmp_path / f"s{i}.fa"
+        with open(path, "wb") as f:
+            for j, rd in enumerate(reads):
+                f.write(b">s%d_%d\n" % (i, j) + rd.tobytes() + b"\n")
+        files.append(str(path))
+        sources.append([rd.tobytes() for rd in reads])
+    L = _native.load()
+    out_s, out_f = tmp_path / "streams.fa", tmp_path / "files.fa"
+    arr, keep = _native.make_streams(sources)
+    c = _native.GpuContext(0)
+    try:
+        assert L.ggcat_gpu_build_from_streams(c.h, arr, 2, os.fsencode(str(out_s)), 31, 4, 0, 10, 2) == 0
+        names = (C.c_char_p * 2)(*[os.fsencode(f) for f in files])
+        assert L.ggcat_gpu_build_from_files(c.h, names, 2, os.fsencode(str(out_f)), 31, 4, 0, 10, 2) == 0
+    finally:
+        c.close()
+    del keep
+
+    def unitig_set(path):
+        lines = open(path, "rb").read().split(b"\n")
+        seqs = [x for x in lines[1::2] if x]
+        return oracle.canonicalize_unitigs(b"".join(x + b"\n" for x in seqs), np.zeros(len(seqs), np.uint8), 31)
+
+    got = unitig_set(out_s)
+    assert got == unitig_set(out_f)
+    ftext, foff, fln = oracle.fasta_parse(b"".join(open(f, "rb").read() for f in files), 30)
+    r = oracle.build_graph(ftext, foff, fln, oracle.params(k=31, m=10, bucket_bits=10, second_bits=3,
+                                                          min_multiplicity=2, threads=8))
+    assert got == r.unitigs()
