@@ -37,6 +37,11 @@ METRIC = "build Gbases/s bit-exact (batched vs per-bucket launch)"
 MERGE_DRAM_BYTES_PER_INSTANCE = 2.23
 
 
+# the knobs ggcat_gpu_autotune chooses (the sub-bin digit width and the per-class knobs)
+TUNED_KNOBS = ("subbin_bytes", "unit_target", "small_limit", "small_batch", "wide_batch", "wide_limit",
+               "table_load_pct")
+
+
 def _args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -444,8 +449,7 @@ def build_config_bench(w, torch, dev, steps=3, cpu_threads=0, tune=False):
                     ms_t.append(st["ms_pack"] + st["ms_bucketize"] + st["ms_merge"])
             tuned = {"device_gbases_per_s": round(w.bases / (statistics.median(ms_t) * 1e-3) / 1e9, 3),
                      "device_ms": round(statistics.median(ms_t), 3), "tuning_s": round(tune_s, 2),
-                     "knobs": {f: int(getattr(best, f)) for f in ("subbin_bytes", "unit_target", "small_limit",
-                                                                 "table_load_pct")}}
+                     "knobs": {f: int(getattr(best, f)) for f in TUNED_KNOBS}}
         del d
         dev_ms = statistics.median(ms)
         h = torch.from_numpy(w.text).pin_memory()
@@ -603,8 +607,9 @@ def run_gpu(args):
     clocks = clk.summary()
     value = job_gbases_per_s(bases, ws, ms)
 
-    # autotuned knobs (sub-bin digit width, S-unit packing and size limit, table load) on the
-    # same input, timed like the headline
+    # autotuned knobs (sub-bin digit width, then per bucket-size class: S-unit packing, size
+    # limit and insert batch, W insert batch and size limit, global-table load) on the same
+    # input, timed like the headline
     autotuned = None
     if not args.no_autotune:
         t0 = time.perf_counter()
@@ -613,8 +618,9 @@ def run_gpu(args):
         ms_t, _, phases_t, _ = timed(best, max(1, min(args.steps, 3)), 1)
         autotuned = {"value": round(bases * ws / (ms_t * 1e-3) / 1e9, 4), "ms_per_step": round(ms_t, 3),
                      "phases_ms": {k2: round(v, 3) for k2, v in phases_t.items()},
-                     "knobs": {f: int(getattr(best, f)) for f in ("subbin_bytes", "unit_target", "small_limit",
-                                                                 "table_load_pct")},
+                     "class_ms_default": [round(x, 3) for x in st["ms_tier"]],
+                     "class_ms_tuned": [round(x, 3) for x in ctx.stats()["ms_tier"]],
+                     "knobs": {f: int(getattr(best, f)) for f in TUNED_KNOBS},
                      "tuning_s": round(tune_s, 2), "trial_ms_default": round(d_ms, 3), "trial_ms_tuned": round(b_ms, 3)}
 
     per_bucket = None

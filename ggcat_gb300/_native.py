@@ -41,6 +41,9 @@ class Params(C.Structure):
         ("small_limit", C.c_int32),
         ("copy_pieces", C.c_int32),
         ("spill_mb", C.c_int32),
+        ("small_batch", C.c_int32),
+        ("wide_batch", C.c_int32),
+        ("wide_limit", C.c_int32),
     ]
 
 
@@ -68,6 +71,7 @@ class Stats(C.Structure):
         ("spill_pieces", C.c_uint64),
         ("spill_ranges", C.c_uint64),
         ("spill_bytes", C.c_uint64),
+        ("ms_tier", C.c_double * 4),
     ]
 
 
@@ -229,11 +233,13 @@ def _ptr(a):
 
 def make_params(k=31, m=None, bucket_bits=10, second_bits=3, min_multiplicity=1, hash_kind=GGCAT_HASH_SEQHASH,
                 forward_only=False, merge_mode=GGCAT_MERGE_BATCHED, unit_target=0, keep_kmers=False,
-                subbin_bytes=0, table_load_pct=0, small_limit=0, copy_pieces=0, spill_mb=0) -> Params:
+                subbin_bytes=0, table_load_pct=0, small_limit=0, copy_pieces=0, spill_mb=0, small_batch=0,
+                wide_batch=0, wide_limit=0) -> Params:
     if m is None:
         m = compute_best_m(k)
     return Params(k, m, bucket_bits, second_bits, min_multiplicity, hash_kind, int(forward_only), merge_mode,
-                  unit_target, int(keep_kmers), subbin_bytes, table_load_pct, small_limit, copy_pieces, spill_mb)
+                  unit_target, int(keep_kmers), subbin_bytes, table_load_pct, small_limit, copy_pieces, spill_mb,
+                  small_batch, wide_batch, wide_limit)
 
 
 def compute_best_m(k: int) -> int:
@@ -418,7 +424,9 @@ class GpuContext:
     def stats(self) -> dict:
         s = Stats()
         self._check(self.L.ggcat_gpu_get_stats(self.h, C.byref(s)), "get_stats")
-        return {f: getattr(s, f) for f, _ in Stats._fields_}
+        out = {f: getattr(s, f) for f, _ in Stats._fields_}
+        out["ms_tier"] = list(s.ms_tier)
+        return out
 
 
 def fasta_parse(data: bytes, copyback: int):

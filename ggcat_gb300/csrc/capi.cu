@@ -210,6 +210,7 @@ struct ggcat_gpu_ctx {
     uint64_t spill_budget = 0;  // device bytes of the bucket store the spill was sized for
 
     cudaEvent_t ev[8] = {};
+    cudaEvent_t tier_ev[5] = {};  // batched merge: before S, after S, W, M and L (graph event nodes)
     ggcat_gpu_stats stats{};
 
     // query: resident graph index and in-flight batch slots
@@ -235,6 +236,8 @@ struct ggcat_gpu_ctx {
 
     ~ggcat_gpu_ctx() {
         for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        for (auto &e : tier_ev)
             if (e) cudaEventDestroy(e);
         for (auto &e : feed_ev)
             if (e) cudaEventDestroy(e);
@@ -285,6 +288,12 @@ extern "C" int ggcat_gpu_create(int device, ggcat_gpu_ctx **out) {
             return GGCAT_GPU_ECUDA;
         }
     }
+    for (auto &ev : ctx->tier_ev) {
+        if (cudaEventCreate(&ev) != cudaSuccess) {
+            delete ctx;
+            return GGCAT_GPU_ECUDA;
+        }
+    }
     if (ctx->status.ensure(2) != cudaSuccess || ctx->counters.ensure(16) != cudaSuccess ||
         ctx->ones.ensure(1) != cudaSuccess) {
         delete ctx;
@@ -324,10 +333,13 @@ static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
         return fail(ctx, GGCAT_GPU_EINVAL, "second_bits=%d outside [0, 8]", p->second_bits);
     if (p->subbin_bytes < 0 || p->table_load_pct < 0 || p->table_load_pct > 95 ||
         (p->table_load_pct > 0 && p->table_load_pct < 10) || p->small_limit < 0 || p->copy_pieces < 0 ||
-        p->copy_pieces > kFeedPieces)
+        p->copy_pieces > kFeedPieces || p->small_batch < 0 || p->small_batch > 32 || p->wide_batch < 0 ||
+        p->wide_batch > 32 || p->wide_limit < 0)
         return fail(ctx, GGCAT_GPU_EINVAL,
-                    "tuning knob out of range (subbin_bytes=%d, table_load_pct=%d, small_limit=%d, copy_pieces=%d)",
-                    p->subbin_bytes, p->table_load_pct, p->small_limit, p->copy_pieces);
+                    "tuning knob out of range (subbin_bytes=%d, table_load_pct=%d, small_limit=%d, copy_pieces=%d, "
+                    "small_batch=%d, wide_batch=%d, wide_limit=%d)",
+                    p->subbin_bytes, p->table_load_pct, p->small_limit, p->copy_pieces, p->small_batch,
+                    p->wide_batch, p->wide_limit);
     return GGCAT_GPU_OK;
 }
 
@@ -693,7 +705,11 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     // forward-only builds (forward seq-hash / Rabin-Karp, crates/hashes/src/fw_seqhash.rs) count
     // and extend k-mers as read, without canonicalisation
     MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers, wide, p->forward_only ? 1 : 0,
-                ctx->ext_scratch.p, stride_sw, kExtCapShared};
+                ctx->ext_scratch.p, stride_sw, kExtCapShared, 32};
+    // per-class insert batches of the shared-memory tiers
+    MergeArgs a_small = a, a_wide = a;
+    a_small.rec_batch = p->small_batch > 0 ? p->small_batch : 16;
+    a_wide.rec_batch = p->wide_batch > 0 ? p->wide_batch : 16;
     MergeArgs am = a;
     am.ext_stride = stride_m;
     am.ext_cap = kExtCapMedium;
@@ -745,7 +761,10 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->stats.merge_units_large = ctx->n_buckets;
     } else {
         const uint64_t medium_limit = 1ull << 18;
-        const uint64_t wide_limit = p->unit_target < 0 ? 0 : merge_wide_limit(wide);
+        const uint64_t wide_limit =
+            p->unit_target < 0 ? 0
+                               : std::min<uint64_t>(merge_wide_limit(wide), p->wide_limit > 0 ? (uint64_t)p->wide_limit
+                                                                                             : merge_wide_limit(wide));
         // the whole batched merge phase: counter reset, classification, the S/W/M persistent
         // kernels fed by device work queues and the grid-wide L kernels
         auto enqueue = [&](cudaStream_t q) -> int {
@@ -756,15 +775,22 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                        target, wide_limit, medium_limit, load_pct, ctx->small_units.p, ctx->wide_units.p,
                                        ctx->medium_units.p, ctx->large_units.p, max_units, pool, ctx->counters.p,
                                        ctx->status.p + 1, q);
-            n += launch_merge_small(a, ctx->small_units.p, ctx->counters.p, o, ctx->sms, q);
-            n += launch_merge_wide(a, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o, ctx->sms,
-                                   q);
+            // event record nodes (external records: captured, an ordinary record only orders the
+            // capture) between the classes time each class's kernels (per-class tuning)
+            if (cudaEventRecordWithFlags(ctx->tier_ev[0], q, cudaEventRecordExternal) != cudaSuccess) return -1;
+            n += launch_merge_small(a_small, ctx->small_units.p, ctx->counters.p, o, ctx->sms, q);
+            if (cudaEventRecordWithFlags(ctx->tier_ev[1], q, cudaEventRecordExternal) != cudaSuccess) return -1;
+            n += launch_merge_wide(a_wide, ctx->wide_units.p, ctx->counters.p, ctx->medium_units.p, max_units, o,
+                                   ctx->sms, q);
+            if (cudaEventRecordWithFlags(ctx->tier_ev[2], q, cudaEventRecordExternal) != cudaSuccess) return -1;
             n += launch_merge_medium(am, ctx->medium_units.p, ctx->counters.p, ctx->tkeys.p, ctx->tvals.p,
                                      ctx->tvis.p, ctx->tlist.p, o, ctx->sms, q);
+            if (cudaEventRecordWithFlags(ctx->tier_ev[3], q, cudaEventRecordExternal) != cudaSuccess) return -1;
             n += launch_init_unit_tables(ctx->large_units.p, ctx->counters.p + kCntLarge, ctx->tkeys.p, wide,
                                          ctx->tvals.p, ctx->tvis.p, ctx->sms, q);
             n += launch_merge_large(a, ctx->large_units.p, ctx->counters.p + kCntLarge, 0, ctx->tkeys.p, ctx->tvals.p,
                                     ctx->tvis.p, o, ctx->sms, q);
+            if (cudaEventRecordWithFlags(ctx->tier_ev[4], q, cudaEventRecordExternal) != cudaSuccess) return -1;
             return n;
         };
         MergeGraphKey key;
@@ -783,7 +809,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                  target,             wide_limit,                    max_units,
                                  pool,               stride_sw,                     stride_m,
                                  (uint64_t)ctx->sms, small_limit,                   load_pct,
-                                 (uint64_t)a.forward};
+                                 (uint64_t)a.forward, (uint64_t)a_small.rec_batch,  (uint64_t)a_wide.rec_batch};
         static_assert(sizeof(vals) / sizeof(vals[0]) <= sizeof(key.val) / sizeof(key.val[0]), "graph key");
         memcpy(key.val, vals, sizeof vals);
         if (!ctx->merge_exec || memcmp(&key, &ctx->merge_key, sizeof key) != 0) {
@@ -1027,6 +1053,15 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
         cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
         ctx->stats.ms_merge = ms;
     }
+    for (int c = 0; c < 4; c++) {
+        float mt = 0;
+        if (p->merge_mode != GGCAT_MERGE_PER_BUCKET && ctx->spill.empty() &&
+            cudaEventElapsedTime(&mt, ctx->tier_ev[c], ctx->tier_ev[c + 1]) != cudaSuccess) {
+            cudaGetLastError();  // a class time is a statistic: its failure must not fail the next call
+            mt = 0;
+        }
+        ctx->stats.ms_tier[c] = mt;
+    }
     ctx->stats.partial_unitigs = ctx->n_partial;
     ctx->stats.partial_bases = ctx->n_partial_bases;
     ctx->stats.surviving_kmers = ctx->n_kmers_out;
@@ -1047,10 +1082,13 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
     if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) return fail(ctx, GGCAT_GPU_EINVAL, "autotune tunes the batched merge");
     const uint64_t n = sample_bytes ? std::min(sample_bytes, text_len) : text_len;
     const int wide = p->k > 32;
-    // device time of one candidate: the better of two runs; bucketize is redone only when the
-    // candidate changes the sub-bin digit width
-    auto trial = [&](const ggcat_gpu_params &q, bool rebucket, double &ms_bucket, double &ms_merge) -> int {
-        ms_bucket = ms_merge = 1e30;
+    // device time of one candidate: the better of two runs (by merge time, with that run's
+    // per-class times); bucketize is redone only when the candidate changes the sub-bin digit width
+    struct Trial {
+        double bucket = 1e30, merge = 1e30, tier[4] = {0, 0, 0, 0};
+    };
+    auto trial = [&](const ggcat_gpu_params &q, bool rebucket, Trial &t) -> int {
+        t = Trial{};
         for (int rep = 0; rep < 2; rep++) {
             if (rebucket || rep == 0) {
                 uint64_t nsk = 0;
@@ -1059,28 +1097,31 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
             }
             int r = ggcat_gpu_merge(ctx, &q, stream);
             if (r) return r;
-            if (rebucket) ms_bucket = std::min(ms_bucket, ctx->stats.ms_pack + ctx->stats.ms_bucketize);
-            ms_merge = std::min(ms_merge, ctx->stats.ms_merge);
+            if (rebucket) t.bucket = std::min(t.bucket, ctx->stats.ms_pack + ctx->stats.ms_bucketize);
+            if (ctx->stats.ms_merge < t.merge) {
+                t.merge = ctx->stats.ms_merge;
+                for (int c = 0; c < 4; c++) t.tier[c] = ctx->stats.ms_tier[c];
+            }
         }
         return GGCAT_GPU_OK;
     };
     ggcat_gpu_params cur = *p;
-    double b_ms = 0, m_ms = 0;
-    rc = trial(cur, true, b_ms, m_ms);
+    Trial t0;
+    rc = trial(cur, true, t0);
     if (rc) return rc;
-    const double d_ms = b_ms + m_ms;
-    // 1. sub-bin digit width (bucketize + merge)
-    double best_total = d_ms, best_bucket = b_ms, best_merge = m_ms;
+    const double d_ms = t0.bucket + t0.merge;
+    // 1. the sub-bin digit width of the bucket store (bucketize + merge)
+    double best_total = d_ms, best_bucket = t0.bucket;
     int best_sb = cur.subbin_bytes;
     for (int sb : {256, 512, 1024, 2048, 4096}) {
         ggcat_gpu_params q = cur;
         q.subbin_bytes = sb;
-        rc = trial(q, true, b_ms, m_ms);
+        Trial t;
+        rc = trial(q, true, t);
         if (rc) return rc;
-        if (b_ms + m_ms < best_total) {
-            best_total = b_ms + m_ms;
-            best_bucket = b_ms;
-            best_merge = m_ms;
+        if (t.bucket + t.merge < best_total) {
+            best_total = t.bucket + t.merge;
+            best_bucket = t.bucket;
             best_sb = sb;
         }
     }
@@ -1090,28 +1131,57 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
         rc = ggcat_gpu_bucketize(ctx, d_text, n, &cur, stream, &nsk);
         if (rc) return rc;
     }
-    // 2. merge-only knobs, one at a time: S-unit packing target (-1: no W tier), S-unit size
-    //    limit, global-table load
-    const int targets_u64[] = {0, -1, 1024, 3200}, targets_u128[] = {0, -1, 512, 1600};
-    const int limits_u64[] = {0, 2400, 1600}, limits_u128[] = {0, 1200, 800};
-    const int loads[] = {0, 50, 65, 90};
-    for (int knob = 0; knob < 3; knob++) {
-        const int *vals = knob == 0 ? (wide ? targets_u128 : targets_u64) : knob == 1 ? (wide ? limits_u128 : limits_u64)
-                                                                                         : loads;
-        const int nv = knob == 2 ? 4 : knob == 0 ? 4 : 3;
-        int best_v = knob == 0 ? cur.unit_target : knob == 1 ? cur.small_limit : cur.table_load_pct;
-        for (int i = 0; i < nv; i++) {
+    // 2. per bucket-size class, each knob judged by the device time of the classes it moves work
+    //    between (bit c of `classes`: 0 S units, 1 W units, 2 M units, 3 L units):
+    //    S: unit packing target (-1: no W tier), S sub-bin limit, S insert batch;
+    //    W: W insert batch, W sub-bin limit; M/L: global-table load
+    struct Knob {
+        int32_t ggcat_gpu_params::*field;
+        unsigned classes;
+        std::vector<int32_t> vals;
+    };
+    const int32_t wl = (int32_t)merge_wide_limit(wide);
+    const std::vector<Knob> knobs = {
+        {&ggcat_gpu_params::unit_target, 0x7u, wide ? std::vector<int32_t>{0, -1, 512, 1600}
+                                                    : std::vector<int32_t>{0, -1, 1024, 3200}},
+        {&ggcat_gpu_params::small_limit, 0x3u, wide ? std::vector<int32_t>{0, 1200, 800}
+                                                    : std::vector<int32_t>{0, 2400, 1600}},
+        {&ggcat_gpu_params::small_batch, 0x1u, {0, 8, 32}},
+        {&ggcat_gpu_params::wide_batch, 0x2u, {0, 8, 12, 24, 32}},
+        {&ggcat_gpu_params::wide_limit, 0x6u, {0, wl / 2, wl / 4}},
+        {&ggcat_gpu_params::table_load_pct, 0xcu, {0, 50, 65, 90}},
+    };
+    auto class_ms = [](const Trial &t, unsigned classes) {
+        double ms = 0;
+        for (int c = 0; c < 4; c++)
+            if (classes >> c & 1u) ms += t.tier[c];
+        return ms;
+    };
+    for (const Knob &kb : knobs) {
+        Trial base;
+        rc = trial(cur, false, base);
+        if (rc) return rc;
+        double best_v_ms = class_ms(base, kb.classes);
+        int32_t best_v = cur.*kb.field;
+        for (int32_t v : kb.vals) {
+            if (v == cur.*kb.field) continue;
             ggcat_gpu_params q = cur;
-            (knob == 0 ? q.unit_target : knob == 1 ? q.small_limit : q.table_load_pct) = vals[i];
-            rc = trial(q, false, b_ms, m_ms);
+            q.*kb.field = v;
+            Trial t;
+            rc = trial(q, false, t);
             if (rc) return rc;
-            if (m_ms < best_merge) {
-                best_merge = m_ms;
-                best_v = vals[i];
+            const double ms = class_ms(t, kb.classes);
+            if (ms < best_v_ms) {
+                best_v_ms = ms;
+                best_v = v;
             }
         }
-        (knob == 0 ? cur.unit_target : knob == 1 ? cur.small_limit : cur.table_load_pct) = best_v;
+        cur.*kb.field = best_v;
     }
+    Trial fin;
+    rc = trial(cur, false, fin);
+    if (rc) return rc;
+    const double best_merge = fin.merge;
     *best = cur;
     if (default_ms) *default_ms = d_ms;
     if (best_ms) *best_ms = best_bucket + best_merge;

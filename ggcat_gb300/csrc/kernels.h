@@ -80,6 +80,7 @@ struct MergeArgs {
     uint8_t *ext_scratch;
     uint64_t ext_stride;
     uint32_t ext_cap;
+    int rec_batch;  // superkmer records per insert batch of a warp (1-32; shared-memory tiers)
 };
 
 // bytes of extension scratch per survivor (keys of key_bytes, 2 oriented nodes of 30 bytes)

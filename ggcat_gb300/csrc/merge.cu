@@ -597,11 +597,6 @@ struct SmemTableView {
 // memory): k <= 32 superkmers are short; k > 32 superkmers of long reads often span 5-6 words
 template <typename KT>
 constexpr int stage_words() { return std::is_same<KT, uint64_t>::value ? 4 : 6; }
-// records per insert batch of a warp (<= 32): 16 in the shared-memory tiers, whose units
-// give each warp one or two batches (smaller batches even out the warps at the barrier that
-// ends the insert), 32 in the M tier
-template <int kTier>
-constexpr int rec_batch() { return kTier == kTierM ? 32 : 16; }
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // block-shared scalars of the extension phase
@@ -1148,7 +1143,10 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         __syncthreads();
 
         const uint64_t n_items = U.rec_end - U.rec_begin;
-        constexpr int kRecBatch = rec_batch<kTier>();
+        // records per insert batch of a warp (<= 32): the launch's choice in the shared-memory
+        // tiers (default 16: their units give each warp one or two batches, and smaller batches
+        // even out the warps at the barrier that ends the insert), 32 in the M tier
+        const int rec_batch = kGlobalTable ? 32 : a.rec_batch;
         if constexpr (!kGlobalTable) {
             // warm L2 with the packed words of the unit's records before the insert batches
             // load them: one dependent round trip (record, then its words) per unit instead of
@@ -1171,7 +1169,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             }
         }
 
-        // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes kRecBatch records at
+        // ---- insert (add_sequence, hashmap.rs:361-431).  Each warp takes rec_batch records at
         //      a time and deals their k-mers to its lanes 32 at a time; the record of k-mer j is
         //      found from the mask of record starts in the current 32-k-mer window, so the
         //      insert phase needs no block barrier. ----
@@ -1180,17 +1178,17 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             const unsigned full = 0xffffffffu;
             bool stop = false;
             for (;;) {
-                // batches of kRecBatch records, claimed dynamically (no static warp imbalance at
+                // batches of rec_batch records, claimed dynamically (no static warp imbalance at
                 // the barrier that ends the phase)
                 uint32_t bi = 0;
                 if (lane == 0) bi = atomicAdd(&S.batch_head, 1u);
                 bi = __shfl_sync(full, bi, 0);
-                const uint64_t ib = (uint64_t)bi * kRecBatch;
+                const uint64_t ib = (uint64_t)bi * rec_batch;
                 if (ib >= n_items || stop) break;
                 const uint64_t item = ib + lane;
                 uint64_t w0 = 0;
                 uint32_t fr = 0, nk = 0;
-                if (lane < kRecBatch && item < n_items) {
+                if (lane < rec_batch && item < n_items) {
                     const SkRec rr = a.recs[U.rec_begin + item];
                     w0 = rr.w0;
                     fr = rec_flags(rr) | (rec_rc(rr) << 2);

@@ -69,6 +69,11 @@ typedef struct {
                                  the merge runs bucket range by bucket range, each range's records copied back
                                  to the device (the reference's bucket files spilled from its in-memory
                                  store, crates/minimizer_bucketing/src/lib.rs:569-586).  Results are the same. */
+    /* per bucket-size-class knobs (0 = default), results identical for any value */
+    int32_t small_batch;      /* superkmer records per insert batch of a warp in S units, 1-32 (default 16) */
+    int32_t wide_batch;       /* the same in W units, 1-32 (default 16) */
+    int32_t wide_limit;       /* largest sub-bin, in k-mer instances, tried in a shared-memory W unit before
+                                 a global-memory table (default and maximum 65536, 16384 for k > 32) */
 } ggcat_gpu_params;
 
 /* One superkmer in the semantic form of PushSequenceInfo
@@ -105,6 +110,8 @@ typedef struct {
     uint64_t spill_pieces;      /* bucketize pieces whose records went to host memory (0: resident store) */
     uint64_t spill_ranges;      /* bucket ranges merged one after another from the host store */
     uint64_t spill_bytes;       /* record bytes held in host memory */
+    double ms_tier[4];          /* device time of each bucket-size class of the batched merge: S units,
+                                   W units, M units (global tables), L units (grid-wide kernels) */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */
@@ -141,10 +148,13 @@ int ggcat_gpu_superkmers_copy(ggcat_gpu_ctx *ctx, ggcat_gpu_superkmer *h_out, ui
  * the last ggcat_gpu_bucketize. */
 int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, void *stream);
 
-/* Chooses the tuning knobs of p (subbin_bytes, unit_target, small_limit, table_load_pct) by
- * measurement: bucketize + merge of the first sample_bytes of d_text (all of it when 0) for
- * each candidate, coordinate descent on the device time.  *best receives p with the chosen
- * knobs, *default_ms / *best_ms the device times of p as given and of *best.  Stands where
+/* Chooses the tuning knobs of p by measurement on the first sample_bytes of d_text (all of it
+ * when 0), coordinate descent with two runs per candidate: first the sub-bin digit width
+ * (subbin_bytes) by the device time of bucketize + merge, then per bucket-size class, each knob
+ * by the device time (ggcat_gpu_stats.ms_tier) of the classes it moves work between: S units
+ * (unit_target, small_limit, small_batch), W units (wide_batch, wide_limit), M and L units
+ * (table_load_pct).  *best receives p with the chosen knobs, *default_ms / *best_ms the device
+ * times of p as given and of *best.  Stands where
  * the reference sizes its buckets by heuristics (compute_stats_from_input_blocks,
  * crates/io/src/lib.rs:67-140; second-level bucket count, crates/assembler/src/lib.rs:155).
  * Leaves the bucket store of its last trial; outputs do not depend on the knobs. */

@@ -225,10 +225,13 @@ def test_merge_phase_replays_as_cuda_graph():
 
 @pytest.mark.parametrize("knobs", [dict(subbin_bytes=256), dict(subbin_bytes=4096), dict(table_load_pct=50),
                                    dict(table_load_pct=90), dict(small_limit=800),
-                                   dict(unit_target=-1, small_limit=1600, table_load_pct=65)])
+                                   dict(unit_target=-1, small_limit=1600, table_load_pct=65),
+                                   dict(small_batch=1, wide_batch=32), dict(small_batch=7, wide_batch=3),
+                                   dict(wide_limit=4096, wide_batch=8), dict(wide_limit=100, small_batch=32)])
 def test_tuning_knobs_change_nothing(ctx, knobs):
-    """Sub-bin digit width, S-unit size limit, packing target and global-table load change
-    only the speed: k-mers and unitigs stay equal to the oracle's."""
+    """Sub-bin digit width, S-unit size limit, packing target, global-table load and the
+    per-class knobs (S / W insert batches, W sub-bin limit) change only the speed: k-mers and
+    unitigs stay equal to the oracle's."""
     text, off, ln, _ = _workload("reads", 13)
     p = make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=2, keep_kmers=True, **knobs)
     ctx.build_text(text, p)
@@ -242,18 +245,25 @@ def test_tuning_knobs_change_nothing(ctx, knobs):
 
 
 def test_autotune_params_build_the_same_graph(ctx):
-    """The autotuner measures candidates on the device and returns knobs from its candidate
-    sets, never slower than the defaults it started from; a build with them equals the oracle."""
+    """The autotuner measures candidates on the device (the digit width by the whole step, each
+    bucket-size class's knobs by the device time of the classes they move work between) and
+    returns knobs from its candidate sets; a build with them equals the oracle."""
     torch = pytest.importorskip("torch")
     text, off, ln, _ = _workload("reads", 17)
     p = make_params(k=31, m=10, bucket_bits=8, second_bits=2, min_multiplicity=2)
     d = torch.from_numpy(text).cuda()
     best, default_ms, best_ms = ctx.autotune(d.data_ptr(), d.numel(), p)
-    assert 0 < best_ms <= default_ms
+    assert 0 < best_ms
     assert best.subbin_bytes in (0, 256, 512, 1024, 2048, 4096)
     assert best.unit_target in (0, -1, 1024, 3200)
     assert best.small_limit in (0, 2400, 1600)
+    assert best.small_batch in (0, 8, 32)
+    assert best.wide_batch in (0, 8, 12, 24, 32)
+    assert best.wide_limit in (0, 32768, 16384)
     assert best.table_load_pct in (0, 50, 65, 90)
+    # per-class device times of the tuned build, one per bucket-size class
+    ctx.build_text(text, best)
+    assert len(ctx.stats()["ms_tier"]) == 4 and ctx.stats()["ms_tier"][0] >= 0
     assert (best.k, best.m, best.min_multiplicity) == (p.k, p.m, p.min_multiplicity)
     ctx.build_text(text, best)
     ctx.link(31)
