@@ -108,6 +108,8 @@ def lib():
         L.orc_build_free.argtypes = [P]
         L.orc_build_kmers.restype = sz
         L.orc_build_kmers.argtypes = [P, P, P, P, sz]
+        L.orc_build_kmers_wide.restype = sz
+        L.orc_build_kmers_wide.argtypes = [P, P, P, sz]
         L.orc_build_kmer_colors.restype = sz
         L.orc_build_kmer_colors.argtypes = [P, P, P, sz]
         L.orc_build_unitigs.restype = sz
@@ -245,6 +247,15 @@ class BuildResult:
         mult = np.zeros(n, np.uint64)
         lib().orc_build_kmers(self.h, _ptr(lo), _ptr(hi), _ptr(mult), n)
         return lo, hi, mult
+
+    def kmers_wide(self):
+        """Surviving k-mers as (n, 4) u64 words (bases 0-31, 32-63, 64-95, 96-127; k <= 128)
+        with their multiplicities."""
+        n = lib().orc_build_kmers_wide(self.h, None, None, 0)
+        words = np.zeros((n, 4), np.uint64)
+        mult = np.zeros(n, np.uint64)
+        lib().orc_build_kmers_wide(self.h, _ptr(words), _ptr(mult), n)
+        return words, mult
 
     def kmer_colors(self):
         n = lib().orc_build_kmers(self.h, None, None, None, 0)

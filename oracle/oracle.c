@@ -543,9 +543,19 @@ size_t orc_fasta_parse(const uint8_t *file, size_t file_len, long copyback, uint
  * unitigs, and this one is restated for every sub-bucket here.
  * ====================================================================== */
 
+/* a packed k-mer of up to 128 bases, base i at bits 2i of (lo | hi << 128) */
+typedef struct {
+    u128 lo, hi;
+} okey;
+static inline int okey_cmp(okey a, okey b) {
+    if (a.hi != b.hi) return a.hi < b.hi ? -1 : 1;
+    if (a.lo != b.lo) return a.lo < b.lo ? -1 : 1;
+    return 0;
+}
+
 typedef struct {
     u128 key;      /* MH unextendable hash */
-    u128 packed;   /* canonical 2-bit packed k-mer (seq-hash layout) */
+    okey packed;   /* canonical 2-bit packed k-mer (seq-hash layout, extended past 64 bases) */
     uint64_t count;
     uint8_t flags, used, occupied;
     uint32_t ordinal;    /* creation order; stable across kmap_grow (colour pairs refer to it) */
@@ -618,16 +628,24 @@ static inline uint64_t entry_mult(const kentry *e) {
     return e->count >> (e->flags == (READ_FLAG_INCL_BEGIN | READ_FLAG_INCL_END));
 }
 
-/* packed canonical k-mer in seq-hash layout (base i at bits 2i) for k <= 64 */
-static u128 pack_canonical(const uint8_t *cb, int k, int canonical) {
-    u128 fw = 0, rc = 0;
+/* packed canonical k-mer in seq-hash layout (base i at bits 2i) for k <= 128; for k <= 64
+ * the seq-hash value itself (hi = 0) */
+static okey pack_canonical(const uint8_t *cb, int k, int canonical) {
+    okey fw = {0, 0}, rc = {0, 0};
     for (int i = 0; i < k; i++) {
-        fw |= (u128)(cb[i] & 3) << (2 * i);
-        rc |= (u128)((cb[k - 1 - i] & 3) ^ 2) << (2 * i);
+        const u128 f = (u128)(cb[i] & 3), r = (u128)((cb[k - 1 - i] & 3) ^ 2);
+        if (i < 64) {
+            fw.lo |= f << (2 * i);
+            rc.lo |= r << (2 * i);
+        } else {
+            fw.hi |= f << (2 * (i - 64));
+            rc.hi |= r << (2 * (i - 64));
+        }
     }
     if (!canonical) return fw;
-    return fw < rc ? fw : rc;
+    return okey_cmp(fw, rc) < 0 ? fw : rc;
 }
+static inline size_t okey_hash(okey k) { return khash(k.lo) ^ (size_t)mix64((uint64_t)k.hi ^ mix64((uint64_t)(k.hi >> 64))); }
 
 typedef struct {
     uint8_t *seq; /* ASCII */
@@ -648,7 +666,7 @@ static void ut_push(unitig_vec *v, unitig_t u) {
 }
 
 typedef struct {
-    u128 packed;
+    okey packed;
     uint64_t mult;
     uint32_t color_off, color_n;
 } kmer_out;
@@ -948,14 +966,14 @@ static void rc_ascii(uint8_t *s, size_t n) {
 /* link key of a boundary k-mer: its unextendable hash identity, i.e. the canonical packed
  * k-mer for the canonical hash families and the k-mer as read for the forward ones
  * (extend_unitigs.rs:142-147, 196-240 key the extremities by hash.to_unextendable()) */
-static u128 pack_ascii_key(const uint8_t *a, int k, int canonical) {
+static okey pack_ascii_key(const uint8_t *a, int k, int canonical) {
     uint8_t tmp[128];
     for (int i = 0; i < k; i++) tmp[i] = orc_compress_base(a[i]);
     return pack_canonical(tmp, k, canonical);
 }
 
 typedef struct {
-    u128 key;
+    okey key;
     int32_t ends[2]; /* endpoint ids (unitig*2 + side), -1 if unused */
     uint8_t occupied;
 } link_entry;
@@ -973,9 +991,9 @@ static void link_stage(unitig_vec *in, int k, int canonical, unitig_vec *out) {
             unitig_t *u = &in->v[i];
             if (!(side ? u->fw_link : u->bw_link)) continue;
             const uint8_t *km = side ? u->seq + u->len - k : u->seq;
-            u128 key = pack_ascii_key(km, k, canonical);
-            size_t h = khash(key) & (cap - 1);
-            while (tab[h].occupied && tab[h].key != key) h = (h + 1) & (cap - 1);
+            okey key = pack_ascii_key(km, k, canonical);
+            size_t h = okey_hash(key) & (cap - 1);
+            while (tab[h].occupied && okey_cmp(tab[h].key, key) != 0) h = (h + 1) & (cap - 1);
             if (!tab[h].occupied) {
                 tab[h].occupied = 1;
                 tab[h].key = key;
@@ -1147,12 +1165,15 @@ struct orc_build_result {
 
 static int cmp_kmer_out(const void *a, const void *b) {
     const kmer_out *x = a, *y = b;
-    return x->packed < y->packed ? -1 : x->packed > y->packed;
+    return okey_cmp(x->packed, y->packed);
 }
 
 orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const uint64_t *seq_len,
                             const uint32_t *seq_colors, size_t nseq, const orc_params *p) {
-    if (p->k - p->m < 2 || p->k > 64) return NULL;
+    /* packed k-mers up to 128 bases; above 64 only the Rabin-Karp families key them
+     * (crates/api/src/utils.rs:10-69: sequence hashes stop at k = 64) */
+    if (p->k - p->m < 2 || p->k > 128) return NULL;
+    if (p->k > 64 && p->hash_kind != ORC_H_CN_RK128 && p->hash_kind != ORC_H_FW_RK128) return NULL;
     orc_hash_init_k(p->hash_kind, p->k);
     sk_vec sk = bucketize_vec(text, seq_off, seq_len, nseq, p);
     /* group by sub-bucket (bucket, second_bucket): counting sort */
@@ -1214,7 +1235,7 @@ orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const 
     qsort(kv.v, kv.n, sizeof(kmer_out), cmp_kmer_out);
     size_t w = 0;
     for (size_t i = 0; i < kv.n; i++) {
-        if (w > 0 && kv.v[w - 1].packed == kv.v[i].packed) {
+        if (w > 0 && okey_cmp(kv.v[w - 1].packed, kv.v[i].packed) == 0) {
             if (kv.v[w - 1].mult != kv.v[i].mult) kv.v[w - 1].mult = UINT64_MAX; /* inconsistency marker */
             continue;
         }
@@ -1253,8 +1274,22 @@ void orc_build_free(orc_build_result *r) {
 size_t orc_build_kmers(const orc_build_result *r, uint64_t *lo, uint64_t *hi, uint64_t *mult, size_t cap) {
     if (lo)
         for (size_t i = 0; i < r->nkmers && i < cap; i++) {
-            lo[i] = (uint64_t)r->kmers[i].packed;
-            hi[i] = (uint64_t)(r->kmers[i].packed >> 64);
+            lo[i] = (uint64_t)r->kmers[i].packed.lo;
+            hi[i] = (uint64_t)(r->kmers[i].packed.lo >> 64);
+            mult[i] = r->kmers[i].mult;
+        }
+    return r->nkmers;
+}
+
+/* the surviving k-mers as four 64-bit words each (bases 0-31, 32-63, 64-95, 96-127) */
+size_t orc_build_kmers_wide(const orc_build_result *r, uint64_t *words, uint64_t *mult, size_t cap) {
+    if (words)
+        for (size_t i = 0; i < r->nkmers && i < cap; i++) {
+            const okey q = r->kmers[i].packed;
+            words[4 * i] = (uint64_t)q.lo;
+            words[4 * i + 1] = (uint64_t)(q.lo >> 64);
+            words[4 * i + 2] = (uint64_t)q.hi;
+            words[4 * i + 3] = (uint64_t)(q.hi >> 64);
             mult[i] = r->kmers[i].mult;
         }
     return r->nkmers;
@@ -1332,7 +1367,7 @@ int orc_query(const uint64_t *graph_lo, const uint64_t *graph_hi, size_t ngraph,
             cb[i] = orc_compress_base(c);
             run++;
             if (run >= (size_t)k) {
-                u128 key = pack_canonical(cb + i + 1 - (size_t)k, k, 1);
+                u128 key = pack_canonical(cb + i + 1 - (size_t)k, k, 1).lo;
                 size_t h = khash(key) & (cap - 1);
                 while (tab[h].occupied && tab[h].key != key) h = (h + 1) & (cap - 1);
                 if (tab[h].occupied) {

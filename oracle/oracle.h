@@ -77,6 +77,8 @@ void orc_build_free(orc_build_result *r);
 /* surviving canonical k-mers: 2-bit packed canonical k-mer (lo, hi words, seq-hash layout)
  * and multiplicity, sorted by (hi, lo). */
 size_t orc_build_kmers(const orc_build_result *r, uint64_t *lo, uint64_t *hi, uint64_t *mult, size_t cap);
+/* the same with four 64-bit words per k-mer (k <= 128: bases 0-31, 32-63, 64-95, 96-127) */
+size_t orc_build_kmers_wide(const orc_build_result *r, uint64_t *words, uint64_t *mult, size_t cap);
 /* colour subset of each surviving k-mer, same order: offsets into a flat colour list */
 size_t orc_build_kmer_colors(const orc_build_result *r, uint64_t *off, uint32_t *colors, size_t cap);
 /* canonical, sorted maximal-unitig set as '\n'-terminated ASCII lines; returns bytes. */

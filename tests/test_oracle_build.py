@@ -148,3 +148,49 @@ def test_build_even_k_palindromes(k, m):
         else:
             assert got[x] == c, (x, got[x], c)
     assert r.unitigs() == naive.canonical_set(naive.maximal_unitigs(set(exp), k), k)
+
+
+def _wide_kmers_to_strings(words, k):
+    dec = b"ACTG"
+    out = []
+    for w in words.tolist():
+        v = w[0] | (w[1] << 64) | (w[2] << 128) | (w[3] << 192)
+        out.append(naive.canon(bytes(dec[(v >> (2 * i)) & 3] for i in range(k))))
+    return out
+
+
+@pytest.mark.parametrize("k,m,min_mult", [(65, 14, 1), (75, 16, 2), (101, 25, 1), (128, 32, 1), (96, 20, 1)])
+def test_build_long_k_rabin_karp(k, m, min_mult):
+    """k > 64: the reference keys k-mers by the canonical Rabin-Karp u128 hash
+    (crates/api/src/utils.rs:10-69); the oracle counts and extends by that hash and reports
+    the packed k-mers in 4 words.  Against the naive global computation: same k-mers with the
+    same multiplicities, same maximal unitigs (genome copies with variants, read sets, and for
+    even k hairpins whose centre k-mer is its own reverse complement)."""
+    rng = np.random.default_rng(k)
+    seqs = [x.tobytes() for x in synth.sample_reads(synth.random_genome(4000, rng), 200, 300, 0.004, 0.0, rng)]
+    seqs += _genome_mix(k, L=3000, copies=2)
+    if k % 2 == 0:
+        for _ in range(20):
+            s = synth.random_genome(int(rng.integers(k // 2, 2 * k)), rng)
+            seqs.append(np.concatenate([s, synth.revcomp(s)]).tobytes())
+    text, off, ln, _ = synth.pack_sequences([np.frombuffer(s, np.uint8) for s in seqs])
+    p = oracle.params(k=k, m=m, bucket_bits=4, second_bits=2, min_multiplicity=min_mult, threads=2,
+                      hash_kind=oracle.H_CN_RK128)
+    r = oracle.build_graph(text, off, ln, p)
+    words, mult = r.kmers_wide()
+    got = dict(zip(_wide_kmers_to_strings(words, k), mult.tolist()))
+    exp_all = naive.kmer_counts(seqs, k)
+    exp = {x: c for x, c in exp_all.items() if c >= min_mult}
+    assert set(got) == set(exp)
+    for x, c in exp.items():
+        if x == naive.rc(x):  # the splitter's double count at rc-symmetric k-mers (even k)
+            assert c <= got[x] <= 2 * c
+        else:
+            assert got[x] == c
+    assert r.unitigs() == naive.canonical_set(naive.maximal_unitigs(set(exp), k), k)
+
+
+def test_seq_hash_rejects_k_above_64():
+    text, off, ln, _ = synth.pack_sequences([np.frombuffer(b"ACGT" * 40, np.uint8)])
+    with pytest.raises(ValueError):
+        oracle.build_graph(text, off, ln, oracle.params(k=65, m=14, hash_kind=oracle.H_CN_SEQ128))
