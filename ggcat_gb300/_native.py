@@ -258,7 +258,7 @@ def compute_best_m(k: int) -> int:
         return 13
     if k <= 64:
         return 14
-    return int(round(k / 4.0))
+    return (k + 2) // 4  # f64::round: halves away from zero
 
 
 class GpuContext:
@@ -328,11 +328,12 @@ class GpuContext:
 
     def kmers(self):
         """Surviving canonical k-mers and multiplicities.  keys: u64 array for k <= 32, an
-        (n, 2) array of (lo, hi) words for k > 32."""
+        (n, 2) array of (lo, hi) words for 32 < k <= 64, an (n, 4) array of words (bases 0-31,
+        32-63, 64-95, 96-126) above."""
         n = C.c_uint64()
         self._check(self.L.ggcat_gpu_kmers_copy(self.h, None, None, 0, C.byref(n)), "kmers_copy")
-        wide = self.k > 32
-        keys = np.zeros((n.value, 2) if wide else n.value, np.uint64)
+        words = 4 if self.k > 64 else 2 if self.k > 32 else 1
+        keys = np.zeros((n.value, words) if words > 1 else n.value, np.uint64)
         mult = np.zeros(n.value, np.uint64)
         self._check(self.L.ggcat_gpu_kmers_copy(self.h, _ptr(keys), _ptr(mult), n.value, C.byref(n)), "kmers_copy")
         return keys, mult

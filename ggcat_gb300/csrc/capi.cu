@@ -322,11 +322,18 @@ extern "C" const char *ggcat_gpu_last_error(const ggcat_gpu_ctx *ctx) { return c
 
 extern "C" uint64_t ggcat_gpu_kernel_launches(const ggcat_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+// merge-table key words as a power of two: u64 (k <= 32), u128 (k <= 64), u256 (k <= 127)
+static int key_width(int k) { return k > 64 ? 2 : k > 32 ? 1 : 0; }
+
 static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
     if (!p) return fail(ctx, GGCAT_GPU_EINVAL, "null params");
     if (p->m < 2 || p->m > 32) return fail(ctx, GGCAT_GPU_EINVAL, "minimizer length m=%d outside [2, 32]", p->m);
     if (p->k - p->m < 2) return fail(ctx, GGCAT_GPU_EINVAL, "need k - m >= 2 (k=%d, m=%d)", p->k, p->m);
-    if (p->k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "k=%d > 64 is not supported on the device", p->k);
+    if (p->k > 127) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "k=%d > 127 is not supported on the device", p->k);
+    // the reference's sequence hashes stop at k = 64; longer k-mers take the Rabin-Karp family
+    // (crates/api/src/utils.rs:10-69)
+    if (p->k > 64 && p->hash_kind == GGCAT_HASH_SEQHASH)
+        return fail(ctx, GGCAT_GPU_EINVAL, "sequence hash for k=%d > 64 (use the Rabin-Karp hash)", p->k);
     if (p->bucket_bits < 1 || p->bucket_bits > 15)
         return fail(ctx, GGCAT_GPU_EINVAL, "bucket_bits=%d outside [1, 15]", p->bucket_bits);
     if (p->second_bits < 0 || p->second_bits > 8)
@@ -672,9 +679,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     CK(ctx->out_off.ensure(u_cap));
     CK(ctx->out_len.ensure(u_cap));
     CK(ctx->out_flags.ensure(u_cap));
-    const int wide = p->k > 32 ? 1 : 0;  // u128 table keys
+    const int wide = key_width(p->k);  // table key words: 1 << wide
     if (p->keep_kmers) {
-        CK(ctx->kmer_keys.ensure(kmer_cap * (wide ? 2 : 1)));
+        CK(ctx->kmer_keys.ensure(kmer_cap << wide));
         CK(ctx->kmer_mult.ensure(kmer_cap));
     }
     const uint64_t max_units = ctx->n_bins + 1;
@@ -689,7 +696,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     const uint32_t load_pct = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : 80u;
     const uint64_t max_big_units = std::min<uint64_t>(ctx->n_bins, ctx->n_kmers / small_limit + 1);
     uint64_t pool = ctx->n_kmers * 200 / load_pct + 2 + 128ull * (ctx->n_buckets + max_big_units) + 1024;
-    CK(ctx->tkeys.ensure(pool * (wide ? 2 : 1)));
+    CK(ctx->tkeys.ensure(pool << wide));
     CK(ctx->tvals.ensure(pool));
     CK(ctx->tvis.ensure(pool));
     CK(ctx->tlist.ensure(pool));
@@ -893,7 +900,7 @@ static int merge_retry(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream
 static int merge_spill(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_t s) {
     const uint64_t nb = ctx->n_bins, nbk = ctx->n_buckets;
     const int fb = ctx->fine_bits;
-    const uint64_t kw = p->k > 32 ? 2 : 1;
+    const uint64_t kw = 1ull << key_width(p->k);
     const uint64_t tot_recs = ctx->n_recs, tot_kmers = ctx->n_kmers;
     std::vector<uint64_t> brec(nbk, 0);
     for (const auto &pc : ctx->spill)
@@ -1026,7 +1033,7 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     if (!ctx->have_buckets) return fail(ctx, GGCAT_GPU_EINVAL, "merge needs a bucketize result");
     if (p->k != ctx->last_params.k || p->m != ctx->last_params.m || p->bucket_bits != ctx->last_params.bucket_bits)
         return fail(ctx, GGCAT_GPU_EINVAL, "merge parameters differ from the bucketize parameters");
-    if (p->k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports k <= 64 (k=%d)", p->k);
+    if (p->k > 127) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "device merge supports k <= 127 (k=%d)", p->k);
     // a forward-only k-mer of all G at k = 32 / 64 is the tables' empty key (all ones); canonical
     // keys never are (the reverse complement, all C, is smaller)
     if (p->forward_only && (p->k == 32 || p->k == 64))
@@ -1237,7 +1244,7 @@ extern "C" int ggcat_gpu_kmers_copy(ggcat_gpu_ctx *ctx, uint64_t *h_kmers, uint6
     if (n) *n = ctx->n_kmers_out;
     if (!h_kmers) return GGCAT_GPU_OK;
     uint64_t cnt = std::min<uint64_t>(cap, ctx->n_kmers_out);
-    const uint64_t words = ctx->last_params.k > 32 ? 2 : 1;
+    const uint64_t words = 1ull << key_width(ctx->last_params.k);
     CK(cudaSetDevice(ctx->device));
     if (cnt) {
         CK(cudaMemcpy(h_kmers, ctx->kmer_keys.p, cnt * words * sizeof(uint64_t), cudaMemcpyDeviceToHost));
@@ -1257,11 +1264,11 @@ static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
     F.clear();
     const uint64_t n = ctx->n_partial, nn = 2 * n;
     if (nn >= 0xffffffffull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage: too many partial unitigs");
-    const int wide = k > 32;
+    const int wide = key_width(k);
     uint64_t cap = 1024;
     while (cap < 2 * nn) cap <<= 1;
     LinkBufs &L = ctx->lk;
-    CK(L.keys.ensure(cap * (wide ? 2 : 1)));
+    CK(L.keys.ensure(cap << wide));
     CK(L.min12.ensure(2 * cap));
     CK(L.eslot.ensure(nn + 1));
     CK(L.succ.ensure(nn + 1));
@@ -1281,7 +1288,7 @@ static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
     CK(L.out_off.ensure(n + 1));
     CK(L.out_len.ensure(n + 1));
     CK(L.out_flags.ensure(n + 1));
-    CK(cudaMemsetAsync(L.keys.p, 0xff, cap * (wide ? 2 : 1) * sizeof(uint64_t), s));
+    CK(cudaMemsetAsync(L.keys.p, 0xff, (cap << wide) * sizeof(uint64_t), s));
     CK(cudaMemsetAsync(L.min12.p, 0xff, 2 * cap * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(L.state.p, 0, nn + 1, s));
     CK(cudaMemsetAsync(L.chain_off.p, 0xff, (nn + 1) * sizeof(unsigned long long), s));
@@ -1373,7 +1380,7 @@ static int link_device(ggcat_gpu_ctx *ctx, int k, cudaStream_t s) {
 extern "C" int ggcat_gpu_link(ggcat_gpu_ctx *ctx, int k) {
     if (!ctx) return GGCAT_GPU_EINVAL;
     if (!ctx->have_merge) return fail(ctx, GGCAT_GPU_EINVAL, "no merge result");
-    if (k < 3 || k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 64");
+    if (k < 3 || k > 127) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "link stage supports k <= 127");
     if (k != ctx->last_params.k) return fail(ctx, GGCAT_GPU_EINVAL, "link k=%d differs from the build k=%d", k,
                                              ctx->last_params.k);
     CK(cudaSetDevice(ctx->device));
@@ -1570,13 +1577,21 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
     // compute_best_m (crates/utils/src/lib.rs:29-40) when minimizer_length == SIZE_MAX
     if (minimizer_length == (size_t)-1) {
         int k = p.k;
-        p.m = k <= 13 ? std::max(k / 2, k - 4) : k <= 15 ? 9 : k <= 21 ? 10 : k <= 30 ? 11 : k <= 37 ? 12 : k <= 42 ? 13 : 14;
+        p.m = k <= 13   ? std::max(k / 2, k - 4)
+              : k <= 15 ? 9
+              : k <= 21 ? 10
+              : k <= 30 ? 11
+              : k <= 37 ? 12
+              : k <= 42 ? 13
+              : k <= 64 ? 14
+                        : (k + 2) / 4;  // round(k / 4), halves away from zero
     } else {
         p.m = (int)minimizer_length;
     }
     bucket_counts_for(est, &p.bucket_bits, &p.second_bits);
     p.min_multiplicity = (int)min_multiplicity;
-    p.hash_kind = GGCAT_HASH_SEQHASH;
+    // HashType::Auto (crates/api/src/utils.rs:17-25): sequence hash up to k = 64, Rabin-Karp above
+    p.hash_kind = p.k <= 64 ? GGCAT_HASH_SEQHASH : GGCAT_HASH_RABIN_KARP128;
     p.forward_only = forward_only;
     p.merge_mode = GGCAT_MERGE_BATCHED;
     p.keep_kmers = colors ? 1 : 0;
@@ -1710,6 +1725,7 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     ctx->have_colors = false;
     const uint64_t nd = ctx->n_kmers_out;
     if (nd >= 0xffffffffull) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "colours support < 2^32 k-mers");
+    if (ctx->last_params.k > 64) return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "colours support k <= 64");
     const int words = (int)((n_colors + 31) / 32);
     uint64_t cap = 1024;
     while (cap < 2 * nd + 64) cap <<= 1;

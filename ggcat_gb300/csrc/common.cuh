@@ -125,6 +125,173 @@ struct KeyOps<u128> {
     }
 };
 
+// ---------------------------------------------------------------------------
+// k > 64 (the Rabin-Karp families of the reference, crates/api/src/utils.rs:10-69): the
+// canonical packed k-mer in four 64-bit words, base i at bit 2i of the 256-bit value (w[0]
+// holds bases 0-31), k <= 127.  The top bit of w[3] is never set by a k-mer, which leaves the
+// all-ones word for an empty slot and kU256Claim for a slot being written.
+// ---------------------------------------------------------------------------
+struct __align__(32) u256 {
+    uint64_t w[4];
+    u256() = default;
+    __host__ __device__ constexpr u256(uint64_t x) : w{x, 0, 0, 0} {}
+    __host__ __device__ constexpr u256(uint64_t a, uint64_t b, uint64_t c, uint64_t d) : w{a, b, c, d} {}
+    __host__ __device__ explicit operator uint64_t() const { return w[0]; }
+    __host__ __device__ explicit operator uint32_t() const { return (uint32_t)w[0]; }
+};
+__host__ __device__ __forceinline__ u256 operator|(const u256 &a, const u256 &b) {
+    return u256(a.w[0] | b.w[0], a.w[1] | b.w[1], a.w[2] | b.w[2], a.w[3] | b.w[3]);
+}
+__host__ __device__ __forceinline__ u256 operator&(const u256 &a, const u256 &b) {
+    return u256(a.w[0] & b.w[0], a.w[1] & b.w[1], a.w[2] & b.w[2], a.w[3] & b.w[3]);
+}
+__host__ __device__ __forceinline__ u256 operator^(const u256 &a, const u256 &b) {
+    return u256(a.w[0] ^ b.w[0], a.w[1] ^ b.w[1], a.w[2] ^ b.w[2], a.w[3] ^ b.w[3]);
+}
+__host__ __device__ __forceinline__ bool operator==(const u256 &a, const u256 &b) {
+    return ((a.w[0] ^ b.w[0]) | (a.w[1] ^ b.w[1]) | (a.w[2] ^ b.w[2]) | (a.w[3] ^ b.w[3])) == 0;
+}
+__host__ __device__ __forceinline__ bool operator!=(const u256 &a, const u256 &b) { return !(a == b); }
+__host__ __device__ __forceinline__ bool operator<(const u256 &a, const u256 &b) {
+    if (a.w[3] != b.w[3]) return a.w[3] < b.w[3];
+    if (a.w[2] != b.w[2]) return a.w[2] < b.w[2];
+    if (a.w[1] != b.w[1]) return a.w[1] < b.w[1];
+    return a.w[0] < b.w[0];
+}
+__host__ __device__ __forceinline__ bool operator<=(const u256 &a, const u256 &b) { return !(b < a); }
+__host__ __device__ __forceinline__ bool operator>(const u256 &a, const u256 &b) { return b < a; }
+// shifts by 0 <= n < 256 bits
+__host__ __device__ __forceinline__ u256 operator>>(const u256 &a, int n) {
+    const int q = n >> 6, r = n & 63;
+    u256 o(0);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = i + q;
+        uint64_t v = j < 4 ? a.w[j] >> r : 0;
+        if (r && j + 1 < 4) v |= a.w[j + 1] << (64 - r);
+        o.w[i] = v;
+    }
+    return o;
+}
+__host__ __device__ __forceinline__ u256 operator<<(const u256 &a, int n) {
+    const int q = n >> 6, r = n & 63;
+    u256 o(0);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = i - q;
+        uint64_t v = j >= 0 ? a.w[j] << r : 0;
+        if (r && j - 1 >= 0) v |= a.w[j - 1] >> (64 - r);
+        o.w[i] = v;
+    }
+    return o;
+}
+
+__host__ __device__ __forceinline__ u256 &operator|=(u256 &a, const u256 &b) { return a = a | b; }
+__host__ __device__ __forceinline__ u256 &operator&=(u256 &a, const u256 &b) { return a = a & b; }
+__host__ __device__ __forceinline__ u256 &operator>>=(u256 &a, int n) { return a = a >> n; }
+__host__ __device__ __forceinline__ u256 &operator<<=(u256 &a, int n) { return a = a << n; }
+
+constexpr uint64_t kU256Claim = 0xfffffffffffffffeull;  // w[3] of a slot whose key is being written
+
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <>
+struct KeyOps<u256> {
+    static constexpr int kMaxK = 127;
+    __device__ static __forceinline__ u256 empty() { return u256(~0ull, ~0ull, ~0ull, ~0ull); }
+    __device__ static __forceinline__ uint32_t hash(const u256 &x) {
+        const uint64_t f = mix64(x.w[0] ^ mix64(x.w[1] ^ mix64(x.w[2] ^ mix64(x.w[3]))));
+        return (uint32_t)(f >> 32);
+    }
+    // the 128-base reverse complement is the rc of the four 32-base words in reverse order
+    __device__ static __forceinline__ u256 rc(const u256 &v, int k) {
+        const u256 r(rc_packed(v.w[3], 32), rc_packed(v.w[2], 32), rc_packed(v.w[1], 32), rc_packed(v.w[0], 32));
+        return r >> (2 * (128 - k));
+    }
+    __device__ static __forceinline__ u256 mask(int k) {
+        u256 m(0);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int bits = 2 * k - 64 * i;
+            m.w[i] = bits >= 64 ? ~0ull : bits > 0 ? ((1ull << bits) - 1) : 0ull;
+        }
+        return m;
+    }
+    // k bases starting at base p of the packed text (up to five words)
+    __device__ static __forceinline__ u256 load(const uint64_t *__restrict__ packed, uint64_t p, int k) {
+        const uint64_t w = p >> 5;
+        const uint32_t sh = (uint32_t)(p & 31) * 2u;
+        const uint32_t need = sh + 2u * (uint32_t)k;  // bits used from word w on
+        u256 o(0);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            if (64u * (uint32_t)i >= need) break;
+            uint64_t v = packed[w + i] >> sh;
+            if (sh && 64u * (uint32_t)(i + 1) < need) v |= packed[w + i + 1] << (64u - sh);
+            o.w[i] = v;
+        }
+        return o & mask(k);
+    }
+    __device__ static __forceinline__ void store(uint64_t *arr, uint64_t i, const u256 &key) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) arr[4 * i + j] = key.w[j];
+    }
+};
+
+// Find-or-insert of `key` at one slot of an open-addressing key array: 1 when the slot holds
+// key (*created when this call wrote it), 0 when it holds another key, -1 when a bounded wait
+// for another thread's write gave up.  Keys of one or two words are claimed by one
+// compare-and-swap.
+template <typename KT>
+__device__ __forceinline__ int slot_claim(KT *slot, const KT &key, bool &created) {
+    const KT kk = *slot;
+    if (kk == key) return 1;
+    if (kk == KeyOps<KT>::empty()) {
+        const KT old = KeyOps<KT>::cas(slot, KeyOps<KT>::empty(), key);
+        if (old == KeyOps<KT>::empty()) {
+            created = true;
+            return 1;
+        }
+        if (old == key) return 1;
+    }
+    return 0;
+}
+// Four-word keys: the writer claims the slot by a compare-and-swap of w[3] from empty to
+// kU256Claim, stores w[0..2], and releases w[3] = key.w[3] after a fence; readers acquire w[3]
+// and wait (bounded) while it reads kU256Claim.
+template <>
+__device__ __forceinline__ int slot_claim<u256>(u256 *slot, const u256 &key, bool &created) {
+    uint64_t w3 = ld_acquire_u64(&slot->w[3]);
+    for (int spin = 0;; spin++) {
+        if (w3 == ~0ull) {
+            const unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long *>(&slot->w[3]), ~0ull,
+                                                      (unsigned long long)kU256Claim);
+            if (prev == ~0ull) {
+                volatile uint64_t *vw = slot->w;
+                vw[0] = key.w[0];
+                vw[1] = key.w[1];
+                vw[2] = key.w[2];
+                __threadfence();
+                atomicExch(reinterpret_cast<unsigned long long *>(&slot->w[3]), (unsigned long long)key.w[3]);
+                created = true;
+                return 1;
+            }
+            w3 = prev;
+        }
+        if (w3 != kU256Claim) break;
+        if (spin >= (1 << 20)) return -1;
+        __nanosleep(32);
+        w3 = ld_acquire_u64(&slot->w[3]);
+    }
+    if (w3 != key.w[3]) return 0;
+    const volatile uint64_t *vw = slot->w;
+    return (vw[0] == key.w[0] && vw[1] == key.w[1] && vw[2] == key.w[2]) ? 1 : 0;
+}
+
 // Superkmer record of the device bucket store (16 bytes):
 //   w0 = start (40 bits) | len << 40 (24 bits)
 //   w1 = bucket (16) | second_bucket << 16 (8) | flags << 24 (2) | rc << 26 (1)
@@ -152,6 +319,7 @@ enum : unsigned {
     kStatusWalkLimit = 8u,      // a unitig walk exceeded its bound (internal error)
     kStatusLookback = 16u,      // bucketing needed more than the maximum lookback (internal error)
     kStatusStageOverflow = 32u, // staging array of the bucket store too small (host retries)
+    kStatusWaitLimit = 64u,     // a bounded wait for another thread's table slot gave up (internal error)
 };
 
 }  // namespace ggcat

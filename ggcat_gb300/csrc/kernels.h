@@ -73,7 +73,7 @@ struct MergeArgs {
     int k;
     int min_mult;
     int keep_kmers;
-    int wide;  // 0: u64 keys (k <= 32); 1: u128 keys (k <= 64)
+    int wide;  // key words as a power of two: 0 u64 (k <= 32), 1 u128 (k <= 64), 2 u256 (k <= 127)
     int forward;  // 1: forward-only build (k-mers keyed and extended as read, not canonicalised)
     // per-CTA global scratch of the extension phase for units with more survivors than the
     // shared-memory arrays hold (CTA i uses ext_scratch + i * ext_stride, up to ext_cap survivors)
@@ -84,7 +84,7 @@ struct MergeArgs {
 };
 
 // bytes of extension scratch per survivor (keys of key_bytes, 2 oriented nodes of 30 bytes)
-inline uint64_t merge_ext_bytes_per_survivor(int wide) { return (wide ? 16 : 8) + 60; }
+inline uint64_t merge_ext_bytes_per_survivor(int wide) { return (8u << wide) + 60; }
 // survivors per CTA the extension scratch is sized for: S and W tiers / M tier
 constexpr uint32_t kExtCapShared = 16384;
 constexpr uint32_t kExtCapMedium = 1u << 18;

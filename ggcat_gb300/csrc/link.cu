@@ -58,17 +58,15 @@ __global__ void __launch_bounds__(256) link_endpoints_kernel(const uint8_t *__re
         uint64_t slot = K::hash(key) & mask;
         uint32_t found = kNoNode;
         for (uint64_t probe = 0; probe <= mask; probe++) {
-            const KT kk = keys[slot];
-            if (kk == key) {
+            bool created = false;
+            const int r = slot_claim(&keys[slot], key, created);
+            if (r > 0) {
                 found = (uint32_t)slot;
                 break;
             }
-            if (kk == K::empty()) {
-                const KT old = K::cas(&keys[slot], K::empty(), key);
-                if (old == K::empty() || old == key) {
-                    found = (uint32_t)slot;
-                    break;
-                }
+            if (r < 0) {
+                atomicOr(status, kStatusWaitLimit);
+                break;
             }
             slot = (slot + 1) & mask;
         }
@@ -305,7 +303,10 @@ int launch_link_endpoints(const uint8_t *bases, const uint64_t *off, const uint3
                           uint64_t n, int k, int fwd, void *keys, uint32_t *min1, uint64_t mask, uint32_t *eslot,
                           unsigned *status, int sms, cudaStream_t s) {
     if (n == 0) return 0;
-    if (k > 32)
+    if (k > 64)
+        link_endpoints_kernel<u256><<<grid_for(2 * n, sms), 256, 0, s>>>(
+            bases, off, len, flags, n, k, fwd, static_cast<u256 *>(keys), min1, mask, eslot, status);
+    else if (k > 32)
         link_endpoints_kernel<u128><<<grid_for(2 * n, sms), 256, 0, s>>>(
             bases, off, len, flags, n, k, fwd, static_cast<u128 *>(keys), min1, mask, eslot, status);
     else

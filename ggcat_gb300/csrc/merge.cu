@@ -50,15 +50,17 @@ __device__ __forceinline__ int64_t tfind(const Table<KT> &t, KT key) {
     return -1;
 }
 
+// find-or-insert; created reports whether this call made the entry
 template <typename KT>
-__device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned *status) {
+__device__ __forceinline__ int64_t tinsert_created(const Table<KT> &t, KT key, unsigned *status, bool &created) {
     uint32_t s = slot_of(key, t.cap);
+    created = false;
     for (uint32_t probe = 0; probe < t.cap; probe++) {
-        const KT kk = t.keys[s];
-        if (kk == key) return s;
-        if (kk == KeyOps<KT>::empty()) {
-            const KT old = KeyOps<KT>::cas(&t.keys[s], KeyOps<KT>::empty(), key);
-            if (old == KeyOps<KT>::empty() || old == key) return s;
+        const int r = slot_claim(&t.keys[s], key, created);
+        if (r > 0) return s;
+        if (r < 0) {
+            atomicOr(status, kStatusWaitLimit);
+            return -1;
         }
         s = next_slot(s, t.cap);
     }
@@ -66,26 +68,10 @@ __device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned 
     return -1;
 }
 
-// tinsert that also reports whether this call created the entry
 template <typename KT>
-__device__ __forceinline__ int64_t tinsert_created(const Table<KT> &t, KT key, unsigned *status, bool &created) {
-    uint32_t s = slot_of(key, t.cap);
-    created = false;
-    for (uint32_t probe = 0; probe < t.cap; probe++) {
-        const KT kk = t.keys[s];
-        if (kk == key) return s;
-        if (kk == KeyOps<KT>::empty()) {
-            const KT old = KeyOps<KT>::cas(&t.keys[s], KeyOps<KT>::empty(), key);
-            if (old == KeyOps<KT>::empty()) {
-                created = true;
-                return s;
-            }
-            if (old == key) return s;
-        }
-        s = next_slot(s, t.cap);
-    }
-    atomicOr(status, kStatusTableFull);
-    return -1;
+__device__ __forceinline__ int64_t tinsert(const Table<KT> &t, KT key, unsigned *status) {
+    bool created;
+    return tinsert_created(t, key, status, created);
 }
 
 // Shared-memory forms of the table operations (explicit state space: the table pointers reach
@@ -104,6 +90,11 @@ __device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
 __device__ __forceinline__ uint64_t cas_shared_u64(uint32_t a, uint64_t cmp, uint64_t val) {
     uint64_t o;
     asm volatile("atom.shared.cas.b64 %0, [%1], %2, %3;" : "=l"(o) : "r"(a), "l"(cmp), "l"(val) : "memory");
+    return o;
+}
+__device__ __forceinline__ uint32_t cas_shared_u32(uint32_t a, uint32_t cmp, uint32_t val) {
+    uint32_t o;
+    asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "r"(a), "r"(cmp), "r"(val) : "memory");
     return o;
 }
 __device__ __forceinline__ void red_shared_add_u32(uint32_t a, uint32_t x) {
@@ -577,6 +568,11 @@ template <>
 struct TierCfg<u128, kTierM> {
     static constexpr int NT = 512, kSlots = 0, kSurv = 1536, kMinBlocks = 2;
 };
+// k > 64: every unit runs in this tier (or the grid-wide L kernels)
+template <>
+struct TierCfg<u256, kTierM> {
+    static constexpr int NT = 512, kSlots = 0, kSurv = 1536, kMinBlocks = 1;
+};
 constexpr uint16_t kNone16 = 0xffff, kMulti16 = 0xfffe;
 
 template <int N>
@@ -594,9 +590,12 @@ struct SmemTableView {
 };
 
 // packed words staged per record in the insert phase (records spanning more read global
-// memory): k <= 32 superkmers are short; k > 32 superkmers of long reads often span 5-6 words
+// memory): k <= 32 superkmers are short; k > 32 superkmers of long reads often span 5-6 words,
+// k > 64 ones up to 8
 template <typename KT>
-constexpr int stage_words() { return std::is_same<KT, uint64_t>::value ? 4 : 6; }
+constexpr int stage_words() {
+    return std::is_same<KT, uint64_t>::value ? 4 : std::is_same<KT, u128>::value ? 6 : 8;
+}
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // block-shared scalars of the extension phase
@@ -637,7 +636,8 @@ struct UnitSmem<KT, kTier, false> : UnitSmemCommon<KT, TierCfg<KT, kTier>::kSurv
 };
 static_assert(sizeof(UnitSmem<uint64_t, kTierW>) <= 227 * 1024 && sizeof(UnitSmem<u128, kTierW>) <= 227 * 1024 &&
                   sizeof(UnitSmem<uint64_t, kTierM>) <= 227 * 1024 && sizeof(UnitSmem<u128, kTierM>) <= 227 * 1024 &&
-                  2 * sizeof(UnitSmem<uint64_t, kTierS>) <= 227 * 1024 && 2 * sizeof(UnitSmem<u128, kTierS>) <= 227 * 1024,
+                  2 * sizeof(UnitSmem<uint64_t, kTierS>) <= 227 * 1024 && 2 * sizeof(UnitSmem<u128, kTierS>) <= 227 * 1024 &&
+                  sizeof(UnitSmem<u256, kTierM>) <= 227 * 1024,
               "shared memory of a merge CTA");
 // a shared-memory table never holds more survivors than the extension scratch of its CTA
 static_assert(TierCfg<uint64_t, kTierS>::kSlots <= (int)kExtCapShared && TierCfg<uint64_t, kTierW>::kSlots <= (int)kExtCapShared &&
@@ -891,6 +891,71 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
     //      A node u -> w is traversable iff u's right side and w's left side are no bucket
     //      boundary, w is u's only successor, u is w's only predecessor (the mirror of w has
     //      one successor) and w is another k-mer. ----
+    bool adj = false;
+    if constexpr (kSharedTable && std::is_same<KT, uint64_t>::value)
+        adj = !fwd && nn < (1u << 14) && 20u * ns <= 7u * t.cap;
+    if constexpr (kSharedTable && std::is_same<KT, uint64_t>::value) {
+        if (adj) {
+            // The k-mer table is dead once the survivors are numbered: its slots become a table
+            // of (k-1)-mers.  Node v's successors are the nodes whose first k-1 bases are v's
+            // last k-1 bases.  Every survivor enters the canonical form of the first k-1 bases
+            // of each of its nodes, with the orientation in which they match; a slot's value
+            // word keeps per orientation a count (0, 1, 2 = more) and the last node, so one
+            // lookup per node gives its unique successor or its degree.  An rc-symmetric
+            // k-mer enters its odd node only (edges into it reach that node).
+            const uint32_t vb = smem_addr(t.vals);
+            for (uint32_t i = threadIdx.x; i < t.cap; i += NT) {
+                t.keys[i] = ~0ull;
+                t.vals[i] = 0u;
+            }
+            __syncthreads();
+            const int k1 = k - 1;
+            const uint64_t m1 = kmer_mask(k1);
+            for (uint32_t i = threadIdx.x; i < ns; i += NT) {
+                const uint64_t x = A.sk[i];
+                const uint64_t rx = rc_packed(x, k);
+                for (uint32_t side = (!(k & 1) && x == rx) ? 1u : 0u; side < 2; side++) {
+                    const uint64_t pre = (side ? rx : x) & m1;
+                    const uint64_t rpre = rc_packed(pre, k1);
+                    const uint64_t key = pre < rpre ? pre : rpre;
+                    const uint32_t ori = pre == key ? 1u : 0u;
+                    bool created;
+                    const int64_t sl = tinsert_shared(t, key, o.status, created);
+                    if (sl < 0) continue;
+                    const uint32_t a = vb + 4u * (uint32_t)sl;
+                    uint32_t old = lds_u32(a);
+                    for (;;) {
+                        const uint32_t c = (old >> (2 * ori)) & 3u;
+                        uint32_t nv = (old & ~(3u << (2 * ori))) | ((c < 2u ? c + 1u : 2u) << (2 * ori));
+                        nv = (nv & ~(0x3fffu << (4 + 14 * ori))) | ((2u * i + side) << (4 + 14 * ori));
+                        const uint32_t seen = cas_shared_u32(a, old, nv);
+                        if (seen == old) break;
+                        old = seen;
+                    }
+                }
+            }
+            __syncthreads();
+            for (uint32_t u = threadIdx.x; u < nn; u += NT) {
+                const uint64_t x = A.sk[u >> 1];
+                const uint64_t rx = rc_packed(x, k);
+                const uint64_t sfx = ((u & 1) ? rx : x) >> 2;
+                const uint64_t rsfx = rc_packed(sfx, k1);
+                const uint64_t key = sfx < rsfx ? sfx : rsfx;
+                const uint32_t ori = sfx == key ? 1u : 0u;
+                const int64_t sl = tfind(t, key);
+                IT code = kNone;
+                if (sl >= 0) {
+                    const uint32_t w = t.vals[sl];
+                    const uint32_t c = (w >> (2 * ori)) & 3u;
+                    if (c == 1u) code = (IT)((w >> (4 + 14 * ori)) & 0x3fffu);
+                    else if (c >= 2u) code = kMulti;
+                }
+                if ((u & 1) && x == rx) code = kNone;  // rc-symmetric k-mer: its odd node ends paths
+                A.succ[u] = code;
+            }
+        }
+    }
+    if (!adj)
     for (uint32_t u = threadIdx.x; u < nn; u += NT) {
         const KT x = A.sk[u >> 1];
         const KT rx = K::rc(x, k);
@@ -1449,9 +1514,10 @@ static cudaError_t merge_attr_t() {
 }
 
 cudaError_t merge_configure() {
-    const cudaError_t e[6] = {merge_attr_t<uint64_t, kTierS>(), merge_attr_t<uint64_t, kTierW>(),
+    const cudaError_t e[7] = {merge_attr_t<uint64_t, kTierS>(), merge_attr_t<uint64_t, kTierW>(),
                               merge_attr_t<uint64_t, kTierM>(), merge_attr_t<u128, kTierS>(),
-                              merge_attr_t<u128, kTierW>(),     merge_attr_t<u128, kTierM>()};
+                              merge_attr_t<u128, kTierW>(),     merge_attr_t<u128, kTierM>(),
+                              merge_attr_t<u256, kTierM>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -1459,7 +1525,10 @@ cudaError_t merge_configure() {
 
 int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters, void *keys,
                         uint32_t *vals, uint8_t *vis, uint32_t *list, const MergeOut &o, int sms, cudaStream_t s) {
-    if (a.wide)
+    if (a.wide == 2)
+        merge_tier_t<u256, kTierM>(a, units, counters, static_cast<u256 *>(keys), vals, vis, list, nullptr, 0, o, sms,
+                                   s);
+    else if (a.wide)
         merge_tier_t<u128, kTierM>(a, units, counters, static_cast<u128 *>(keys), vals, vis, list, nullptr, 0, o, sms,
                                    s);
     else
@@ -1470,6 +1539,7 @@ int launch_merge_medium(const MergeArgs &a, const MergeUnit *units, const unsign
 
 int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                        const MergeOut &o, int sms, cudaStream_t s) {
+    if (a.wide == 2) return 0;  // k > 64: no shared-memory tiers
     if (a.wide)
         merge_tier_t<u128, kTierS>(a, units, counters, nullptr, nullptr, nullptr, nullptr, nullptr, 0, o, sms, s);
     else
@@ -1479,6 +1549,7 @@ int launch_merge_small(const MergeArgs &a, const MergeUnit *units, const unsigne
 
 int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned long long *counters,
                       MergeUnit *spill, uint64_t max_units, const MergeOut &o, int sms, cudaStream_t s) {
+    if (a.wide == 2) return 0;
     if (a.wide)
         merge_tier_t<u128, kTierW>(a, units, counters, nullptr, nullptr, nullptr, nullptr, spill, max_units, o, sms, s);
     else
@@ -1488,6 +1559,7 @@ int launch_merge_wide(const MergeArgs &a, const MergeUnit *units, const unsigned
 }
 
 int merge_ctas_per_sm(int tier, int wide) {
+    if (wide == 2) return TierCfg<u256, kTierM>::kMinBlocks;
     if (wide)
         return tier == 0 ? TierCfg<u128, kTierS>::kMinBlocks
                          : tier == 1 ? TierCfg<u128, kTierW>::kMinBlocks : TierCfg<u128, kTierM>::kMinBlocks;
@@ -1495,18 +1567,20 @@ int merge_ctas_per_sm(int tier, int wide) {
                      : tier == 1 ? TierCfg<uint64_t, kTierW>::kMinBlocks : TierCfg<uint64_t, kTierM>::kMinBlocks;
 }
 
-uint64_t merge_wide_limit(int wide) { return wide ? 16384 : 65536; }
+uint64_t merge_wide_limit(int wide) { return wide == 2 ? 0 : wide ? 16384 : 65536; }
 
 uint64_t merge_small_limit(int wide) {
     // instances of an S unit, so that its table (Tier slots) stays at load <= 0.8
     static_assert(3200 * 5 <= TierCfg<uint64_t, kTierS>::kSlots * 4 && 1600 * 5 <= TierCfg<u128, kTierS>::kSlots * 4,
                   "S table load");
-    return wide ? 1600 : 3200;
+    return wide == 2 ? 0 : wide ? 1600 : 3200;
 }
 
 int launch_init_tables(void *keys, int wide, uint32_t *vals, uint8_t *vis, uint64_t slots, int sms, cudaStream_t s) {
     if (slots == 0) return 0;
-    if (wide)
+    if (wide == 2)
+        init_tables_kernel<u256><<<sms * 4, 256, 0, s>>>(static_cast<u256 *>(keys), vals, vis, slots);
+    else if (wide)
         init_tables_kernel<u128><<<sms * 4, 256, 0, s>>>(static_cast<u128 *>(keys), vals, vis, slots);
     else
         init_tables_kernel<uint64_t><<<sms * 4, 256, 0, s>>>(static_cast<uint64_t *>(keys), vals, vis, slots);
@@ -1515,7 +1589,9 @@ int launch_init_tables(void *keys, int wide, uint32_t *vals, uint8_t *vis, uint6
 
 int launch_init_unit_tables(const MergeUnit *units, const unsigned long long *n_units_dev, void *keys, int wide,
                             uint32_t *vals, uint8_t *vis, int sms, cudaStream_t s) {
-    if (wide)
+    if (wide == 2)
+        init_unit_tables_kernel<u256><<<sms * 4, 256, 0, s>>>(units, n_units_dev, static_cast<u256 *>(keys), vals, vis);
+    else if (wide)
         init_unit_tables_kernel<u128><<<sms * 4, 256, 0, s>>>(units, n_units_dev, static_cast<u128 *>(keys), vals, vis);
     else
         init_unit_tables_kernel<uint64_t>
@@ -1535,7 +1611,9 @@ int launch_merge_large(const MergeArgs &a, const MergeUnit *units, const unsigne
                        uint64_t n_units_host_hint, void *keys, uint32_t *vals, uint8_t *vis, const MergeOut &o,
                        int sms, cudaStream_t s) {
     (void)n_units_host_hint;
-    if (a.wide)
+    if (a.wide == 2)
+        merge_large_t<u256>(a, units, n_units_dev, static_cast<u256 *>(keys), vals, vis, o, sms, s);
+    else if (a.wide)
         merge_large_t<u128>(a, units, n_units_dev, static_cast<u128 *>(keys), vals, vis, o, sms, s);
     else
         merge_large_t<uint64_t>(a, units, n_units_dev, static_cast<uint64_t *>(keys), vals, vis, o, sms, s);

@@ -40,9 +40,11 @@ extern "C" {
 typedef struct ggcat_gpu_ctx ggcat_gpu_ctx;
 
 typedef struct {
-    int32_t k;                /* k-mer length <= 64 (u64 keys for k <= 32, u128 keys above), odd or even;
-                                 forward-only merges exclude k = 32 and 64 (their all-G k-mer is the
-                                 tables' empty key) */
+    int32_t k;                /* k-mer length <= 127, odd or even: merge tables keyed by the canonical packed
+                                 k-mer in one word (k <= 32), two (k <= 64) or four (k > 64, global-memory
+                                 tables only; the Rabin-Karp hash_kind, as the reference requires above 64;
+                                 colours, queries and unitig links stop at 64); forward-only merges exclude
+                                 k = 32 and 64 (their all-G k-mer is the tables' empty key) */
     int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
     int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
     int32_t second_bits;      /* second-level bucket bits reported in superkmer records */

@@ -28,8 +28,8 @@ def _digest(*arrays) -> str:
 
 def device_kmers(keys: np.ndarray, mult: np.ndarray):
     """Sorted unique (lo, hi, mult) of the device k-mer dump.  ``keys`` is (n,) u64 for
-    k <= 32 or (n, 2) u64 (lo, hi) above.  Returns also whether every copy of a k-mer
-    (one per sub-bucket) carries the same multiplicity."""
+    k <= 32 or (n, 2) u64 (lo, hi) above (see ``compare_kmers_wide`` for k > 64).  Returns
+    also whether every copy of a k-mer (one per sub-bucket) carries the same multiplicity."""
     keys = np.asarray(keys)
     mult = np.asarray(mult).astype(np.uint64)
     if keys.ndim == 1:
@@ -60,6 +60,22 @@ def compare_kmers(keys, mult, oracle_result) -> dict:
         (glo == olo).all() and (ghi == ohi).all() and (gm == om).all())
     return {"equal": bool(equal), "kmers_gpu": int(glo.size), "kmers_oracle": int(olo.size),
             "digest_gpu": _digest(glo, ghi, gm), "digest_oracle": _digest(olo, ohi, om)}
+
+
+def compare_kmers_wide(keys, mult, oracle_result) -> dict:
+    """k > 64: the device dump ((n, 4) words) against the oracle's wide k-mers, both reduced
+    to sorted unique rows of (w3, w2, w1, w0, mult); every copy of a k-mer must agree."""
+    keys = np.asarray(keys, np.uint64).reshape(-1, 4)
+    mult = np.asarray(mult).astype(np.uint64)
+    rows = np.column_stack([keys[:, 3], keys[:, 2], keys[:, 1], keys[:, 0], mult])
+    rows = np.unique(rows, axis=0)
+    keys_only = rows[:, :4]
+    consistent = keys_only.shape[0] == 0 or bool((keys_only[1:] != keys_only[:-1]).any(axis=1).all())
+    ow, om = oracle_result.kmers_wide()
+    orows = np.unique(np.column_stack([ow[:, 3], ow[:, 2], ow[:, 1], ow[:, 0], om.astype(np.uint64)]), axis=0)
+    equal = consistent and rows.shape == orows.shape and bool((rows == orows).all())
+    return {"equal": bool(equal), "kmers_gpu": int(rows.shape[0]), "kmers_oracle": int(orows.shape[0]),
+            "digest_gpu": _digest(rows), "digest_oracle": _digest(orows)}
 
 
 def compare_unitigs(canonical_gpu_lines: bytes, oracle_result) -> dict:
