@@ -72,6 +72,7 @@ class Stats(C.Structure):
         ("spill_ranges", C.c_uint64),
         ("spill_bytes", C.c_uint64),
         ("ms_tier", C.c_double * 4),
+        ("colors_collected", C.c_uint64),
     ]
 
 
@@ -116,6 +117,7 @@ EXPORTED = [
     "ggcat_gpu_build_from_files",
     "ggcat_gpu_build_from_files_ex",
     "ggcat_gpu_colors",
+    "ggcat_gpu_colors_prepare",
     "ggcat_gpu_kmer_subsets_copy",
     "ggcat_gpu_subsets_copy",
     "ggcat_gpu_query_index",
@@ -208,6 +210,7 @@ def load(build: bool = True):
     L.ggcat_gpu_bucket_histogram_noalloc.argtypes = [P, u64, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
     L.ggcat_gpu_kmer_hashes.argtypes = [P, P, u64, C.c_int, C.c_int, P, P]
     L.ggcat_gpu_colors.argtypes = [P, P, P, u64, C.c_uint32, P]
+    L.ggcat_gpu_colors_prepare.argtypes = [P, P, P, u64, C.c_uint32]
     L.ggcat_gpu_kmer_subsets_copy.argtypes = [P, P, u64, pu64]
     L.ggcat_gpu_subsets_copy.argtypes = [P, P, u64, pu64, C.POINTER(C.c_uint32)]
     L.ggcat_gpu_query_index.argtypes = [P, P, u64, C.c_int, P]
@@ -349,6 +352,13 @@ class GpuContext:
                                                  C.c_void_p(d_out_ptr), C.c_void_p(stream)), "kmer_hashes")
 
     # ---- colours ----
+    def colors_prepare(self, seq_off, seq_color, n_colors: int):
+        """Announces the colour table of the next build, so that its merge collects the colours."""
+        off = np.ascontiguousarray(seq_off, np.uint64)
+        col = np.ascontiguousarray(seq_color, np.uint32)
+        self._check(self.L.ggcat_gpu_colors_prepare(self.h, _ptr(off), _ptr(col), off.size, n_colors),
+                    "colors_prepare")
+
     def colors(self, seq_off, seq_color, n_colors: int, stream: int = 0):
         so = np.ascontiguousarray(seq_off, np.uint64)
         sc = np.ascontiguousarray(seq_color, np.uint32)

@@ -438,15 +438,35 @@ __global__ void __launch_bounds__(256) partition_kernel(const SkRec *__restrict_
         begin = (uint64_t)n_regions * region_cap + s0;
         end = (uint64_t)n_regions * region_cap + min(used, s0 + kOvfSlice);
     }
-    for (uint64_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
-        const SkRec r = stage[i];
-        const uint64_t bin = ((uint64_t)rec_bucket(r) << fbits) | ((r.w1 >> 48) & 0xffffull);
-        const unsigned long long slot = bin_off[bin] + atomicAdd(&bin_cursor[bin], 1u);
-        if (slot >= bin_off[bin + 1]) {
-            atomicOr(status, kStatusLookback);
-            continue;
+    // four records per thread in flight: their cursor atomics and offset loads are independent,
+    // so one round trip to L2 serves four scatters
+    constexpr int kIlp = 4;
+    for (uint64_t i0 = begin + threadIdx.x; i0 < end; i0 += kIlp * blockDim.x) {
+        SkRec r[kIlp];
+        uint64_t bin[kIlp];
+        unsigned long long slot[kIlp], lim[kIlp];
+#pragma unroll
+        for (int q = 0; q < kIlp; q++) {
+            const uint64_t i = i0 + (uint64_t)q * blockDim.x;
+            if (i < end) r[q] = stage[i];
         }
-        recs[slot] = r;
+#pragma unroll
+        for (int q = 0; q < kIlp; q++) {
+            if (i0 + (uint64_t)q * blockDim.x >= end) continue;
+            bin[q] = ((uint64_t)rec_bucket(r[q]) << fbits) | ((r[q].w1 >> 48) & 0xffffull);
+            slot[q] = atomicAdd(&bin_cursor[bin[q]], 1u);
+            lim[q] = bin_off[bin[q] + 1];
+            slot[q] += bin_off[bin[q]];
+        }
+#pragma unroll
+        for (int q = 0; q < kIlp; q++) {
+            if (i0 + (uint64_t)q * blockDim.x >= end) continue;
+            if (slot[q] >= lim[q]) {
+                atomicOr(status, kStatusLookback);
+                continue;
+            }
+            recs[slot[q]] = r[q];
+        }
     }
 }
 

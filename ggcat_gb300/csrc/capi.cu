@@ -41,6 +41,11 @@ struct DevBuf {
         if (e == cudaSuccess) n = want;
         return e;
     }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
 };
 
 constexpr int kFeedPieces = 4;  // pieces of build_text's pipelined host text copy
@@ -114,8 +119,8 @@ struct HostUnitigs {
 // Everything the captured merge launches depend on: a replay is valid while all of it is
 // unchanged (zero-initialised with memset so padding compares equal).
 struct MergeGraphKey {
-    const void *ptr[24];
-    uint64_t val[24];
+    const void *ptr[32];
+    uint64_t val[32];
 };
 
 // device buffers of the link stage
@@ -167,6 +172,16 @@ struct ggcat_gpu_ctx {
     uint32_t c_colors = 0;
     int c_words = 0;
     bool have_colors = false;
+    // colours announced before the build (ggcat_gpu_colors_prepare): the merge collects them
+    bool cprep = false;
+    std::vector<uint64_t> cprep_off;
+    std::vector<uint32_t> cprep_col;
+    uint32_t cprep_colors = 0;
+    DevBuf<uint64_t> cprep_off_d;
+    DevBuf<uint32_t> cprep_col_d;
+    DevBuf<uint32_t> cbm_scratch;  // per merge CTA, one bitmap row per table slot
+    bool collect_now = false;      // this merge collects colours
+    bool merge_collected = false;  // the last merge collected every dumped k-mer's colours
 
     // merge
     DevBuf<MergeUnit> small_units, wide_units, medium_units, large_units, bucket_units;
@@ -713,6 +728,34 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     // and extend k-mers as read, without canonicalisation
     MergeArgs a{ctx->packed.p, ctx->recs.p, p->k, p->min_multiplicity, p->keep_kmers, wide, p->forward_only ? 1 : 0,
                 ctx->ext_scratch.p, stride_sw, kExtCapShared, 32};
+    if (ctx->collect_now) {
+        // colours collected by the merge: one bitmap row per table slot and CTA, sized for the
+        // largest table of the shared-memory tiers and of the M tier (units up to 2^18 instances)
+        const int words = (int)((ctx->cprep_colors + 31) / 32);
+        const uint32_t load = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : 80u;
+        uint64_t mcap = 64;
+        while (mcap < (1ull << 18) * 100 / load + 64) mcap <<= 1;
+        const uint64_t rows = std::max<uint64_t>(mcap, 11264);
+        const uint64_t ctas = (uint64_t)ctx->sms * 2;  // S and M: 2 CTAs per SM, W: 1
+        if (ctx->cbm_scratch.ensure(ctas * rows * (uint64_t)words) != cudaSuccess ||
+            ctx->cbitmaps.ensure((kmer_cap + 1) * (uint64_t)words) != cudaSuccess) {
+            cudaGetLastError();  // no room: the colour phase reads the text instead
+            ctx->cbm_scratch.release();
+            ctx->collect_now = false;
+        }
+    }
+    if (ctx->collect_now) {
+        const int words = (int)((ctx->cprep_colors + 31) / 32);
+        const uint64_t rows = ctx->cbm_scratch.n / ((uint64_t)ctx->sms * 2 * (uint64_t)words);
+        CK(cudaMemsetAsync(ctx->cbm_scratch.p, 0, ctx->cbm_scratch.n * sizeof(uint32_t), s));
+        a.seq_off = ctx->cprep_off_d.p;
+        a.seq_color = ctx->cprep_col_d.p;
+        a.n_seq = (uint32_t)ctx->cprep_off.size();
+        a.bm_words = words;
+        a.bm_scratch = ctx->cbm_scratch.p;
+        a.bm_stride = rows * (uint64_t)words;
+        a.bm_out = ctx->cbitmaps.p;
+    }
     // per-class insert batches of the shared-memory tiers
     MergeArgs a_small = a, a_wide = a;
     a_small.rec_batch = p->small_batch > 0 ? p->small_batch : 16;
@@ -807,7 +850,8 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                               ctx->kmer_mult.p,    ctx->counters.p,    ctx->status.p,       ctx->bin_off.p,
                               ctx->kmer_off.p,     ctx->small_units.p, ctx->wide_units.p,   ctx->medium_units.p,
                               ctx->large_units.p,  ctx->tkeys.p,       ctx->tvals.p,        ctx->tvis.p,
-                              ctx->tlist.p};
+                              ctx->tlist.p,        a.bm_scratch,       a.bm_out,            a.seq_off,
+                              a.seq_color};
         static_assert(sizeof(ptrs) / sizeof(ptrs[0]) <= sizeof(key.ptr) / sizeof(key.ptr[0]), "graph key");
         memcpy(key.ptr, ptrs, sizeof ptrs);
         const uint64_t vals[] = {(uint64_t)p->k,     (uint64_t)p->min_multiplicity, (uint64_t)p->keep_kmers,
@@ -816,7 +860,8 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                  target,             wide_limit,                    max_units,
                                  pool,               stride_sw,                     stride_m,
                                  (uint64_t)ctx->sms, small_limit,                   load_pct,
-                                 (uint64_t)a.forward, (uint64_t)a_small.rec_batch,  (uint64_t)a_wide.rec_batch};
+                                 (uint64_t)a.forward, (uint64_t)a_small.rec_batch,  (uint64_t)a_wide.rec_batch,
+                                 (uint64_t)a.bm_words, a.bm_stride,                 (uint64_t)a.n_seq};
         static_assert(sizeof(vals) / sizeof(vals[0]) <= sizeof(key.val) / sizeof(key.val[0]), "graph key");
         memcpy(key.val, vals, sizeof vals);
         if (!ctx->merge_exec || memcmp(&key, &ctx->merge_key, sizeof key) != 0) {
@@ -863,6 +908,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         ctx->stats.merge_units_spilled = cnt[kCntSpilled];
         ctx->stats.merge_units_ext_global = cnt[kCntExtGlobal];
         ctx->stats.merge_units_walk = cnt[kCntWalk] + cnt[kCntLarge];
+        // collected colours are complete unless a unit ran in the grid-wide L kernels or the
+        // walk fallback, which do not collect them
+        ctx->merge_collected = ctx->collect_now && cnt[kCntWalk] == 0 && cnt[kCntLarge] == 0;
         if (cnt[kCntSlots] > pool) return fail(ctx, GGCAT_GPU_EDEVICE, "table pool exceeded");
     }
     *st_out = st;
@@ -1049,6 +1097,11 @@ extern "C" int ggcat_gpu_merge(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, vo
     CK(cudaSetDevice(ctx->device));
     ctx->have_merge = false;
     ctx->partial_on_host = false;
+    ctx->merge_collected = false;
+    // colours announced before the build are collected by the batched, resident merge when its
+    // bitmap buffers can be allocated (else ggcat_gpu_colors reads them from the text)
+    ctx->collect_now = ctx->cprep && p->keep_kmers && p->k <= 64 && p->merge_mode == GGCAT_MERGE_BATCHED &&
+                       ctx->spill.empty() && !ctx->cprep_off.empty() && ctx->cprep_off.back() < ctx->n_text;
     rc = ctx->spill.empty() ? merge_retry(ctx, p, s) : merge_spill(ctx, p, s);
     if (rc) return rc;
     float ms = 0;
@@ -1595,15 +1648,18 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
     p.forward_only = forward_only;
     p.merge_mode = GGCAT_MERGE_BATCHED;
     p.keep_kmers = colors ? 1 : 0;
-    int rc = ggcat_gpu_build_text(ctx, text.data(), text.size(), &p, nullptr);
+    // colour i = input file i (MinBkSingleColor); announced so that the merge collects them
+    const uint64_t nc = colors && seq_off ? seq_off->size() : 0;
+    if (colors && (nc == 0 || nc > 65536))
+        return fail(ctx, GGCAT_GPU_EINVAL, "colours need 1 to 65536 inputs (%llu)", (unsigned long long)nc);
+    std::vector<uint32_t> col(nc);
+    for (uint64_t i = 0; i < nc; i++) col[i] = (uint32_t)i;
+    int rc = ggcat_gpu_colors_prepare(ctx, nc ? seq_off->data() : nullptr, col.data(), nc, (uint32_t)nc);
+    if (rc) return rc;
+    rc = ggcat_gpu_build_text(ctx, text.data(), text.size(), &p, nullptr);
     if (rc) return rc;
     std::vector<std::string> names;
     if (colors) {
-        const uint64_t nc = seq_off ? seq_off->size() : 0;
-        if (nc == 0 || nc > 65536) return fail(ctx, GGCAT_GPU_EINVAL, "colours need 1 to 65536 inputs (%llu)",
-                                               (unsigned long long)nc);
-        std::vector<uint32_t> col(nc);
-        for (uint64_t i = 0; i < nc; i++) col[i] = (uint32_t)i;
         rc = ggcat_gpu_colors(ctx, seq_off->data(), col.data(), nc, (uint32_t)nc, nullptr);
         if (rc) return rc;
         if (color_names) names = *color_names;
@@ -1702,6 +1758,31 @@ extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *con
 // ---------------------------------------------------------------------------
 // colour subsets
 // ---------------------------------------------------------------------------
+extern "C" int ggcat_gpu_colors_prepare(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, const uint32_t *h_seq_color,
+                                        uint64_t n_seq, uint32_t n_colors) {
+    if (!ctx) return GGCAT_GPU_EINVAL;
+    ctx->cprep = false;
+    if (n_seq == 0) return GGCAT_GPU_OK;  // withdraws an earlier announcement
+    if (!h_seq_off || !h_seq_color || n_colors == 0 || n_colors > 65536 || n_seq >= 0xffffffffull)
+        return fail(ctx, GGCAT_GPU_EINVAL, "bad colour table (n_seq=%llu, n_colors=%u)", (unsigned long long)n_seq,
+                    n_colors);
+    for (uint64_t i = 0; i < n_seq; i++) {
+        if (h_seq_color[i] >= n_colors) return fail(ctx, GGCAT_GPU_EINVAL, "colour out of range at sequence %llu",
+                                                    (unsigned long long)i);
+        if (i && h_seq_off[i] < h_seq_off[i - 1]) return fail(ctx, GGCAT_GPU_EINVAL, "sequence offsets not sorted");
+    }
+    CK(cudaSetDevice(ctx->device));
+    ctx->cprep_off.assign(h_seq_off, h_seq_off + n_seq);
+    ctx->cprep_col.assign(h_seq_color, h_seq_color + n_seq);
+    ctx->cprep_colors = n_colors;
+    CK(ctx->cprep_off_d.ensure(n_seq));
+    CK(ctx->cprep_col_d.ensure(n_seq));
+    CK(cudaMemcpy(ctx->cprep_off_d.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->cprep_col_d.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    ctx->cprep = true;
+    return GGCAT_GPU_OK;
+}
+
 extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, const uint32_t *h_seq_color,
                                 uint64_t n_seq, uint32_t n_colors, void *stream) {
     if (!ctx) return GGCAT_GPU_EINVAL;
@@ -1744,20 +1825,36 @@ extern "C" int ggcat_gpu_colors(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, c
     CK(ctx->ccounters.ensure(4));
     CK(ctx->cseq_off.ensure(n_seq));
     CK(ctx->cseq_color.ensure(n_seq));
-    CK(cudaMemcpyAsync(ctx->cseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->cseq_color.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    // the merge collected these colours (the same table was announced before the build): no
+    // pass over the text, the dumped copies' bitmaps are merged into their owners
+    const bool collected = ctx->merge_collected && ctx->cprep && ctx->cprep_colors == n_colors &&
+                           ctx->cprep_off.size() == n_seq &&
+                           std::equal(ctx->cprep_off.begin(), ctx->cprep_off.end(), h_seq_off) &&
+                           std::equal(ctx->cprep_col.begin(), ctx->cprep_col.end(), h_seq_color);
+    if (!collected) {
+        CK(cudaMemcpyAsync(ctx->cseq_off.p, h_seq_off, n_seq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->cseq_color.p, h_seq_color, n_seq * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(ctx->cbitmaps.p, 0, (nd + 1) * words * sizeof(uint32_t), s));
+    }
     CK(cudaMemsetAsync(ctx->cslots.p, 0xff, slot_words * cap * sizeof(uint64_t), s));
-    CK(cudaMemsetAsync(ctx->cbitmaps.p, 0, (nd + 1) * words * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->csub_hash.p, 0, scap * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->csub_state.p, 0, scap * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(ctx->ccounters.p, 0, 4 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->status.p + 1, 0, sizeof(unsigned), s));
-    ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
-                                        ctx->last_params.forward_only ? 0 : 1, wide, ctx->cseq_off.p, ctx->cseq_color.p,
-                                        n_seq, h_seq_off[0] == 0 ? max_len : 0, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
-                                        ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p, ctx->csub_arena.p,
-                                        scap - 1, ctx->cid_subset.p, ctx->cdump_subset.p, ctx->status.p + 1,
-                                        ctx->sms, s);
+    if (collected)
+        ctx->launches += launch_color_phase_collected(
+            ctx->kmer_keys.p, nd, wide, words, ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
+            ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p, ctx->csub_arena.p, scap - 1, ctx->cid_subset.p,
+            ctx->cdump_subset.p, ctx->status.p + 1, ctx->sms, s);
+    else
+        ctx->launches += launch_color_phase(ctx->kmer_keys.p, nd, ctx->last_text, ctx->n_text, ctx->last_params.k,
+                                            ctx->last_params.forward_only ? 0 : 1, wide, ctx->cseq_off.p,
+                                            ctx->cseq_color.p, n_seq, h_seq_off[0] == 0 ? max_len : 0, words,
+                                            ctx->cslots.p, cap - 1, ctx->cowner.p, ctx->cbitmaps.p,
+                                            ctx->ccounters.p + 1, ctx->csub_hash.p, ctx->csub_state.p,
+                                            ctx->csub_arena.p, scap - 1, ctx->cid_subset.p, ctx->cdump_subset.p,
+                                            ctx->status.p + 1, ctx->sms, s);
+    ctx->stats.colors_collected = collected ? 1 : 0;
     CK(cudaGetLastError());
     unsigned long long cnt[2];
     unsigned st = 0;

@@ -316,6 +316,23 @@ __global__ void color_subset_kernel(const uint32_t *__restrict__ bitmaps, uint64
     }
 }
 
+// Colours collected by the merge: every dumped copy of a k-mer holds the colours of the
+// occurrences its sub-bucket saw (its own sub-bucket sees all of them, a neighbouring one only
+// the occurrences where it is a superkmer's ignored end); the union goes to the owner's row,
+// and the other copies' rows are cleared so that they are holes for the subset pass.
+__global__ void color_union_copies_kernel(const uint32_t *__restrict__ owner, uint64_t n, int words,
+                                          uint32_t *bitmaps) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t o = owner[i];
+        if (o == i) continue;
+        for (int w = 0; w < words; w++) {
+            const uint32_t v = bitmaps[i * words + w];
+            if (v) atomicOr(&bitmaps[o * words + w], v);
+            bitmaps[i * words + w] = 0u;
+        }
+    }
+}
+
 // subset id of every dumped k-mer: a gather through its owner (almost always itself)
 __global__ void color_dump_subsets_kernel(const uint32_t *__restrict__ owner, uint64_t n,
                                           const uint32_t *__restrict__ id_subset, uint32_t *out) {
@@ -324,6 +341,23 @@ __global__ void color_dump_subsets_kernel(const uint32_t *__restrict__ owner, ui
 }
 
 // ---------------------------------------------------------------------------
+int launch_color_phase_collected(const uint64_t *dump, uint64_t n_dump, int wide, int words, uint64_t *slots,
+                                 uint64_t mask, uint32_t *owner, uint32_t *bitmaps, unsigned long long *sub_count,
+                                 unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena,
+                                 uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset, unsigned *status,
+                                 int sms, cudaStream_t s) {
+    if (!n_dump) return 0;
+    if (wide)
+        color_kmer_insert_kernel<u128><<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
+    else
+        color_kmer_insert_kernel<uint64_t><<<sms * 8, 256, 0, s>>>(dump, n_dump, slots, mask, owner, status);
+    color_union_copies_kernel<<<sms * 8, 256, 0, s>>>(owner, n_dump, words, bitmaps);
+    color_subset_kernel<<<sms * 8, 256, 0, s>>>(bitmaps, n_dump, words, sub_hash, sub_state, sub_arena, sub_mask,
+                                                sub_count, id_subset, status);
+    color_dump_subsets_kernel<<<sms * 8, 256, 0, s>>>(owner, n_dump, id_subset, dump_subset);
+    return 4;
+}
+
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
                        int canonical, int wide, const uint64_t *seq_off, const uint32_t *seq_color,
                        uint64_t n_seq, uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,

@@ -81,6 +81,18 @@ struct MergeArgs {
     uint64_t ext_stride;
     uint32_t ext_cap;
     int rec_batch;  // superkmer records per insert batch of a warp (1-32; shared-memory tiers)
+    // colours collected during the merge (bm_words = 0: off).  A superkmer's colour is that of
+    // the sequence holding its first base (seq_off ascending); every k-mer instance sets its
+    // colour's bit in the CTA's bitmap scratch (bm_stride words per CTA, bm_words per table
+    // slot), and the dense numbering moves a surviving k-mer's bitmap to bm_out at its dump
+    // index, leaving the scratch zero for the next unit
+    const uint64_t *seq_off = nullptr;
+    const uint32_t *seq_color = nullptr;
+    uint32_t n_seq = 0;
+    int bm_words = 0;
+    uint32_t *bm_scratch = nullptr;
+    uint64_t bm_stride = 0;
+    uint32_t *bm_out = nullptr;
 };
 
 // bytes of extension scratch per survivor (keys of key_bytes, 2 oriented nodes of 30 bytes)
@@ -201,6 +213,13 @@ int launch_kmer_hash(const uint8_t *text, uint64_t n, int k, int kind, uint64_t 
 // (wide ? 4 : 2) x (mask + 1) words ({key, id} slots, all-ones when empty); owner, id_subset,
 // dump_subset: n_dump entries; bitmaps: n_dump x words (zeroed); max_seq_len: the longest
 // sequence (seq_off[i + 1] - seq_off[i], the last one up to n_text), 0 when seq_off[0] > 0
+// the colour phase when the merge collected every dumped copy's colours (ggcat_gpu_colors_prepare):
+// k-mer table (owners), union of the copies into their owner, subset dedup, per-copy subset
+int launch_color_phase_collected(const uint64_t *dump, uint64_t n_dump, int wide, int words, uint64_t *slots,
+                                 uint64_t mask, uint32_t *owner, uint32_t *bitmaps, unsigned long long *sub_count,
+                                 unsigned long long *sub_hash, uint32_t *sub_state, uint32_t *sub_arena,
+                                 uint64_t sub_mask, uint32_t *id_subset, uint32_t *dump_subset, unsigned *status,
+                                 int sms, cudaStream_t s);
 int launch_color_phase(const uint64_t *dump, uint64_t n_dump, const uint8_t *text, uint64_t n_text, int k,
                        int canonical, int wide, const uint64_t *seq_off, const uint32_t *seq_color,
                        uint64_t n_seq, uint64_t max_seq_len, int words, uint64_t *slots, uint64_t mask, uint32_t *owner, uint32_t *bitmaps,

@@ -598,6 +598,19 @@ constexpr int stage_words() {
 }
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+// colour of the sequence holding text position pos (the last sequence starting at or before it)
+__device__ __forceinline__ uint32_t colour_at(const MergeArgs &a, uint64_t pos) {
+    uint32_t lo = 0, hi = a.n_seq;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.seq_off[mid] <= pos)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return a.seq_color[lo];
+}
+
 // block-shared scalars of the extension phase
 struct ExtShared {
     uint32_t n_surv, loc_bases, loc_count, ok;
@@ -828,7 +841,8 @@ template <typename KT, typename IT, int NT, int kRegJ, bool kGlobalArr, bool kSh
 __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *t_list, bool list_scan,
                                             uint32_t seg_lo, uint32_t seg_hi, uint32_t warp_base, uint32_t n_surv,
                                             const ExtArrays<KT, IT> &A, ExtShared &X, int k, uint32_t min_mult,
-                                            int keep_kmers, int fwd, const MergeOut &o) {
+                                            int keep_kmers, int fwd, const MergeOut &o, uint32_t *bm_cta = nullptr,
+                                            int bm_words = 0, uint32_t *bm_out = nullptr) {
     using K = KeyOps<KT>;
     constexpr IT kNone = (IT)~(IT)0;
     constexpr IT kMulti = (IT)(kNone - 1);
@@ -872,12 +886,17 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
                     if (di < o.kmer_cap) {
                         K::store(o.kmer_keys, di, key);
                         o.kmer_mult[di] = val_mult(v);
+                        if (bm_cta)  // the colours collected by the insert
+                            for (int w = 0; w < bm_words; w++)
+                                bm_out[di * (uint64_t)bm_words + w] = bm_cta[(uint64_t)sl * bm_words + w];
                     } else {
                         atomicOr(o.status, kStatusKmerOverflow);
                     }
                 }
             }
             if (ix < seg_hi) t.vals[sl] = alive ? (0x80000000u | ((v >> 30) << 28) | idx) : 0u;
+            if (bm_cta && ix < seg_hi && v != 0)  // the scratch stays zero for the next unit
+                for (int w = 0; w < bm_words; w++) bm_cta[(uint64_t)sl * bm_words + w] = 0u;
             base += __popc(bm);
         }
         if (threadIdx.x == 0) X.n_surv = n_surv;
@@ -1168,6 +1187,8 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
     const uint64_t n_units = counters_ro[kCount];
     const int k = a.k;
     const uint32_t min_mult = (uint32_t)a.min_mult;
+    // this CTA's colour bitmaps, one row of bm_words per table slot (colours collected here)
+    uint32_t *const bm_cta = a.bm_words ? a.bm_scratch + (uint64_t)blockIdx.x * a.bm_stride : nullptr;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kHead], 1ull);
@@ -1257,6 +1278,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                     const SkRec rr = a.recs[U.rec_begin + item];
                     w0 = rr.w0;
                     fr = rec_flags(rr) | (rec_rc(rr) << 2);
+                    if (bm_cta) fr |= colour_at(a, rec_start(rr)) << 4;  // bits 4-31: the record's colour
                     nk = rec_len(rr) - (uint32_t)k + 1;  // >= 1: records hold at least one k-mer
                     // stage the record's packed words in shared memory (one round of independent
                     // loads per 32 records instead of one dependent load per k-mer window)
@@ -1337,6 +1359,10 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                         }
                     }
                     if (sl < 0) continue;
+                    if (bm_cta) {
+                        const uint32_t col = rfr >> 4;
+                        atomicOr(bm_cta + (uint64_t)sl * a.bm_words + (col >> 5), 1u << (col & 31));
+                    }
                     if constexpr (!kGlobalTable) {
                         const uint32_t va = smem_addr(t.vals + sl);
                         if (fbits) red_shared_or_b32(va, fbits << 30);
@@ -1352,7 +1378,11 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
         }
         if (optimistic && S.distinct >= kOptLimit) {
             // too many distinct k-mers for the shared-memory table: the M tier redoes the
-            // unit with its reserved global table
+            // unit with its reserved global table (the colour scratch is left zero)
+            if (bm_cta)
+                for (uint32_t sl = threadIdx.x; sl < cap; sl += NT)
+                    if (t.keys[sl] != K::empty())
+                        for (int w = 0; w < a.bm_words; w++) bm_cta[(uint64_t)sl * a.bm_words + w] = 0u;
             if (threadIdx.x == 0) {
                 atomicAdd(&o.counters[kCntSpilled], 1ull);
                 const unsigned long long i = atomicAdd(&o.counters[kCntMedium], 1ull);
@@ -1393,7 +1423,8 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             ExtArrays<KT, uint16_t> A{S.sk,          S.succ,    S.bflag,      S.u.r.jump, S.u.r.rank,
                                       nullptr,       nullptr,   S.u.r.offs,   S.u.r.uidx, S.u.r.haspred};
             extend_unit<KT, uint16_t, NT, (kMaxSurv * 2 + NT - 1) / NT, false, !kGlobalTable>(
-                t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, a.forward, o);
+                t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x, k, min_mult, a.keep_kmers, a.forward, o,
+                bm_cta, a.bm_words, a.bm_out);
         } else if (a.ext_scratch != nullptr && n_surv <= a.ext_cap) {
             // more survivors than the shared-memory arrays hold: the same ranking on this
             // CTA's scratch in global memory
@@ -1401,7 +1432,8 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
             const ExtArrays<KT, uint32_t> A =
                 ext_global_arrays<KT>(a.ext_scratch + (size_t)blockIdx.x * a.ext_stride, a.ext_cap);
             extend_unit<KT, uint32_t, NT, 1, true, !kGlobalTable>(t, t_list, kGlobalTable, seg_lo, seg_hi, warp_base, n_surv, A, S.x,
-                                                  k, min_mult, a.keep_kmers, a.forward, o);
+                                                  k, min_mult, a.keep_kmers, a.forward, o, bm_cta, a.bm_words,
+                                                  a.bm_out);
         } else {
             // walk fallback (no scratch for this many survivors; a shared-memory table never has
             // more survivors than the scratch holds)
@@ -1412,6 +1444,11 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
                     extend_slot(g, sl, o, a.keep_kmers, min_mult);
                 __syncthreads();
                 for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x) cycle_slot(g, sl, o, min_mult);
+                // (these k-mers get no collected colours: the host falls back to the text pass)
+                if (bm_cta)
+                    for (uint32_t sl = threadIdx.x; sl < cap; sl += blockDim.x)
+                        if (t.keys[sl] != K::empty())
+                            for (int w = 0; w < a.bm_words; w++) bm_cta[(uint64_t)sl * a.bm_words + w] = 0u;
             } else {
                 if (threadIdx.x == 0) atomicOr(o.status, kStatusWalkLimit);
             }

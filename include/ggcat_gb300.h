@@ -114,6 +114,7 @@ typedef struct {
     uint64_t spill_bytes;       /* record bytes held in host memory */
     double ms_tier[4];          /* device time of each bucket-size class of the batched merge: S units,
                                    W units, M units (global tables), L units (grid-wide kernels) */
+    uint64_t colors_collected;  /* 1 when the last ggcat_gpu_colors used the colours collected by the merge */
 } ggcat_gpu_stats;
 
 /* ---- context ---- */
@@ -303,6 +304,18 @@ int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_f
                                   const char *output_file, const char *const *color_names, size_t n_color_names,
                                   size_t kmer_length, size_t threads_count, int forward_only, size_t minimizer_length,
                                   int colors, size_t min_multiplicity, int extra_elab, int gfa_output_version);
+
+/* Announces the colour table of the next build (the arguments of ggcat_gpu_colors, before
+ * ggcat_gpu_build_text / ggcat_gpu_merge): the batched merge then collects every k-mer
+ * instance's colour into its table entry, like the reference's buckets carry each superkmer's
+ * colour into the merge (MinimizerBucketingMultipleSeqColorDataType, add_temp_buffer_structure_el,
+ * crates/assembler_kmers_merge/src/unitigs_extender/hashmap.rs:361-431), and ggcat_gpu_colors
+ * called with the same table merges the dumped copies instead of reading the text again.
+ * Results are identical either way; the merge skips the collection (and ggcat_gpu_colors reads
+ * the text) when its bitmap scratch would pass a quarter of the free device memory, for the
+ * spilled store, the per-bucket form or k > 64.  n_seq = 0 withdraws the announcement. */
+int ggcat_gpu_colors_prepare(ggcat_gpu_ctx *ctx, const uint64_t *h_seq_off, const uint32_t *h_seq_color,
+                             uint64_t n_seq, uint32_t n_colors);
 
 /* ---- colour subsets ----
  * Replaces the per-k-mer colour sets and subset dedup of MultipleColorsManager

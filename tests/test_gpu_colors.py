@@ -174,3 +174,33 @@ def test_color_sets_and_query_k63_match_oracle():
         assert (counts == epc).all()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("k,m,bbits", [(31, 10, 6), (31, 10, 3), (45, 12, 5)])
+def test_colors_collected_by_the_merge(k, m, bbits):
+    """Colours announced before the build (ggcat_gpu_colors_prepare) are collected by the merge
+    units; ggcat_gpu_colors then merges the dumped copies of a k-mer (a copy in a neighbouring
+    sub-bucket sees only its boundary occurrences) instead of reading the text.  The per-k-mer
+    colour sets equal the oracle's and the text pass's, and each set is one subset."""
+    from oracle import parity
+
+    text, off, ln, col, gs, nc = _colored_input(seed=31 + k + bbits)
+    p = _native.make_params(k=k, m=m, bucket_bits=bbits, second_bits=2, min_multiplicity=1, keep_kmers=True)
+    r = oracle.build_graph(text, off, ln, oracle.params(k=k, m=m, bucket_bits=bbits, second_bits=2, threads=4,
+                                                         colors=True), seq_colors=col)
+    digests = []
+    for prepare in (True, False):
+        ctx = _native.GpuContext(0)
+        try:
+            if prepare:
+                ctx.colors_prepare(off, col, nc)
+            ctx.build_text(text, p)
+            ctx.colors(off, col, nc)
+            assert ctx.stats()["colors_collected"] == (1 if prepare else 0)
+            keys, _ = ctx.kmers()
+            res = parity.compare_color_sets(keys, ctx.kmer_subsets(), ctx.subsets(), r)
+            assert res["equal"], res
+            digests.append(res["digest_gpu"])
+        finally:
+            ctx.close()
+    assert digests[0] == digests[1]
