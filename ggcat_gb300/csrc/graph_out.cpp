@@ -33,8 +33,16 @@ namespace {
 
 using u128 = unsigned __int128;
 
+// a (k-1)-mer of up to 126 bases as a 256-bit integer hi * 2^128 + lo
+struct Key256 {
+    u128 hi = 0, lo = 0;
+};
+inline bool operator<(const Key256 &a, const Key256 &b) { return a.hi != b.hi ? a.hi < b.hi : a.lo < b.lo; }
+inline bool operator==(const Key256 &a, const Key256 &b) { return a.hi == b.hi && a.lo == b.lo; }
+inline bool operator!=(const Key256 &a, const Key256 &b) { return !(a == b); }
+
 struct EndEntry {
-    u128 key;          // canonical (k-1)-mer, 2 bits per base
+    Key256 key;        // canonical (k-1)-mer, 2 bits per base
     uint64_t unitig;
     uint64_t overlap;  // start of the (k-1)-mer in the unitig
     uint8_t ending;    // 0 Beginning, 1 Ending
@@ -54,13 +62,17 @@ int code_of(uint8_t c) {
 
 // forward and reverse-complement packing of s[0, n), base i at bits 2(n-1-i) (lexicographic
 // order of the integers = order of the strings); false on a non-ACGT byte
-bool pack(const uint8_t *s, int n, u128 &fw, u128 &rc) {
-    fw = rc = 0;
+bool pack(const uint8_t *s, int n, Key256 &fw, Key256 &rc) {
+    fw = rc = Key256{};
     for (int i = 0; i < n; i++) {
         const int c = code_of(s[i]);
         if (c < 0) return false;
-        fw = (fw << 2) | (u128)c;
-        rc |= (u128)(3 - c) << (2 * i);
+        fw.hi = (fw.hi << 2) | (fw.lo >> 126);
+        fw.lo = (fw.lo << 2) | (u128)c;
+        if (2 * i < 128)
+            rc.lo |= (u128)(3 - c) << (2 * i);
+        else
+            rc.hi |= (u128)(3 - c) << (2 * i - 128);
     }
     return true;
 }
@@ -71,22 +83,22 @@ int unitig_links(const uint8_t *bases, const uint64_t *off, const uint64_t *len,
                  std::vector<UnitigLink> &links, std::vector<uint64_t> &list_off, std::string &err) {
     links.clear();
     list_off.assign(2 * n + 1, 0);
-    if (k < 2 || k > 64) return err = "unitig links support 2 <= k <= 64", GGCAT_GPU_EUNSUPPORTED;
+    if (k < 2 || k > 127) return err = "unitig links support 2 <= k <= 127", GGCAT_GPU_EUNSUPPORTED;
     const int w = k - 1;
     std::vector<EndEntry> ent;
     ent.reserve(4 * n);
     for (uint64_t i = 0; i < n; i++) {
         if (len[i] < (uint64_t)k) return err = "unitig shorter than k", GGCAT_GPU_EINVAL;
         const uint8_t *s = bases + off[i];
-        u128 f, r;
+        Key256 f, r;
         if (!pack(s, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
-        const u128 kb = f < r ? f : r;
+        const Key256 kb = f < r ? f : r;
         const uint8_t fwd_b = f < r;
         ent.push_back({kb, i, 0, 0, fwd_b, 1});
         if (f == r) ent.push_back({kb, i, 0, 0, (uint8_t)!fwd_b, 0});
         const uint64_t ov = len[i] - (uint64_t)w;
         if (!pack(s + ov, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
-        const u128 ke = f < r ? f : r;
+        const Key256 ke = f < r ? f : r;
         const uint8_t fwd_e = f < r;
         ent.push_back({ke, i, ov, 1, (uint8_t)!fwd_e, 1});
         if (f == r) ent.push_back({ke, i, ov, 1, fwd_e, 0});

@@ -1168,8 +1168,9 @@ __device__ __forceinline__ void extend_unit(const Table<KT> &t, const uint32_t *
 }
 
 // One merge unit per CTA, persistent over a device work queue (tiers above).  All tiers use
-// the shared-memory list-ranking arrays for the extension.
-template <typename KT, int kTier>
+// the shared-memory list-ranking arrays for the extension.  kColors: the instantiation that
+// collects colours (the uncoloured one carries none of that code).
+template <typename KT, int kTier, bool kColors = false>
 __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kMinBlocks)
     merge_unit_kernel(MergeArgs a, const MergeUnit *__restrict__ units, const unsigned long long *__restrict__ counters_ro,
                       KT *pool_keys, uint32_t *pool_vals, uint8_t *pool_vis, uint32_t *pool_list, MergeUnit *spill,
@@ -1188,7 +1189,7 @@ __global__ void __launch_bounds__(TierCfg<KT, kTier>::NT, TierCfg<KT, kTier>::kM
     const int k = a.k;
     const uint32_t min_mult = (uint32_t)a.min_mult;
     // this CTA's colour bitmaps, one row of bm_words per table slot (colours collected here)
-    uint32_t *const bm_cta = a.bm_words ? a.bm_scratch + (uint64_t)blockIdx.x * a.bm_stride : nullptr;
+    uint32_t *const bm_cta = kColors ? a.bm_scratch + (uint64_t)blockIdx.x * a.bm_stride : nullptr;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) S.unit = atomicAdd(&o.counters[kHead], 1ull);
@@ -1540,21 +1541,31 @@ static void merge_tier_t(const MergeArgs &a, const MergeUnit *units, const unsig
                          const MergeOut &o, int sms, cudaStream_t s) {
     using Cfg = TierCfg<KT, kTier>;
     const int smem = (int)sizeof(UnitSmem<KT, kTier>);
+    if constexpr (!std::is_same<KT, u256>::value) {
+        if (a.bm_words) {  // colours collected (k <= 64)
+            merge_unit_kernel<KT, kTier, true><<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(
+                a, units, counters, keys, vals, vis, list, spill, max_units, o);
+            return;
+        }
+    }
     merge_unit_kernel<KT, kTier>
         <<<sms * Cfg::kMinBlocks, Cfg::NT, smem, s>>>(a, units, counters, keys, vals, vis, list, spill, max_units, o);
 }
 
-template <typename KT, int kTier>
+template <typename KT, int kTier, bool kColors = false>
 static cudaError_t merge_attr_t() {
-    return cudaFuncSetAttribute(merge_unit_kernel<KT, kTier>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(merge_unit_kernel<KT, kTier, kColors>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(UnitSmem<KT, kTier>));
 }
 
 cudaError_t merge_configure() {
-    const cudaError_t e[7] = {merge_attr_t<uint64_t, kTierS>(), merge_attr_t<uint64_t, kTierW>(),
-                              merge_attr_t<uint64_t, kTierM>(), merge_attr_t<u128, kTierS>(),
-                              merge_attr_t<u128, kTierW>(),     merge_attr_t<u128, kTierM>(),
-                              merge_attr_t<u256, kTierM>()};
+    const cudaError_t e[13] = {merge_attr_t<uint64_t, kTierS>(),       merge_attr_t<uint64_t, kTierW>(),
+                               merge_attr_t<uint64_t, kTierM>(),       merge_attr_t<u128, kTierS>(),
+                               merge_attr_t<u128, kTierW>(),           merge_attr_t<u128, kTierM>(),
+                               merge_attr_t<u256, kTierM>(),           merge_attr_t<uint64_t, kTierS, true>(),
+                               merge_attr_t<uint64_t, kTierW, true>(), merge_attr_t<uint64_t, kTierM, true>(),
+                               merge_attr_t<u128, kTierS, true>(),     merge_attr_t<u128, kTierW, true>(),
+                               merge_attr_t<u128, kTierM, true>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;

@@ -43,7 +43,7 @@ typedef struct {
     int32_t k;                /* k-mer length <= 127, odd or even: merge tables keyed by the canonical packed
                                  k-mer in one word (k <= 32), two (k <= 64) or four (k > 64, global-memory
                                  tables only; the Rabin-Karp hash_kind, as the reference requires above 64;
-                                 colours, queries and unitig links stop at 64); forward-only merges exclude
+                                 colours and queries stop at 64); forward-only merges exclude
                                  k = 32 and 64 (their all-G k-mer is the tables' empty key) */
     int32_t m;                /* minimizer length, 2 <= m <= 32, k - m >= 2 */
     int32_t bucket_bits;      /* first-level buckets = 2^bucket_bits (+1 duplicates bucket) */
@@ -228,7 +228,7 @@ int ggcat_gpu_read_sequences_files(const char *const *paths, uint64_t n, int64_t
 
 /* Maximal-unitig links (build_maximal_unitigs_links,
  * crates/assembler_pipeline/src/maximal_unitig_links.rs:55-417) of n unitigs
- * bases[off[i], off[i] + len[i]) (ACGT, len >= k, k <= 64): list 2i = links from unitig i's
+ * bases[off[i], off[i] + len[i]) (ACGT, len >= k, k <= 127): list 2i = links from unitig i's
  * end, list 2i + 1 = from its beginning, entries [list_off[l], list_off[l + 1]) (list_off:
  * 2n + 1 entries).  Per link: the other unitig, the start of the shared (k-1)-mer in it, flags
  * bit 0 = flip_current, bit 1 = flip_other.  Pass other = NULL to query *n_links. */

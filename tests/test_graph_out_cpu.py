@@ -54,13 +54,16 @@ def test_links_random_short_strings(seed):
     _same(_native_links(unitigs, k), naive.unitig_links(unitigs, k))
 
 
-@pytest.mark.parametrize("k", [31, 63])
+@pytest.mark.parametrize("k", [31, 63, 65, 101, 127])
 def test_links_of_built_unitigs(k):
+    """Links of built unitigs against the string restatement; above k = 64 the (k-1)-mers take
+    up to 126 bases (the oracle builds those graphs with the Rabin-Karp u128 hash)."""
     rng = np.random.default_rng(k)
-    g = synth.add_repeats(synth.random_genome(60_000, rng), 0.05, 200, 3, 10, rng)
+    g = synth.add_repeats(synth.random_genome(60_000, rng), 0.05, 3 * k, 3, 10, rng)
     text, off, ln, _ = synth.pack_sequences([g, synth.substitute(g, 0.01, rng)])
     r = oracle.build_graph(text, off, ln, oracle.params(k=k, m=12 if k > 32 else 10, bucket_bits=4, second_bits=2,
-                                                         threads=4))
+                                                         threads=4,
+                                                         hash_kind=oracle.H_CN_RK128 if k > 64 else None))
     unitigs = [line for line in r.unitigs().split(b"\n") if line]
     got, exp = _native_links(unitigs, k), naive.unitig_links(unitigs, k)
     _same(got, exp)
