@@ -103,6 +103,27 @@ __global__ void index_from_colors_kernel(const uint64_t *__restrict__ cslots, ui
     }
 }
 
+// Lookups of a query run are issued four at a time: the canonical keys of the next four valid
+// k-mers are rolled first, their first slots loaded together, and only collisions probe on
+// (one round trip to memory per four k-mers instead of one per k-mer).
+constexpr int kQueryIlp = 4;
+
+// slot of key in the index given its first probe's key (first); -1 when absent
+template <typename KT>
+__device__ __forceinline__ int64_t query_resolve(const KT *__restrict__ keys, uint64_t mask, const KT &key, uint64_t s,
+                                                 const KT &first) {
+    using K = KeyOps<KT>;
+    if (first == key) return (int64_t)s;
+    if (first == K::empty()) return -1;
+    for (uint64_t probe = 1; probe <= mask; probe++) {
+        s = (s + 1) & mask;
+        const KT kk = keys[s];
+        if (kk == key) return (int64_t)s;
+        if (kk == K::empty()) return -1;
+    }
+    return -1;
+}
+
 // One work item = a run of k-mer positions of one query; matches are summed per query.
 template <typename KT>
 __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ text, int k,
@@ -120,28 +141,42 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
     const KT kmask = K::mask(k);
     KT fw = 0, rc = 0;
     uint64_t run = 0, hits = 0;
-    for (uint64_t p = x0; p < x1 + (uint64_t)k - 1; p++) {
-        const uint32_t c = text[p];
-        const uint32_t u = c & 0xDFu;
-        if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
-            run = 0;
-            continue;
-        }
-        const uint32_t b = (c >> 1) & 3u;
-        fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
-        rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
-        if (++run < (uint64_t)k) continue;
-        const KT key = fw < rc ? fw : rc;
-        uint64_t s = qslot_key(key, mask);
-        for (uint64_t probe = 0; probe <= mask; probe++) {
-            const KT kk = keys[s];
-            if (kk == key) {
-                hits++;
-                break;
+    const uint64_t pend = x1 + (uint64_t)k - 1;
+    uint64_t p = x0;
+    for (;;) {
+        KT key[kQueryIlp];
+        int nk = 0;
+#pragma unroll
+        for (int j = 0; j < kQueryIlp; j++) {  // (static indices keep key[] in registers)
+            bool got = false;
+            while (!got && p < pend) {
+                const uint32_t c = text[p++];
+                const uint32_t u = c & 0xDFu;
+                if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                    run = 0;
+                    continue;
+                }
+                const uint32_t b = (c >> 1) & 3u;
+                fw = (fw >> 2) | ((KT)b << (2 * (k - 1)));
+                rc = ((rc << 2) | (KT)(b ^ 2u)) & kmask;
+                if (++run >= (uint64_t)k) got = true;
             }
-            if (kk == K::empty()) break;
-            s = (s + 1) & mask;
+            if (!got) break;
+            key[j] = fw < rc ? fw : rc;
+            nk = j + 1;
         }
+        if (nk == 0) break;
+        uint64_t sl[kQueryIlp];
+        KT first[kQueryIlp];
+#pragma unroll
+        for (int j = 0; j < kQueryIlp; j++)
+            if (j < nk) {
+                sl[j] = qslot_key(key[j], mask);
+                first[j] = keys[sl[j]];
+            }
+#pragma unroll
+        for (int j = 0; j < kQueryIlp; j++)
+            if (j < nk && query_resolve(keys, mask, key[j], sl[j], first[j]) >= 0) hits++;
     }
     if (hits) atomicAdd(&matched[q], (unsigned long long)hits);
 }
@@ -196,33 +231,52 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
         };
         if (a < b) {
             const uint64_t base = q_off[q];
-            for (uint64_t p = base + a; p < base + b + (uint64_t)k - 1; p++) {
-                const uint32_t c = text[p];
-                const uint32_t u = c & 0xDFu;
-                if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
-                    run = 0;
-                    continue;
-                }
-                const uint32_t bb = (c >> 1) & 3u;
-                fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
-                rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
-                if (++run < (uint64_t)k) continue;
-                const KT key = fw < rc ? fw : rc;
-                uint64_t s = qslot_key(key, mask);
-                for (uint64_t probe = 0; probe <= mask; probe++) {
-                    const KT kk = keys[s];
-                    if (kk == key) {
-                        hits++;
-                        const uint32_t sub = vals[s];
-                        if (sub != cur_sub) {
-                            flush();
-                            cur_sub = sub;
+            const uint64_t pend = base + b + (uint64_t)k - 1;
+            uint64_t p = base + a;
+            for (;;) {
+                KT key[kQueryIlp];
+                int nk = 0;
+#pragma unroll
+                for (int j = 0; j < kQueryIlp; j++) {
+                    bool got = false;
+                    while (!got && p < pend) {
+                        const uint32_t c = text[p++];
+                        const uint32_t u = c & 0xDFu;
+                        if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                            run = 0;
+                            continue;
                         }
-                        cur_cnt++;
-                        break;
+                        const uint32_t bb = (c >> 1) & 3u;
+                        fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
+                        rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
+                        if (++run >= (uint64_t)k) got = true;
                     }
-                    if (kk == K::empty()) break;
-                    s = (s + 1) & mask;
+                    if (!got) break;
+                    key[j] = fw < rc ? fw : rc;
+                    nk = j + 1;
+                }
+                if (nk == 0) break;
+                uint64_t sl[kQueryIlp];
+                KT first[kQueryIlp];
+#pragma unroll
+                for (int j = 0; j < kQueryIlp; j++)
+                    if (j < nk) {
+                        sl[j] = qslot_key(key[j], mask);
+                        first[j] = keys[sl[j]];
+                    }
+                // resolved in position order: runs of equal subsets stay runs
+#pragma unroll
+                for (int j = 0; j < kQueryIlp; j++) {
+                    if (j >= nk) continue;
+                    const int64_t s = query_resolve(keys, mask, key[j], sl[j], first[j]);
+                    if (s < 0) continue;
+                    hits++;
+                    const uint32_t sub = vals[s];
+                    if (sub != cur_sub) {
+                        flush();
+                        cur_sub = sub;
+                    }
+                    cur_cnt++;
                 }
             }
             flush();

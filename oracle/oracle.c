@@ -555,7 +555,8 @@ static inline int okey_cmp(okey a, okey b) {
 
 typedef struct {
     u128 key;      /* MH unextendable hash */
-    okey packed;   /* canonical 2-bit packed k-mer (seq-hash layout, extended past 64 bases) */
+    u128 packed;   /* canonical 2-bit packed k-mer, bases 0-63 (seq-hash layout); bases 64-127 of
+                      a k > 64 k-mer in the merge's side array, by ordinal */
     uint64_t count;
     uint8_t flags, used, occupied;
     uint32_t ordinal;    /* creation order; stable across kmap_grow (colour pairs refer to it) */
@@ -631,6 +632,15 @@ static inline uint64_t entry_mult(const kentry *e) {
 /* packed canonical k-mer in seq-hash layout (base i at bits 2i) for k <= 128; for k <= 64
  * the seq-hash value itself (hi = 0) */
 static okey pack_canonical(const uint8_t *cb, int k, int canonical) {
+    if (k <= 64) {  /* the seq-hash value (one 128-bit word) */
+        u128 f = 0, r = 0;
+        for (int i = 0; i < k; i++) {
+            f |= (u128)(cb[i] & 3) << (2 * i);
+            r |= (u128)((cb[k - 1 - i] & 3) ^ 2) << (2 * i);
+        }
+        okey o = {canonical && r < f ? r : f, 0};
+        return o;
+    }
     okey fw = {0, 0}, rc = {0, 0};
     for (int i = 0; i < k; i++) {
         const u128 f = (u128)(cb[i] & 3), r = (u128)((cb[k - 1 - i] & 3) ^ 2);
@@ -666,7 +676,7 @@ static void ut_push(unitig_vec *v, unitig_t u) {
 }
 
 typedef struct {
-    okey packed;
+    u128 packed; /* bases 0-63; bases 64-127 of a k > 64 k-mer in the vector's hi array */
     uint64_t mult;
     uint32_t color_off, color_n;
 } kmer_out;
@@ -676,12 +686,15 @@ typedef struct {
     size_t n, cap;
     uint32_t *colors;
     size_t ncol, colcap;
+    u128 *hi; /* k > 64 only, parallel to v */
 } kmer_vec;
-static void kv_push(kmer_vec *v, kmer_out k) {
+static void kv_push(kmer_vec *v, kmer_out k, int wide, u128 hi) {
     if (v->n == v->cap) {
         v->cap = v->cap ? v->cap * 2 : 1024;
         v->v = xrealloc(v->v, v->cap * sizeof(kmer_out));
+        if (wide) v->hi = xrealloc(v->hi, v->cap * sizeof(u128));
     }
+    if (wide) v->hi[v->n] = hi;
     v->v[v->n++] = k;
 }
 static uint32_t kv_push_colors(kmer_vec *v, const uint32_t *c, size_t n) {
@@ -794,6 +807,8 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
     size_t cap = 0;
     color_pair *cpairs = NULL;
     size_t ncp = 0, cpcap = 0;
+    u128 *packed_hi = NULL; /* k > 64: bases 64-127 of each entry, by ordinal */
+    size_t hi_cap = 0;
     /* add_sequence, hashmap.rs:361-431; reads in stored orientation (rc applied) */
     for (size_t r = 0; r < nrec; r++) {
         const orc_superkmer *s = &recs[r];
@@ -819,8 +834,16 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
             int created;
             kentry *e = kmap_insert(&m, orc_hash_unext(kind, hs[idx]), &created);
             if (created) {
-                e->packed = pack_canonical(cb + idx, k, orc_hash_is_canonical(kind));
+                const okey q = pack_canonical(cb + idx, k, orc_hash_is_canonical(kind));
+                e->packed = q.lo;
                 e->ordinal = (uint32_t)(m.n - 1);
+                if (k > 64) {
+                    if (e->ordinal >= hi_cap) {
+                        hi_cap = hi_cap ? hi_cap * 2 : 1024;
+                        packed_hi = xrealloc(packed_hi, hi_cap * sizeof(u128));
+                    }
+                    packed_hi[e->ordinal] = q.hi;
+                }
             }
             e->flags |= (uint8_t)(((unsigned)begin_ignored << (unsigned)!isf) | ((unsigned)end_ignored << (unsigned)isf));
             e->count += 1; /* every record has multiplicity 1 (no compaction) */
@@ -862,7 +885,7 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
             ko.color_off = kv_push_colors(&job->kmers, ucolors + slot_col_off[e->ordinal], slot_col_n[e->ordinal]);
             ko.color_n = slot_col_n[e->ordinal];
         }
-        kv_push(&job->kmers, ko);
+        kv_push(&job->kmers, ko, k > 64, k > 64 ? packed_hi[e->ordinal] : 0);
     }
 
     /* compute_unitigs, hashmap.rs:442-601; k-mers visited in read order (get_kmers,
@@ -926,6 +949,7 @@ static void merge_unit(merge_job *job, const orc_superkmer *recs, size_t nrec) {
     free(hs);
     free(m.e);
     free(cpairs);
+    free(packed_hi);
     free(slot_col_off);
     free(slot_col_n);
     free(ucolors);
@@ -1156,6 +1180,7 @@ size_t orc_canonicalize_unitigs(const uint8_t *lines, size_t len, const uint8_t 
 struct orc_build_result {
     int k;
     kmer_out *kmers;
+    u128 *kmers_hi; /* k > 64: bases 64-127 of each k-mer */
     size_t nkmers;
     uint32_t *colors;
     size_t ncolors;
@@ -1165,7 +1190,18 @@ struct orc_build_result {
 
 static int cmp_kmer_out(const void *a, const void *b) {
     const kmer_out *x = a, *y = b;
-    return okey_cmp(x->packed, y->packed);
+    return x->packed < y->packed ? -1 : x->packed > y->packed;
+}
+/* k > 64: the k-mers sorted by (lo, hi) through an index */
+typedef struct {
+    u128 lo, hi;
+    size_t i;
+} wide_ref;
+static int cmp_wide_ref(const void *a, const void *b) {
+    const wide_ref *x = a, *y = b;
+    if (x->lo != y->lo) return x->lo < y->lo ? -1 : 1;
+    if (x->hi != y->hi) return x->hi < y->hi ? -1 : 1;
+    return 0;
 }
 
 orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const uint64_t *seq_len,
@@ -1209,17 +1245,18 @@ orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const 
             merge_worker(&jobs[t]);
     }
     unitig_vec partial = {0, 0, 0};
-    kmer_vec kv = {0, 0, 0, 0, 0, 0};
+    kmer_vec kv = {0, 0, 0, 0, 0, 0, 0};
     for (int t = 0; t < nt; t++) {
         if (nt > 1) pthread_join(th[t], NULL);
         for (size_t i = 0; i < jobs[t].unitigs.n; i++) ut_push(&partial, jobs[t].unitigs.v[i]);
         for (size_t i = 0; i < jobs[t].kmers.n; i++) {
             kmer_out ko = jobs[t].kmers.v[i];
             if (ko.color_n) ko.color_off = kv_push_colors(&kv, jobs[t].kmers.colors + ko.color_off, ko.color_n);
-            kv_push(&kv, ko);
+            kv_push(&kv, ko, p->k > 64, p->k > 64 ? jobs[t].kmers.hi[i] : 0);
         }
         free(jobs[t].unitigs.v);
         free(jobs[t].kmers.v);
+        free(jobs[t].kmers.hi);
         free(jobs[t].kmers.colors);
     }
     pthread_mutex_destroy(&sh.lock);
@@ -1232,16 +1269,35 @@ orc_build_result *orc_build(const uint8_t *text, const uint64_t *seq_off, const 
     res->k = p->k;
     /* k-mers at a sub-bucket boundary are counted in both sub-buckets with the same
      * multiplicity: keep one copy. */
-    qsort(kv.v, kv.n, sizeof(kmer_out), cmp_kmer_out);
+    if (p->k > 64) {
+        wide_ref *ref = xmalloc((kv.n + 1) * sizeof(wide_ref));
+        for (size_t i = 0; i < kv.n; i++) ref[i] = (wide_ref){kv.v[i].packed, kv.hi[i], i};
+        qsort(ref, kv.n, sizeof(wide_ref), cmp_wide_ref);
+        kmer_out *sv = xmalloc((kv.n + 1) * sizeof(kmer_out));
+        u128 *sh = xmalloc((kv.n + 1) * sizeof(u128));
+        for (size_t i = 0; i < kv.n; i++) {
+            sv[i] = kv.v[ref[i].i];
+            sh[i] = ref[i].hi;
+        }
+        free(ref);
+        free(kv.v);
+        free(kv.hi);
+        kv.v = sv;
+        kv.hi = sh;
+    } else {
+        qsort(kv.v, kv.n, sizeof(kmer_out), cmp_kmer_out);
+    }
     size_t w = 0;
     for (size_t i = 0; i < kv.n; i++) {
-        if (w > 0 && okey_cmp(kv.v[w - 1].packed, kv.v[i].packed) == 0) {
+        if (w > 0 && kv.v[w - 1].packed == kv.v[i].packed && (p->k <= 64 || kv.hi[w - 1] == kv.hi[i])) {
             if (kv.v[w - 1].mult != kv.v[i].mult) kv.v[w - 1].mult = UINT64_MAX; /* inconsistency marker */
             continue;
         }
+        if (p->k > 64) kv.hi[w] = kv.hi[i];
         kv.v[w++] = kv.v[i];
     }
     res->kmers = kv.v;
+    res->kmers_hi = kv.hi;
     res->nkmers = w;
     res->colors = kv.colors;
     res->ncolors = kv.ncol;
@@ -1267,6 +1323,7 @@ void orc_build_free(orc_build_result *r) {
     for (size_t i = 0; i < r->final_unitigs.n; i++) free(r->final_unitigs.v[i].seq);
     free(r->final_unitigs.v);
     free(r->kmers);
+    free(r->kmers_hi);
     free(r->colors);
     free(r);
 }
@@ -1274,8 +1331,8 @@ void orc_build_free(orc_build_result *r) {
 size_t orc_build_kmers(const orc_build_result *r, uint64_t *lo, uint64_t *hi, uint64_t *mult, size_t cap) {
     if (lo)
         for (size_t i = 0; i < r->nkmers && i < cap; i++) {
-            lo[i] = (uint64_t)r->kmers[i].packed.lo;
-            hi[i] = (uint64_t)(r->kmers[i].packed.lo >> 64);
+            lo[i] = (uint64_t)r->kmers[i].packed;
+            hi[i] = (uint64_t)(r->kmers[i].packed >> 64);
             mult[i] = r->kmers[i].mult;
         }
     return r->nkmers;
@@ -1285,11 +1342,11 @@ size_t orc_build_kmers(const orc_build_result *r, uint64_t *lo, uint64_t *hi, ui
 size_t orc_build_kmers_wide(const orc_build_result *r, uint64_t *words, uint64_t *mult, size_t cap) {
     if (words)
         for (size_t i = 0; i < r->nkmers && i < cap; i++) {
-            const okey q = r->kmers[i].packed;
-            words[4 * i] = (uint64_t)q.lo;
-            words[4 * i + 1] = (uint64_t)(q.lo >> 64);
-            words[4 * i + 2] = (uint64_t)q.hi;
-            words[4 * i + 3] = (uint64_t)(q.hi >> 64);
+            const u128 lo = r->kmers[i].packed, hi = r->kmers_hi ? r->kmers_hi[i] : 0;
+            words[4 * i] = (uint64_t)lo;
+            words[4 * i + 1] = (uint64_t)(lo >> 64);
+            words[4 * i + 2] = (uint64_t)hi;
+            words[4 * i + 3] = (uint64_t)(hi >> 64);
             mult[i] = r->kmers[i].mult;
         }
     return r->nkmers;
