@@ -340,6 +340,15 @@ extern "C" uint64_t ggcat_gpu_kernel_launches(const ggcat_gpu_ctx *ctx) { return
 // merge-table key words as a power of two: u64 (k <= 32), u128 (k <= 64), u256 (k <= 127)
 static int key_width(int k) { return k > 64 ? 2 : k > 32 ? 1 : 0; }
 
+// Defaults of the tuning knobs (0 in ggcat_gpu_params).  Above k = 32 they are the autotuner's
+// choice on the 2 Gbp long-k reads (k = 63, 250-bp reads): sub-bins of 4096 text bytes, 90 %
+// global-table load, 8-record insert batches, W units up to 8192 instances (longer records
+// carry more k-mers each, so smaller batches and units balance the warps).
+static uint64_t default_subbin_bytes(int k) { return k > 32 ? 4096 : 1024; }
+static uint32_t default_load_pct(int k) { return k > 32 ? 90 : 80; }
+static int default_rec_batch(int k) { return k > 32 ? 8 : 16; }
+static uint64_t default_wide_limit(int k, uint64_t tier_max) { return k > 32 ? std::min<uint64_t>(8192, tier_max) : tier_max; }
+
 static int check_params(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p) {
     if (!p) return fail(ctx, GGCAT_GPU_EINVAL, "null params");
     if (p->m < 2 || p->m > 32) return fail(ctx, GGCAT_GPU_EINVAL, "minimizer length m=%d outside [2, 32]", p->m);
@@ -515,7 +524,7 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     CK(ctx->valid.ensure(n_words));
     ctx->n_buckets = (1u << p->bucket_bits) + 1;
     // sub-bins per bucket: about subbin_bytes (default 1K) text bytes per sub-bin on average
-    const uint64_t subbin = p->subbin_bytes > 0 ? (uint64_t)p->subbin_bytes : 1024ull;
+    const uint64_t subbin = p->subbin_bytes > 0 ? (uint64_t)p->subbin_bytes : default_subbin_bytes(p->k);
     int fb = 0;
     while (fb < kMaxFineBits && ((uint64_t)ctx->n_buckets << fb) * subbin < text_len) fb++;
     ctx->fine_bits = fb < 4 ? 4 : fb;
@@ -708,7 +717,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
                                                     : merge_small_limit(wide);
     // worst-case slot pool of the global-memory tables: cap < 2 * (x * 100 / load + 64) per unit,
     // units of more than small_limit instances each
-    const uint32_t load_pct = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : 80u;
+    const uint32_t load_pct = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : default_load_pct(p->k);
     const uint64_t max_big_units = std::min<uint64_t>(ctx->n_bins, ctx->n_kmers / small_limit + 1);
     uint64_t pool = ctx->n_kmers * 200 / load_pct + 2 + 128ull * (ctx->n_buckets + max_big_units) + 1024;
     CK(ctx->tkeys.ensure(pool << wide));
@@ -732,7 +741,7 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         // colours collected by the merge: one bitmap row per table slot and CTA, sized for the
         // largest table of the shared-memory tiers and of the M tier (units up to 2^18 instances)
         const int words = (int)((ctx->cprep_colors + 31) / 32);
-        const uint32_t load = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : 80u;
+        const uint32_t load = p->table_load_pct > 0 ? (uint32_t)p->table_load_pct : default_load_pct(p->k);
         uint64_t mcap = 64;
         while (mcap < (1ull << 18) * 100 / load + 64) mcap <<= 1;
         const uint64_t rows = std::max<uint64_t>(mcap, 11264);
@@ -758,15 +767,15 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     }
     // per-class insert batches of the shared-memory tiers
     MergeArgs a_small = a, a_wide = a;
-    a_small.rec_batch = p->small_batch > 0 ? p->small_batch : 16;
-    a_wide.rec_batch = p->wide_batch > 0 ? p->wide_batch : 16;
+    a_small.rec_batch = p->small_batch > 0 ? p->small_batch : default_rec_batch(p->k);
+    a_wide.rec_batch = p->wide_batch > 0 ? p->wide_batch : default_rec_batch(p->k);
     MergeArgs am = a;
     am.ext_stride = stride_m;
     am.ext_cap = kExtCapMedium;
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
-    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1024 : 2048);
+    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1600 : 2048);
     if (target > small_limit) target = small_limit;
 
     if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) {
@@ -813,8 +822,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
         const uint64_t medium_limit = 1ull << 18;
         const uint64_t wide_limit =
             p->unit_target < 0 ? 0
-                               : std::min<uint64_t>(merge_wide_limit(wide), p->wide_limit > 0 ? (uint64_t)p->wide_limit
-                                                                                             : merge_wide_limit(wide));
+                               : std::min<uint64_t>(merge_wide_limit(wide),
+                                                    p->wide_limit > 0 ? (uint64_t)p->wide_limit
+                                                                      : default_wide_limit(p->k, merge_wide_limit(wide)));
         // the whole batched merge phase: counter reset, classification, the S/W/M persistent
         // kernels fed by device work queues and the grid-wide L kernels
         auto enqueue = [&](cudaStream_t q) -> int {
@@ -1206,8 +1216,8 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
                                                     : std::vector<int32_t>{0, -1, 1024, 3200}},
         {&ggcat_gpu_params::small_limit, 0x3u, wide ? std::vector<int32_t>{0, 1200, 800}
                                                     : std::vector<int32_t>{0, 2400, 1600}},
-        {&ggcat_gpu_params::small_batch, 0x1u, {0, 8, 32}},
-        {&ggcat_gpu_params::wide_batch, 0x2u, {0, 8, 12, 24, 32}},
+        {&ggcat_gpu_params::small_batch, 0x1u, {0, 8, 16, 32}},
+        {&ggcat_gpu_params::wide_batch, 0x2u, {0, 8, 12, 16, 24, 32}},
         {&ggcat_gpu_params::wide_limit, 0x6u, {0, wl / 2, wl / 4}},
         {&ggcat_gpu_params::table_load_pct, 0xcu, {0, 50, 65, 90}},
     };

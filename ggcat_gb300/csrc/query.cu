@@ -103,9 +103,10 @@ __global__ void index_from_colors_kernel(const uint64_t *__restrict__ cslots, ui
     }
 }
 
-// Lookups of a query run are issued four at a time: the canonical keys of the next four valid
-// k-mers are rolled first, their first slots loaded together, and only collisions probe on
-// (one round trip to memory per four k-mers instead of one per k-mer).
+// Lookups of an uncoloured query run are issued four at a time: the canonical keys of the next
+// four valid k-mers are rolled first, their first slots loaded together, and only collisions
+// probe on (one round trip to memory per four k-mers instead of one per k-mer).  The coloured
+// lookup keeps one at a time: batching it measured slower (its per-colour counting dominates).
 constexpr int kQueryIlp = 4;
 
 // slot of key in the index given its first probe's key (first); -1 when absent
@@ -231,53 +232,29 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
         };
         if (a < b) {
             const uint64_t base = q_off[q];
-            const uint64_t pend = base + b + (uint64_t)k - 1;
-            uint64_t p = base + a;
-            for (;;) {
-                KT key[kQueryIlp];
-                int nk = 0;
-#pragma unroll
-                for (int j = 0; j < kQueryIlp; j++) {
-                    bool got = false;
-                    while (!got && p < pend) {
-                        const uint32_t c = text[p++];
-                        const uint32_t u = c & 0xDFu;
-                        if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
-                            run = 0;
-                            continue;
-                        }
-                        const uint32_t bb = (c >> 1) & 3u;
-                        fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
-                        rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
-                        if (++run >= (uint64_t)k) got = true;
-                    }
-                    if (!got) break;
-                    key[j] = fw < rc ? fw : rc;
-                    nk = j + 1;
+            for (uint64_t p = base + a; p < base + b + (uint64_t)k - 1; p++) {
+                const uint32_t c = text[p];
+                const uint32_t u = c & 0xDFu;
+                if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                    run = 0;
+                    continue;
                 }
-                if (nk == 0) break;
-                uint64_t sl[kQueryIlp];
-                KT first[kQueryIlp];
-#pragma unroll
-                for (int j = 0; j < kQueryIlp; j++)
-                    if (j < nk) {
-                        sl[j] = qslot_key(key[j], mask);
-                        first[j] = keys[sl[j]];
-                    }
-                // resolved in position order: runs of equal subsets stay runs
-#pragma unroll
-                for (int j = 0; j < kQueryIlp; j++) {
-                    if (j >= nk) continue;
-                    const int64_t s = query_resolve(keys, mask, key[j], sl[j], first[j]);
-                    if (s < 0) continue;
-                    hits++;
-                    const uint32_t sub = vals[s];
-                    if (sub != cur_sub) {
-                        flush();
-                        cur_sub = sub;
-                    }
-                    cur_cnt++;
+                const uint32_t bb = (c >> 1) & 3u;
+                fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
+                rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
+                if (++run < (uint64_t)k) continue;
+                const KT key = fw < rc ? fw : rc;
+                uint64_t s = qslot_key(key, mask);
+                const KT first = keys[s];
+                const int64_t sl = query_resolve(keys, mask, key, s, first);
+                if (sl < 0) continue;
+                hits++;
+                const uint32_t sub = vals[sl];
+                if (sub != cur_sub) {
+                    flush();
+                    cur_sub = sub;
                 }
+                cur_cnt++;
             }
             flush();
         }

@@ -57,8 +57,9 @@ typedef struct {
     int32_t keep_kmers;       /* 1 = also output the surviving k-mers and multiplicities */
     /* tuning knobs (0 = default; ggcat_gpu_autotune chooses them), results are identical for any value */
     int32_t subbin_bytes;     /* text bytes per sub-bin: sets the sub-bin digit width of the bucket store
-                                 partition (default 1024) */
-    int32_t table_load_pct;   /* largest load of a global-memory merge table, percent (default 80) */
+                                 partition (default 1024, 4096 for k > 32) */
+    int32_t table_load_pct;   /* largest load of a global-memory merge table, percent (default 80, 90 for
+                                 k > 32) */
     int32_t small_limit;      /* largest sub-bin, in k-mer instances, merged in a shared-memory S unit
                                  (default and maximum 3200, 1600 for k > 32) */
     int32_t copy_pieces;      /* pieces of the host text copy of ggcat_gpu_build_text from pinned memory,
@@ -72,10 +73,12 @@ typedef struct {
                                  to the device (the reference's bucket files spilled from its in-memory
                                  store, crates/minimizer_bucketing/src/lib.rs:569-586).  Results are the same. */
     /* per bucket-size-class knobs (0 = default), results identical for any value */
-    int32_t small_batch;      /* superkmer records per insert batch of a warp in S units, 1-32 (default 16) */
-    int32_t wide_batch;       /* the same in W units, 1-32 (default 16) */
+    int32_t small_batch;      /* superkmer records per insert batch of a warp in S units, 1-32 (default 16,
+                                 8 for k > 32) */
+    int32_t wide_batch;       /* the same in W units, 1-32 (default 16, 8 for k > 32) */
     int32_t wide_limit;       /* largest sub-bin, in k-mer instances, tried in a shared-memory W unit before
-                                 a global-memory table (default and maximum 65536, 16384 for k > 32) */
+                                 a global-memory table (default and maximum 65536; k > 32: default 8192,
+                                 maximum 16384) */
 } ggcat_gpu_params;
 
 /* One superkmer in the semantic form of PushSequenceInfo

@@ -257,8 +257,8 @@ def test_autotune_params_build_the_same_graph(ctx):
     assert best.subbin_bytes in (0, 256, 512, 1024, 2048, 4096)
     assert best.unit_target in (0, -1, 1024, 3200)
     assert best.small_limit in (0, 2400, 1600)
-    assert best.small_batch in (0, 8, 32)
-    assert best.wide_batch in (0, 8, 12, 24, 32)
+    assert best.small_batch in (0, 8, 16, 32)
+    assert best.wide_batch in (0, 8, 12, 16, 24, 32)
     assert best.wide_limit in (0, 32768, 16384)
     assert best.table_load_pct in (0, 50, 65, 90)
     # per-class device times of the tuned build, one per bucket-size class
