@@ -245,16 +245,21 @@ __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restr
                 if (++run < (uint64_t)k) continue;
                 const KT key = fw < rc ? fw : rc;
                 uint64_t s = qslot_key(key, mask);
-                const KT first = keys[s];
-                const int64_t sl = query_resolve(keys, mask, key, s, first);
-                if (sl < 0) continue;
-                hits++;
-                const uint32_t sub = vals[sl];
-                if (sub != cur_sub) {
-                    flush();
-                    cur_sub = sub;
+                for (uint64_t probe = 0; probe <= mask; probe++) {
+                    const KT kk = keys[s];
+                    if (kk == key) {
+                        hits++;
+                        const uint32_t sub = vals[s];
+                        if (sub != cur_sub) {
+                            flush();
+                            cur_sub = sub;
+                        }
+                        cur_cnt++;
+                        break;
+                    }
+                    if (kk == K::empty()) break;
+                    s = (s + 1) & mask;
                 }
-                cur_cnt++;
             }
             flush();
         }
