@@ -48,7 +48,7 @@ struct DevBuf {
     }
 };
 
-constexpr int kFeedPieces = 4;  // pieces of build_text's pipelined host text copy
+constexpr int kFeedPieces = 16;  // pieces of build_text's pipelined host text copy
 
 struct PinnedBuf {
     uint8_t *p = nullptr;
@@ -197,6 +197,8 @@ struct ggcat_gpu_ctx {
     // the batched merge phase as a CUDA graph, captured once per buffer/parameter layout
     cudaStream_t cap_stream = nullptr;
     cudaStream_t copy_stream = nullptr;         // pipelined host text copies of build_text
+    cudaStream_t piece_stream[kFeedPieces] = {};  // pack + bucketize of each piece (they overlap)
+    cudaEvent_t pack_ev[kFeedPieces] = {}, piece_done_ev[kFeedPieces] = {}, feed_start_ev = nullptr;
     cudaEvent_t feed_ev[kFeedPieces + 1] = {};  // [0]: compute stream ready, [1 + i]: piece i copied
     cudaGraphExec_t merge_exec = nullptr;
     MergeGraphKey merge_key{};
@@ -256,6 +258,13 @@ struct ggcat_gpu_ctx {
             if (e) cudaEventDestroy(e);
         for (auto &e : feed_ev)
             if (e) cudaEventDestroy(e);
+        for (auto &e : pack_ev)
+            if (e) cudaEventDestroy(e);
+        for (auto &e : piece_done_ev)
+            if (e) cudaEventDestroy(e);
+        if (feed_start_ev) cudaEventDestroy(feed_start_ev);
+        for (auto &q : piece_stream)
+            if (q) cudaStreamDestroy(q);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         for (auto &q : qslots) {
             if (q.done) cudaEventDestroy(q.done);
@@ -558,11 +567,11 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     const uint64_t block_bases = bucketize_block_bases(geo);
     CK(ctx->rec_total.ensure(1));
     int split_counts = 0;
-    auto bucketize_blocks = [&](uint64_t b0, uint64_t b1) {
+    auto bucketize_blocks = [&](uint64_t b0, uint64_t b1, cudaStream_t q) {
         return launch_bucketize(ctx->packed.p, ctx->valid.p, text_len, p->k, p->m, p->bucket_bits, p->second_bits,
                                 ctx->fine_bits, canonical, geo, ctx->bin_count.p, ctx->bin_kmers.p, split_counts,
                                 ctx->rec_total.p, ctx->stage.p, ctx->block_count.p, ovf_cap, ctx->ovf_cursor.p,
-                                ctx->status.p, (uint32_t)b0, (uint32_t)(b1 - b0), s);
+                                ctx->status.p, (uint32_t)b0, (uint32_t)(b1 - b0), q);
     };
     auto clear_counts = [&]() -> int {
         CK(ctx->stage.ensure((uint64_t)geo.blocks * geo.region_cap + ovf_cap));
@@ -576,19 +585,36 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
     };
     CK(cudaEventRecord(ctx->ev[0], s));
     if (feed) {
-        // pipelined: pack each piece as it arrives, bucketize a piece's blocks one piece later
+        // pipelined: each piece on its own stream, packed when it arrives and bucketized once the
+        // next piece is packed too (a block reads k - 1 bases and a prefetched word past its
+        // last window); the pieces' kernels overlap, so a piece may be smaller than a wave.
         // (ms_pack stays 0; ms_bucketize covers the whole pipeline, copy waits included)
         CK(cudaEventRecord(ctx->ev[1], s));
         rc = clear_counts();
         if (rc) return rc;
-        for (int i = 0; i < feed->pieces; i++) {
+        if (!ctx->feed_start_ev) CK(cudaEventCreateWithFlags(&ctx->feed_start_ev, cudaEventDisableTiming));
+        CK(cudaEventRecord(ctx->feed_start_ev, s));  // the counters are clear
+        const int np = feed->pieces;
+        for (int i = 0; i < np; i++) {
+            if (!ctx->piece_stream[i]) CK(cudaStreamCreateWithFlags(&ctx->piece_stream[i], cudaStreamNonBlocking));
+            if (!ctx->pack_ev[i]) CK(cudaEventCreateWithFlags(&ctx->pack_ev[i], cudaEventDisableTiming));
+            if (!ctx->piece_done_ev[i]) CK(cudaEventCreateWithFlags(&ctx->piece_done_ev[i], cudaEventDisableTiming));
+            cudaStream_t q = ctx->piece_stream[i];
             const uint64_t o0 = feed->off[i], o1 = feed->off[i + 1];
-            CK(cudaStreamWaitEvent(s, feed->ev[i], 0));
-            ctx->launches += launch_pack(d_text + o0, o1 - o0, ctx->packed.p + o0 / 32, ctx->valid.p + o0 / 32, s,
+            CK(cudaStreamWaitEvent(q, ctx->feed_start_ev, 0));
+            CK(cudaStreamWaitEvent(q, feed->ev[i], 0));
+            ctx->launches += launch_pack(d_text + o0, o1 - o0, ctx->packed.p + o0 / 32, ctx->valid.p + o0 / 32, q,
                                          ctx->sms);
-            if (i > 0) ctx->launches += bucketize_blocks(feed->off[i - 1] / block_bases, o0 / block_bases);
+            CK(cudaEventRecord(ctx->pack_ev[i], q));
         }
-        ctx->launches += bucketize_blocks(feed->off[feed->pieces - 1] / block_bases, geo.blocks);
+        for (int i = 0; i < np; i++) {
+            cudaStream_t q = ctx->piece_stream[i];
+            if (i + 1 < np) CK(cudaStreamWaitEvent(q, ctx->pack_ev[i + 1], 0));
+            const uint64_t b0 = feed->off[i] / block_bases, b1 = i + 1 < np ? feed->off[i + 1] / block_bases : geo.blocks;
+            ctx->launches += bucketize_blocks(b0, b1, q);
+            CK(cudaEventRecord(ctx->piece_done_ev[i], q));
+        }
+        for (int i = 0; i < np; i++) CK(cudaStreamWaitEvent(s, ctx->piece_done_ev[i], 0));
         CK(cudaGetLastError());
     } else {
         ctx->launches += launch_pack(d_text, text_len, ctx->packed.p, ctx->valid.p, s, ctx->sms);
@@ -600,7 +626,7 @@ static int bucketize_impl(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uint64_t te
         if (attempt > 0 || !feed) {
             rc = clear_counts();
             if (rc) return rc;
-            ctx->launches += bucketize_blocks(0, geo.blocks);
+            ctx->launches += bucketize_blocks(0, geo.blocks, s);
         }
         CK(cudaGetLastError());
         ctx->launches += launch_exclusive_scan(ctx->bin_count.p, nb, ctx->bin_off.p, ctx->scan_tmp.p, s,
@@ -1483,11 +1509,11 @@ extern "C" int ggcat_gpu_build_text(ggcat_gpu_ctx *ctx, const uint8_t *h_text, u
         if (rc) return rc;
         const BucketizeGeometry geo = bucketize_geometry(text_len, p->k, p->m);
         const uint64_t bb = bucketize_block_bases(geo);
-        // every piece at least two full waves of bucketize blocks (3 per SM): the pieces'
-        // launches run one after another, so a piece of less than a wave costs a whole wave
+        // every piece at least half a wave of bucketize blocks (3 per SM): the pieces' kernels
+        // run on their own streams and overlap, so small pieces start the bucketing early
         const uint64_t wave = (uint64_t)ctx->sms * 3;
         const int want = p->copy_pieces > 0 ? (int)std::min<uint64_t>(p->copy_pieces, geo.blocks)
-                                            : (int)std::min<uint64_t>(kFeedPieces, geo.blocks / (2 * wave));
+                                            : (int)std::min<uint64_t>(kFeedPieces, geo.blocks / (wave / 2));
         const uint64_t per = want > 1 ? (geo.blocks + want - 1) / want : geo.blocks;
         uint64_t off[kFeedPieces + 1];
         int pieces = 0;

@@ -435,18 +435,21 @@ def _unitig_multiset(ctx):
     return sorted(out)
 
 
+@pytest.mark.parametrize("pieces", [4, 16])
 @pytest.mark.parametrize("k,m,read_len", [(31, 10, 150), (63, 12, 250)])
-def test_pinned_text_pipelined_equals_pageable(ctx, k, m, read_len):
+def test_pinned_text_pipelined_equals_pageable(ctx, k, m, read_len, pieces):
     """build_text from pinned host memory copies the text in pieces on its own stream and
-    packs / bucketizes each piece while the next ones are in flight; the records, k-mers and
-    partial unitigs equal those of the one-copy (pageable) path."""
+    packs / bucketizes each piece on a stream of its own while the next ones are in flight (16
+    pieces: one or two bucketize blocks each, their kernels overlapping); the records, k-mers
+    and partial unitigs equal those of the one-copy (pageable) path."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(k)
     g = synth.random_genome(300_000, rng)
     reads = synth.sample_reads(g, 6_000_000 // read_len, read_len, 0.005, 0.0002, rng)
     text, _, _, _ = synth.pack_reads(reads)
     assert len(text) > 8 * 262144  # several bucketize blocks per piece
-    p = make_params(k=k, m=m, bucket_bits=8, second_bits=3, min_multiplicity=2, keep_kmers=True, copy_pieces=4)
+    p = make_params(k=k, m=m, bucket_bits=8, second_bits=3, min_multiplicity=2, keep_kmers=True,
+                    copy_pieces=pieces)
 
     def run(t):
         ctx.build_text(t, p)
