@@ -64,8 +64,8 @@ typedef struct {
                                  (default and maximum 3200, 1600 for k > 32) */
     int32_t copy_pieces;      /* pieces of the host text copy of ggcat_gpu_build_text from pinned memory,
                                  each packed and bucketized on its own stream while the next ones are in
-                                 flight (0 = auto: up to 16, each at least half a wave of bucketize
-                                 blocks; 1 = one copy; at most 16) */
+                                 flight (0 = auto: up to 16, each at least a wave of bucketize blocks;
+                                 1 = one copy; at most 16) */
     int32_t spill_mb;         /* device memory for the bucket store, MiB (0 = no limit).  When the superkmer
                                  records would exceed it, or do not fit the device's free memory, the text is
                                  bucketized in pieces whose partitioned records go to pinned host memory, and
