@@ -801,7 +801,9 @@ static int merge_once(ggcat_gpu_ctx *ctx, const ggcat_gpu_params *p, cudaStream_
     MergeOut o{ctx->out_bases.p, bases_cap,       ctx->out_off.p,   ctx->out_len.p, ctx->out_flags.p,
                u_cap,            ctx->counters.p, ctx->kmer_keys.p, ctx->kmer_mult.p,
                p->keep_kmers ? kmer_cap : 0,      ctx->status.p + 1};
-    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1600 : 2048);
+    // S packing target: the size limit itself (fewer, fuller S units; the tuner's choice on the
+    // skewed reads, S class 2.16 -> 1.95 ms, and on the long-k reads)
+    uint64_t target = p->unit_target > 0 ? (uint64_t)p->unit_target : (wide ? 1600 : 3200);
     if (target > small_limit) target = small_limit;
 
     if (p->merge_mode == GGCAT_MERGE_PER_BUCKET) {
@@ -1238,8 +1240,8 @@ extern "C" int ggcat_gpu_autotune(ggcat_gpu_ctx *ctx, const uint8_t *d_text, uin
     };
     const int32_t wl = (int32_t)merge_wide_limit(wide);
     const std::vector<Knob> knobs = {
-        {&ggcat_gpu_params::unit_target, 0x7u, wide ? std::vector<int32_t>{0, -1, 512, 1600}
-                                                    : std::vector<int32_t>{0, -1, 1024, 3200}},
+        {&ggcat_gpu_params::unit_target, 0x7u, wide ? std::vector<int32_t>{0, -1, 512, 1024}
+                                                    : std::vector<int32_t>{0, -1, 1024, 2048}},
         {&ggcat_gpu_params::small_limit, 0x3u, wide ? std::vector<int32_t>{0, 1200, 800}
                                                     : std::vector<int32_t>{0, 2400, 1600}},
         {&ggcat_gpu_params::small_batch, 0x1u, {0, 8, 16, 32}},

@@ -255,7 +255,7 @@ def test_autotune_params_build_the_same_graph(ctx):
     best, default_ms, best_ms = ctx.autotune(d.data_ptr(), d.numel(), p)
     assert 0 < best_ms
     assert best.subbin_bytes in (0, 256, 512, 1024, 2048, 4096)
-    assert best.unit_target in (0, -1, 1024, 3200)
+    assert best.unit_target in (0, -1, 1024, 2048)
     assert best.small_limit in (0, 2400, 1600)
     assert best.small_batch in (0, 8, 16, 32)
     assert best.wide_batch in (0, 8, 12, 16, 24, 32)
