@@ -273,6 +273,25 @@ struct ggcat_gpu_ctx {
     }
 };
 
+// Host copy split over up to 8 threads when large (one core copies ~14 GB/s, a batch of query
+// text is a few hundred MB).
+static void par_memcpy(void *dst, const void *src, uint64_t n) {
+    const uint64_t kMin = 32ull << 20;
+    const int t = (int)std::min<uint64_t>({8, n / kMin, (uint64_t)std::max(1u, std::thread::hardware_concurrency())});
+    if (t <= 1) {
+        if (n) memcpy(dst, src, n);
+        return;
+    }
+    const uint64_t per = (n + t - 1) / t;
+    std::vector<std::thread> th;
+    for (int i = 1; i < t; i++) {
+        const uint64_t a = std::min<uint64_t>(n, per * i), b = std::min<uint64_t>(n, a + per);
+        th.emplace_back([=] { memcpy(static_cast<uint8_t *>(dst) + a, static_cast<const uint8_t *>(src) + a, b - a); });
+    }
+    memcpy(dst, src, std::min<uint64_t>(n, per));
+    for (auto &x : th) x.join();
+}
+
 static int fail(ggcat_gpu_ctx *c, int code, const char *fmt, ...) {
     char buf[512];
     va_list ap;
@@ -2015,7 +2034,7 @@ extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_
             return fail(ctx, GGCAT_GPU_EINVAL, "query %llu outside the text", (unsigned long long)i);
     cudaStream_t s = q.stream;
     CK(q.h_text.ensure(len + 1));
-    memcpy(q.h_text.p, h_text, len);
+    par_memcpy(q.h_text.p, h_text, len);
     CK(q.d_text.ensure(len + 1));
     CK(q.d_matched.ensure(nq + 1));
     CK(q.d_status.ensure(1));
@@ -2023,9 +2042,10 @@ extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_
     CK(cudaMemcpyAsync(q.d_text.p, q.h_text.p, len, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(q.d_matched.p, 0, nq * sizeof(unsigned long long), s));
     q.colored = ctx->qcolored;
-    if (!ctx->qcolored) {
+    const bool warp_colored = ctx->qcolored && ctx->c_words <= kColorWarpMaxWords;
+    if (!ctx->qcolored || warp_colored) {
         // work items: runs of at most kChunk k-mer positions of one query
-        const uint64_t kChunk = 2048;
+        const uint64_t kChunk = warp_colored ? query_color_chunk() : 2048;
         uint64_t n_items = 0;
         for (uint64_t i = 0; i < nq; i++) {
             const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
@@ -2050,8 +2070,21 @@ extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_
         CK(cudaMemcpyAsync(q.d_iq.p, iq, n_items * 4, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(q.d_is.p, is, n_items * 8, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(q.d_il.p, il, n_items * 4, cudaMemcpyHostToDevice, s));
-        ctx->launches += launch_query(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items, ctx->qkeys.p, ctx->qmask,
-                                      q.d_matched.p, s);
+        if (!warp_colored) {
+            ctx->launches += launch_query(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items, ctx->qkeys.p,
+                                          ctx->qmask, q.d_matched.p, s);
+        } else {
+            const uint64_t nc = ctx->c_colors;
+            CK(q.d_counts.ensure(nq * nc + 1));
+            CK(q.h_counts.ensure(nq * nc * sizeof(unsigned long long) + 16));
+            CK(cudaMemsetAsync(q.d_counts.p, 0, nq * nc * sizeof(unsigned long long), s));
+            ctx->launches += launch_query_color_items(q.d_text.p, k, q.d_iq.p, q.d_is.p, q.d_il.p, n_items,
+                                                      ctx->qkeys.p, ctx->qvals.p, ctx->qmask, ctx->csub_arena.p,
+                                                      ctx->c_words, ctx->c_colors, q.d_matched.p, q.d_counts.p,
+                                                      ctx->sms, s);
+            CK(cudaMemcpyAsync(q.h_counts.p, q.d_counts.p, nq * nc * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, s));
+        }
         q.n_items = n_items;
     } else {
         const uint64_t nc = ctx->c_colors;
@@ -2111,7 +2144,8 @@ extern "C" int ggcat_gpu_query_color_counts(ggcat_gpu_ctx *ctx, int slot, uint64
     if (!q.colored) return fail(ctx, GGCAT_GPU_EINVAL, "slot %d ran an uncoloured batch", slot);
     if (n_colors) *n_colors = ctx->c_colors;
     if (h_counts)
-        memcpy(h_counts, q.h_counts.p, std::min<uint64_t>(cap, q.nq * (uint64_t)ctx->c_colors) * sizeof(uint64_t));
+        par_memcpy(h_counts, q.h_counts.p,
+                   std::min<uint64_t>(cap, q.nq * (uint64_t)ctx->c_colors) * sizeof(uint64_t));
     return GGCAT_GPU_OK;
 }
 

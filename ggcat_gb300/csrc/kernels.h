@@ -166,6 +166,16 @@ int launch_index_from_colors(const uint64_t *cslots, uint64_t ccap, const uint32
 int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
                  const uint32_t *item_len, uint64_t n_items, const void *keys, uint64_t mask,
                  unsigned long long *matched, cudaStream_t s);
+// Coloured lookup over work items (runs of at most query_color_chunk() k-mer positions of one
+// query, as for launch_query), for subsets of at most kColorWarpMaxWords bitmap words (256
+// colours); matched and counts (nq x n_colors) must be zeroed first.  Returns 0 (nothing
+// launched) above that width: launch_query_color covers any width.
+constexpr int kColorWarpMaxWords = 8;
+uint32_t query_color_chunk();
+int launch_query_color_items(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
+                             const uint32_t *item_len, uint64_t n_items, const void *keys, const uint32_t *vals,
+                             uint64_t mask, const uint32_t *sub_arena, int words, uint32_t n_colors,
+                             unsigned long long *matched, unsigned long long *counts, int sms, cudaStream_t s);
 int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,
                        const void *keys, const uint32_t *vals, uint64_t mask, const uint32_t *sub_arena, int words,
                        uint32_t n_colors, unsigned long long *matched, unsigned long long *counts,

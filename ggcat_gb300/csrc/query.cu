@@ -105,8 +105,7 @@ __global__ void index_from_colors_kernel(const uint64_t *__restrict__ cslots, ui
 
 // Lookups of an uncoloured query run are issued four at a time: the canonical keys of the next
 // four valid k-mers are rolled first, their first slots loaded together, and only collisions
-// probe on (one round trip to memory per four k-mers instead of one per k-mer).  The coloured
-// lookup keeps one at a time: batching it measured slower (its per-colour counting dominates).
+// probe on (one round trip to memory per four k-mers instead of one per k-mer).
 constexpr int kQueryIlp = 4;
 
 // slot of key in the index given its first probe's key (first); -1 when absent
@@ -182,9 +181,113 @@ __global__ void __launch_bounds__(256) query_kernel(const uint8_t *__restrict__ 
     if (hits) atomicAdd(&matched[q], (unsigned long long)hits);
 }
 
-// Coloured lookup, one CTA per query from a device queue: runs of equal subset ids are
-// expanded into per-colour counts in shared memory (colored_query_output.rs:264-309 sums
-// the per-subset counters of a query per colour).
+// Coloured lookup for up to 32 * W colours (W bitmap words per subset), one warp per work item
+// (a run of at most kColorChunk k-mer positions of one query; colored_query_output.rs:264-309
+// sums the per-subset counters of a query per colour).  Each lane rolls a contiguous span of
+// the run and merges its consecutive equal subset ids; a changed id is emitted with its
+// multiplicity: the lane stages the subset's words in shared memory and the warp walks the
+// emitting lanes, lane l adding bit l of every word (colours 32 w + l) into its own register
+// counters.  Counting therefore costs ~3 W instructions per emitted run and no atomics; each
+// item adds its counters to the query's row once.
+constexpr uint32_t kColorChunk = 4096;
+constexpr int kColorWarps = 8;  // warps per CTA
+
+template <typename KT, int W>
+__global__ void __launch_bounds__(32 * kColorWarps) query_color_warp_kernel(
+    const uint8_t *__restrict__ text, int k, const uint32_t *__restrict__ item_query,
+    const uint64_t *__restrict__ item_start, const uint32_t *__restrict__ item_len, uint64_t n_items,
+    const KT *__restrict__ keys, const uint32_t *__restrict__ vals, uint64_t mask,
+    const uint32_t *__restrict__ sub_arena, int words, uint32_t n_colors, unsigned long long *__restrict__ matched,
+    unsigned long long *__restrict__ counts) {
+    using K = KeyOps<KT>;
+    constexpr uint32_t kNone = 0xffffffffu;
+    __shared__ __align__(16) uint32_t stage[kColorWarps][32][W];
+    __shared__ uint32_t stage_mult[kColorWarps][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const KT kmask = K::mask(k);
+    const uint64_t nwarps = (uint64_t)gridDim.x * kColorWarps;
+    for (uint64_t it = (uint64_t)blockIdx.x * kColorWarps + wib; it < n_items; it += nwarps) {
+        const uint32_t q = item_query[it];
+        const uint64_t x0 = item_start[it];
+        const uint32_t len = item_len[it];
+        const uint32_t per = (len + 31) / 32;
+        const uint32_t a = min(len, (uint32_t)lane * per), b = min(len, a + per);
+        uint32_t cnt[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) cnt[w] = 0;
+        // warp-collective: adds every emitting lane's run (e_sub, e_mult) to the counters
+        auto emit = [&](uint32_t e_sub, uint32_t e_mult) {
+            const unsigned ball = __ballot_sync(0xffffffffu, e_sub != kNone);
+            if (!ball) return;
+            if (e_sub != kNone) {
+                const uint32_t *bm = sub_arena + (uint64_t)e_sub * (uint64_t)words;
+#pragma unroll
+                for (int w = 0; w < W; w++) stage[wib][lane][w] = w < words ? bm[w] : 0u;
+                stage_mult[wib][lane] = e_mult;
+            }
+            __syncwarp();
+            for (unsigned m = ball; m; m &= m - 1) {
+                const int j = __ffs(m) - 1;
+                const uint32_t mj = stage_mult[wib][j];
+#pragma unroll
+                for (int w = 0; w < W; w++) cnt[w] += ((stage[wib][j][w] >> lane) & 1u) * mj;
+            }
+            __syncwarp();
+        };
+        KT fw = 0, rc = 0;
+        uint32_t run = 0, hits = 0, cur = kNone, mult = 0;
+        uint64_t p = x0 + a;
+        for (uint32_t i = 0; i < per; i++) {  // the same trip count on every lane
+            uint32_t sub = kNone;
+            if (a + i < b) {
+                const uint64_t e = x0 + a + i + (uint64_t)k - 1;  // last base of k-mer a + i
+                while (p <= e) {
+                    const uint32_t c = text[p++];
+                    const uint32_t u = c & 0xDFu;
+                    if (!((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T'))) {
+                        run = 0;
+                        continue;
+                    }
+                    const uint32_t bb = (c >> 1) & 3u;
+                    fw = (fw >> 2) | ((KT)bb << (2 * (k - 1)));
+                    rc = ((rc << 2) | (KT)(bb ^ 2u)) & kmask;
+                    run++;
+                }
+                if (run >= (uint32_t)k) {
+                    const KT key = fw < rc ? fw : rc;
+                    const uint64_t s0 = qslot_key(key, mask);
+                    const int64_t sl = query_resolve(keys, mask, key, s0, keys[s0]);
+                    if (sl >= 0) {
+                        sub = vals[sl];
+                        hits++;
+                    }
+                }
+            }
+            uint32_t e_sub = kNone, e_mult = 0;
+            if (sub != cur) {
+                e_sub = cur;
+                e_mult = mult;
+                cur = sub;
+                mult = sub != kNone ? 1u : 0u;
+            } else if (sub != kNone) {
+                mult++;
+            }
+            emit(e_sub, e_mult);
+        }
+        emit(cur, mult);
+        unsigned long long *row = counts + (uint64_t)q * n_colors;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            const uint32_t c = 32u * w + lane;
+            if (cnt[w] && c < n_colors) atomicAdd(&row[c], (unsigned long long)cnt[w]);
+        }
+        for (int o = 16; o; o >>= 1) hits += __shfl_xor_sync(0xffffffffu, hits, o);
+        if (lane == 0 && hits) atomicAdd(&matched[q], (unsigned long long)hits);
+    }
+}
+
+// Coloured lookup for any number of colours, one CTA per query from a device queue: runs of
+// equal subset ids are expanded into per-colour counts in shared memory.
 template <typename KT>
 __global__ void __launch_bounds__(256) query_color_kernel(const uint8_t *__restrict__ text, int k,
                                                          const uint64_t *__restrict__ q_off,
@@ -377,6 +480,52 @@ int launch_query(const uint8_t *text, int k, const uint32_t *item_query, const u
         query_kernel<uint64_t><<<grid, 256, 0, s>>>(text, k, item_query, item_start, item_len, n_items,
                                                     static_cast<const uint64_t *>(keys), mask, matched);
     return 1;
+}
+
+uint32_t query_color_chunk() { return kColorChunk; }
+
+template <typename KT, int W>
+static void color_warp_launch(const uint8_t *text, int k, const uint32_t *iq, const uint64_t *is, const uint32_t *il,
+                              uint64_t n_items, const void *keys, const uint32_t *vals, uint64_t mask,
+                              const uint32_t *sub_arena, int words, uint32_t n_colors, unsigned long long *matched,
+                              unsigned long long *counts, int sms, cudaStream_t s) {
+    const uint64_t blocks = (n_items + kColorWarps - 1) / kColorWarps;
+    const unsigned grid = (unsigned)std::min<uint64_t>(blocks, (uint64_t)sms * 8);
+    query_color_warp_kernel<KT, W><<<grid, 32 * kColorWarps, 0, s>>>(text, k, iq, is, il, n_items,
+                                                                     static_cast<const KT *>(keys), vals, mask,
+                                                                     sub_arena, words, n_colors, matched, counts);
+}
+
+template <typename KT>
+static int color_warp_dispatch(const uint8_t *text, int k, const uint32_t *iq, const uint64_t *is, const uint32_t *il,
+                               uint64_t n_items, const void *keys, const uint32_t *vals, uint64_t mask,
+                               const uint32_t *sub_arena, int words, uint32_t n_colors, unsigned long long *matched,
+                               unsigned long long *counts, int sms, cudaStream_t s) {
+    if (words <= 1)
+        color_warp_launch<KT, 1>(text, k, iq, is, il, n_items, keys, vals, mask, sub_arena, words, n_colors, matched,
+                                 counts, sms, s);
+    else if (words <= 2)
+        color_warp_launch<KT, 2>(text, k, iq, is, il, n_items, keys, vals, mask, sub_arena, words, n_colors, matched,
+                                 counts, sms, s);
+    else if (words <= 4)
+        color_warp_launch<KT, 4>(text, k, iq, is, il, n_items, keys, vals, mask, sub_arena, words, n_colors, matched,
+                                 counts, sms, s);
+    else
+        color_warp_launch<KT, 8>(text, k, iq, is, il, n_items, keys, vals, mask, sub_arena, words, n_colors, matched,
+                                 counts, sms, s);
+    return 1;
+}
+
+int launch_query_color_items(const uint8_t *text, int k, const uint32_t *item_query, const uint64_t *item_start,
+                             const uint32_t *item_len, uint64_t n_items, const void *keys, const uint32_t *vals,
+                             uint64_t mask, const uint32_t *sub_arena, int words, uint32_t n_colors,
+                             unsigned long long *matched, unsigned long long *counts, int sms, cudaStream_t s) {
+    if (n_items == 0 || words > kColorWarpMaxWords) return 0;
+    if (k > 32)
+        return color_warp_dispatch<u128>(text, k, item_query, item_start, item_len, n_items, keys, vals, mask,
+                                         sub_arena, words, n_colors, matched, counts, sms, s);
+    return color_warp_dispatch<uint64_t>(text, k, item_query, item_start, item_len, n_items, keys, vals, mask,
+                                         sub_arena, words, n_colors, matched, counts, sms, s);
 }
 
 int launch_query_color(const uint8_t *text, int k, const uint64_t *q_off, const uint64_t *q_len, uint64_t nq,

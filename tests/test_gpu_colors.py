@@ -204,3 +204,42 @@ def test_colors_collected_by_the_merge(k, m, bbits):
         finally:
             ctx.close()
     assert digests[0] == digests[1]
+
+
+@pytest.mark.parametrize("n_genomes,max_rate", [(40, 0.03), (70, 0.0005), (200, 0.03), (300, 0.002)])
+def test_colored_query_counts_many_colours(n_genomes, max_rate):
+    """Subset bitmaps of 2, 3, 7 and 10 words: the warp-per-run lookup (up to 8 words; 70 and
+    200 colours end in a partial word) and the per-query CTA lookup (above 8 words).  Queries
+    are longer than one work item (4096 k-mer positions) and some hold N runs; the low
+    divergence cases give long runs of one subset (multiplicities above 1)."""
+    rng = np.random.default_rng(1000 + n_genomes)
+    anc = synth.random_genome(12_000, rng)
+    gs = [synth.indels(synth.substitute(anc, float(rng.uniform(0.0, max_rate)), rng), 0.0005, 10, rng)
+          for _ in range(n_genomes)]
+    text, off, ln, col = synth.pack_sequences(gs, list(range(n_genomes)))
+    ctx = _native.GpuContext(0)
+    try:
+        p = _native.make_params(k=31, m=10, bucket_bits=6, second_bits=2, min_multiplicity=1, keep_kmers=True)
+        ctx.build_text(text, p)
+        ctx.colors(off, col, n_genomes)
+        r = oracle.build_graph(text, off, ln, oracle.params(k=31, m=10, bucket_bits=6, second_bits=2, threads=8,
+                                                             colors=True), seq_colors=col)
+        ctx.query_index_colored()
+        queries, _ = synth.query_stream(gs, 50, rng, min_len=20, max_len=12_000)
+        qt, qo, ql = serve._pack(queries)
+        for i in range(0, len(qo), 3):  # N runs inside every third query
+            if ql[i] > 100:
+                at = int(qo[i]) + int(rng.integers(0, int(ql[i]) - 10))
+                qt[at:at + int(rng.integers(1, 6))] = ord("N")
+        ctx.query_submit(2, qt, qo, ql)
+        matched = ctx.query_wait(2)
+        counts = ctx.query_color_counts(2)
+        lo, hi, _ = r.kmers()
+        coff, ccol = r.kmer_colors()
+        em, _, epc = oracle.query(lo, hi, qt, qo, ql, 31, gc_off=coff, gc_colors=ccol, ncolors=n_genomes)
+        assert counts.shape == (len(qo), n_genomes)
+        assert (matched == em).all()
+        assert (counts == epc).all()
+        assert epc[:, -1].sum() > 0 and epc.sum() > 0
+    finally:
+        ctx.close()
