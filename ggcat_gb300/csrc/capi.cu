@@ -2044,8 +2044,14 @@ extern "C" int ggcat_gpu_query_submit(ggcat_gpu_ctx *ctx, int slot, const uint8_
     q.colored = ctx->qcolored;
     const bool warp_colored = ctx->qcolored && ctx->c_words <= kColorWarpMaxWords;
     if (!ctx->qcolored || warp_colored) {
-        // work items: runs of at most kChunk k-mer positions of one query
-        const uint64_t kChunk = warp_colored ? query_color_chunk() : 2048;
+        // work items: runs of at most kChunk k-mer positions of one query, sized so that a small
+        // batch still spreads over every warp (coloured: one warp per item) or thread (one
+        // thread per item) the GPU holds at once, and a large one takes the longest runs
+        uint64_t total_nk = 0;
+        for (uint64_t i = 0; i < nq; i++) total_nk += h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
+        const uint64_t workers = warp_colored ? (uint64_t)ctx->sms * 64 : (uint64_t)ctx->sms * 2048;
+        const uint64_t lo_chunk = warp_colored ? 256 : 64, hi_chunk = warp_colored ? query_color_chunk() : 2048;
+        const uint64_t kChunk = std::min<uint64_t>(hi_chunk, std::max<uint64_t>(lo_chunk, (total_nk / workers + 31) & ~(uint64_t)31));
         uint64_t n_items = 0;
         for (uint64_t i = 0; i < nq; i++) {
             const uint64_t nk = h_len[i] >= (uint64_t)k ? h_len[i] - (uint64_t)k + 1 : 0;
