@@ -394,6 +394,10 @@ def colored_bench(args, ctx, torch, dev):
     # arrival-rate sweep (the knee): the same queries with the Poisson gaps scaled; "inf" = all
     # queries waiting at t = 0
     sweep = []
+    # untimed pass with every query waiting at t = 0: the slots' pinned staging buffers grow to
+    # the largest batch here, not inside the measured runs
+    serve.serve(ctx, 31, qt, qo, ql, np.zeros_like(arr), slots=4, max_batch_kmers=budget, colored=True,
+                free_bytes=free_fn)
     for rate in (80_000.0, 320_000.0, float("inf")):
         a2 = np.zeros_like(arr) if rate == float("inf") else arr * (args.query_rate / rate)
         r2 = serve.serve(ctx, 31, qt, qo, ql, a2, slots=4, max_batch_kmers=budget, colored=True, free_bytes=free_fn)
@@ -463,9 +467,12 @@ def build_config_bench(w, torch, dev, steps=3, cpu_threads=0, tune=False):
         h = torch.from_numpy(w.text).pin_memory()
         ctx.build_text(h.numpy(), p)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.build_text(h.numpy(), p)
-        e2e_s = time.perf_counter() - t0
+        e2e_runs = []
+        for _ in range(3):  # median of three host-memory builds (one is noisy on the host side)
+            t0 = time.perf_counter()
+            ctx.build_text(h.numpy(), p)
+            e2e_runs.append(time.perf_counter() - t0)
+        e2e_s = statistics.median(e2e_runs)
         ctx.link(w.k)
         st = ctx.stats()
         link_ms = st["ms_link"]
