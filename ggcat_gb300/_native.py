@@ -110,6 +110,7 @@ EXPORTED = [
     "ggcat_gpu_read_sequences_file",
     "ggcat_gpu_read_sequences_files",
     "ggcat_gpu_unitig_links",
+    "ggcat_gpu_compute_tigs",
     "ggcat_gpu_write_graph",
     "ggcat_gpu_dump_unitigs",
     "ggcat_gpu_collect_streams",
@@ -196,6 +197,7 @@ def load(build: bool = True):
     L.ggcat_gpu_read_sequences_files.argtypes = [C.POINTER(C.c_char_p), u64, C.c_int64, C.c_int, P, u64, pu64,
                                                  C.c_char_p, u64]
     L.ggcat_gpu_unitig_links.argtypes = [P, P, P, u64, C.c_int, P, P, P, P, u64, pu64]
+    L.ggcat_gpu_compute_tigs.argtypes = [P, P, P, u64, C.c_int, C.c_int, P, u64, P, P, u64, pu64, pu64]
     L.ggcat_gpu_write_graph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, u64]
     L.ggcat_gpu_dump_unitigs.argtypes = [C.c_char_p, C.c_int, C.c_int, DUMP_FN, C.c_void_p]
     L.ggcat_gpu_colormap_file.argtypes = [C.c_char_p, C.c_char_p, u64]
@@ -522,6 +524,29 @@ def unitig_links(bases: np.ndarray, off: np.ndarray, ln: np.ndarray, k: int):
     if rc:
         raise GgcatGpuError(f"unitig_links failed ({_ERRORS.get(rc, rc)})")
     return lo, other, overlap, flags
+
+
+TIGS_GREEDY_MATCHTIGS, TIGS_EULERTIGS, TIGS_PATHTIGS = 2, 3, 4
+
+
+def compute_tigs(bases: np.ndarray, off: np.ndarray, ln: np.ndarray, k: int, mode: int):
+    """Greedy matchtigs / eulertigs / pathtigs (mode 2 / 3 / 4) of the unitigs
+    bases[off[i]:off[i] + ln[i]]: (bases, off, len) of the strings."""
+    L = load()
+    b = np.ascontiguousarray(bases, np.uint8)
+    o = np.ascontiguousarray(off, np.uint64)
+    n_ = np.ascontiguousarray(ln, np.uint64)
+    n = len(o)
+    cap_b = int(n_.sum()) if n else 0
+    ob = np.zeros(max(cap_b, 1), np.uint8)
+    oo = np.zeros(max(n, 1), np.uint64)
+    ol = np.zeros(max(n, 1), np.uint64)
+    cnt, nb = C.c_uint64(), C.c_uint64()
+    rc = L.ggcat_gpu_compute_tigs(_ptr(b), _ptr(o), _ptr(n_), n, k, mode, _ptr(ob), ob.size, _ptr(oo), _ptr(ol),
+                                  oo.size, C.byref(cnt), C.byref(nb))
+    if rc:
+        raise GgcatGpuError(f"compute_tigs failed ({_ERRORS.get(rc, rc)})")
+    return ob[:nb.value].copy(), oo[:cnt.value].copy(), ol[:cnt.value].copy()
 
 
 def dump_unitigs(graph_input: str, k: int, colors: bool = False) -> list:

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libggcat_gb300.so")
 SOURCES = ["bucketing.cu", "merge.cu", "link.cu", "query.cu", "colors.cu", "hashes.cu", "capi.cu", "noalloc.cu",
-           "input.cpp", "graph_out.cpp", "colormap.cpp"]
+           "input.cpp", "graph_out.cpp", "colormap.cpp", "tigs.cpp"]
 HEADERS = ["common.cuh", "kernels.h", "input.h", "graph_out.h", "colormap.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1750,6 +1750,17 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
     std::vector<uint64_t> off64(F.off.data(), F.off.data() + n), len64(n);
     for (uint64_t i = 0; i < n; i++) len64[i] = F.len[i];
     std::string err;
+    if (extra_elab >= 2) {
+        // matchtigs / eulertigs / pathtigs of the final unitigs, written in their place
+        std::vector<uint8_t> tb;
+        std::vector<uint64_t> to, tl;
+        rc = ggcat::compute_tigs(F.bases.data(), off64.data(), len64.data(), n, p.k, extra_elab, tb, to, tl, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+        rc = ggcat::write_graph_arrays(tb.data(), to.data(), tl.data(), to.size(), p.k, 0, gfa_output_version, nullptr,
+                                       output_file, err);
+        if (rc) return fail(ctx, rc, "%s", err.c_str());
+        return GGCAT_GPU_OK;
+    }
     rc = ggcat::write_graph_arrays(F.bases.data(), off64.data(), len64.data(), n, p.k, extra_elab == 1,
                                    gfa_output_version, colors ? &runs : nullptr, output_file, err);
     if (rc) return fail(ctx, rc, "%s", err.c_str());
@@ -1786,7 +1797,8 @@ extern "C" int ggcat_gpu_build_from_streams(ggcat_gpu_ctx *ctx, const ggcat_gpu_
 
 // ggcat_build_from_files with every argument (crates/capi/src/lib.rs:58-139, same order):
 // colour names and colours (colour i = input file i), extra_elab (0 none, 1 unitig links;
-// 2-4 matchtigs, eulertigs, pathtigs are not built) and gfa_output_version (0 FASTA, 1, 2)
+// 2-4 greedy matchtigs, eulertigs, pathtigs of an uncoloured graph) and gfa_output_version
+// (0 FASTA, 1, 2)
 extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                              const char *output_file, const char *const *color_names,
                                              size_t n_color_names, size_t kmer_length, size_t threads_count,
@@ -1796,8 +1808,8 @@ extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *con
     if (extra_elab < 0 || extra_elab > 4 || gfa_output_version < 0 || gfa_output_version > 2)
         return fail(ctx, GGCAT_GPU_EINVAL, "extra_elab %d / gfa_output_version %d out of range", extra_elab,
                     gfa_output_version);
-    if (extra_elab >= 2)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "matchtigs, eulertigs and pathtigs are not built");
+    if (extra_elab >= 2 && colors)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "matchtigs, eulertigs and pathtigs of a coloured graph are not built");
     std::vector<uint8_t> text;
     std::vector<uint64_t> file_off;
     {

@@ -31,16 +31,6 @@
 namespace ggcat {
 namespace {
 
-using u128 = unsigned __int128;
-
-// a (k-1)-mer of up to 126 bases as a 256-bit integer hi * 2^128 + lo
-struct Key256 {
-    u128 hi = 0, lo = 0;
-};
-inline bool operator<(const Key256 &a, const Key256 &b) { return a.hi != b.hi ? a.hi < b.hi : a.lo < b.lo; }
-inline bool operator==(const Key256 &a, const Key256 &b) { return a.hi == b.hi && a.lo == b.lo; }
-inline bool operator!=(const Key256 &a, const Key256 &b) { return !(a == b); }
-
 struct EndEntry {
     Key256 key;        // canonical (k-1)-mer, 2 bits per base
     uint64_t unitig;
@@ -49,33 +39,6 @@ struct EndEntry {
     uint8_t dir;
     uint8_t primary;   // 0 for the extra entry of a self-reverse-complement (k-1)-mer
 };
-
-int code_of(uint8_t c) {
-    switch (c) {
-        case 'A': return 0;
-        case 'C': return 1;
-        case 'G': return 2;
-        case 'T': return 3;
-        default: return -1;
-    }
-}
-
-// forward and reverse-complement packing of s[0, n), base i at bits 2(n-1-i) (lexicographic
-// order of the integers = order of the strings); false on a non-ACGT byte
-bool pack(const uint8_t *s, int n, Key256 &fw, Key256 &rc) {
-    fw = rc = Key256{};
-    for (int i = 0; i < n; i++) {
-        const int c = code_of(s[i]);
-        if (c < 0) return false;
-        fw.hi = (fw.hi << 2) | (fw.lo >> 126);
-        fw.lo = (fw.lo << 2) | (u128)c;
-        if (2 * i < 128)
-            rc.lo |= (u128)(3 - c) << (2 * i);
-        else
-            rc.hi |= (u128)(3 - c) << (2 * i - 128);
-    }
-    return true;
-}
 
 }  // namespace
 
@@ -91,13 +54,13 @@ int unitig_links(const uint8_t *bases, const uint64_t *off, const uint64_t *len,
         if (len[i] < (uint64_t)k) return err = "unitig shorter than k", GGCAT_GPU_EINVAL;
         const uint8_t *s = bases + off[i];
         Key256 f, r;
-        if (!pack(s, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
+        if (!pack_bases(s, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
         const Key256 kb = f < r ? f : r;
         const uint8_t fwd_b = f < r;
         ent.push_back({kb, i, 0, 0, fwd_b, 1});
         if (f == r) ent.push_back({kb, i, 0, 0, (uint8_t)!fwd_b, 0});
         const uint64_t ov = len[i] - (uint64_t)w;
-        if (!pack(s + ov, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
+        if (!pack_bases(s + ov, w, f, r)) return err = "unitig with a non-ACGT base", GGCAT_GPU_EINVAL;
         const Key256 ke = f < r ? f : r;
         const uint8_t fwd_e = f < r;
         ent.push_back({ke, i, ov, 1, (uint8_t)!fwd_e, 1});

@@ -1,0 +1,406 @@
+// Spectrum-preserving string sets over the final unitigs, on the host: eulertigs, pathtigs and
+// greedy matchtigs (ExtraElaboration::{Eulertigs, Pathtigs, GreedyMatchtigs},
+// crates/api/src/lib.rs:101-116; compute_matchtigs_thread,
+// crates/assembler_pipeline/src/compute_matchtigs.rs:380-537, which hands the unitig graph to
+// the matchtigs crate 2.1.x: EulertigAlgorithm, PathtigAlgorithm, GreedytigAlgorithm).  The
+// crate is a third-party dependency; this file restates the published algorithms (Schmidt and
+// Alanko, "Eulertigs: minimum plain text representation of k-mer sets without repetitions in
+// linear time", 2023; Schmidt, Khan, Alanko, Pibiri, Tomescu, "Matchtigs: minimum plain text
+// representation of k-mer sets", 2023) on our own graph structures.
+//
+// Graph.  A binode is a canonical (k-1)-mer; every unitig joins the binodes of its first and
+// last (k-1)-mer.  A unitig end has a type: 0 when its (k-1)-mer, read into the unitig, is the
+// canonical one, 1 otherwise.  A walk passing a binode leaves a unitig through one end and
+// enters the next through another end of the other type (same (k-1)-mer, same orientation);
+// at a binode whose (k-1)-mer is its own reverse complement any two ends pair.  A string is a
+// walk: its first unitig in full, every later one from offset k-1.
+//
+// Eulertigs: every binode is balanced with dummy edges to a virtual binode (|#type 0 - #type 1|
+// of them, one for an odd palindromic binode), Hierholzer's algorithm runs with the type
+// constraint, and the circuits are cut at the dummy edges: max(1, sum of imbalances / 2)
+// strings per connected component, each k-mer once — the minimum.
+// Pathtigs: a greedy walk cover (each unused unitig extended forwards, then backwards, along
+// unused unitigs), each k-mer once.
+// Greedy matchtigs: the eulertig construction where two surplus ends are first joined, cheapest
+// first, by a shortest walk of at most k-2 k-mers (Dijkstra over (binode, type) states); a join
+// of w k-mers repeats them and costs w characters instead of the k-1 of a new string, and is
+// written by appending the next unitig from offset k-1-w (compute_matchtigs.rs:490-515).
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <queue>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "ggcat_gb300.h"
+#include "graph_out.h"
+
+namespace ggcat {
+namespace {
+
+constexpr uint8_t kAny = 2;  // the "need" of a palindromic binode (and of the virtual one)
+
+struct TigGraph {
+    uint64_t n = 0;              // real unitigs; edges >= n are dummies
+    uint32_t n_bins = 0;         // real binodes; the virtual binode is n_bins
+    std::vector<uint32_t> bin;   // per end (2e start, 2e + 1 end of edge e)
+    std::vector<uint8_t> type;   // per end
+    std::vector<uint8_t> pal;    // per binode (+ virtual)
+    std::vector<int64_t> weight;  // per dummy edge: -1 virtual, else the join's k-mers
+    std::vector<uint64_t> kmers;  // per real unitig
+    // unused ends by (binode, type) (palindromic binodes: type 0 only), popped from the back
+    std::vector<uint64_t> pool_off, pool_top, pool;
+    std::vector<uint8_t> used;   // per edge
+
+    uint64_t edges() const { return bin.size() / 2; }
+    uint8_t need_after_exit(uint64_t e) const { return pal[bin[e]] ? kAny : (uint8_t)(1u - type[e]); }
+    uint8_t need_of_departure(uint64_t f) const { return pal[bin[f]] ? kAny : type[f]; }
+
+    void add_dummy(uint32_t b1, uint8_t t1, uint32_t b2, uint8_t t2, int64_t w) {
+        bin.push_back(b1);
+        type.push_back(t1);
+        bin.push_back(b2);
+        type.push_back(t2);
+        weight.push_back(w);
+    }
+
+    void build_pools() {
+        const uint64_t ne = bin.size();
+        const uint64_t slots = 2ull * (n_bins + 1);
+        pool_off.assign(slots + 1, 0);
+        for (uint64_t e = 0; e < ne; e++) pool_off[2ull * bin[e] + (pal[bin[e]] ? 0 : type[e]) + 1]++;
+        for (uint64_t s = 0; s < slots; s++) pool_off[s + 1] += pool_off[s];
+        pool.assign(ne, 0);
+        pool_top.assign(slots, 0);
+        std::vector<uint64_t> cur(pool_off.begin(), pool_off.end() - 1);
+        // ends pushed in decreasing order so that pops come out in increasing order
+        for (uint64_t e = ne; e-- > 0;) pool[cur[2ull * bin[e] + (pal[bin[e]] ? 0 : type[e])]++] = e;
+        for (uint64_t s = 0; s < slots; s++) pool_top[s] = pool_off[s + 1];
+        used.assign(edges(), 0);
+    }
+
+    // an unused end at binode b of type `need` (any type at a palindromic binode), or -1
+    int64_t take(uint32_t b, uint8_t need) {
+        const uint64_t s = 2ull * b + (need == kAny ? 0 : need);
+        uint64_t &top = pool_top[s];
+        while (top > pool_off[s]) {
+            const uint64_t f = pool[top - 1];
+            if (!used[f >> 1]) return (int64_t)f;
+            top--;
+        }
+        return -1;
+    }
+};
+
+// binodes and end types of the unitigs; false on a unitig shorter than k or a non-ACGT base
+bool build_graph(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k, TigGraph &g,
+                 std::string &err) {
+    const int w = k - 1;
+    g.n = n;
+    g.bin.assign(2 * n, 0);
+    g.type.assign(2 * n, 0);
+    g.kmers.assign(n, 0);
+    std::vector<std::pair<Key256, uint64_t>> keyed(2 * n);
+    std::vector<uint8_t> end_pal(2 * n, 0);
+    for (uint64_t u = 0; u < n; u++) {
+        if (len[u] < (uint64_t)k) return err = "unitig shorter than k", false;
+        g.kmers[u] = len[u] - (uint64_t)k + 1;
+        const uint8_t *s = bases + off[u];
+        for (uint64_t i = 0; i < len[u]; i++)
+            if (base_code(s[i]) < 0) return err = "unitig with a non-ACGT base", false;
+        Key256 f, r;
+        if (!pack_bases(s, w, f, r)) return err = "unitig with a non-ACGT base", false;
+        // start end: read into the unitig as its first (k-1)-mer
+        keyed[2 * u] = {f < r ? f : r, 2 * u};
+        g.type[2 * u] = f < r || f == r ? 0 : 1;
+        end_pal[2 * u] = f == r;
+        if (!pack_bases(s + len[u] - (uint64_t)w, w, f, r)) return err = "unitig with a non-ACGT base", false;
+        // end end: read into the unitig as the reverse complement of its last (k-1)-mer
+        keyed[2 * u + 1] = {f < r ? f : r, 2 * u + 1};
+        g.type[2 * u + 1] = r < f || f == r ? 0 : 1;
+        end_pal[2 * u + 1] = f == r;
+    }
+    std::sort(keyed.begin(), keyed.end(), [](const std::pair<Key256, uint64_t> &a, const std::pair<Key256, uint64_t> &b) {
+        return a.first != b.first ? a.first < b.first : a.second < b.second;
+    });
+    uint32_t nb = 0;
+    for (uint64_t i = 0; i < keyed.size(); i++) {
+        if (i && keyed[i].first != keyed[i - 1].first) nb++;
+        g.bin[keyed[i].second] = nb;
+    }
+    g.n_bins = keyed.empty() ? 0 : nb + 1;
+    g.pal.assign(g.n_bins + 1, 0);
+    for (uint64_t e = 0; e < 2 * n; e++) g.pal[g.bin[e]] = end_pal[e];
+    g.pal[g.n_bins] = 1;  // the virtual binode pairs any two dummy ends
+    return true;
+}
+
+// per binode: surplus ends (unmatched in any walk cover) and their type (kAny when palindromic)
+void surplus(const TigGraph &g, std::vector<uint64_t> &cnt, std::vector<uint8_t> &ty) {
+    std::vector<uint64_t> c0(g.n_bins, 0), c1(g.n_bins, 0);
+    for (uint64_t e = 0; e < 2 * g.n; e++) (g.type[e] ? c1 : c0)[g.bin[e]]++;
+    cnt.assign(g.n_bins, 0);
+    ty.assign(g.n_bins, 0);
+    for (uint32_t b = 0; b < g.n_bins; b++) {
+        if (g.pal[b]) {
+            cnt[b] = (c0[b] + c1[b]) & 1;
+            ty[b] = kAny;
+        } else if (c0[b] != c1[b]) {
+            cnt[b] = c0[b] > c1[b] ? c0[b] - c1[b] : c1[b] - c0[b];
+            ty[b] = c0[b] > c1[b] ? 0 : 1;
+        }
+    }
+}
+
+// the end type a dummy needs at binode b to pair with a surplus end of type t there
+inline uint8_t dummy_type(uint8_t t) { return t == kAny ? 0 : (uint8_t)(1u - t); }
+
+// Hierholzer with the type constraint from state (b, need); appends the circuit's entered ends
+void circuit(TigGraph &g, uint32_t b0, uint8_t need0, std::vector<uint64_t> &out) {
+    std::vector<uint64_t> stack, rev;
+    uint32_t b = b0;
+    uint8_t need = need0;
+    for (;;) {
+        const int64_t f = g.take(b, need);
+        if (f >= 0) {
+            g.used[(uint64_t)f >> 1] = 1;
+            stack.push_back((uint64_t)f);
+            const uint64_t x = (uint64_t)f ^ 1u;
+            b = g.bin[x];
+            need = g.need_after_exit(x);
+            continue;
+        }
+        if (stack.empty()) break;
+        const uint64_t top = stack.back();
+        stack.pop_back();
+        rev.push_back(top);
+        b = g.bin[top];
+        need = g.need_of_departure(top);
+    }
+    out.insert(out.end(), rev.rbegin(), rev.rend());
+}
+
+// a walk (entered ends of real unitigs and joins) spelled into the output
+struct TigOut {
+    std::vector<uint8_t> bases;
+    std::vector<uint64_t> off, len;
+};
+
+void spell(const TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k,
+           const std::vector<uint64_t> &walk, TigOut &o) {
+    const uint64_t start = o.bases.size();
+    bool first = true;
+    int64_t join = 0;
+    for (const uint64_t f : walk) {
+        const uint64_t e = f >> 1;
+        if (e >= g.n) {
+            join = g.weight[e - g.n];
+            continue;
+        }
+        const uint8_t *s = bases + off[e];
+        const uint64_t L = len[e];
+        const uint64_t from = first ? 0 : (uint64_t)(k - 1 - join);
+        if (!(f & 1)) {
+            o.bases.insert(o.bases.end(), s + from, s + L);
+        } else {
+            for (uint64_t i = from; i < L; i++) {
+                const uint8_t c = s[L - 1 - i];
+                o.bases.push_back(c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A');
+            }
+        }
+        first = false;
+        join = 0;
+    }
+    if (o.bases.size() > start) {
+        o.off.push_back(start);
+        o.len.push_back(o.bases.size() - start);
+    }
+}
+
+// circuits of the balanced graph cut at the virtual dummies; a closed circuit without them is
+// one string, opened after a join when it holds one (that join's k-mers are then not repeated)
+void emit_circuits(TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k, TigOut &o) {
+    g.build_pools();
+    std::vector<uint64_t> c;
+    auto is_virtual = [&](uint64_t f) { return (f >> 1) >= g.n && g.weight[(f >> 1) - g.n] < 0; };
+    auto is_join = [&](uint64_t f) { return (f >> 1) >= g.n && g.weight[(f >> 1) - g.n] >= 0; };
+    if (g.edges() > g.n) {
+        c.clear();
+        circuit(g, g.n_bins, kAny, c);
+        std::vector<uint64_t> walk;
+        for (const uint64_t f : c) {
+            if (is_virtual(f)) {
+                if (!walk.empty()) spell(g, bases, off, len, k, walk, o);
+                walk.clear();
+            } else {
+                walk.push_back(f);
+            }
+        }
+        if (!walk.empty()) spell(g, bases, off, len, k, walk, o);
+    }
+    for (uint64_t u = 0; u < g.n; u++) {
+        if (g.used[u]) continue;
+        c.clear();
+        circuit(g, g.bin[2 * u], g.need_of_departure(2 * u), c);
+        size_t j = 0;
+        while (j < c.size() && !is_join(c[j])) j++;
+        if (j < c.size()) std::rotate(c.begin(), c.begin() + (long)j + 1, c.end());  // the join now ends it
+        if (!c.empty() && is_join(c.back())) c.pop_back();
+        spell(g, bases, off, len, k, c, o);
+    }
+}
+
+void eulertigs(TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k, TigOut &o) {
+    std::vector<uint64_t> cnt;
+    std::vector<uint8_t> ty;
+    surplus(g, cnt, ty);
+    for (uint32_t b = 0; b < g.n_bins; b++)
+        for (uint64_t i = 0; i < cnt[b]; i++) g.add_dummy(b, dummy_type(ty[b]), g.n_bins, 0, -1);
+    emit_circuits(g, bases, off, len, k, o);
+}
+
+void pathtigs(TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k, TigOut &o) {
+    g.build_pools();
+    std::vector<uint64_t> fwd, bwd, walk;
+    for (uint64_t u = 0; u < g.n; u++) {
+        if (g.used[u]) continue;
+        g.used[u] = 1;
+        // a unitig that leaves through end x is followed by one entered through an unused end of
+        // the other type at x's binode; extending backwards is the same step from the start end
+        auto extend = [&](uint64_t x, std::vector<uint64_t> &chain) {
+            chain.clear();
+            for (;;) {
+                const int64_t f = g.take(g.bin[x], g.need_after_exit(x));
+                if (f < 0) break;
+                g.used[(uint64_t)f >> 1] = 1;
+                chain.push_back((uint64_t)f);
+                x = (uint64_t)f ^ 1u;
+            }
+        };
+        extend(2 * u + 1, fwd);
+        extend(2 * u, bwd);
+        walk.clear();
+        for (size_t i = bwd.size(); i-- > 0;) walk.push_back(bwd[i] ^ 1u);  // entered through the other end
+        walk.push_back(2 * u);
+        walk.insert(walk.end(), fwd.begin(), fwd.end());
+        spell(g, bases, off, len, k, walk, o);
+    }
+}
+
+void greedy_matchtigs(TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k,
+                      TigOut &o) {
+    std::vector<uint64_t> cnt;
+    std::vector<uint8_t> ty;
+    surplus(g, cnt, ty);
+    g.build_pools();  // adjacency for the searches (nothing is used yet)
+    const int64_t max_cost = k - 2;
+    // states (binode, need): 2b + need, a palindromic binode only 2b
+    auto sid = [&](uint32_t b, uint8_t need) { return 2ull * b + (need == kAny ? 0 : need); };
+    struct Cand {
+        int64_t cost;
+        uint32_t b1, b2;
+    };
+    std::vector<Cand> cand;
+    std::vector<int64_t> dist(2ull * (g.n_bins + 1), -1);
+    std::vector<uint64_t> touched;
+    using QE = std::pair<int64_t, uint64_t>;
+    for (uint32_t b1 = 0; b1 < g.n_bins && max_cost > 0; b1++) {
+        if (!cnt[b1]) continue;
+        // leave b1 as the walk ending at one of its surplus ends would: through an end of the
+        // other type (any type at a palindromic binode)
+        const uint8_t n0 = ty[b1] == kAny ? kAny : (uint8_t)(1u - ty[b1]);
+        std::priority_queue<QE, std::vector<QE>, std::greater<QE>> pq;
+        const uint64_t s0 = sid(b1, n0);
+        dist[s0] = 0;
+        touched.push_back(s0);
+        pq.push({0, s0});
+        while (!pq.empty()) {
+            const auto [d, s] = pq.top();
+            pq.pop();
+            if (d != dist[s]) continue;
+            const uint32_t b = (uint32_t)(s >> 1);
+            // a surplus end at b can start the next walk when the state's need is its type
+            if (d > 0 && cnt[b] && (ty[b] == kAny || (uint8_t)(s & 1) == ty[b])) cand.push_back({d, b1, b});
+            for (uint64_t p = g.pool_off[s]; p < g.pool_off[s + 1]; p++) {
+                const uint64_t f = g.pool[p];
+                const uint64_t x = f ^ 1u;
+                const int64_t nd = d + (int64_t)g.kmers[f >> 1];
+                if (nd > max_cost) continue;
+                const uint64_t t = sid(g.bin[x], g.need_after_exit(x));
+                if (dist[t] < 0 || nd < dist[t]) {
+                    if (dist[t] < 0) touched.push_back(t);
+                    dist[t] = nd;
+                    pq.push({nd, t});
+                }
+            }
+        }
+        for (const uint64_t t : touched) dist[t] = -1;
+        touched.clear();
+    }
+    std::sort(cand.begin(), cand.end(), [](const Cand &a, const Cand &b) {
+        if (a.cost != b.cost) return a.cost < b.cost;
+        if (a.b1 != b.b1) return a.b1 < b.b1;
+        return a.b2 < b.b2;
+    });
+    std::vector<uint64_t> rem = cnt;
+    for (const Cand &c : cand) {
+        if (c.b1 == c.b2 ? rem[c.b1] < 2 : (!rem[c.b1] || !rem[c.b2])) continue;
+        rem[c.b1]--;
+        rem[c.b2]--;
+        g.add_dummy(c.b1, dummy_type(ty[c.b1]), c.b2, dummy_type(ty[c.b2]), c.cost);
+    }
+    for (uint32_t b = 0; b < g.n_bins; b++)
+        for (uint64_t i = 0; i < rem[b]; i++) g.add_dummy(b, dummy_type(ty[b]), g.n_bins, 0, -1);
+    emit_circuits(g, bases, off, len, k, o);
+}
+
+}  // namespace
+
+// mode: GGCAT_GPU_TIGS_GREEDY_MATCHTIGS / _EULERTIGS / _PATHTIGS (the extra_elab numbers)
+int compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k, int mode,
+                 std::vector<uint8_t> &out_bases, std::vector<uint64_t> &out_off, std::vector<uint64_t> &out_len,
+                 std::string &err) {
+    out_bases.clear();
+    out_off.clear();
+    out_len.clear();
+    if (k < 3 || k > 127) return err = "tigs support 3 <= k <= 127", GGCAT_GPU_EUNSUPPORTED;
+    if (mode != GGCAT_GPU_TIGS_GREEDY_MATCHTIGS && mode != GGCAT_GPU_TIGS_EULERTIGS && mode != GGCAT_GPU_TIGS_PATHTIGS)
+        return err = "unknown tig mode", GGCAT_GPU_EINVAL;
+    TigGraph g;
+    if (!build_graph(bases, off, len, n, k, g, err)) return GGCAT_GPU_EINVAL;
+    TigOut o;
+    if (mode == GGCAT_GPU_TIGS_EULERTIGS)
+        eulertigs(g, bases, off, len, k, o);
+    else if (mode == GGCAT_GPU_TIGS_PATHTIGS)
+        pathtigs(g, bases, off, len, k, o);
+    else
+        greedy_matchtigs(g, bases, off, len, k, o);
+    out_bases.swap(o.bases);
+    out_off.swap(o.off);
+    out_len.swap(o.len);
+    return GGCAT_GPU_OK;
+}
+
+}  // namespace ggcat
+
+extern "C" int ggcat_gpu_compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k,
+                                      int mode, uint8_t *out_bases, uint64_t bases_cap, uint64_t *out_off,
+                                      uint64_t *out_len, uint64_t n_cap, uint64_t *n_out, uint64_t *bases_out) {
+    if ((n && (!bases || !off || !len)) || !n_out || !bases_out) return GGCAT_GPU_EINVAL;
+    std::vector<uint8_t> b;
+    std::vector<uint64_t> o, l;
+    std::string err;
+    const int rc = ggcat::compute_tigs(bases, off, len, n, k, mode, b, o, l, err);
+    if (rc) return rc;
+    *n_out = o.size();
+    *bases_out = b.size();
+    if (!out_bases || !out_off || !out_len) return GGCAT_GPU_OK;  // sizes only
+    if (bases_cap < b.size() || n_cap < o.size()) return GGCAT_GPU_EINVAL;
+    if (!b.empty()) memcpy(out_bases, b.data(), b.size());
+    if (!o.empty()) {
+        memcpy(out_off, o.data(), o.size() * sizeof(uint64_t));
+        memcpy(out_len, l.data(), l.size() * sizeof(uint64_t));
+    }
+    return GGCAT_GPU_OK;
+}

@@ -229,6 +229,25 @@ int ggcat_gpu_read_sequences_files(const char *const *paths, uint64_t n, int64_t
                                    uint8_t *h_text, uint64_t text_cap, uint64_t *text_len, char *err,
                                    uint64_t err_cap);
 
+/* Spectrum-preserving string sets over n unitigs bases[off[i], off[i] + len[i]) (ACGT,
+ * len >= k, 3 <= k <= 127): the matchtigs family of ExtraElaboration (crates/api/src/lib.rs:101-116;
+ * compute_matchtigs_thread, crates/assembler_pipeline/src/compute_matchtigs.rs:380-537, which
+ * runs the third-party matchtigs crate 2.1.x; the published algorithms are restated here):
+ *   GGCAT_GPU_TIGS_EULERTIGS: the minimum number of strings with every k-mer once (per
+ *     connected component max(1, sum of binode imbalances / 2));
+ *   GGCAT_GPU_TIGS_PATHTIGS: a greedy walk cover, every k-mer once;
+ *   GGCAT_GPU_TIGS_GREEDY_MATCHTIGS: eulertigs whose walks are first joined, cheapest first,
+ *     through at most k-2 repeated k-mers when that is shorter than a new string.
+ * Strings are walks of unitigs overlapping by k-1 bases (a join of w repeated k-mers by
+ * k-1-w).  Output: out_bases[out_off[i], out_off[i] + out_len[i]) for i < *n_out, *bases_out
+ * bytes in all; Σ len bytes and n entries always suffice.  NULL outputs query the sizes. */
+#define GGCAT_GPU_TIGS_GREEDY_MATCHTIGS 2
+#define GGCAT_GPU_TIGS_EULERTIGS 3
+#define GGCAT_GPU_TIGS_PATHTIGS 4
+int ggcat_gpu_compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k, int mode,
+                           uint8_t *out_bases, uint64_t bases_cap, uint64_t *out_off, uint64_t *out_len,
+                           uint64_t n_cap, uint64_t *n_out, uint64_t *bases_out);
+
 /* Maximal-unitig links (build_maximal_unitigs_links,
  * crates/assembler_pipeline/src/maximal_unitig_links.rs:55-417) of n unitigs
  * bases[off[i], off[i] + len[i]) (ACGT, len >= k, k <= 127): list 2i = links from unitig i's
@@ -300,8 +319,10 @@ int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_file
  *     (UnitigColorData::write_as_ident, crates/colors/src/managers/multiple.rs:705-740) and the
  *     subsets go to the colormap "<output_file without its extension>.colors.dat"
  *     (ggcat_gpu_colormap_file); canonical builds only;
- *   extra_elab: 0 none, 1 unitig links (" L:+:j:-" after the colour runs, or GFA L / E lines);
- *     2-4 (matchtigs, eulertigs, pathtigs) return GGCAT_GPU_EUNSUPPORTED;
+ *   extra_elab: 0 none, 1 unitig links (" L:+:j:-" after the colour runs, or GFA L / E lines),
+ *     2 greedy matchtigs, 3 eulertigs, 4 pathtigs (ggcat_gpu_compute_tigs over the final
+ *     unitigs, written as ">{i} LN:i:{len}" records or GFA segments without links; not with
+ *     colours: the reference's matchtig writer stops on coloured joins, compute_matchtigs.rs:496-503);
  *   gfa_output_version: 0 FASTA, 1 GFA v1, 2 GFA v2 (not with colours, as in the reference). */
 int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                   const char *output_file, const char *const *color_names, size_t n_color_names,

@@ -194,3 +194,39 @@ def unitig_links(unitigs: list[bytes], k: int):
             if cur is None or (primary and not cur[1]):
                 slots[i][s] = (lst, primary)
     return [tuple(s[0] if s else [] for s in sl) for sl in slots]
+
+
+def tig_lower_bound(seqs, k: int) -> int:
+    """The fewest strings that hold every k-mer of the unitigs `seqs` once (eulertigs): per
+    connected component of the unitig graph max(1, sum of binode imbalances / 2), a binode
+    being a canonical (k-1)-mer, its imbalance |#ends read into a unitig as the canonical
+    (k-1)-mer - #ends read as its reverse complement| (the parity of its ends when it is its
+    own reverse complement)."""
+    binode = {}
+    counts = {}
+    parent = list(range(len(seqs)))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for u, s in enumerate(seqs):
+        for into in (s[:k - 1], rc(s[len(s) - k + 1:])):
+            c = canon(into)
+            pal = into == rc(into)
+            t = 0 if (pal or into == c) else 1
+            if c in binode:
+                parent[find(u)] = find(binode[c])
+            else:
+                binode[c] = u
+            cnt = counts.setdefault(c, [0, 0, pal])
+            cnt[t] += 1
+    comp_imb = {}
+    for c, (n0, n1, pal) in counts.items():
+        imb = (n0 + n1) % 2 if pal else abs(n0 - n1)
+        r = find(binode[c])
+        comp_imb[r] = comp_imb.get(r, 0) + imb
+    roots = {find(u) for u in range(len(seqs))}
+    return sum(max(1, comp_imb.get(r, 0) // 2) for r in roots)
