@@ -36,7 +36,8 @@ __all__ = [
 
 class ExtraElaboration:
     """crates/api/src/lib.rs:99-116 as numbered by the C API (capi/src/lib.rs:115-121); the
-    matchtig family (2-4) is computed over the final unitigs of an uncoloured graph."""
+    matchtig family (2-4) is computed over the final unitigs (greedy matchtigs of an
+    uncoloured graph only)."""
 
     NONE = 0
     UNITIG_LINKS = 1
@@ -104,8 +105,8 @@ class GGCATInstance:
         if extra_elab not in (ExtraElaboration.NONE, ExtraElaboration.UNITIG_LINKS, ExtraElaboration.GREEDY_MATCHTIGS,
                               ExtraElaboration.EULERTIGS, ExtraElaboration.PATHTIGS):
             raise GgcatGpuError(f"extra_elab {extra_elab} is not an ExtraElaboration")
-        if colors and extra_elab >= ExtraElaboration.GREEDY_MATCHTIGS:
-            raise GgcatGpuError("matchtigs, eulertigs and pathtigs of a coloured graph are not built")
+        if colors and extra_elab == ExtraElaboration.GREEDY_MATCHTIGS:
+            raise GgcatGpuError("greedy matchtigs of a coloured graph are not built")
         gfa = int(gfa_output_version or 0)
         if gfa not in (0, GfaVersion.V1, GfaVersion.V2):
             raise GgcatGpuError(f"gfa_output_version {gfa_output_version} is not 1 or 2")

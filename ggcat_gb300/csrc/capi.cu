@@ -1751,13 +1751,43 @@ static int build_and_write(ggcat_gpu_ctx *ctx, const std::vector<uint8_t> &text,
     for (uint64_t i = 0; i < n; i++) len64[i] = F.len[i];
     std::string err;
     if (extra_elab >= 2) {
-        // matchtigs / eulertigs / pathtigs of the final unitigs, written in their place
+        // matchtigs / eulertigs / pathtigs of the final unitigs, written in their place; with
+        // colours (eulertigs and pathtigs: every k-mer once, in the order of its unitig or
+        // reversed) the runs of the k-mers' subsets along each string
         std::vector<uint8_t> tb;
-        std::vector<uint64_t> to, tl;
-        rc = ggcat::compute_tigs(F.bases.data(), off64.data(), len64.data(), n, p.k, extra_elab, tb, to, tl, err);
+        std::vector<uint64_t> to, tl, walk, walk_end;
+        rc = ggcat::compute_tigs(F.bases.data(), off64.data(), len64.data(), n, p.k, extra_elab, tb, to, tl, err, &walk,
+                                 &walk_end);
         if (rc) return fail(ctx, rc, "%s", err.c_str());
-        rc = ggcat::write_graph_arrays(tb.data(), to.data(), tl.data(), to.size(), p.k, 0, gfa_output_version, nullptr,
-                                       output_file, err);
+        HeaderExtra tig_runs = [&](uint64_t t, std::string &line) {
+            char buf[48];
+            uint32_t cur = 0;
+            uint64_t cnt = 0;
+            auto flush = [&]() {
+                if (!cnt) return;
+                snprintf(buf, sizeof buf, " C:%x:%llu", cur, (unsigned long long)cnt);
+                line += buf;
+            };
+            auto add = [&](uint32_t sub) {
+                if (cnt && sub == cur) {
+                    cnt++;
+                    return;
+                }
+                flush();
+                cur = sub;
+                cnt = 1;
+            };
+            for (uint64_t w = t ? walk_end[t - 1] : 0; w < walk_end[t]; w++) {
+                const uint64_t u = walk[w] >> 1;
+                if (!(walk[w] & 1))
+                    for (uint64_t j = kbase[u]; j < kbase[u + 1]; j++) add(subs[j]);
+                else
+                    for (uint64_t j = kbase[u + 1]; j-- > kbase[u];) add(subs[j]);
+            }
+            flush();
+        };
+        rc = ggcat::write_graph_arrays(tb.data(), to.data(), tl.data(), to.size(), p.k, 0, gfa_output_version,
+                                       colors ? &tig_runs : nullptr, output_file, err);
         if (rc) return fail(ctx, rc, "%s", err.c_str());
         return GGCAT_GPU_OK;
     }
@@ -1808,8 +1838,8 @@ extern "C" int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *con
     if (extra_elab < 0 || extra_elab > 4 || gfa_output_version < 0 || gfa_output_version > 2)
         return fail(ctx, GGCAT_GPU_EINVAL, "extra_elab %d / gfa_output_version %d out of range", extra_elab,
                     gfa_output_version);
-    if (extra_elab >= 2 && colors)
-        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "matchtigs, eulertigs and pathtigs of a coloured graph are not built");
+    if (extra_elab == GGCAT_GPU_TIGS_GREEDY_MATCHTIGS && colors)
+        return fail(ctx, GGCAT_GPU_EUNSUPPORTED, "greedy matchtigs of a coloured graph are not built");
     std::vector<uint8_t> text;
     std::vector<uint64_t> file_off;
     {

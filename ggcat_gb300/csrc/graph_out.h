@@ -68,9 +68,11 @@ int write_graph_arrays(const uint8_t *bases, const uint64_t *off, const uint64_t
                        int with_links, int gfa_version, const HeaderExtra *extra, const char *output_file,
                        std::string &err);
 
-// tigs.cpp: eulertigs / pathtigs / greedy matchtigs of the unitigs (mode = GGCAT_GPU_TIGS_*)
+// tigs.cpp: eulertigs / pathtigs / greedy matchtigs of the unitigs (mode = GGCAT_GPU_TIGS_*);
+// with walk / walk_end, string i's unitigs in order as the ends they are entered through
+// (2u: unitig u forwards, 2u + 1: reverse complemented), walk[walk_end[i - 1], walk_end[i])
 int compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k, int mode,
                  std::vector<uint8_t> &out_bases, std::vector<uint64_t> &out_off, std::vector<uint64_t> &out_len,
-                 std::string &err);
+                 std::string &err, std::vector<uint64_t> *walk = nullptr, std::vector<uint64_t> *walk_end = nullptr);
 
 }  // namespace ggcat

@@ -185,6 +185,7 @@ void circuit(TigGraph &g, uint32_t b0, uint8_t need0, std::vector<uint64_t> &out
 struct TigOut {
     std::vector<uint8_t> bases;
     std::vector<uint64_t> off, len;
+    std::vector<uint64_t> walk, walk_off;  // per string: the entered ends of its real unitigs
 };
 
 void spell(const TigGraph &g, const uint8_t *bases, const uint64_t *off, const uint64_t *len, int k,
@@ -201,6 +202,7 @@ void spell(const TigGraph &g, const uint8_t *bases, const uint64_t *off, const u
         const uint8_t *s = bases + off[e];
         const uint64_t L = len[e];
         const uint64_t from = first ? 0 : (uint64_t)(k - 1 - join);
+        o.walk.push_back(f);
         if (!(f & 1)) {
             o.bases.insert(o.bases.end(), s + from, s + L);
         } else {
@@ -215,6 +217,7 @@ void spell(const TigGraph &g, const uint8_t *bases, const uint64_t *off, const u
     if (o.bases.size() > start) {
         o.off.push_back(start);
         o.len.push_back(o.bases.size() - start);
+        o.walk_off.push_back(o.walk.size());
     }
 }
 
@@ -360,7 +363,7 @@ void greedy_matchtigs(TigGraph &g, const uint8_t *bases, const uint64_t *off, co
 // mode: GGCAT_GPU_TIGS_GREEDY_MATCHTIGS / _EULERTIGS / _PATHTIGS (the extra_elab numbers)
 int compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len, uint64_t n, int k, int mode,
                  std::vector<uint8_t> &out_bases, std::vector<uint64_t> &out_off, std::vector<uint64_t> &out_len,
-                 std::string &err) {
+                 std::string &err, std::vector<uint64_t> *walk, std::vector<uint64_t> *walk_end) {
     out_bases.clear();
     out_off.clear();
     out_len.clear();
@@ -379,6 +382,8 @@ int compute_tigs(const uint8_t *bases, const uint64_t *off, const uint64_t *len,
     out_bases.swap(o.bases);
     out_off.swap(o.off);
     out_len.swap(o.len);
+    if (walk) walk->swap(o.walk);
+    if (walk_end) walk_end->swap(o.walk_off);
     return GGCAT_GPU_OK;
 }
 

@@ -321,8 +321,9 @@ int ggcat_gpu_build_from_files(ggcat_gpu_ctx *ctx, const char *const *input_file
  *     (ggcat_gpu_colormap_file); canonical builds only;
  *   extra_elab: 0 none, 1 unitig links (" L:+:j:-" after the colour runs, or GFA L / E lines),
  *     2 greedy matchtigs, 3 eulertigs, 4 pathtigs (ggcat_gpu_compute_tigs over the final
- *     unitigs, written as ">{i} LN:i:{len}" records or GFA segments without links; not with
- *     colours: the reference's matchtig writer stops on coloured joins, compute_matchtigs.rs:496-503);
+ *     unitigs, written as ">{i} LN:i:{len}" records, with the C: runs of their k-mers along
+ *     each string when coloured, or GFA segments without links; greedy matchtigs not with
+ *     colours: the reference's writer stops on coloured joins, compute_matchtigs.rs:496-503);
  *   gfa_output_version: 0 FASTA, 1 GFA v1, 2 GFA v2 (not with colours, as in the reference). */
 int ggcat_gpu_build_from_files_ex(ggcat_gpu_ctx *ctx, const char *const *input_files, size_t n_inputs,
                                   const char *output_file, const char *const *color_names, size_t n_color_names,

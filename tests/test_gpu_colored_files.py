@@ -162,3 +162,45 @@ def test_colored_dump_unitigs(colored_graph):
     inst.dump_unitigs(out, K, None, True, 1, True, fn)
     lo, _, _ = r.kmers()
     assert len(got) == len(lo)
+
+
+def _kmer_colours(inst, path):
+    """k-mer -> colour tuple from a coloured graph FASTA (C: runs) and its colormap; also the
+    number of records.  Every k-mer must appear once."""
+    cmap = inst.get_colormap_file(path)
+    recs = _read_graph(path)
+    subs = sorted({s for _, runs in recs for s, _ in runs})
+    colours = {}
+    inst.query_colormap(cmap, subs, True, lambda s, c: colours.__setitem__(s, tuple(c)))
+    got = {}
+    for seq, runs in recs:
+        assert sum(c for _, c in runs) == len(seq) - K + 1
+        j = 0
+        for s, c in runs:
+            for t in range(c):
+                km = _canon(seq[j + t:j + t + K])
+                assert km not in got
+                got[km] = colours[s]
+            j += c
+    return got, len(recs)
+
+
+@pytest.mark.parametrize("mode", [3, 4])
+def test_colored_eulertigs_and_pathtigs_keep_every_kmer_colour(colored_graph, mode):
+    """Eulertigs (3) and pathtigs (4) of a coloured graph: every k-mer once, with the colour set
+    it has in the unitig graph (the C: runs follow each string, reversed through unitigs it
+    reads reverse complemented), in fewer records than the unitigs."""
+    import ggcat_gb300
+
+    inst, out, genomes, names, r, tmp = colored_graph
+    paths = [str(tmp / (f"genome{i}.fa.gz" if i == 2 else f"genome{i}.fa")) for i in range(len(names))]
+    exp, n_unitigs = _kmer_colours(inst, out)
+    tout = str(tmp / f"tigs{mode}.fa")
+    assert inst.build_graph(paths, tout, color_names=names, kmer_length=K, colors=True, min_multiplicity=1,
+                            extra_elab=mode) == tout
+    got, n_tigs = _kmer_colours(inst, tout)
+    assert got == exp
+    assert n_tigs < n_unitigs
+    with pytest.raises(ggcat_gb300.GgcatGpuError):
+        inst.build_graph(paths, str(tmp / "mt.fa"), kmer_length=K, colors=True, min_multiplicity=1,
+                         extra_elab=ggcat_gb300.ExtraElaboration.GREEDY_MATCHTIGS)

@@ -85,11 +85,13 @@ def test_tigs_through_build_graph(inputs):
     assert set(_kmers(segs)) == kset and len(segs) == lb
 
 
-def test_tigs_of_a_coloured_graph_are_refused(inputs):
+def test_greedy_matchtigs_of_a_coloured_graph_are_refused(inputs):
+    """A join repeats k-mers whose colours the strings would have to carry twice; the
+    reference's writer stops there too (compute_matchtigs.rs:496-503)."""
     import ggcat_gb300
 
     d, files = inputs
     inst = ggcat_gb300.GGCATInstance.create(ggcat_gb300.GGCATConfig())
     with pytest.raises(ggcat_gb300.GgcatGpuError):
         inst.build_graph(files, str(d / "c.fa"), kmer_length=K, min_multiplicity=1, colors=True,
-                         extra_elab=ggcat_gb300.ExtraElaboration.EULERTIGS)
+                         extra_elab=ggcat_gb300.ExtraElaboration.GREEDY_MATCHTIGS)
