@@ -142,3 +142,34 @@ def test_tigs_reject_bad_input():
     b2, o2, l2 = _arrays([(b"ACGTNCGTA", False)])
     with pytest.raises(_native.GgcatGpuError):
         _native.compute_tigs(b2, o2, l2, 5, _native.TIGS_PATHTIGS)
+
+
+def test_compute_tigs_c_abi_size_query_and_capacity():
+    """NULL outputs return the sizes; a buffer smaller than the strings is refused (not
+    overrun); Σ len bytes and n entries hold any mode's output."""
+    import ctypes as C
+
+    k = 7
+    rng = random.Random(11)
+    kmers = _kmer_set(rng, k, 6, 120, 5)
+    unitigs = naive.maximal_unitigs(kmers, k)
+    b, o, l = _arrays(unitigs)
+    L = _native.load()
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    for mode in (2, 3, 4):
+        n_out, b_out = C.c_uint64(), C.c_uint64()
+        rc = L.ggcat_gpu_compute_tigs(P(b), P(o), P(l), len(o), k, mode, None, 0, None, None, 0, C.byref(n_out),
+                                      C.byref(b_out))
+        assert rc == 0 and 0 < n_out.value <= len(o) and 0 < b_out.value <= int(l.sum())
+        ob = np.zeros(b_out.value, np.uint8)
+        oo = np.zeros(n_out.value, np.uint64)
+        ol = np.zeros(n_out.value, np.uint64)
+        small = np.zeros(b_out.value - 1, np.uint8)
+        rc = L.ggcat_gpu_compute_tigs(P(b), P(o), P(l), len(o), k, mode, P(small), small.size, P(oo), P(ol), oo.size,
+                                      C.byref(n_out), C.byref(b_out))
+        assert rc == -1  # GGCAT_GPU_EINVAL
+        rc = L.ggcat_gpu_compute_tigs(P(b), P(o), P(l), len(o), k, mode, P(ob), ob.size, P(oo), P(ol), oo.size,
+                                      C.byref(n_out), C.byref(b_out))
+        assert rc == 0 and int(ol.sum()) == ob.size
+        tb, to, tl = _native.compute_tigs(b, o, l, k, mode)
+        assert bytes(tb) == bytes(ob) and (to == oo).all() and (tl == ol).all()
