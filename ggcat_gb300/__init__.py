@@ -35,15 +35,23 @@ __all__ = [
 
 
 class ExtraElaboration:
-    """crates/api/src/lib.rs:99-116 as numbered by the C API (capi/src/lib.rs:115-121); the
-    matchtig family (2-4) is computed over the final unitigs (greedy matchtigs of an
-    uncoloured graph only)."""
+    """crates/api/src/lib.rs:99-116, numbered as the C API numbers the first five
+    (capi/src/lib.rs:115-121).  The matchtig family (2-4) is computed over the final unitigs
+    (greedy matchtigs of an uncoloured graph only).  FAST_SIMPLITIGS and FAST_EULERTIGS (Rust
+    API only; GGCAT builds them inside its merge, eulertigs.rs) are served by the same host
+    pathtigs and eulertigs: a simplitig set and the minimum eulertig set, every k-mer once,
+    not GGCAT's own strings."""
 
     NONE = 0
     UNITIG_LINKS = 1
     GREEDY_MATCHTIGS = 2
     EULERTIGS = 3
     PATHTIGS = 4
+    FAST_SIMPLITIGS = 5
+    FAST_EULERTIGS = 6
+
+    # the C ABI's extra_elab for each value
+    _C = {0: 0, 1: 1, 2: 2, 3: 3, 4: 4, 5: 4, 6: 3}
 
 
 class GfaVersion:
@@ -102,8 +110,7 @@ class GGCATInstance:
         """crates/api/src/lib.rs:217-322 — returns the output path ("" on failure, like
         the C API's ``unwrap_or_default``).  With ``colors`` every input is one colour and the
         colormap is written beside the graph (``get_colormap_file``)."""
-        if extra_elab not in (ExtraElaboration.NONE, ExtraElaboration.UNITIG_LINKS, ExtraElaboration.GREEDY_MATCHTIGS,
-                              ExtraElaboration.EULERTIGS, ExtraElaboration.PATHTIGS):
+        if extra_elab not in ExtraElaboration._C:
             raise GgcatGpuError(f"extra_elab {extra_elab} is not an ExtraElaboration")
         if colors and extra_elab == ExtraElaboration.GREEDY_MATCHTIGS:
             raise GgcatGpuError("greedy matchtigs of a coloured graph are not built")
@@ -117,7 +124,7 @@ class GGCATInstance:
         carr = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
         rc = L.ggcat_gpu_build_from_files_ex(self.ctx.h, arr, len(input_streams), os.fsencode(output_file), carr,
                                              len(names), kmer_length, threads_count, int(forward_only), m,
-                                             int(bool(colors)), min_multiplicity, int(extra_elab), gfa)
+                                             int(bool(colors)), min_multiplicity, ExtraElaboration._C[extra_elab], gfa)
         if rc != 0:
             msg = L.ggcat_gpu_last_error(self.ctx.h)
             if self.config.messages_callback:

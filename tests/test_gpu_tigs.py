@@ -58,7 +58,7 @@ def test_tigs_through_build_graph(inputs):
     kset = set(kmers)
     lb = naive.tig_lower_bound(useqs, K)
     got = {}
-    for mode in (E.EULERTIGS, E.PATHTIGS, E.GREEDY_MATCHTIGS):
+    for mode in (E.EULERTIGS, E.PATHTIGS, E.GREEDY_MATCHTIGS, E.FAST_SIMPLITIGS, E.FAST_EULERTIGS):
         out = str(d / f"tigs{mode}.fa")
         assert inst.build_graph(files, out, kmer_length=K, min_multiplicity=1, extra_elab=mode) == out
         heads, seqs = _records(open(out, "rb").read())
@@ -71,7 +71,8 @@ def test_tigs_through_build_graph(inputs):
         got[mode] = seqs
     # the eulertigs of this run's unitigs are minimal; a rebuild may number the unitigs
     # differently but not change the graph
-    assert len(got[E.EULERTIGS]) == lb
+    assert len(got[E.EULERTIGS]) == len(got[E.FAST_EULERTIGS]) == lb
+    assert len(got[E.FAST_SIMPLITIGS]) >= lb
     assert len(got[E.PATHTIGS]) >= lb
     assert len(got[E.GREEDY_MATCHTIGS]) <= lb
     assert sum(map(len, got[E.GREEDY_MATCHTIGS])) <= sum(map(len, got[E.EULERTIGS]))
